@@ -1,0 +1,169 @@
+/*
+ * trans_gpu.h -- C ABI of the GB300 implementation of the TRANS per-iteration hot path.
+ *
+ * The reference (TRANS, Fortran 90) has no plugin API: its hot path is a set of argument-less
+ * subroutines that act on the block selected by GLOBAL_SetPointers(iBlock)
+ * (Module_Global.F90:274-392) and read module globals.  This header replaces that driver loop
+ * body (main.F90:54-197) and the subroutine calls inside it with plain C entry points that a
+ * Fortran caller binds through ISO_C_BINDING:
+ *
+ *   trans_create            replaces the per-block allocation of Input/Read_BlockDimensions.F90:306-478
+ *                           and takes the connectivity built by Input/PLOT3DReadInit.F90:123-348
+ *   trans_set_field         takes one Fortran array of the block (geometry from Geom/CalcDst.F90 +
+ *                           Geom/startup.F90:396-755, state from Input/Init.F90) in its allocated layout
+ *   trans_get_field         returns one Fortran array in the same layout (Output/OUTPUT_SaveField.F90:8-32
+ *                           writes V and Rmiu from it)
+ *   trans_iterate           one outer iteration = main.F90:54-171 (+ :192-197 TIME_Update_U)
+ *   trans_run_stage         one hot-path subroutine over all blocks, for subroutine-granular drop-in
+ *   trans_get_norms         per-block DRSa/DUa/DRSk/DRSo of Time/TIME_Update_V.F90:106-294
+ *   trans_destroy
+ *
+ * Conventions
+ *   - All arrays are FP64 in Fortran column-major order, exactly as allocated by the reference
+ *     (Input/Read_BlockDimensions.F90:306-478); the lower bounds are listed per field below.
+ *   - Return value 0 = OK, negative = error (see TRANS_E_*).  The library never aborts or exits.
+ *   - A context owns one CUDA stream; calls on one context are not re-entrant.
+ *   - Node counts NI,NJ,NK follow the reference (cells are 1..NI-1 etc., 3 ghost layers per side).
+ */
+#ifndef TRANS_GPU_H
+#define TRANS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TRANS_OK 0
+#define TRANS_E_ARG (-1)        /* invalid argument or unsupported option                 */
+#define TRANS_E_CUDA (-2)       /* CUDA runtime error                                      */
+#define TRANS_E_NAN (-3)        /* NaN in the density increment (TIME_Update_V.F90:124-131) */
+#define TRANS_E_TIMEOUT (-4)    /* a bounded device-side wait expired                      */
+#define TRANS_E_MEMORY (-5)     /* device memory budget exhausted                          */
+
+/* Precision modes */
+#define TRANS_FP64 0            /* all-FP64 path, drop-in for the reference subroutines    */
+#define TRANS_MIXED 1           /* FP32 reconstruction/flux/SST/sweeps, FP64 update/metrics */
+
+/*
+ * Module globals read by the hot path (Module_Global.F90:39-148), with the values they hold
+ * after INPUT_ReadOrg, ParameterSet and NonDimensionlization (Input/ReadOrg.F90:12-62,
+ * Input/ParameterSet.F90:1-96).
+ */
+typedef struct trans_params {
+    double XM, RXM2, PPF, Csthlnd, Csth1, Ref, Tiny;
+    double VxF, VyF, VzF;
+    double omega[3];
+    double P0in, T0in, Pouthub;
+    double VisRatio, FSTI, Rkf, Rof, Rmiuf;
+    double A1, Beta_star, Sigk1, Sigo1, Beta1, Gama1, Sigk2, Sigo2, Beta2, Gama2;
+    double Prod_Lmt;
+    double F_limiter1, gama_max, gama_min;
+    double DT_LUSGS_Main, DT_LUSGS_Sub, CFL_Main, CFL_Sub_start, CFL_Sub_end;
+    double Trans_location, Alscale;
+    int CFL_Sub_step, IF_Local_Main, IF_Local_Sub;
+    int Kind_Spatial, Kind_Roe, Kind_Model, Kind_Hybrid, Kind_SubHY;
+    int Kind_Dual, Kchld, IF_RK;
+    int IF_Euler, IF_Turb_org, KItm, IF_Comppress, IF_Precondition, Kind_RotMod;
+    int If_fix_Transition, KI_ini;
+    int precision;                 /* TRANS_FP64 or TRANS_MIXED (not a reference global) */
+    int pad_;
+} trans_params;
+
+/*
+ * One entry of AConnectivity (Module_Block.F90:4-23) after PLOT3D_Read_And_Init
+ * (Input/PLOT3DReadInit.F90:135-348).  Index fields keep the reference's 1-based values.
+ */
+typedef struct trans_conn {
+    int BCType, SubBCType, PerType, lcross;
+    int pointStart[3], pointEnd[3];
+    int IJKDirect, LeftOrRight;
+    int IJKAdd[3], CIJKAdd[3], CIJKAdd1[3], CIJKAdd2[3];
+    int CEIJKAdd[3], CEIJKAdd1[3], CEIJKAdd2[3];
+    int Transform[3], TransformT[3], revMatrix[3];
+    int TargetBlock, TargetConn;       /* global block id (1-based), segment index (1-based) */
+    double rotateAngle;                /* rotateAngle(1) */
+} trans_conn;
+
+/*
+ * One block.  ni,nj,nk are node counts (Block%NI etc.), id = NBlockGlobal.  The six MARKWALL
+ * arrays (Input/Read_BlockDimensions.F90:146-283) are Fortran arrays MARKWALLi0(NJ1,NK1),
+ * MARKWALLim(NJ1,NK1), MARKWALLj0(NI1,NK1), MARKWALLjm(NI1,NK1), MARKWALLk0(NI1,NJ1),
+ * MARKWALLkm(NI1,NJ1); NULL means all zero.
+ */
+typedef struct trans_block {
+    int ni, nj, nk, id;
+    int nconn, pad_;
+    const trans_conn* conn;
+    const int* markwall[6];
+} trans_block;
+
+/* Per-block residual norms of TIME_Update_V (Time/TIME_Update_V.F90:106-294, 892-908). */
+typedef struct trans_norms {
+    double DRSa, DUa, DRSk, DUk, DRSo, DUo;
+    int Ima, Jma, Kma, nan_flag;
+} trans_norms;
+
+/*
+ * Field ids for trans_set_field / trans_get_field, with the Fortran allocation each pointer
+ * must have (Input/Read_BlockDimensions.F90:306-478; NIp2 = NI+2):
+ */
+enum trans_field {
+    TRANS_V = 0,      /* V(7,-2:NIp2,-2:NJp2,-2:NKp2)          conserved variables            */
+    TRANS_PP = 1,     /* PP(-2:NIp2,-2:NJp2,-2:NKp2)           pressure                       */
+    TRANS_T = 2,      /* T(-2:NIp2,-2:NJp2,-2:NKp2)            temperature                    */
+    TRANS_RMIU = 3,   /* Rmiu(-2:NIp2,-2:NJp2,-2:NKp2)         eddy viscosity                 */
+    TRANS_WT0 = 4,    /* Wt0(7,NIp2,NJp2,NKp2)                 time level n                   */
+    TRANS_WT1 = 5,    /* Wt1(7,NIp2,NJp2,NKp2)                 time level n-1                 */
+    TRANS_SD = 6,     /* SD(3,3,-2:NIp2,-2:NJp2,-2:NKp2)       face area vectors (dir,comp)   */
+    TRANS_GRAD = 7,   /* Grad(3,-2:NIp2,-2:NJp2,-2:NKp2)       face areas                     */
+    TRANS_VOL = 8,    /* Vol(-2:NIp2,-2:NJp2,-2:NKp2)                                         */
+    TRANS_ALAGM = 9,  /* Alagm(3,-2:NIp2,-2:NJp2,-2:NKp2)      face-centre spacing            */
+    TRANS_DST = 10,   /* Dst(-2:NIp2,-2:NJp2,-2:NKp2)          wall distance                  */
+    TRANS_ALENG = 11, /* ALeng(-2:NIp2,-2:NJp2,-2:NKp2)        DES length scale               */
+    TRANS_ASENG = 12, /* ASeng(NIp2,NJp2,NKp2)                                                */
+    TRANS_XC = 13,    /* Xc(0:NIp2,0:NJp2,0:NKp2)                                             */
+    TRANS_YC = 14,    /* Yc(0:NIp2,0:NJp2,0:NKp2)                                             */
+    TRANS_ZC = 15,    /* Zc(0:NIp2,0:NJp2,0:NKp2)                                             */
+    TRANS_RAD = 16,   /* rad(-2:NIp2,-2:NJp2,-2:NKp2)                                         */
+    TRANS_THTC = 17,  /* thtc(-2:NIp2,-2:NJp2,-2:NKp2)                                        */
+    /* work arrays, readable for subroutine-granular parity */
+    TRANS_D = 18,     /* D(7,0:NIp2,0:NJp2,0:NKp2)             residual / increment           */
+    TRANS_RDS = 19,   /* Rds(3,0:NIp2,0:NJp2,0:NKp2)           spectral radii                 */
+    TRANS_DTM = 20,   /* Dtm(NIp2,NJp2,NKp2)                   local time step                */
+    TRANS_DQDXYZ = 21,/* DQdxyz(18,-1:NIp2,-1:NJp2,-1:NKp2)    cell gradients                 */
+    TRANS_SHOCK = 22, /* shock(-2:NIp2,-2:NJp2,-2:NKp2)        shock sensor                   */
+    TRANS_NFIELDS = 23
+};
+
+/* Hot-path stages for trans_run_stage (each acts on all blocks, as main.F90 does). */
+enum trans_stage {
+    TRANS_STAGE_SPECRAD = 0,   /* TIME_SpectralRadius                         main.F90:66-69   */
+    TRANS_STAGE_BC_STATE = 1,  /* BC_Boundarys(-1) (+ PARALLEL_BCs(-1))       main.F90:72-73   */
+    TRANS_STAGE_GRADIENT = 2,  /* SPACEINTERP + DIFF_DqDxyz                   main.F90:74-83   */
+    TRANS_STAGE_BC_GRAD = 3,   /* BC_Boundarys(0) (+ PARALLEL_BCs(0))         main.F90:84-85   */
+    TRANS_STAGE_RESIDUAL = 4,  /* D=0, diffusion, reconstruction, fluxes      main.F90:92-133  */
+    TRANS_STAGE_LUSGS = 5,     /* TIME_LUSGS + TURBTWO_TIME_LUSGS_SST         main.F90:139-142 */
+    TRANS_STAGE_UPDATE = 6,    /* TIME_Update_V                               main.F90:143     */
+    TRANS_STAGE_UPDATE_U = 7,  /* TIME_Update_U                               main.F90:192-197 */
+    TRANS_NSTAGES = 8
+};
+
+int trans_create(const trans_params* p, int nblocks, const trans_block* blocks, void** ctx);
+int trans_destroy(void* ctx);
+int trans_set_field(void* ctx, int ib, int field, const double* fortran_array);
+int trans_get_field(void* ctx, int ib, int field, double* fortran_array);
+/* One outer iteration KI (main.F90:48-197).  norms: array of nblocks entries, may be NULL. */
+int trans_iterate(void* ctx, int ki, trans_norms* norms);
+/* One stage of one sub-iteration for all blocks; itr_chld is the sub-iteration index (1-based). */
+int trans_run_stage(void* ctx, int stage, int ki, int itr_chld);
+int trans_get_norms(void* ctx, trans_norms* norms);
+int trans_sync(void* ctx);
+/* Device bytes held by the context. */
+long long trans_device_bytes(void* ctx);
+/* Kernel launches issued since the context was created (all kernels of this library). */
+long long trans_kernel_launches(void* ctx);
+const char* trans_last_error(void* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

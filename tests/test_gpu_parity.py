@@ -1,0 +1,88 @@
+"""GPU FP64 path against the CPU oracle, through the C ABI.
+
+Tolerance: 1e-11 relative (normwise per component, max|gpu-oracle| / max|oracle|) on every
+per-cell quantity and on the residual history, the bar the plain FP64 path is held to.
+"""
+import numpy as np
+import pytest
+
+from helpers import bit_equal_fraction, face_ghosts, interior, rel_err, small_channel
+
+TOL = 1e-11
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(c, conns, geo, st):
+    from oracle.oracle import OracleSolver
+    from trans_gb300.solver import Solver
+    return Solver(c, conns, geo, st), OracleSolver(c, conns, geo, st)
+
+
+STAGE_FIELDS = {
+    "SPECRAD": [("RDS", "int"), ("DTM", "int")],
+    "BC_STATE": [("V", "ghost"), ("PP", "ghost"), ("T", "ghost"), ("RMIU", "ghost")],
+    "GRADIENT": [("DQDXYZ", "int"), ("SHOCK", "int"), ("SHOCK", "ghost")],
+    "BC_GRAD": [("DQDXYZ", "ghost1")],
+    "RESIDUAL": [("D", "int")],
+    "LUSGS": [("D", "int")],
+    "UPDATE": [("V", "int"), ("PP", "int"), ("T", "int"), ("RMIU", "int")],
+}
+
+
+def _mask(kind, dims):
+    if kind == "int":
+        return interior(dims)
+    if kind == "ghost":
+        return face_ghosts(dims, 3)
+    return face_ghosts(dims, 1)
+
+
+@pytest.mark.parametrize("scheme", [dict(Kind_Spatial=2, Kind_Roe=1), dict(Kind_Spatial=3, Kind_Roe=3)],
+                         ids=["muscl_roe", "mdcd_ausmpw"])
+def test_stage_by_stage(gpu_lib, scheme):
+    c, conns, geo, st = small_channel(**scheme)
+    g, o = _pair(c, conns, geo, st)
+    dims = c.blocks[0].dims
+    for ki in (1, 2):
+        for stage, fields in STAGE_FIELDS.items():
+            g.run_stage(stage, ki)
+            o.run_stage(stage, ki)
+            for name, mk in fields:
+                m = _mask(mk, dims)
+                a, b = g.get_field(0, name), o.get_field(0, name)
+                err = np.max(rel_err(a, b, m))
+                assert err <= TOL, f"iteration {ki} stage {stage} field {name}/{mk}: rel err {err:.3e}"
+        g.run_stage("UPDATE_U", ki)
+        o.run_stage("UPDATE_U", ki)
+
+
+@pytest.mark.parametrize("scheme", [dict(Kind_Spatial=2, Kind_Roe=1), dict(Kind_Spatial=3, Kind_Roe=3)],
+                         ids=["muscl_roe", "mdcd_ausmpw"])
+def test_iterations_and_residual_history(gpu_lib, scheme):
+    c, conns, geo, st = small_channel(**scheme)
+    g, o = _pair(c, conns, geo, st)
+    dims = c.blocks[0].dims
+    m = interior(dims)
+    hg, ho = [], []
+    for ki in range(1, 21):
+        ng = g.iterate(ki)
+        no = o.iterate(ki)
+        hg.append(ng[0]["DRSa"]); ho.append(no[0]["DRSa"])
+    hist = np.max(np.abs(np.array(hg) - np.array(ho)) / np.abs(np.array(ho)))
+    assert hist <= TOL, f"L2 residual history differs by {hist:.3e}"
+    for name in ("V", "PP", "T", "RMIU"):
+        err = np.max(rel_err(g.get_field(0, name), o.get_field(0, name), m))
+        assert err <= TOL, f"{name} after 20 iterations: {err:.3e}"
+
+
+def test_bitwise_agreement_first_residual(gpu_lib):
+    """Without fused multiply-add the FP64 residual matches the oracle bit for bit on almost
+    every cell (libm tanh/exp/pow may differ by an ulp)."""
+    c, conns, geo, st = small_channel(Kind_Spatial=3, Kind_Roe=3)
+    g, o = _pair(c, conns, geo, st)
+    for s in ("SPECRAD", "BC_STATE", "GRADIENT", "BC_GRAD", "RESIDUAL"):
+        g.run_stage(s, 1)
+        o.run_stage(s, 1)
+    frac = bit_equal_fraction(g.get_field(0, "D"), o.get_field(0, "D"), interior(c.blocks[0].dims))
+    assert frac > 0.9, f"only {frac:.3f} of residual values are bit-identical"

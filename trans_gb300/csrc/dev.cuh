@@ -1,0 +1,310 @@
+// dev.cuh -- device data layout and per-face / per-cell physics of the TRANS hot path.
+//
+// Layout: every block of every case lives in one device arena.  A block owns NSLOT scalar
+// arrays ("slots") of ncell = (NI+5)(NJ+5)(NK+5) doubles each, i fastest, covering the full
+// ghost extent -2..N+2 of the reference's arrays.  Cell-centred and face-centred quantities
+// share the index: face i of direction d is stored at cell i (the cell on its +d side).
+//
+// The physics functions below restate the reference's expressions operation by operation
+// (same association, same divisions).  In the FP64 path they are compiled without fused
+// multiply-add, so they reproduce a CPU evaluation of the same expressions bit for bit,
+// except where a libm function (exp, tanh, pow) is evaluated.  They are templated on the
+// arithmetic type R so that the mixed-precision path reuses them in FP32.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tg {
+
+enum Slot {
+    S_V = 0,            // 7
+    S_PP = 7, S_T = 8, S_RMIU = 9,
+    S_WT0 = 10,         // 7
+    S_WT1 = 17,         // 7
+    S_SD = 24,          // 9: (dir-1)*3 + (comp-1)
+    S_GRAD = 33,        // 3
+    S_VOL = 36,
+    S_ALAGM = 37,       // 3
+    S_DST = 40, S_ALENG = 41, S_ASENG = 42,
+    S_XC = 43, S_YC = 44, S_ZC = 45,
+    S_RAD = 46, S_THTC = 47, S_SINT = 48, S_COST = 49,
+    S_AINV = 50,        // 3: 1/(Alagm(d,i)+Alagm(d,i-1)) on faces
+    S_VINV = 53,        // 3: 1/(Vol(i)+Vol(i-1)) on faces
+    S_ASD = 56,         // 9: 0.5*(SD(d,c,i)+SD(d,c,i+1)) per cell
+    S_WALL = 65,        // 3: MARKWALL flag on faces
+    S_D = 68,           // 7
+    S_RDS = 75,         // 3
+    S_DTM = 78, S_STEPT = 79, S_CVS = 80,
+    S_DQ = 81,          // 18
+    S_SHOCK = 99,
+    S_FM = 100, S_FT = 101,
+    S_PRIM = 102,       // 5: u, v, w, k/rho, omega/rho
+    S_FX = 107,         // 39: face fluxes, (dir-1)*13 + m
+    S_FC1 = 146,        // SST F1 per cell (for the DES length scale of the next cell)
+    S_RINV = 147,       // 1/rho
+    S_SVEL = 148,       // 3: rho*u * (1/rho) etc., the velocities of the LU-SGS Jacobians
+    NSLOT = 151
+};
+
+// face-flux components (per face and direction)
+enum FX { FX_VX = 0, FX_VY = 1, FX_VZ = 2, FX_VE = 3, FX_TK = 4, FX_TO = 5,
+          FX_C0 = 6, FX_CK = 11, FX_CO = 12, NFX = 13 };
+
+struct DevBlock {
+    int NI, NJ, NK, NI1, NJ1, NK1, PI, PJ, PK;
+    int ncell;            // PI*PJ*PK
+    int nint;             // NI1*NJ1*NK1
+    int pad_;
+    double* base;
+};
+
+struct Tile {             // a run of consecutive interior cells (or faces) of one block
+    int blk, start, count, pad_;
+};
+
+struct Params {           // module globals the kernels read (trans_params + derived)
+    double XM, RXM2, PPF, Csthlnd, Csth1, Ref, Tiny, VxF, VyF, VzF, omega0;
+    double P0in, T0in, Pouthub, VisRatio, FSTI;
+    double A1, Beta_star, Sigk1, Sigo1, Beta1, Gama1, Sigk2, Sigo2, Beta2, Gama2, Prod_Lmt;
+    double gama_max, gama_min, DT_LUSGS_Main, DT_LUSGS_Sub, CFL_Main, Trans_location;
+    int Kind_Spatial, Kind_Roe, Kind_Hybrid, Kind_SubHY, Kind_Dual, IF_Local_Main, IF_Local_Sub;
+    int IF_Comppress, If_fix_Transition, pad_;
+};
+
+__host__ __device__ inline int cidx(const DevBlock& b, int i, int j, int k) {
+    return (i + 2) + b.PI * ((j + 2) + b.PJ * (k + 2));
+}
+__device__ inline double* slot(const DevBlock& b, int s) { return b.base + (size_t)s * (size_t)b.ncell; }
+
+template <typename R> __device__ inline R dmax(R a, R b) { return (a < b) ? b : a; }   // std::max
+template <typename R> __device__ inline R dmin(R a, R b) { return (b < a) ? b : a; }   // std::min
+template <typename R> __device__ inline R sgn1(R b) { return b >= R(0) ? R(1) : R(-1); }
+template <typename R> __device__ inline R sq(R x) { return x * x; }
+template <typename R> __device__ inline R p15(R x) { return x * sqrt(x); }
+
+// Sutherland viscosity (Time/SpectralRadius.F90:59 and every copy of it)
+template <typename R> __device__ inline R mu_suth(const Params& p, R TT) {
+    return (R(1.0) + R(p.Csthlnd)) / (TT * R(p.Csth1) + R(p.Csthlnd)) * p15(R(p.Csth1) * TT);
+}
+// the variant without Csth1 (Space/TURBTWO_DIFFUSION_Centered.F90:160)
+template <typename R> __device__ inline R mu_suth_nocs(const Params& p, R TT) {
+    return (R(1.0) + R(p.Csthlnd)) / (TT + R(p.Csthlnd)) * p15(TT);
+}
+
+// Space/UTIL_MUSCL.F90:2-18
+template <typename R> __device__ inline R alimiter(R var1, R var2) {
+    const R epsm = R(1.0e-7);
+    return (var1 * (var2 * var2 + R(2.0) * epsm * epsm) + var2 * (R(2.0) * var1 * var1 + epsm * epsm)) /
+           (R(2.0) * var1 * var1 - var1 * var2 + R(2.0) * var2 * var2 + R(3.0) * epsm * epsm) * R(0.5) *
+           fabs(sgn1(var1) + sgn1(var2));
+}
+
+// Space/CONVECT_MDCD.F90:62-120: left (ql) and right (qr) face states from six cells
+template <typename R> __device__ inline void mdcd_pair(const R* s6, R gama, R& ql, R& qr) {
+    const R beta = R(sqrt(13.0 / 12.0));
+    const R epsm = R(1.0e-6);
+    R aw0 = R(1.5) * (R(0.0463783) + gama);
+    R aw1 = R(0.5 - 1.5 * 0.0463783) + R(4.5) * gama;
+    R aw2 = R(0.5 - 1.5 * 0.0463783) - R(4.5) * gama;
+    R aw3 = R(1.5) * (R(0.0463783) - gama);
+    const R c26 = R(2. / 6.), c76 = R(7. / 6.), c116 = R(11. / 6.), c16 = R(1. / 6.), c56 = R(5. / 6.), c13 = R(1. / 3.);
+    {
+        R v_2 = s6[0], v_1 = s6[1], v0 = s6[2], v1 = s6[3], v2 = s6[4], v3 = s6[5];
+        R ISK1 = sq(R(0.5) * v_2 - R(2.0) * v_1 + R(1.5) * v0) + sq(beta * v_2 - R(2.0) * beta * v_1 + beta * v0);
+        R ISK2 = sq(-(R(0.5) * v_1) + R(0.0) * v0 + R(0.5) * v1) + sq(beta * v_1 - R(2.0) * beta * v0 + beta * v1);
+        R ISK3 = sq(-(R(1.5) * v0) + R(2.0) * v1 - R(0.5) * v2) + sq(beta * v0 - R(2.0) * beta * v1 + beta * v2);
+        R ISK4 = sq(R(2.5) * v1 - R(4.0) * v2 + R(1.5) * v3) + sq(beta * v1 - R(2.0) * beta * v2 + beta * v3);
+        ISK4 = dmax(dmax(dmax(ISK1, ISK2), ISK3), ISK4);
+        R ak1 = aw0 / sq(epsm + ISK1), ak2 = aw1 / sq(epsm + ISK2), ak3 = aw2 / sq(epsm + ISK3), ak4 = aw3 / sq(epsm + ISK4);
+        R w0 = ak1 / (ak1 + ak2 + ak3 + ak4), w1 = ak2 / (ak1 + ak2 + ak3 + ak4);
+        R w2 = ak3 / (ak1 + ak2 + ak3 + ak4), w3 = ak4 / (ak1 + ak2 + ak3 + ak4);
+        R qq0 = c26 * v_2 - c76 * v_1 + c116 * v0;
+        R qq1 = -(c16 * v_1) + c56 * v0 + c26 * v1;
+        R qq2 = c26 * v0 + c56 * v1 - c16 * v2;
+        R qq3 = c116 * v1 - c76 * v2 + c13 * v3;
+        ql = w0 * qq0 + w1 * qq1 + w2 * qq2 + w3 * qq3;
+    }
+    {
+        R v_3 = s6[0], v_2 = s6[1], v_1 = s6[2], v0 = s6[3], v1 = s6[4], v2 = s6[5];
+        R ISK1 = sq(R(0.5) * v2 - R(2.0) * v1 + R(1.5) * v0) + sq(beta * v2 - R(2.0) * beta * v1 + beta * v0);
+        R ISK2 = sq(-(R(0.5) * v1) + R(0.0) * v0 + R(0.5) * v_1) + sq(beta * v1 - R(2.0) * beta * v0 + beta * v_1);
+        R ISK3 = sq(-(R(1.5) * v0) + R(2.0) * v_1 - R(0.5) * v_2) + sq(beta * v0 - R(2.0) * beta * v_1 + beta * v_2);
+        R ISK4 = sq(R(2.5) * v_1 - R(4.0) * v_2 + R(1.5) * v_3) + sq(beta * v_1 - R(2.0) * beta * v_2 + beta * v_3);
+        ISK4 = dmax(dmax(dmax(ISK1, ISK2), ISK3), ISK4);
+        R ak1 = aw0 / sq(epsm + ISK1), ak2 = aw1 / sq(epsm + ISK2), ak3 = aw2 / sq(epsm + ISK3), ak4 = aw3 / sq(epsm + ISK4);
+        R w0 = ak1 / (ak1 + ak2 + ak3 + ak4), w1 = ak2 / (ak1 + ak2 + ak3 + ak4);
+        R w2 = ak3 / (ak1 + ak2 + ak3 + ak4), w3 = ak4 / (ak1 + ak2 + ak3 + ak4);
+        R qq0 = c26 * v2 - c76 * v1 + c116 * v0;
+        R qq1 = -(c16 * v1) + c56 * v0 + c26 * v_1;
+        R qq2 = c26 * v0 + c56 * v_1 - c16 * v_2;
+        R qq3 = c116 * v_1 - c76 * v_2 + c13 * v_3;
+        qr = w0 * qq0 + w1 * qq1 + w2 * qq2 + w3 * qq3;
+    }
+}
+
+// Space/CONVECT_Roe_Original.F90:242-407 (non-preconditioned, no rotation); out = flux / |S|
+template <typename R>
+__device__ inline void roe_flux(const Params& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo, R WRo,
+                                R sav1, R sav2, R sav3, R sav, R* out) {
+    R rcpcv = R(p.PPF);
+    R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
+    const R ga = R(1.4), ga1 = R(1.4 - 1.0);
+    R VAMLo = ULo * ULo + VLo * VLo + WLo * WLo;
+    R VAMRo = URo * URo + VRo * VRo + WRo * WRo;
+    R rLo = R(0.0), rRo = R(0.0);
+    R HLo = PLo * ga / (DENLo * ga1) + R(0.5) * VAMLo - R(0.5) * (rLo * rLo);
+    R HRo = PRo * ga / (DENRo * ga1) + R(0.5) * VAMRo - R(0.5) * (rRo * rRo);
+    R rrorl = sqrt(DENRo / DENLo);
+    R rrorlp1 = R(1.0) + rrorl;
+    R rm = sqrt(DENRo * DENLo);
+    R um = (ULo + URo * rrorl) / rrorlp1;
+    R vm = (VLo + VRo * rrorl) / rrorlp1;
+    R wm = (WLo + WRo * rrorl) / rrorlp1;
+    R hm = (HLo + HRo * rrorl) / rrorlp1;
+    R vm2 = um * um + vm * vm + wm * wm;
+    R rccm = (rLo + rrorl * rRo) / rrorlp1;
+    R am2 = ga1 * fabs(hm - R(0.5) * vm2 + R(0.5) * (rccm * rccm));
+    R am = sqrt(am2);
+    R sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
+    R unormaln = (sav1n * um + sav2n * vm + sav3n * wm);
+    R eig1 = fabs(unormaln);
+    R eig2 = fabs(unormaln + am);
+    R eig3 = fabs(unormaln - am);
+    const R e01 = R(0.1), ee = R(0.1 * 0.1), e02 = R(0.2);
+    if (eig1 < e01) eig1 = (eig1 * eig1 + ee) / e02;
+    if (eig2 < e01) eig2 = (eig2 * eig2 + ee) / e02;
+    if (eig3 < e01) eig3 = (eig3 * eig3 + ee) / e02;
+    const R alf = R(0.0), ubetac2 = R(1.0);
+    R amrev = am;
+    R dunormaln = (sav1n * (URo - ULo) + sav2n * (VRo - VLo) + sav3n * (WRo - WLo));
+    R astar = (eig2 + eig3) / R(2.0);
+    R Mstar = (eig2 - eig3) / R(2.0) / amrev;
+    R dW1 = DENRo - DENLo;
+    R dU1 = URo - ULo, dU2 = VRo - VLo, dU3 = WRo - WLo;
+    R dP1 = PRo - PLo;
+    R dW2 = rm * dU1 + dW1 * um;
+    R dW3 = rm * dU2 + dW1 * vm;
+    R dW4 = rm * dU3 + dW1 * wm;
+    R dW5 = dP1 / ga1 + R(0.5) * vm2 * dW1 + rm * um * dU1 + rm * vm * dU2 + rm * wm * dU3;
+    R dUroe = Mstar * dunormaln + (astar - (R(1) - R(2.0) * alf) * eig1 - alf * unormaln * Mstar) * (PRo - PLo) / rm / (ubetac2 * am2);
+    R dProe = Mstar * (PRo - PLo) + (astar - eig1 + alf * unormaln * Mstar) * rm * dunormaln;
+    R droR1 = eig1 * dW1 + dUroe * rm;
+    R drxR1 = eig1 * dW2 + dUroe * rm * um + dProe * sav1n;
+    R dryR1 = eig1 * dW3 + dUroe * rm * vm + dProe * sav2n;
+    R drzR1 = eig1 * dW4 + dUroe * rm * wm + dProe * sav3n;
+    R dreR1 = eig1 * dW5 + dUroe * rm * hm + dProe * unormaln;
+    R ulnormaln = (sav1n * ULo + sav2n * VLo + sav3n * WLo);
+    R urnormaln = (sav1n * URo + sav2n * VRo + sav3n * WRo);
+    R rulnormaln = DENLo * ulnormaln, rurnormaln = DENRo * urnormaln;
+    out[0] = R(-0.5) * (rulnormaln + rurnormaln - droR1);
+    out[1] = R(-0.5) * (rulnormaln * ULo + rurnormaln * URo + sav1n * (PLo + PRo) - drxR1);
+    out[2] = R(-0.5) * (rulnormaln * VLo + rurnormaln * VRo + sav2n * (PLo + PRo) - dryR1);
+    out[3] = R(-0.5) * (rulnormaln * WLo + rurnormaln * WRo + sav3n * (PLo + PRo) - drzR1);
+    out[4] = R(-0.5) * (rulnormaln * HLo + rurnormaln * HRo - dreR1);
+}
+
+// Space/CONVECT_AUSMPW_Plus.F90:204-317; out = flux / |S|
+template <typename R>
+__device__ inline void ausmpw_flux(const Params& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo, R WRo,
+                                   R sav1, R sav2, R sav3, R sav, R* out) {
+    R rcpcv = R(p.PPF);
+    R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
+    R sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
+    const R ga = R(1.4), ga1 = R(1.4 - 1.0);
+    R VAMLo = ULo * ULo + VLo * VLo + WLo * WLo;
+    R VAMRo = URo * URo + VRo * VRo + WRo * WRo;
+    R HLo = PLo * ga / (DENLo * ga1) + R(0.5) * VAMLo;
+    R HRo = PRo * ga / (DENRo * ga1) + R(0.5) * VAMRo;
+    R ULn = (sav1n * ULo + sav2n * VLo + sav3n * WLo);
+    R URn = (sav1n * URo + sav2n * VRo + sav3n * WRo);
+    R astar_L = sqrt(R(2) * ga1 * HLo / (ga + R(1)));
+    R astar_R = sqrt(R(2) * ga1 * HRo / (ga + R(1)));
+    R aas_L = astar_L * astar_L / dmax(sqrt(VAMLo), astar_L);
+    R aas_R = astar_R * astar_R / dmax(sqrt(VAMRo), astar_R);
+    R Acc = dmin(aas_L, aas_R);
+    R MaL = ULn / Acc, MaR = URn / Acc;
+    const R c316 = R(0.0);    // 3/16 is integer division in the reference (CONVECT_AUSMPW_Plus.F90:274,286)
+    const R tiny = R(p.Tiny);
+    R MaL_plus, pL_plus, MaR_neg, pR_neg;
+    if (fabs(MaL) > R(1.0)) {
+        MaL_plus = R(0.5) * (MaL + fabs(MaL));
+        pL_plus = R(0.5) * (MaL + fabs(MaL)) / (MaL + tiny);
+    } else {
+        MaL_plus = R(0.25) * sq(MaL + R(1));
+        pL_plus = R(0.25) * sq(MaL + R(1)) * (R(2) - MaL) + c316 * MaL * sq(MaL * MaL - R(1));
+    }
+    if (fabs(MaR) > R(1.0)) {
+        MaR_neg = R(0.5) * (MaR - fabs(MaR));
+        pR_neg = R(0.5) * (MaR - fabs(MaR)) / (MaR + tiny);
+    } else {
+        MaR_neg = R(-1) * R(0.25) * sq(MaR - R(1));
+        pR_neg = R(0.25) * sq(MaR - R(1)) * (R(2) + MaR) - c316 * MaR * sq(MaR * MaR - R(1));
+    }
+    R pS = pL_plus * PLo + pR_neg * PRo;
+    R Mas = MaL_plus + MaR_neg;
+    R mn = dmin(PLo / PRo, PRo / PLo);
+    R wP = R(1.0) - mn * mn * mn;
+    R fL = fabs(MaL) < R(1) ? PLo / (pS + tiny) - R(1) : R(0.0);
+    R fR = fabs(MaR) < R(1) ? PRo / (pS + tiny) - R(1) : R(0.0);
+    R MMaL_plus, MMaR_neg;
+    if (Mas >= R(0)) {
+        MMaL_plus = MaL_plus + MaR_neg * ((R(1) - wP) * (R(1) + fR) - fL);
+        MMaR_neg = MaR_neg * wP * (R(1) + fR);
+    } else {
+        MMaL_plus = MaL_plus * wP * (R(1) + fL);
+        MMaR_neg = MaR_neg + MaL_plus * ((R(1) - wP) * (R(1) + fL) - fR);
+    }
+    out[0] = R(-1) * MMaL_plus * Acc * DENLo - MMaR_neg * Acc * DENRo;
+    out[1] = R(-1) * MMaL_plus * Acc * DENLo * ULo - MMaR_neg * Acc * DENRo * URo - sav1n * (pL_plus * PLo + pR_neg * PRo);
+    out[2] = R(-1) * MMaL_plus * Acc * DENLo * VLo - MMaR_neg * Acc * DENRo * VRo - sav2n * (pL_plus * PLo + pR_neg * PRo);
+    out[3] = R(-1) * MMaL_plus * Acc * DENLo * WLo - MMaR_neg * Acc * DENRo * WRo - sav3n * (pL_plus * PLo + pR_neg * PRo);
+    out[4] = R(-1) * MMaL_plus * Acc * DENLo * HLo - MMaR_neg * Acc * DENRo * HRo;
+}
+
+// Time/TIME_LUSGS.F90:696-768 with pGam = 1.4 and zero grid speed
+template <typename R>
+__device__ inline void lusgs_adq(R pVx, R pVy, R pVz, R aSDx, R aSDy, R aSDz, R pPP, R roinv,
+                                 R AinRo, R AinRx, R AinRy, R AinRz, R AinRe, R* Dif) {
+    const R pGam = R(1.4);
+    R VP = pVx * aSDx + pVy * aSDy + pVz * aSDz + R(0.0);
+    R Ut2 = pVx * pVx + pVy * pVy + pVz * pVz;
+    const R aSDt = R(0.0);
+    const R Gm1 = R(1.4 - 1.0), Gm2 = R(1.4 - 2.0);
+    R AA2 = pGam * pPP * roinv;
+    R gUt2 = R(0.5) * Gm1 * Ut2;
+    Dif[0] = AinRo * aSDt + AinRx * aSDx + AinRy * aSDy + AinRz * aSDz + AinRe * R(0.0);
+    Dif[1] = AinRo * (aSDx * gUt2 - pVx * VP) + AinRx * (aSDt + VP - aSDx * Gm2 * pVx) + AinRy * (aSDy * pVx - aSDx * Gm1 * pVy)
+             + AinRz * (aSDz * pVx - aSDx * Gm1 * pVz) + AinRe * (aSDx * Gm1);
+    Dif[2] = AinRo * (aSDy * gUt2 - pVy * VP) + AinRx * (aSDx * pVy - aSDy * Gm1 * pVx) + AinRy * (aSDt + VP - aSDy * Gm2 * pVy)
+             + AinRz * (aSDz * pVy - aSDy * Gm1 * pVz) + AinRe * (aSDy * Gm1);
+    Dif[3] = AinRo * (aSDz * gUt2 - pVz * VP) + AinRx * (aSDx * pVz - aSDz * Gm1 * pVx) + AinRy * (aSDy * pVz - aSDz * Gm1 * pVy)
+             + AinRz * (aSDt + VP - aSDz * Gm2 * pVz) + AinRe * (aSDz * Gm1);
+    R GEt1 = R(0.5) * Gm2 * Ut2 - AA2 / Gm1;
+    R GEt2 = R(0.5) * Ut2 + AA2 / Gm1;
+    Dif[4] = AinRo * VP * GEt1 + AinRx * (aSDx * GEt2 - Gm1 * pVx * VP) + AinRy * (aSDy * GEt2 - Gm1 * pVy * VP)
+             + AinRz * (aSDz * GEt2 - Gm1 * pVz * VP) + AinRe * (aSDt + pGam * VP);
+}
+
+// Time/Hybrid_function.F90:1-39
+template <typename R>
+__device__ inline R fsst(const Params& p, R Den, R vK, R vOmega, R Dist, R RmiuL, R CDiff) {
+    R Ref = R(p.Ref);
+    if (p.Kind_SubHY == 1 || p.Kind_SubHY == 3) {
+        R arg1 = sqrt(vK) / (R(0.09) * vOmega * Dist * Ref);
+        R arg2 = R(500.) * RmiuL / (Den * Dist * Dist * vOmega * Ref * Ref);
+        R arga = dmax(arg1, arg2);
+        R temp = dmax(Den * CDiff * Ref, R(1.0e-10));
+        R argb = R(4.) * Den * R(0.856) * vK / (temp * Dist * Dist);
+        R arg = dmin(arga, argb);
+        return tanh(arg * arg * arg * arg);
+    }
+    if (p.Kind_SubHY == 2) {
+        R arg1 = R(2.) * sqrt(vK) / (R(0.09) * vOmega * Dist * Ref);
+        R arg2 = R(500.) * RmiuL / (Den * Dist * Dist * vOmega * Ref * Ref);
+        R arg = dmax(arg1, arg2);
+        return tanh(arg * arg);
+    }
+    return R(0.0);
+}
+
+}  // namespace tg

@@ -1,0 +1,40 @@
+// k_fp64.cu -- FP64 kernels of the hot path.  Compiled with -fmad=false so that every FP64
+// expression rounds exactly as the reference's (built with -fp-model strict) would.
+#define TG_R double
+#define TG_NAME flux_launchers_f64
+#define TG_COMMON_KERNELS
+#include "flux_inst.cuh"
+
+namespace tg {
+void launch_specrad(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, double CFL_sub) {
+    if (nt > 0) k_specrad<<<nt, CELL_TILE, 0, s>>>(blks, tiles, p, CFL_sub);
+}
+void launch_bc_state(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, const Params& p, int turb) {
+    if (n > 0) k_bc_state<<<(n + 127) / 128, 128, 0, s>>>(blks, ent, n, p, turb);
+}
+void launch_bc_outlet(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const OutletLine* lines, int nl,
+                      const Params& p, int turb) {
+    if (nl > 0) k_bc_outlet<<<(nl + 63) / 64, 64, 0, s>>>(blks, ent, lines, nl, p, turb);
+}
+void launch_bc_grad(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, int turb) {
+    if (n > 0) k_bc_grad<<<(n + 127) / 128, 128, 0, s>>>(blks, ent, n, turb);
+}
+void launch_prims(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off) {
+    if (total > 0) k_prims<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off);
+}
+void launch_gradient(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int turb) {
+    if (nt > 0) k_gradient<<<nt, CELL_TILE, 0, s>>>(blks, tiles, turb);
+}
+void launch_shock_ghost(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt) {
+    if (nt > 0) k_shock_ghost<<<nt, CELL_TILE, 0, s>>>(blks, tiles);
+}
+void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts) {
+    if (nt > 0) k_update<<<nt, CELL_TILE, 0, s>>>(blks, tiles, p, turb_upd, parts);
+}
+void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int kind_dual) {
+    if (nt > 0) k_update_u<<<nt, CELL_TILE, 0, s>>>(blks, tiles, kind_dual);
+}
+void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off) {
+    if (total > 0) k_geom_static<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off);
+}
+}  // namespace tg

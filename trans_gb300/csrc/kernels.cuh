@@ -1,0 +1,1045 @@
+// kernels.cuh -- CUDA kernels of the TRANS hot path, templated on the flux arithmetic type R.
+//
+// One thread per interior cell, face or boundary face cell; blocks of every case are covered
+// by tile lists (a tile never straddles two blocks).  Kernel order within one sub-iteration:
+//   specrad -> bc_state (+ outlet lines) -> prims -> gradient -> shock_ghost -> bc_grad
+//   -> face_flux(i,j,k) -> gather -> lusgs_rhs -> sweep_L(h ascending) -> sweep_U(h descending)
+//   -> update (+ norms)
+// which is the order of main.F90:65-151.
+#pragma once
+#include "dev.cuh"
+#include "types.cuh"
+
+namespace tg {
+
+#ifdef TG_COMMON_KERNELS
+// ---------------------------------------------------------------------------------------
+// Time/SpectralRadius.F90:47-180
+// ---------------------------------------------------------------------------------------
+__global__ void k_specrad(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, double CFL_sub) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    int n = t.start + threadIdx.x;
+    int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+    int c = cidx(b, I, J, K);
+    const double* V = slot(b, S_V);
+    double Den = V[c];
+    double Vxi = slot(b, S_V + 1)[c] / Den;
+    double Vyi = slot(b, S_V + 2)[c] / Den;
+    double Vzi = slot(b, S_V + 3)[c] / Den;
+    double AAc = sqrt(1.4 * slot(b, S_PP)[c] / Den);
+    double TT = slot(b, S_T)[c];
+    double RmiuL = mu_suth<double>(p, TT);
+    double RmiuTL = slot(b, S_RMIU)[c];
+    double uvmu = (RmiuL + RmiuTL + 1.0e-20) * 4.0 / 3.0;
+    double uvmupr = (RmiuL / 0.72 + RmiuTL / 0.9 + 1.0e-20) * 1.4;
+    double pruvmu = dmax(uvmu, uvmupr) / Den;
+    double vol = slot(b, S_VOL)[c];
+    double rs = 0.0;
+    double Rd[3];
+    for (int d = 0; d < 3; ++d) {
+        double ARX = slot(b, S_ASD + 3 * d)[c], ARY = slot(b, S_ASD + 3 * d + 1)[c], ARZ = slot(b, S_ASD + 3 * d + 2)[c];
+        double STsq = ARX * ARX + ARY * ARY + ARZ * ARZ;
+        double UU = Vxi * ARX + Vyi * ARY + Vzi * ARZ + 0.0;
+        Rd[d] = fabs(UU) * (1.0 - 0.0) + sqrt(STsq) * AAc + 2.0 * STsq / vol * pruvmu / p.Ref;
+        slot(b, S_RDS + d)[c] = Rd[d];
+    }
+    rs = Rd[0] + Rd[1] + Rd[2];
+    double Dtm_local = vol / rs;
+    double dtm = p.IF_Local_Main == 1 ? p.CFL_Main * Dtm_local : p.DT_LUSGS_Main;
+    if (p.Kind_Dual != 0) dtm = p.IF_Local_Sub == 1 ? CFL_sub * Dtm_local : p.DT_LUSGS_Sub;
+    slot(b, S_DTM)[c] = dtm;
+}
+
+// ---------------------------------------------------------------------------------------
+// BC/BC_Wall.F90, BC/BC_far.F90, BC/BC_Symm.F90, BC/BC_Inlet.F90, BC/BC_P2P.F90 (sweep -1)
+// ---------------------------------------------------------------------------------------
+__device__ inline void farbond(double XM, double P2, double RR, double Vxi, double Vyi, double Vzi, double DNx, double DNy,
+                               double DNz, double VxF, double VyF, double VzF, double& PP0, double& RR0, double& VX0,
+                               double& VY0, double& VZ0, double& dir) {
+    const double pGam = 1.4;
+    double AF = 1.0 / XM;
+    double AE = sqrt(pGam * P2 / RR);
+    double QNE = Vxi * DNx + Vyi * DNy + Vzi * DNz;
+    double QNF = VxF * DNx + VyF * DNy + VzF * DNz;
+    double RF = QNF - 5.0 * AF;
+    double RE = QNE + 5.0 * AE;
+    double QN = 0.5 * (RE + RF);
+    double AS = 0.1 * (RE - RF);
+    if (QN > -AS && QN < 0.0) {
+        double SON = 1.0 / pGam / (XM * XM);
+        double QTX = VxF - QNF * DNx, QTY = VyF - QNF * DNy, QTZ = VzF - QNF * DNz;
+        VX0 = QTX + QN * DNx; VY0 = QTY + QN * DNy; VZ0 = QTZ + QN * DNz;
+        RR0 = pow(AS * AS / SON / pGam, 2.5);
+        PP0 = AS * AS * RR0 / pGam;
+        dir = -1.0;
+    }
+    if (QN >= 0.0 && QN < AS) {
+        double SON = P2 / pow(RR, pGam);
+        double QTX = Vxi - QNE * DNx, QTY = Vyi - QNE * DNy, QTZ = Vzi - QNE * DNz;
+        VX0 = QTX + QN * DNx; VY0 = QTY + QN * DNy; VZ0 = QTZ + QN * DNz;
+        RR0 = pow(AS * AS / SON / pGam, 2.5);
+        PP0 = AS * AS * RR0 / pGam;
+        dir = 1.0;
+    }
+    if (QN <= -AS) {
+        VX0 = VxF; VY0 = VyF; VZ0 = VzF;
+        RR0 = 1.0;
+        PP0 = 1.0 / pGam / XM / XM;
+        dir = -1.0;
+    }
+    if (QN >= AS) {
+        VX0 = Vxi; VY0 = Vyi; VZ0 = Vzi;
+        RR0 = RR; PP0 = P2;
+        dir = 1.0;
+    }
+}
+
+__global__ void k_bc_state(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n, Params p, int turb) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const BCEntry E = ent[e];
+    if (E.kind == 7) return;                       // outlets run line by line in k_bc_outlet
+    const DevBlock b = blks[E.blk];
+    double* V[7];
+    for (int m = 0; m < 7; ++m) V[m] = slot(b, S_V + m);
+    double* PP = slot(b, S_PP);
+    double* T = slot(b, S_T);
+    double* Rm = slot(b, S_RMIU);
+    const int s0 = E.s[0], l0 = E.l[0];
+    if (E.kind == 1) {                              // BC/BC_Wall.F90:42-117
+        double vibc = 0.0, vjbc = 0.0, vkbc = 0.0;   // zero grid speed (omega = 0)
+        for (int L = 0; L < 3; ++L) {
+            int is = E.s[L], il = E.l[L];
+            PP[il] = PP[is];
+            T[il] = T[is];
+            V[0][il] = PP[il] / (T[il] + p.Tiny) * p.RXM2;
+            double den = V[0][il];
+            V[1][il] = vibc * den;
+            V[2][il] = vjbc * den;
+            V[3][il] = vkbc * den;
+        }
+        if (turb) {
+            double Dn = slot(b, S_DST)[l0];
+            double Den = V[0][l0];
+            double TT = T[l0];
+            double Rmiuw = mu_suth<double>(p, TT);
+            double Omegaw = 60.0 * Rmiuw / (Den * 0.075 * Dn * Dn * p.Ref * p.Ref);
+            Rmiuw = Rm[s0];
+            for (int L = 0; L < 3; ++L) {
+                int il = E.l[L];
+                V[5][il] = 0.0;
+                V[6][il] = Omegaw;
+                Rm[il] = Rmiuw;
+            }
+        }
+    } else if (E.kind == 2) {                       // BC/BC_far.F90:40-118
+        int d = E.dir - 1;
+        double out_n = (double)(2 * E.lor - 4);
+        double grad = slot(b, S_GRAD + d)[E.face];
+        double Sout1 = slot(b, S_SD + 3 * d)[E.face] / grad;
+        double Sout2 = slot(b, S_SD + 3 * d + 1)[E.face] / grad;
+        double Sout3 = slot(b, S_SD + 3 * d + 2)[E.face] / grad;
+        double Dnx = Sout1 * out_n, Dny = Sout2 * out_n, Dnz = Sout3 * out_n;
+        double Den = V[0][s0];
+        double Vxi = V[1][s0] / Den, Vyi = V[2][s0] / Den, Vzi = V[3][s0] / Den;
+        double P2 = PP[s0];
+        double PP0 = 0, Den0 = 0, Vx0 = 0, Vy0 = 0, Vz0 = 0, dir = 0;
+        farbond(p.XM, P2, Den, Vxi, Vyi, Vzi, Dnx, Dny, Dnz, p.VxF, p.VyF, p.VzF, PP0, Den0, Vx0, Vy0, Vz0, dir);
+        V[0][l0] = 2 * Den0 - V[0][s0];
+        double den = V[0][l0];
+        V[1][l0] = 2.0 * Vx0 - Vxi;
+        V[2][l0] = 2.0 * Vy0 - Vyi;
+        V[3][l0] = 2.0 * Vz0 - Vzi;
+        PP[l0] = 2.0 * PP0 - P2;
+        T[l0] = p.RXM2 * PP[l0] / den;
+        for (int L = 1; L < 3; ++L) {
+            int ig = E.l[L];
+            for (int m = 0; m < 5; ++m) V[m][ig] = V[m][l0];
+            PP[ig] = PP[l0];
+            T[ig] = T[l0];
+        }
+        if (turb) {
+            if (dir > 0.0) {
+                V[5][l0] = V[5][s0];
+                V[6][l0] = V[6][s0];
+                Rm[l0] = Rm[s0];
+            } else {
+                double TT = T[l0];
+                double Dn = V[0][l0];
+                double RmiuFar = mu_suth<double>(p, TT);
+                Rm[l0] = 2.0 * p.VisRatio * RmiuFar - Rm[s0];
+                V[5][l0] = 2.0 * 1.5 * p.FSTI * p.FSTI * Dn - V[5][s0];
+                V[6][l0] = V[5][l0] / (Rm[l0] + p.Tiny) * Dn;
+            }
+            for (int L = 1; L < 3; ++L) {
+                int ig = E.l[L];
+                V[5][ig] = V[5][l0];
+                V[6][ig] = V[6][l0];
+                Rm[ig] = Rm[l0];
+            }
+        }
+    } else if (E.kind == 3) {                       // BC/BC_Symm.F90:42-110
+        int d = E.dir - 1;
+        double grad = slot(b, S_GRAD + d)[E.face];
+        double Sout1 = slot(b, S_SD + 3 * d)[E.face] / grad;
+        double Sout2 = slot(b, S_SD + 3 * d + 1)[E.face] / grad;
+        double Sout3 = slot(b, S_SD + 3 * d + 2)[E.face] / grad;
+        double den = V[0][s0];
+        double Vxi = V[1][s0] / den, Vyi = V[2][s0] / den, Vzi = V[3][s0] / den;
+        double Vc1 = Vxi * Sout1 + Vyi * Sout2 + Vzi * Sout3;
+        for (int L = 0; L < 3; ++L) {
+            int is = E.s[L], il = E.l[L];
+            if (L != 1) V[0][il] = V[0][is];       // the second ghost layer keeps its density (BC_Symm.F90:70-75)
+            V[1][il] = V[1][is] - 2 * Sout1 * Vc1 * V[0][is];
+            V[2][il] = V[2][is] - 2 * Sout2 * Vc1 * V[0][is];
+            V[3][il] = V[3][is] - 2 * Sout3 * Vc1 * V[0][is];
+            V[4][il] = V[4][is];
+            PP[il] = PP[is];
+            T[il] = T[is];
+        }
+        if (turb)
+            for (int L = 0; L < 3; ++L) {
+                int is = E.s[L], il = E.l[L];
+                V[5][il] = V[5][is];
+                V[6][il] = V[6][is];
+                Rm[il] = Rm[is];
+            }
+    } else if (E.kind == 5) {                       // BC/BC_Inlet.F90:38-110
+        double PsIn = PP[s0];
+        PsIn = dmin(PsIn, 0.999 * p.P0in);
+        double comm = dmax(1.0, pow(p.P0in / PsIn, 1.0 / 3.5));
+        double mach = sqrt((comm - 1.0) * 2 / 0.4);
+        double TsIn = p.T0in / comm;
+        double Roin = p.RXM2 * PsIn / TsIn;
+        double asonic = sqrt(1.4 * PsIn / Roin);
+        double Vabs = mach * asonic;
+        V[0][l0] = Roin;
+        V[1][l0] = Roin * Vabs;
+        V[2][l0] = Roin * (p.omega0 * slot(b, S_ZC)[s0]);
+        V[3][l0] = Roin * (-p.omega0 * slot(b, S_YC)[s0]);
+        double rr = p.omega0 * slot(b, S_RAD)[l0];
+        V[4][l0] = PsIn / 0.4 + 0.5 * (sq(V[1][l0]) + sq(V[2][l0]) + sq(V[3][l0])) / Roin - 0.5 * sq(rr) * Roin;
+        PP[l0] = PsIn;
+        T[l0] = TsIn;
+        for (int L = 1; L < 3; ++L) {
+            int ig = E.l[L];
+            for (int m = 0; m < 5; ++m) V[m][ig] = V[m][l0];
+            PP[ig] = PsIn;
+            T[ig] = TsIn;
+        }
+        if (turb) {
+            double TT = T[l0];
+            double RmiuIn = mu_suth<double>(p, TT);
+            Rm[l0] = p.VisRatio * RmiuIn;
+            double Den = V[0][l0];
+            V[5][l0] = 1.5 * p.FSTI * p.FSTI * Den;
+            V[6][l0] = V[5][l0] / (Rm[l0] + p.Tiny) * Den;
+            for (int L = 1; L < 3; ++L) {
+                int ig = E.l[L];
+                V[5][ig] = V[5][l0];
+                V[6][ig] = V[6][l0];
+                Rm[ig] = Rm[l0];
+            }
+        }
+    } else if (E.kind == 9) {                       // BC/BC_P2P.F90:76-139
+        const DevBlock r = blks[E.src_blk];
+        const double cost = E.cost, sint = E.sint;
+        for (int L = 0; L < 3; ++L) {
+            int is = E.s[L], il = E.l[L];
+            V[0][il] = slot(r, S_V)[is];
+            V[1][il] = slot(r, S_V + 1)[is];
+            double txy = slot(r, S_V + 2)[is], txz = slot(r, S_V + 3)[is];
+            V[2][il] = cost * txy + sint * txz;
+            V[3][il] = -sint * txy + cost * txz;
+            for (int m = 4; m < 7; ++m) V[m][il] = slot(r, S_V + m)[is];
+            PP[il] = slot(r, S_PP)[is];
+            T[il] = slot(r, S_T)[is];
+            Rm[il] = slot(r, S_RMIU)[is];
+        }
+    }
+}
+
+// BC/BC_Outlet.F90:50-106: the static pressure recurrence runs along j, one thread per line
+__global__ void k_bc_outlet(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent,
+                            const OutletLine* __restrict__ lines, int nl, Params p, int turb) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nl) return;
+    const OutletLine Ln = lines[q];
+    const DevBlock b = blks[Ln.blk];
+    double* V[7];
+    for (int m = 0; m < 7; ++m) V[m] = slot(b, S_V + m);
+    double* PP = slot(b, S_PP);
+    double* T = slot(b, S_T);
+    double* Rm = slot(b, S_RMIU);
+    const double* rad = slot(b, S_RAD);
+    const double* sint = slot(b, S_SINT);
+    const double* cost = slot(b, S_COST);
+    for (int e = Ln.first; e < Ln.first + Ln.n; ++e) {
+        const BCEntry E = ent[e];
+        int s0 = E.s[0], l0 = E.l[0];
+        T[l0] = T[s0];
+        if (E.sub == 1) {                              // j == Jbgn
+            PP[l0] = p.Pouthub;
+        } else {
+            int lm = l0 - b.PI;                         // (il, jl-1, kl)
+            double rcs1 = rad[l0], rcs2 = rad[lm];
+            double sinr = sint[lm], cosr = cost[lm];
+            double den = V[0][lm];
+            double RoVr2 = sq(V[3][lm] / den * cosr - sinr * V[2][lm] / den + p.omega0 * rcs2);
+            PP[l0] = PP[lm] + fabs((rcs1 - rcs2) * den * RoVr2) / (rcs2 + p.Tiny);
+        }
+        V[0][l0] = PP[l0] / T[l0] * p.RXM2;
+        double den_ratio = V[0][l0] / V[0][s0];
+        V[1][l0] = V[1][s0] * den_ratio;
+        V[2][l0] = V[2][s0] * den_ratio;
+        V[3][l0] = V[3][s0] * den_ratio;
+        for (int L = 1; L < 3; ++L) {
+            int ig = E.l[L];
+            for (int m = 0; m < 4; ++m) V[m][ig] = V[m][l0];
+            PP[ig] = PP[l0];
+            T[ig] = T[l0];
+        }
+        if (turb) {
+            V[5][l0] = V[5][s0];
+            V[6][l0] = V[6][s0];
+            Rm[l0] = Rm[s0];
+            for (int L = 1; L < 3; ++L) {
+                int ig = E.l[L];
+                V[5][ig] = V[5][l0];
+                V[6][ig] = V[6][l0];
+                Rm[ig] = Rm[l0];
+            }
+        }
+    }
+}
+
+// BC_Boundarys(0): gradients of the first ghost layer (BC/*.F90 sweep 0, BC/BC_P2P.F90:140-184)
+__global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n, int turb) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const BCEntry E = ent[e];
+    const DevBlock b = blks[E.blk];
+    const int il = E.l[0], is = E.s[0];
+    if (E.kind != 9) {
+        for (int L = 0; L < 18; ++L) slot(b, S_DQ + L)[il] = slot(b, S_DQ + L)[is];
+        return;
+    }
+    const DevBlock r = blks[E.src_blk];
+    double cost = E.cost, sint = E.sint;
+    double cos2t = cost * cost, sin2t = sint * sint, sct = sint * cost;
+    auto R_ = [&](int L) { return slot(r, S_DQ + L - 1)[is]; };
+    auto W_ = [&](int L, double v) { slot(b, S_DQ + L - 1)[il] = v; };
+    double ugx = R_(1), ugy = R_(2), ugz = R_(3);
+    double vgx = R_(4), vgy = R_(5), vgz = R_(6);
+    double wgx = R_(7), wgy = R_(8), wgz = R_(9);
+    W_(1, ugx);
+    W_(2, cost * ugy + sint * ugz);
+    W_(3, -sint * ugy + cost * ugz);
+    W_(4, cost * vgx + sint * wgx);
+    W_(5, cos2t * vgy + sct * (vgz + wgy) + sin2t * wgz);
+    W_(6, cos2t * vgz + sct * (-vgy + wgz) - sin2t * wgy);
+    W_(7, -sint * vgx + cost * wgx);
+    W_(8, -sin2t * vgz + sct * (-vgy + wgz) + cos2t * wgy);
+    W_(9, sin2t * vgy + sct * (vgz + wgy) + cos2t * wgz);
+    for (int LL = 4; LL <= 6; ++LL) {
+        int L = (LL - 1) * 3 + 1;
+        W_(L, R_(L));
+        double gy = R_(L + 1), gz = R_(L + 2);
+        W_(L + 1, cost * gy + sint * gz);
+        W_(L + 2, -sint * gy + cost * gz);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// primitives used by every stencil: u=V2/V1, v, w, k=V6/V1, omega=V7/V1, 1/V1 and V*(1/V1)
+// ---------------------------------------------------------------------------------------
+__global__ void k_prims(const DevBlock* __restrict__ blks, int nblk, long long total, const long long* __restrict__ off) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = nblk - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (off[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DevBlock b = blks[lo];
+    int c = (int)(g - off[lo]);
+    double v1 = slot(b, S_V)[c];
+    slot(b, S_PRIM)[c] = slot(b, S_V + 1)[c] / v1;
+    slot(b, S_PRIM + 1)[c] = slot(b, S_V + 2)[c] / v1;
+    slot(b, S_PRIM + 2)[c] = slot(b, S_V + 3)[c] / v1;
+    slot(b, S_PRIM + 3)[c] = slot(b, S_V + 5)[c] / v1;
+    slot(b, S_PRIM + 4)[c] = slot(b, S_V + 6)[c] / v1;
+    double ri = 1.0 / v1;
+    slot(b, S_RINV)[c] = ri;
+    slot(b, S_SVEL)[c] = slot(b, S_V + 1)[c] * ri;
+    slot(b, S_SVEL + 1)[c] = slot(b, S_V + 2)[c] * ri;
+    slot(b, S_SVEL + 2)[c] = slot(b, S_V + 3)[c] * ri;
+}
+
+#endif  // TG_COMMON_KERNELS
+
+// face average of a cell quantity at the face stored at cell cf (Space/SPACEINTERP_GetSurfCenterVars.F90)
+__device__ inline double favg(const double* q, const double* al, const double* ainv, int cf, int s) {
+    return (al[cf] * q[cf - s] + al[cf - s] * q[cf]) * ainv[cf];
+}
+
+#ifdef TG_COMMON_KERNELS
+// ---------------------------------------------------------------------------------------
+// Space/DIFF_DqDxyz.F90:25-74, 232-265, 300-381 (gradients and shock sensor, interior cells)
+// ---------------------------------------------------------------------------------------
+__global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, int turb) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    int n = t.start + threadIdx.x;
+    int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+    int c = cidx(b, I, J, K);
+    const int st[3] = {1, b.PI, b.PI * b.PJ};
+    double volinv = 1.0 / slot(b, S_VOL)[c];
+    const double* qs[6] = {slot(b, S_PRIM), slot(b, S_PRIM + 1), slot(b, S_PRIM + 2), slot(b, S_T),
+                           slot(b, S_PRIM + 3), slot(b, S_PRIM + 4)};
+    int nq = turb ? 6 : 4;
+    const double* SD = slot(b, S_SD);
+    double g9[3][3];
+    for (int q = 0; q < nq; ++q) {
+        double fw[3], fe[3];
+        for (int d = 0; d < 3; ++d) {
+            const double* al = slot(b, S_ALAGM + d);
+            const double* ai = slot(b, S_AINV + d);
+            fw[d] = favg(qs[q], al, ai, c, st[d]);
+            fe[d] = favg(qs[q], al, ai, c + st[d], st[d]);
+        }
+        for (int m = 0; m < 3; ++m) {
+            const double* S1 = SD + (size_t)(0 * 3 + m) * b.ncell;
+            const double* S2 = SD + (size_t)(1 * 3 + m) * b.ncell;
+            const double* S3 = SD + (size_t)(2 * 3 + m) * b.ncell;
+            double g = volinv * (fe[0] * S1[c + st[0]] - fw[0] * S1[c] + fe[1] * S2[c + st[1]] - fw[1] * S2[c]
+                                 + fe[2] * S3[c + st[2]] - fw[2] * S3[c]);
+            slot(b, S_DQ + 3 * q + m)[c] = g;
+            if (q < 3) g9[q][m] = g;
+        }
+    }
+    double DuDx = g9[0][0], DuDy = g9[0][1], DuDz = g9[0][2];
+    double DvDx = g9[1][0], DvDy = g9[1][1], DvDz = g9[1][2];
+    double DwDx = g9[2][0], DwDy = g9[2][1], DwDz = g9[2][2];
+    double W12 = (DuDy - DvDx) / 2.0, W13 = (DuDz - DwDx) / 2.0, W23 = (DvDz - DwDy) / 2.0;
+    double Vort = sqrt(2.0 * (2.0 * W12 * W12 + 2.0 * W13 * W13 + 2.0 * W23 * W23));
+    double DivU = sqrt(DuDx * DuDx + DvDy * DvDy + DwDz * DwDz);
+    slot(b, S_SHOCK)[c] = DivU * DivU / dmax(DivU * DivU + Vort * Vort, 1.0);
+}
+
+// shock of the three ghost layers of every face = shock of the adjacent interior cell
+// (Space/DIFF_DqDxyz.F90:388-396 restricted to the face ghosts the stencils read)
+__global__ void k_shock_ghost(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    int n = t.start + threadIdx.x;
+    // enumerate 6 faces x 3 layers of face cells
+    int nf[3] = {b.NJ1 * b.NK1, b.NI1 * b.NK1, b.NI1 * b.NJ1};
+    int d = 0;
+    while (n >= 6 * nf[d]) { n -= 6 * nf[d]; ++d; }
+    int side = n / (3 * nf[d]); n -= side * 3 * nf[d];
+    int L = n / nf[d] + 1; n -= (L - 1) * nf[d];
+    int i, j, k, ii, jj, kk;
+    if (d == 0) { j = n % b.NJ1 + 1; k = n / b.NJ1 + 1; i = side ? b.NI1 + L : 1 - L; ii = side ? b.NI1 : 1; jj = j; kk = k; }
+    else if (d == 1) { i = n % b.NI1 + 1; k = n / b.NI1 + 1; j = side ? b.NJ1 + L : 1 - L; jj = side ? b.NJ1 : 1; ii = i; kk = k; }
+    else { i = n % b.NI1 + 1; j = n / b.NI1 + 1; k = side ? b.NK1 + L : 1 - L; kk = side ? b.NK1 : 1; ii = i; jj = j; }
+    double* sh = slot(b, S_SHOCK);
+    sh[cidx(b, i, j, k)] = sh[cidx(b, ii, jj, kk)];
+}
+
+#endif  // TG_COMMON_KERNELS
+
+// ---------------------------------------------------------------------------------------
+// Face fluxes of direction DIR (faces 1..N along DIR, interior in the other two):
+//   Space/DIFFUSION_Centered.F90, Space/TURBTWO_DIFFUSION_Centered.F90,
+//   Space/CONVECT_MUSCL.F90 | Space/CONVECT_MDCD.F90, Space/TURBTWO_CONVECT_MUSCL.F90,
+//   Space/CONVECT_Roe_Original.F90 | Space/CONVECT_AUSMPW_Plus.F90, Space/TURBTWO_CONVECT_Upwind.F90
+// ---------------------------------------------------------------------------------------
+template <typename R, int DIR>
+__global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, int turb) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    int n = t.start + threadIdx.x;
+    const int ni = DIR == 1 ? b.NI : b.NI1, nj = DIR == 2 ? b.NJ : b.NJ1;
+    int i = n % ni + 1, j = (n / ni) % nj + 1, k = n / (ni * nj) + 1;
+    const int d = DIR - 1;
+    const int s = DIR == 1 ? 1 : (DIR == 2 ? b.PI : b.PI * b.PJ);
+    const int c = cidx(b, i, j, k);
+    const int cm = c - s, cp = c + s;
+    const double* al = slot(b, S_ALAGM + d);
+    const double* ainv = slot(b, S_AINV + d);
+    const double* pu = slot(b, S_PRIM);
+    const double* pv = slot(b, S_PRIM + 1);
+    const double* pw = slot(b, S_PRIM + 2);
+    const double* pk = slot(b, S_PRIM + 3);
+    const double* po = slot(b, S_PRIM + 4);
+    const double* PT = slot(b, S_T);
+    const double* PPp = slot(b, S_PP);
+    const double* SDd = slot(b, S_SD + 3 * d);
+    const size_t nc = (size_t)b.ncell;
+    double* FX = slot(b, S_FX + NFX * d);
+    // ---------------- viscous flux (DIFFUSION_Centered) ----------------
+    const bool wall = slot(b, S_WALL + d)[c] != 0.0;
+    const double vinv = slot(b, S_VINV + d)[c];
+    const double vall = slot(b, S_VOL)[cm] * vinv;
+    const double valr = slot(b, S_VOL)[c] * vinv;
+    const R alsinv = wall ? R(0.0) : R(vinv);
+    const double* qv[4] = {pu, pv, pw, PT};
+    R g[4][3];
+    for (int q = 0; q < 4; ++q) {
+        const double* Q = qv[q];
+        R disfpp = R(favg(Q, al, ainv, cp, s));
+        R disfnn = R(favg(Q, al, ainv, cm, s));
+        R disfp = R(Q[c]), disfn = R(Q[cm]);
+        const double* DQ0 = slot(b, S_DQ + 3 * q);
+        for (int m = 0; m < 3; ++m) {
+            const double* G = DQ0 + (size_t)m * nc;
+            R xL = R(vall) * R(G[cm]) + R(valr) * R(G[c]);
+            const double* S = SDd + (size_t)m * nc;
+            R cmv = alsinv * (-R(S[cp]) * (disfpp - disfp) - R(S[cm]) * (disfn - disfnn) + R(S[c]) * (disfp - disfn));
+            g[q][m] = cmv + xL;
+        }
+    }
+    const R a0 = R(al[c]), a1 = R(al[cm]);
+    const R ai = R(ainv[c]);
+    const R all = a0 * ai, alr = a1 * ai;
+    const R TTL = R(favg(PT, al, ainv, c, s));
+    const R RmiuL = mu_suth<R>(p, TTL);
+    const double* Rm = slot(b, S_RMIU);
+    R RmiuTL = all * R(Rm[cm]) + alr * R(Rm[c]);
+    if (wall) RmiuTL = R(0.0);
+    {
+        const R NMD = R(-2.0 / 3.0);
+        R DuDxL = g[0][0], DuDyL = g[0][1], DuDzL = g[0][2];
+        R DvDxL = g[1][0], DvDyL = g[1][1], DvDzL = g[1][2];
+        R DwDxL = g[2][0], DwDyL = g[2][1], DwDzL = g[2][2];
+        R DTDxL = g[3][0], DTDyL = g[3][1], DTDzL = g[3][2];
+        R div = DuDxL + DvDyL + DwDzL;
+        R Txx = RmiuL * (NMD * div + R(2.0) * DuDxL) + RmiuTL * (NMD * div + R(2.0) * DuDxL);
+        R Tyy = RmiuL * (NMD * div + R(2.0) * DvDyL) + RmiuTL * (NMD * div + R(2.0) * DvDyL);
+        R Tzz = RmiuL * (NMD * div + R(2.0) * DwDzL) + RmiuTL * (NMD * div + R(2.0) * DwDzL);
+        R Txy = RmiuL * (DuDyL + DvDxL) + RmiuTL * (DuDyL + DvDxL);
+        R Tyz = RmiuL * (DvDzL + DwDyL) + RmiuTL * (DvDzL + DwDyL);
+        R Tzx = RmiuL * (DuDzL + DwDxL) + RmiuTL * (DuDzL + DwDxL);
+        R cp_ = R(1.4) * R(p.PPF) / R(1.4 - 1.0);
+        R akmu = cp_ * (RmiuL / R(0.72) + RmiuTL / R(0.9));
+        R ucc = R(favg(pu, al, ainv, c, s)), vcc = R(favg(pv, al, ainv, c, s)), wcc = R(favg(pw, al, ainv, c, s));
+        R Phix = akmu * DTDxL + ucc * Txx + vcc * Txy + wcc * Tzx;
+        R Phiy = akmu * DTDyL + ucc * Txy + vcc * Tyy + wcc * Tyz;
+        R Phiz = akmu * DTDzL + ucc * Tzx + vcc * Tyz + wcc * Tzz;
+        R Dx = R(SDd[c]), Dy = R(SDd[c + nc]), Dz = R(SDd[c + 2 * nc]);
+        R Ref = R(p.Ref);
+        FX[(size_t)FX_VX * nc + c] = (double)((Txx * Dx + Txy * Dy + Tzx * Dz) / Ref);
+        FX[(size_t)FX_VY * nc + c] = (double)((Txy * Dx + Tyy * Dy + Tyz * Dz) / Ref);
+        FX[(size_t)FX_VZ * nc + c] = (double)((Tzx * Dx + Tyz * Dy + Tzz * Dz) / Ref);
+        FX[(size_t)FX_VE * nc + c] = (double)((Phix * Dx + Phiy * Dy + Phiz * Dz) / Ref);
+    }
+    // ---------------- k-omega diffusion (TURBTWO_DIFFUSION_Centered) ----------------
+    if (turb) {
+        R gt[2][3];
+        const double* qt[2] = {pk, po};
+        for (int q = 0; q < 2; ++q) {
+            const double* Q = qt[q];
+            R disfpp = R(favg(Q, al, ainv, cp, s));
+            R disfnn = R(favg(Q, al, ainv, cm, s));
+            R disfp = R(Q[c]), disfn = R(Q[cm]);
+            const double* DQ0 = slot(b, S_DQ + 12 + 3 * q);
+            for (int m = 0; m < 3; ++m) {
+                const double* G = DQ0 + (size_t)m * nc;
+                R xL = R(vall) * R(G[cm]) + R(valr) * R(G[c]);
+                const double* S = SDd + (size_t)m * nc;
+                R cmv = alsinv * (-R(S[cp]) * (disfpp - disfp) - R(S[cm]) * (disfn - disfnn) + R(S[c]) * (disfp - disfn));
+                gt[q][m] = cmv + xL;
+            }
+        }
+        R TTLt = all * R(PT[cm]) + alr * R(PT[c]);
+        R RmiuLt = mu_suth_nocs<R>(p, TTLt);
+        const double* V1 = slot(b, S_V);
+        R DEN0 = R(V1[c]), TKK0 = R(pk[c]), TOO0 = R(po[c]);
+        R DEN1 = R(V1[cm]), TKK1 = R(pk[cm]), TOO1 = R(po[cm]);
+        R Den = all * DEN1 + alr * DEN0;
+        R TKK = all * TKK1 + alr * TKK0;
+        R TOO = all * TOO1 + alr * TOO0;
+        R dTKO = gt[0][0] * gt[1][0] + gt[0][1] * gt[1][1] + gt[0][2] * gt[1][2];
+        R Sigo2 = R(p.Sigo2), Bs = R(p.Beta_star), Ref = R(p.Ref);
+        R CDKO = dmax(R(2.0) * Den * Sigo2 / TOO * (dTKO), R(1.0e-10));
+        const double* Dst = slot(b, S_DST);
+        R distfc = alr * R(Dst[c]) + all * R(Dst[cm]);
+        R arg1 = dmax(sqrt(TKK) / Bs / TOO / distfc / Ref, R(500.0) * RmiuLt / Den / distfc / distfc / TOO / Ref / Ref);
+        arg1 = dmin(arg1, R(4.0) * Den * Sigo2 * TKK / CDKO / distfc / distfc);
+        R a2 = arg1 * arg1;
+        R fc1c = tanh(a2 * a2);
+        R SigkAB = fc1c * R(p.Sigk1) + (R(1.0) - fc1c) * R(p.Sigk2);
+        R SigoAB = fc1c * R(p.Sigo1) + (R(1.0) - fc1c) * Sigo2;
+        R vmute = RmiuLt + RmiuTL * SigkAB;
+        R vmuoq = RmiuLt + RmiuTL * SigoAB;
+        R Dx = R(SDd[c]), Dy = R(SDd[c + nc]), Dz = R(SDd[c + 2 * nc]);
+        FX[(size_t)FX_TK * nc + c] = (double)((vmute * (gt[0][0] * Dx + gt[0][1] * Dy + gt[0][2] * Dz)) / Ref);
+        FX[(size_t)FX_TO * nc + c] = (double)((vmuoq * (gt[1][0] * Dx + gt[1][1] * Dy + gt[1][2] * Dz)) / Ref);
+    }
+    // ---------------- reconstruction ----------------
+    R qL[7], qR[7];
+    const double* qc[5] = {pu, pv, pw, PPp, PT};
+    if (p.Kind_Spatial == 2) {
+        for (int q = 0; q < 5; ++q) {
+            const double* Q = qc[q];
+            R fm = R(favg(Q, al, ainv, cm, s)), f0 = R(favg(Q, al, ainv, c, s)), fp = R(favg(Q, al, ainv, cp, s));
+            R q1 = R(Q[cm]), q0 = R(Q[c]);
+            R DR = f0 - q1, DL = q1 - fm;
+            qL[q] = q1 + alimiter(DR, DL);
+            DR = fp - q0; DL = q0 - f0;
+            qR[q] = q0 - alimiter(DL, DR);
+        }
+    } else {
+        const double* sh = slot(b, S_SHOCK);
+        R sensor = R(sh[c - 3 * s]);
+        sensor = dmax(sensor, R(sh[c - 2 * s]));
+        sensor = dmax(sensor, R(sh[c - s]));
+        sensor = dmax(sensor, R(sh[c]));
+        sensor = dmax(sensor, R(sh[c + s]));
+        sensor = dmax(sensor, R(sh[c + 2 * s]));
+        if (DIR == 3) sensor = dmax(sensor, R(0.0));
+        R gama = R(p.gama_min) + sensor * (R(p.gama_max) - R(p.gama_min));
+        for (int q = 0; q < 5; ++q) {
+            const double* Q = qc[q];
+            R s6[6];
+            for (int o = 0; o < 6; ++o) s6[o] = R(Q[c + (o - 3) * s]);
+            mdcd_pair(s6, gama, qL[q], qR[q]);
+        }
+    }
+    if (turb) {
+        const double* qk[2] = {pk, po};
+        for (int q = 0; q < 2; ++q) {
+            const double* Q = qk[q];
+            R fm = R(favg(Q, al, ainv, cm, s)), f0 = R(favg(Q, al, ainv, c, s)), fp = R(favg(Q, al, ainv, cp, s));
+            R q1 = R(Q[cm]), q0 = R(Q[c]);
+            R DR = f0 - q1, DL = q1 - fm;
+            qL[5 + q] = q1 + alimiter(DR, DL);
+            DR = fp - q0; DL = q0 - f0;
+            qR[5 + q] = q0 - alimiter(DL, DR);
+        }
+    }
+    // ---------------- inviscid flux ----------------
+    R sav1 = R(SDd[c]), sav2 = R(SDd[c + nc]), sav3 = R(SDd[c + 2 * nc]);
+    R sav = R(slot(b, S_GRAD + d)[c]);
+    R f[5];
+    if (p.Kind_Roe == 1)
+        roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
+    else
+        ausmpw_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
+    for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = (double)(f[L] * sav);
+    if (turb) {
+        R rcpcv = R(p.PPF);
+        R DENL = qL[3] / (rcpcv * qL[4]), DENR = qR[3] / (rcpcv * qR[4]);
+        R ulnormal = (sav1 * qL[0] + sav2 * qL[1] + sav3 * qL[2]);
+        R urnormal = (sav1 * qR[0] + sav2 * qR[1] + sav3 * qR[2]);
+        R rulnormal = DENL * ulnormal, rurnormal = DENR * urnormal;
+        const R small = R(1.e-10);
+        R eigTKO = R(0.5) * dmax(fabs(ulnormal), fabs(urnormal));
+        R TKL = dmax(qL[5], small), TKR = dmax(qR[5], small);
+        R dTK = R(-0.5) * (rulnormal * TKL + rurnormal * TKR - eigTKO * (DENR * TKR - DENL * TKL));
+        R TOL = dmax(qL[6], small), TOR = dmax(qR[6], small);
+        R dTO = R(-0.5) * (rulnormal * TOL + rurnormal * TOR - eigTKO * (DENR * TOR - DENL * TOL));
+        FX[(size_t)FX_CK * nc + c] = (double)dTK;
+        FX[(size_t)FX_CO * nc + c] = (double)dTO;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// D of every interior cell in the reference's accumulation order (main.F90:92-133):
+//   D = 0 - Fv(i) + Fv(i+1) - Fv(j) + Fv(j+1) - Fv(k) + Fv(k+1) - Fc(i) + Fc(i+1) - ...
+// ---------------------------------------------------------------------------------------
+template <typename R>
+__global__ void k_gather(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, int turb) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    int n = t.start + threadIdx.x;
+    int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+    int c = cidx(b, I, J, K);
+    const int st[3] = {1, b.PI, b.PI * b.PJ};
+    const size_t nc = (size_t)b.ncell;
+    const double* FX = slot(b, S_FX);
+    auto fx = [&](int d, int m, int cc) { return R(FX[(size_t)(NFX * d + m) * nc + cc]); };
+    {   // rho: no viscous flux
+        R acc = R(0.0);
+        for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_C0, c); acc = acc + fx(d, FX_C0, c + st[d]); }
+        slot(b, S_D)[c] = (double)acc;
+    }
+    for (int L = 1; L < 5; ++L) {
+        R acc = R(0.0);
+        for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_VX + L - 1, c); acc = acc + fx(d, FX_VX + L - 1, c + st[d]); }
+        for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_C0 + L, c); acc = acc + fx(d, FX_C0 + L, c + st[d]); }
+        slot(b, S_D + L)[c] = (double)acc;
+    }
+    if (turb) {
+        for (int q = 0; q < 2; ++q) {
+            R acc = R(0.0);
+            for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_TK + q, c); acc = acc + fx(d, FX_TK + q, c + st[d]); }
+            for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_CK + q, c); acc = acc + fx(d, FX_CK + q, c + st[d]); }
+            slot(b, S_D + 5 + q)[c] = (double)acc;
+        }
+    } else {
+        slot(b, S_D + 5)[c] = 0.0;
+        slot(b, S_D + 6)[c] = 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// F1 of SST per cell (Time/TURBTWO_TIME_LUSGS_SST.F90:265-273), read by the DES length scale
+// of the lexicographically next cell
+// ---------------------------------------------------------------------------------------
+template <typename R>
+__device__ inline R sst_fc1(const Params& p, const DevBlock& b, int c) {
+    R ARo = R(slot(b, S_V)[c]), ARTk = R(slot(b, S_V + 5)[c]), ARTO = R(slot(b, S_V + 6)[c]);
+    R cdif = R(slot(b, S_DQ + 12)[c]) * R(slot(b, S_DQ + 15)[c]) + R(slot(b, S_DQ + 13)[c]) * R(slot(b, S_DQ + 16)[c])
+             + R(slot(b, S_DQ + 14)[c]) * R(slot(b, S_DQ + 17)[c]);
+    R TT = R(slot(b, S_T)[c]);
+    R RmiuL = mu_suth<R>(p, TT);
+    R DistN = R(slot(b, S_DST)[c]);
+    R Ref = R(p.Ref), Sigo2 = R(p.Sigo2), Bs = R(p.Beta_star);
+    R CDKO = dmax(R(2.0) * ARo * Sigo2 / (ARTO / ARo) * cdif, R(1.0e-10));
+    R arg1 = dmax(sqrt(ARTk / ARo) / Bs / (ARTO / ARo) / DistN / Ref, R(500.0) * RmiuL / DistN / DistN / ARTO / Ref / Ref);
+    arg1 = dmin(arg1, R(4.0) * Sigo2 * ARTk / CDKO / DistN / DistN);
+    R a2 = arg1 * arg1;
+    return tanh(a2 * a2);
+}
+
+template <typename R>
+__global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    int n = t.start + threadIdx.x;
+    int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+    int c = cidx(b, I, J, K);
+    slot(b, S_FC1)[c] = (double)sst_fc1<R>(p, b, c);
+}
+
+// ---------------------------------------------------------------------------------------
+// Time/TIME_LUSGS.F90:60-108 and Time/TURBTWO_TIME_LUSGS_SST.F90:118-411: right-hand sides,
+// SST sources and the two diagonals
+// ---------------------------------------------------------------------------------------
+template <typename R>
+__global__ void k_lusgs_rhs(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, int turb) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    int n = t.start + threadIdx.x;
+    int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+    int c = cidx(b, I, J, K);
+    const double DT = p.DT_LUSGS_Main;
+    double Dtm = slot(b, S_DTM)[c];
+    double vol = slot(b, S_VOL)[c];
+    double stept = 2.0 * Dtm / (3.0 * Dtm / DT + 2.0);
+    double cvs = stept / vol;
+    slot(b, S_STEPT)[c] = stept;
+    slot(b, S_CVS)[c] = cvs;
+    for (int L = 0; L < 5; ++L) {
+        double* D = slot(b, S_D + L);
+        D[c] = D[c] / vol - (3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c]) * 0.5 / DT;
+    }
+    double rsum = slot(b, S_RDS)[c] + slot(b, S_RDS + 1)[c] + slot(b, S_RDS + 2)[c];
+    double fm = 1.0 + rsum * cvs;
+    slot(b, S_FM)[c] = fm;
+    if (!turb) return;
+    for (int L = 5; L < 7; ++L) {
+        double* D = slot(b, S_D + L);
+        D[c] = D[c] / vol - (3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c]) * 0.5 / DT;
+    }
+    auto G = [&](int q) { return R(slot(b, S_DQ + q)[c]); };
+    R dudx = G(0), dudy = G(1), dudz = G(2), dvdx = G(3), dvdy = G(4), dvdz = G(5), dwdx = G(6), dwdy = G(7), dwdz = G(8);
+    R dtkdx = G(12), dtkdy = G(13), dtkdz = G(14), dtodx = G(15), dtody = G(16), dtodz = G(17);
+    R Div = dudx + dvdy + dwdz;
+    R Votg = sq(dudy - dvdx) + sq(dvdz - dwdy) + sq(dwdx - dudz);
+    R prod = (R(2.0) * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) + sq(dudy + dvdx) + sq(dvdz + dwdy) + sq(dwdx + dudz)
+              - R(2.0 / 3.0) * Div * Div);
+    R cdif = dtkdx * dtodx + dtkdy * dtody + dtkdz * dtodz;
+    const R Ref = R(p.Ref), Bs = R(p.Beta_star), Sigo2 = R(p.Sigo2);
+    R tprod = dmin(prod, Votg) * R(slot(b, S_RMIU)[c]) / Ref;
+    R ARo = R(slot(b, S_V)[c]), ARTk = R(slot(b, S_V + 5)[c]), ARTO = R(slot(b, S_V + 6)[c]);
+    R tprodl1 = R(p.Prod_Lmt) * Bs * ARTk * ARTO / ARo * Ref;
+    tprod = dmin(tprod, tprodl1);
+    R TT = R(slot(b, S_T)[c]);
+    R RmiuL = mu_suth<R>(p, TT);
+    R Fdes = R(1.0);
+    if (p.Kind_Hybrid == 3) {
+        // DES length scale with the loop-carried F1 and omega of the previous interior cell
+        // (TURBTWO_TIME_LUSGS_SST.F90:192-213); the first cell uses F1 = 0 and its own omega
+        int np = n - 1;
+        R arg1p = R(0.0), Vomp = ARTO / ARo;
+        if (np >= 0) {
+            int Ip = np % b.NI1 + 1, Jp = (np / b.NI1) % b.NJ1 + 1, Kp = np / (b.NI1 * b.NJ1) + 1;
+            int cq = cidx(b, Ip, Jp, Kp);
+            arg1p = R(slot(b, S_FC1)[cq]);
+            Vomp = R(slot(b, S_V + 6)[cq]) / R(slot(b, S_V)[cq]);
+        }
+        R aLt = sqrt(ARTk / ARo) / (Bs * ARTO / ARo * Ref);
+        R Cdiff = (R(2. * 0.856) / Vomp) / Ref * cdif;
+        R vOmega = ARTO / ARo;
+        R Fsst = fsst<R>(p, ARo, ARTk / ARo, vOmega, R(slot(b, S_DST)[c]), RmiuL, Cdiff);
+        R aLgrd = ((R(1.) - arg1p) * R(0.61) + arg1p * R(0.78)) * R(slot(b, S_ALENG)[c]);
+        Fdes = dmax(aLt * (R(1.) - Fsst) / aLgrd, R(1.0));
+    }
+    R DistN = R(slot(b, S_DST)[c]);
+    R CDKO = dmax(R(2.0) * ARo * Sigo2 / (ARTO / ARo) * cdif, R(1.0e-10));
+    R arg1 = dmax(sqrt(ARTk / ARo) / Bs / (ARTO / ARo) / DistN / Ref, R(500.0) * RmiuL / DistN / DistN / ARTO / Ref / Ref);
+    arg1 = dmin(arg1, R(4.0) * Sigo2 * ARTk / CDKO / DistN / DistN);
+    R a2 = arg1 * arg1;
+    arg1 = tanh(a2 * a2);
+    R AA = sqrt(R(1.4) * R(slot(b, S_PP)[c]) / ARo);
+    R Mt = sqrt(ARTk / ARo) / AA;
+    const R Alf1 = R(1.0), Alf2 = R(0.4), Alf3 = R(0.2);
+    const R c23 = R(2.0 / 3.0);
+    R SourceP, SourceN1, Source, CnegTk, CnegTO;
+    if (p.IF_Comppress == 0) {
+        SourceP = tprod - c23 * dmin(Div, R(0.0)) * ARTk;
+        SourceN1 = -(c23 * dmax(Div, R(0.0))) - Bs * ARTO / ARo * Ref * Fdes;
+    } else {
+        SourceP = (R(1.) - (R(1.) - arg1) * Alf2 * Mt * Mt) * tprod - c23 * dmin(Div, R(0.0)) * ARTk;
+        SourceN1 = -(c23 * dmax(Div, R(0.0))) - (R(1.) + (R(1.) - arg1) * (Alf1 - Alf3) * Mt * Mt) * Bs * ARTO / ARo * Ref * Fdes;
+    }
+    Source = SourceP + SourceN1 * ARTk;
+    CnegTk = fabs(SourceN1);
+    if (p.If_fix_Transition && slot(b, S_XC)[c] < p.Trans_location) Source = R(0.0);
+    slot(b, S_D + 5)[c] = slot(b, S_D + 5)[c] + (double)Source;
+    tprod = dmin(prod, Votg) / Ref;
+    R GamaAB = R(p.Gama1) * arg1 + R(p.Gama2) * (R(1.0) - arg1);
+    R BetaAB = R(p.Beta1) * arg1 + R(p.Beta2) * (R(1.0) - arg1);
+    if (p.IF_Comppress == 0) {
+        SourceP = GamaAB * ARo * tprod - c23 * GamaAB * dmin(Div, R(0.0)) * ARTO;
+        SourceN1 = -(c23 * GamaAB * dmax(Div, R(0.0))) - BetaAB * ARTO / ARo * Ref;
+    } else {
+        SourceP = (GamaAB + (R(1.) - arg1) * Alf2 * Mt * Mt) * ARo * tprod - c23 * GamaAB * dmin(Div, R(0.0)) * ARTO;
+        SourceN1 = -(c23 * GamaAB * dmax(Div, R(0.0))) - (R(1.) - (R(1.) - arg1) * (Alf1 - Alf3) * Mt * Mt) * BetaAB * ARTO / ARo * Ref;
+    }
+    Source = SourceP + SourceN1 * ARTO;
+    R SourceCross = R(2.0) * (R(1) - arg1) * ARo * Sigo2 / (ARTO / ARo) * cdif / Ref;
+    SourceCross = sgn1(SourceCross) * dmin(fabs(SourceCross), fabs(SourceP) * R(0.5));
+    Source = Source + SourceCross;
+    slot(b, S_D + 6)[c] = slot(b, S_D + 6)[c] + (double)Source;
+    CnegTO = R(2.0) * fabs(SourceN1);
+    slot(b, S_FT)[c] = fm + (double)((CnegTk + CnegTO) * R(stept));
+}
+
+// ---------------------------------------------------------------------------------------
+// LU-SGS sweeps on one i+j+k hyperplane of every block (Time/TIME_LUSGS.F90:172-675,
+// Time/TURBTWO_TIME_LUSGS_SST.F90:562-766).  Any order of the (i-1,j-1,k-1) dependency graph
+// reproduces the lexicographic sweep exactly; hyperplanes are such an order.
+// ---------------------------------------------------------------------------------------
+template <typename R>
+__device__ inline void sweep_nb(const DevBlock& b, int d, int nbc, R sgn, int turb, R* out5, R* out2) {
+    R roinv = R(slot(b, S_RINV)[nbc]);
+    R pVx = R(slot(b, S_SVEL)[nbc]), pVy = R(slot(b, S_SVEL + 1)[nbc]), pVz = R(slot(b, S_SVEL + 2)[nbc]);
+    R aSDx = R(slot(b, S_ASD + 3 * d)[nbc]), aSDy = R(slot(b, S_ASD + 3 * d + 1)[nbc]), aSDz = R(slot(b, S_ASD + 3 * d + 2)[nbc]);
+    R Din[5];
+    for (int L = 0; L < 5; ++L) Din[L] = R(slot(b, S_D + L)[nbc]);
+    R Dif[5];
+    lusgs_adq<R>(pVx, pVy, pVz, aSDx, aSDy, aSDz, R(slot(b, S_PP)[nbc]), roinv, Din[0], Din[1], Din[2], Din[3], Din[4], Dif);
+    R RDSt = R(slot(b, S_RDS + d)[nbc]);
+    for (int L = 0; L < 5; ++L) out5[L] = R(0.5) * (Dif[L] + sgn * (RDSt * Din[L]));
+    if (turb) {
+        R VP = pVx * aSDx + pVy * aSDy + pVz * aSDz;
+        for (int q = 0; q < 2; ++q) {
+            R Dq = R(slot(b, S_D + 5 + q)[nbc]);
+            out2[q] = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
+        }
+    }
+}
+
+template <typename R, bool LOWER>
+__global__ void k_sweep(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, int first, int count, int turb) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const SweepCell sc = cells[first + e];
+    const DevBlock b = blks[sc.blk];
+    const int I = sc.i, J = sc.j, K = sc.k;
+    const int c = cidx(b, I, J, K);
+    const int st[3] = {1, b.PI, b.PI * b.PJ};
+    const bool has[3] = {LOWER ? I != 1 : I != b.NI1, LOWER ? J != 1 : J != b.NJ1, LOWER ? K != 1 : K != b.NK1};
+    const R sgn = LOWER ? R(1.0) : R(-1.0);
+    R acc5[3][5], acc2[3][2];
+    for (int d = 0; d < 3; ++d) {
+        for (int L = 0; L < 5; ++L) acc5[d][L] = R(0.0);
+        acc2[d][0] = acc2[d][1] = R(0.0);
+        if (has[d]) sweep_nb<R>(b, d, LOWER ? c - st[d] : c + st[d], sgn, turb, acc5[d], acc2[d]);
+    }
+    R stept = R(slot(b, S_STEPT)[c]), cvs = R(slot(b, S_CVS)[c]), fm = R(slot(b, S_FM)[c]);
+    for (int L = 0; L < 5; ++L) {
+        double* D = slot(b, S_D + L);
+        R sum = acc5[0][L] + acc5[1][L] + acc5[2][L];
+        if (LOWER) D[c] = (double)((R(D[c]) * stept + sum * cvs) / fm);
+        else D[c] = (double)(R(D[c]) - sum * cvs / fm);
+    }
+    if (turb) {
+        R ft = R(slot(b, S_FT)[c]);
+        for (int q = 0; q < 2; ++q) {
+            double* D = slot(b, S_D + 5 + q);
+            R sum = acc2[0][q] + acc2[1][q] + acc2[2][q];
+            if (LOWER) D[c] = (double)((R(D[c]) * stept + sum * cvs) / ft);
+            else D[c] = (double)(R(D[c]) - sum * cvs / ft);
+        }
+    }
+}
+
+#ifdef TG_COMMON_KERNELS
+// ---------------------------------------------------------------------------------------
+// Time/TIME_Update_V.F90:106-294 (norms) and :502-859 (update), FP64 in both paths
+// ---------------------------------------------------------------------------------------
+__global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, int turb_upd,
+                         NormPart* __restrict__ parts) {
+    const Tile t = tiles[blockIdx.x];
+    const DevBlock b = blks[t.blk];
+    __shared__ double s_sum[3][256];
+    __shared__ double s_max[3][256];
+    __shared__ long long s_idx[256];
+    __shared__ int s_nan[256];
+    int tid = threadIdx.x;
+    double sa = 0, ma = -1, sk = 0, mk = 0, so = 0, mo = 0;
+    long long ia = -1;
+    int nanf = 0;
+    if (tid < t.count) {
+        int n = t.start + tid;
+        int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+        int c = cidx(b, I, J, K);
+        double* V[7];
+        for (int m = 0; m < 7; ++m) V[m] = slot(b, S_V + m);
+        double* PP = slot(b, S_PP);
+        double* T = slot(b, S_T);
+        double v1 = V[0][c];
+        double d1 = slot(b, S_D)[c], d6 = slot(b, S_D + 5)[c], d7 = slot(b, S_D + 6)[c];
+        double DR = fabs(d1 / v1);
+        nanf = isnan(d1) ? 1 : 0;
+        sa = DR * DR; ma = DR; ia = n;
+        double DRk = fabs(d6 / v1), DRo = fabs(d7 / v1);
+        sk = DRk * DRk; mk = DRk; so = DRo * DRo; mo = DRo;
+        // mean flow (non-preconditioned, TIME_Update_V.F90:621-689)
+        double AinRo = d1, AinRx = slot(b, S_D + 1)[c], AinRy = slot(b, S_D + 2)[c], AinRz = slot(b, S_D + 3)[c];
+        double AinRe = slot(b, S_D + 4)[c];
+        double pRo = v1;
+        double roinv = 1.0 / pRo;
+        double pVx = V[1][c] * roinv, pVy = V[2][c] * roinv, pVz = V[3][c] * roinv;
+        double AinX = (AinRx - pVx * AinRo) * roinv;
+        double AinY = (AinRy - pVy * AinRo) * roinv;
+        double AinZ = (AinRz - pVz * AinRo) * roinv;
+        double AinP = (1.4 - 1.0) * (AinRe - 0.5 * AinRo * (pVx * pVx + pVy * pVy + pVz * pVz) - pRo * (AinX * pVx + AinY * pVy + AinZ * pVz));
+        if (AinRo >= 0.) pRo = pRo + AinRo;
+        else pRo = pRo * exp(AinRo / (pRo + 1.e-10));
+        pRo = fabs(pRo);
+        double pp = PP[c];
+        if (AinP >= 0.) pp = pp + AinP;
+        else pp = pp * exp(AinP / (pp + 1.e-10));
+        pp = fabs(pp);
+        PP[c] = pp;
+        T[c] = p.RXM2 * pp / pRo;
+        pVx = pVx + AinX; pVy = pVy + AinY; pVz = pVz + AinZ;
+        V[0][c] = pRo;
+        V[1][c] = pRo * pVx;
+        V[2][c] = pRo * pVy;
+        V[3][c] = pRo * pVz;
+        double DV = 0.5 * (pVx * pVx + pVy * pVy + pVz * pVz);
+        double rr = p.omega0 * slot(b, S_RAD)[c];
+        V[4][c] = pp / (1.4 - 1.0) + DV * pRo - 0.5 * sq(rr) * pRo;
+        if (turb_upd) {   // TIME_Update_V.F90:709-816
+            double ARTk = V[5][c], ARTO = V[6][c];
+            if (d6 >= 0.0) ARTk = ARTk + d6;
+            else ARTk = ARTk * exp(d6 / (ARTk + 1.e-10));
+            ARTk = dmax(ARTk, 1.0e-10);
+            if (d7 >= 0.0) ARTO = ARTO + d7;
+            else ARTO = ARTO * exp(d7 / (ARTO + 1.e-10));
+            ARTO = dmax(ARTO, 1.0e-10);
+            double VV = sq(V[1][c]) + sq(V[2][c]) + sq(V[3][c]);
+            double PPP = (1.4 - 1.0) * V[4][c] - 0.5 * (1.4 - 1.0) * (VV / pRo - sq(rr) * pRo);
+            double TT = p.RXM2 * PPP / pRo;
+            double RmiuL = mu_suth<double>(p, TT);
+            double DistN = slot(b, S_DST)[c];
+            auto G = [&](int q) { return slot(b, S_DQ + q)[c]; };
+            double Dudx = G(0), Dudy = G(1), Dudz = G(2), Dvdx = G(3), Dvdy = G(4), Dvdz = G(5), Dwdx = G(6), Dwdy = G(7), Dwdz = G(8);
+            double Div = Dudx + Dvdy + Dwdz;
+            double prod = (2.0 * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy) + sq(Dwdx + Dudz)
+                           - 2.0 / 3.0 * Div * Div);
+            double arg2 = 2.0 * sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
+            arg2 = dmax(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
+            arg2 = tanh(arg2 * arg2);
+            double Sii = Dudx, Sjj = Dvdy, Skk = Dwdz;
+            double Sij = (Dudy + Dvdx) / 2.0, Sik = (Dudz + Dwdx) / 2.0, Sjk = (Dvdz + Dwdy) / 2.0;
+            double Skl = sqrt(2.0 * (1.0 * Sii * Sii + 1.0 * Sjj * Sjj + 1.0 * Skk * Skk + 2.0 * Sij * Sij + 2.0 * Sik * Sik + 2.0 * Sjk * Sjk));
+            double Cmua = dmin(1.0, p.A1 * ARTO / pRo / ((Skl) * arg2 + 1.e-10) * p.Ref);
+            ARTO = dmax(ARTO, sqrt(pRo * Cmua * fabs(prod) / (p.Prod_Lmt * p.Beta_star)) / p.Ref);
+            ARTk = dmin(ARTk, 100000.0 * RmiuL * ARTO / pRo / Cmua);
+            V[5][c] = ARTk;
+            V[6][c] = ARTO;
+            slot(b, S_RMIU)[c] = Cmua * ARTk / ARTO * pRo;
+        }
+    }
+    s_sum[0][tid] = sa; s_sum[1][tid] = sk; s_sum[2][tid] = so;
+    s_max[0][tid] = ma; s_max[1][tid] = mk; s_max[2][tid] = mo;
+    s_idx[tid] = ia; s_nan[tid] = nanf;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (tid < w) {
+            for (int q = 0; q < 3; ++q) s_sum[q][tid] += s_sum[q][tid + w];
+            // max of |D1/V1| with the later cell winning ties (IF(DUa<=DR), TIME_Update_V.F90:135)
+            double a = s_max[0][tid], bb = s_max[0][tid + w];
+            if (bb > a || (bb == a && s_idx[tid + w] > s_idx[tid])) { s_max[0][tid] = bb; s_idx[tid] = s_idx[tid + w]; }
+            s_max[1][tid] = dmax(s_max[1][tid], s_max[1][tid + w]);
+            s_max[2][tid] = dmax(s_max[2][tid], s_max[2][tid + w]);
+            s_nan[tid] |= s_nan[tid + w];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        NormPart P;
+        P.sa = s_sum[0][0]; P.sk = s_sum[1][0]; P.so = s_sum[2][0];
+        P.ma = s_max[0][0]; P.mk = s_max[1][0]; P.mo = s_max[2][0];
+        P.ia = s_idx[0]; P.nan = s_nan[0]; P.pad_ = 0;
+        parts[blockIdx.x] = P;
+    }
+}
+
+// Time/TIME_Update_U.F90:16-44
+__global__ void k_update_u(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, int kind_dual) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    int n = t.start + threadIdx.x;
+    int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+    int c = cidx(b, I, J, K);
+    for (int L = 0; L < 7; ++L) {
+        if (kind_dual == 2) slot(b, S_WT1 + L)[c] = slot(b, S_WT0 + L)[c];
+        slot(b, S_WT0 + L)[c] = slot(b, S_V + L)[c];
+    }
+}
+
+// static metric products (computed once per geometry upload)
+__global__ void k_geom_static(const DevBlock* __restrict__ blks, int nblk, long long total, const long long* __restrict__ off) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = nblk - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (off[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DevBlock b = blks[lo];
+    int c = (int)(g - off[lo]);
+    int i = c % b.PI, j = (c / b.PI) % b.PJ, k = c / (b.PI * b.PJ);
+    const int st[3] = {1, b.PI, b.PI * b.PJ};
+    const int pos[3] = {i, j, k};
+    const int ext[3] = {b.PI, b.PJ, b.PK};
+    for (int d = 0; d < 3; ++d) {
+        if (pos[d] >= 1) {
+            const double* al = slot(b, S_ALAGM + d);
+            slot(b, S_AINV + d)[c] = 1.0 / (al[c] + al[c - st[d]]);
+            const double* vo = slot(b, S_VOL);
+            slot(b, S_VINV + d)[c] = 1.0 / (vo[c] + vo[c - st[d]]);
+        }
+        if (pos[d] + 1 < ext[d])
+            for (int m = 0; m < 3; ++m) {
+                const double* S = slot(b, S_SD + 3 * d + m);
+                slot(b, S_ASD + 3 * d + m)[c] = 0.5 * (S[c] + S[c + st[d]]);
+            }
+    }
+}
+
+#endif  // TG_COMMON_KERNELS
+
+}  // namespace tg

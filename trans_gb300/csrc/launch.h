@@ -1,0 +1,39 @@
+// launch.h -- host-side launchers of the hot-path kernels (defined in k_fp64.cu / k_mixed.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "dev.cuh"
+
+namespace tg {
+struct BCEntry;
+struct OutletLine;
+struct SweepCell;
+struct NormPart;
+
+// FP64 kernels shared by both precision modes
+void launch_specrad(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, double CFL_sub);
+void launch_bc_state(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, const Params& p, int turb);
+void launch_bc_outlet(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const OutletLine* lines, int nl,
+                      const Params& p, int turb);
+void launch_bc_grad(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, int turb);
+void launch_prims(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
+void launch_gradient(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int turb);
+void launch_shock_ghost(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt);
+void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts);
+void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int kind_dual);
+void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
+
+// flux, source and sweep kernels, instantiated per arithmetic type
+struct FluxLaunchers {
+    void (*face_flux[3])(cudaStream_t, const DevBlock*, const Tile*, int, const Params&, int);
+    void (*gather)(cudaStream_t, const DevBlock*, const Tile*, int, int);
+    void (*sst_fc1)(cudaStream_t, const DevBlock*, const Tile*, int, const Params&);
+    void (*lusgs_rhs)(cudaStream_t, const DevBlock*, const Tile*, int, const Params&, int);
+    void (*sweep_lower)(cudaStream_t, const DevBlock*, const SweepCell*, int, int, int);
+    void (*sweep_upper)(cudaStream_t, const DevBlock*, const SweepCell*, int, int, int);
+};
+const FluxLaunchers& flux_launchers_f64();
+const FluxLaunchers& flux_launchers_f32();
+
+constexpr int CELL_TILE = 256;
+constexpr int FACE_TILE = 128;
+}  // namespace tg

@@ -1,0 +1,29 @@
+// types.cuh -- host/device tables of the boundary gathers, sweeps and residual norms.
+#pragma once
+#include "dev.cuh"
+
+namespace tg {
+
+struct BCEntry {          // one boundary face cell of one connection (BC/Boundary.F90 dispatch)
+    int kind, blk, conn, sub;
+    int i, j, k, src_blk;           // face cell (node-face index along the normal)
+    int s[3], l[3];                 // interior source cells (layers 0,1,2) and ghost cells (1,2,3)
+    int face;                       // face cell index for SD/Grad (i + IJKAdd)
+    int dir;                        // IJKDirect (1..3)
+    int lor, pad_;                  // LeftOrRight
+    double cost, sint;              // interface rotation
+};
+
+struct OutletLine {       // one line of an outlet segment along j (BC/BC_Outlet.F90:50-106)
+    int blk, n, first, pad_;        // entries [first, first+n) of the BC table, ascending j
+};
+
+struct SweepCell { int blk, i, j, k; };
+
+struct NormPart {         // per-tile partial residual norms (Time/TIME_Update_V.F90:106-294)
+    double sa, ma, sk, mk, so, mo;
+    long long ia;                   // lexicographic index of the max of |D1/V1|
+    int nan, pad_;
+};
+
+}  // namespace tg

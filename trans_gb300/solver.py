@@ -1,0 +1,123 @@
+"""Python driver over the C ABI of include/trans_gpu.h.
+
+``Solver`` plays the role of the reference's main program (main.F90): it hands the blocks,
+connectivity, geometry and initial state of a case to an implementation of the ABI, then
+iterates.  The implementation is the CUDA library of this package by default; any other
+library exporting the same entry points under another prefix can be driven the same way.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .case import fortran_view, full_from_fortran, markwall_arrays
+
+GEOMETRY_FIELDS = ("SD", "GRAD", "VOL", "ALAGM", "DST", "ALENG", "ASENG", "XC", "YC", "ZC", "RAD", "THTC")
+STATE_FIELDS = ("V", "PP", "T", "RMIU", "WT0", "WT1")
+
+
+class SolverError(RuntimeError):
+    pass
+
+
+class Solver:
+    def __init__(self, case, conns, geo, state, lib=None, prefix="trans_", params=None):
+        if lib is None:
+            from . import native
+            lib = native.load()
+        self.lib = lib
+        self.pre = prefix
+        self.case = case
+        self.params = params if params is not None else case.params
+        self.blocks = case.blocks
+        self._keep = []
+        nb = len(self.blocks)
+        tb = (abi.TransBlock * nb)()
+        for n, b in enumerate(self.blocks):
+            ni, nj, nk = b.dims
+            cl = conns[b.id]
+            carr = (abi.TransConn * len(cl))(*cl)
+            mw = markwall_arrays(b)
+            self._keep += [carr, mw]
+            tb[n].ni, tb[n].nj, tb[n].nk, tb[n].id = ni, nj, nk, b.id
+            tb[n].nconn = len(cl)
+            tb[n].conn = C.cast(carr, C.POINTER(abi.TransConn))
+            for f in range(6):
+                tb[n].markwall[f] = mw[f].ctypes.data_as(C.POINTER(C.c_int))
+        self._keep.append(tb)
+        ctx = C.c_void_p()
+        rc = self._fn("create")(C.byref(self.params), nb, tb, C.byref(ctx))
+        if rc != 0:
+            raise SolverError(f"{prefix}create failed ({rc}: {abi.ERRORS.get(rc, '?')})")
+        self.ctx = ctx
+        for n, b in enumerate(self.blocks):
+            for name in GEOMETRY_FIELDS:
+                self.set_field(n, name, geo[b.id][name])
+            for name in STATE_FIELDS:
+                self.set_field(n, name, state[b.id][name])
+
+    def _fn(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = ""
+            if self.pre == "trans_":
+                m = self.lib.trans_last_error(self.ctx)
+                msg = m.decode() if m else ""
+            raise SolverError(f"{self.pre}{what} failed ({rc}: {abi.ERRORS.get(rc, '?')}) {msg}")
+
+    def set_field(self, ib, name, full):
+        ni, nj, nk = self.blocks[ib].dims
+        f = fortran_view(name, full)
+        assert f.shape == abi.field_shape(name, ni, nj, nk), (name, f.shape)
+        self._check(self._fn("set_field")(self.ctx, ib, abi.FIELD_ID[name], f.ctypes.data_as(C.POINTER(C.c_double))),
+                    "set_field")
+
+    def get_field(self, ib, name, full=True):
+        ni, nj, nk = self.blocks[ib].dims
+        f = np.zeros(abi.field_shape(name, ni, nj, nk), order="F")
+        self._check(self._fn("get_field")(self.ctx, ib, abi.FIELD_ID[name], f.ctypes.data_as(C.POINTER(C.c_double))),
+                    "get_field")
+        return full_from_fortran(name, f, ni, nj, nk) if full else f
+
+    def iterate(self, ki):
+        nb = len(self.blocks)
+        norms = (abi.TransNorms * nb)()
+        rc = self._fn("iterate")(self.ctx, ki, norms)
+        if rc == abi.TRANS_E_NAN:
+            raise SolverError(f"NaN in iteration {ki}")
+        self._check(rc, "iterate")
+        return [{f: getattr(x, f) for f, _ in abi.TransNorms._fields_} for x in norms]
+
+    def run_stage(self, stage, ki, itr=1):
+        sid = abi.STAGE_ID[stage] if isinstance(stage, str) else stage
+        self._check(self._fn("run_stage")(self.ctx, sid, ki, itr), "run_stage")
+
+    def norms(self):
+        nb = len(self.blocks)
+        norms = (abi.TransNorms * nb)()
+        self._check(self._fn("get_norms")(self.ctx, norms), "get_norms")
+        return [{f: getattr(x, f) for f, _ in abi.TransNorms._fields_} for x in norms]
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self._fn("destroy")(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def global_residual(norms, blocks):
+    """sqrt(sum N_b DRSa_b^2 / sum N_b): the block RMS norms of TIME_Update_V aggregated."""
+    num = 0.0
+    den = 0
+    for nrm, b in zip(norms, blocks):
+        n = int(np.prod([d - 1 for d in b.dims]))
+        num += n * nrm["DRSa"] ** 2
+        den += n
+    return float(np.sqrt(num / den))
