@@ -1,0 +1,299 @@
+"""Benchmark of the TRANS per-iteration hot path on GB300.
+
+One step = one outer iteration (one pass of the hot path, Kchld = 1 sub-iteration) over every
+interior cell of the workload.  The metric is cell-iterations per second (Mcell-iter/s).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--case cascade|channel]
+                  [--precision fp64|mixed] [--impl gb300|reference]
+
+--impl reference times the reference's algorithm on the host cores: the C++ FP64 restatement
+in oracle/ (the Fortran reference cannot be built here), parallel over blocks with OpenMP as
+the reference is parallel over blocks with MPI.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from trans_gb300 import abi  # noqa: E402
+from trans_gb300 import case as CS  # noqa: E402
+from trans_gb300 import cases  # noqa: E402
+from trans_gb300.solver import Solver, STATE_FIELDS  # noqa: E402
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+
+
+def make_case(name, precision):
+    prec = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
+    if name == "channel":
+        c = cases.channel_bump(precision=prec)
+    elif name == "cascade":
+        c = cases.cascade(precision=prec)
+    else:
+        raise SystemExit(f"unknown case {name}")
+    conns, geo = CS.compute_geometry(c)
+    st = CS.initial_state(c, geo, Q_dst=c.meta.get("Q_dst", 0.01))
+    return c, conns, geo, st
+
+
+def interior_cells(c):
+    return int(sum(np.prod([d - 1 for d in b.dims]) for b in c.blocks))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(PEAKS_FILE))
+    except Exception:
+        return {}
+
+
+def time_resident(s, ki0, steps):
+    ms = C.c_double()
+    nb = len(s.blocks)
+    norms = (abi.TransNorms * nb)()
+    rc = s.lib.trans_time_iterations(s.ctx, ki0, steps, C.byref(ms), norms)
+    if rc != 0:
+        raise RuntimeError(f"trans_time_iterations failed {rc}: {s.lib.trans_last_error(s.ctx)}")
+    return ms.value
+
+
+def pinned_copy(arr):
+    """A page-locked host copy of a Fortran array (the caller's buffers in the end-to-end leg)."""
+    import torch
+    t = torch.empty(arr.size, dtype=torch.float64, pin_memory=True)
+    out = t.numpy().reshape(arr.shape, order="F")
+    out[...] = arr
+    return out, t
+
+
+def run_e2e(s, c, st, ki0, steps):
+    """Per step through the C ABI with host buffers: upload the state (V, PP, T, Rmiu, Wt0,
+    Wt1 as the Fortran caller holds them), iterate, download V, PP, T, Rmiu and the norms."""
+    lib = s.lib
+    keep = []
+    up, down = [], []
+    h2d = d2h = 0
+    for ib, b in enumerate(c.blocks):
+        for name in STATE_FIELDS:
+            a, t = pinned_copy(CS.fortran_view(name, st[b.id][name]))
+            keep.append(t)
+            up.append((ib, abi.FIELD_ID[name], a))
+            h2d += a.nbytes
+        for name in ("V", "PP", "T", "RMIU"):
+            shape = abi.field_shape(name, *b.dims)
+            a, t = pinned_copy(np.zeros(shape, order="F"))
+            keep.append(t)
+            down.append((ib, abi.FIELD_ID[name], a))
+            d2h += a.nbytes
+    nb = len(c.blocks)
+    norms = (abi.TransNorms * nb)()
+    d2h += C.sizeof(norms)
+    dp = C.POINTER(C.c_double)
+    lib.trans_sync(s.ctx)
+    t0 = time.perf_counter()
+    for q in range(steps):
+        for ib, fid, a in up:
+            lib.trans_set_field(s.ctx, ib, fid, a.ctypes.data_as(dp))
+        rc = lib.trans_iterate(s.ctx, ki0 + q, norms)
+        if rc != 0:
+            raise RuntimeError(f"iterate failed {rc}")
+        for ib, fid, a in down:
+            lib.trans_get_field(s.ctx, ib, fid, a.ctypes.data_as(dp))
+    lib.trans_sync(s.ctx)
+    dt = time.perf_counter() - t0
+    return dt, h2d, d2h
+
+
+def cpu_sample(c, conns, geo, st, seconds=15.0):
+    """The oracle on the host cores for a bounded number of iterations of the same workload."""
+    from oracle.oracle import OracleSolver
+    o = OracleSolver(c, conns, geo, st)
+    o.iterate(1)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.iterate(2 + n)
+        n += 1
+        if time.perf_counter() - t0 > seconds or n >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return interior_cells(c) * n / dt / 1e6, n, dt
+
+
+def reference_arm(args):
+    """--impl reference: the reference algorithm on the host cores (oracle, OpenMP over blocks)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    c, conns, geo, st = make_case(args.case, "fp64")
+    from oracle.oracle import OracleSolver
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    o = OracleSolver(c, conns, geo, st)
+    for w in range(args.warmup):
+        o.iterate(1 + w)
+    t0 = time.perf_counter()
+    for q in range(args.steps):
+        o.iterate(1 + args.warmup + q)
+    dt = time.perf_counter() - t0
+    ncell = interior_cells(c)
+    v = ncell * args.steps / dt / 1e6
+    line = {"metric": "Mcell-iter/s", "value": v, "unit": "Mcell-iter/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": c.name, "cells": ncell, "blocks": len(c.blocks)},
+            "cpu_baseline": {"value": v, "unit": "Mcell-iter/s", "cores": min(threads, len(c.blocks)),
+                             "kind": "port", "sample": f"{args.steps} iterations of {c.name}"},
+            "e2e": {"value": v, "unit": "Mcell-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--case", default=os.environ.get("TRANS_BENCH_CASE", "cascade"))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    if args.case == "cascade" and not hasattr(cases, "cascade"):
+        args.case = "channel"
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    c, conns, geo, st = make_case(args.case, args.precision)
+    ncell = interior_cells(c)
+    s = Solver(c, conns, geo, st)
+    lib = s.lib
+    ki = 1
+    for _ in range(args.warmup):
+        s.iterate(ki); ki += 1
+    stage_ms = (C.c_double * len(abi.STAGES))()
+    lib.trans_stage_times(s.ctx, ki, stage_ms); ki += 1
+    launches0 = lib.trans_kernel_launches(s.ctx)
+    clk = ClockSampler()
+    clk.start()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = time_resident(s, ki, args.steps)
+    ki += args.steps
+    launches = lib.trans_kernel_launches(s.ctx) - launches0
+    clocks = clk.stop()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ncell * args.steps / (ms * 1e-3) / 1e6 * world
+    # end-to-end through the C ABI with pinned host buffers
+    e2e_steps = max(2, min(args.steps, 10))
+    dt, h2d, d2h = run_e2e(s, c, st, ki, e2e_steps)
+    e2e = ncell * e2e_steps / dt / 1e6 * world
+    # roofline of the dominant stage
+    pk = peaks()
+    hbm = pk.get("hbm_gbs", FALLBACK_HBM)
+    fp64 = lib.trans_probe_fma_gflops(1)
+    fp32 = lib.trans_probe_fma_gflops(0)
+    st_ms = {n: stage_ms[i] for i, n in enumerate(abi.STAGES)}
+    dom = max(st_ms, key=st_ms.get)
+    # algorithmic bytes per interior cell of each stage (FP64 words x 8)
+    words = {"SPECRAD": 10 + 9 + 1 + 4, "BC_STATE": 0, "GRADIENT": 7 + 2 + 9 + 3 + 1 + 18 + 1 + 5,
+             "BC_GRAD": 0, "RESIDUAL": 10 + 18 + 1 + 9 + 3 + 3 + 1 + 7,
+             "LUSGS": 7 + 14 + 7 + 3 + 1 + 1 + 9 + 24, "UPDATE": 10 + 7 + 9 + 1 + 10, "UPDATE_U": 21}
+    alg_bytes = words[dom] * 8.0 * ncell
+    achieved = alg_bytes / (st_ms[dom] * 1e-3) / 1e9
+    line = {
+        "metric": "Mcell-iter/s", "value": value, "unit": "Mcell-iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32-flux/f64-update",
+        "data": "synthetic",
+        "config": {"workload": c.name, "cells": ncell, "blocks": len(c.blocks), "precision": args.precision,
+                   "l2": f"working set {lib.trans_device_bytes(s.ctx) / 1e9:.2f} GB > L2 (no flush needed)"},
+        "e2e": {"value": e2e, "unit": "Mcell-iter/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": dom,
+                     "fp64_pipe_gflops_peak_measured": fp64, "fp32_pipe_gflops_peak_measured": fp32,
+                     "peak_source": "measured" if "hbm_gbs" in pk else "fallback"},
+        "stage_ms": st_ms,
+    }
+    if rank == 0 and not args.no_cpu:
+        v, n, dt2 = cpu_sample(c, conns, geo, st)
+        line["cpu_baseline"] = {"value": v, "unit": "Mcell-iter/s", "cores": 1, "kind": "port",
+                                "sample": f"{n} iterations of {c.name} on one core ({dt2:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line))
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -156,6 +156,15 @@ int trans_iterate(void* ctx, int ki, trans_norms* norms);
 /* One stage of one sub-iteration for all blocks; itr_chld is the sub-iteration index (1-based). */
 int trans_run_stage(void* ctx, int stage, int ki, int itr_chld);
 int trans_get_norms(void* ctx, trans_norms* norms);
+/* One outer iteration with CUDA events around every stage on the context's stream; ms receives
+ * TRANS_NSTAGES elapsed times (no reference counterpart: instrumentation). */
+int trans_stage_times(void* ctx, int ki, double* ms);
+/* Measured fused multiply-add throughput of the FP64 (fp64=1) or FP32 pipe in GFLOP/s (no
+ * reference counterpart: the compute roof the FP64 kernels are reported against). */
+double trans_probe_fma_gflops(int fp64);
+/* n outer iterations KI = ki_first.. timed with CUDA events on the context's stream (ms: total).
+ * norms as for trans_iterate (last iteration).  No reference counterpart: benchmarking. */
+int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norms* norms);
 int trans_sync(void* ctx);
 /* Device bytes held by the context. */
 long long trans_device_bytes(void* ctx);

@@ -43,6 +43,12 @@ def load():
         lib.oracle_ausmpw.argtypes = [C.POINTER(abi.TransParams), dp, dp]
         lib.oracle_roe.argtypes = [C.POINTER(abi.TransParams), dp, dp]
         lib.oracle_mdcd.argtypes = [dp, C.c_double, dp]
+        for f in ("exp", "expm1", "tanh", "log"):
+            fn = getattr(lib, "oracle_tm_" + f)
+            fn.argtypes = [C.c_double]
+            fn.restype = C.c_double
+        lib.oracle_tm_pow.argtypes = [C.c_double, C.c_double]
+        lib.oracle_tm_pow.restype = C.c_double
         _lib = lib
     return _lib
 

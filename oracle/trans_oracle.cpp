@@ -15,6 +15,9 @@
 // Restatement choices, each equal to the reference's mathematics:
 //   x**2 -> x*x, x**3 -> (x*x)*x, x**4 -> (x*x)*(x*x)   (integer powers)
 //   x**0.5 -> sqrt(x)      x**1.5 -> x*sqrt(x)            (for x >= 0)
+//   exp, tanh, x**y -> the functions of tmath.h (published methods in plain IEEE arithmetic,
+//   within a few ulp of libm), so that the GPU library, which uses the same methods, can be
+//   compared bit for bit
 //   SIGN(1,b) -> +1 for b >= 0 (including -0.0), -1 otherwise
 // Dead code of the reference is not restated: the residual smoothing of TIME_Update_V
 // (its writes to D are commented out), Fscheme (read only by CONVECT_Roe_Rotated), ghost Rds
@@ -27,6 +30,7 @@
 #include <algorithm>
 
 #include "../include/trans_gpu.h"
+#include "tmath.h"
 
 namespace {
 
@@ -226,15 +230,15 @@ void bc_farbond(double XM, double P2, double RR, double Vxi, double Vyi, double 
         double SON = 1.0 / pGam / (XM * XM);
         double QTX = VxF - QNF * DNx, QTY = VyF - QNF * DNy, QTZ = VzF - QNF * DNz;
         VX0 = QTX + QN * DNx; VY0 = QTY + QN * DNy; VZ0 = QTZ + QN * DNz;
-        RR0 = std::pow(AS * AS / SON / pGam, 2.5);
+        RR0 = otm::pow_(AS * AS / SON / pGam, 2.5);
         PP0 = AS * AS * RR0 / pGam;
         dir = -1.0;
     }
     if (QN >= 0.0 && QN < AS) {
-        double SON = P2 / std::pow(RR, pGam);
+        double SON = P2 / otm::pow_(RR, pGam);
         double QTX = Vxi - QNE * DNx, QTY = Vyi - QNE * DNy, QTZ = Vzi - QNE * DNz;
         VX0 = QTX + QN * DNx; VY0 = QTY + QN * DNy; VZ0 = QTZ + QN * DNz;
-        RR0 = std::pow(AS * AS / SON / pGam, 2.5);
+        RR0 = otm::pow_(AS * AS / SON / pGam, 2.5);
         PP0 = AS * AS * RR0 / pGam;
         dir = 1.0;
     }
@@ -399,7 +403,7 @@ void bc_inlet(Ctx& c, Blk& b, const trans_conn& a, int sweep) {
             int il = I + s.Eiadd, jl = J + s.Ejadd, kl = K + s.Ekadd;
             double PsIn = b.PP(is, js, ks);
             PsIn = std::min(PsIn, 0.999 * p.P0in);
-            double comm = std::max(1.0, std::pow(p.P0in / PsIn, 1.0 / 3.5));
+            double comm = std::max(1.0, otm::pow_(p.P0in / PsIn, 1.0 / 3.5));
             double mach = std::sqrt((comm - 1.0) * 2 / 0.4);
             double TsIn = p.T0in / comm;
             double Roin = p.RXM2 * PsIn / TsIn;
@@ -889,7 +893,7 @@ void turbtwo_diffusion(Ctx& c, Blk& b) {
                                    500.0 * RmiuL / Den / distfc / distfc / TOO / p.Ref / p.Ref);
             arg1 = std::min(arg1, 4.0 * Den * p.Sigo2 * TKK / CDKO / distfc / distfc);
             double a2 = arg1 * arg1;
-            double fc1c = std::tanh(a2 * a2);
+            double fc1c = otm::tanh_(a2 * a2);
             double SigkAB = fc1c * p.Sigk1 + (1.0 - fc1c) * p.Sigk2;
             double SigoAB = fc1c * p.Sigo1 + (1.0 - fc1c) * p.Sigo2;
             double vmute = RmiuL + RmiuTL * SigkAB;
@@ -1357,13 +1361,13 @@ double fsst(const trans_params& p, double Den, double vK, double vOmega, double 
         double temp = std::max(Den * CDiff * p.Ref, 1.0e-10);
         double argb = 4. * Den * 0.856 * vK / (temp * Dist * Dist);
         double arg = std::min(arga, argb);
-        return std::tanh(arg * arg * arg * arg);
+        return otm::tanh_(arg * arg * arg * arg);
     }
     if (p.Kind_SubHY == 2) {
         double arg1 = 2. * std::sqrt(vK) / (0.09 * vOmega * Dist * p.Ref);
         double arg2 = 500. * RmiuL / (Den * Dist * Dist * vOmega * p.Ref * p.Ref);
         double arg = std::max(arg1, arg2);
-        return std::tanh(arg * arg);
+        return otm::tanh_(arg * arg);
     }
     return 0.0;
 }
@@ -1417,7 +1421,7 @@ void turbtwo_lusgs_sst(Ctx& c, Blk& b) {
                                500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
         arg1 = std::min(arg1, 4.0 * p.Sigo2 * ARTk / CDKO / DistN / DistN);
         double a2 = arg1 * arg1;
-        arg1 = std::tanh(a2 * a2);
+        arg1 = otm::tanh_(a2 * a2);
         arg1_prev = arg1;
         double AA = std::sqrt(1.4 * b.PP(I, J, K) / ARo);
         double Mt = std::sqrt(ARTk / ARo) / AA;
@@ -1556,10 +1560,10 @@ void time_update_v(Ctx& c, Blk& b) {
         double AinZ = (AinRz - pVz * AinRo) * roinv;
         double AinP = (1.4 - 1.0) * (AinRe - 0.5 * AinRo * (pVx * pVx + pVy * pVy + pVz * pVz) - pRo * (AinX * pVx + AinY * pVy + AinZ * pVz));
         if (AinRo >= 0.) pRo = pRo + AinRo;
-        else pRo = pRo * std::exp(AinRo / (pRo + 1.e-10));
+        else pRo = pRo * otm::exp_(AinRo / (pRo + 1.e-10));
         pRo = std::fabs(pRo);
         if (AinP >= 0.) b.PP(I, J, K) = b.PP(I, J, K) + AinP;
-        else b.PP(I, J, K) = b.PP(I, J, K) * std::exp(AinP / (b.PP(I, J, K) + 1.e-10));
+        else b.PP(I, J, K) = b.PP(I, J, K) * otm::exp_(AinP / (b.PP(I, J, K) + 1.e-10));
         b.PP(I, J, K) = std::fabs(b.PP(I, J, K));
         b.T(I, J, K) = p.RXM2 * b.PP(I, J, K) / pRo;
         pVx = pVx + AinX; pVy = pVy + AinY; pVz = pVz + AinZ;
@@ -1573,10 +1577,10 @@ void time_update_v(Ctx& c, Blk& b) {
         double AinRTk = b.D(6, I, J, K), AinRTO = b.D(7, I, J, K);
         double ARTk = b.V(6, I, J, K), ARTO = b.V(7, I, J, K);
         if (AinRTk >= 0.0) ARTk = ARTk + AinRTk;
-        else ARTk = ARTk * std::exp(AinRTk / (ARTk + 1.e-10));
+        else ARTk = ARTk * otm::exp_(AinRTk / (ARTk + 1.e-10));
         ARTk = std::max(ARTk, 1.0e-10);
         if (AinRTO >= 0.0) ARTO = ARTO + AinRTO;
-        else ARTO = ARTO * std::exp(AinRTO / (ARTO + 1.e-10));
+        else ARTO = ARTO * otm::exp_(AinRTO / (ARTO + 1.e-10));
         ARTO = std::max(ARTO, 1.0e-10);
         pRo = b.V(1, I, J, K);
         double VV = sq(b.V(2, I, J, K)) + sq(b.V(3, I, J, K)) + sq(b.V(4, I, J, K));
@@ -1592,7 +1596,7 @@ void time_update_v(Ctx& c, Blk& b) {
                        - 2.0 / 3.0 * Div * Div);
         double arg2 = 2.0 * std::sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
         arg2 = std::max(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
-        arg2 = std::tanh(arg2 * arg2);
+        arg2 = otm::tanh_(arg2 * arg2);
         double Sii = Dudx, Sjj = Dvdy, Skk = Dwdz;
         double Sij = (Dudy + Dvdx) / 2.0, Sik = (Dudz + Dwdx) / 2.0, Sjk = (Dvdz + Dwdy) / 2.0;
         double Skl = std::sqrt(2.0 * (1.0 * Sii * Sii + 1.0 * Sjj * Sjj + 1.0 * Skk * Skk + 2.0 * Sij * Sij + 2.0 * Sik * Sik + 2.0 * Sjk * Sjk));
@@ -1828,3 +1832,11 @@ void oracle_roe(const trans_params* p, const double* in, double* out) {
 void oracle_mdcd(const double* s6, double gama, double* out) { mdcd_pair(s6, gama, out[0], out[1]); }
 
 }  // extern "C"
+
+extern "C" {
+double oracle_tm_exp(double x) { return otm::exp_(x); }
+double oracle_tm_expm1(double x) { return otm::expm1_(x); }
+double oracle_tm_tanh(double x) { return otm::tanh_(x); }
+double oracle_tm_log(double x) { return otm::log_(x); }
+double oracle_tm_pow(double x, double y) { return otm::pow_(x, y); }
+}

@@ -1,0 +1,81 @@
+"""Case generator and caller-side set-up: block connectivity, interface node matching, metrics."""
+import numpy as np
+import pytest
+
+from trans_gb300 import case as C
+from trans_gb300 import cases
+
+SMALL_CASCADE = dict(nle=4, nte=2, ns=8, npitch=3, nr=6, nh=6, nk=4)
+
+
+def _face_centre(X, c, i, j, k):
+    """Centre of the boundary face of cell (i,j,k) on connection c (node arrays are 0-based)."""
+    d = c.IJKDirect - 1
+    n = [i, j, k]
+    n[d] = c.pointStart[d]           # node index of the face plane
+    ids = []
+    for a in (0, 1):
+        for b in (0, 1):
+            q = list(n)
+            t = [x for x in range(3) if x != d]
+            q[t[0]] += a
+            q[t[1]] += b
+            ids.append(q)
+    return np.mean([X[q[0] - 1, q[1] - 1, q[2] - 1] for q in ids], axis=0)
+
+
+@pytest.mark.parametrize("make", [lambda: cases.cascade(**SMALL_CASCADE), lambda: cases.channel_bump(25, 17, 6)],
+                         ids=["cascade", "channel"])
+def test_interfaces_match_node_for_node(make):
+    c = make()
+    conns = C.derive_connectivity(c.blocks)
+    by_id = {b.id: b for b in c.blocks}
+    pitch = c.meta.get("pitch")
+    for b in c.blocks:
+        for ic, cn in enumerate(conns[b.id]):
+            if cn.BCType != 9:
+                continue
+            tb = by_id[cn.TargetBlock]
+            tc = conns[tb.id][cn.TargetConn - 1]
+            # the target of the target is this connection
+            assert tc.TargetBlock == b.id and tc.TargetConn == ic + 1
+            I, J, K = C.face_cells(cn)
+            ib, jb, kb = C.p2p_source(cn, tc, I, J, K)
+            for q in range(len(I)):
+                p0 = _face_centre(b.xyz, cn, I[q], J[q], K[q])
+                p1 = _face_centre(tb.xyz, tc, ib[q], jb[q], kb[q])
+                d = p1 - p0
+                if pitch and abs(abs(d[1]) - pitch) < 1e-9 * pitch:
+                    d[1] = 0.0          # translational pitch periodicity
+                if abs(d[2]) > 0 and by_id is not None and np.allclose(d[:2], 0) and "channel" in c.name:
+                    d[2] = 0.0          # spanwise periodicity of the channel
+                assert np.max(np.abs(d)) < 1e-9 * np.max(np.abs(p0)), (b.id, ic + 1, q, d)
+
+
+def test_cascade_block_sizes():
+    c = cases.cascade()
+    dims = sorted(b.dims for b in c.blocks)
+    assert (257, 49, 65) in dims
+    assert dims.count((65, 41, 65)) == 2
+    assert dims.count((121, 17, 65)) == 2
+
+
+def test_cascade_metrics_positive():
+    c = cases.cascade(**SMALL_CASCADE)
+    conns, geo = C.compute_geometry(c)
+    for b in c.blocks:
+        ni, nj, nk = b.dims
+        v = geo[b.id]["VOL"][3:ni + 2, 3:nj + 2, 3:nk + 2]
+        assert np.all(v > 0)
+        d = geo[b.id]["DST"][3:ni + 2, 3:nj + 2, 3:nk + 2]
+        assert np.all(d > 0)
+
+
+def test_parameters_follow_parameterset():
+    c = cases.channel_bump(25, 17, 6)
+    p = c.params
+    assert p.RXM2 == pytest.approx(0.5 * 0.5 * 1.4)
+    assert p.PPF == pytest.approx(1.0 / 1.4 / 0.25)
+    assert p.Rof == pytest.approx(1.2 * p.Rkf / p.Rmiuf)
+    # static inflow pressure 1/(1.4 M^2) with rho = 1: the total-pressure ratio of M = 0.5
+    assert p.P0in / p.PPF == pytest.approx((1 + 0.2 * 0.25) ** 3.5, rel=1e-12)

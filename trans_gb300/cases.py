@@ -71,3 +71,190 @@ def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, **
     b = Block(1, X, segs, walls=[(3, 0, 0, 0, 0)])
     return Case("channel_bump_%dx%dx%d" % (ni, nj, nk), p, [b], [X[:, 0, :, :]], ph,
                 dict(Q_dst=0.05 / alscale, iterations=300))
+
+
+# --------------------------------------------------------------------------------------------
+# Linear compressor cascade, five blocks (O-grid around the blade + inlet/outlet H blocks +
+# two passage blocks), pitch-periodic 1-to-1 interfaces, endwalls.
+# --------------------------------------------------------------------------------------------
+def _blade(camber_deg=40.0, stagger_deg=30.0, thick=0.08, rot_deg=0.0):
+    """Circular-arc camber line (chord 1), elliptic-nosed thickness 2*t*sqrt(x(1-x)),
+    staggered, then rotated by rot_deg.  Returns functions of the chord fraction."""
+    th = math.radians(camber_deg)
+    R = 1.0 / (2.0 * math.sin(th / 2))
+    yc0 = -R * math.cos(th / 2)
+    ca, sa = math.cos(math.radians(stagger_deg + rot_deg)), math.sin(math.radians(stagger_deg + rot_deg))
+
+    def camber(xi):
+        z = np.sqrt(R * R - (xi - 0.5) ** 2) + yc0
+        dz = -(xi - 0.5) / np.sqrt(R * R - (xi - 0.5) ** 2)
+        return z, dz
+
+    def surface(xi, side):
+        z, dz = camber(xi)
+        nrm = np.sqrt(1.0 + dz * dz)
+        nx, nz = -dz / nrm, 1.0 / nrm              # unit normal towards +z (suction side)
+        h = thick * np.sqrt(np.clip(xi * (1.0 - xi), 0.0, None))
+        px = xi + side * h * nx
+        pz = z + side * h * nz
+        return ca * px - sa * pz, sa * px + ca * pz
+
+    def mean(xi):
+        z, dz = camber(xi)
+        return ca * xi - sa * z, sa * xi + ca * z
+
+    return surface, mean
+
+
+def _stretch(n, first_frac):
+    """n cells from 0 to 1 with geometric growth from first_frac."""
+    return geometric_spacing(n, first_frac, 1.0)
+
+
+def _two_sided(n, first):
+    """n cells on [0,1] clustered at both ends with first spacing `first` (n even)."""
+    h = geometric_spacing(n // 2, first, 0.5)
+    return np.concatenate([h, 1.0 - h[::-1][1:]])
+
+
+def cascade(nle=8, nte=4, ns=120, npitch=16, nr=48, nh=64, nk=64, Re_c=1.0e6, XM=0.6, inflow_deg=40.0,
+            p_ratio=0.85, pitch=0.8, span=1.0, radius=10.0, **switches):
+    """Linear compressor cascade passage with the block structure of a turbomachinery mesh:
+    O-block (2*nte+2*ns+nle around x nr x nk) on a circular-arc blade (8% thick, 40 deg camber,
+    30 deg stagger), inlet/outlet H-blocks (nh x (2*npitch+nle) x nk) and two passage blocks
+    (ns x npitch x nk).  The geometry is rotated so that the inflow (inflow_deg from axial) is
+    along +x, since the total-pressure inlet (BC/BC_Inlet.F90:54-56) imposes axial velocity;
+    the passage sits at mean radius `radius` chords, which the outlet radial-equilibrium
+    recurrence (BC/BC_Outlet.F90:57-70) reads.  Outlet static pressure = p_ratio x inlet total.
+    """
+    ph = _flow(XM, p_out_ratio=p_ratio)
+    sw = dict(Kind_Spatial=3, Kind_Roe=3, CFL_Sub_start=10.0, CFL_Sub_end=10.0, CFL_Sub_step=1,
+              Kind_Dual=2, Kchld=1, DT_LUSGS_Main=1.0e8, gama_max=0.0463783, gama_min=0.0)
+    sw.update(switches)
+    p0 = make_params(ph, **sw)
+    alscale = p0.Ref / (Re_c * mu_laminar_nd(p0, 1.0))
+    sw["Alscale"] = alscale
+    p = make_params(ph, **sw)
+    surf, mean = _blade(rot_deg=-inflow_deg)
+    # chord-fraction parameters of the blade loop segments
+    xi_l, xi_t = 0.02, 0.98
+    u = 0.5 * (1.0 - np.cos(np.pi * np.linspace(0.0, 1.0, ns + 1)))
+    xi_side = xi_l + (xi_t - xi_l) * u                   # LE -> TE
+    # mean line of the passage: camber line on the blade, continued with the end slopes
+    xm_le, ym_le = mean(np.array(0.0))
+    xm_te, ym_te = mean(np.array(1.0))
+    xq = np.linspace(0.0, 1.0, 401)
+    mx, my = mean(xq)
+    s_le = (my[1] - my[0]) / (mx[1] - mx[0])
+    s_te = (my[-1] - my[-2]) / (mx[-1] - mx[-2])
+    L_up, L_dn = 1.0, 1.0
+    h = 0.15
+    dlt = 0.08
+    xa, xb = float(mx[0]) - dlt, float(mx[-1]) + dlt
+
+    def ymean(x):
+        x = np.asarray(x, float)
+        y = np.interp(x, mx, my)
+        up = x < mx[0]
+        # upstream: slope decays from the leading-edge slope to 0 at the inlet
+        d = x - mx[0]
+        y = np.where(up, my[0] + s_le * d * (1.0 + d / (2.0 * (L_up + dlt))), y)
+        dn = x > mx[-1]
+        y = np.where(dn, my[-1] + s_te * (x - mx[-1]), y)
+        return y
+
+    # ---- O-block loop (outer rectangle in (x, eta)) and blade loop, i = 1..NIo ----
+    xs_p, ys_p = surf(xi_side[::-1], -1.0)               # pressure side TE -> LE
+    xs_s, ys_s = surf(xi_side, +1.0)                     # suction side LE -> TE
+    # TE caps (pressure side from xi=1 to xi_t, suction from xi_t to 1) and LE cap
+    cap_t = np.linspace(1.0, xi_t, nte + 1)
+    xtp, ytp = surf(cap_t, -1.0)
+    xts, yts = surf(cap_t[::-1], +1.0)
+    ang = np.linspace(0.0, 1.0, nle + 1)
+    xi_cap = np.where(ang <= 0.5, xi_l * (1 - 2 * ang), xi_l * (2 * ang - 1))
+    side = np.where(ang < 0.5, -1.0, 1.0)
+    xlc, ylc = surf(xi_cap, side)
+    bx = np.concatenate([xtp, xs_p[1:], xlc[1:], xs_s[1:], xts[1:]])
+    by = np.concatenate([ytp, ys_p[1:], ylc[1:], ys_s[1:], yts[1:]])
+    # outer loop: x positions of the sides follow the blade points, rescaled to [xa, xb]
+    xr = (xs_s - xs_s[0]) / (xs_s[-1] - xs_s[0])
+    x_top = xa + (xb - xa) * xr
+    eta_te = np.linspace(0.0, -h, nte + 1)
+    eta_le = np.linspace(-h, h, nle + 1)
+    ox = np.concatenate([np.full(nte + 1, xb), x_top[::-1][1:], np.full(nle, xa), x_top[1:], np.full(nte, xb)])
+    oe = np.concatenate([eta_te, np.full(ns, -h), eta_le[1:], np.full(ns, h), (-eta_te[::-1])[1:]])
+    oy = ymean(ox) + oe
+    nio = len(bx)
+    assert nio == 2 * nte + 2 * ns + nle + 1 and len(ox) == nio
+    bx[-1], by[-1] = bx[0], by[0]
+    first = 1.0 / (Re_c * math.sqrt(0.5 * 0.0576 * Re_c ** -0.2))
+    dist = np.hypot(ox - bx, oy - by)
+    sig = _stretch(nr, first / float(np.min(dist)))
+    z = _two_sided(nk, first / span) * span
+    Xo = np.empty((nio, nr + 1, nk + 1, 3))
+    Xo[:, :, :, 0] = (bx[:, None] + (ox - bx)[:, None] * sig[None, :])[:, :, None]
+    Xo[:, :, :, 1] = (by[:, None] + (oy - by)[:, None] * sig[None, :])[:, :, None]
+    Xo[:, :, :, 2] = z[None, None, :]
+    # ---- passage and H blocks on the (x, eta) lattice ----
+    eta_p = h + (pitch / 2 - h) * _stretch(npitch, 0.03)          # eta of P1 from h to pitch/2
+    eta_h = np.concatenate([-eta_p[::-1], eta_le[1:-1], eta_p])   # full pitch, 2*npitch+nle cells
+
+    def lattice(xv, etav):
+        X = np.empty((len(xv), len(etav), nk + 1, 3))
+        X[:, :, :, 0] = xv[:, None, None]
+        X[:, :, :, 1] = (ymean(xv)[:, None] + etav[None, :])[:, :, None]
+        X[:, :, :, 2] = z[None, None, :]
+        return X
+
+    dx_a = float(x_top[1] - x_top[0])
+    x_in = xa - L_up
+    x_up = xa - L_up * _stretch(nh, dx_a / L_up)[::-1]
+    x_up[0] = x_in
+    x_dn = xb + L_dn * _stretch(nh, float(x_top[-1] - x_top[-2]) / L_dn)
+    Xh1 = lattice(x_up, eta_h)
+    Xh2 = lattice(x_dn, eta_h)
+    Xp1 = lattice(x_top, eta_p)
+    Xp2 = lattice(x_top, -eta_p[::-1])
+    scale = 1.0 / alscale
+    blocks_xyz = []
+    for X in (Xo, Xh1, Xh2, Xp1, Xp2):
+        Y = X.copy()
+        Y[..., 1] += radius
+        blocks_xyz.append(Y * scale)
+    Xo, Xh1, Xh2, Xp1, Xp2 = blocks_xyz
+    nlo = 2 * npitch + nle
+    S = Segment
+    # O = 1, H1 = 2, H2 = 3, P1 = 4, P2 = 5
+    o_segs = [S(1, kind=9, blk_ex=1, blkbd_ex=2), S(2, kind=9, blk_ex=1, blkbd_ex=1), S(3, kind=1),
+              S(4, 1, nte, kind=9, blk_ex=3, blkbd_ex=3, lrev_a=1),
+              S(4, nte + 1, nte + ns, kind=9, blk_ex=5, blkbd_ex=4, lrev_a=1),
+              S(4, nte + ns + 1, nte + ns + nle, kind=9, blk_ex=2, blkbd_ex=3),
+              S(4, nte + ns + nle + 1, nte + 2 * ns + nle, kind=9, blk_ex=4, blkbd_ex=3),
+              S(4, nte + 2 * ns + nle + 1, 2 * nte + 2 * ns + nle, kind=9, blk_ex=3, blkbd_ex=4, lrev_a=1),
+              S(5, kind=1), S(6, kind=1)]
+    h1_segs = [S(1, kind=5),
+               S(2, 1, npitch, kind=9, blk_ex=5, blkbd_ex=1),
+               S(2, npitch + 1, npitch + nle, kind=9, blk_ex=1, blkbd_ex=6),
+               S(2, npitch + nle + 1, nlo, kind=9, blk_ex=4, blkbd_ex=1),
+               S(3, kind=9, blk_ex=2, blkbd_ex=6), S(4, kind=9, blk_ex=2, blkbd_ex=5),
+               S(5, kind=1), S(6, kind=1)]
+    h2_segs = [S(2, kind=7),
+               S(1, 1, npitch, kind=9, blk_ex=5, blkbd_ex=2),
+               S(1, npitch + 1, npitch + nte, kind=9, blk_ex=1, blkbd_ex=4, lrev_a=1),
+               S(1, npitch + nte + 1, npitch + nle, kind=9, blk_ex=1, blkbd_ex=8, lrev_a=1),
+               S(1, npitch + nle + 1, nlo, kind=9, blk_ex=4, blkbd_ex=2),
+               S(3, kind=9, blk_ex=3, blkbd_ex=7), S(4, kind=9, blk_ex=3, blkbd_ex=6),
+               S(5, kind=1), S(6, kind=1)]
+    p1_segs = [S(1, kind=9, blk_ex=2, blkbd_ex=4), S(2, kind=9, blk_ex=3, blkbd_ex=5),
+               S(3, kind=9, blk_ex=1, blkbd_ex=7), S(4, kind=9, blk_ex=5, blkbd_ex=3),
+               S(5, kind=1), S(6, kind=1)]
+    p2_segs = [S(1, kind=9, blk_ex=2, blkbd_ex=2), S(2, kind=9, blk_ex=3, blkbd_ex=2),
+               S(3, kind=9, blk_ex=4, blkbd_ex=4), S(4, kind=9, blk_ex=1, blkbd_ex=5, lrev_a=1),
+               S(5, kind=1), S(6, kind=1)]
+    end = [(5, 0, 0, 0, 0), (6, 0, 0, 0, 0)]
+    blocks = [Block(1, Xo, o_segs, walls=[(3, 0, 0, 0, 0)] + end), Block(2, Xh1, h1_segs, walls=end),
+              Block(3, Xh2, h2_segs, walls=end), Block(4, Xp1, p1_segs, walls=end),
+              Block(5, Xp2, p2_segs, walls=end)]
+    surfaces = [Xo[:, 0, :, :]] + [X[:, :, kk, :] for X in blocks_xyz for kk in (0, -1)]
+    name = "cascade_5blk_%dcells" % sum(int(np.prod([d - 1 for d in b.dims])) for b in blocks)
+    return Case(name, p, blocks, surfaces, ph, dict(Q_dst=0.02 / alscale, chord=scale, pitch=pitch * scale))

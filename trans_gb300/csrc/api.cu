@@ -54,6 +54,8 @@ struct Ctx {
     int KI = 1;
     std::string err;
     const FluxLaunchers* fl = nullptr;
+    double* d_stage = nullptr;           // Fortran-layout staging buffer of trans_set/get_field
+    size_t stage_doubles = 0;
 };
 
 int fail(Ctx* c, int code, const std::string& msg) {
@@ -498,6 +500,12 @@ int trans_create(const trans_params* p, int nblocks, const trans_block* blocks, 
                                   cudaMemcpyHostToDevice) != cudaSuccess) { trans_destroy(c); return TRANS_E_CUDA; }
         }
     }
+    {   // staging buffer for the largest Fortran field (DQdxyz: 18 components, lower bound -1)
+        size_t mx = 0;
+        for (auto& b : c->blk) mx = std::max(mx, (size_t)(b.NI + 4) * (b.NJ + 4) * (b.NK + 4) * 18);
+        c->stage_doubles = mx;
+        if (cudaMalloc(&c->d_stage, mx * sizeof(double)) != cudaSuccess) { trans_destroy(c); return TRANS_E_MEMORY; }
+    }
     c->h_parts.resize(c->cell_tiles.size());
     if (cudaMalloc(&c->d_parts, sizeof(NormPart) * std::max<size_t>(1, c->h_parts.size())) != cudaSuccess) { trans_destroy(c); return TRANS_E_CUDA; }
     c->norms.assign(nblocks, trans_norms{});
@@ -512,7 +520,7 @@ int trans_destroy(void* ctx) {
     cudaFree(c->arena); cudaFree(c->d_blk); cudaFree(c->d_off);
     cudaFree(c->d_cell); cudaFree(c->d_ghost);
     for (int d = 0; d < 3; ++d) cudaFree(c->d_face[d]);
-    cudaFree(c->d_bc); cudaFree(c->d_outlet); cudaFree(c->d_lines); cudaFree(c->d_sweep); cudaFree(c->d_parts);
+    cudaFree(c->d_bc); cudaFree(c->d_outlet); cudaFree(c->d_lines); cudaFree(c->d_sweep); cudaFree(c->d_parts); cudaFree(c->d_stage);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TRANS_OK;
@@ -523,35 +531,31 @@ static int field_io(Ctx* c, int ib, int f, double* host, bool upload) {
     FieldMap fm = field_map(f);
     if (fm.slot < 0) return fail(c, TRANS_E_ARG, "bad field id");
     const DevBlock& b = c->blk[ib];
-    int ei = b.NI + 2 - fm.lb + 1, ej = b.NJ + 2 - fm.lb + 1, ek = b.NK + 2 - fm.lb + 1;
-    std::vector<double> buf((size_t)b.ncell);
-    CK(cudaStreamSynchronize(c->stream));
-    for (int m = 0; m < fm.ncomp; ++m) {
-        double* dslot = b.base + (size_t)(fm.slot + comp_slot(f, m)) * b.ncell;
-        if (upload) {
-            CK(cudaMemcpy(buf.data(), dslot, sizeof(double) * b.ncell, cudaMemcpyDeviceToHost));
-            size_t n = (size_t)m;
-            for (int k = 0; k < ek; ++k)
-                for (int j = 0; j < ej; ++j)
-                    for (int i = 0; i < ei; ++i, n += fm.ncomp)
-                        buf[cidx(b, i + fm.lb, j + fm.lb, k + fm.lb)] = host[n];
-            CK(cudaMemcpy(dslot, buf.data(), sizeof(double) * b.ncell, cudaMemcpyHostToDevice));
-            if (f == TRANS_THTC) {      // sin/cos of the outlet recurrence, evaluated once on the host
-                std::vector<double> sn(buf.size()), cs(buf.size());
-                for (size_t q = 0; q < buf.size(); ++q) { sn[q] = std::sin(buf[q]); cs[q] = std::cos(buf[q]); }
-                CK(cudaMemcpy(b.base + (size_t)S_SINT * b.ncell, sn.data(), sizeof(double) * b.ncell, cudaMemcpyHostToDevice));
-                CK(cudaMemcpy(b.base + (size_t)S_COST * b.ncell, cs.data(), sizeof(double) * b.ncell, cudaMemcpyHostToDevice));
-            }
-        } else {
-            CK(cudaMemcpy(buf.data(), dslot, sizeof(double) * b.ncell, cudaMemcpyDeviceToHost));
-            size_t n = (size_t)m;
-            for (int k = 0; k < ek; ++k)
-                for (int j = 0; j < ej; ++j)
-                    for (int i = 0; i < ei; ++i, n += fm.ncomp)
-                        host[n] = buf[cidx(b, i + fm.lb, j + fm.lb, k + fm.lb)];
+    size_t ncells = (size_t)(b.NI + 3 - fm.lb) * (b.NJ + 3 - fm.lb) * (b.NK + 3 - fm.lb);
+    size_t bytes = ncells * fm.ncomp * sizeof(double);
+    cudaStream_t s = c->stream;
+    int is_sd = f == TRANS_SD ? 1 : 0;
+    if (upload) {
+        CK(cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, s));
+        launch_field_xfer(s, b, fm.slot, fm.ncomp, fm.lb, is_sd, c->d_stage, 1);
+        c->launches++;
+        if (f == TRANS_THTC) {      // sin/cos of the outlet recurrence, evaluated once on the host
+            std::vector<double> sn(ncells), cs(ncells);
+            for (size_t q = 0; q < ncells; ++q) { sn[q] = std::sin(host[q]); cs[q] = std::cos(host[q]); }
+            CK(cudaMemcpyAsync(c->d_stage, sn.data(), ncells * sizeof(double), cudaMemcpyHostToDevice, s));
+            launch_field_xfer(s, b, S_SINT, 1, fm.lb, 0, c->d_stage, 1);
+            CK(cudaMemcpyAsync(c->d_stage, cs.data(), ncells * sizeof(double), cudaMemcpyHostToDevice, s));
+            launch_field_xfer(s, b, S_COST, 1, fm.lb, 0, c->d_stage, 1);
+            CK(cudaStreamSynchronize(s));
         }
+        if (is_geometry(f)) c->geom_dirty = true;
+    } else {
+        launch_field_xfer(s, b, fm.slot, fm.ncomp, fm.lb, is_sd, c->d_stage, 0);
+        c->launches++;
+        CK(cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, s));
     }
-    if (upload && is_geometry(f)) c->geom_dirty = true;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
     return TRANS_OK;
 }
 
@@ -581,6 +585,51 @@ int trans_iterate(void* ctx, int ki, trans_norms* norms) {
     if (rc) return rc;
     if (norms) std::copy(c->norms.begin(), c->norms.end(), norms);
     return TRANS_OK;
+}
+
+int trans_stage_times(void* ctx, int ki, double* ms) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !ms) return TRANS_E_ARG;
+    c->KI = ki;
+    cudaEvent_t ev[TRANS_NSTAGES + 1];
+    for (int q = 0; q <= TRANS_NSTAGES; ++q) CK(cudaEventCreate(&ev[q]));
+    for (int q = 0; q < TRANS_NSTAGES; ++q) ms[q] = 0.0;
+    int nsub = c->p.Kind_Dual != 0 ? c->p.Kchld : 1;
+    int rc = TRANS_OK;
+    for (int it = 1; it <= nsub && rc == TRANS_OK; ++it)
+        for (int st = TRANS_STAGE_SPECRAD; st <= TRANS_STAGE_UPDATE_U && rc == TRANS_OK; ++st) {
+            if (st == TRANS_STAGE_UPDATE_U && it != nsub) continue;
+            CK(cudaEventRecord(ev[st], c->stream));
+            rc = run_stage(c, st, it);
+            CK(cudaEventRecord(ev[st + 1], c->stream));
+            CK(cudaEventSynchronize(ev[st + 1]));
+            float t = 0;
+            CK(cudaEventElapsedTime(&t, ev[st], ev[st + 1]));
+            ms[st] += t;
+        }
+    for (int q = 0; q <= TRANS_NSTAGES; ++q) cudaEventDestroy(ev[q]);
+    return rc;
+}
+
+double trans_probe_fma_gflops(int fp64) { return probe_fma_gflops(fp64); }
+
+int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norms* norms) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !ms || n < 0) return TRANS_E_ARG;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->stream));
+    int rc = TRANS_OK;
+    for (int q = 0; q < n && rc == TRANS_OK; ++q) rc = trans_iterate(ctx, ki_first + q, norms);
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
 }
 
 int trans_get_norms(void* ctx, trans_norms* norms) {

@@ -13,6 +13,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include "tmath.cuh"
 
 namespace tg {
 
@@ -81,6 +82,10 @@ template <typename R> __device__ inline R dmin(R a, R b) { return (b < a) ? b : 
 template <typename R> __device__ inline R sgn1(R b) { return b >= R(0) ? R(1) : R(-1); }
 template <typename R> __device__ inline R sq(R x) { return x * x; }
 template <typename R> __device__ inline R p15(R x) { return x * sqrt(x); }
+// tanh: the bit-reproducible FP64 restatement, or the CUDA single-precision function
+template <typename R> __device__ inline R ttanh(R x);
+template <> __device__ inline double ttanh<double>(double x) { return tmx::tanh_(x); }
+template <> __device__ inline float ttanh<float>(float x) { return tanhf(x); }
 
 // Sutherland viscosity (Time/SpectralRadius.F90:59 and every copy of it)
 template <typename R> __device__ inline R mu_suth(const Params& p, R TT) {
@@ -296,13 +301,13 @@ __device__ inline R fsst(const Params& p, R Den, R vK, R vOmega, R Dist, R RmiuL
         R temp = dmax(Den * CDiff * Ref, R(1.0e-10));
         R argb = R(4.) * Den * R(0.856) * vK / (temp * Dist * Dist);
         R arg = dmin(arga, argb);
-        return tanh(arg * arg * arg * arg);
+        return ttanh(arg * arg * arg * arg);
     }
     if (p.Kind_SubHY == 2) {
         R arg1 = R(2.) * sqrt(vK) / (R(0.09) * vOmega * Dist * Ref);
         R arg2 = R(500.) * RmiuL / (Den * Dist * Dist * vOmega * Ref * Ref);
         R arg = dmax(arg1, arg2);
-        return tanh(arg * arg);
+        return ttanh(arg * arg);
     }
     return R(0.0);
 }

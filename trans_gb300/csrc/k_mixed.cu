@@ -3,3 +3,45 @@
 #define TG_R float
 #define TG_NAME flux_launchers_f32
 #include "flux_inst.cuh"
+
+// Throughput probes of the FP64 and FP32 pipes (independent fused multiply-add chains in
+// every thread of a grid covering all SMs); used to state the compute roof of the kernels.
+namespace tg {
+template <typename T>
+__global__ void k_fma_probe(T* out, int iters, T a, T b) {
+    T x0 = (T)threadIdx.x, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3;
+    T x4 = x0 + (T)4, x5 = x0 + (T)5, x6 = x0 + (T)6, x7 = x0 + (T)7;
+    for (int q = 0; q < iters; ++q) {
+        x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+        x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+    }
+    T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == (T)-1.2345) out[blockIdx.x] = s;      // keeps the chains alive
+}
+
+double probe_fma_gflops(int fp64) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int blocks = nsm * 8, threads = 256, iters = fp64 ? 2000 : 40000;
+    void* out = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * blocks) != cudaSuccess) return -1.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        if (fp64) k_fma_probe<double><<<blocks, threads>>>((double*)out, iters, 0.999999, 1e-7);
+        else k_fma_probe<float><<<blocks, threads>>>((float*)out, iters, 0.999999f, 1e-7f);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) best = ms < best ? ms : best;
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    cudaFree(out);
+    double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+    return flops / (best * 1e-3) / 1e9;
+}
+}  // namespace tg

@@ -71,15 +71,15 @@ __device__ inline void farbond(double XM, double P2, double RR, double Vxi, doub
         double SON = 1.0 / pGam / (XM * XM);
         double QTX = VxF - QNF * DNx, QTY = VyF - QNF * DNy, QTZ = VzF - QNF * DNz;
         VX0 = QTX + QN * DNx; VY0 = QTY + QN * DNy; VZ0 = QTZ + QN * DNz;
-        RR0 = pow(AS * AS / SON / pGam, 2.5);
+        RR0 = tmx::pow_(AS * AS / SON / pGam, 2.5);
         PP0 = AS * AS * RR0 / pGam;
         dir = -1.0;
     }
     if (QN >= 0.0 && QN < AS) {
-        double SON = P2 / pow(RR, pGam);
+        double SON = P2 / tmx::pow_(RR, pGam);
         double QTX = Vxi - QNE * DNx, QTY = Vyi - QNE * DNy, QTZ = Vzi - QNE * DNz;
         VX0 = QTX + QN * DNx; VY0 = QTY + QN * DNy; VZ0 = QTZ + QN * DNz;
-        RR0 = pow(AS * AS / SON / pGam, 2.5);
+        RR0 = tmx::pow_(AS * AS / SON / pGam, 2.5);
         PP0 = AS * AS * RR0 / pGam;
         dir = 1.0;
     }
@@ -209,7 +209,7 @@ __global__ void k_bc_state(const DevBlock* __restrict__ blks, const BCEntry* __r
     } else if (E.kind == 5) {                       // BC/BC_Inlet.F90:38-110
         double PsIn = PP[s0];
         PsIn = dmin(PsIn, 0.999 * p.P0in);
-        double comm = dmax(1.0, pow(p.P0in / PsIn, 1.0 / 3.5));
+        double comm = dmax(1.0, tmx::pow_(p.P0in / PsIn, 1.0 / 3.5));
         double mach = sqrt((comm - 1.0) * 2 / 0.4);
         double TsIn = p.T0in / comm;
         double Roin = p.RXM2 * PsIn / TsIn;
@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
         R arg1 = dmax(sqrt(TKK) / Bs / TOO / distfc / Ref, R(500.0) * RmiuLt / Den / distfc / distfc / TOO / Ref / Ref);
         arg1 = dmin(arg1, R(4.0) * Den * Sigo2 * TKK / CDKO / distfc / distfc);
         R a2 = arg1 * arg1;
-        R fc1c = tanh(a2 * a2);
+        R fc1c = ttanh(a2 * a2);
         R SigkAB = fc1c * R(p.Sigk1) + (R(1.0) - fc1c) * R(p.Sigk2);
         R SigoAB = fc1c * R(p.Sigo1) + (R(1.0) - fc1c) * Sigo2;
         R vmute = RmiuLt + RmiuTL * SigkAB;
@@ -704,7 +704,7 @@ __device__ inline R sst_fc1(const Params& p, const DevBlock& b, int c) {
     R arg1 = dmax(sqrt(ARTk / ARo) / Bs / (ARTO / ARo) / DistN / Ref, R(500.0) * RmiuL / DistN / DistN / ARTO / Ref / Ref);
     arg1 = dmin(arg1, R(4.0) * Sigo2 * ARTk / CDKO / DistN / DistN);
     R a2 = arg1 * arg1;
-    return tanh(a2 * a2);
+    return ttanh(a2 * a2);
 }
 
 template <typename R>
@@ -788,7 +788,7 @@ __global__ void k_lusgs_rhs(const DevBlock* __restrict__ blks, const Tile* __res
     R arg1 = dmax(sqrt(ARTk / ARo) / Bs / (ARTO / ARo) / DistN / Ref, R(500.0) * RmiuL / DistN / DistN / ARTO / Ref / Ref);
     arg1 = dmin(arg1, R(4.0) * Sigo2 * ARTk / CDKO / DistN / DistN);
     R a2 = arg1 * arg1;
-    arg1 = tanh(a2 * a2);
+    arg1 = ttanh(a2 * a2);
     R AA = sqrt(R(1.4) * R(slot(b, S_PP)[c]) / ARo);
     R Mt = sqrt(ARTk / ARo) / AA;
     const R Alf1 = R(1.0), Alf2 = R(0.4), Alf3 = R(0.2);
@@ -926,11 +926,11 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
         double AinZ = (AinRz - pVz * AinRo) * roinv;
         double AinP = (1.4 - 1.0) * (AinRe - 0.5 * AinRo * (pVx * pVx + pVy * pVy + pVz * pVz) - pRo * (AinX * pVx + AinY * pVy + AinZ * pVz));
         if (AinRo >= 0.) pRo = pRo + AinRo;
-        else pRo = pRo * exp(AinRo / (pRo + 1.e-10));
+        else pRo = pRo * tmx::exp_(AinRo / (pRo + 1.e-10));
         pRo = fabs(pRo);
         double pp = PP[c];
         if (AinP >= 0.) pp = pp + AinP;
-        else pp = pp * exp(AinP / (pp + 1.e-10));
+        else pp = pp * tmx::exp_(AinP / (pp + 1.e-10));
         pp = fabs(pp);
         PP[c] = pp;
         T[c] = p.RXM2 * pp / pRo;
@@ -945,10 +945,10 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
         if (turb_upd) {   // TIME_Update_V.F90:709-816
             double ARTk = V[5][c], ARTO = V[6][c];
             if (d6 >= 0.0) ARTk = ARTk + d6;
-            else ARTk = ARTk * exp(d6 / (ARTk + 1.e-10));
+            else ARTk = ARTk * tmx::exp_(d6 / (ARTk + 1.e-10));
             ARTk = dmax(ARTk, 1.0e-10);
             if (d7 >= 0.0) ARTO = ARTO + d7;
-            else ARTO = ARTO * exp(d7 / (ARTO + 1.e-10));
+            else ARTO = ARTO * tmx::exp_(d7 / (ARTO + 1.e-10));
             ARTO = dmax(ARTO, 1.0e-10);
             double VV = sq(V[1][c]) + sq(V[2][c]) + sq(V[3][c]);
             double PPP = (1.4 - 1.0) * V[4][c] - 0.5 * (1.4 - 1.0) * (VV / pRo - sq(rr) * pRo);
@@ -962,7 +962,7 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
                            - 2.0 / 3.0 * Div * Div);
             double arg2 = 2.0 * sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
             arg2 = dmax(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
-            arg2 = tanh(arg2 * arg2);
+            arg2 = tmx::tanh_(arg2 * arg2);
             double Sii = Dudx, Sjj = Dvdy, Skk = Dwdz;
             double Sij = (Dudy + Dvdx) / 2.0, Sik = (Dudz + Dwdx) / 2.0, Sjk = (Dvdz + Dwdy) / 2.0;
             double Skl = sqrt(2.0 * (1.0 * Sii * Sii + 1.0 * Sjj * Sjj + 1.0 * Skk * Skk + 2.0 * Sij * Sij + 2.0 * Sik * Sik + 2.0 * Sjk * Sjk));
@@ -1042,4 +1042,23 @@ __global__ void k_geom_static(const DevBlock* __restrict__ blks, int nblk, long 
 
 #endif  // TG_COMMON_KERNELS
 
+}  // namespace tg
+
+namespace tg {
+#ifdef TG_COMMON_KERNELS
+// Fortran-layout (component fastest, lower bound lb) <-> slots, one thread per Fortran cell
+__global__ void k_field_xfer(DevBlock b, int slot0, int ncomp, int lb, int is_sd, double* __restrict__ stage, int to_slots) {
+    int ei = b.NI + 2 - lb + 1, ej = b.NJ + 2 - lb + 1, ek = b.NK + 2 - lb + 1;
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= (long long)ei * ej * ek) return;
+    int i = (int)(n % ei), j = (int)((n / ei) % ej), k = (int)(n / ((long long)ei * ej));
+    int c = cidx(b, i + lb, j + lb, k + lb);
+    for (int m = 0; m < ncomp; ++m) {
+        int so = is_sd ? 3 * (m % 3) + m / 3 : m;
+        double* sl = slot(b, slot0 + so);
+        if (to_slots) sl[c] = stage[n * ncomp + m];
+        else stage[n * ncomp + m] = sl[c];
+    }
+}
+#endif  // TG_COMMON_KERNELS
 }  // namespace tg

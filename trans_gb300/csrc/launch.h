@@ -20,6 +20,8 @@ void launch_gradient(cudaStream_t s, const DevBlock* blks, const Tile* tiles, in
 void launch_shock_ghost(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt);
 void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts);
 void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int kind_dual);
+void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, int lb, int is_sd, double* stage, int to_slots);
+double probe_fma_gflops(int fp64);
 void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
 
 // flux, source and sweep kernels, instantiated per arithmetic type
