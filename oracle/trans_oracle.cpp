@@ -587,7 +587,10 @@ void bc_p2p(Ctx& c, Blk& b, const trans_conn& a, Blk& r, int sweep) {
 
 // BC/Boundary.F90:1-48
 void bc_boundarys(Ctx& c, int sweep) {
-    for (auto& b : c.B) {
+    // blocks are independent within one BC pass: a 1-to-1 copy reads interior cells only
+#pragma omp parallel for schedule(dynamic)
+    for (size_t nb = 0; nb < c.B.size(); ++nb) {
+        Blk& b = c.B[nb];
         for (auto& a : b.conn) {
             switch (a.BCType) {
                 case 1: bc_wall(c, b, a, sweep); break;
@@ -1518,13 +1521,14 @@ void turbtwo_lusgs_sst(Ctx& c, Blk& b) {
 // ---------------------------------------------------------------------------------------
 void time_update_v(Ctx& c, Blk& b) {
     const trans_params& p = c.p;
+    b.nrm.nan_flag = 0;
     double DRSa = 0.0, DUa = 0.0;
     int Ima = 0, Jma = 0, Kma = 0;
     for (int K = 1; K <= b.NK1; ++K)
     for (int J = 1; J <= b.NJ1; ++J)
     for (int I = 1; I <= b.NI1; ++I) {
         double DR = std::fabs(b.D(1, I, J, K) / b.V(1, I, J, K));
-        if (std::isnan(b.D(1, I, J, K))) c.nan_flag = 1;
+        if (std::isnan(b.D(1, I, J, K))) b.nrm.nan_flag = 1;
         if (DUa <= DR) { DUa = DR; Ima = I; Jma = J; Kma = K; }
         DRSa = DRSa + DR * DR;
     }
@@ -1609,7 +1613,6 @@ void time_update_v(Ctx& c, Blk& b) {
     }
     b.nrm.DRSa = DRSa; b.nrm.DUa = DUa; b.nrm.Ima = Ima; b.nrm.Jma = Jma; b.nrm.Kma = Kma;
     b.nrm.DRSk = DRSk; b.nrm.DUk = DUk; b.nrm.DRSo = DRSo; b.nrm.DUo = DUo;
-    b.nrm.nan_flag = c.nan_flag;
 }
 
 // Time/TIME_Update_U.F90:16-44
@@ -1637,45 +1640,54 @@ void set_turb(Ctx& c) {
 int run_stage(Ctx& c, int stage) {
     switch (stage) {
         case TRANS_STAGE_SPECRAD:
-            for (auto& b : c.B) spectral_radius(c, b);
+#pragma omp parallel for schedule(dynamic)
+            for (size_t n = 0; n < c.B.size(); ++n) spectral_radius(c, c.B[n]);
             break;
         case TRANS_STAGE_BC_STATE:
             bc_boundarys(c, -1);
             break;
         case TRANS_STAGE_GRADIENT:
-            for (auto& b : c.B) spaceinterp(c, b);
-            if (c.p.IF_Euler == 0) for (auto& b : c.B) diff_dqdxyz(c, b);
+#pragma omp parallel for schedule(dynamic)
+            for (size_t n = 0; n < c.B.size(); ++n) {
+                spaceinterp(c, c.B[n]);
+                if (c.p.IF_Euler == 0) diff_dqdxyz(c, c.B[n]);
+            }
             break;
         case TRANS_STAGE_BC_GRAD:
             bc_boundarys(c, 0);
             break;
         case TRANS_STAGE_RESIDUAL:
-            for (auto& b : c.B) {
+            // per block: the three loops of main.F90:92-133 touch only the block's own arrays
+#pragma omp parallel for schedule(dynamic)
+            for (size_t n = 0; n < c.B.size(); ++n) {
+                Blk& b = c.B[n];
                 std::fill(b.D.v.begin(), b.D.v.end(), 0.0);
                 if (c.p.IF_Euler == 0) diffusion_centered(c, b);
                 if (c.IF_turb) turbtwo_diffusion(c, b);
-            }
-            for (auto& b : c.B) {
                 if (c.p.Kind_Spatial == 2) convect_muscl(c, b);
                 else convect_mdcd(c, b);
                 if (c.IF_turb) turbtwo_convect_muscl(c, b);
-            }
-            for (auto& b : c.B) {
                 convect_inviscid(c, b);
                 if (c.IF_turb) turbtwo_convect_upwind(c, b);
             }
             break;
         case TRANS_STAGE_LUSGS:
-            for (auto& b : c.B) {
-                time_lusgs(c, b);
-                if (c.IF_turb) turbtwo_lusgs_sst(c, b);
+#pragma omp parallel for schedule(dynamic)
+            for (size_t n = 0; n < c.B.size(); ++n) {
+                time_lusgs(c, c.B[n]);
+                if (c.IF_turb) turbtwo_lusgs_sst(c, c.B[n]);
             }
             break;
         case TRANS_STAGE_UPDATE:
-            for (auto& b : c.B) time_update_v(c, b);
+#pragma omp parallel for schedule(dynamic)
+            for (size_t n = 0; n < c.B.size(); ++n) time_update_v(c, c.B[n]);
+            for (auto& b : c.B) c.nan_flag |= b.nrm.nan_flag;
             break;
         case TRANS_STAGE_UPDATE_U:
-            if (c.p.Kind_Dual != 0) for (auto& b : c.B) time_update_u(c, b);
+            if (c.p.Kind_Dual != 0) {
+#pragma omp parallel for schedule(dynamic)
+                for (size_t n = 0; n < c.B.size(); ++n) time_update_u(c, c.B[n]);
+            }
             break;
         default:
             return TRANS_E_ARG;

@@ -57,3 +57,13 @@ def bit_equal_fraction(a, b, mask):
         eq += int(np.sum(x.view(np.int64) == y.view(np.int64)))
         tot += x.size
     return eq / max(tot, 1)
+
+
+SMALL_CASCADE = dict(nle=4, nte=2, ns=8, npitch=3, nr=6, nh=6, nk=4)
+
+
+def small_cascade(**sw):
+    c = cases.cascade(**SMALL_CASCADE, **sw)
+    conns, geo = C.compute_geometry(c)
+    st = C.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
+    return c, conns, geo, st

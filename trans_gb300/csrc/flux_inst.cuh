@@ -19,10 +19,10 @@ void rh(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const Params& 
     if (nt > 0) k_lusgs_rhs<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, p, turb);
 }
 void swl(cudaStream_t s, const DevBlock* b, const SweepCell* c, int first, int count, int turb) {
-    if (count > 0) k_sweep<TG_R, true><<<(count + 127) / 128, 128, 0, s>>>(b, c, first, count, turb);
+    if (count > 0) k_sweep<TG_R, true><<<(count + 31) / 32, 32, 0, s>>>(b, c, first, count, turb);
 }
 void swu(cudaStream_t s, const DevBlock* b, const SweepCell* c, int first, int count, int turb) {
-    if (count > 0) k_sweep<TG_R, false><<<(count + 127) / 128, 128, 0, s>>>(b, c, first, count, turb);
+    if (count > 0) k_sweep<TG_R, false><<<(count + 31) / 32, 32, 0, s>>>(b, c, first, count, turb);
 }
 }  // namespace
 

@@ -276,42 +276,47 @@ __global__ void k_bc_outlet(const DevBlock* __restrict__ blks, const BCEntry* __
     const double* rad = slot(b, S_RAD);
     const double* sint = slot(b, S_SINT);
     const double* cost = slot(b, S_COST);
+    // the recurrence values of the previous j stay in registers (PP, rho, rho*v, rho*w of the
+    // first ghost layer at j-1), so each step is a short dependent chain
+    double pp_prev = 0.0, den_prev = 1.0, v3_prev = 0.0, v4_prev = 0.0;
     for (int e = Ln.first; e < Ln.first + Ln.n; ++e) {
         const BCEntry E = ent[e];
         int s0 = E.s[0], l0 = E.l[0];
-        T[l0] = T[s0];
+        double Tl = T[s0];
+        T[l0] = Tl;
+        double pp;
         if (E.sub == 1) {                              // j == Jbgn
-            PP[l0] = p.Pouthub;
+            pp = p.Pouthub;
         } else {
             int lm = l0 - b.PI;                         // (il, jl-1, kl)
             double rcs1 = rad[l0], rcs2 = rad[lm];
             double sinr = sint[lm], cosr = cost[lm];
-            double den = V[0][lm];
-            double RoVr2 = sq(V[3][lm] / den * cosr - sinr * V[2][lm] / den + p.omega0 * rcs2);
-            PP[l0] = PP[lm] + fabs((rcs1 - rcs2) * den * RoVr2) / (rcs2 + p.Tiny);
+            double RoVr2 = sq(v4_prev / den_prev * cosr - sinr * v3_prev / den_prev + p.omega0 * rcs2);
+            pp = pp_prev + fabs((rcs1 - rcs2) * den_prev * RoVr2) / (rcs2 + p.Tiny);
         }
-        V[0][l0] = PP[l0] / T[l0] * p.RXM2;
-        double den_ratio = V[0][l0] / V[0][s0];
-        V[1][l0] = V[1][s0] * den_ratio;
-        V[2][l0] = V[2][s0] * den_ratio;
-        V[3][l0] = V[3][s0] * den_ratio;
+        PP[l0] = pp;
+        double den = pp / Tl * p.RXM2;
+        V[0][l0] = den;
+        double den_ratio = den / V[0][s0];
+        double v2 = V[1][s0] * den_ratio, v3 = V[2][s0] * den_ratio, v4 = V[3][s0] * den_ratio;
+        V[1][l0] = v2;
+        V[2][l0] = v3;
+        V[3][l0] = v4;
         for (int L = 1; L < 3; ++L) {
             int ig = E.l[L];
-            for (int m = 0; m < 4; ++m) V[m][ig] = V[m][l0];
-            PP[ig] = PP[l0];
-            T[ig] = T[l0];
+            V[0][ig] = den; V[1][ig] = v2; V[2][ig] = v3; V[3][ig] = v4;
+            PP[ig] = pp;
+            T[ig] = Tl;
         }
         if (turb) {
-            V[5][l0] = V[5][s0];
-            V[6][l0] = V[6][s0];
-            Rm[l0] = Rm[s0];
+            double k6 = V[5][s0], k7 = V[6][s0], rm = Rm[s0];
+            V[5][l0] = k6; V[6][l0] = k7; Rm[l0] = rm;
             for (int L = 1; L < 3; ++L) {
                 int ig = E.l[L];
-                V[5][ig] = V[5][l0];
-                V[6][ig] = V[6][l0];
-                Rm[ig] = Rm[l0];
+                V[5][ig] = k6; V[6][ig] = k7; Rm[ig] = rm;
             }
         }
+        pp_prev = pp; den_prev = den; v3_prev = v3; v4_prev = v4;
     }
 }
 
