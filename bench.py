@@ -33,12 +33,12 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
 
 
-def make_case(name, precision):
+def make_case(name, precision, nk=64):
     prec = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
     if name == "channel":
         c = cases.channel_bump(precision=prec)
     elif name == "cascade":
-        c = cases.cascade(precision=prec)
+        c = cases.cascade(nk=nk, precision=prec)
     else:
         raise SystemExit(f"unknown case {name}")
     conns, geo = CS.compute_geometry(c)
@@ -182,7 +182,7 @@ def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    c, conns, geo, st = make_case(args.case, "fp64")
+    c, conns, geo, st = make_case(args.case, "fp64", args.nk)
     from oracle.oracle import OracleSolver
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
@@ -214,6 +214,7 @@ def main():
     ap.add_argument("--case", default=os.environ.get("TRANS_BENCH_CASE", "cascade"))
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nk", type=int, default=64, help="spanwise cells of the cascade (64 = full size)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -227,7 +228,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    c, conns, geo, st = make_case(args.case, args.precision)
+    c, conns, geo, st = make_case(args.case, args.precision, args.nk)
     ncell = interior_cells(c)
     s = Solver(c, conns, geo, st)
     lib = s.lib

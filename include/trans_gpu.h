@@ -148,7 +148,7 @@ enum trans_stage {
 };
 
 int trans_create(const trans_params* p, int nblocks, const trans_block* blocks, void** ctx);
-int trans_destroy(void* ctx);
+int trans_destroy(void* ctx);         /* NULL is a no-op returning TRANS_OK */
 int trans_set_field(void* ctx, int ib, int field, const double* fortran_array);
 int trans_get_field(void* ctx, int ib, int field, double* fortran_array);
 /* One outer iteration KI (main.F90:48-197).  norms: array of nblocks entries, may be NULL. */

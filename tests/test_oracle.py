@@ -123,18 +123,40 @@ def test_oracle_iterates_and_residual_drops():
     assert h[-1] < h[0]
 
 
-def test_golden_vectors(lib):
+GOLDEN = sorted(f for f in os.listdir(GOLD) if f.endswith(".json")) if os.path.isdir(GOLD) else []
+
+# The fixtures were generated on x86; the geometry's numpy trigonometry may differ in the last
+# ulp on another CPU, which ten iterations grow to ~1e-13.  Same machine: bit-identical.
+GOLD_TOL = 1e-10
+
+
+def golden_case(g):
+    from helpers import small_cascade
+    return small_channel(**g["switches"]) if g["case"] == "channel" else small_cascade(**g["switches"])
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_golden_vectors(lib, name):
     """The oracle reproduces the committed golden vectors (tests/golden/make_golden.py)."""
-    path = os.path.join(GOLD, "channel_small.json")
-    if not os.path.exists(path):
-        pytest.skip("golden vectors not generated")
-    g = json.load(open(path))
+    g = json.load(open(os.path.join(GOLD, name)))
     from oracle.oracle import OracleSolver
-    c, conns, geo, st = small_channel(**g["switches"])
+    c, conns, geo, st = golden_case(g)
     o = OracleSolver(c, conns, geo, st)
-    hist = [o.iterate(k)[0]["DRSa"] for k in range(1, len(g["DRSa"]) + 1)]
-    np.testing.assert_allclose(hist, g["DRSa"], rtol=1e-12)
-    V = o.get_field(0, "V")
-    for probe in g["probes"]:
-        L, i, j, k = probe["at"]
-        assert V[L, i + 2, j + 2, k + 2] == pytest.approx(probe["V"], rel=1e-12)
+    for s in ("SPECRAD", "BC_STATE", "GRADIENT", "BC_GRAD", "RESIDUAL"):
+        o.run_stage(s, 1)
+    for ib, b in enumerate(c.blocks):
+        ni, nj, nk = b.dims
+        D = o.get_field(ib, "D")[:, 3:ni + 2, 3:nj + 2, 3:nk + 2]
+        ref = g["first_residual"][ib]
+        scale = max(abs(x) for x in ref["sumsq"]) ** 0.5
+        for q in range(7):
+            assert abs(np.sum(D[q]) - ref["sum"][q]) <= GOLD_TOL * scale * D[q].size
+            assert np.sum(D[q] ** 2) == pytest.approx(ref["sumsq"][q], rel=GOLD_TOL, abs=1e-300)
+    o.close()
+    o = OracleSolver(c, conns, geo, st)
+    hist = [[n["DRSa"] for n in o.iterate(k)] for k in range(1, len(g["DRSa"]) + 1)]
+    np.testing.assert_allclose(hist, g["DRSa"], rtol=GOLD_TOL)
+    for p in g["probes"]:
+        V = o.get_field(p["block"], "V")
+        i, j, k = p["at"]
+        np.testing.assert_allclose([V[L, i + 2, j + 2, k + 2] for L in range(7)], p["V"], rtol=GOLD_TOL)

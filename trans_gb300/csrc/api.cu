@@ -269,6 +269,35 @@ int finalize_geometry(Ctx* c) {
     return TRANS_OK;
 }
 
+// Per-block norms from the per-tile partials in c->h_parts, summed in tile order (deterministic).
+int reduce_norms(Ctx* c) {
+    int nan = 0;
+    for (size_t b = 0; b < c->blk.size(); ++b) {
+        trans_norms& N = c->norms[b];
+        double sa = 0, sk = 0, so = 0, ma = -1, mk = 0, mo = 0;
+        long long ia = 0;
+        int bnan = 0;
+        for (size_t t = 0; t < c->cell_tiles.size(); ++t) {
+            if (c->cell_tile_blk[t] != (int)b) continue;
+            const NormPart& P = c->h_parts[t];
+            sa += P.sa; sk += P.sk; so += P.so;
+            if (P.ma > ma || (P.ma == ma && P.ia > ia)) { ma = P.ma; ia = P.ia; }
+            mk = std::max(mk, P.mk); mo = std::max(mo, P.mo);
+            bnan |= P.nan;
+        }
+        const DevBlock& B = c->blk[b];
+        N.DRSa = std::sqrt(sa / B.NI1 / B.NJ1 / B.NK1);
+        N.DRSk = std::sqrt(sk / B.NI1 / B.NJ1 / B.NK1);
+        N.DRSo = std::sqrt(so / B.NI1 / B.NJ1 / B.NK1);
+        N.DUa = ma; N.DUk = mk; N.DUo = mo;
+        N.Ima = (int)(ia % B.NI1) + 1; N.Jma = (int)((ia / B.NI1) % B.NJ1) + 1; N.Kma = (int)(ia / ((long long)B.NI1 * B.NJ1)) + 1;
+        N.nan_flag = bnan;
+        nan |= bnan;
+    }
+    if (nan) return fail(c, TRANS_E_NAN, "NaN in the density increment");
+    return TRANS_OK;
+}
+
 int run_stage(Ctx* c, int stage, int itr) {
     (void)itr;
     int rc = finalize_geometry(c);
@@ -329,31 +358,8 @@ int run_stage(Ctx* c, int stage, int itr) {
             c->launches++;
             CK(cudaMemcpyAsync(c->h_parts.data(), c->d_parts, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
-            // per-block reduction in tile order (deterministic)
-            int nan = 0;
-            for (size_t b = 0; b < c->blk.size(); ++b) {
-                trans_norms& N = c->norms[b];
-                double sa = 0, sk = 0, so = 0, ma = -1, mk = 0, mo = 0;
-                long long ia = 0;
-                int bnan = 0;
-                for (size_t t = 0; t < c->cell_tiles.size(); ++t) {
-                    if (c->cell_tile_blk[t] != (int)b) continue;
-                    const NormPart& P = c->h_parts[t];
-                    sa += P.sa; sk += P.sk; so += P.so;
-                    if (P.ma > ma || (P.ma == ma && P.ia > ia)) { ma = P.ma; ia = P.ia; }
-                    mk = std::max(mk, P.mk); mo = std::max(mo, P.mo);
-                    bnan |= P.nan;
-                }
-                const DevBlock& B = c->blk[b];
-                N.DRSa = std::sqrt(sa / B.NI1 / B.NJ1 / B.NK1);
-                N.DRSk = std::sqrt(sk / B.NI1 / B.NJ1 / B.NK1);
-                N.DRSo = std::sqrt(so / B.NI1 / B.NJ1 / B.NK1);
-                N.DUa = ma; N.DUk = mk; N.DUo = mo;
-                N.Ima = (int)(ia % B.NI1) + 1; N.Jma = (int)((ia / B.NI1) % B.NJ1) + 1; N.Kma = (int)(ia / ((long long)B.NI1 * B.NJ1)) + 1;
-                N.nan_flag = bnan;
-                nan |= bnan;
-            }
-            if (nan) return fail(c, TRANS_E_NAN, "NaN in the density increment");
+            rc = reduce_norms(c);
+            if (rc) return rc;
             break;
         }
         case TRANS_STAGE_UPDATE_U:
