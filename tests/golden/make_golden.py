@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from helpers import small_cascade, small_channel  # noqa: E402
+from helpers import inputs_digest, small_cascade, small_channel  # noqa: E402
 from oracle.oracle import OracleSolver  # noqa: E402
 
 NITER = 10
@@ -43,7 +43,8 @@ def make_case(kind, sw):
 def record(kind, sw):
     c, conns, geo, st = make_case(kind, sw)
     o = OracleSolver(c, conns, geo, st)
-    out = {"case": kind, "switches": sw, "blocks": [list(b.dims) for b in c.blocks]}
+    out = {"case": kind, "switches": sw, "blocks": [list(b.dims) for b in c.blocks],
+           "inputs_sha256": inputs_digest(c, geo, st)}
     # first residual, per block and component: sum and sum of squares over interior cells
     for s in ("SPECRAD", "BC_STATE", "GRADIENT", "BC_GRAD", "RESIDUAL"):
         o.run_stage(s, 1)

@@ -1,4 +1,6 @@
 """Shared helpers of the test-suite: cases, masks over the ghost-padded arrays, comparisons."""
+import hashlib
+
 import numpy as np
 
 from trans_gb300 import case as C
@@ -67,3 +69,15 @@ def small_cascade(**sw):
     conns, geo = C.compute_geometry(c)
     st = C.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
     return c, conns, geo, st
+
+
+def inputs_digest(c, geo, st):
+    """SHA-256 over every geometry and state array handed to the solver, in a fixed order:
+    equal digests mean bit-identical inputs (the host set-up is platform-independent)."""
+    h = hashlib.sha256()
+    for b in c.blocks:
+        for name in sorted(geo[b.id]):
+            h.update(np.ascontiguousarray(geo[b.id][name]).tobytes())
+        for name in sorted(st[b.id]):
+            h.update(np.ascontiguousarray(st[b.id][name]).tobytes())
+    return h.hexdigest()

@@ -12,6 +12,7 @@ import math
 import numpy as np
 
 from . import abi
+from . import detmath as dm
 
 G = 2  # index offset of Fortran index 0 (arrays start at -2)
 
@@ -63,9 +64,9 @@ def make_params(ph: Physical, **kw):
     PI = 4 * math.atan(1.0)
     Alfa = ph.AoA / 180.0 * PI
     Beta_Yaw = ph.AoYaw / 180.0 * PI
-    p.VxF = math.cos(Beta_Yaw) * math.cos(Alfa)
-    p.VyF = math.cos(Beta_Yaw) * math.sin(Alfa)
-    p.VzF = math.sin(Beta_Yaw)
+    p.VxF = dm.cos(Beta_Yaw) * dm.cos(Alfa)
+    p.VyF = dm.cos(Beta_Yaw) * dm.sin(Alfa)
+    p.VzF = dm.sin(Beta_Yaw)
     gam0 = 1.4
     XM2 = ph.XM * ph.XM
     p.XM = ph.XM
@@ -90,7 +91,7 @@ def make_params(ph: Physical, **kw):
     asonic = math.sqrt(1.4 * ph.Tinf * 287)
     Vref = ph.XM * asonic
     Lref = 1.0
-    miuref = (1.0 + p.Csthlnd) / (T0in * p.Csth1 + p.Csthlnd) * math.pow(p.Csth1 * T0in, 1.5) * 1.7e-5
+    miuref = (1.0 + p.Csthlnd) / (T0in * p.Csth1 + p.Csthlnd) * dm.pow(p.Csth1 * T0in, 1.5) * 1.7e-5
     Roref = 1.2
     p.Ref = Roref * Vref * Lref / miuref
     Pref = Roref * Vref * Vref
@@ -380,7 +381,7 @@ def block_metrics(b, surfaces, tiny=1.0e-20):
         s = (n8(A, 1, 1, 1) + n8(A, 1, 1, 0) + n8(A, 1, 0, 1) + n8(A, 1, 0, 0) + n8(A, 0, 1, 1)
              + n8(A, 0, 1, 0) + n8(A, 0, 0, 1) + n8(A, 0, 0, 0))
         Cc[ci, cj, ck] = s / 8.0
-    g["THTC"][ci, cj, ck] = np.arctan2(Zc[ci, cj, ck], Yc[ci, cj, ck])
+    g["THTC"][ci, cj, ck] = dm.atan2(Zc[ci, cj, ck], Yc[ci, cj, ck])
     g["RAD"][ci, cj, ck] = np.sqrt(Yc[ci, cj, ck] * Yc[ci, cj, ck] + Zc[ci, cj, ck] * Zc[ci, cj, ck])
     # wall distance
     g["DST"][ci, cj, ck] = wall_distance(Xc[ci, cj, ck], Yc[ci, cj, ck], Zc[ci, cj, ck], surfaces, tiny)
@@ -619,7 +620,7 @@ def geom_transform1(blocks, conns, geo):
             i, j, k = face_cells(c)
             d = c.IJKDirect - 1
             dcita = c.rotateAngle
-            sint, cost = math.sin(dcita), math.cos(dcita)
+            sint, cost = dm.sin(dcita), dm.cos(dcita)
             Ibgn, Jbgn, Kbgn = c.pointStart
             Iend, Jend, Kend = c.pointEnd
             IIadd, JJadd, KKadd = Iend - Ibgn + 2, Jend - Jbgn + 2, Kend - Kbgn + 2
@@ -674,6 +675,19 @@ def compute_geometry(case):
 # --------------------------------------------------------------------------------------------
 # Initial field (Input/Init.F90:94-169) and the seeded restart perturbation
 # --------------------------------------------------------------------------------------------
+def standard_normal(rng, shape):
+    """N(0,1) draws by the Box-Muller transform of the generator's uniform doubles, with the
+    platform-independent log/sin/cos of detmath (numpy's own normal sampler calls libm)."""
+    n = int(np.prod(shape))
+    m = (n + 1) // 2
+    u1 = 1.0 - rng.random(m)                  # (0, 1]
+    u2 = rng.random(m)
+    r = np.sqrt(-2.0 * dm.log(u1))
+    t = 2.0 * dm.pi * u2
+    z = np.concatenate([r * dm.cos(t), r * dm.sin(t)])[:n]
+    return z.reshape(shape)
+
+
 def initial_state(case, geo, Q_dst=0.01, If_NS_uniform=0, noise=1.0e-4, seed=0):
     p = case.params
     rng = np.random.default_rng(seed)
@@ -694,7 +708,7 @@ def initial_state(case, geo, Q_dst=0.01, If_NS_uniform=0, noise=1.0e-4, seed=0):
         ptemp = 1.0 / (1.4 * p.XM * p.XM)
         P = np.full_like(Dst, ptemp)
         if If_NS_uniform == 0:
-            Rat = 1.0 - np.exp(-Coff_dst * Dst)
+            Rat = 1.0 - dm.exp(-Coff_dst * Dst)
             V2 = np.where(Dst < Q_dst, V2 * Rat, V2)
         V5 = P / 0.4 + 0.5 * (V2 * V2 + V3 * V3 + V4 * V4) - 0.5 * ((om * rad) * (om * rad))
         C1, C2 = 45.8, 1.68
@@ -708,7 +722,7 @@ def initial_state(case, geo, Q_dst=0.01, If_NS_uniform=0, noise=1.0e-4, seed=0):
         Rmiu[c0] = p.Rmiuf
         # seeded restart perturbation of the density
         if noise:
-            V[0][c0] = V[0][c0] * (1.0 + noise * rng.standard_normal(Dst.shape))
+            V[0][c0] = V[0][c0] * (1.0 + noise * standard_normal(rng, Dst.shape))
         Wt0 = V.copy(order="F")
         Wt1 = V.copy(order="F")
         # PP and T from V (Input/Init.F90:156-169)

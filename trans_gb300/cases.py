@@ -9,8 +9,20 @@ import math
 import numpy as np
 
 from . import abi
+from . import detmath as dm
 from .case import (Block, Case, Physical, Segment, make_params, mu_laminar_nd,
                    static_pressure_Pa)
+
+
+def _ipow(r, n):
+    """r**n for an integer n >= 0 by repeated squaring (platform-independent rounding)."""
+    out, base = 1.0, r
+    while n:
+        if n & 1:
+            out *= base
+        base *= base
+        n >>= 1
+    return out
 
 
 def geometric_spacing(n_cells, first, total):
@@ -18,13 +30,13 @@ def geometric_spacing(n_cells, first, total):
     lo, hi = 1.0 + 1e-12, 2.0
     for _ in range(200):
         r = 0.5 * (lo + hi)
-        s = first * (r ** n_cells - 1.0) / (r - 1.0)
+        s = first * (_ipow(r, n_cells) - 1.0) / (r - 1.0)
         if s > total:
             hi = r
         else:
             lo = r
     r = 0.5 * (lo + hi)
-    d = first * r ** np.arange(n_cells)
+    d = first * np.array([_ipow(r, n) for n in range(n_cells)])
     x = np.concatenate([[0.0], np.cumsum(d)])
     return x * (total / x[-1])
 
@@ -32,7 +44,7 @@ def geometric_spacing(n_cells, first, total):
 def _flow(XM, Tinf=288.15, p_out_ratio=None, FSTI=0.01, VisRatio=1.0):
     ps = static_pressure_Pa(Tinf)
     comm = 1.0 + 0.2 * XM * XM
-    P0 = ps * comm ** 3.5
+    P0 = ps * dm.pow(comm, 3.5)
     pout = ps if p_out_ratio is None else p_out_ratio * P0
     return Physical(XM=XM, Tinf=Tinf, T0in_K=Tinf * comm, P0in_Pa=P0, Pouthub_Pa=pout,
                     FSTI=FSTI, VisRatio=VisRatio)
@@ -55,8 +67,8 @@ def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, **
     sw["Alscale"] = alscale
     p = make_params(ph, **sw)
     x = np.linspace(-1.0, 2.0, ni)
-    yw = np.where((x >= 0) & (x <= 1), bump * np.sin(math.pi * x) ** 2, 0.0)
-    cf = 0.0576 * Re_L ** -0.2
+    yw = np.where((x >= 0) & (x <= 1), bump * dm.sin(dm.pi * x) ** 2, 0.0)
+    cf = 0.0576 * dm.pow(Re_L, -0.2)
     dy1 = 1.0 / (Re_L * math.sqrt(0.5 * cf))
     s = geometric_spacing(nj - 1, dy1, 1.0)
     z = np.linspace(0.0, span, nk)
@@ -80,10 +92,10 @@ def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, **
 def _blade(camber_deg=40.0, stagger_deg=30.0, thick=0.08, rot_deg=0.0):
     """Circular-arc camber line (chord 1), elliptic-nosed thickness 2*t*sqrt(x(1-x)),
     staggered, then rotated by rot_deg.  Returns functions of the chord fraction."""
-    th = math.radians(camber_deg)
-    R = 1.0 / (2.0 * math.sin(th / 2))
-    yc0 = -R * math.cos(th / 2)
-    ca, sa = math.cos(math.radians(stagger_deg + rot_deg)), math.sin(math.radians(stagger_deg + rot_deg))
+    th = dm.radians(camber_deg)
+    R = 1.0 / (2.0 * dm.sin(th / 2))
+    yc0 = -R * dm.cos(th / 2)
+    ca, sa = dm.cos(dm.radians(stagger_deg + rot_deg)), dm.sin(dm.radians(stagger_deg + rot_deg))
 
     def camber(xi):
         z = np.sqrt(R * R - (xi - 0.5) ** 2) + yc0
@@ -138,7 +150,7 @@ def cascade(nle=8, nte=4, ns=120, npitch=16, nr=48, nh=64, nk=64, Re_c=1.0e6, XM
     surf, mean = _blade(rot_deg=-inflow_deg)
     # chord-fraction parameters of the blade loop segments
     xi_l, xi_t = 0.02, 0.98
-    u = 0.5 * (1.0 - np.cos(np.pi * np.linspace(0.0, 1.0, ns + 1)))
+    u = 0.5 * (1.0 - dm.cos(dm.pi * np.linspace(0.0, 1.0, ns + 1)))
     xi_side = xi_l + (xi_t - xi_l) * u                   # LE -> TE
     # mean line of the passage: camber line on the blade, continued with the end slopes
     xm_le, ym_le = mean(np.array(0.0))
@@ -187,8 +199,8 @@ def cascade(nle=8, nte=4, ns=120, npitch=16, nr=48, nh=64, nk=64, Re_c=1.0e6, XM
     nio = len(bx)
     assert nio == 2 * nte + 2 * ns + nle + 1 and len(ox) == nio
     bx[-1], by[-1] = bx[0], by[0]
-    first = 1.0 / (Re_c * math.sqrt(0.5 * 0.0576 * Re_c ** -0.2))
-    dist = np.hypot(ox - bx, oy - by)
+    first = 1.0 / (Re_c * math.sqrt(0.5 * 0.0576 * dm.pow(Re_c, -0.2)))
+    dist = dm.hypot(ox - bx, oy - by)
     sig = _stretch(nr, first / float(np.min(dist)))
     z = _two_sided(nk, first / span) * span
     Xo = np.empty((nio, nr + 1, nk + 1, 3))
