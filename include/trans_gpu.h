@@ -170,6 +170,21 @@ int trans_sync(void* ctx);
 long long trans_device_bytes(void* ctx);
 /* Kernel launches issued since the context was created (all kernels of this library). */
 long long trans_kernel_launches(void* ctx);
+/*
+ * TIME_Update_V (Time/TIME_Update_V.F90:91-908) over all blocks, as trans_run_stage(ctx,
+ * TRANS_STAGE_UPDATE, ki, ...), but with the per-tile residual-norm partials kept in a fixed
+ * 4 MiB buffer that is part of the library image instead of the context's own buffer.  No
+ * counterpart in the reference.  It is for callers that cannot allocate device memory at this
+ * point -- for instance a serving loop that has committed its whole device-memory budget to
+ * resident solves -- and it allocates nothing: no cudaMalloc, no allocating library routine.
+ * Limit: 65536 cell tiles (16,777,216 interior cells per context); larger contexts get
+ * TRANS_E_ARG with a message in trans_last_error.  Call it with the context's device current.
+ * The first call on a device looks the buffer up (cudaGetSymbolAddress) and should come
+ * before any stream capture.  The buffer is shared by every context and call on a device and
+ * keeps the last call's contents; concurrent calls race on it and must be serialised by the
+ * caller.  norms: nblocks entries, may be NULL.
+ */
+int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms);
 const char* trans_last_error(void* ctx);
 
 #ifdef __cplusplus

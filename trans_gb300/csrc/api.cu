@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <mutex>
 
 #include "../../include/trans_gpu.h"
 #include "types.cuh"
@@ -660,6 +661,70 @@ long long trans_device_bytes(void* ctx) {
 long long trans_kernel_launches(void* ctx) {
     Ctx* c = static_cast<Ctx*>(ctx);
     return c ? c->launches : 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// TIME_Update_V with its per-tile norm partials in a fixed device buffer.
+//
+// The buffer is a file-scope __device__ array, part of the loaded library image: the call
+// makes no device allocation of any kind.  Its address is taken once per device with
+// cudaGetSymbolAddress, with that device current, on the first call made on it (so that first
+// call should come before any stream capture), and handed to the kernel as a plain pointer.
+// All contexts and calls share the array and it keeps the last call's contents; every entry a
+// call reads is written earlier in the same call, so nothing needs clearing.  Calls that
+// overlap (two host threads, or two contexts whose streams run concurrently) race on it.
+// ---------------------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+constexpr int kStaticNormTiles = 65536;              // 16,777,216 interior cells; 4 MiB
+static __device__ __align__(256) NormPart g_norm_scratch[kStaticNormTiles];
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+NormPart* g_scratch_ptr[kMaxDevices] = {};
+
+int static_norm_scratch(Ctx* c, NormPart** out) {
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(c, TRANS_E_ARG, "device ordinal beyond the static scratch table");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_norm_scratch);
+        if (e != cudaSuccess)
+            return fail(c, TRANS_E_CUDA, std::string("cudaGetSymbolAddress(static norm scratch): ") + cudaGetErrorString(e));
+        g_scratch_ptr[dev] = static_cast<NormPart*>(ptr);
+    }
+    *out = g_scratch_ptr[dev];
+    return TRANS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return TRANS_E_ARG;
+    if (c->cell_tiles.size() > (size_t)kStaticNormTiles)
+        return fail(c, TRANS_E_ARG, "trans_update_static_scratch: " + std::to_string(c->cell_tiles.size()) +
+                    " cell tiles exceed the static scratch of 65536 tiles (16,777,216 interior cells)");
+    NormPart* scratch = nullptr;
+    int rc = static_norm_scratch(c, &scratch);
+    if (rc) return rc;
+    c->KI = ki;
+    rc = finalize_geometry(c);
+    if (rc) return rc;
+    const trans_params& p = c->p;
+    const int turb = turb_on(c);
+    const int turb_upd = (p.IF_Euler == 0 && turb == 1 && c->KI >= p.KItm) ? 1 : 0;
+    launch_update(c->stream, c->d_blk, c->d_cell, (int)c->cell_tiles.size(), c->dp, turb_upd, scratch);
+    c->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->h_parts.data(), scratch, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    rc = reduce_norms(c);
+    if (norms) std::copy(c->norms.begin(), c->norms.end(), norms);
+    return rc;
 }
 
 const char* trans_last_error(void* ctx) {
