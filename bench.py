@@ -275,7 +275,8 @@ def main():
         "dtype": "f64" if args.precision == "fp64" else "f32-flux/f64-update",
         "data": "synthetic",
         "config": {"workload": c.name, "cells": ncell, "blocks": len(c.blocks), "precision": args.precision,
-                   "l2": f"working set {lib.trans_device_bytes(s.ctx) / 1e9:.2f} GB > L2 (no flush needed)"},
+                   "l2": f"working set {lib.trans_device_bytes(s.ctx) / 1e9:.2f} GB > L2 (no flush needed)",
+                   "sweep_schedule": lib.trans_tuning(s.ctx).decode()},
         "e2e": {"value": e2e, "unit": "Mcell-iter/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "clocks": clocks,

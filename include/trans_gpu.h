@@ -185,6 +185,9 @@ long long trans_kernel_launches(void* ctx);
  * caller.  norms: nblocks entries, may be NULL.
  */
 int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms);
+/* The schedule the context's tuner picked for the LU-SGS sweeps and what it measured (no
+ * reference counterpart).  The string lives until the next call on this thread. */
+const char* trans_tuning(void* ctx);
 const char* trans_last_error(void* ctx);
 
 #ifdef __cplusplus

@@ -6,11 +6,14 @@
 // Fortran-layout arrays in and out, and sequence the kernels as main.F90:54-197 does.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <initializer_list>
 #include <mutex>
+#include <utility>
 
 #include "../../include/trans_gpu.h"
 #include "types.cuh"
@@ -34,6 +37,8 @@ struct Ctx {
     DevBlock* d_blk = nullptr;
     double* arena = nullptr;
     size_t arena_doubles = 0;
+    float* farena = nullptr;             // FP32 copies of the slots (mixed path only)
+    bool mixed = false;
     long long* d_off = nullptr;          // padded-cell offsets of the blocks (for flat kernels)
     long long total_cells = 0;
     std::vector<Tile> cell_tiles, face_tiles[3], ghost_tiles;
@@ -56,6 +61,19 @@ struct Ctx {
     std::string err;
     const FluxLaunchers* fl = nullptr;
     double* d_stage = nullptr;           // Fortran-layout staging buffer of trans_set/get_field
+    cudaGraphExec_t sweep_exec[2] = {nullptr, nullptr};   // both sweeps as one CUDA graph (per turb flag)
+    // sweep schedule: 0 = one launch per hyperplane (graph), 1 = one cooperative launch with
+    // grid barriers; -1 = pick the faster on first use (both give bit-identical DeltaQ)
+    int sweep_mode = -1, sweep_grid = 0, sweep_block = 0;
+    int* d_plane_off = nullptr;
+    SweepView sv{};                      // sweep-order arrays (cells, neighbour positions, records, DeltaQ)
+    int* d_nbp = nullptr;
+    void* d_rec = nullptr;
+    void* d_dqs = nullptr;
+    void* d_dq_save = nullptr;           // DeltaQ backup while the schedule tuner runs trials
+    SweepSync* d_sync = nullptr;
+    SweepSync* h_sync = nullptr;         // pinned
+    std::string sweep_tuning;            // what the schedule tuner measured
     size_t stage_doubles = 0;
 };
 
@@ -261,10 +279,21 @@ int turb_on(const Ctx* c) {
     return (p.IF_Euler == 0 && p.IF_Turb_org == 1 && (c->KI >= p.KItm || p.Kind_Hybrid > 0)) ? 1 : 0;
 }
 
+// FP32 copies of slot ranges {first, count} (mixed path); to_fp64 copies back
+void mirror(Ctx* c, std::initializer_list<std::pair<int, int>> ranges, int to_fp64 = 0) {
+    MirrorList ml;
+    std::memset(&ml, 0, sizeof(ml));
+    ml.to_fp64 = to_fp64;
+    for (auto& r : ranges) { ml.first[ml.n] = r.first; ml.count[ml.n] = r.second; ml.n++; }
+    launch_mirror(c->stream, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off, ml);
+    c->launches++;
+}
+
 int finalize_geometry(Ctx* c) {
     if (!c->geom_dirty) return TRANS_OK;
     launch_geom_static(c->stream, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off);
     c->launches++;
+    if (c->mixed) mirror(c, {{S_SD, S_WALL + 3 - S_SD}});
     CK(cudaGetLastError());
     c->geom_dirty = false;
     return TRANS_OK;
@@ -299,6 +328,104 @@ int reduce_norms(Ctx* c) {
     return TRANS_OK;
 }
 
+// both LU-SGS sweeps with the schedule `mode` (grid/block for the cooperative one)
+int sweep_once(Ctx* c, int turb, int mode, int grid, int block) {
+    cudaStream_t s = c->stream;
+    int nh = (int)c->plane_off.size() - 1;
+    if (mode == 1) {
+        CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
+        CK(c->fl->sweep_all(s, c->sv, c->d_plane_off, nh, turb, c->d_sync, grid, block));
+        CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
+        c->launches++;
+        return TRANS_OK;
+    }
+    // one launch per hyperplane, L ascending then U descending, replayed as one graph
+    if (!c->sweep_exec[turb]) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int h = 0; h < nh; ++h) {
+            int cnt = c->plane_off[h + 1] - c->plane_off[h];
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, turb);
+        }
+        for (int h = nh - 1; h >= 0; --h) {
+            int cnt = c->plane_off[h + 1] - c->plane_off[h];
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, turb);
+        }
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c->sweep_exec[turb], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph instantiate: ") + cudaGetErrorString(e));
+    }
+    CK(cudaGraphLaunch(c->sweep_exec[turb], s));
+    for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
+    return TRANS_OK;
+}
+
+// keep a copy of the sweep-order DeltaQ (restore = copy it back)
+int save_dq(Ctx* c, bool restore) {
+    size_t bytes = (size_t)7 * (size_t)c->sv.n * c->fl->elem;
+    if (!c->d_dq_save) CK(cudaMalloc(&c->d_dq_save, bytes));
+    CK(cudaMemcpyAsync(restore ? c->sv.dq : c->d_dq_save, restore ? c->d_dq_save : c->sv.dq, bytes, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    return TRANS_OK;
+}
+
+// Schedule tuner: time every candidate schedule on the live right-hand side (DeltaQ saved and
+// restored around each trial), keep the fastest.
+int tune_sweeps(Ctx* c, int turb) {
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    struct Cand { int mode, grid, block; };
+    std::vector<Cand> cands = {{0, 0, 0}};
+    for (int block : {128, 256, 512}) {
+        int occ = c->fl->sweep_all_occupancy(block);
+        for (int per : {1, 2, 4})
+            if (per <= occ) cands.push_back({1, per * nsm, block});
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    Cand pick = cands[0];
+    c->sweep_tuning.clear();
+    int rc = save_dq(c, false);
+    for (const Cand& k : cands) {
+        for (int rep = 0; rep < 2 && rc == TRANS_OK; ++rep) {      // first run warms up (graph build)
+            if ((rc = save_dq(c, true))) break;
+            CK(cudaEventRecord(e0, c->stream));
+            if ((rc = sweep_once(c, turb, k.mode, k.grid, k.block))) break;
+            CK(cudaEventRecord(e1, c->stream));
+            CK(cudaEventSynchronize(e1));
+            if (k.mode == 1 && c->h_sync->err) { rc = -100; break; }
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep == 1) {
+                c->sweep_tuning += (k.mode ? "coop " + std::to_string(k.grid) + "x" + std::to_string(k.block) : std::string("planes"))
+                                   + ":" + std::to_string(ms) + "ms ";
+                if (ms < best) { best = ms; pick = k; }
+            }
+        }
+        if (rc == -100) rc = TRANS_OK;         // a schedule that timed out is just not picked
+        if (rc) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = save_dq(c, true))) return rc;
+    c->sweep_mode = pick.mode; c->sweep_grid = pick.grid; c->sweep_block = pick.block;
+    return TRANS_OK;
+}
+
+int run_sweeps(Ctx* c, int turb) {
+    if (c->sweep_mode < 0) {
+        int rc = tune_sweeps(c, turb);
+        if (rc) return rc;
+    }
+    return sweep_once(c, turb, c->sweep_mode, c->sweep_grid, c->sweep_block);
+}
+
 int run_stage(Ctx* c, int stage, int itr) {
     (void)itr;
     int rc = finalize_geometry(c);
@@ -331,6 +458,8 @@ int run_stage(Ctx* c, int stage, int itr) {
             c->launches++;
             break;
         case TRANS_STAGE_RESIDUAL:
+            // the FP32 kernels read FP32 copies of this sub-iteration's state, gradients and radii
+            if (c->mixed) mirror(c, {{S_V, 10}, {S_RDS, 4}, {S_DQ, 19}, {S_PRIM, 5}, {S_RINV, 4}});
             for (int d = 0; d < 3; ++d) c->fl->face_flux[d](s, c->d_blk, c->d_face[d], (int)c->face_tiles[d].size(), c->dp, turb);
             c->fl->gather(s, c->d_blk, c->d_cell, nct, turb);
             c->launches += 4;
@@ -340,25 +469,21 @@ int run_stage(Ctx* c, int stage, int itr) {
                 c->fl->sst_fc1(s, c->d_blk, c->d_cell, nct, c->dp);
                 c->launches++;
             }
-            c->fl->lusgs_rhs(s, c->d_blk, c->d_cell, nct, c->dp, turb);
+            c->fl->prep(s, c->d_blk, c->sv, c->dp, turb);
             c->launches++;
-            int nh = (int)c->plane_off.size() - 1;
-            for (int h = 0; h < nh; ++h) {
-                int cnt = c->plane_off[h + 1] - c->plane_off[h];
-                if (cnt) { c->fl->sweep_lower(s, c->d_blk, c->d_sweep, c->plane_off[h], cnt, turb); c->launches++; }
-            }
-            for (int h = nh - 1; h >= 0; --h) {
-                int cnt = c->plane_off[h + 1] - c->plane_off[h];
-                if (cnt) { c->fl->sweep_upper(s, c->d_blk, c->d_sweep, c->plane_off[h], cnt, turb); c->launches++; }
-            }
+            rc = run_sweeps(c, turb);
+            if (rc) return rc;
+            c->fl->scatter(s, c->d_blk, c->sv);
+            c->launches++;
             break;
         }
         case TRANS_STAGE_UPDATE: {
             int turb_upd = (p.IF_Euler == 0 && turb == 1 && c->KI >= p.KItm) ? 1 : 0;
-            launch_update(s, c->d_blk, c->d_cell, nct, c->dp, turb_upd, c->d_parts);
+            launch_update(s, c->d_blk, c->d_cell, nct, c->dp, turb_upd, c->d_parts, c->mixed ? 1 : 0);
             c->launches++;
             CK(cudaMemcpyAsync(c->h_parts.data(), c->d_parts, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
+            if (c->sweep_mode == 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep grid barrier timed out");
             rc = reduce_norms(c);
             if (rc) return rc;
             break;
@@ -423,14 +548,20 @@ int trans_create(const trans_params* p, int nblocks, const trans_block* blocks, 
         total += (size_t)NSLOT * (size_t)ncell;
     }
     c->arena_doubles = total;
+    c->mixed = p->precision == TRANS_MIXED;
     cudaError_t e = cudaMalloc(&c->arena, total * sizeof(double));
     if (e != cudaSuccess) { delete c; return TRANS_E_MEMORY; }
     if (cudaMemset(c->arena, 0, total * sizeof(double)) != cudaSuccess) { cudaFree(c->arena); delete c; return TRANS_E_CUDA; }
+    if (c->mixed) {
+        if (cudaMalloc(&c->farena, total * sizeof(float)) != cudaSuccess) { cudaFree(c->arena); delete c; return TRANS_E_MEMORY; }
+        if (cudaMemset(c->farena, 0, total * sizeof(float)) != cudaSuccess) { cudaFree(c->arena); cudaFree(c->farena); delete c; return TRANS_E_CUDA; }
+    }
     {
         long long acc = 0;
         size_t pos = 0;
         for (int n = 0; n < nblocks; ++n) {
             c->blk[n].base = c->arena + pos;
+            c->blk[n].fbase = c->farena ? c->farena + pos : nullptr;
             pos += (size_t)NSLOT * (size_t)c->blk[n].ncell;
             off[n] = acc;
             acc += c->blk[n].ncell;
@@ -480,6 +611,49 @@ int trans_create(const trans_params* p, int nblocks, const trans_block* blocks, 
         c->plane_off.push_back((int)c->sweep.size());
     }
     if ((rc = upload_vec(c, c->sweep.data(), sizeof(SweepCell) * c->sweep.size(), (void**)&c->d_sweep))) { trans_destroy(c); return rc; }
+    if ((rc = upload_vec(c, c->plane_off.data(), sizeof(int) * c->plane_off.size(), (void**)&c->d_plane_off))) { trans_destroy(c); return rc; }
+    {   // neighbour positions in sweep order: lower i,j,k (0..2) and upper (3..5), -1 = none
+        const long long N = (long long)c->sweep.size();
+        std::vector<std::vector<int>> pos(nblocks);
+        for (int n = 0; n < nblocks; ++n) pos[n].assign((size_t)c->blk[n].nint, -1);
+        for (long long q = 0; q < N; ++q) {
+            const SweepCell& sc = c->sweep[q];
+            const DevBlock& b = c->blk[sc.blk];
+            pos[sc.blk][(size_t)(sc.i - 1) + (size_t)b.NI1 * ((sc.j - 1) + (size_t)b.NJ1 * (sc.k - 1))] = (int)q;
+        }
+        std::vector<int> nbp((size_t)6 * N, -1);
+        for (long long q = 0; q < N; ++q) {
+            const SweepCell& sc = c->sweep[q];
+            const DevBlock& b = c->blk[sc.blk];
+            const int ijk[3] = {sc.i, sc.j, sc.k}, hi[3] = {b.NI1, b.NJ1, b.NK1};
+            for (int side = 0; side < 2; ++side)
+                for (int d = 0; d < 3; ++d) {
+                    int x[3] = {ijk[0], ijk[1], ijk[2]};
+                    x[d] += side == 0 ? -1 : 1;
+                    if (x[d] < 1 || x[d] > hi[d]) continue;
+                    nbp[(size_t)(3 * side + d) * N + q] =
+                        pos[sc.blk][(size_t)(x[0] - 1) + (size_t)b.NI1 * ((x[1] - 1) + (size_t)b.NJ1 * (x[2] - 1))];
+                }
+        }
+        if ((rc = upload_vec(c, nbp.data(), sizeof(int) * nbp.size(), (void**)&c->d_nbp))) { trans_destroy(c); return rc; }
+        if (cudaMalloc(&c->d_rec, (size_t)NREC * N * c->fl->elem) != cudaSuccess ||
+            cudaMalloc(&c->d_dqs, (size_t)7 * N * c->fl->elem) != cudaSuccess) { trans_destroy(c); return TRANS_E_MEMORY; }
+        c->sv.cells = c->d_sweep; c->sv.nbp = c->d_nbp; c->sv.rec = c->d_rec; c->sv.dq = c->d_dqs; c->sv.n = N;
+    }
+    if (cudaMalloc(&c->d_sync, sizeof(SweepSync)) != cudaSuccess || cudaMallocHost(&c->h_sync, sizeof(SweepSync)) != cudaSuccess) {
+        trans_destroy(c); return TRANS_E_MEMORY;
+    }
+    std::memset(c->h_sync, 0, sizeof(SweepSync));
+    {   // sweep schedule: TRANS_SWEEP=planes | coop forces one (for tests); default: tuned
+        const char* m = std::getenv("TRANS_SWEEP");
+        if (m && std::string(m) == "planes") c->sweep_mode = 0;
+        if (m && std::string(m) == "coop") {
+            int dev = 0, nsm = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            c->sweep_mode = 1; c->sweep_block = 256; c->sweep_grid = nsm * std::max(1, std::min(2, c->fl->sweep_all_occupancy(256)));
+        }
+    }
     // wall marks on faces (Input/Read_BlockDimensions.F90:240-283)
     for (int n = 0; n < nblocks; ++n) {
         const DevBlock& b = c->blk[n];
@@ -524,10 +698,15 @@ int trans_destroy(void* ctx) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c) return TRANS_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    cudaFree(c->arena); cudaFree(c->d_blk); cudaFree(c->d_off);
+    cudaFree(c->arena); cudaFree(c->farena); cudaFree(c->d_blk); cudaFree(c->d_off);
     cudaFree(c->d_cell); cudaFree(c->d_ghost);
     for (int d = 0; d < 3; ++d) cudaFree(c->d_face[d]);
     cudaFree(c->d_bc); cudaFree(c->d_outlet); cudaFree(c->d_lines); cudaFree(c->d_sweep); cudaFree(c->d_parts); cudaFree(c->d_stage);
+    cudaFree(c->d_plane_off); cudaFree(c->d_sync);
+    cudaFree(c->d_nbp); cudaFree(c->d_rec); cudaFree(c->d_dqs); cudaFree(c->d_dq_save);
+    if (c->h_sync) cudaFreeHost(c->h_sync);
+    for (int q = 0; q < 2; ++q)
+        if (c->sweep_exec[q]) cudaGraphExecDestroy(c->sweep_exec[q]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TRANS_OK;
@@ -556,7 +735,9 @@ static int field_io(Ctx* c, int ib, int f, double* host, bool upload) {
             CK(cudaStreamSynchronize(s));
         }
         if (is_geometry(f)) c->geom_dirty = true;
+        if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}});
     } else {
+        if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}}, 1);      // DeltaQ lives in FP32 there
         launch_field_xfer(s, b, fm.slot, fm.ncomp, fm.lb, is_sd, c->d_stage, 0);
         c->launches++;
         CK(cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, s));
@@ -655,7 +836,11 @@ int trans_sync(void* ctx) {
 
 long long trans_device_bytes(void* ctx) {
     Ctx* c = static_cast<Ctx*>(ctx);
-    return c ? (long long)(c->arena_doubles * sizeof(double)) : 0;
+    if (!c) return 0;
+    long long b = (long long)(c->arena_doubles * sizeof(double));
+    if (c->farena) b += (long long)(c->arena_doubles * sizeof(float));
+    b += (long long)c->sv.n * ((long long)(NREC + 7) * (long long)c->fl->elem + 6LL * (long long)sizeof(int));
+    return b;
 }
 
 long long trans_kernel_launches(void* ctx) {
@@ -717,7 +902,7 @@ int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms) {
     const trans_params& p = c->p;
     const int turb = turb_on(c);
     const int turb_upd = (p.IF_Euler == 0 && turb == 1 && c->KI >= p.KItm) ? 1 : 0;
-    launch_update(c->stream, c->d_blk, c->d_cell, (int)c->cell_tiles.size(), c->dp, turb_upd, scratch);
+    launch_update(c->stream, c->d_blk, c->d_cell, (int)c->cell_tiles.size(), c->dp, turb_upd, scratch, c->mixed ? 1 : 0);
     c->launches++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c->h_parts.data(), scratch, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -725,6 +910,16 @@ int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms) {
     rc = reduce_norms(c);
     if (norms) std::copy(c->norms.begin(), c->norms.end(), norms);
     return rc;
+}
+
+const char* trans_tuning(void* ctx) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return "no context";
+    static thread_local std::string out;
+    out = "sweep=" + std::string(c->sweep_mode == 1 ? "coop " + std::to_string(c->sweep_grid) + "x" + std::to_string(c->sweep_block)
+                                 : c->sweep_mode == 0 ? "planes" : "untuned")
+          + "; measured: " + c->sweep_tuning;
+    return out.c_str();
 }
 
 const char* trans_last_error(void* ctx) {

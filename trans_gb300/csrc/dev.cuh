@@ -47,6 +47,20 @@ enum Slot {
     NSLOT = 151
 };
 
+// The DeltaQ-independent parts of A(Q)*DeltaQ (Time/TIME_LUSGS.F90:696-768) of one cell and
+// one direction:
+//   row L of A*dQ = AinRo*c[L][0] + AinRx*c[L][1] + AinRy*c[L][2] + AinRz*c[L][3] + AinRe*c[L][4]
+// row 0 is the unit normal (0, aSDx, aSDy, aSDz, 0); rows 1..3 are stored whole; row 4 keeps
+// (AinRo*VP)*GEt1 as two factors; VPT is the contravariant speed of the k-omega sweep.
+enum JacTerm { JC_R0 = 0, JC_R1 = 3, JC_R2 = 8, JC_R3 = 13, JC_VP = 18, JC_GET1 = 19, JC_R4 = 20, JC_VPT = 24, NJAC = 25 };
+
+// Per-cell record of the sweeps, stored in sweep (hyperplane) order so that the cells of one
+// hyperplane read consecutive addresses: the Jacobian terms and spectral radii of the three
+// lower (L sweep) and three upper (U sweep) neighbours, and the cell's own diagonal terms.
+enum SweepRec { REC_JL = 0, REC_JU = 3 * NJAC, REC_RDSL = 6 * NJAC, REC_RDSU = 6 * NJAC + 3,
+                REC_STEPT = 6 * NJAC + 6, REC_CVS = REC_STEPT + 1, REC_FM = REC_STEPT + 2, REC_FT = REC_STEPT + 3,
+                NREC = REC_STEPT + 4 };
+
 // face-flux components (per face and direction)
 enum FX { FX_VX = 0, FX_VY = 1, FX_VZ = 2, FX_VE = 3, FX_TK = 4, FX_TO = 5,
           FX_C0 = 6, FX_CK = 11, FX_CO = 12, NFX = 13 };
@@ -57,25 +71,62 @@ struct DevBlock {
     int nint;             // NI1*NJ1*NK1
     int pad_;
     double* base;
+    float* fbase;         // FP32 copies of the slots read by the FP32 kernels (mixed mode only)
+};
+
+constexpr int SWEEP_LANES = 8;   // threads per cell in the LU-SGS sweeps (one per DeltaQ component)
+
+struct MirrorList {       // slot ranges [first, first+count) copied FP64 -> FP32 (or back if to_fp64)
+    int n, to_fp64, first[6], count[6];
 };
 
 struct Tile {             // a run of consecutive interior cells (or faces) of one block
     int blk, start, count, pad_;
 };
 
-struct Params {           // module globals the kernels read (trans_params + derived)
-    double XM, RXM2, PPF, Csthlnd, Csth1, Ref, Tiny, VxF, VyF, VzF, omega0;
-    double P0in, T0in, Pouthub, VisRatio, FSTI;
-    double A1, Beta_star, Sigk1, Sigo1, Beta1, Gama1, Sigk2, Sigo2, Beta2, Gama2, Prod_Lmt;
-    double gama_max, gama_min, DT_LUSGS_Main, DT_LUSGS_Sub, CFL_Main, Trans_location;
+#define TG_PARAM_REALS(X) X(XM) X(RXM2) X(PPF) X(Csthlnd) X(Csth1) X(Ref) X(Tiny) X(VxF) X(VyF) X(VzF) \
+    X(omega0) X(P0in) X(T0in) X(Pouthub) X(VisRatio) X(FSTI) X(A1) X(Beta_star) X(Sigk1) X(Sigo1)    \
+    X(Beta1) X(Gama1) X(Sigk2) X(Sigo2) X(Beta2) X(Gama2) X(Prod_Lmt) X(gama_max) X(gama_min)        \
+    X(DT_LUSGS_Main) X(DT_LUSGS_Sub) X(CFL_Main) X(Trans_location)
+
+template <typename R>
+struct ParamsT {          // module globals the kernels read (trans_params + derived), in type R
+#define TG_DECL(n) R n;
+    TG_PARAM_REALS(TG_DECL)
+#undef TG_DECL
     int Kind_Spatial, Kind_Roe, Kind_Hybrid, Kind_SubHY, Kind_Dual, IF_Local_Main, IF_Local_Sub;
     int IF_Comppress, If_fix_Transition, pad_;
 };
+using Params = ParamsT<double>;
+
+template <typename R>
+inline ParamsT<R> params_as(const Params& p) {
+    ParamsT<R> q;
+#define TG_CONV(n) q.n = (R)p.n;
+    TG_PARAM_REALS(TG_CONV)
+#undef TG_CONV
+    q.Kind_Spatial = p.Kind_Spatial; q.Kind_Roe = p.Kind_Roe; q.Kind_Hybrid = p.Kind_Hybrid;
+    q.Kind_SubHY = p.Kind_SubHY; q.Kind_Dual = p.Kind_Dual; q.IF_Local_Main = p.IF_Local_Main;
+    q.IF_Local_Sub = p.IF_Local_Sub; q.IF_Comppress = p.IF_Comppress; q.If_fix_Transition = p.If_fix_Transition;
+    q.pad_ = 0;
+    return q;
+}
 
 __host__ __device__ inline int cidx(const DevBlock& b, int i, int j, int k) {
     return (i + 2) + b.PI * ((j + 2) + b.PJ * (k + 2));
 }
 __device__ inline double* slot(const DevBlock& b, int s) { return b.base + (size_t)s * (size_t)b.ncell; }
+__device__ inline float* fslot(const DevBlock& b, int s) { return b.fbase + (size_t)s * (size_t)b.ncell; }
+// slot s in the arithmetic type R: the FP64 arrays, or their FP32 copies in the mixed path
+template <typename R> __device__ inline R* rs(const DevBlock& b, int s);
+template <> __device__ inline double* rs<double>(const DevBlock& b, int s) { return slot(b, s); }
+template <> __device__ inline float* rs<float>(const DevBlock& b, int s) { return fslot(b, s); }
+
+// face average of a cell quantity at the face stored at cell cf (Space/SPACEINTERP_GetSurfCenterVars.F90)
+template <typename R>
+__device__ inline R favg(const R* q, const R* al, const R* ainv, int cf, int s) {
+    return (al[cf] * q[cf - s] + al[cf - s] * q[cf]) * ainv[cf];
+}
 
 template <typename R> __device__ inline R dmax(R a, R b) { return (a < b) ? b : a; }   // std::max
 template <typename R> __device__ inline R dmin(R a, R b) { return (b < a) ? b : a; }   // std::min
@@ -88,11 +139,11 @@ template <> __device__ inline double ttanh<double>(double x) { return tmx::tanh_
 template <> __device__ inline float ttanh<float>(float x) { return tanhf(x); }
 
 // Sutherland viscosity (Time/SpectralRadius.F90:59 and every copy of it)
-template <typename R> __device__ inline R mu_suth(const Params& p, R TT) {
+template <typename R> __device__ inline R mu_suth(const ParamsT<R>& p, R TT) {
     return (R(1.0) + R(p.Csthlnd)) / (TT * R(p.Csth1) + R(p.Csthlnd)) * p15(R(p.Csth1) * TT);
 }
 // the variant without Csth1 (Space/TURBTWO_DIFFUSION_Centered.F90:160)
-template <typename R> __device__ inline R mu_suth_nocs(const Params& p, R TT) {
+template <typename R> __device__ inline R mu_suth_nocs(const ParamsT<R>& p, R TT) {
     return (R(1.0) + R(p.Csthlnd)) / (TT + R(p.Csthlnd)) * p15(TT);
 }
 
@@ -149,7 +200,7 @@ template <typename R> __device__ inline void mdcd_pair(const R* s6, R gama, R& q
 
 // Space/CONVECT_Roe_Original.F90:242-407 (non-preconditioned, no rotation); out = flux / |S|
 template <typename R>
-__device__ inline void roe_flux(const Params& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo, R WRo,
+__device__ inline void roe_flux(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo, R WRo,
                                 R sav1, R sav2, R sav3, R sav, R* out) {
     R rcpcv = R(p.PPF);
     R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
@@ -210,7 +261,7 @@ __device__ inline void roe_flux(const Params& p, R PLo, R PRo, R TLo, R TRo, R U
 
 // Space/CONVECT_AUSMPW_Plus.F90:204-317; out = flux / |S|
 template <typename R>
-__device__ inline void ausmpw_flux(const Params& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo, R WRo,
+__device__ inline void ausmpw_flux(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo, R WRo,
                                    R sav1, R sav2, R sav3, R sav, R* out) {
     R rcpcv = R(p.PPF);
     R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
@@ -266,10 +317,12 @@ __device__ inline void ausmpw_flux(const Params& p, R PLo, R PRo, R TLo, R TRo, 
     out[4] = R(-1) * MMaL_plus * Acc * DENLo * HLo - MMaR_neg * Acc * DENRo * HRo;
 }
 
-// Time/TIME_LUSGS.F90:696-768 with pGam = 1.4 and zero grid speed
+// Time/TIME_LUSGS.F90:696-768 (LUSGS_ADQ) with pGam = 1.4 and zero grid speed, split into
+// the DeltaQ-independent terms (jac_terms, once per cell and direction) and the products with
+// DeltaQ (jac_row, inside the sweeps).  Every term is the reference's own subexpression, so
+// the split rounds exactly as the undivided expression does.
 template <typename R>
-__device__ inline void lusgs_adq(R pVx, R pVy, R pVz, R aSDx, R aSDy, R aSDz, R pPP, R roinv,
-                                 R AinRo, R AinRx, R AinRy, R AinRz, R AinRe, R* Dif) {
+__device__ inline void jac_terms(R pVx, R pVy, R pVz, R aSDx, R aSDy, R aSDz, R pPP, R roinv, R* J) {
     const R pGam = R(1.4);
     R VP = pVx * aSDx + pVy * aSDy + pVz * aSDz + R(0.0);
     R Ut2 = pVx * pVx + pVy * pVy + pVz * pVz;
@@ -277,22 +330,39 @@ __device__ inline void lusgs_adq(R pVx, R pVy, R pVz, R aSDx, R aSDy, R aSDz, R 
     const R Gm1 = R(1.4 - 1.0), Gm2 = R(1.4 - 2.0);
     R AA2 = pGam * pPP * roinv;
     R gUt2 = R(0.5) * Gm1 * Ut2;
-    Dif[0] = AinRo * aSDt + AinRx * aSDx + AinRy * aSDy + AinRz * aSDz + AinRe * R(0.0);
-    Dif[1] = AinRo * (aSDx * gUt2 - pVx * VP) + AinRx * (aSDt + VP - aSDx * Gm2 * pVx) + AinRy * (aSDy * pVx - aSDx * Gm1 * pVy)
-             + AinRz * (aSDz * pVx - aSDx * Gm1 * pVz) + AinRe * (aSDx * Gm1);
-    Dif[2] = AinRo * (aSDy * gUt2 - pVy * VP) + AinRx * (aSDx * pVy - aSDy * Gm1 * pVx) + AinRy * (aSDt + VP - aSDy * Gm2 * pVy)
-             + AinRz * (aSDz * pVy - aSDy * Gm1 * pVz) + AinRe * (aSDy * Gm1);
-    Dif[3] = AinRo * (aSDz * gUt2 - pVz * VP) + AinRx * (aSDx * pVz - aSDz * Gm1 * pVx) + AinRy * (aSDy * pVz - aSDz * Gm1 * pVy)
-             + AinRz * (aSDt + VP - aSDz * Gm2 * pVz) + AinRe * (aSDz * Gm1);
+    J[JC_R1 + 0] = aSDx * gUt2 - pVx * VP;
+    J[JC_R1 + 1] = aSDt + VP - aSDx * Gm2 * pVx;
+    J[JC_R1 + 2] = aSDy * pVx - aSDx * Gm1 * pVy;
+    J[JC_R1 + 3] = aSDz * pVx - aSDx * Gm1 * pVz;
+    J[JC_R1 + 4] = aSDx * Gm1;
+    J[JC_R2 + 0] = aSDy * gUt2 - pVy * VP;
+    J[JC_R2 + 1] = aSDx * pVy - aSDy * Gm1 * pVx;
+    J[JC_R2 + 2] = aSDt + VP - aSDy * Gm2 * pVy;
+    J[JC_R2 + 3] = aSDz * pVy - aSDy * Gm1 * pVz;
+    J[JC_R2 + 4] = aSDy * Gm1;
+    J[JC_R3 + 0] = aSDz * gUt2 - pVz * VP;
+    J[JC_R3 + 1] = aSDx * pVz - aSDz * Gm1 * pVx;
+    J[JC_R3 + 2] = aSDy * pVz - aSDz * Gm1 * pVy;
+    J[JC_R3 + 3] = aSDt + VP - aSDz * Gm2 * pVz;
+    J[JC_R3 + 4] = aSDz * Gm1;
+    J[JC_R0 + 0] = aSDx;
+    J[JC_R0 + 1] = aSDy;
+    J[JC_R0 + 2] = aSDz;
     R GEt1 = R(0.5) * Gm2 * Ut2 - AA2 / Gm1;
     R GEt2 = R(0.5) * Ut2 + AA2 / Gm1;
-    Dif[4] = AinRo * VP * GEt1 + AinRx * (aSDx * GEt2 - Gm1 * pVx * VP) + AinRy * (aSDy * GEt2 - Gm1 * pVy * VP)
-             + AinRz * (aSDz * GEt2 - Gm1 * pVz * VP) + AinRe * (aSDt + pGam * VP);
+    J[JC_VP] = VP;
+    J[JC_GET1] = GEt1;
+    J[JC_R4 + 0] = aSDx * GEt2 - Gm1 * pVx * VP;
+    J[JC_R4 + 1] = aSDy * GEt2 - Gm1 * pVy * VP;
+    J[JC_R4 + 2] = aSDz * GEt2 - Gm1 * pVz * VP;
+    J[JC_R4 + 3] = aSDt + pGam * VP;
+    // contravariant speed of TURBTWO_TIME_LUSGS_SST (no "+ 0" there)
+    J[JC_VPT] = pVx * aSDx + pVy * aSDy + pVz * aSDz;
 }
 
 // Time/Hybrid_function.F90:1-39
 template <typename R>
-__device__ inline R fsst(const Params& p, R Den, R vK, R vOmega, R Dist, R RmiuL, R CDiff) {
+__device__ inline R fsst(const ParamsT<R>& p, R Den, R vK, R vOmega, R Dist, R RmiuL, R CDiff) {
     R Ref = R(p.Ref);
     if (p.Kind_SubHY == 1 || p.Kind_SubHY == 3) {
         R arg1 = sqrt(vK) / (R(0.09) * vOmega * Dist * Ref);

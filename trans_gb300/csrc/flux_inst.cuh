@@ -7,27 +7,52 @@ namespace tg {
 namespace {
 template <int DIR>
 void ff(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const Params& p, int turb) {
-    if (nt > 0) k_face_flux<TG_R, DIR><<<nt, FACE_TILE, 0, s>>>(b, t, p, turb);
+    if (nt > 0) k_face_flux<TG_R, DIR><<<nt, FACE_TILE, 0, s>>>(b, t, params_as<TG_R>(p), turb);
 }
 void ga(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, int turb) {
     if (nt > 0) k_gather<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, turb);
 }
 void fc(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const Params& p) {
-    if (nt > 0) k_sst_fc1<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, p);
+    if (nt > 0) k_sst_fc1<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, params_as<TG_R>(p));
 }
-void rh(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const Params& p, int turb) {
-    if (nt > 0) k_lusgs_rhs<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, p, turb);
+void prep(cudaStream_t s, const DevBlock* b, const SweepView& v, const Params& p, int turb) {
+    if (v.n > 0)
+        k_lusgs_prep<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(
+            b, v.cells, v.nbp, (TG_R*)v.rec, (TG_R*)v.dq, v.n, p, params_as<TG_R>(p), turb);
 }
-void swl(cudaStream_t s, const DevBlock* b, const SweepCell* c, int first, int count, int turb) {
-    if (count > 0) k_sweep<TG_R, true><<<(count + 31) / 32, 32, 0, s>>>(b, c, first, count, turb);
+void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb) {
+    if (count > 0)
+        k_sweep<TG_R, true><<<(count * SWEEP_LANES + SWEEP_CTA - 1) / SWEEP_CTA, SWEEP_CTA, 0, s>>>(
+            v.nbp, (const TG_R*)v.rec, (TG_R*)v.dq, v.n, first, count, turb);
 }
-void swu(cudaStream_t s, const DevBlock* b, const SweepCell* c, int first, int count, int turb) {
-    if (count > 0) k_sweep<TG_R, false><<<(count + 31) / 32, 32, 0, s>>>(b, c, first, count, turb);
+void swu(cudaStream_t s, const SweepView& v, int first, int count, int turb) {
+    if (count > 0)
+        k_sweep<TG_R, false><<<(count * SWEEP_LANES + SWEEP_CTA - 1) / SWEEP_CTA, SWEEP_CTA, 0, s>>>(
+            v.nbp, (const TG_R*)v.rec, (TG_R*)v.dq, v.n, first, count, turb);
+}
+cudaError_t swa(cudaStream_t s, const SweepView& v, const int* po, int nplanes, int turb, SweepSync* sy, int grid, int block) {
+    unsigned limit = SWEEP_SPIN_LIMIT;
+    const int* nbp = v.nbp;
+    const TG_R* rec = (const TG_R*)v.rec;
+    TG_R* dq = (TG_R*)v.dq;
+    long long n = v.n;
+    void* args[] = {(void*)&nbp, (void*)&rec, (void*)&dq, (void*)&n, (void*)&po, (void*)&nplanes, (void*)&turb,
+                    (void*)&sy, (void*)&limit};
+    return cudaLaunchCooperativeKernel((const void*)k_sweep_all<TG_R>, dim3(grid), dim3(block), args, 0, s);
+}
+int swa_occ(int block) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_all<TG_R>, block, 0) != cudaSuccess) return 0;
+    return n;
+}
+void scat(cudaStream_t s, const DevBlock* b, const SweepView& v) {
+    if (v.n > 0)
+        k_sweep_scatter<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(b, v.cells, (const TG_R*)v.dq, v.n);
 }
 }  // namespace
 
 const FluxLaunchers& TG_NAME() {
-    static const FluxLaunchers L = {{ff<1>, ff<2>, ff<3>}, ga, fc, rh, swl, swu};
+    static const FluxLaunchers L = {{ff<1>, ff<2>, ff<3>}, ga, fc, prep, swl, swu, swa, swa_occ, scat, sizeof(TG_R)};
     return L;
 }
 }  // namespace tg

@@ -28,8 +28,12 @@ void launch_gradient(cudaStream_t s, const DevBlock* blks, const Tile* tiles, in
 void launch_shock_ghost(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt) {
     if (nt > 0) k_shock_ghost<<<nt, CELL_TILE, 0, s>>>(blks, tiles);
 }
-void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts) {
-    if (nt > 0) k_update<<<nt, CELL_TILE, 0, s>>>(blks, tiles, p, turb_upd, parts);
+void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts,
+                   int d_fp32) {
+    if (nt > 0) k_update<<<nt, CELL_TILE, 0, s>>>(blks, tiles, p, turb_upd, parts, d_fp32);
+}
+void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml) {
+    if (total > 0) k_mirror<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off, ml);
 }
 void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int kind_dual) {
     if (nt > 0) k_update_u<<<nt, CELL_TILE, 0, s>>>(blks, tiles, kind_dual);

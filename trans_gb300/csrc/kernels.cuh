@@ -380,12 +380,23 @@ __global__ void k_prims(const DevBlock* __restrict__ blks, int nblk, long long t
     slot(b, S_SVEL + 2)[c] = slot(b, S_V + 3)[c] * ri;
 }
 
-#endif  // TG_COMMON_KERNELS
-
-// face average of a cell quantity at the face stored at cell cf (Space/SPACEINTERP_GetSurfCenterVars.F90)
-__device__ inline double favg(const double* q, const double* al, const double* ainv, int cf, int s) {
-    return (al[cf] * q[cf - s] + al[cf - s] * q[cf]) * ainv[cf];
+// FP32 copies of FP64 slot ranges over every padded cell (mixed path)
+__global__ void k_mirror(const DevBlock* __restrict__ blks, int nblk, long long total, const long long* __restrict__ off,
+                         MirrorList ml) {
+    long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = nblk - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (off[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DevBlock b = blks[lo];
+    int c = (int)(g - off[lo]);
+    for (int r = 0; r < ml.n; ++r)
+        for (int q = ml.first[r]; q < ml.first[r] + ml.count[r]; ++q) {
+            if (ml.to_fp64) slot(b, q)[c] = (double)fslot(b, q)[c];
+            else fslot(b, q)[c] = (float)slot(b, q)[c];
+        }
 }
+
+#endif  // TG_COMMON_KERNELS
 
 #ifdef TG_COMMON_KERNELS
 // ---------------------------------------------------------------------------------------
@@ -462,7 +473,7 @@ __global__ void k_shock_ghost(const DevBlock* __restrict__ blks, const Tile* __r
 //   Space/CONVECT_Roe_Original.F90 | Space/CONVECT_AUSMPW_Plus.F90, Space/TURBTWO_CONVECT_Upwind.F90
 // ---------------------------------------------------------------------------------------
 template <typename R, int DIR>
-__global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, int turb) {
+__global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, ParamsT<R> p, int turb) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
@@ -473,36 +484,36 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
     const int s = DIR == 1 ? 1 : (DIR == 2 ? b.PI : b.PI * b.PJ);
     const int c = cidx(b, i, j, k);
     const int cm = c - s, cp = c + s;
-    const double* al = slot(b, S_ALAGM + d);
-    const double* ainv = slot(b, S_AINV + d);
-    const double* pu = slot(b, S_PRIM);
-    const double* pv = slot(b, S_PRIM + 1);
-    const double* pw = slot(b, S_PRIM + 2);
-    const double* pk = slot(b, S_PRIM + 3);
-    const double* po = slot(b, S_PRIM + 4);
-    const double* PT = slot(b, S_T);
-    const double* PPp = slot(b, S_PP);
-    const double* SDd = slot(b, S_SD + 3 * d);
+    const R* al = rs<R>(b, S_ALAGM + d);
+    const R* ainv = rs<R>(b, S_AINV + d);
+    const R* pu = rs<R>(b, S_PRIM);
+    const R* pv = rs<R>(b, S_PRIM + 1);
+    const R* pw = rs<R>(b, S_PRIM + 2);
+    const R* pk = rs<R>(b, S_PRIM + 3);
+    const R* po = rs<R>(b, S_PRIM + 4);
+    const R* PT = rs<R>(b, S_T);
+    const R* PPp = rs<R>(b, S_PP);
+    const R* SDd = rs<R>(b, S_SD + 3 * d);
     const size_t nc = (size_t)b.ncell;
-    double* FX = slot(b, S_FX + NFX * d);
+    R* FX = rs<R>(b, S_FX + NFX * d);
     // ---------------- viscous flux (DIFFUSION_Centered) ----------------
-    const bool wall = slot(b, S_WALL + d)[c] != 0.0;
-    const double vinv = slot(b, S_VINV + d)[c];
-    const double vall = slot(b, S_VOL)[cm] * vinv;
-    const double valr = slot(b, S_VOL)[c] * vinv;
+    const bool wall = rs<R>(b, S_WALL + d)[c] != R(0.0);
+    const R vinv = rs<R>(b, S_VINV + d)[c];
+    const R vall = rs<R>(b, S_VOL)[cm] * vinv;
+    const R valr = rs<R>(b, S_VOL)[c] * vinv;
     const R alsinv = wall ? R(0.0) : R(vinv);
-    const double* qv[4] = {pu, pv, pw, PT};
+    const R* qv[4] = {pu, pv, pw, PT};
     R g[4][3];
     for (int q = 0; q < 4; ++q) {
-        const double* Q = qv[q];
-        R disfpp = R(favg(Q, al, ainv, cp, s));
-        R disfnn = R(favg(Q, al, ainv, cm, s));
+        const R* Q = qv[q];
+        R disfpp = (favg<R>(Q, al, ainv, cp, s));
+        R disfnn = (favg<R>(Q, al, ainv, cm, s));
         R disfp = R(Q[c]), disfn = R(Q[cm]);
-        const double* DQ0 = slot(b, S_DQ + 3 * q);
+        const R* DQ0 = rs<R>(b, S_DQ + 3 * q);
         for (int m = 0; m < 3; ++m) {
-            const double* G = DQ0 + (size_t)m * nc;
+            const R* G = DQ0 + (size_t)m * nc;
             R xL = R(vall) * R(G[cm]) + R(valr) * R(G[c]);
-            const double* S = SDd + (size_t)m * nc;
+            const R* S = SDd + (size_t)m * nc;
             R cmv = alsinv * (-R(S[cp]) * (disfpp - disfp) - R(S[cm]) * (disfn - disfnn) + R(S[c]) * (disfp - disfn));
             g[q][m] = cmv + xL;
         }
@@ -510,9 +521,9 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
     const R a0 = R(al[c]), a1 = R(al[cm]);
     const R ai = R(ainv[c]);
     const R all = a0 * ai, alr = a1 * ai;
-    const R TTL = R(favg(PT, al, ainv, c, s));
+    const R TTL = (favg<R>(PT, al, ainv, c, s));
     const R RmiuL = mu_suth<R>(p, TTL);
-    const double* Rm = slot(b, S_RMIU);
+    const R* Rm = rs<R>(b, S_RMIU);
     R RmiuTL = all * R(Rm[cm]) + alr * R(Rm[c]);
     if (wall) RmiuTL = R(0.0);
     {
@@ -530,38 +541,38 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
         R Tzx = RmiuL * (DuDzL + DwDxL) + RmiuTL * (DuDzL + DwDxL);
         R cp_ = R(1.4) * R(p.PPF) / R(1.4 - 1.0);
         R akmu = cp_ * (RmiuL / R(0.72) + RmiuTL / R(0.9));
-        R ucc = R(favg(pu, al, ainv, c, s)), vcc = R(favg(pv, al, ainv, c, s)), wcc = R(favg(pw, al, ainv, c, s));
+        R ucc = (favg<R>(pu, al, ainv, c, s)), vcc = (favg<R>(pv, al, ainv, c, s)), wcc = (favg<R>(pw, al, ainv, c, s));
         R Phix = akmu * DTDxL + ucc * Txx + vcc * Txy + wcc * Tzx;
         R Phiy = akmu * DTDyL + ucc * Txy + vcc * Tyy + wcc * Tyz;
         R Phiz = akmu * DTDzL + ucc * Tzx + vcc * Tyz + wcc * Tzz;
         R Dx = R(SDd[c]), Dy = R(SDd[c + nc]), Dz = R(SDd[c + 2 * nc]);
         R Ref = R(p.Ref);
-        FX[(size_t)FX_VX * nc + c] = (double)((Txx * Dx + Txy * Dy + Tzx * Dz) / Ref);
-        FX[(size_t)FX_VY * nc + c] = (double)((Txy * Dx + Tyy * Dy + Tyz * Dz) / Ref);
-        FX[(size_t)FX_VZ * nc + c] = (double)((Tzx * Dx + Tyz * Dy + Tzz * Dz) / Ref);
-        FX[(size_t)FX_VE * nc + c] = (double)((Phix * Dx + Phiy * Dy + Phiz * Dz) / Ref);
+        FX[(size_t)FX_VX * nc + c] = ((Txx * Dx + Txy * Dy + Tzx * Dz) / Ref);
+        FX[(size_t)FX_VY * nc + c] = ((Txy * Dx + Tyy * Dy + Tyz * Dz) / Ref);
+        FX[(size_t)FX_VZ * nc + c] = ((Tzx * Dx + Tyz * Dy + Tzz * Dz) / Ref);
+        FX[(size_t)FX_VE * nc + c] = ((Phix * Dx + Phiy * Dy + Phiz * Dz) / Ref);
     }
     // ---------------- k-omega diffusion (TURBTWO_DIFFUSION_Centered) ----------------
     if (turb) {
         R gt[2][3];
-        const double* qt[2] = {pk, po};
+        const R* qt[2] = {pk, po};
         for (int q = 0; q < 2; ++q) {
-            const double* Q = qt[q];
-            R disfpp = R(favg(Q, al, ainv, cp, s));
-            R disfnn = R(favg(Q, al, ainv, cm, s));
+            const R* Q = qt[q];
+            R disfpp = (favg<R>(Q, al, ainv, cp, s));
+            R disfnn = (favg<R>(Q, al, ainv, cm, s));
             R disfp = R(Q[c]), disfn = R(Q[cm]);
-            const double* DQ0 = slot(b, S_DQ + 12 + 3 * q);
+            const R* DQ0 = rs<R>(b, S_DQ + 12 + 3 * q);
             for (int m = 0; m < 3; ++m) {
-                const double* G = DQ0 + (size_t)m * nc;
+                const R* G = DQ0 + (size_t)m * nc;
                 R xL = R(vall) * R(G[cm]) + R(valr) * R(G[c]);
-                const double* S = SDd + (size_t)m * nc;
+                const R* S = SDd + (size_t)m * nc;
                 R cmv = alsinv * (-R(S[cp]) * (disfpp - disfp) - R(S[cm]) * (disfn - disfnn) + R(S[c]) * (disfp - disfn));
                 gt[q][m] = cmv + xL;
             }
         }
         R TTLt = all * R(PT[cm]) + alr * R(PT[c]);
         R RmiuLt = mu_suth_nocs<R>(p, TTLt);
-        const double* V1 = slot(b, S_V);
+        const R* V1 = rs<R>(b, S_V);
         R DEN0 = R(V1[c]), TKK0 = R(pk[c]), TOO0 = R(po[c]);
         R DEN1 = R(V1[cm]), TKK1 = R(pk[cm]), TOO1 = R(po[cm]);
         R Den = all * DEN1 + alr * DEN0;
@@ -570,7 +581,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
         R dTKO = gt[0][0] * gt[1][0] + gt[0][1] * gt[1][1] + gt[0][2] * gt[1][2];
         R Sigo2 = R(p.Sigo2), Bs = R(p.Beta_star), Ref = R(p.Ref);
         R CDKO = dmax(R(2.0) * Den * Sigo2 / TOO * (dTKO), R(1.0e-10));
-        const double* Dst = slot(b, S_DST);
+        const R* Dst = rs<R>(b, S_DST);
         R distfc = alr * R(Dst[c]) + all * R(Dst[cm]);
         R arg1 = dmax(sqrt(TKK) / Bs / TOO / distfc / Ref, R(500.0) * RmiuLt / Den / distfc / distfc / TOO / Ref / Ref);
         arg1 = dmin(arg1, R(4.0) * Den * Sigo2 * TKK / CDKO / distfc / distfc);
@@ -581,16 +592,16 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
         R vmute = RmiuLt + RmiuTL * SigkAB;
         R vmuoq = RmiuLt + RmiuTL * SigoAB;
         R Dx = R(SDd[c]), Dy = R(SDd[c + nc]), Dz = R(SDd[c + 2 * nc]);
-        FX[(size_t)FX_TK * nc + c] = (double)((vmute * (gt[0][0] * Dx + gt[0][1] * Dy + gt[0][2] * Dz)) / Ref);
-        FX[(size_t)FX_TO * nc + c] = (double)((vmuoq * (gt[1][0] * Dx + gt[1][1] * Dy + gt[1][2] * Dz)) / Ref);
+        FX[(size_t)FX_TK * nc + c] = ((vmute * (gt[0][0] * Dx + gt[0][1] * Dy + gt[0][2] * Dz)) / Ref);
+        FX[(size_t)FX_TO * nc + c] = ((vmuoq * (gt[1][0] * Dx + gt[1][1] * Dy + gt[1][2] * Dz)) / Ref);
     }
     // ---------------- reconstruction ----------------
     R qL[7], qR[7];
-    const double* qc[5] = {pu, pv, pw, PPp, PT};
+    const R* qc[5] = {pu, pv, pw, PPp, PT};
     if (p.Kind_Spatial == 2) {
         for (int q = 0; q < 5; ++q) {
-            const double* Q = qc[q];
-            R fm = R(favg(Q, al, ainv, cm, s)), f0 = R(favg(Q, al, ainv, c, s)), fp = R(favg(Q, al, ainv, cp, s));
+            const R* Q = qc[q];
+            R fm = (favg<R>(Q, al, ainv, cm, s)), f0 = (favg<R>(Q, al, ainv, c, s)), fp = (favg<R>(Q, al, ainv, cp, s));
             R q1 = R(Q[cm]), q0 = R(Q[c]);
             R DR = f0 - q1, DL = q1 - fm;
             qL[q] = q1 + alimiter(DR, DL);
@@ -598,7 +609,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
             qR[q] = q0 - alimiter(DL, DR);
         }
     } else {
-        const double* sh = slot(b, S_SHOCK);
+        const R* sh = rs<R>(b, S_SHOCK);
         R sensor = R(sh[c - 3 * s]);
         sensor = dmax(sensor, R(sh[c - 2 * s]));
         sensor = dmax(sensor, R(sh[c - s]));
@@ -608,17 +619,17 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
         if (DIR == 3) sensor = dmax(sensor, R(0.0));
         R gama = R(p.gama_min) + sensor * (R(p.gama_max) - R(p.gama_min));
         for (int q = 0; q < 5; ++q) {
-            const double* Q = qc[q];
+            const R* Q = qc[q];
             R s6[6];
             for (int o = 0; o < 6; ++o) s6[o] = R(Q[c + (o - 3) * s]);
             mdcd_pair(s6, gama, qL[q], qR[q]);
         }
     }
     if (turb) {
-        const double* qk[2] = {pk, po};
+        const R* qk[2] = {pk, po};
         for (int q = 0; q < 2; ++q) {
-            const double* Q = qk[q];
-            R fm = R(favg(Q, al, ainv, cm, s)), f0 = R(favg(Q, al, ainv, c, s)), fp = R(favg(Q, al, ainv, cp, s));
+            const R* Q = qk[q];
+            R fm = (favg<R>(Q, al, ainv, cm, s)), f0 = (favg<R>(Q, al, ainv, c, s)), fp = (favg<R>(Q, al, ainv, cp, s));
             R q1 = R(Q[cm]), q0 = R(Q[c]);
             R DR = f0 - q1, DL = q1 - fm;
             qL[5 + q] = q1 + alimiter(DR, DL);
@@ -628,13 +639,13 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
     }
     // ---------------- inviscid flux ----------------
     R sav1 = R(SDd[c]), sav2 = R(SDd[c + nc]), sav3 = R(SDd[c + 2 * nc]);
-    R sav = R(slot(b, S_GRAD + d)[c]);
+    R sav = R(rs<R>(b, S_GRAD + d)[c]);
     R f[5];
     if (p.Kind_Roe == 1)
         roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
     else
         ausmpw_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
-    for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = (double)(f[L] * sav);
+    for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = (f[L] * sav);
     if (turb) {
         R rcpcv = R(p.PPF);
         R DENL = qL[3] / (rcpcv * qL[4]), DENR = qR[3] / (rcpcv * qR[4]);
@@ -647,8 +658,8 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
         R dTK = R(-0.5) * (rulnormal * TKL + rurnormal * TKR - eigTKO * (DENR * TKR - DENL * TKL));
         R TOL = dmax(qL[6], small), TOR = dmax(qR[6], small);
         R dTO = R(-0.5) * (rulnormal * TOL + rurnormal * TOR - eigTKO * (DENR * TOR - DENL * TOL));
-        FX[(size_t)FX_CK * nc + c] = (double)dTK;
-        FX[(size_t)FX_CO * nc + c] = (double)dTO;
+        FX[(size_t)FX_CK * nc + c] = dTK;
+        FX[(size_t)FX_CO * nc + c] = dTO;
     }
 }
 
@@ -666,29 +677,29 @@ __global__ void k_gather(const DevBlock* __restrict__ blks, const Tile* __restri
     int c = cidx(b, I, J, K);
     const int st[3] = {1, b.PI, b.PI * b.PJ};
     const size_t nc = (size_t)b.ncell;
-    const double* FX = slot(b, S_FX);
+    const R* FX = rs<R>(b, S_FX);
     auto fx = [&](int d, int m, int cc) { return R(FX[(size_t)(NFX * d + m) * nc + cc]); };
     {   // rho: no viscous flux
         R acc = R(0.0);
         for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_C0, c); acc = acc + fx(d, FX_C0, c + st[d]); }
-        slot(b, S_D)[c] = (double)acc;
+        rs<R>(b, S_D)[c] = acc;
     }
     for (int L = 1; L < 5; ++L) {
         R acc = R(0.0);
         for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_VX + L - 1, c); acc = acc + fx(d, FX_VX + L - 1, c + st[d]); }
         for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_C0 + L, c); acc = acc + fx(d, FX_C0 + L, c + st[d]); }
-        slot(b, S_D + L)[c] = (double)acc;
+        rs<R>(b, S_D + L)[c] = acc;
     }
     if (turb) {
         for (int q = 0; q < 2; ++q) {
             R acc = R(0.0);
             for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_TK + q, c); acc = acc + fx(d, FX_TK + q, c + st[d]); }
             for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_CK + q, c); acc = acc + fx(d, FX_CK + q, c + st[d]); }
-            slot(b, S_D + 5 + q)[c] = (double)acc;
+            rs<R>(b, S_D + 5 + q)[c] = acc;
         }
     } else {
-        slot(b, S_D + 5)[c] = 0.0;
-        slot(b, S_D + 6)[c] = 0.0;
+        rs<R>(b, S_D + 5)[c] = R(0.0);
+        rs<R>(b, S_D + 6)[c] = R(0.0);
     }
 }
 
@@ -697,13 +708,13 @@ __global__ void k_gather(const DevBlock* __restrict__ blks, const Tile* __restri
 // of the lexicographically next cell
 // ---------------------------------------------------------------------------------------
 template <typename R>
-__device__ inline R sst_fc1(const Params& p, const DevBlock& b, int c) {
-    R ARo = R(slot(b, S_V)[c]), ARTk = R(slot(b, S_V + 5)[c]), ARTO = R(slot(b, S_V + 6)[c]);
-    R cdif = R(slot(b, S_DQ + 12)[c]) * R(slot(b, S_DQ + 15)[c]) + R(slot(b, S_DQ + 13)[c]) * R(slot(b, S_DQ + 16)[c])
-             + R(slot(b, S_DQ + 14)[c]) * R(slot(b, S_DQ + 17)[c]);
-    R TT = R(slot(b, S_T)[c]);
+__device__ inline R sst_fc1(const ParamsT<R>& p, const DevBlock& b, int c) {
+    R ARo = (rs<R>(b, S_V)[c]), ARTk = (rs<R>(b, S_V + 5)[c]), ARTO = (rs<R>(b, S_V + 6)[c]);
+    R cdif = (rs<R>(b, S_DQ + 12)[c]) * (rs<R>(b, S_DQ + 15)[c]) + (rs<R>(b, S_DQ + 13)[c]) * (rs<R>(b, S_DQ + 16)[c])
+             + (rs<R>(b, S_DQ + 14)[c]) * (rs<R>(b, S_DQ + 17)[c]);
+    R TT = (rs<R>(b, S_T)[c]);
     R RmiuL = mu_suth<R>(p, TT);
-    R DistN = R(slot(b, S_DST)[c]);
+    R DistN = (rs<R>(b, S_DST)[c]);
     R Ref = R(p.Ref), Sigo2 = R(p.Sigo2), Bs = R(p.Beta_star);
     R CDKO = dmax(R(2.0) * ARo * Sigo2 / (ARTO / ARo) * cdif, R(1.0e-10));
     R arg1 = dmax(sqrt(ARTk / ARo) / Bs / (ARTO / ARo) / DistN / Ref, R(500.0) * RmiuL / DistN / DistN / ARTO / Ref / Ref);
@@ -713,48 +724,74 @@ __device__ inline R sst_fc1(const Params& p, const DevBlock& b, int c) {
 }
 
 template <typename R>
-__global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p) {
+__global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, ParamsT<R> p) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
     int n = t.start + threadIdx.x;
     int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     int c = cidx(b, I, J, K);
-    slot(b, S_FC1)[c] = (double)sst_fc1<R>(p, b, c);
+    rs<R>(b, S_FC1)[c] = sst_fc1<R>(p, b, c);
 }
 
 // ---------------------------------------------------------------------------------------
 // Time/TIME_LUSGS.F90:60-108 and Time/TURBTWO_TIME_LUSGS_SST.F90:118-411: right-hand sides,
-// SST sources and the two diagonals
+// SST sources and the two diagonals, one thread per sweep position; the results go to the
+// sweep-order arrays together with the neighbours' Jacobian terms and spectral radii.
 // ---------------------------------------------------------------------------------------
 template <typename R>
-__global__ void k_lusgs_rhs(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, int turb) {
-    const Tile t = tiles[blockIdx.x];
-    if ((int)threadIdx.x >= t.count) return;
-    const DevBlock b = blks[t.blk];
-    int n = t.start + threadIdx.x;
-    int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
-    int c = cidx(b, I, J, K);
-    const double DT = p.DT_LUSGS_Main;
+__global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, const int* __restrict__ nbp,
+                             R* __restrict__ rec, R* __restrict__ dq, long long N, Params pd, ParamsT<R> p, int turb) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    const SweepCell sc = cells[q];
+    const DevBlock b = blks[sc.blk];
+    const int I = sc.i, J = sc.j, K = sc.k;
+    const int nlex = (I - 1) + b.NI1 * ((J - 1) + b.NJ1 * (K - 1));     // lexicographic interior index
+    const int c = cidx(b, I, J, K);
+    const size_t nc = (size_t)b.ncell;
+    auto REC = [&](int m) -> R& { return rec[(size_t)m * N + q]; };
+    auto DQ = [&](int L) -> R& { return dq[(size_t)L * N + q]; };
+    // BDF2 right-hand side and the mean-flow diagonal, in FP64 in both paths
+    const double DT = pd.DT_LUSGS_Main;
     double Dtm = slot(b, S_DTM)[c];
     double vol = slot(b, S_VOL)[c];
     double stept = 2.0 * Dtm / (3.0 * Dtm / DT + 2.0);
     double cvs = stept / vol;
-    slot(b, S_STEPT)[c] = stept;
-    slot(b, S_CVS)[c] = cvs;
-    for (int L = 0; L < 5; ++L) {
-        double* D = slot(b, S_D + L);
-        D[c] = D[c] / vol - (3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c]) * 0.5 / DT;
-    }
+    REC(REC_STEPT) = R(stept);
+    REC(REC_CVS) = R(cvs);
+    for (int L = 0; L < 5; ++L)
+        DQ(L) = R((double)rs<R>(b, S_D + L)[c] / vol
+                  - (3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c]) * 0.5 / DT);
     double rsum = slot(b, S_RDS)[c] + slot(b, S_RDS + 1)[c] + slot(b, S_RDS + 2)[c];
     double fm = 1.0 + rsum * cvs;
-    slot(b, S_FM)[c] = fm;
-    if (!turb) return;
-    for (int L = 5; L < 7; ++L) {
-        double* D = slot(b, S_D + L);
-        D[c] = D[c] / vol - (3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c]) * 0.5 / DT;
+    REC(REC_FM) = R(fm);
+    {   // Jacobian terms and spectral radii of the lower and upper neighbours (nbp < 0: none)
+        const R* sv = rs<R>(b, S_SVEL);
+        const R* PPr = rs<R>(b, S_PP);
+        const R* RIr = rs<R>(b, S_RINV);
+        const int st[3] = {1, b.PI, b.PI * b.PJ};
+        for (int side = 0; side < 2; ++side)
+            for (int d = 0; d < 3; ++d) {
+                if (nbp[(size_t)(3 * side + d) * N + q] < 0) continue;
+                const int nb = side == 0 ? c - st[d] : c + st[d];
+                const R* asd = rs<R>(b, S_ASD + 3 * d);
+                R Jt[NJAC];
+                jac_terms<R>(sv[nb], sv[nb + nc], sv[nb + 2 * nc], asd[nb], asd[nb + nc], asd[nb + 2 * nc], PPr[nb], RIr[nb], Jt);
+                const int base = (side == 0 ? REC_JL : REC_JU) + NJAC * d;
+                for (int m = 0; m < NJAC; ++m) REC(base + m) = Jt[m];
+                REC((side == 0 ? REC_RDSL : REC_RDSU) + d) = rs<R>(b, S_RDS + d)[nb];
+            }
     }
-    auto G = [&](int q) { return R(slot(b, S_DQ + q)[c]); };
+    if (!turb) {
+        DQ(5) = rs<R>(b, S_D + 5)[c];
+        DQ(6) = rs<R>(b, S_D + 6)[c];
+        return;
+    }
+    for (int L = 5; L < 7; ++L)
+        DQ(L) = R((double)rs<R>(b, S_D + L)[c] / vol
+                  - (3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c]) * 0.5 / DT);
+    auto G = [&](int q) { return rs<R>(b, S_DQ + q)[c]; };
     R dudx = G(0), dudy = G(1), dudz = G(2), dvdx = G(3), dvdy = G(4), dvdz = G(5), dwdx = G(6), dwdy = G(7), dwdz = G(8);
     R dtkdx = G(12), dtkdy = G(13), dtkdz = G(14), dtodx = G(15), dtody = G(16), dtodz = G(17);
     R Div = dudx + dvdy + dwdz;
@@ -763,38 +800,38 @@ __global__ void k_lusgs_rhs(const DevBlock* __restrict__ blks, const Tile* __res
               - R(2.0 / 3.0) * Div * Div);
     R cdif = dtkdx * dtodx + dtkdy * dtody + dtkdz * dtodz;
     const R Ref = R(p.Ref), Bs = R(p.Beta_star), Sigo2 = R(p.Sigo2);
-    R tprod = dmin(prod, Votg) * R(slot(b, S_RMIU)[c]) / Ref;
-    R ARo = R(slot(b, S_V)[c]), ARTk = R(slot(b, S_V + 5)[c]), ARTO = R(slot(b, S_V + 6)[c]);
+    R tprod = dmin(prod, Votg) * (rs<R>(b, S_RMIU)[c]) / Ref;
+    R ARo = (rs<R>(b, S_V)[c]), ARTk = (rs<R>(b, S_V + 5)[c]), ARTO = (rs<R>(b, S_V + 6)[c]);
     R tprodl1 = R(p.Prod_Lmt) * Bs * ARTk * ARTO / ARo * Ref;
     tprod = dmin(tprod, tprodl1);
-    R TT = R(slot(b, S_T)[c]);
+    R TT = (rs<R>(b, S_T)[c]);
     R RmiuL = mu_suth<R>(p, TT);
     R Fdes = R(1.0);
     if (p.Kind_Hybrid == 3) {
         // DES length scale with the loop-carried F1 and omega of the previous interior cell
         // (TURBTWO_TIME_LUSGS_SST.F90:192-213); the first cell uses F1 = 0 and its own omega
-        int np = n - 1;
+        int np = nlex - 1;
         R arg1p = R(0.0), Vomp = ARTO / ARo;
         if (np >= 0) {
             int Ip = np % b.NI1 + 1, Jp = (np / b.NI1) % b.NJ1 + 1, Kp = np / (b.NI1 * b.NJ1) + 1;
             int cq = cidx(b, Ip, Jp, Kp);
-            arg1p = R(slot(b, S_FC1)[cq]);
-            Vomp = R(slot(b, S_V + 6)[cq]) / R(slot(b, S_V)[cq]);
+            arg1p = (rs<R>(b, S_FC1)[cq]);
+            Vomp = (rs<R>(b, S_V + 6)[cq]) / (rs<R>(b, S_V)[cq]);
         }
         R aLt = sqrt(ARTk / ARo) / (Bs * ARTO / ARo * Ref);
         R Cdiff = (R(2. * 0.856) / Vomp) / Ref * cdif;
         R vOmega = ARTO / ARo;
-        R Fsst = fsst<R>(p, ARo, ARTk / ARo, vOmega, R(slot(b, S_DST)[c]), RmiuL, Cdiff);
-        R aLgrd = ((R(1.) - arg1p) * R(0.61) + arg1p * R(0.78)) * R(slot(b, S_ALENG)[c]);
+        R Fsst = fsst<R>(p, ARo, ARTk / ARo, vOmega, (rs<R>(b, S_DST)[c]), RmiuL, Cdiff);
+        R aLgrd = ((R(1.) - arg1p) * R(0.61) + arg1p * R(0.78)) * (rs<R>(b, S_ALENG)[c]);
         Fdes = dmax(aLt * (R(1.) - Fsst) / aLgrd, R(1.0));
     }
-    R DistN = R(slot(b, S_DST)[c]);
+    R DistN = (rs<R>(b, S_DST)[c]);
     R CDKO = dmax(R(2.0) * ARo * Sigo2 / (ARTO / ARo) * cdif, R(1.0e-10));
     R arg1 = dmax(sqrt(ARTk / ARo) / Bs / (ARTO / ARo) / DistN / Ref, R(500.0) * RmiuL / DistN / DistN / ARTO / Ref / Ref);
     arg1 = dmin(arg1, R(4.0) * Sigo2 * ARTk / CDKO / DistN / DistN);
     R a2 = arg1 * arg1;
     arg1 = ttanh(a2 * a2);
-    R AA = sqrt(R(1.4) * R(slot(b, S_PP)[c]) / ARo);
+    R AA = sqrt(R(1.4) * (rs<R>(b, S_PP)[c]) / ARo);
     R Mt = sqrt(ARTk / ARo) / AA;
     const R Alf1 = R(1.0), Alf2 = R(0.4), Alf3 = R(0.2);
     const R c23 = R(2.0 / 3.0);
@@ -808,8 +845,8 @@ __global__ void k_lusgs_rhs(const DevBlock* __restrict__ blks, const Tile* __res
     }
     Source = SourceP + SourceN1 * ARTk;
     CnegTk = fabs(SourceN1);
-    if (p.If_fix_Transition && slot(b, S_XC)[c] < p.Trans_location) Source = R(0.0);
-    slot(b, S_D + 5)[c] = slot(b, S_D + 5)[c] + (double)Source;
+    if (p.If_fix_Transition && rs<R>(b, S_XC)[c] < p.Trans_location) Source = R(0.0);
+    DQ(5) = DQ(5) + Source;
     tprod = dmin(prod, Votg) / Ref;
     R GamaAB = R(p.Gama1) * arg1 + R(p.Gama2) * (R(1.0) - arg1);
     R BetaAB = R(p.Beta1) * arg1 + R(p.Beta2) * (R(1.0) - arg1);
@@ -824,69 +861,136 @@ __global__ void k_lusgs_rhs(const DevBlock* __restrict__ blks, const Tile* __res
     R SourceCross = R(2.0) * (R(1) - arg1) * ARo * Sigo2 / (ARTO / ARo) * cdif / Ref;
     SourceCross = sgn1(SourceCross) * dmin(fabs(SourceCross), fabs(SourceP) * R(0.5));
     Source = Source + SourceCross;
-    slot(b, S_D + 6)[c] = slot(b, S_D + 6)[c] + (double)Source;
+    DQ(6) = DQ(6) + Source;
     CnegTO = R(2.0) * fabs(SourceN1);
-    slot(b, S_FT)[c] = fm + (double)((CnegTk + CnegTO) * R(stept));
+    REC(REC_FT) = R(fm) + (CnegTk + CnegTO) * R(stept);
 }
 
 // ---------------------------------------------------------------------------------------
-// LU-SGS sweeps on one i+j+k hyperplane of every block (Time/TIME_LUSGS.F90:172-675,
-// Time/TURBTWO_TIME_LUSGS_SST.F90:562-766).  Any order of the (i-1,j-1,k-1) dependency graph
-// reproduces the lexicographic sweep exactly; hyperplanes are such an order.
+// LU-SGS sweeps (Time/TIME_LUSGS.F90:172-675, Time/TURBTWO_TIME_LUSGS_SST.F90:562-766) on the
+// i+j+k hyperplanes of every block.  Any order of the (i-1,j-1,k-1) dependency graph
+// reproduces the lexicographic sweep exactly; hyperplanes are such an order.  A hyperplane is
+// a contiguous range of sweep positions.
+//
+// SWEEP_LANES lanes per cell, lane L = component L of DeltaQ (0..4 mean flow, 5..6 k and
+// omega, the rest idle), so that the few FP64 operations left on the critical path (the
+// products with the neighbours' DeltaQ and one division) spread over many SM sub-partitions.
 // ---------------------------------------------------------------------------------------
-template <typename R>
-__device__ inline void sweep_nb(const DevBlock& b, int d, int nbc, R sgn, int turb, R* out5, R* out2) {
-    R roinv = R(slot(b, S_RINV)[nbc]);
-    R pVx = R(slot(b, S_SVEL)[nbc]), pVy = R(slot(b, S_SVEL + 1)[nbc]), pVz = R(slot(b, S_SVEL + 2)[nbc]);
-    R aSDx = R(slot(b, S_ASD + 3 * d)[nbc]), aSDy = R(slot(b, S_ASD + 3 * d + 1)[nbc]), aSDz = R(slot(b, S_ASD + 3 * d + 2)[nbc]);
-    R Din[5];
-    for (int L = 0; L < 5; ++L) Din[L] = R(slot(b, S_D + L)[nbc]);
-    R Dif[5];
-    lusgs_adq<R>(pVx, pVy, pVz, aSDx, aSDy, aSDz, R(slot(b, S_PP)[nbc]), roinv, Din[0], Din[1], Din[2], Din[3], Din[4], Dif);
-    R RDSt = R(slot(b, S_RDS + d)[nbc]);
-    for (int L = 0; L < 5; ++L) out5[L] = R(0.5) * (Dif[L] + sgn * (RDSt * Din[L]));
-    if (turb) {
-        R VP = pVx * aSDx + pVy * aSDy + pVz * aSDz;
-        for (int q = 0; q < 2; ++q) {
-            R Dq = R(slot(b, S_D + 5 + q)[nbc]);
-            out2[q] = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
-        }
-    }
-}
-
 template <typename R, bool LOWER>
-__global__ void k_sweep(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, int first, int count, int turb) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= count) return;
-    const SweepCell sc = cells[first + e];
-    const DevBlock b = blks[sc.blk];
-    const int I = sc.i, J = sc.j, K = sc.k;
-    const int c = cidx(b, I, J, K);
-    const int st[3] = {1, b.PI, b.PI * b.PJ};
-    const bool has[3] = {LOWER ? I != 1 : I != b.NI1, LOWER ? J != 1 : J != b.NJ1, LOWER ? K != 1 : K != b.NK1};
+__device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
+                                  int L, int turb) {
+    if (L >= 7 || (L >= 5 && !turb)) return;
+    const int side = LOWER ? 0 : 3;
+    const int jb = LOWER ? REC_JL : REC_JU, rb = LOWER ? REC_RDSL : REC_RDSU;
     const R sgn = LOWER ? R(1.0) : R(-1.0);
-    R acc5[3][5], acc2[3][2];
+    auto REC = [&](int m) { return rec[(size_t)m * N + q]; };
+    R acc[3];
     for (int d = 0; d < 3; ++d) {
-        for (int L = 0; L < 5; ++L) acc5[d][L] = R(0.0);
-        acc2[d][0] = acc2[d][1] = R(0.0);
-        if (has[d]) sweep_nb<R>(b, d, LOWER ? c - st[d] : c + st[d], sgn, turb, acc5[d], acc2[d]);
-    }
-    R stept = R(slot(b, S_STEPT)[c]), cvs = R(slot(b, S_CVS)[c]), fm = R(slot(b, S_FM)[c]);
-    for (int L = 0; L < 5; ++L) {
-        double* D = slot(b, S_D + L);
-        R sum = acc5[0][L] + acc5[1][L] + acc5[2][L];
-        if (LOWER) D[c] = (double)((R(D[c]) * stept + sum * cvs) / fm);
-        else D[c] = (double)(R(D[c]) - sum * cvs / fm);
-    }
-    if (turb) {
-        R ft = R(slot(b, S_FT)[c]);
-        for (int q = 0; q < 2; ++q) {
-            double* D = slot(b, S_D + 5 + q);
-            R sum = acc2[0][q] + acc2[1][q] + acc2[2][q];
-            if (LOWER) D[c] = (double)((R(D[c]) * stept + sum * cvs) / ft);
-            else D[c] = (double)(R(D[c]) - sum * cvs / ft);
+        acc[d] = R(0.0);
+        const long long np = nbp[(size_t)(side + d) * N + q];
+        if (np < 0) continue;
+        const int jd = jb + NJAC * d;
+        const R RDSt = REC(rb + d);
+        // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1 line)
+        if (L < 5) {
+            R AinRo = __ldcg(dq + np), AinRx = __ldcg(dq + N + np), AinRy = __ldcg(dq + 2 * N + np);
+            R AinRz = __ldcg(dq + 3 * N + np), AinRe = __ldcg(dq + 4 * N + np);
+            R Dif;
+            if (L == 0) {
+                const R aSDt = R(0.0);
+                Dif = AinRo * aSDt + AinRx * REC(jd + JC_R0) + AinRy * REC(jd + JC_R0 + 1) + AinRz * REC(jd + JC_R0 + 2)
+                      + AinRe * R(0.0);
+            } else if (L < 4) {
+                const int r = jd + JC_R1 + 5 * (L - 1);
+                Dif = AinRo * REC(r) + AinRx * REC(r + 1) + AinRy * REC(r + 2) + AinRz * REC(r + 3) + AinRe * REC(r + 4);
+            } else {
+                const int r = jd + JC_R4;
+                Dif = AinRo * REC(jd + JC_VP) * REC(jd + JC_GET1) + AinRx * REC(r) + AinRy * REC(r + 1) + AinRz * REC(r + 2)
+                      + AinRe * REC(r + 3);
+            }
+            const R Din = L == 0 ? AinRo : L == 1 ? AinRx : L == 2 ? AinRy : L == 3 ? AinRz : AinRe;
+            acc[d] = R(0.5) * (Dif + sgn * (RDSt * Din));
+        } else {
+            const R VP = REC(jd + JC_VPT);
+            const R Dq = __ldcg(dq + (size_t)L * N + np);
+            acc[d] = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
         }
     }
+    const R stept = REC(REC_STEPT), cvs = REC(REC_CVS);
+    const R den = L < 5 ? REC(REC_FM) : REC(REC_FT);
+    R* D = dq + (size_t)L * N + q;
+    const R own = __ldcg(D);
+    const R sum = acc[0] + acc[1] + acc[2];
+    if (LOWER) *D = (own * stept + sum * cvs) / den;
+    else *D = own - sum * cvs / den;
+}
+
+// one hyperplane [first, first+count) per launch
+template <typename R, bool LOWER>
+__global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int first, int count, int turb) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = g / SWEEP_LANES, L = g % SWEEP_LANES;
+    if (e >= count) return;
+    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, turb);
+}
+
+// Grid-wide barrier of a co-resident (cooperative) grid.  The wait is bounded: after `limit`
+// polls the barrier records an error and every block leaves the kernel at its next check.
+__device__ inline bool grid_barrier(SweepSync* sy, unsigned nblocks, unsigned limit) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = &sy->gen;
+        const unsigned g0 = *vgen;
+        __threadfence();
+        if (atomicAdd(&sy->count, 1u) == nblocks - 1) {
+            atomicExch(&sy->count, 0u);
+            __threadfence();
+            atomicAdd(&sy->gen, 1u);
+        } else {
+            unsigned it = 0;
+            while (*vgen == g0) {
+                if (++it > limit) { atomicExch(&sy->err, 1); break; }
+            }
+        }
+        __threadfence();
+        ok = *((volatile int*)&sy->err) == 0;      // one answer for the whole block
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Both sweeps over all hyperplanes in one cooperative launch: the items of hyperplane h are
+// spread over the whole grid, then a grid barrier; U runs the hyperplanes in reverse.
+template <typename R>
+__global__ void k_sweep_all(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N,
+                            const int* __restrict__ plane_off, int nplanes, int turb, SweepSync* sy, unsigned limit) {
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int h = 0; h < nplanes; ++h) {
+        const int first = plane_off[h], items = (plane_off[h + 1] - first) * SWEEP_LANES;
+        for (int g = tid; g < items; g += stride)
+            sweep_item<R, true>(nbp, rec, dq, N, (long long)first + g / SWEEP_LANES, g % SWEEP_LANES, turb);
+        if (!grid_barrier(sy, gridDim.x, limit)) return;
+    }
+    for (int h = nplanes - 1; h >= 0; --h) {
+        const int first = plane_off[h], items = (plane_off[h + 1] - first) * SWEEP_LANES;
+        for (int g = tid; g < items; g += stride)
+            sweep_item<R, false>(nbp, rec, dq, N, (long long)first + g / SWEEP_LANES, g % SWEEP_LANES, turb);
+        if (h > 0 && !grid_barrier(sy, gridDim.x, limit)) return;
+    }
+}
+
+// DeltaQ back to the cells (the update and trans_get_field read it there)
+template <typename R>
+__global__ void k_sweep_scatter(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, const R* __restrict__ dq,
+                                long long N) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    const SweepCell sc = cells[q];
+    const DevBlock b = blks[sc.blk];
+    const int c = cidx(b, sc.i, sc.j, sc.k);
+    for (int L = 0; L < 7; ++L) rs<R>(b, S_D + L)[c] = dq[(size_t)L * N + q];
 }
 
 #ifdef TG_COMMON_KERNELS
@@ -894,7 +998,7 @@ __global__ void k_sweep(const DevBlock* __restrict__ blks, const SweepCell* __re
 // Time/TIME_Update_V.F90:106-294 (norms) and :502-859 (update), FP64 in both paths
 // ---------------------------------------------------------------------------------------
 __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, int turb_upd,
-                         NormPart* __restrict__ parts) {
+                         NormPart* __restrict__ parts, int d_fp32) {
     const Tile t = tiles[blockIdx.x];
     const DevBlock b = blks[t.blk];
     __shared__ double s_sum[3][256];
@@ -914,15 +1018,17 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
         double* PP = slot(b, S_PP);
         double* T = slot(b, S_T);
         double v1 = V[0][c];
-        double d1 = slot(b, S_D)[c], d6 = slot(b, S_D + 5)[c], d7 = slot(b, S_D + 6)[c];
+        // DeltaQ from the sweeps: FP64, or FP32 in the mixed path
+        auto Dq = [&](int L) { return d_fp32 ? (double)fslot(b, S_D + L)[c] : slot(b, S_D + L)[c]; };
+        double d1 = Dq(0), d6 = Dq(5), d7 = Dq(6);
         double DR = fabs(d1 / v1);
         nanf = isnan(d1) ? 1 : 0;
         sa = DR * DR; ma = DR; ia = n;
         double DRk = fabs(d6 / v1), DRo = fabs(d7 / v1);
         sk = DRk * DRk; mk = DRk; so = DRo * DRo; mo = DRo;
         // mean flow (non-preconditioned, TIME_Update_V.F90:621-689)
-        double AinRo = d1, AinRx = slot(b, S_D + 1)[c], AinRy = slot(b, S_D + 2)[c], AinRz = slot(b, S_D + 3)[c];
-        double AinRe = slot(b, S_D + 4)[c];
+        double AinRo = d1, AinRx = Dq(1), AinRy = Dq(2), AinRz = Dq(3);
+        double AinRe = Dq(4);
         double pRo = v1;
         double roinv = 1.0 / pRo;
         double pVx = V[1][c] * roinv, pVy = V[2][c] * roinv, pVz = V[3][c] * roinv;

@@ -20,10 +20,24 @@ struct OutletLine {       // one line of an outlet segment along j (BC/BC_Outlet
 
 struct SweepCell { int blk, i, j, k; };
 
+// the sweep-order arrays of one context (element type R = the sweep arithmetic)
+struct SweepView {
+    const SweepCell* cells;     // cell of each sweep position
+    const int* nbp;             // 6 x n: positions of the lower (0..2) and upper (3..5) neighbours, -1 = none
+    void* rec;                  // NREC x n records
+    void* dq;                   // 7 x n DeltaQ
+    long long n;
+};
+
 struct NormPart {         // per-tile partial residual norms (Time/TIME_Update_V.F90:106-294)
     double sa, ma, sk, mk, so, mo;
     long long ia;                   // lexicographic index of the max of |D1/V1|
     int nan, pad_;
+};
+
+struct SweepSync {        // grid barrier state of the persistent sweep kernel
+    unsigned count, gen;
+    int err, pad_;
 };
 
 }  // namespace tg

@@ -1,0 +1,147 @@
+"""Integrated quantities of a solution, for the precision error table and for retirement
+decisions: mass flow through every inlet and outlet, mass-averaged total pressure and the
+total-pressure loss coefficient, blade loading (pressure coefficient on the blade wall),
+pressure force on the walls, and field L-inf differences.
+
+Semantics follow the reference's output routines, generalised to every inlet/outlet face:
+  mass flow       Output/OUTPUT_Residual_NS.F90:37-75 (face momentum from the two cells'
+                  volume-weighted average, dotted with SD of the face; nondimensional units)
+  pressure coeff. Output/OUTPUT_Surfaces.F90:303-305 (Cp = 2 (p - PPF) at the wall cell)
+  total pressure  Output/Average_Field.F90:112,210 (p (1 + 0.2 M^2)^3.5, mass averaged)
+Inputs are the full-extent (-2..N+2) arrays of trans_gb300.solver / oracle get_field.
+"""
+import numpy as np
+
+from .case import G, face_cells
+
+GAM = 1.4
+
+
+def _face_pairs(cn):
+    """Interior cell and ghost cell (Fortran indices) on both sides of each face of a
+    boundary connection, and the face index at which SD of the face is stored."""
+    I, J, K = face_cells(cn)
+    d = cn.IJKDirect - 1
+    n = [I.copy(), J.copy(), K.copy()]
+    inner = [I.copy(), J.copy(), K.copy()]
+    ghost = [I.copy(), J.copy(), K.copy()]
+    face = [I.copy(), J.copy(), K.copy()]
+    if cn.pointStart[d] == 1:            # min face: face 1 between ghost 0 and cell 1
+        ghost[d] = n[d] - 1
+        face[d] = n[d]
+    else:                                 # max face N: between cell N-1 and ghost N
+        inner[d] = n[d] - 1
+        face[d] = n[d]
+    return d, tuple(inner), tuple(ghost), tuple(face), cn.pointStart[d] == 1
+
+
+def _at(a, ijk, comp=()):
+    i, j, k = ijk
+    comp = comp if isinstance(comp, tuple) else (comp,)
+    return a[comp + (i + G, j + G, k + G)]
+
+
+def boundary_flux(case, conns, geo, fields, kind):
+    """Mass flow and mass-averaged total pressure and static pressure through every face of
+    the given BC kind.  Returns (mass, p0_mass_avg, p_mass_avg); mass > 0 into the domain for
+    inflow faces (kind 5) and out of it for outflow faces (kind 7)."""
+    m_tot, p0m, pm = 0.0, 0.0, 0.0
+    for ib, b in enumerate(case.blocks):
+        g = geo[b.id]
+        V, PP = fields[ib]["V"], fields[ib]["PP"]
+        vol = g["VOL"]
+        for cn in conns[b.id]:
+            if cn.BCType != kind:
+                continue
+            d, ci, cg, cf, is_min = _face_pairs(cn)
+            w1 = _at(vol, cg)             # weights crossed as in the reference
+            w2 = _at(vol, ci)
+            wsum = w1 + w2
+            ru = [(w1 * _at(V, ci, q) + w2 * _at(V, cg, q)) / wsum for q in (1, 2, 3)]
+            rho = (w1 * _at(V, ci, 0) + w2 * _at(V, cg, 0)) / wsum
+            p = (w1 * _at(PP, ci) + w2 * _at(PP, cg)) / wsum
+            S = [_at(g["SD"], cf, (d, q)) for q in range(3)]
+            flux = ru[0] * S[0] + ru[1] * S[1] + ru[2] * S[2]      # along +IJKDirect
+            into = (kind == 5) == is_min      # inflow through a min face, outflow through a max face
+            mf = flux if into else -flux
+            u2 = (ru[0] ** 2 + ru[1] ** 2 + ru[2] ** 2) / (rho * rho)
+            M2 = u2 / (GAM * p / rho)
+            p0 = p * (1.0 + 0.5 * (GAM - 1.0) * M2) ** (GAM / (GAM - 1.0))
+            m_tot += float(np.sum(mf))
+            p0m += float(np.sum(mf * p0))
+            pm += float(np.sum(mf * p))
+    if m_tot == 0.0:
+        return 0.0, 0.0, 0.0
+    return m_tot, p0m / m_tot, pm / m_tot
+
+
+def loss_coefficient(case, conns, geo, fields):
+    """Total-pressure loss (P0in - P0out) / (P0in - pin), mass averaged over inlet/outlet."""
+    _, p0i, pi = boundary_flux(case, conns, geo, fields, 5)
+    _, p0o, _ = boundary_flux(case, conns, geo, fields, 7)
+    return (p0i - p0o) / (p0i - pi)
+
+
+def wall_cp(case, conns, geo, fields, block_index=0, surf_dir=2, k_index=None):
+    """Pressure coefficient 2 (p - PPF) on the wall cells of the j-min face of one block
+    (the blade of the cascade O-block) at span station k_index (default mid-span)."""
+    b = case.blocks[block_index]
+    ni, nj, nk = b.dims
+    k = (nk - 1) // 2 + 1 if k_index is None else k_index
+    PP = fields[block_index]["PP"]
+    p = PP[G + 1:G + ni, G + 1, G + k]
+    return 2.0 * (p - case.params.PPF)
+
+
+def wall_force(case, conns, geo, fields):
+    """Pressure force sum(p_wall * S) over every wall face (kind 1), nondimensional."""
+    F = np.zeros(3)
+    for ib, b in enumerate(case.blocks):
+        g = geo[b.id]
+        PP = fields[ib]["PP"]
+        for cn in conns[b.id]:
+            if cn.BCType != 1:
+                continue
+            d, ci, cg, cf, is_min = _face_pairs(cn)
+            p = _at(PP, ci)
+            sgn = -1.0 if is_min else 1.0          # outward normal of the fluid domain
+            for q in range(3):
+                F[q] += float(np.sum(sgn * p * _at(g["SD"], cf, (d, q))))
+    return F
+
+
+def summary(case, conns, geo, fields):
+    m_in, p0i, pi = boundary_flux(case, conns, geo, fields, 5)
+    m_out, p0o, _ = boundary_flux(case, conns, geo, fields, 7)
+    out = {"mass_in": m_in, "mass_out": m_out, "p0_in": p0i, "p0_out": p0o,
+           "loss": (p0i - p0o) / (p0i - pi) if p0i != pi else 0.0,
+           "force": wall_force(case, conns, geo, fields).tolist(),
+           "cp_blade": wall_cp(case, conns, geo, fields).tolist()}
+    return out
+
+
+def error_table(case, conns, geo, fa, fb):
+    """Relative differences of solution a from reference solution b (e.g. mixed vs FP64)."""
+    sa, sb = summary(case, conns, geo, fa), summary(case, conns, geo, fb)
+
+    def rel(x, y):
+        return abs(x - y) / max(abs(y), 1e-300)
+    cpa, cpb = np.array(sa["cp_blade"]), np.array(sb["cp_blade"])
+    fa3, fb3 = np.array(sa["force"]), np.array(sb["force"])
+    linf = 0.0
+    for ib, b in enumerate(case.blocks):
+        ni, nj, nk = b.dims
+        sl = (slice(None), slice(G + 1, G + ni), slice(G + 1, G + nj), slice(G + 1, G + nk))
+        A, B = fa[ib]["V"][sl], fb[ib]["V"][sl]
+        for q in range(5):
+            linf = max(linf, float(np.max(np.abs(A[q] - B[q])) / np.max(np.abs(B[q]))))
+    return {
+        "mass_in": rel(sa["mass_in"], sb["mass_in"]),
+        "mass_out": rel(sa["mass_out"], sb["mass_out"]),
+        "p0_loss": rel(sa["loss"], sb["loss"]) if sb["loss"] != 0 else abs(sa["loss"]),
+        "p0_loss_abs": abs(sa["loss"] - sb["loss"]),
+        "blade_loading": float(np.max(np.abs(cpa - cpb)) / np.max(np.abs(cpb))),
+        "force": float(np.linalg.norm(fa3 - fb3) / max(np.linalg.norm(fb3), 1e-300)),
+        "field_linf": linf,
+        "values_ref": {k: sb[k] for k in ("mass_in", "mass_out", "loss", "force")},
+    }
