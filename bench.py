@@ -115,6 +115,40 @@ def time_resident(s, ki0, steps):
     return ms.value
 
 
+# Algorithmic words (FP64 = 8 B) per unit of each kernel class: the compulsory reads and
+# writes of one unit (interior cell, or face for the face fluxes) with halos excluded.
+ALG_WORDS = {
+    "k_face_flux": 51,      # per face: stencil 38 words in, 13 face fluxes out
+    "k_sweep": 24,          # the L -> U hand-off: DeltaQ 7 + Rds 3 + diagonals 2, written and read once
+    "k_update": 37, "k_gradient": 46, "k_specrad": 24, "k_lusgs_prep": 60, "k_gather": 46,
+}
+# FP64 thread-instructions per face of k_face_flux<double> (MDCD + AUSMPW+ + SST), counted by
+# ncu (DADD + DMUL + DFMA over the three directions) on the 339,968-cell cascade, and DRAM
+# bytes per face from the same capture (profiles/k_face_flux_fp64_cascade_339968cells.md)
+FACE_FP64_INST = 2541.0
+FACE_DRAM_BYTES = 391.3
+
+
+def units(c, kernel):
+    """Units a kernel class processes per iteration: faces of all three directions for the
+    face fluxes, interior cells otherwise."""
+    if kernel == "k_face_flux":
+        return sum(ni * (nj - 1) * (nk - 1) + (ni - 1) * nj * (nk - 1) + (ni - 1) * (nj - 1) * nk
+                   for ni, nj, nk in (b.dims for b in c.blocks))
+    return interior_cells(c)
+
+
+def kernel_times(s, ki):
+    """One iteration with CUDA events around every launch: {kernel: (ms, launches)}."""
+    lib = s.lib
+    ms = (C.c_double * abi.TRANS_NKCLASS)()
+    nl = (C.c_int * abi.TRANS_NKCLASS)()
+    rc = lib.trans_kernel_times(s.ctx, ki, ms, nl, abi.TRANS_NKCLASS)
+    if rc != 0:
+        raise RuntimeError(f"trans_kernel_times failed {rc}")
+    return {lib.trans_kernel_class(k).decode(): (ms[k], nl[k]) for k in range(abi.TRANS_NKCLASS) if nl[k] > 0}
+
+
 def pinned_copy(arr):
     """A page-locked host copy of a Fortran array (the caller's buffers in the end-to-end leg)."""
     import torch
@@ -255,19 +289,35 @@ def main():
     e2e_steps = max(2, min(args.steps, 10))
     dt, h2d, d2h = run_e2e(s, c, st, ki, e2e_steps)
     e2e = ncell * e2e_steps / dt / 1e6 * world
-    # roofline of the dominant stage
+    # roofline of the dominant kernel, from per-launch CUDA events of one more iteration
+    kt = kernel_times(s, ki)
+    ki += 1
     pk = peaks()
     hbm = pk.get("hbm_gbs", FALLBACK_HBM)
     fp64 = lib.trans_probe_fma_gflops(1)
     fp32 = lib.trans_probe_fma_gflops(0)
     st_ms = {n: stage_ms[i] for i, n in enumerate(abi.STAGES)}
-    dom = max(st_ms, key=st_ms.get)
-    # algorithmic bytes per interior cell of each stage (FP64 words x 8)
-    words = {"SPECRAD": 10 + 9 + 1 + 4, "BC_STATE": 0, "GRADIENT": 7 + 2 + 9 + 3 + 1 + 18 + 1 + 5,
-             "BC_GRAD": 0, "RESIDUAL": 10 + 18 + 1 + 9 + 3 + 3 + 1 + 7,
-             "LUSGS": 7 + 14 + 7 + 3 + 1 + 1 + 9 + 24, "UPDATE": 10 + 7 + 9 + 1 + 10, "UPDATE_U": 21}
-    alg_bytes = words[dom] * 8.0 * ncell
-    achieved = alg_bytes / (st_ms[dom] * 1e-3) / 1e9
+    dom = max(kt, key=lambda k: kt[k][0])
+    dom_ms, dom_n = kt[dom]
+    per_launch_ms = dom_ms / dom_n
+    nunit = units(c, dom)
+    alg_bytes = ALG_WORDS.get(dom, 0) * 8.0 * nunit / dom_n
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "kernel": dom, "launches_per_step": dom_n, "ms_per_launch": per_launch_ms,
+            "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
+            "fp64_pipe_gflops_peak_measured": fp64, "fp32_pipe_gflops_peak_measured": fp32}
+    if dom == "k_face_flux" and args.precision == "fp64":
+        # the binding roof of the FP64 residual is the FP64 pipe: thread-instructions per second
+        # against the probe's FMA rate (one FMA = one FP64 thread-instruction)
+        inst = FACE_FP64_INST * nunit / dom_n / (per_launch_ms * 1e-3)
+        roof["binding"] = "fp64_pipe"
+        roof["fp64_inst_per_s"] = inst
+        roof["fp64_pipe_frac"] = inst / (fp64 * 1e9 / 2.0)
+        roof["traffic"] = FACE_DRAM_BYTES * nunit / dom_n
+        roof["traffic_source"] = "ncu dram__bytes_read+write per face on the 339,968-cell cascade, scaled by faces"
+    elif dom == "k_sweep":
+        roof["binding"] = "latency (one dependent step per i+j+k hyperplane)"
     line = {
         "metric": "Mcell-iter/s", "value": value, "unit": "Mcell-iter/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -280,11 +330,9 @@ def main():
         "e2e": {"value": e2e, "unit": "Mcell-iter/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "clocks": clocks,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": dom,
-                     "fp64_pipe_gflops_peak_measured": fp64, "fp32_pipe_gflops_peak_measured": fp32,
-                     "peak_source": "measured" if "hbm_gbs" in pk else "fallback"},
+        "roofline": roof,
         "stage_ms": st_ms,
+        "kernel_ms": {k: round(v[0], 4) for k, v in sorted(kt.items(), key=lambda x: -x[1][0])},
     }
     if rank == 0 and not args.no_cpu:
         v, n, dt2 = cpu_sample(c, conns, geo, st)

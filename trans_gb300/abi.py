@@ -133,6 +133,9 @@ def bind_common(lib):
     lib.trans_probe_fma_gflops.restype = C.c_double
     lib.trans_time_iterations.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(TransNorms)]
     lib.trans_update_static_scratch.argtypes = [vp, C.c_int, C.POINTER(TransNorms)]
+    lib.trans_kernel_times.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int]
+    lib.trans_kernel_class.argtypes = [C.c_int]
+    lib.trans_kernel_class.restype = C.c_char_p
     lib.trans_tuning.argtypes = [vp]
     lib.trans_tuning.restype = C.c_char_p
     lib.trans_last_error.argtypes = [vp]
@@ -143,4 +146,6 @@ def bind_common(lib):
 EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field", "trans_iterate",
             "trans_run_stage", "trans_get_norms", "trans_sync", "trans_device_bytes",
             "trans_kernel_launches", "trans_last_error", "trans_stage_times", "trans_probe_fma_gflops",
-            "trans_time_iterations", "trans_update_static_scratch", "trans_tuning"]
+            "trans_time_iterations", "trans_update_static_scratch", "trans_tuning", "trans_kernel_times",
+            "trans_kernel_class"]
+TRANS_NKCLASS = 16

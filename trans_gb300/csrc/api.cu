@@ -74,7 +74,29 @@ struct Ctx {
     SweepSync* d_sync = nullptr;
     SweepSync* h_sync = nullptr;         // pinned
     std::string sweep_tuning;            // what the schedule tuner measured
+    // per-kernel timing (trans_kernel_times): events around each launch while enabled
+    bool ktime_on = false;
+    struct KEv { int k, n; cudaEvent_t a, b; };
+    std::vector<KEv> kev;
     size_t stage_doubles = 0;
+};
+
+// kernel classes of trans_kernel_times
+enum KClass { K_SPECRAD, K_BC_STATE, K_BC_OUTLET, K_PRIMS, K_MIRROR, K_GRADIENT, K_SHOCK_GHOST, K_BC_GRAD,
+              K_FACE, K_GATHER, K_SST_FC1, K_PREP, K_SWEEP, K_SCATTER, K_UPDATE, K_UPDATE_U, NKCLASS };
+const char* const kclass_name[NKCLASS] = {"k_specrad", "k_bc_state", "k_bc_outlet", "k_prims", "k_mirror", "k_gradient",
+    "k_shock_ghost", "k_bc_grad", "k_face_flux", "k_gather", "k_sst_fc1", "k_lusgs_prep", "k_sweep", "k_sweep_scatter",
+    "k_update", "k_update_u"};
+
+// times the launches issued in its lifetime as kernel class k (n launches) when enabled
+struct KScope {
+    Ctx* c; int k, n; cudaEvent_t a = nullptr, b = nullptr;
+    KScope(Ctx* c_, int k_, int n_ = 1) : c(c_), k(k_), n(n_) {
+        if (c->ktime_on && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess) cudaEventRecord(a, c->stream);
+    }
+    ~KScope() {
+        if (c->ktime_on && a && b) { cudaEventRecord(b, c->stream); c->kev.push_back({k, n, a, b}); }
+    }
 };
 
 int fail(Ctx* c, int code, const std::string& msg) {
@@ -364,7 +386,7 @@ int sweep_once(Ctx* c, int turb, int mode, int grid, int block) {
 
 // keep a copy of the sweep-order DeltaQ (restore = copy it back)
 int save_dq(Ctx* c, bool restore) {
-    size_t bytes = (size_t)7 * (size_t)c->sv.n * c->fl->elem;
+    size_t bytes = (size_t)DQ_STRIDE * (size_t)((c->sv.n + 31) / 32 * 32) * c->fl->elem;
     if (!c->d_dq_save) CK(cudaMalloc(&c->d_dq_save, bytes));
     CK(cudaMemcpyAsync(restore ? c->sv.dq : c->d_dq_save, restore ? c->d_dq_save : c->sv.dq, bytes, cudaMemcpyDeviceToDevice,
                        c->stream));
@@ -438,48 +460,57 @@ int run_stage(Ctx* c, int stage, int itr) {
         case TRANS_STAGE_SPECRAD: {
             double CFL_sub = p.CFL_Sub_start + (p.CFL_Sub_end - p.CFL_Sub_start) * (double)(c->KI - p.KI_ini) / (double)p.CFL_Sub_step;
             CFL_sub = std::min(CFL_sub, p.CFL_Sub_end);
-            launch_specrad(s, c->d_blk, c->d_cell, nct, c->dp, CFL_sub);
+            { KScope t(c, K_SPECRAD); launch_specrad(s, c->d_blk, c->d_cell, nct, c->dp, CFL_sub); }
             c->launches++;
             break;
         }
         case TRANS_STAGE_BC_STATE:
-            launch_bc_state(s, c->d_blk, c->d_bc, (int)c->bc.size(), c->dp, turb);
-            launch_bc_outlet(s, c->d_blk, c->d_outlet, c->d_lines, (int)c->lines.size(), c->dp, turb);
+            { KScope t(c, K_BC_STATE); launch_bc_state(s, c->d_blk, c->d_bc, (int)c->bc.size(), c->dp, turb); }
+            { KScope t(c, K_BC_OUTLET); launch_bc_outlet(s, c->d_blk, c->d_outlet, c->d_lines, (int)c->lines.size(), c->dp, turb); }
             c->launches += 1 + (c->lines.empty() ? 0 : 1);
             break;
         case TRANS_STAGE_GRADIENT:
-            launch_prims(s, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off);
-            launch_gradient(s, c->d_blk, c->d_cell, nct, turb);
-            launch_shock_ghost(s, c->d_blk, c->d_ghost, (int)c->ghost_tiles.size());
+            { KScope t(c, K_PRIMS); launch_prims(s, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off); }
+            // the FP32 kernels read FP32 copies of this sub-iteration's state, primitives and radii
+            if (c->mixed) { KScope t(c, K_MIRROR); mirror(c, {{S_V, 10}, {S_RDS, 4}, {S_PRIM, 5}, {S_RINV, 4}}); }
+            { KScope t(c, K_GRADIENT); c->fl->gradient(s, c->d_blk, c->d_cell, nct, turb); }
+            { KScope t(c, K_SHOCK_GHOST); c->fl->shock_ghost(s, c->d_blk, c->d_ghost, (int)c->ghost_tiles.size()); }
             c->launches += 3;
             break;
         case TRANS_STAGE_BC_GRAD:
-            launch_bc_grad(s, c->d_blk, c->d_bc, (int)c->bc.size(), turb);
+            { KScope t(c, K_BC_GRAD); c->fl->bc_grad(s, c->d_blk, c->d_bc, (int)c->bc.size(), turb); }
             c->launches++;
             break;
         case TRANS_STAGE_RESIDUAL:
-            // the FP32 kernels read FP32 copies of this sub-iteration's state, gradients and radii
-            if (c->mixed) mirror(c, {{S_V, 10}, {S_RDS, 4}, {S_DQ, 19}, {S_PRIM, 5}, {S_RINV, 4}});
-            for (int d = 0; d < 3; ++d) c->fl->face_flux[d](s, c->d_blk, c->d_face[d], (int)c->face_tiles[d].size(), c->dp, turb);
-            c->fl->gather(s, c->d_blk, c->d_cell, nct, turb);
+            for (int d = 0; d < 3; ++d) {
+                KScope t(c, K_FACE);
+                c->fl->face_flux[d](s, c->d_blk, c->d_face[d], (int)c->face_tiles[d].size(), c->dp, turb);
+            }
+            { KScope t(c, K_GATHER); c->fl->gather(s, c->d_blk, c->d_cell, nct, turb); }
             c->launches += 4;
             break;
         case TRANS_STAGE_LUSGS: {
             if (turb && p.Kind_Hybrid == 3) {
+                KScope t(c, K_SST_FC1);
                 c->fl->sst_fc1(s, c->d_blk, c->d_cell, nct, c->dp);
                 c->launches++;
             }
-            c->fl->prep(s, c->d_blk, c->sv, c->dp, turb);
+            { KScope t(c, K_PREP); c->fl->prep(s, c->d_blk, c->sv, c->dp, turb); }
             c->launches++;
-            rc = run_sweeps(c, turb);
+            {
+                int nh = (int)c->plane_off.size() - 1, nl = 0;
+                for (int h = 0; h < nh; ++h) nl += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
+                KScope t(c, K_SWEEP, c->sweep_mode == 1 ? 1 : nl);
+                rc = run_sweeps(c, turb);
+            }
             if (rc) return rc;
-            c->fl->scatter(s, c->d_blk, c->sv);
+            { KScope t(c, K_SCATTER); c->fl->scatter(s, c->d_blk, c->sv); }
             c->launches++;
             break;
         }
         case TRANS_STAGE_UPDATE: {
             int turb_upd = (p.IF_Euler == 0 && turb == 1 && c->KI >= p.KItm) ? 1 : 0;
-            launch_update(s, c->d_blk, c->d_cell, nct, c->dp, turb_upd, c->d_parts, c->mixed ? 1 : 0);
+            { KScope t(c, K_UPDATE); launch_update(s, c->d_blk, c->d_cell, nct, c->dp, turb_upd, c->d_parts, c->mixed ? 1 : 0); }
             c->launches++;
             CK(cudaMemcpyAsync(c->h_parts.data(), c->d_parts, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
@@ -490,6 +521,7 @@ int run_stage(Ctx* c, int stage, int itr) {
         }
         case TRANS_STAGE_UPDATE_U:
             if (p.Kind_Dual != 0) {
+                KScope t(c, K_UPDATE_U);
                 launch_update_u(s, c->d_blk, c->d_cell, nct, p.Kind_Dual);
                 c->launches++;
             }
@@ -621,7 +653,8 @@ int trans_create(const trans_params* p, int nblocks, const trans_block* blocks, 
             const DevBlock& b = c->blk[sc.blk];
             pos[sc.blk][(size_t)(sc.i - 1) + (size_t)b.NI1 * ((sc.j - 1) + (size_t)b.NJ1 * (sc.k - 1))] = (int)q;
         }
-        std::vector<int> nbp((size_t)6 * N, -1);
+        const long long Np = (N + 31) / 32 * 32;           // whole tiles of 32 positions
+        std::vector<int> nbp((size_t)6 * Np, -1);
         for (long long q = 0; q < N; ++q) {
             const SweepCell& sc = c->sweep[q];
             const DevBlock& b = c->blk[sc.blk];
@@ -631,13 +664,13 @@ int trans_create(const trans_params* p, int nblocks, const trans_block* blocks, 
                     int x[3] = {ijk[0], ijk[1], ijk[2]};
                     x[d] += side == 0 ? -1 : 1;
                     if (x[d] < 1 || x[d] > hi[d]) continue;
-                    nbp[(size_t)(3 * side + d) * N + q] =
+                    nbp[sw_at(q, 3 * side + d, 6)] =
                         pos[sc.blk][(size_t)(x[0] - 1) + (size_t)b.NI1 * ((x[1] - 1) + (size_t)b.NJ1 * (x[2] - 1))];
                 }
         }
         if ((rc = upload_vec(c, nbp.data(), sizeof(int) * nbp.size(), (void**)&c->d_nbp))) { trans_destroy(c); return rc; }
-        if (cudaMalloc(&c->d_rec, (size_t)NREC * N * c->fl->elem) != cudaSuccess ||
-            cudaMalloc(&c->d_dqs, (size_t)7 * N * c->fl->elem) != cudaSuccess) { trans_destroy(c); return TRANS_E_MEMORY; }
+        if (cudaMalloc(&c->d_rec, (size_t)NREC * Np * c->fl->elem) != cudaSuccess ||
+            cudaMalloc(&c->d_dqs, (size_t)DQ_STRIDE * Np * c->fl->elem) != cudaSuccess) { trans_destroy(c); return TRANS_E_MEMORY; }
         c->sv.cells = c->d_sweep; c->sv.nbp = c->d_nbp; c->sv.rec = c->d_rec; c->sv.dq = c->d_dqs; c->sv.n = N;
     }
     if (cudaMalloc(&c->d_sync, sizeof(SweepSync)) != cudaSuccess || cudaMallocHost(&c->h_sync, sizeof(SweepSync)) != cudaSuccess) {
@@ -736,8 +769,13 @@ static int field_io(Ctx* c, int ib, int f, double* host, bool upload) {
         }
         if (is_geometry(f)) c->geom_dirty = true;
         if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}});
+        if (c->mixed && f == TRANS_DQDXYZ) mirror(c, {{S_DQ, 18}});
+        if (c->mixed && f == TRANS_SHOCK) mirror(c, {{S_SHOCK, 1}});
     } else {
-        if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}}, 1);      // DeltaQ lives in FP32 there
+        // the mixed path keeps DeltaQ, the gradients and the shock sensor in FP32
+        if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}}, 1);
+        if (c->mixed && f == TRANS_DQDXYZ) mirror(c, {{S_DQ, 18}}, 1);
+        if (c->mixed && f == TRANS_SHOCK) mirror(c, {{S_SHOCK, 1}}, 1);
         launch_field_xfer(s, b, fm.slot, fm.ncomp, fm.lb, is_sd, c->d_stage, 0);
         c->launches++;
         CK(cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, s));
@@ -839,7 +877,7 @@ long long trans_device_bytes(void* ctx) {
     if (!c) return 0;
     long long b = (long long)(c->arena_doubles * sizeof(double));
     if (c->farena) b += (long long)(c->arena_doubles * sizeof(float));
-    b += (long long)c->sv.n * ((long long)(NREC + 7) * (long long)c->fl->elem + 6LL * (long long)sizeof(int));
+    b += (c->sv.n + 31) / 32 * 32 * ((long long)(NREC + DQ_STRIDE) * (long long)c->fl->elem + 6LL * (long long)sizeof(int));
     return b;
 }
 
@@ -911,6 +949,32 @@ int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms) {
     if (norms) std::copy(c->norms.begin(), c->norms.end(), norms);
     return rc;
 }
+
+int trans_kernel_times(void* ctx, int ki, double* ms, int* launches, int n) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !ms || !launches || n < NKCLASS) return TRANS_E_ARG;
+    for (int k = 0; k < n; ++k) { ms[k] = 0.0; launches[k] = 0; }
+    if (c->sweep_mode < 0) {                   // tune outside the timed iteration
+        int rc = trans_iterate(ctx, ki, nullptr);
+        if (rc) return rc;
+        ++ki;
+    }
+    c->ktime_on = true;
+    c->kev.clear();
+    int rc = trans_iterate(ctx, ki, nullptr);
+    c->ktime_on = false;
+    cudaStreamSynchronize(c->stream);
+    for (auto& e : c->kev) {
+        float t = 0;
+        if (cudaEventElapsedTime(&t, e.a, e.b) == cudaSuccess) { ms[e.k] += t; launches[e.k] += e.n; }
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    c->kev.clear();
+    return rc;
+}
+
+const char* trans_kernel_class(int k) { return (k >= 0 && k < NKCLASS) ? kclass_name[k] : ""; }
 
 const char* trans_tuning(void* ctx) {
     Ctx* c = static_cast<Ctx*>(ctx);

@@ -54,12 +54,19 @@ enum Slot {
 // (AinRo*VP)*GEt1 as two factors; VPT is the contravariant speed of the k-omega sweep.
 enum JacTerm { JC_R0 = 0, JC_R1 = 3, JC_R2 = 8, JC_R3 = 13, JC_VP = 18, JC_GET1 = 19, JC_R4 = 20, JC_VPT = 24, NJAC = 25 };
 
-// Per-cell record of the sweeps, stored in sweep (hyperplane) order so that the cells of one
-// hyperplane read consecutive addresses: the Jacobian terms and spectral radii of the three
-// lower (L sweep) and three upper (U sweep) neighbours, and the cell's own diagonal terms.
+// Per-cell record of the sweeps, in sweep (hyperplane) order: the Jacobian terms and spectral
+// radii of the three lower (L sweep) and three upper (U sweep) neighbours, and the cell's own
+// diagonal terms.
 enum SweepRec { REC_JL = 0, REC_JU = 3 * NJAC, REC_RDSL = 6 * NJAC, REC_RDSU = 6 * NJAC + 3,
                 REC_STEPT = 6 * NJAC + 6, REC_CVS = REC_STEPT + 1, REC_FM = REC_STEPT + 2, REC_FT = REC_STEPT + 3,
                 NREC = REC_STEPT + 4 };
+constexpr int DQ_STRIDE = 8;     // DeltaQ of one sweep position: 7 components + 1 pad
+// Sweep-order arrays are stored in tiles of 32 positions ("AoSoA"): element m of position q is
+// at (q/32)*32*width + m*32 + q%32, so that a warp writing element m of 32 consecutive
+// positions writes one contiguous 128-byte run, and one hyperplane stays one contiguous range.
+__host__ __device__ inline size_t sw_at(long long q, int m, int width) {
+    return (size_t)(q >> 5) * (size_t)(32 * width) + (size_t)m * 32 + (size_t)(q & 31);
+}
 
 // face-flux components (per face and direction)
 enum FX { FX_VX = 0, FX_VY = 1, FX_VZ = 2, FX_VE = 3, FX_TK = 4, FX_TO = 5,

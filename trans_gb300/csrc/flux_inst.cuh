@@ -5,6 +5,15 @@
 
 namespace tg {
 namespace {
+void grd(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, int turb) {
+    if (nt > 0) k_gradient<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, turb);
+}
+void shg(cudaStream_t s, const DevBlock* b, const Tile* t, int nt) {
+    if (nt > 0) k_shock_ghost<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t);
+}
+void bcg(cudaStream_t s, const DevBlock* b, const BCEntry* e, int n, int turb) {
+    if (n > 0) k_bc_grad<TG_R><<<(n + 127) / 128, 128, 0, s>>>(b, e, n, turb);
+}
 template <int DIR>
 void ff(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const Params& p, int turb) {
     if (nt > 0) k_face_flux<TG_R, DIR><<<nt, FACE_TILE, 0, s>>>(b, t, params_as<TG_R>(p), turb);
@@ -52,7 +61,7 @@ void scat(cudaStream_t s, const DevBlock* b, const SweepView& v) {
 }  // namespace
 
 const FluxLaunchers& TG_NAME() {
-    static const FluxLaunchers L = {{ff<1>, ff<2>, ff<3>}, ga, fc, prep, swl, swu, swa, swa_occ, scat, sizeof(TG_R)};
+    static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, prep, swl, swu, swa, swa_occ, scat, sizeof(TG_R)};
     return L;
 }
 }  // namespace tg

@@ -16,17 +16,8 @@ void launch_bc_outlet(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, 
                       const Params& p, int turb) {
     if (nl > 0) k_bc_outlet<<<(nl + 63) / 64, 64, 0, s>>>(blks, ent, lines, nl, p, turb);
 }
-void launch_bc_grad(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, int turb) {
-    if (n > 0) k_bc_grad<<<(n + 127) / 128, 128, 0, s>>>(blks, ent, n, turb);
-}
 void launch_prims(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off) {
     if (total > 0) k_prims<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off);
-}
-void launch_gradient(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int turb) {
-    if (nt > 0) k_gradient<<<nt, CELL_TILE, 0, s>>>(blks, tiles, turb);
-}
-void launch_shock_ghost(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt) {
-    if (nt > 0) k_shock_ghost<<<nt, CELL_TILE, 0, s>>>(blks, tiles);
 }
 void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts,
                    int d_fp32) {

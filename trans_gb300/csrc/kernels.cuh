@@ -320,43 +320,6 @@ __global__ void k_bc_outlet(const DevBlock* __restrict__ blks, const BCEntry* __
     }
 }
 
-// BC_Boundarys(0): gradients of the first ghost layer (BC/*.F90 sweep 0, BC/BC_P2P.F90:140-184)
-__global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n, int turb) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n) return;
-    const BCEntry E = ent[e];
-    const DevBlock b = blks[E.blk];
-    const int il = E.l[0], is = E.s[0];
-    if (E.kind != 9) {
-        for (int L = 0; L < 18; ++L) slot(b, S_DQ + L)[il] = slot(b, S_DQ + L)[is];
-        return;
-    }
-    const DevBlock r = blks[E.src_blk];
-    double cost = E.cost, sint = E.sint;
-    double cos2t = cost * cost, sin2t = sint * sint, sct = sint * cost;
-    auto R_ = [&](int L) { return slot(r, S_DQ + L - 1)[is]; };
-    auto W_ = [&](int L, double v) { slot(b, S_DQ + L - 1)[il] = v; };
-    double ugx = R_(1), ugy = R_(2), ugz = R_(3);
-    double vgx = R_(4), vgy = R_(5), vgz = R_(6);
-    double wgx = R_(7), wgy = R_(8), wgz = R_(9);
-    W_(1, ugx);
-    W_(2, cost * ugy + sint * ugz);
-    W_(3, -sint * ugy + cost * ugz);
-    W_(4, cost * vgx + sint * wgx);
-    W_(5, cos2t * vgy + sct * (vgz + wgy) + sin2t * wgz);
-    W_(6, cos2t * vgz + sct * (-vgy + wgz) - sin2t * wgy);
-    W_(7, -sint * vgx + cost * wgx);
-    W_(8, -sin2t * vgz + sct * (-vgy + wgz) + cos2t * wgy);
-    W_(9, sin2t * vgy + sct * (vgz + wgy) + cos2t * wgz);
-    for (int LL = 4; LL <= 6; ++LL) {
-        int L = (LL - 1) * 3 + 1;
-        W_(L, R_(L));
-        double gy = R_(L + 1), gz = R_(L + 2);
-        W_(L + 1, cost * gy + sint * gz);
-        W_(L + 2, -sint * gy + cost * gz);
-    }
-}
-
 // ---------------------------------------------------------------------------------------
 // primitives used by every stencil: u=V2/V1, v, w, k=V6/V1, omega=V7/V1, 1/V1 and V*(1/V1)
 // ---------------------------------------------------------------------------------------
@@ -398,10 +361,12 @@ __global__ void k_mirror(const DevBlock* __restrict__ blks, int nblk, long long 
 
 #endif  // TG_COMMON_KERNELS
 
-#ifdef TG_COMMON_KERNELS
+
+// ---------------------------------------------------------------------------------------
 // ---------------------------------------------------------------------------------------
 // Space/DIFF_DqDxyz.F90:25-74, 232-265, 300-381 (gradients and shock sensor, interior cells)
 // ---------------------------------------------------------------------------------------
+template <typename R>
 __global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, int turb) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
@@ -410,41 +375,42 @@ __global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __rest
     int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     int c = cidx(b, I, J, K);
     const int st[3] = {1, b.PI, b.PI * b.PJ};
-    double volinv = 1.0 / slot(b, S_VOL)[c];
-    const double* qs[6] = {slot(b, S_PRIM), slot(b, S_PRIM + 1), slot(b, S_PRIM + 2), slot(b, S_T),
-                           slot(b, S_PRIM + 3), slot(b, S_PRIM + 4)};
+    R volinv = R(1.0) / rs<R>(b, S_VOL)[c];
+    const R* qs[6] = {rs<R>(b, S_PRIM), rs<R>(b, S_PRIM + 1), rs<R>(b, S_PRIM + 2), rs<R>(b, S_T),
+                      rs<R>(b, S_PRIM + 3), rs<R>(b, S_PRIM + 4)};
     int nq = turb ? 6 : 4;
-    const double* SD = slot(b, S_SD);
-    double g9[3][3];
+    const R* SD = rs<R>(b, S_SD);
+    R g9[3][3];
     for (int q = 0; q < nq; ++q) {
-        double fw[3], fe[3];
+        R fw[3], fe[3];
         for (int d = 0; d < 3; ++d) {
-            const double* al = slot(b, S_ALAGM + d);
-            const double* ai = slot(b, S_AINV + d);
+            const R* al = rs<R>(b, S_ALAGM + d);
+            const R* ai = rs<R>(b, S_AINV + d);
             fw[d] = favg(qs[q], al, ai, c, st[d]);
             fe[d] = favg(qs[q], al, ai, c + st[d], st[d]);
         }
         for (int m = 0; m < 3; ++m) {
-            const double* S1 = SD + (size_t)(0 * 3 + m) * b.ncell;
-            const double* S2 = SD + (size_t)(1 * 3 + m) * b.ncell;
-            const double* S3 = SD + (size_t)(2 * 3 + m) * b.ncell;
-            double g = volinv * (fe[0] * S1[c + st[0]] - fw[0] * S1[c] + fe[1] * S2[c + st[1]] - fw[1] * S2[c]
+            const R* S1 = SD + (size_t)(0 * 3 + m) * b.ncell;
+            const R* S2 = SD + (size_t)(1 * 3 + m) * b.ncell;
+            const R* S3 = SD + (size_t)(2 * 3 + m) * b.ncell;
+            R g = volinv * (fe[0] * S1[c + st[0]] - fw[0] * S1[c] + fe[1] * S2[c + st[1]] - fw[1] * S2[c]
                                  + fe[2] * S3[c + st[2]] - fw[2] * S3[c]);
-            slot(b, S_DQ + 3 * q + m)[c] = g;
+            rs<R>(b, S_DQ + 3 * q + m)[c] = g;
             if (q < 3) g9[q][m] = g;
         }
     }
-    double DuDx = g9[0][0], DuDy = g9[0][1], DuDz = g9[0][2];
-    double DvDx = g9[1][0], DvDy = g9[1][1], DvDz = g9[1][2];
-    double DwDx = g9[2][0], DwDy = g9[2][1], DwDz = g9[2][2];
-    double W12 = (DuDy - DvDx) / 2.0, W13 = (DuDz - DwDx) / 2.0, W23 = (DvDz - DwDy) / 2.0;
-    double Vort = sqrt(2.0 * (2.0 * W12 * W12 + 2.0 * W13 * W13 + 2.0 * W23 * W23));
-    double DivU = sqrt(DuDx * DuDx + DvDy * DvDy + DwDz * DwDz);
-    slot(b, S_SHOCK)[c] = DivU * DivU / dmax(DivU * DivU + Vort * Vort, 1.0);
+    R DuDx = g9[0][0], DuDy = g9[0][1], DuDz = g9[0][2];
+    R DvDx = g9[1][0], DvDy = g9[1][1], DvDz = g9[1][2];
+    R DwDx = g9[2][0], DwDy = g9[2][1], DwDz = g9[2][2];
+    R W12 = (DuDy - DvDx) / R(2.0), W13 = (DuDz - DwDx) / R(2.0), W23 = (DvDz - DwDy) / R(2.0);
+    R Vort = sqrt(R(2.0) * (R(2.0) * W12 * W12 + R(2.0) * W13 * W13 + R(2.0) * W23 * W23));
+    R DivU = sqrt(DuDx * DuDx + DvDy * DvDy + DwDz * DwDz);
+    rs<R>(b, S_SHOCK)[c] = DivU * DivU / dmax(DivU * DivU + Vort * Vort, R(1.0));
 }
 
 // shock of the three ghost layers of every face = shock of the adjacent interior cell
 // (Space/DIFF_DqDxyz.F90:388-396 restricted to the face ghosts the stencils read)
+template <typename R>
 __global__ void k_shock_ghost(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
@@ -460,11 +426,47 @@ __global__ void k_shock_ghost(const DevBlock* __restrict__ blks, const Tile* __r
     if (d == 0) { j = n % b.NJ1 + 1; k = n / b.NJ1 + 1; i = side ? b.NI1 + L : 1 - L; ii = side ? b.NI1 : 1; jj = j; kk = k; }
     else if (d == 1) { i = n % b.NI1 + 1; k = n / b.NI1 + 1; j = side ? b.NJ1 + L : 1 - L; jj = side ? b.NJ1 : 1; ii = i; kk = k; }
     else { i = n % b.NI1 + 1; j = n / b.NI1 + 1; k = side ? b.NK1 + L : 1 - L; kk = side ? b.NK1 : 1; ii = i; jj = j; }
-    double* sh = slot(b, S_SHOCK);
+    R* sh = rs<R>(b, S_SHOCK);
     sh[cidx(b, i, j, k)] = sh[cidx(b, ii, jj, kk)];
 }
 
-#endif  // TG_COMMON_KERNELS
+// BC_Boundarys(0): gradients of the first ghost layer (BC/*.F90 sweep 0, BC/BC_P2P.F90:140-184)
+template <typename R>
+__global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n, int turb) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const BCEntry E = ent[e];
+    const DevBlock b = blks[E.blk];
+    const int il = E.l[0], is = E.s[0];
+    if (E.kind != 9) {
+        for (int L = 0; L < 18; ++L) rs<R>(b, S_DQ + L)[il] = rs<R>(b, S_DQ + L)[is];
+        return;
+    }
+    const DevBlock r = blks[E.src_blk];
+    R cost = R(E.cost), sint = R(E.sint);
+    R cos2t = cost * cost, sin2t = sint * sint, sct = sint * cost;
+    auto R_ = [&](int L) { return rs<R>(r, S_DQ + L - 1)[is]; };
+    auto W_ = [&](int L, R v) { rs<R>(b, S_DQ + L - 1)[il] = v; };
+    R ugx = R_(1), ugy = R_(2), ugz = R_(3);
+    R vgx = R_(4), vgy = R_(5), vgz = R_(6);
+    R wgx = R_(7), wgy = R_(8), wgz = R_(9);
+    W_(1, ugx);
+    W_(2, cost * ugy + sint * ugz);
+    W_(3, -sint * ugy + cost * ugz);
+    W_(4, cost * vgx + sint * wgx);
+    W_(5, cos2t * vgy + sct * (vgz + wgy) + sin2t * wgz);
+    W_(6, cos2t * vgz + sct * (-vgy + wgz) - sin2t * wgy);
+    W_(7, -sint * vgx + cost * wgx);
+    W_(8, -sin2t * vgz + sct * (-vgy + wgz) + cos2t * wgy);
+    W_(9, sin2t * vgy + sct * (vgz + wgy) + cos2t * wgz);
+    for (int LL = 4; LL <= 6; ++LL) {
+        int L = (LL - 1) * 3 + 1;
+        W_(L, R_(L));
+        R gy = R_(L + 1), gz = R_(L + 2);
+        W_(L + 1, cost * gy + sint * gz);
+        W_(L + 2, -sint * gy + cost * gz);
+    }
+}
 
 // ---------------------------------------------------------------------------------------
 // Face fluxes of direction DIR (faces 1..N along DIR, interior in the other two):
@@ -750,8 +752,8 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell*
     const int nlex = (I - 1) + b.NI1 * ((J - 1) + b.NJ1 * (K - 1));     // lexicographic interior index
     const int c = cidx(b, I, J, K);
     const size_t nc = (size_t)b.ncell;
-    auto REC = [&](int m) -> R& { return rec[(size_t)m * N + q]; };
-    auto DQ = [&](int L) -> R& { return dq[(size_t)L * N + q]; };
+    auto REC = [&](int m) -> R& { return rec[sw_at(q, m, NREC)]; };
+    auto DQ = [&](int L) -> R& { return dq[sw_at(q, L, DQ_STRIDE)]; };
     // BDF2 right-hand side and the mean-flow diagonal, in FP64 in both paths
     const double DT = pd.DT_LUSGS_Main;
     double Dtm = slot(b, S_DTM)[c];
@@ -773,7 +775,7 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell*
         const int st[3] = {1, b.PI, b.PI * b.PJ};
         for (int side = 0; side < 2; ++side)
             for (int d = 0; d < 3; ++d) {
-                if (nbp[(size_t)(3 * side + d) * N + q] < 0) continue;
+                if (nbp[sw_at(q, 3 * side + d, 6)] < 0) continue;
                 const int nb = side == 0 ? c - st[d] : c + st[d];
                 const R* asd = rs<R>(b, S_ASD + 3 * d);
                 R Jt[NJAC];
@@ -883,18 +885,25 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
     const int side = LOWER ? 0 : 3;
     const int jb = LOWER ? REC_JL : REC_JU, rb = LOWER ? REC_RDSL : REC_RDSU;
     const R sgn = LOWER ? R(1.0) : R(-1.0);
-    auto REC = [&](int m) { return rec[(size_t)m * N + q]; };
+    auto REC = [&](int m) { return rec[sw_at(q, m, NREC)]; };
+    // all loads of the three neighbours are issued together: a missing neighbour (nbp < 0)
+    // reads this cell's own entries instead and its term is replaced by 0 afterwards
+    long long npv[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) npv[d] = nbp[sw_at(q, side + d, 6)];
     R acc[3];
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
-        acc[d] = R(0.0);
-        const long long np = nbp[(size_t)(side + d) * N + q];
-        if (np < 0) continue;
+        const bool has = npv[d] >= 0;
+        const long long np = has ? npv[d] : q;
         const int jd = jb + NJAC * d;
         const R RDSt = REC(rb + d);
+        R val;
         // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1 line)
         if (L < 5) {
-            R AinRo = __ldcg(dq + np), AinRx = __ldcg(dq + N + np), AinRy = __ldcg(dq + 2 * N + np);
-            R AinRz = __ldcg(dq + 3 * N + np), AinRe = __ldcg(dq + 4 * N + np);
+            R AinRo = __ldcg(dq + sw_at(np, 0, DQ_STRIDE)), AinRx = __ldcg(dq + sw_at(np, 1, DQ_STRIDE));
+            R AinRy = __ldcg(dq + sw_at(np, 2, DQ_STRIDE)), AinRz = __ldcg(dq + sw_at(np, 3, DQ_STRIDE));
+            R AinRe = __ldcg(dq + sw_at(np, 4, DQ_STRIDE));
             R Dif;
             if (L == 0) {
                 const R aSDt = R(0.0);
@@ -909,16 +918,17 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
                       + AinRe * REC(r + 3);
             }
             const R Din = L == 0 ? AinRo : L == 1 ? AinRx : L == 2 ? AinRy : L == 3 ? AinRz : AinRe;
-            acc[d] = R(0.5) * (Dif + sgn * (RDSt * Din));
+            val = R(0.5) * (Dif + sgn * (RDSt * Din));
         } else {
             const R VP = REC(jd + JC_VPT);
-            const R Dq = __ldcg(dq + (size_t)L * N + np);
-            acc[d] = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
+            const R Dq = __ldcg(dq + sw_at(np, L, DQ_STRIDE));
+            val = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
         }
+        acc[d] = has ? val : R(0.0);
     }
     const R stept = REC(REC_STEPT), cvs = REC(REC_CVS);
     const R den = L < 5 ? REC(REC_FM) : REC(REC_FT);
-    R* D = dq + (size_t)L * N + q;
+    R* D = dq + sw_at(q, L, DQ_STRIDE);
     const R own = __ldcg(D);
     const R sum = acc[0] + acc[1] + acc[2];
     if (LOWER) *D = (own * stept + sum * cvs) / den;
@@ -990,7 +1000,7 @@ __global__ void k_sweep_scatter(const DevBlock* __restrict__ blks, const SweepCe
     const SweepCell sc = cells[q];
     const DevBlock b = blks[sc.blk];
     const int c = cidx(b, sc.i, sc.j, sc.k);
-    for (int L = 0; L < 7; ++L) rs<R>(b, S_D + L)[c] = dq[(size_t)L * N + q];
+    for (int L = 0; L < 7; ++L) rs<R>(b, S_D + L)[c] = dq[sw_at(q, L, DQ_STRIDE)];
 }
 
 #ifdef TG_COMMON_KERNELS
@@ -1066,7 +1076,7 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
             double TT = p.RXM2 * PPP / pRo;
             double RmiuL = mu_suth<double>(p, TT);
             double DistN = slot(b, S_DST)[c];
-            auto G = [&](int q) { return slot(b, S_DQ + q)[c]; };
+            auto G = [&](int q) { return d_fp32 ? (double)fslot(b, S_DQ + q)[c] : slot(b, S_DQ + q)[c]; };
             double Dudx = G(0), Dudy = G(1), Dudz = G(2), Dvdx = G(3), Dvdy = G(4), Dvdz = G(5), Dwdx = G(6), Dwdy = G(7), Dwdz = G(8);
             double Div = Dudx + Dvdy + Dwdz;
             double prod = (2.0 * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy) + sq(Dwdx + Dudz)

@@ -16,10 +16,7 @@ void launch_specrad(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int
 void launch_bc_state(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, const Params& p, int turb);
 void launch_bc_outlet(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const OutletLine* lines, int nl,
                       const Params& p, int turb);
-void launch_bc_grad(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, int turb);
 void launch_prims(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
-void launch_gradient(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int turb);
-void launch_shock_ghost(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt);
 void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts,
                    int d_fp32);
 void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml);
@@ -30,6 +27,9 @@ void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long lon
 
 // flux, source and sweep kernels, instantiated per arithmetic type
 struct FluxLaunchers {
+    void (*gradient)(cudaStream_t, const DevBlock*, const Tile*, int, int turb);
+    void (*shock_ghost)(cudaStream_t, const DevBlock*, const Tile*, int);
+    void (*bc_grad)(cudaStream_t, const DevBlock*, const BCEntry*, int, int turb);
     void (*face_flux[3])(cudaStream_t, const DevBlock*, const Tile*, int, const Params&, int);
     void (*gather)(cudaStream_t, const DevBlock*, const Tile*, int, int);
     void (*sst_fc1)(cudaStream_t, const DevBlock*, const Tile*, int, const Params&);

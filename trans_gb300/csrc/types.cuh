@@ -23,9 +23,9 @@ struct SweepCell { int blk, i, j, k; };
 // the sweep-order arrays of one context (element type R = the sweep arithmetic)
 struct SweepView {
     const SweepCell* cells;     // cell of each sweep position
-    const int* nbp;             // 6 x n: positions of the lower (0..2) and upper (3..5) neighbours, -1 = none
-    void* rec;                  // NREC x n records
-    void* dq;                   // 7 x n DeltaQ
+    const int* nbp;             // n x 6: positions of the lower (0..2) and upper (3..5) neighbours, -1 = none
+    void* rec;                  // n x NREC records
+    void* dq;                   // n x DQ_STRIDE DeltaQ
     long long n;
 };
 
