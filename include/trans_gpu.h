@@ -171,6 +171,34 @@ long long trans_device_bytes(void* ctx);
 /* Kernel launches issued since the context was created (all kernels of this library). */
 long long trans_kernel_launches(void* ctx);
 /*
+ * Batches (no reference counterpart: the batching and serving layer).  A batch context holds
+ * independent cases -- each with its own blocks, module globals, iteration counter and norms --
+ * that are advanced together: every kernel launch covers the blocks of all cases.  Cases are
+ * added and removed while the context runs (continuous batching); a case is admitted only if
+ * its device bytes fit the context's budget (TRANS_E_MEMORY otherwise, nothing allocated).
+ * All cases of one context share the precision mode and the sub-iteration count (Kchld).
+ * A case's KI starts at its KI_ini and advances by one per trans_batch_iterate step, so its
+ * results do not depend on which other cases share the context.
+ */
+int trans_batch_create(int precision, long long device_budget_bytes /* 0 = no limit */, void** ctx);
+/* Device bytes a case would take in a batch context (-1: the case is not supported). */
+long long trans_batch_case_bytes(const trans_params* p, int nblocks, const trans_block* blocks);
+int trans_batch_add(void* ctx, const trans_params* p, int nblocks, const trans_block* blocks, int* case_id);
+int trans_batch_remove(void* ctx, int case_id);
+/* As trans_set_field / trans_get_field for block ib of one case. */
+int trans_batch_set_field(void* ctx, int case_id, int ib, int field, const double* fortran_array);
+int trans_batch_get_field(void* ctx, int case_id, int ib, int field, double* fortran_array);
+/* n outer iterations of every case.  TRANS_E_NAN: some case produced a NaN (its norms carry
+ * nan_flag); the iteration is complete and the caller removes that case. */
+int trans_batch_iterate(void* ctx, int n);
+/* Iterations done by a case, its per-block norms of its first and of its last iteration
+ * (arrays of nblocks entries, either may be NULL). */
+int trans_batch_case_norms(void* ctx, int case_id, int* iterations, trans_norms* first, trans_norms* last);
+long long trans_batch_bytes_in_use(void* ctx);
+/* Number of cases; their ids in ids[0..max-1]. */
+int trans_batch_cases(void* ctx, int* ids, int max);
+
+/*
  * TIME_Update_V (Time/TIME_Update_V.F90:91-908) over all blocks, as trans_run_stage(ctx,
  * TRANS_STAGE_UPDATE, ki, ...), but with the per-tile residual-norm partials kept in a fixed
  * 4 MiB buffer that is part of the library image instead of the context's own buffer.  No

@@ -145,14 +145,14 @@ def test_gpu_against_golden_vectors(gpu_lib, name):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
-    """The hyperplane-per-launch schedule and the single cooperative launch with grid
-    barriers (and the tuner's pick) compute every DeltaQ with the same operations: states
-    after 6 iterations are bit-identical."""
+    """The hyperplane-per-launch schedule, the single cooperative launch with grid barriers, the
+    dataflow schedule (and the tuner's pick) compute every DeltaQ with the same operations:
+    states after 6 iterations are bit-identical."""
     from helpers import small_cascade
     from trans_gb300 import abi
     from trans_gb300.solver import Solver
     out = {}
-    for mode in ("planes", "coop", "auto"):
+    for mode in ("planes", "coop", "flow", "auto"):
         monkeypatch.setenv("TRANS_SWEEP", mode)
         c, conns, geo, st = small_cascade(Kind_Spatial=3, Kind_Roe=3)
         c.params.precision = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
@@ -161,7 +161,7 @@ def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
             s.iterate(ki)
         out[mode] = [s.get_field(ib, "V") for ib in range(len(c.blocks))]
         s.close()
-    for mode in ("coop", "auto"):
+    for mode in ("coop", "flow", "auto"):
         for ib in range(len(out["planes"])):
             m = interior(c.blocks[ib].dims)
             assert bit_equal_fraction(out[mode][ib], out["planes"][ib], m) == 1.0, (mode, ib)

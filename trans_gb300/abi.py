@@ -136,6 +136,18 @@ def bind_common(lib):
     lib.trans_kernel_times.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int]
     lib.trans_kernel_class.argtypes = [C.c_int]
     lib.trans_kernel_class.restype = C.c_char_p
+    lib.trans_batch_create.argtypes = [C.c_int, C.c_longlong, C.POINTER(vp)]
+    lib.trans_batch_case_bytes.argtypes = [C.POINTER(TransParams), C.c_int, C.POINTER(TransBlock)]
+    lib.trans_batch_case_bytes.restype = C.c_longlong
+    lib.trans_batch_add.argtypes = [vp, C.POINTER(TransParams), C.c_int, C.POINTER(TransBlock), C.POINTER(C.c_int)]
+    lib.trans_batch_remove.argtypes = [vp, C.c_int]
+    lib.trans_batch_set_field.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    lib.trans_batch_get_field.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    lib.trans_batch_iterate.argtypes = [vp, C.c_int]
+    lib.trans_batch_case_norms.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(TransNorms), C.POINTER(TransNorms)]
+    lib.trans_batch_bytes_in_use.argtypes = [vp]
+    lib.trans_batch_bytes_in_use.restype = C.c_longlong
+    lib.trans_batch_cases.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
     lib.trans_tuning.argtypes = [vp]
     lib.trans_tuning.restype = C.c_char_p
     lib.trans_last_error.argtypes = [vp]
@@ -147,5 +159,7 @@ EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field
             "trans_run_stage", "trans_get_norms", "trans_sync", "trans_device_bytes",
             "trans_kernel_launches", "trans_last_error", "trans_stage_times", "trans_probe_fma_gflops",
             "trans_time_iterations", "trans_update_static_scratch", "trans_tuning", "trans_kernel_times",
-            "trans_kernel_class"]
+            "trans_kernel_class", "trans_batch_create", "trans_batch_case_bytes", "trans_batch_add",
+            "trans_batch_remove", "trans_batch_set_field", "trans_batch_get_field", "trans_batch_iterate",
+            "trans_batch_case_norms", "trans_batch_bytes_in_use", "trans_batch_cases"]
 TRANS_NKCLASS = 16

@@ -17,6 +17,11 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr"]
 UNITS = {
     "api.cu": ["-fmad=false"],
+    "engine.cu": ["-fmad=false"],
+    "worklist.cu": ["-fmad=false"],
+    "stages.cu": ["-fmad=false"],
+    "noalloc.cu": ["-fmad=false"],
+    "batch.cu": ["-fmad=false"],
     "k_fp64.cu": ["-fmad=false"],
     "k_mixed.cu": ["-fmad=true"],
 }

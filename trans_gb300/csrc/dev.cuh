@@ -57,15 +57,15 @@ enum JacTerm { JC_R0 = 0, JC_R1 = 3, JC_R2 = 8, JC_R3 = 13, JC_VP = 18, JC_GET1 
 // Per-cell record of the sweeps, in sweep (hyperplane) order: the Jacobian terms and spectral
 // radii of the three lower (L sweep) and three upper (U sweep) neighbours, and the cell's own
 // diagonal terms.
-enum SweepRec { REC_JL = 0, REC_JU = 3 * NJAC, REC_RDSL = 6 * NJAC, REC_RDSU = 6 * NJAC + 3,
-                REC_STEPT = 6 * NJAC + 6, REC_CVS = REC_STEPT + 1, REC_FM = REC_STEPT + 2, REC_FT = REC_STEPT + 3,
-                NREC = REC_STEPT + 4 };
+// Neighbour k (0..2 lower i,j,k; 3..5 upper) occupies NBREC entries from NBREC*k: its NJAC
+// Jacobian terms, then its spectral radius in that direction.
+enum SweepRec { NBREC = NJAC + 1, REC_STEPT = 6 * NBREC, REC_CVS = REC_STEPT + 1, REC_FM = REC_STEPT + 2,
+                REC_FT = REC_STEPT + 3, NREC = REC_STEPT + 4 };
 constexpr int DQ_STRIDE = 8;     // DeltaQ of one sweep position: 7 components + 1 pad
-// Sweep-order arrays are stored in tiles of 32 positions ("AoSoA"): element m of position q is
-// at (q/32)*32*width + m*32 + q%32, so that a warp writing element m of 32 consecutive
-// positions writes one contiguous 128-byte run, and one hyperplane stays one contiguous range.
+// Sweep-order arrays keep the entries of one position together (element m of position q at
+// q*width + m): a hyperplane is one contiguous range, and one cell's record spans a few lines.
 __host__ __device__ inline size_t sw_at(long long q, int m, int width) {
-    return (size_t)(q >> 5) * (size_t)(32 * width) + (size_t)m * 32 + (size_t)(q & 31);
+    return (size_t)q * (size_t)width + (size_t)m;
 }
 
 // face-flux components (per face and direction)
@@ -76,7 +76,7 @@ struct DevBlock {
     int NI, NJ, NK, NI1, NJ1, NK1, PI, PJ, PK;
     int ncell;            // PI*PJ*PK
     int nint;             // NI1*NJ1*NK1
-    int pad_;
+    int cs;               // case slot: index of the block's case in the CaseDev array
     double* base;
     float* fbase;         // FP32 copies of the slots read by the FP32 kernels (mixed mode only)
 };
@@ -118,6 +118,18 @@ inline ParamsT<R> params_as(const Params& p) {
     q.pad_ = 0;
     return q;
 }
+
+// One case of a batch as the kernels see it: its module globals (FP64 and FP32 copies) and the
+// switches of the current sub-iteration (CFL ramp, turbulence on, turbulence update on).
+struct CaseDev {
+    Params p;
+    ParamsT<float> pf;
+    double CFL_sub;
+    int turb, turb_upd;
+};
+template <typename R> __host__ __device__ inline const ParamsT<R>& cparams(const CaseDev& c);
+template <> __host__ __device__ inline const ParamsT<double>& cparams<double>(const CaseDev& c) { return c.p; }
+template <> __host__ __device__ inline const ParamsT<float>& cparams<float>(const CaseDev& c) { return c.pf; }
 
 __host__ __device__ inline int cidx(const DevBlock& b, int i, int j, int k) {
     return (i + 2) + b.PI * ((j + 2) + b.PJ * (k + 2));

@@ -1,0 +1,141 @@
+// engine.h -- host side of the GB300 hot path: contexts holding one or many cases (batches),
+// their device memory, work lists and the stage sequence of main.F90:54-197.
+//
+// A context owns a set of cases.  Each case is one independent solve (its own blocks, module
+// globals, iteration counter and norms) with its blocks in its own device arena.  All cases
+// of a context are advanced together: the work lists (cell/face tiles, boundary gathers,
+// sweep hyperplanes) cover every block of every case, so each kernel is one launch for the
+// whole batch.  Adding or removing a case rebuilds the work lists; the arenas stay put.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/trans_gpu.h"
+#include "launch.h"
+#include "types.cuh"
+
+namespace tg {
+namespace eng {
+
+struct HostBlock {
+    int NI, NJ, NK, id;
+    std::vector<trans_conn> conn;
+    std::vector<int> mw[6];
+};
+
+struct CaseRec {
+    int id = 0;                          // handle of the batch API
+    trans_params p{};
+    Params dp{};
+    std::vector<HostBlock> hb;
+    std::vector<DevBlock> blk;           // base pointers into this case's arena; cs set at rebuild
+    double* arena = nullptr;
+    float* farena = nullptr;             // FP32 copies of the slots (mixed path only)
+    size_t arena_doubles = 0;
+    long long bytes = 0;                 // device bytes charged to the budget
+    int KI = 0;                          // outer iteration of the next/last call
+    int iters = 0;                       // iterations done since the case was added
+    int blk0 = 0;                        // index of its first block in the context's block list
+    bool geom_dirty = true;
+    std::vector<trans_norms> norms, first_norms;
+};
+
+// kernel classes of trans_kernel_times
+enum KClass { K_SPECRAD, K_BC_STATE, K_BC_OUTLET, K_PRIMS, K_MIRROR, K_GRADIENT, K_SHOCK_GHOST, K_BC_GRAD,
+              K_FACE, K_GATHER, K_SST_FC1, K_PREP, K_SWEEP, K_SCATTER, K_UPDATE, K_UPDATE_U, NKCLASS };
+extern const char* const kclass_name[NKCLASS];
+
+struct Ctx {
+    int precision = TRANS_FP64;
+    bool mixed = false;
+    const FluxLaunchers* fl = nullptr;
+    long long budget = 0;                // device bytes the cases may take (0 = no limit)
+    long long in_use = 0;
+    int next_id = 0;
+    std::vector<CaseRec*> cases;
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+    std::string err;
+    // ---- rebuilt when the set of cases changes ----
+    std::vector<DevBlock> blk;           // all blocks of all cases
+    DevBlock* d_blk = nullptr;
+    long long* d_off = nullptr;          // padded-cell offsets of the blocks (for flat kernels)
+    long long total_cells = 0;
+    std::vector<Tile> cell_tiles, face_tiles[3], ghost_tiles;
+    Tile *d_cell = nullptr, *d_face[3] = {nullptr, nullptr, nullptr}, *d_ghost = nullptr;
+    std::vector<int> cell_tile_blk;      // block of each cell tile (norm reduction)
+    std::vector<BCEntry> bc, outlet;
+    std::vector<OutletLine> lines;
+    BCEntry *d_bc = nullptr, *d_outlet = nullptr;
+    OutletLine* d_lines = nullptr;
+    std::vector<SweepCell> sweep;
+    std::vector<int> plane_off;          // sweep positions of hyperplane h: [plane_off[h], plane_off[h+1])
+    SweepCell* d_sweep = nullptr;
+    int* d_plane_off = nullptr;
+    SweepView sv{};
+    int* d_nbp = nullptr;
+    int* d_flags = nullptr;
+    void* d_rec = nullptr;
+    void* d_dqs = nullptr;
+    void* d_dq_save = nullptr;
+    NormPart* d_parts = nullptr;
+    std::vector<NormPart> h_parts;
+    std::vector<trans_norms> norms;      // per block of the context
+    CaseDev* d_cdev = nullptr;           // per case slot
+    CaseDev* h_cdev = nullptr;           // pinned
+    std::vector<CaseDev> cdev_last;      // what was last uploaded
+    double* d_stage = nullptr;           // Fortran-layout staging buffer of trans_set/get_field
+    size_t stage_doubles = 0;
+    bool built = false;
+    // ---- sweep schedule ----
+    cudaGraphExec_t sweep_exec = nullptr;
+    // 0 = one launch per hyperplane (graph), 1 = one cooperative launch with grid barriers,
+    // 2 = dataflow over ready flags; -1 = pick the fastest on first use (all bit-identical)
+    int sweep_mode = -1, sweep_grid = 0, sweep_block = 0;
+    bool sweep_forced = false;
+    SweepSync* d_sync = nullptr;
+    SweepSync* h_sync = nullptr;         // pinned
+    std::string sweep_tuning;
+    // ---- instrumentation ----
+    bool ktime_on = false;
+    struct KEv { int k, n; cudaEvent_t a, b; };
+    std::vector<KEv> kev;
+};
+
+int fail(Ctx* c, int code, const std::string& msg);
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// times the launches issued in its lifetime as kernel class k (n launches) when enabled
+struct KScope {
+    Ctx* c; int k, n; cudaEvent_t a = nullptr, b = nullptr;
+    KScope(Ctx* c_, int k_, int n_ = 1);
+    ~KScope();
+};
+
+bool params_supported(const trans_params* p);
+int validate_case(const trans_params* p, int nblocks, const trans_block* blocks);
+int ctx_init(Ctx* c, int precision, long long budget);
+void ctx_free(Ctx* c);
+long long case_bytes(int precision, int nblocks, const trans_block* blocks);
+int case_add(Ctx* c, const trans_params* p, int nblocks, const trans_block* blocks, CaseRec** out);
+int case_remove(Ctx* c, int id);
+CaseRec* case_find(Ctx* c, int id);
+int rebuild(Ctx* c);
+void free_worklists(Ctx* c);
+int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload);
+int run_stage(Ctx* c, int stage, int itr);
+int upload_cdev(Ctx* c);
+int finalize_geometry(Ctx* c);
+int reduce_norms(Ctx* c);
+int run_iteration(Ctx* c);               // one outer iteration of every case at its KI
+int kernel_times(Ctx* c, double* ms, int* launches);
+
+}  // namespace eng
+}  // namespace tg

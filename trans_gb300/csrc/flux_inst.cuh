@@ -5,29 +5,33 @@
 
 namespace tg {
 namespace {
-void grd(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, int turb) {
-    if (nt > 0) k_gradient<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, turb);
+void grd(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
+    if (nt > 0) k_gradient<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, cd);
 }
 void shg(cudaStream_t s, const DevBlock* b, const Tile* t, int nt) {
     if (nt > 0) k_shock_ghost<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t);
 }
-void bcg(cudaStream_t s, const DevBlock* b, const BCEntry* e, int n, int turb) {
-    if (n > 0) k_bc_grad<TG_R><<<(n + 127) / 128, 128, 0, s>>>(b, e, n, turb);
+void bcg(cudaStream_t s, const DevBlock* b, const BCEntry* e, int n) {
+    if (n > 0) k_bc_grad<TG_R><<<(n + 127) / 128, 128, 0, s>>>(b, e, n);
 }
 template <int DIR>
-void ff(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const Params& p, int turb) {
-    if (nt > 0) k_face_flux<TG_R, DIR><<<nt, FACE_TILE, 0, s>>>(b, t, params_as<TG_R>(p), turb);
+void ff(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
+    if (nt > 0) k_face_flux<TG_R, DIR><<<nt, FACE_TILE, 0, s>>>(b, t, cd);
 }
-void ga(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, int turb) {
-    if (nt > 0) k_gather<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, turb);
+void ga(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
+    if (nt > 0) k_gather<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, cd);
 }
-void fc(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const Params& p) {
-    if (nt > 0) k_sst_fc1<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, params_as<TG_R>(p));
+void fc(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
+    if (nt > 0) k_sst_fc1<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, cd);
 }
-void prep(cudaStream_t s, const DevBlock* b, const SweepView& v, const Params& p, int turb) {
+void prep(cudaStream_t s, const DevBlock* b, const SweepView& v, const CaseDev* cd) {
     if (v.n > 0)
         k_lusgs_prep<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(
-            b, v.cells, v.nbp, (TG_R*)v.rec, (TG_R*)v.dq, v.n, p, params_as<TG_R>(p), turb);
+            b, v.cells, v.nbp, (TG_R*)v.rec, (TG_R*)v.dq, v.n, cd);
+}
+void jac(cudaStream_t s, const DevBlock* b, const SweepView& v) {
+    if (v.n > 0)
+        k_lusgs_jac<TG_R><<<(unsigned)((v.n + 31) / 32), 6 * 32, 0, s>>>(b, v.cells, v.nbp, (TG_R*)v.rec, v.n);
 }
 void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb) {
     if (count > 0)
@@ -54,6 +58,20 @@ int swa_occ(int block) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_all<TG_R>, block, 0) != cudaSuccess) return 0;
     return n;
 }
+cudaError_t swf(cudaStream_t s, const SweepView& v, int* flagL, int* flagU, SweepSync* sy, int grid, int block) {
+    unsigned limit = SWEEP_SPIN_LIMIT;
+    const int* nbp = v.nbp;
+    const TG_R* rec = (const TG_R*)v.rec;
+    TG_R* dq = (TG_R*)v.dq;
+    long long n = v.n;
+    void* args[] = {(void*)&nbp, (void*)&rec, (void*)&dq, (void*)&n, (void*)&flagL, (void*)&flagU, (void*)&sy, (void*)&limit};
+    return cudaLaunchCooperativeKernel((const void*)k_sweep_flow<TG_R>, dim3(grid), dim3(block), args, 0, s);
+}
+int swf_occ(int block) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_flow<TG_R>, block, 0) != cudaSuccess) return 0;
+    return n;
+}
 void scat(cudaStream_t s, const DevBlock* b, const SweepView& v) {
     if (v.n > 0)
         k_sweep_scatter<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(b, v.cells, (const TG_R*)v.dq, v.n);
@@ -61,7 +79,7 @@ void scat(cudaStream_t s, const DevBlock* b, const SweepView& v) {
 }  // namespace
 
 const FluxLaunchers& TG_NAME() {
-    static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, prep, swl, swu, swa, swa_occ, scat, sizeof(TG_R)};
+    static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, prep, jac, swl, swu, swa, swa_occ, swf, swf_occ, scat, sizeof(TG_R)};
     return L;
 }
 }  // namespace tg

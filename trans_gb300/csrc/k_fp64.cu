@@ -6,28 +6,28 @@
 #include "flux_inst.cuh"
 
 namespace tg {
-void launch_specrad(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, double CFL_sub) {
-    if (nt > 0) k_specrad<<<nt, CELL_TILE, 0, s>>>(blks, tiles, p, CFL_sub);
+void launch_specrad(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev) {
+    if (nt > 0) k_specrad<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev);
 }
-void launch_bc_state(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, const Params& p, int turb) {
-    if (n > 0) k_bc_state<<<(n + 127) / 128, 128, 0, s>>>(blks, ent, n, p, turb);
+void launch_bc_state(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, const CaseDev* cdev) {
+    if (n > 0) k_bc_state<<<(n + 127) / 128, 128, 0, s>>>(blks, ent, n, cdev);
 }
 void launch_bc_outlet(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const OutletLine* lines, int nl,
-                      const Params& p, int turb) {
-    if (nl > 0) k_bc_outlet<<<(nl + 63) / 64, 64, 0, s>>>(blks, ent, lines, nl, p, turb);
+                      const CaseDev* cdev) {
+    if (nl > 0) k_bc_outlet<<<(nl + 63) / 64, 64, 0, s>>>(blks, ent, lines, nl, cdev);
 }
 void launch_prims(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off) {
     if (total > 0) k_prims<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off);
 }
-void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts,
+void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts,
                    int d_fp32) {
-    if (nt > 0) k_update<<<nt, CELL_TILE, 0, s>>>(blks, tiles, p, turb_upd, parts, d_fp32);
+    if (nt > 0) k_update<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev, parts, d_fp32);
 }
 void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml) {
     if (total > 0) k_mirror<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off, ml);
 }
-void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int kind_dual) {
-    if (nt > 0) k_update_u<<<nt, CELL_TILE, 0, s>>>(blks, tiles, kind_dual);
+void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev) {
+    if (nt > 0) k_update_u<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev);
 }
 void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off) {
     if (total > 0) k_geom_static<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off);

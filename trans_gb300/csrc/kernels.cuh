@@ -16,10 +16,12 @@ namespace tg {
 // ---------------------------------------------------------------------------------------
 // Time/SpectralRadius.F90:47-180
 // ---------------------------------------------------------------------------------------
-__global__ void k_specrad(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, double CFL_sub) {
+__global__ void k_specrad(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
+    const Params p = cdev[b.cs].p;
+    const double CFL_sub = cdev[b.cs].CFL_sub;
     int n = t.start + threadIdx.x;
     int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     int c = cidx(b, I, J, K);
@@ -96,12 +98,15 @@ __device__ inline void farbond(double XM, double P2, double RR, double Vxi, doub
     }
 }
 
-__global__ void k_bc_state(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n, Params p, int turb) {
+__global__ void k_bc_state(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n,
+                           const CaseDev* __restrict__ cdev) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
     const BCEntry E = ent[e];
     if (E.kind == 7) return;                       // outlets run line by line in k_bc_outlet
     const DevBlock b = blks[E.blk];
+    const Params p = cdev[b.cs].p;
+    const int turb = cdev[b.cs].turb;
     double* V[7];
     for (int m = 0; m < 7; ++m) V[m] = slot(b, S_V + m);
     double* PP = slot(b, S_PP);
@@ -263,11 +268,13 @@ __global__ void k_bc_state(const DevBlock* __restrict__ blks, const BCEntry* __r
 
 // BC/BC_Outlet.F90:50-106: the static pressure recurrence runs along j, one thread per line
 __global__ void k_bc_outlet(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent,
-                            const OutletLine* __restrict__ lines, int nl, Params p, int turb) {
+                            const OutletLine* __restrict__ lines, int nl, const CaseDev* __restrict__ cdev) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nl) return;
     const OutletLine Ln = lines[q];
     const DevBlock b = blks[Ln.blk];
+    const Params p = cdev[b.cs].p;
+    const int turb = cdev[b.cs].turb;
     double* V[7];
     for (int m = 0; m < 7; ++m) V[m] = slot(b, S_V + m);
     double* PP = slot(b, S_PP);
@@ -367,10 +374,11 @@ __global__ void k_mirror(const DevBlock* __restrict__ blks, int nblk, long long 
 // Space/DIFF_DqDxyz.F90:25-74, 232-265, 300-381 (gradients and shock sensor, interior cells)
 // ---------------------------------------------------------------------------------------
 template <typename R>
-__global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, int turb) {
+__global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
+    const int turb = cdev[b.cs].turb;
     int n = t.start + threadIdx.x;
     int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     int c = cidx(b, I, J, K);
@@ -432,7 +440,7 @@ __global__ void k_shock_ghost(const DevBlock* __restrict__ blks, const Tile* __r
 
 // BC_Boundarys(0): gradients of the first ghost layer (BC/*.F90 sweep 0, BC/BC_P2P.F90:140-184)
 template <typename R>
-__global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n, int turb) {
+__global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
     const BCEntry E = ent[e];
@@ -475,10 +483,13 @@ __global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __re
 //   Space/CONVECT_Roe_Original.F90 | Space/CONVECT_AUSMPW_Plus.F90, Space/TURBTWO_CONVECT_Upwind.F90
 // ---------------------------------------------------------------------------------------
 template <typename R, int DIR>
-__global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, ParamsT<R> p, int turb) {
+__global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
+                                                          const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
+    const ParamsT<R> p = cparams<R>(cdev[b.cs]);
+    const int turb = cdev[b.cs].turb;
     int n = t.start + threadIdx.x;
     const int ni = DIR == 1 ? b.NI : b.NI1, nj = DIR == 2 ? b.NJ : b.NJ1;
     int i = n % ni + 1, j = (n / ni) % nj + 1, k = n / (ni * nj) + 1;
@@ -670,10 +681,11 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ 
 //   D = 0 - Fv(i) + Fv(i+1) - Fv(j) + Fv(j+1) - Fv(k) + Fv(k+1) - Fc(i) + Fc(i+1) - ...
 // ---------------------------------------------------------------------------------------
 template <typename R>
-__global__ void k_gather(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, int turb) {
+__global__ void k_gather(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
+    const int turb = cdev[b.cs].turb;
     int n = t.start + threadIdx.x;
     int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     int c = cidx(b, I, J, K);
@@ -726,10 +738,12 @@ __device__ inline R sst_fc1(const ParamsT<R>& p, const DevBlock& b, int c) {
 }
 
 template <typename R>
-__global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, ParamsT<R> p) {
+__global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
+    if (!cdev[b.cs].turb || cdev[b.cs].p.Kind_Hybrid != 3) return;     // only the DES cases need F1
+    const ParamsT<R> p = cparams<R>(cdev[b.cs]);
     int n = t.start + threadIdx.x;
     int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     int c = cidx(b, I, J, K);
@@ -743,15 +757,17 @@ __global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restr
 // ---------------------------------------------------------------------------------------
 template <typename R>
 __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, const int* __restrict__ nbp,
-                             R* __restrict__ rec, R* __restrict__ dq, long long N, Params pd, ParamsT<R> p, int turb) {
+                             R* __restrict__ rec, R* __restrict__ dq, long long N, const CaseDev* __restrict__ cdev) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= N) return;
     const SweepCell sc = cells[q];
     const DevBlock b = blks[sc.blk];
+    const Params pd = cdev[b.cs].p;
+    const ParamsT<R> p = cparams<R>(cdev[b.cs]);
+    const int turb = cdev[b.cs].turb;
     const int I = sc.i, J = sc.j, K = sc.k;
     const int nlex = (I - 1) + b.NI1 * ((J - 1) + b.NJ1 * (K - 1));     // lexicographic interior index
     const int c = cidx(b, I, J, K);
-    const size_t nc = (size_t)b.ncell;
     auto REC = [&](int m) -> R& { return rec[sw_at(q, m, NREC)]; };
     auto DQ = [&](int L) -> R& { return dq[sw_at(q, L, DQ_STRIDE)]; };
     // BDF2 right-hand side and the mean-flow diagonal, in FP64 in both paths
@@ -768,26 +784,10 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell*
     double rsum = slot(b, S_RDS)[c] + slot(b, S_RDS + 1)[c] + slot(b, S_RDS + 2)[c];
     double fm = 1.0 + rsum * cvs;
     REC(REC_FM) = R(fm);
-    {   // Jacobian terms and spectral radii of the lower and upper neighbours (nbp < 0: none)
-        const R* sv = rs<R>(b, S_SVEL);
-        const R* PPr = rs<R>(b, S_PP);
-        const R* RIr = rs<R>(b, S_RINV);
-        const int st[3] = {1, b.PI, b.PI * b.PJ};
-        for (int side = 0; side < 2; ++side)
-            for (int d = 0; d < 3; ++d) {
-                if (nbp[sw_at(q, 3 * side + d, 6)] < 0) continue;
-                const int nb = side == 0 ? c - st[d] : c + st[d];
-                const R* asd = rs<R>(b, S_ASD + 3 * d);
-                R Jt[NJAC];
-                jac_terms<R>(sv[nb], sv[nb + nc], sv[nb + 2 * nc], asd[nb], asd[nb + nc], asd[nb + 2 * nc], PPr[nb], RIr[nb], Jt);
-                const int base = (side == 0 ? REC_JL : REC_JU) + NJAC * d;
-                for (int m = 0; m < NJAC; ++m) REC(base + m) = Jt[m];
-                REC((side == 0 ? REC_RDSL : REC_RDSU) + d) = rs<R>(b, S_RDS + d)[nb];
-            }
-    }
-    if (!turb) {
+    if (!turb) {            // the k-omega lanes of the sweeps then produce zeros
         DQ(5) = rs<R>(b, S_D + 5)[c];
         DQ(6) = rs<R>(b, S_D + 6)[c];
+        REC(REC_FT) = R(1.0);
         return;
     }
     for (int L = 5; L < 7; ++L)
@@ -868,6 +868,41 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell*
     REC(REC_FT) = R(fm) + (CnegTk + CnegTO) * R(stept);
 }
 
+// The neighbours' Jacobian terms and spectral radii of the sweep records: 6 threads per
+// position (one per neighbour) compute into shared memory, then the block writes its 32
+// consecutive records as one contiguous, coalesced range (the diagonal entries excepted,
+// which k_lusgs_prep writes).  A missing neighbour (nbp < 0) leaves its entries unused.
+template <typename R>
+__global__ void __launch_bounds__(6 * 32) k_lusgs_jac(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells,
+                                                      const int* __restrict__ nbp, R* __restrict__ rec, long long N) {
+    __shared__ R stage[32][6 * NBREC];
+    const long long q0 = (long long)blockIdx.x * 32;
+    const int t = threadIdx.x, r = t / 6, k = t % 6;
+    const long long q = q0 + r;
+    if (q < N && nbp[sw_at(q, k, 6)] >= 0) {
+        const SweepCell sc = cells[q];
+        const DevBlock b = blks[sc.blk];
+        const int c = cidx(b, sc.i, sc.j, sc.k);
+        const size_t nc = (size_t)b.ncell;
+        const int d = k % 3;
+        const int st = d == 0 ? 1 : (d == 1 ? b.PI : b.PI * b.PJ);
+        const int nb = k < 3 ? c - st : c + st;
+        const R* sv = rs<R>(b, S_SVEL);
+        const R* asd = rs<R>(b, S_ASD + 3 * d);
+        R Jt[NJAC];
+        jac_terms<R>(sv[nb], sv[nb + nc], sv[nb + 2 * nc], asd[nb], asd[nb + nc], asd[nb + 2 * nc], rs<R>(b, S_PP)[nb],
+                     rs<R>(b, S_RINV)[nb], Jt);
+        for (int m = 0; m < NJAC; ++m) stage[r][NBREC * k + m] = Jt[m];
+        stage[r][NBREC * k + NJAC] = rs<R>(b, S_RDS + d)[nb];
+    }
+    __syncthreads();
+    const long long nq = N - q0 < 32 ? N - q0 : 32;
+    for (int e = t; e < nq * NREC; e += blockDim.x) {
+        const int rr = e / NREC, m = e % NREC;
+        if (m < 6 * NBREC) rec[sw_at(q0 + rr, m, NREC)] = stage[rr][m];
+    }
+}
+
 // ---------------------------------------------------------------------------------------
 // LU-SGS sweeps (Time/TIME_LUSGS.F90:172-675, Time/TURBTWO_TIME_LUSGS_SST.F90:562-766) on the
 // i+j+k hyperplanes of every block.  Any order of the (i-1,j-1,k-1) dependency graph
@@ -883,7 +918,6 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
                                   int L, int turb) {
     if (L >= 7 || (L >= 5 && !turb)) return;
     const int side = LOWER ? 0 : 3;
-    const int jb = LOWER ? REC_JL : REC_JU, rb = LOWER ? REC_RDSL : REC_RDSU;
     const R sgn = LOWER ? R(1.0) : R(-1.0);
     auto REC = [&](int m) { return rec[sw_at(q, m, NREC)]; };
     // all loads of the three neighbours are issued together: a missing neighbour (nbp < 0)
@@ -896,8 +930,8 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
     for (int d = 0; d < 3; ++d) {
         const bool has = npv[d] >= 0;
         const long long np = has ? npv[d] : q;
-        const int jd = jb + NJAC * d;
-        const R RDSt = REC(rb + d);
+        const int jd = NBREC * (side + d);
+        const R RDSt = REC(jd + NJAC);
         R val;
         // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1 line)
         if (L < 5) {
@@ -991,6 +1025,62 @@ __global__ void k_sweep_all(const int* __restrict__ nbp, const R* __restrict__ r
     }
 }
 
+// Both sweeps as one dataflow over all positions (one cooperative launch): item (q, L) starts
+// as soon as its three neighbours of the previous hyperplane have published their DeltaQ
+// (flag[q'] counts the 7 lanes of q' that have written), instead of waiting for the whole
+// hyperplane.  Items go to threads round-robin in sweep order (L sweep ascending, then U
+// descending), so a thread only ever waits on items that come earlier in that order: with the
+// whole grid resident nothing can wait forever.  Every wait is bounded; on expiry the kernel
+// records an error and all threads leave.
+template <typename R>
+__device__ inline bool flow_wait(const int* flag, long long q, int want, SweepSync* sy, unsigned limit) {
+    const volatile int* f = flag + q;
+    unsigned it = 0;
+    while (*f < want) {
+        if ((++it & 255) == 0 && *((volatile int*)&sy->err)) return false;
+        if (it > limit) { atomicExch(&sy->err, 2); return false; }
+        __nanosleep(32);
+    }
+    __threadfence();
+    return true;
+}
+
+template <typename R>
+__global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int* flagL, int* flagU,
+                             SweepSync* sy, unsigned limit) {
+    const long long T = (long long)gridDim.x * blockDim.x;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long items = N * SWEEP_LANES;
+    for (long long it = t; it < items; it += T) {                  // L sweep, ascending
+        const long long q = it / SWEEP_LANES;
+        const int L = (int)(it % SWEEP_LANES);
+        if (L >= 7) continue;
+        bool ok = true;
+        for (int d = 0; d < 3 && ok; ++d) {
+            const long long np = nbp[sw_at(q, d, 6)];
+            if (np >= 0) ok = flow_wait<R>(flagL, np, 7, sy, limit);
+        }
+        if (!ok) return;
+        sweep_item<R, true>(nbp, rec, dq, N, q, L, 1);
+        __threadfence();
+        atomicAdd(flagL + q, 1);
+    }
+    for (long long it = t; it < items; it += T) {                  // U sweep, descending
+        const long long q = N - 1 - it / SWEEP_LANES;
+        const int L = (int)(it % SWEEP_LANES);
+        if (L >= 7) continue;
+        bool ok = flow_wait<R>(flagL, q, 7, sy, limit);             // own L result
+        for (int d = 0; d < 3 && ok; ++d) {
+            const long long np = nbp[sw_at(q, 3 + d, 6)];
+            if (np >= 0) ok = flow_wait<R>(flagU, np, 7, sy, limit);
+        }
+        if (!ok) return;
+        sweep_item<R, false>(nbp, rec, dq, N, q, L, 1);
+        __threadfence();
+        atomicAdd(flagU + q, 1);
+    }
+}
+
 // DeltaQ back to the cells (the update and trans_get_field read it there)
 template <typename R>
 __global__ void k_sweep_scatter(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, const R* __restrict__ dq,
@@ -1007,10 +1097,12 @@ __global__ void k_sweep_scatter(const DevBlock* __restrict__ blks, const SweepCe
 // ---------------------------------------------------------------------------------------
 // Time/TIME_Update_V.F90:106-294 (norms) and :502-859 (update), FP64 in both paths
 // ---------------------------------------------------------------------------------------
-__global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, Params p, int turb_upd,
+__global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const CaseDev* __restrict__ cdev,
                          NormPart* __restrict__ parts, int d_fp32) {
     const Tile t = tiles[blockIdx.x];
     const DevBlock b = blks[t.blk];
+    const Params p = cdev[b.cs].p;
+    const int turb_upd = cdev[b.cs].turb_upd;
     __shared__ double s_sum[3][256];
     __shared__ double s_max[3][256];
     __shared__ long long s_idx[256];
@@ -1121,10 +1213,12 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
 }
 
 // Time/TIME_Update_U.F90:16-44
-__global__ void k_update_u(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, int kind_dual) {
+__global__ void k_update_u(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
+    const int kind_dual = cdev[b.cs].p.Kind_Dual;
+    if (kind_dual == 0) return;
     int n = t.start + threadIdx.x;
     int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     int c = cidx(b, I, J, K);

@@ -12,35 +12,39 @@ struct SweepSync;
 struct SweepView;
 
 // FP64 kernels shared by both precision modes
-void launch_specrad(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, double CFL_sub);
-void launch_bc_state(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, const Params& p, int turb);
+void launch_specrad(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev);
+void launch_bc_state(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int n, const CaseDev* cdev);
 void launch_bc_outlet(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const OutletLine* lines, int nl,
-                      const Params& p, int turb);
+                      const CaseDev* cdev);
 void launch_prims(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
-void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const Params& p, int turb_upd, NormPart* parts,
+void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts,
                    int d_fp32);
 void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml);
-void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, int kind_dual);
+void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev);
 void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, int lb, int is_sd, double* stage, int to_slots);
 double probe_fma_gflops(int fp64);
 void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
 
 // flux, source and sweep kernels, instantiated per arithmetic type
 struct FluxLaunchers {
-    void (*gradient)(cudaStream_t, const DevBlock*, const Tile*, int, int turb);
+    void (*gradient)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
     void (*shock_ghost)(cudaStream_t, const DevBlock*, const Tile*, int);
-    void (*bc_grad)(cudaStream_t, const DevBlock*, const BCEntry*, int, int turb);
-    void (*face_flux[3])(cudaStream_t, const DevBlock*, const Tile*, int, const Params&, int);
-    void (*gather)(cudaStream_t, const DevBlock*, const Tile*, int, int);
-    void (*sst_fc1)(cudaStream_t, const DevBlock*, const Tile*, int, const Params&);
+    void (*bc_grad)(cudaStream_t, const DevBlock*, const BCEntry*, int);
+    void (*face_flux[3])(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
+    void (*gather)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
+    void (*sst_fc1)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
     // LU-SGS right-hand sides + neighbour Jacobian terms into the sweep-order arrays
-    void (*prep)(cudaStream_t, const DevBlock*, const SweepView&, const Params&, int turb);
+    void (*prep)(cudaStream_t, const DevBlock*, const SweepView&, const CaseDev*);
+    void (*jac)(cudaStream_t, const DevBlock*, const SweepView&);     // neighbours' Jacobian terms
     void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int turb);
     void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int turb);
     // both sweeps in one cooperative launch (grid must be co-resident: grid <= SMs x occupancy)
     cudaError_t (*sweep_all)(cudaStream_t, const SweepView&, const int* plane_off, int nplanes, int turb, SweepSync*,
                              int grid, int block);
     int (*sweep_all_occupancy)(int block);          // resident blocks per SM
+    // both sweeps as a dataflow over per-position ready flags (one cooperative launch)
+    cudaError_t (*sweep_flow)(cudaStream_t, const SweepView&, int* flagL, int* flagU, SweepSync*, int grid, int block);
+    int (*sweep_flow_occupancy)(int block);
     void (*scatter)(cudaStream_t, const DevBlock*, const SweepView&);     // DeltaQ back to cell order
     size_t elem;                                    // bytes of the sweep arithmetic type
 };
@@ -50,5 +54,5 @@ const FluxLaunchers& flux_launchers_f32();
 constexpr int CELL_TILE = 256;
 constexpr int FACE_TILE = 128;
 constexpr int SWEEP_CTA = 128;
-constexpr unsigned SWEEP_SPIN_LIMIT = 1u << 22;     // polls of one grid barrier before it gives up (~1 s)
+constexpr unsigned SWEEP_SPIN_LIMIT = 1u << 22;     // polls of one wait before it gives up (~1 s)
 }  // namespace tg

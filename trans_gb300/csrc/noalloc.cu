@@ -1,0 +1,64 @@
+// noalloc.cu -- TIME_Update_V with its per-tile norm partials in a fixed device buffer.
+//
+// The buffer is a file-scope __device__ array, part of the loaded library image: the call
+// makes no device allocation of any kind.  Its address is taken once per device with
+// cudaGetSymbolAddress, with that device current, on the first call made on it (so that first
+// call should come before any stream capture), and handed to the kernel as a plain pointer.
+// All contexts and calls share the array and it keeps the last call's contents; every entry a
+// call reads is written earlier in the same call, so nothing needs clearing.  Calls that
+// overlap (two host threads, or two contexts whose streams run concurrently) race on it.
+#include <algorithm>
+#include <mutex>
+#include <string>
+
+#include "engine.h"
+
+using namespace tg;
+using namespace tg::eng;
+
+namespace {
+constexpr int kStaticNormTiles = 65536;              // 16,777,216 interior cells; 4 MiB
+static __device__ __align__(256) NormPart g_norm_scratch[kStaticNormTiles];
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+NormPart* g_scratch_ptr[kMaxDevices] = {};
+
+int static_norm_scratch(Ctx* c, NormPart** out) {
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(c, TRANS_E_ARG, "device ordinal beyond the static scratch table");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_norm_scratch);
+        if (e != cudaSuccess)
+            return fail(c, TRANS_E_CUDA, std::string("cudaGetSymbolAddress(static norm scratch): ") + cudaGetErrorString(e));
+        g_scratch_ptr[dev] = static_cast<NormPart*>(ptr);
+    }
+    *out = g_scratch_ptr[dev];
+    return TRANS_OK;
+}
+}  // namespace
+
+extern "C" int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || c->cases.empty()) return TRANS_E_ARG;
+    int rc;
+    if (!c->built && (rc = rebuild(c))) return rc;
+    if (c->cell_tiles.size() > (size_t)kStaticNormTiles)
+        return fail(c, TRANS_E_ARG, "trans_update_static_scratch: " + std::to_string(c->cell_tiles.size()) +
+                    " cell tiles exceed the static scratch of 65536 tiles (16,777,216 interior cells)");
+    NormPart* scratch = nullptr;
+    if ((rc = static_norm_scratch(c, &scratch))) return rc;
+    for (CaseRec* cs : c->cases) cs->KI = ki;
+    if ((rc = finalize_geometry(c))) return rc;
+    if ((rc = upload_cdev(c))) return rc;
+    launch_update(c->stream, c->d_blk, c->d_cell, (int)c->cell_tiles.size(), c->d_cdev, scratch, c->mixed ? 1 : 0);
+    c->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->h_parts.data(), scratch, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    rc = reduce_norms(c);
+    if (norms) std::copy(c->cases[0]->norms.begin(), c->cases[0]->norms.end(), norms);
+    return rc;
+}

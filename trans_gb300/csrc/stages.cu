@@ -1,0 +1,433 @@
+// stages.cu -- one outer iteration of every case of a context, stage by stage in the order of
+// main.F90:54-197, with the LU-SGS sweep schedules, the residual norms and field transfer.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <initializer_list>
+#include <utility>
+
+#include "engine.h"
+
+namespace tg {
+namespace eng {
+
+namespace {
+
+struct FieldMap { int slot; int ncomp; int lb; };
+FieldMap field_map(int f) {
+    switch (f) {
+        case TRANS_V: return {S_V, 7, -2};
+        case TRANS_PP: return {S_PP, 1, -2};
+        case TRANS_T: return {S_T, 1, -2};
+        case TRANS_RMIU: return {S_RMIU, 1, -2};
+        case TRANS_WT0: return {S_WT0, 7, 1};
+        case TRANS_WT1: return {S_WT1, 7, 1};
+        case TRANS_SD: return {S_SD, 9, -2};
+        case TRANS_GRAD: return {S_GRAD, 3, -2};
+        case TRANS_VOL: return {S_VOL, 1, -2};
+        case TRANS_ALAGM: return {S_ALAGM, 3, -2};
+        case TRANS_DST: return {S_DST, 1, -2};
+        case TRANS_ALENG: return {S_ALENG, 1, -2};
+        case TRANS_ASENG: return {S_ASENG, 1, 1};
+        case TRANS_XC: return {S_XC, 1, 0};
+        case TRANS_YC: return {S_YC, 1, 0};
+        case TRANS_ZC: return {S_ZC, 1, 0};
+        case TRANS_RAD: return {S_RAD, 1, -2};
+        case TRANS_THTC: return {S_THTC, 1, -2};
+        case TRANS_D: return {S_D, 7, 0};
+        case TRANS_RDS: return {S_RDS, 3, 0};
+        case TRANS_DTM: return {S_DTM, 1, 1};
+        case TRANS_DQDXYZ: return {S_DQ, 18, -1};
+        case TRANS_SHOCK: return {S_SHOCK, 1, -2};
+        default: return {-1, 0, 0};
+    }
+}
+
+bool is_geometry(int f) { return f >= TRANS_SD && f <= TRANS_THTC; }
+
+// FP32 copies of slot ranges {first, count} of every block (mixed path); to_fp64 copies back
+void mirror(Ctx* c, std::initializer_list<std::pair<int, int>> ranges, int to_fp64 = 0) {
+    MirrorList ml;
+    std::memset(&ml, 0, sizeof(ml));
+    ml.to_fp64 = to_fp64;
+    for (auto& r : ranges) { ml.first[ml.n] = r.first; ml.count[ml.n] = r.second; ml.n++; }
+    launch_mirror(c->stream, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off, ml);
+    c->launches++;
+}
+
+}  // namespace
+
+int finalize_geometry(Ctx* c) {
+    bool dirty = false;
+    for (CaseRec* cs : c->cases) dirty |= cs->geom_dirty;
+    if (!dirty) return TRANS_OK;
+    launch_geom_static(c->stream, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off);
+    c->launches++;
+    if (c->mixed) mirror(c, {{S_SD, S_WALL + 3 - S_SD}});
+    CK(cudaGetLastError());
+    for (CaseRec* cs : c->cases) cs->geom_dirty = false;
+    return TRANS_OK;
+}
+
+namespace {
+
+// switches of one case for its current KI (Time/SpectralRadius.F90:159-160, main.F90:60-64)
+CaseDev case_dev(const CaseRec* cs) {
+    const trans_params& p = cs->p;
+    CaseDev d;
+    std::memset(&d, 0, sizeof(d));
+    d.p = cs->dp;
+    d.pf = params_as<float>(cs->dp);
+    double CFL_sub = p.CFL_Sub_start + (p.CFL_Sub_end - p.CFL_Sub_start) * (double)(cs->KI - p.KI_ini) / (double)p.CFL_Sub_step;
+    d.CFL_sub = std::min(CFL_sub, p.CFL_Sub_end);
+    d.turb = (p.IF_Euler == 0 && p.IF_Turb_org == 1 && (cs->KI >= p.KItm || p.Kind_Hybrid > 0)) ? 1 : 0;
+    d.turb_upd = (p.IF_Euler == 0 && d.turb == 1 && cs->KI >= p.KItm) ? 1 : 0;
+    return d;
+}
+
+}  // namespace
+
+int upload_cdev(Ctx* c) {
+    const size_t n = c->cases.size();
+    std::vector<CaseDev> now(n);
+    for (size_t k = 0; k < n; ++k) now[k] = case_dev(c->cases[k]);
+    if (c->cdev_last.size() == n && std::memcmp(now.data(), c->cdev_last.data(), n * sizeof(CaseDev)) == 0) return TRANS_OK;
+    CK(cudaStreamSynchronize(c->stream));          // the pinned copy may still be in flight
+    std::memcpy(c->h_cdev, now.data(), n * sizeof(CaseDev));
+    CK(cudaMemcpyAsync(c->d_cdev, c->h_cdev, n * sizeof(CaseDev), cudaMemcpyHostToDevice, c->stream));
+    c->cdev_last = now;
+    return TRANS_OK;
+}
+
+namespace {
+
+bool any_case(const Ctx* c, bool (*pred)(const CaseRec*)) {
+    for (const CaseRec* cs : c->cases)
+        if (pred(cs)) return true;
+    return false;
+}
+
+}  // namespace
+
+// Per-block norms from the per-tile partials in c->h_parts, summed in tile order
+// (deterministic), then handed to the blocks' cases.
+int reduce_norms(Ctx* c) {
+    int nan = 0;
+    for (size_t b = 0; b < c->blk.size(); ++b) {
+        trans_norms& N = c->norms[b];
+        double sa = 0, sk = 0, so = 0, ma = -1, mk = 0, mo = 0;
+        long long ia = 0;
+        int bnan = 0;
+        for (size_t t = 0; t < c->cell_tiles.size(); ++t) {
+            if (c->cell_tile_blk[t] != (int)b) continue;
+            const NormPart& P = c->h_parts[t];
+            sa += P.sa; sk += P.sk; so += P.so;
+            if (P.ma > ma || (P.ma == ma && P.ia > ia)) { ma = P.ma; ia = P.ia; }
+            mk = std::max(mk, P.mk); mo = std::max(mo, P.mo);
+            bnan |= P.nan;
+        }
+        const DevBlock& B = c->blk[b];
+        N.DRSa = std::sqrt(sa / B.NI1 / B.NJ1 / B.NK1);
+        N.DRSk = std::sqrt(sk / B.NI1 / B.NJ1 / B.NK1);
+        N.DRSo = std::sqrt(so / B.NI1 / B.NJ1 / B.NK1);
+        N.DUa = ma; N.DUk = mk; N.DUo = mo;
+        N.Ima = (int)(ia % B.NI1) + 1; N.Jma = (int)((ia / B.NI1) % B.NJ1) + 1; N.Kma = (int)(ia / ((long long)B.NI1 * B.NJ1)) + 1;
+        N.nan_flag = bnan;
+        nan |= bnan;
+    }
+    for (CaseRec* cs : c->cases)
+        std::copy(c->norms.begin() + cs->blk0, c->norms.begin() + cs->blk0 + cs->blk.size(), cs->norms.begin());
+    if (nan) return fail(c, TRANS_E_NAN, "NaN in the density increment");
+    return TRANS_OK;
+}
+
+int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
+    if (!c || !cs || ib < 0 || ib >= (int)cs->blk.size() || !host) return TRANS_E_ARG;
+    if (!c->built) {
+        int rc = rebuild(c);
+        if (rc) return rc;
+    }
+    FieldMap fm = field_map(f);
+    if (fm.slot < 0) return fail(c, TRANS_E_ARG, "bad field id");
+    const DevBlock& b = c->blk[cs->blk0 + ib];
+    size_t ncells = (size_t)(b.NI + 3 - fm.lb) * (b.NJ + 3 - fm.lb) * (b.NK + 3 - fm.lb);
+    size_t bytes = ncells * fm.ncomp * sizeof(double);
+    cudaStream_t s = c->stream;
+    int is_sd = f == TRANS_SD ? 1 : 0;
+    if (upload) {
+        CK(cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, s));
+        launch_field_xfer(s, b, fm.slot, fm.ncomp, fm.lb, is_sd, c->d_stage, 1);
+        c->launches++;
+        if (f == TRANS_THTC) {      // sin/cos of the outlet recurrence, evaluated once on the host
+            std::vector<double> sn(ncells), co(ncells);
+            for (size_t q = 0; q < ncells; ++q) { sn[q] = std::sin(host[q]); co[q] = std::cos(host[q]); }
+            CK(cudaMemcpyAsync(c->d_stage, sn.data(), ncells * sizeof(double), cudaMemcpyHostToDevice, s));
+            launch_field_xfer(s, b, S_SINT, 1, fm.lb, 0, c->d_stage, 1);
+            CK(cudaMemcpyAsync(c->d_stage, co.data(), ncells * sizeof(double), cudaMemcpyHostToDevice, s));
+            launch_field_xfer(s, b, S_COST, 1, fm.lb, 0, c->d_stage, 1);
+            CK(cudaStreamSynchronize(s));
+        }
+        if (is_geometry(f)) cs->geom_dirty = true;
+        if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}});
+        if (c->mixed && f == TRANS_DQDXYZ) mirror(c, {{S_DQ, 18}});
+        if (c->mixed && f == TRANS_SHOCK) mirror(c, {{S_SHOCK, 1}});
+    } else {
+        // the mixed path keeps DeltaQ, the gradients and the shock sensor in FP32
+        if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}}, 1);
+        if (c->mixed && f == TRANS_DQDXYZ) mirror(c, {{S_DQ, 18}}, 1);
+        if (c->mixed && f == TRANS_SHOCK) mirror(c, {{S_SHOCK, 1}}, 1);
+        launch_field_xfer(s, b, fm.slot, fm.ncomp, fm.lb, is_sd, c->d_stage, 0);
+        c->launches++;
+        CK(cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    return TRANS_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// LU-SGS sweep schedules (all compute every DeltaQ with the same operations)
+// ---------------------------------------------------------------------------------------
+namespace {
+
+int sweep_once(Ctx* c, int mode, int grid, int block) {
+    cudaStream_t s = c->stream;
+    const int nh = (int)c->plane_off.size() - 1;
+    if (mode == 2) {
+        const size_t np = (size_t)((c->sv.n + 31) / 32 * 32);
+        CK(cudaMemsetAsync(c->d_flags, 0, 2 * np * sizeof(int), s));
+        CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
+        CK(c->fl->sweep_flow(s, c->sv, c->d_flags, c->d_flags + np, c->d_sync, grid, block));
+        CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
+        c->launches++;
+        return TRANS_OK;
+    }
+    if (mode == 1) {
+        CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
+        CK(c->fl->sweep_all(s, c->sv, c->d_plane_off, nh, 1, c->d_sync, grid, block));
+        CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
+        c->launches++;
+        return TRANS_OK;
+    }
+    // one launch per hyperplane, L ascending then U descending, replayed as one graph
+    if (!c->sweep_exec) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int h = 0; h < nh; ++h) {
+            int cnt = c->plane_off[h + 1] - c->plane_off[h];
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, 1);
+        }
+        for (int h = nh - 1; h >= 0; --h) {
+            int cnt = c->plane_off[h + 1] - c->plane_off[h];
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, 1);
+        }
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c->sweep_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph instantiate: ") + cudaGetErrorString(e));
+    }
+    CK(cudaGraphLaunch(c->sweep_exec, s));
+    for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
+    return TRANS_OK;
+}
+
+// keep a copy of the sweep-order DeltaQ (restore = copy it back)
+int save_dq(Ctx* c, bool restore) {
+    size_t bytes = (size_t)DQ_STRIDE * (size_t)((c->sv.n + 31) / 32 * 32) * c->fl->elem;
+    if (!c->d_dq_save) CK(cudaMalloc(&c->d_dq_save, bytes));
+    CK(cudaMemcpyAsync(restore ? c->sv.dq : c->d_dq_save, restore ? c->d_dq_save : c->sv.dq, bytes, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    return TRANS_OK;
+}
+
+// Schedule tuner: time every candidate schedule on the live right-hand side (DeltaQ saved and
+// restored around each trial), keep the fastest.
+int tune_sweeps(Ctx* c) {
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    struct Cand { int mode, grid, block; };
+    std::vector<Cand> cands = {{0, 0, 0}};
+    for (int block : {128, 256, 512}) {
+        int occ = c->fl->sweep_all_occupancy(block);
+        for (int per : {1, 2, 4})
+            if (per <= occ) cands.push_back({1, per * nsm, block});
+        int occf = c->fl->sweep_flow_occupancy(block);
+        if (block == 256 && occf >= 4) cands.push_back({2, 4 * nsm, block});
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    Cand pick = cands[0];
+    c->sweep_tuning.clear();
+    int rc = save_dq(c, false);
+    for (const Cand& k : cands) {
+        for (int rep = 0; rep < 2 && rc == TRANS_OK; ++rep) {      // first run warms up (graph build)
+            if ((rc = save_dq(c, true))) break;
+            CK(cudaEventRecord(e0, c->stream));
+            if ((rc = sweep_once(c, k.mode, k.grid, k.block))) break;
+            CK(cudaEventRecord(e1, c->stream));
+            CK(cudaEventSynchronize(e1));
+            if (k.mode != 0 && c->h_sync->err) { rc = -100; break; }
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep == 1) {
+                c->sweep_tuning += (k.mode ? std::string(k.mode == 1 ? "coop " : "flow ") + std::to_string(k.grid) + "x"
+                                                 + std::to_string(k.block) : std::string("planes"))
+                                   + ":" + std::to_string(ms) + "ms ";
+                if (ms < best) { best = ms; pick = k; }
+            }
+        }
+        if (rc == -100) rc = TRANS_OK;         // a schedule that timed out is just not picked
+        if (rc) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = save_dq(c, true))) return rc;
+    c->sweep_mode = pick.mode; c->sweep_grid = pick.grid; c->sweep_block = pick.block;
+    return TRANS_OK;
+}
+
+int run_sweeps(Ctx* c) {
+    if (c->sweep_mode < 0) {
+        int rc = tune_sweeps(c);
+        if (rc) return rc;
+    }
+    return sweep_once(c, c->sweep_mode, c->sweep_grid, c->sweep_block);
+}
+
+bool wants_des(const CaseRec* cs) { return cs->p.Kind_Hybrid == 3; }
+bool wants_dual(const CaseRec* cs) { return cs->p.Kind_Dual != 0; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// One hot-path subroutine over every block of every case (trans_run_stage)
+// ---------------------------------------------------------------------------------------
+int run_stage(Ctx* c, int stage, int itr) {
+    (void)itr;
+    if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
+    int rc;
+    if (!c->built && (rc = rebuild(c))) return rc;
+    if ((rc = finalize_geometry(c))) return rc;
+    cudaStream_t s = c->stream;
+    const int nct = (int)c->cell_tiles.size();
+    switch (stage) {
+        case TRANS_STAGE_SPECRAD: {
+            if ((rc = upload_cdev(c))) return rc;
+            KScope t(c, K_SPECRAD);
+            launch_specrad(s, c->d_blk, c->d_cell, nct, c->d_cdev);
+            c->launches++;
+            break;
+        }
+        case TRANS_STAGE_BC_STATE:
+            if ((rc = upload_cdev(c))) return rc;
+            { KScope t(c, K_BC_STATE); launch_bc_state(s, c->d_blk, c->d_bc, (int)c->bc.size(), c->d_cdev); }
+            { KScope t(c, K_BC_OUTLET); launch_bc_outlet(s, c->d_blk, c->d_outlet, c->d_lines, (int)c->lines.size(), c->d_cdev); }
+            c->launches += 1 + (c->lines.empty() ? 0 : 1);
+            break;
+        case TRANS_STAGE_GRADIENT:
+            if ((rc = upload_cdev(c))) return rc;
+            { KScope t(c, K_PRIMS); launch_prims(s, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off); }
+            // the FP32 kernels read FP32 copies of this sub-iteration's state, primitives and radii
+            if (c->mixed) { KScope t(c, K_MIRROR); mirror(c, {{S_V, 10}, {S_RDS, 4}, {S_PRIM, 5}, {S_RINV, 4}}); }
+            { KScope t(c, K_GRADIENT); c->fl->gradient(s, c->d_blk, c->d_cell, nct, c->d_cdev); }
+            { KScope t(c, K_SHOCK_GHOST); c->fl->shock_ghost(s, c->d_blk, c->d_ghost, (int)c->ghost_tiles.size()); }
+            c->launches += 3;
+            break;
+        case TRANS_STAGE_BC_GRAD:
+            { KScope t(c, K_BC_GRAD); c->fl->bc_grad(s, c->d_blk, c->d_bc, (int)c->bc.size()); }
+            c->launches++;
+            break;
+        case TRANS_STAGE_RESIDUAL:
+            if ((rc = upload_cdev(c))) return rc;
+            for (int d = 0; d < 3; ++d) {
+                KScope t(c, K_FACE);
+                c->fl->face_flux[d](s, c->d_blk, c->d_face[d], (int)c->face_tiles[d].size(), c->d_cdev);
+            }
+            { KScope t(c, K_GATHER); c->fl->gather(s, c->d_blk, c->d_cell, nct, c->d_cdev); }
+            c->launches += 4;
+            break;
+        case TRANS_STAGE_LUSGS: {
+            if ((rc = upload_cdev(c))) return rc;
+            if (any_case(c, wants_des)) {
+                KScope t(c, K_SST_FC1);
+                c->fl->sst_fc1(s, c->d_blk, c->d_cell, nct, c->d_cdev);
+                c->launches++;
+            }
+            { KScope t(c, K_PREP); c->fl->prep(s, c->d_blk, c->sv, c->d_cdev); c->fl->jac(s, c->d_blk, c->sv); }
+            c->launches += 2;
+            {
+                int nh = (int)c->plane_off.size() - 1, nl = 0;
+                for (int h = 0; h < nh; ++h) nl += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
+                KScope t(c, K_SWEEP, c->sweep_mode >= 1 ? 1 : nl);
+                if ((rc = run_sweeps(c))) return rc;
+            }
+            { KScope t(c, K_SCATTER); c->fl->scatter(s, c->d_blk, c->sv); }
+            c->launches++;
+            break;
+        }
+        case TRANS_STAGE_UPDATE: {
+            if ((rc = upload_cdev(c))) return rc;
+            { KScope t(c, K_UPDATE); launch_update(s, c->d_blk, c->d_cell, nct, c->d_cdev, c->d_parts, c->mixed ? 1 : 0); }
+            c->launches++;
+            CK(cudaMemcpyAsync(c->h_parts.data(), c->d_parts, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
+            if ((rc = reduce_norms(c))) return rc;
+            break;
+        }
+        case TRANS_STAGE_UPDATE_U:
+            if ((rc = upload_cdev(c))) return rc;
+            if (any_case(c, wants_dual)) {
+                KScope t(c, K_UPDATE_U);
+                launch_update_u(s, c->d_blk, c->d_cell, nct, c->d_cdev);
+                c->launches++;
+            }
+            break;
+        default:
+            return fail(c, TRANS_E_ARG, "bad stage");
+    }
+    CK(cudaGetLastError());
+    return TRANS_OK;
+}
+
+// One outer iteration (main.F90:54-171 + :192-197) of every case at its current KI.
+int run_iteration(Ctx* c) {
+    if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
+    const CaseRec* c0 = c->cases[0];
+    const int nsub = c0->p.Kind_Dual != 0 ? c0->p.Kchld : 1;
+    int rc;
+    for (int it = 1; it <= nsub; ++it)
+        for (int st = TRANS_STAGE_SPECRAD; st <= TRANS_STAGE_UPDATE; ++st)
+            if ((rc = run_stage(c, st, it))) return rc;
+    if ((rc = run_stage(c, TRANS_STAGE_UPDATE_U, nsub))) return rc;
+    for (CaseRec* cs : c->cases) {
+        if (cs->iters == 0) cs->first_norms = cs->norms;
+        cs->iters++;
+    }
+    return TRANS_OK;
+}
+
+int kernel_times(Ctx* c, double* ms, int* launches) {
+    for (int k = 0; k < NKCLASS; ++k) { ms[k] = 0.0; launches[k] = 0; }
+    c->ktime_on = true;
+    c->kev.clear();
+    int rc = run_iteration(c);
+    c->ktime_on = false;
+    cudaStreamSynchronize(c->stream);
+    for (auto& e : c->kev) {
+        float t = 0;
+        if (cudaEventElapsedTime(&t, e.a, e.b) == cudaSuccess) { ms[e.k] += t; launches[e.k] += e.n; }
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    c->kev.clear();
+    return rc;
+}
+
+}  // namespace eng
+}  // namespace tg

@@ -1,0 +1,265 @@
+// worklist.cu -- the work lists of a context, rebuilt whenever its set of cases changes:
+// tiles of interior cells and faces, the boundary gather tables built from the reference's
+// ConnectivityStruct, outlet lines, the i+j+k hyperplane order of the LU-SGS sweeps with the
+// neighbour positions, and the per-case parameter array the kernels read.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "engine.h"
+
+namespace tg {
+namespace eng {
+
+namespace {
+
+int upload_vec(Ctx* c, const void* h, size_t bytes, void** d) {
+    if (*d) { cudaFree(*d); *d = nullptr; }
+    if (bytes == 0) return TRANS_OK;
+    CK(cudaMalloc(d, bytes));
+    CK(cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice));
+    return TRANS_OK;
+}
+
+// Geom/startup.F90:1-25
+void ijk_start_end(int I, int J, int K, int& Is, int& Js, int& Ks, const int* TL, const int* TT, int lcross) {
+    int l1 = 1 - lcross;
+    int t1 = TL[0] * I + TL[1] * J + TL[2] * K;
+    int t2 = TL[0] * (J * l1 + K * lcross) + TL[1] * (I * l1 + K * lcross) + TL[2] * (I * l1 + J * lcross);
+    int t3 = TL[0] * (J * lcross + K * l1) + TL[1] * (I * lcross + K * l1) + TL[2] * (I * lcross + J * l1);
+    Is = TT[0] * t1 + (TT[1] + TT[2]) * t2;
+    Js = TT[1] * t1 + TT[0] * t2 + TT[2] * t3;
+    Ks = TT[2] * t1 + (TT[0] + TT[1]) * t3;
+}
+
+int block_index(const CaseRec* cs, int id) {
+    for (size_t n = 0; n < cs->hb.size(); ++n)
+        if (cs->hb[n].id == id) return (int)n;
+    return -1;
+}
+
+// Gather tables of BC_Boundarys (BC/Boundary.F90:22-47) for one case: one entry per boundary
+// face cell, in block / connection / (k,j,i) order; outlets in a separate table ordered line by
+// line.  Block indices are the context's (case's first block + local index).
+int build_bc(Ctx* c, const CaseRec* cs) {
+    const int g0 = cs->blk0;
+    for (size_t nb = 0; nb < cs->hb.size(); ++nb) {
+        const HostBlock& h = cs->hb[nb];
+        const DevBlock& b = cs->blk[nb];
+        for (size_t ic = 0; ic < h.conn.size(); ++ic) {
+            const trans_conn& a = h.conn[ic];
+            int kind = a.BCType;
+            if (kind != 1 && kind != 2 && kind != 3 && kind != 5 && kind != 7 && kind != 9)
+                return fail(c, TRANS_E_ARG, "unsupported BC kind " + std::to_string(kind));
+            int tb = -1;
+            const trans_conn* ta = nullptr;
+            if (kind == 9) {
+                tb = block_index(cs, a.TargetBlock);
+                if (tb < 0 || a.TargetConn < 1 || a.TargetConn > (int)cs->hb[tb].conn.size())
+                    return fail(c, TRANS_E_ARG, "bad 1-to-1 target");
+                ta = &cs->hb[tb].conn[a.TargetConn - 1];
+            }
+            {   // the face cells must lie on one face of the block, tangential indices interior
+                const int n3[3] = {b.NI, b.NJ, b.NK};
+                int d = a.IJKDirect - 1;
+                if (d < 0 || d > 2) return fail(c, TRANS_E_ARG, "bad IJKDirect");
+                for (int q = 0; q < 3; ++q) {
+                    int lo = a.pointStart[q], hi = a.pointEnd[q];
+                    bool ok = (q == d) ? (lo == hi && (lo == 1 || lo == n3[q])) : (lo >= 1 && hi <= n3[q] - 1 && lo <= hi);
+                    if (!ok) return fail(c, TRANS_E_ARG, "connection range outside the block");
+                }
+                if (b.NI1 < 3 || b.NJ1 < 3 || b.NK1 < 3) return fail(c, TRANS_E_ARG, "blocks need 3 interior cells per direction");
+            }
+            std::vector<BCEntry> seg;
+            for (int K = a.pointStart[2]; K <= a.pointEnd[2]; ++K)
+            for (int J = a.pointStart[1]; J <= a.pointEnd[1]; ++J)
+            for (int I = a.pointStart[0]; I <= a.pointEnd[0]; ++I) {
+                BCEntry E;
+                std::memset(&E, 0, sizeof(E));
+                E.kind = kind; E.blk = g0 + (int)nb; E.conn = (int)ic; E.i = I; E.j = J; E.k = K;
+                E.dir = a.IJKDirect; E.lor = a.LeftOrRight;
+                E.sub = (J == a.pointStart[1]) ? 1 : 0;
+                const int* E3[3] = {a.CEIJKAdd, a.CEIJKAdd1, a.CEIJKAdd2};
+                for (int L = 0; L < 3; ++L) E.l[L] = cidx(b, I + E3[L][0], J + E3[L][1], K + E3[L][2]);
+                E.face = cidx(b, I + a.IJKAdd[0], J + a.IJKAdd[1], K + a.IJKAdd[2]);
+                if (kind == 9) {
+                    int IIadd = a.pointEnd[0] - a.pointStart[0] + 2, JJadd = a.pointEnd[1] - a.pointStart[1] + 2;
+                    int KKadd = a.pointEnd[2] - a.pointStart[2] + 2;
+                    int iL = I - a.pointStart[0] + 1, jL = J - a.pointStart[1] + 1, kL = K - a.pointStart[2] + 1;
+                    iL = a.revMatrix[0] * IIadd + (1 - 2 * a.revMatrix[0]) * iL;
+                    jL = a.revMatrix[1] * JJadd + (1 - 2 * a.revMatrix[1]) * jL;
+                    kL = a.revMatrix[2] * KKadd + (1 - 2 * a.revMatrix[2]) * kL;
+                    int ib, jb, kb;
+                    ijk_start_end(iL, jL, kL, ib, jb, kb, a.Transform, a.TransformT, a.lcross);
+                    ib += ta->pointStart[0] - 1; jb += ta->pointStart[1] - 1; kb += ta->pointStart[2] - 1;
+                    const int* S3[3] = {ta->CIJKAdd, ta->CIJKAdd1, ta->CIJKAdd2};
+                    const DevBlock& r = cs->blk[tb];
+                    for (int L = 0; L < 3; ++L) {
+                        int ii = ib + S3[L][0], jj = jb + S3[L][1], kk = kb + S3[L][2];
+                        if (ii < 1 || ii > r.NI1 || jj < 1 || jj > r.NJ1 || kk < 1 || kk > r.NK1)
+                            return fail(c, TRANS_E_ARG, "1-to-1 source cell outside the target block");
+                        E.s[L] = cidx(r, ii, jj, kk);
+                    }
+                    E.src_blk = g0 + tb;
+                    E.cost = std::cos(a.rotateAngle);
+                    E.sint = std::sin(a.rotateAngle);
+                } else {
+                    const int* S3[3] = {a.CIJKAdd, a.CIJKAdd1, a.CIJKAdd2};
+                    for (int L = 0; L < 3; ++L) E.s[L] = cidx(b, I + S3[L][0], J + S3[L][1], K + S3[L][2]);
+                    E.src_blk = g0 + (int)nb;
+                    E.cost = 1.0; E.sint = 0.0;
+                }
+                seg.push_back(E);
+            }
+            c->bc.insert(c->bc.end(), seg.begin(), seg.end());
+            if (kind == 7) {
+                // lines along j: key = (k for i-faces, i for k-faces, cell for j-faces)
+                std::stable_sort(seg.begin(), seg.end(), [&](const BCEntry& x, const BCEntry& y) {
+                    int kx = a.IJKDirect == 1 ? x.k : (a.IJKDirect == 3 ? x.i : x.i + 100000 * x.k);
+                    int ky = a.IJKDirect == 1 ? y.k : (a.IJKDirect == 3 ? y.i : y.i + 100000 * y.k);
+                    if (kx != ky) return kx < ky;
+                    return x.j < y.j;
+                });
+                size_t q = 0;
+                while (q < seg.size()) {
+                    size_t r = q + 1;
+                    if (a.IJKDirect != 2)
+                        while (r < seg.size() && ((a.IJKDirect == 1 && seg[r].k == seg[q].k) || (a.IJKDirect == 3 && seg[r].i == seg[q].i))) ++r;
+                    OutletLine L;
+                    L.blk = g0 + (int)nb; L.first = (int)(c->outlet.size() + q); L.n = (int)(r - q); L.pad_ = 0;
+                    c->lines.push_back(L);
+                    q = r;
+                }
+                c->outlet.insert(c->outlet.end(), seg.begin(), seg.end());
+            }
+        }
+    }
+    return TRANS_OK;
+}
+
+void make_tiles(int nblk, const std::vector<long long>& counts, int tile, std::vector<Tile>& out, std::vector<int>* owner) {
+    for (int b = 0; b < nblk; ++b)
+        for (long long s = 0; s < counts[b]; s += tile) {
+            Tile t;
+            t.blk = b; t.start = (int)s; t.count = (int)std::min<long long>(tile, counts[b] - s); t.pad_ = 0;
+            out.push_back(t);
+            if (owner) owner->push_back(b);
+        }
+}
+
+}  // namespace
+
+int rebuild(Ctx* c) {
+    CK(cudaStreamSynchronize(c->stream));
+    free_worklists(c);
+    c->blk.clear(); c->cell_tiles.clear(); c->cell_tile_blk.clear(); c->ghost_tiles.clear();
+    for (int d = 0; d < 3; ++d) c->face_tiles[d].clear();
+    c->bc.clear(); c->outlet.clear(); c->lines.clear(); c->sweep.clear(); c->plane_off.clear();
+    c->cdev_last.clear();
+    if (c->cases.empty()) return TRANS_OK;
+    // blocks of all cases, in case order
+    for (size_t k = 0; k < c->cases.size(); ++k) {
+        CaseRec* cs = c->cases[k];
+        cs->blk0 = (int)c->blk.size();
+        for (DevBlock b : cs->blk) {
+            b.cs = (int)k;
+            c->blk.push_back(b);
+        }
+    }
+    const int nblk = (int)c->blk.size();
+    std::vector<long long> off(nblk);
+    long long acc = 0;
+    for (int n = 0; n < nblk; ++n) { off[n] = acc; acc += c->blk[n].ncell; }
+    c->total_cells = acc;
+    int rc;
+    if ((rc = upload_vec(c, c->blk.data(), sizeof(DevBlock) * nblk, (void**)&c->d_blk))) return rc;
+    if ((rc = upload_vec(c, off.data(), sizeof(long long) * nblk, (void**)&c->d_off))) return rc;
+    // tiles of interior cells, faces of each direction and face ghosts (shock extrapolation)
+    std::vector<long long> cnt(nblk), fcnt[3], gcnt(nblk);
+    for (int d = 0; d < 3; ++d) fcnt[d].resize(nblk);
+    for (int n = 0; n < nblk; ++n) {
+        const DevBlock& b = c->blk[n];
+        cnt[n] = b.nint;
+        fcnt[0][n] = (long long)b.NI * b.NJ1 * b.NK1;
+        fcnt[1][n] = (long long)b.NI1 * b.NJ * b.NK1;
+        fcnt[2][n] = (long long)b.NI1 * b.NJ1 * b.NK;
+        gcnt[n] = 6LL * ((long long)b.NJ1 * b.NK1 + (long long)b.NI1 * b.NK1 + (long long)b.NI1 * b.NJ1);
+    }
+    make_tiles(nblk, cnt, CELL_TILE, c->cell_tiles, &c->cell_tile_blk);
+    for (int d = 0; d < 3; ++d) make_tiles(nblk, fcnt[d], FACE_TILE, c->face_tiles[d], nullptr);
+    make_tiles(nblk, gcnt, CELL_TILE, c->ghost_tiles, nullptr);
+    if ((rc = upload_vec(c, c->cell_tiles.data(), sizeof(Tile) * c->cell_tiles.size(), (void**)&c->d_cell))) return rc;
+    for (int d = 0; d < 3; ++d)
+        if ((rc = upload_vec(c, c->face_tiles[d].data(), sizeof(Tile) * c->face_tiles[d].size(), (void**)&c->d_face[d]))) return rc;
+    if ((rc = upload_vec(c, c->ghost_tiles.data(), sizeof(Tile) * c->ghost_tiles.size(), (void**)&c->d_ghost))) return rc;
+    // boundary tables
+    for (CaseRec* cs : c->cases)
+        if ((rc = build_bc(c, cs))) return rc;
+    if ((rc = upload_vec(c, c->bc.data(), sizeof(BCEntry) * c->bc.size(), (void**)&c->d_bc))) return rc;
+    if ((rc = upload_vec(c, c->outlet.data(), sizeof(BCEntry) * c->outlet.size(), (void**)&c->d_outlet))) return rc;
+    if ((rc = upload_vec(c, c->lines.data(), sizeof(OutletLine) * c->lines.size(), (void**)&c->d_lines))) return rc;
+    // hyperplane order of the LU-SGS sweeps over all blocks of all cases: h = i+j+k = 3 ..
+    int hmax = 3;
+    for (auto& b : c->blk) hmax = std::max(hmax, b.NI1 + b.NJ1 + b.NK1);
+    c->plane_off.assign(1, 0);
+    for (int h = 3; h <= hmax; ++h) {
+        for (int n = 0; n < nblk; ++n) {
+            const DevBlock& b = c->blk[n];
+            for (int k = 1; k <= b.NK1; ++k)
+                for (int j = 1; j <= b.NJ1; ++j) {
+                    int i = h - j - k;
+                    if (i >= 1 && i <= b.NI1) c->sweep.push_back(SweepCell{n, i, j, k});
+                }
+        }
+        c->plane_off.push_back((int)c->sweep.size());
+    }
+    if ((rc = upload_vec(c, c->sweep.data(), sizeof(SweepCell) * c->sweep.size(), (void**)&c->d_sweep))) return rc;
+    if ((rc = upload_vec(c, c->plane_off.data(), sizeof(int) * c->plane_off.size(), (void**)&c->d_plane_off))) return rc;
+    {   // neighbour positions in sweep order: lower i,j,k (0..2) and upper (3..5), -1 = none
+        const long long N = (long long)c->sweep.size();
+        const long long Np = (N + 31) / 32 * 32;
+        std::vector<std::vector<int>> pos(nblk);
+        for (int n = 0; n < nblk; ++n) pos[n].assign((size_t)c->blk[n].nint, -1);
+        for (long long q = 0; q < N; ++q) {
+            const SweepCell& sc = c->sweep[q];
+            const DevBlock& b = c->blk[sc.blk];
+            pos[sc.blk][(size_t)(sc.i - 1) + (size_t)b.NI1 * ((sc.j - 1) + (size_t)b.NJ1 * (sc.k - 1))] = (int)q;
+        }
+        std::vector<int> nbp((size_t)6 * Np, -1);
+        for (long long q = 0; q < N; ++q) {
+            const SweepCell& sc = c->sweep[q];
+            const DevBlock& b = c->blk[sc.blk];
+            const int ijk[3] = {sc.i, sc.j, sc.k}, hi[3] = {b.NI1, b.NJ1, b.NK1};
+            for (int side = 0; side < 2; ++side)
+                for (int d = 0; d < 3; ++d) {
+                    int x[3] = {ijk[0], ijk[1], ijk[2]};
+                    x[d] += side == 0 ? -1 : 1;
+                    if (x[d] < 1 || x[d] > hi[d]) continue;
+                    nbp[sw_at(q, 3 * side + d, 6)] =
+                        pos[sc.blk][(size_t)(x[0] - 1) + (size_t)b.NI1 * ((x[1] - 1) + (size_t)b.NJ1 * (x[2] - 1))];
+                }
+        }
+        if ((rc = upload_vec(c, nbp.data(), sizeof(int) * nbp.size(), (void**)&c->d_nbp))) return rc;
+        CK(cudaMalloc(&c->d_rec, (size_t)NREC * Np * c->fl->elem));
+        CK(cudaMalloc(&c->d_dqs, (size_t)DQ_STRIDE * Np * c->fl->elem));
+        CK(cudaMalloc(&c->d_flags, (size_t)2 * Np * sizeof(int)));
+        c->sv.cells = c->d_sweep; c->sv.nbp = c->d_nbp; c->sv.rec = c->d_rec; c->sv.dq = c->d_dqs; c->sv.n = N;
+    }
+    {   // staging buffer for the largest Fortran field (DQdxyz: 18 components, lower bound -1)
+        size_t mx = 0;
+        for (auto& b : c->blk) mx = std::max(mx, (size_t)(b.NI + 4) * (b.NJ + 4) * (b.NK + 4) * 18);
+        c->stage_doubles = mx;
+        CK(cudaMalloc(&c->d_stage, mx * sizeof(double)));
+    }
+    c->h_parts.assign(c->cell_tiles.size(), NormPart{});
+    CK(cudaMalloc(&c->d_parts, sizeof(NormPart) * std::max<size_t>(1, c->h_parts.size())));
+    c->norms.assign(nblk, trans_norms{});
+    CK(cudaMalloc(&c->d_cdev, sizeof(CaseDev) * c->cases.size()));
+    CK(cudaMallocHost(&c->h_cdev, sizeof(CaseDev) * c->cases.size()));
+    if (!c->sweep_forced) c->sweep_mode = -1;     // re-tune the sweep schedule for the new work
+    c->built = true;
+    return TRANS_OK;
+}
+
+}  // namespace eng
+}  // namespace tg

@@ -20,6 +20,30 @@ class SolverError(RuntimeError):
     pass
 
 
+def block_table(case, conns, keep):
+    """trans_block descriptors of a case (Module_Block.F90 fields); `keep` holds the buffers
+    they point to for as long as the library may read them."""
+    nb = len(case.blocks)
+    tb = (abi.TransBlock * nb)()
+    for n, b in enumerate(case.blocks):
+        ni, nj, nk = b.dims
+        cl = conns[b.id]
+        carr = (abi.TransConn * len(cl))(*cl)
+        mw = markwall_arrays(b)
+        keep += [carr, mw]
+        tb[n].ni, tb[n].nj, tb[n].nk, tb[n].id = ni, nj, nk, b.id
+        tb[n].nconn = len(cl)
+        tb[n].conn = C.cast(carr, C.POINTER(abi.TransConn))
+        for f in range(6):
+            tb[n].markwall[f] = mw[f].ctypes.data_as(C.POINTER(C.c_int))
+    keep.append(tb)
+    return tb
+
+
+def _norm_dicts(arr):
+    return [{f: getattr(x, f) for f, _ in abi.TransNorms._fields_} for x in arr]
+
+
 class Solver:
     def __init__(self, case, conns, geo, state, lib=None, prefix="trans_", params=None):
         if lib is None:
@@ -32,19 +56,7 @@ class Solver:
         self.blocks = case.blocks
         self._keep = []
         nb = len(self.blocks)
-        tb = (abi.TransBlock * nb)()
-        for n, b in enumerate(self.blocks):
-            ni, nj, nk = b.dims
-            cl = conns[b.id]
-            carr = (abi.TransConn * len(cl))(*cl)
-            mw = markwall_arrays(b)
-            self._keep += [carr, mw]
-            tb[n].ni, tb[n].nj, tb[n].nk, tb[n].id = ni, nj, nk, b.id
-            tb[n].nconn = len(cl)
-            tb[n].conn = C.cast(carr, C.POINTER(abi.TransConn))
-            for f in range(6):
-                tb[n].markwall[f] = mw[f].ctypes.data_as(C.POINTER(C.c_int))
-        self._keep.append(tb)
+        tb = block_table(case, conns, self._keep)
         ctx = C.c_void_p()
         rc = self._fn("create")(C.byref(self.params), nb, tb, C.byref(ctx))
         if rc != 0:
@@ -103,6 +115,102 @@ class Solver:
     def close(self):
         if getattr(self, "ctx", None):
             self._fn("destroy")(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """A batch context (trans_batch_*): independent cases added and removed while it runs,
+    all advanced by the same kernel launches, admitted within a device-memory budget."""
+
+    def __init__(self, precision=abi.TRANS_FP64, budget_bytes=0, lib=None):
+        if lib is None:
+            from . import native
+            lib = native.load()
+        self.lib = lib
+        ctx = C.c_void_p()
+        rc = lib.trans_batch_create(precision, int(budget_bytes), C.byref(ctx))
+        if rc != 0:
+            raise SolverError(f"trans_batch_create failed ({rc}: {abi.ERRORS.get(rc, '?')})")
+        self.ctx = ctx
+        self.precision = precision
+        self.cases = {}                     # id -> (case, keep)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            m = self.lib.trans_last_error(self.ctx)
+            raise SolverError(f"trans_batch_{what} failed ({rc}: {abi.ERRORS.get(rc, '?')}) {m.decode() if m else ''}")
+
+    def case_bytes(self, case, conns):
+        keep = []
+        tb = block_table(case, conns, keep)
+        p = case.params
+        p.precision = self.precision
+        return int(self.lib.trans_batch_case_bytes(C.byref(p), len(case.blocks), tb))
+
+    def add(self, case, conns, geo, state):
+        """Admit a case; returns its id, or None if it does not fit the budget."""
+        keep = []
+        tb = block_table(case, conns, keep)
+        p = case.params
+        p.precision = self.precision
+        cid = C.c_int()
+        rc = self.lib.trans_batch_add(self.ctx, C.byref(p), len(case.blocks), tb, C.byref(cid))
+        if rc == abi.TRANS_E_MEMORY:
+            return None
+        self._check(rc, "add")
+        self.cases[cid.value] = (case, keep)
+        for n, b in enumerate(case.blocks):
+            for name in GEOMETRY_FIELDS:
+                self.set_field(cid.value, n, name, geo[b.id][name])
+            for name in STATE_FIELDS:
+                self.set_field(cid.value, n, name, state[b.id][name])
+        return cid.value
+
+    def remove(self, cid):
+        self._check(self.lib.trans_batch_remove(self.ctx, cid), "remove")
+        del self.cases[cid]
+
+    def set_field(self, cid, ib, name, full):
+        ni, nj, nk = self.cases[cid][0].blocks[ib].dims
+        f = fortran_view(name, full)
+        self._check(self.lib.trans_batch_set_field(self.ctx, cid, ib, abi.FIELD_ID[name],
+                                                   f.ctypes.data_as(C.POINTER(C.c_double))), "set_field")
+
+    def get_field(self, cid, ib, name, full=True):
+        ni, nj, nk = self.cases[cid][0].blocks[ib].dims
+        f = np.zeros(abi.field_shape(name, ni, nj, nk), order="F")
+        self._check(self.lib.trans_batch_get_field(self.ctx, cid, ib, abi.FIELD_ID[name],
+                                                   f.ctypes.data_as(C.POINTER(C.c_double))), "get_field")
+        return full_from_fortran(name, f, ni, nj, nk) if full else f
+
+    def iterate(self, n=1):
+        """n iterations of every case; returns True if some case produced a NaN."""
+        rc = self.lib.trans_batch_iterate(self.ctx, n)
+        if rc == abi.TRANS_E_NAN:
+            return True
+        self._check(rc, "iterate")
+        return False
+
+    def norms(self, cid):
+        """(iterations done, per-block norms of the first iteration, of the last)."""
+        nb = len(self.cases[cid][0].blocks)
+        first, last = (abi.TransNorms * nb)(), (abi.TransNorms * nb)()
+        it = C.c_int()
+        self._check(self.lib.trans_batch_case_norms(self.ctx, cid, C.byref(it), first, last), "case_norms")
+        return it.value, _norm_dicts(first), _norm_dicts(last)
+
+    def bytes_in_use(self):
+        return int(self.lib.trans_batch_bytes_in_use(self.ctx))
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.trans_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):
