@@ -267,10 +267,14 @@ def main():
     s = Solver(c, conns, geo, st)
     lib = s.lib
     ki = 1
-    for _ in range(args.warmup):
+    # W warm-up steps, the last one with CUDA events around every stage (stage_ms)
+    for _ in range(max(args.warmup - 1, 0)):
         s.iterate(ki); ki += 1
     stage_ms = (C.c_double * len(abi.STAGES))()
     lib.trans_stage_times(s.ctx, ki, stage_ms); ki += 1
+    # untimed set-up: sweep schedule tuning and capture of the iteration graph (no iteration runs)
+    if lib.trans_prepare(s.ctx, ki) != 0:
+        raise RuntimeError(f"trans_prepare failed: {lib.trans_last_error(s.ctx)}")
     launches0 = lib.trans_kernel_launches(s.ctx)
     clk = ClockSampler()
     clk.start()

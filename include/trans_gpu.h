@@ -156,6 +156,11 @@ int trans_iterate(void* ctx, int ki, trans_norms* norms);
 /* One stage of one sub-iteration for all blocks; itr_chld is the sub-iteration index (1-based). */
 int trans_run_stage(void* ctx, int stage, int ki, int itr_chld);
 int trans_get_norms(void* ctx, trans_norms* norms);
+/* Prepares the context for iteration KI without running it (no reference counterpart): builds
+ * the work lists and geometry terms, tunes the LU-SGS sweep schedule on a right-hand side of
+ * the current state and captures the iteration graph that trans_time_iterations and
+ * trans_batch_iterate replay (8 outer iterations per replay).  The interior state is unchanged. */
+int trans_prepare(void* ctx, int ki);
 /* One outer iteration with CUDA events around every stage on the context's stream; ms receives
  * TRANS_NSTAGES elapsed times (no reference counterpart: instrumentation). */
 int trans_stage_times(void* ctx, int ki, double* ms);

@@ -110,3 +110,25 @@ def test_admission_by_device_budget(gpu_lib):
     assert bt.norms(ib)[0] == 1
     assert np.isfinite(bt.norms(ib)[2][0]["DRSa"])
     bt.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_replay_equals_direct_launches(gpu_lib, precision, monkeypatch):
+    """Whole iterations replayed as one CUDA graph give the same state as launching every
+    kernel directly (TRANS_GRAPHS=0)."""
+    from trans_gb300 import abi
+    from trans_gb300.solver import Batch
+    prec = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
+    out = {}
+    for graphs in ("1", "0"):
+        monkeypatch.setenv("TRANS_GRAPHS", graphs)
+        c, conns, geo, st = _case_a()
+        bt = Batch(prec)
+        cid = bt.add(c, conns, geo, st)
+        bt.iterate(9)
+        out[graphs] = (_fields(bt, cid, c), bt.norms(cid))
+        bt.close()
+    for q, b in enumerate(c.blocks):
+        assert bit_equal_fraction(out["1"][0][q], out["0"][0][q], interior(b.dims)) == 1.0
+    assert out["1"][1][0] == out["0"][1][0] == 9
+    assert [n["DRSa"] for n in out["1"][1][2]] == [n["DRSa"] for n in out["0"][1][2]]

@@ -105,13 +105,13 @@ double trans_probe_fma_gflops(int fp64) { return probe_fma_gflops(fp64); }
 
 int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norms* norms) {
     Ctx* c = as_ctx(ctx);
-    if (!c || !ms || n < 0) return TRANS_E_ARG;
+    if (!c || !ms || n < 0 || c->cases.empty()) return TRANS_E_ARG;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     CK(cudaEventRecord(e0, c->stream));
-    int rc = TRANS_OK;
-    for (int q = 0; q < n && rc == TRANS_OK; ++q) rc = trans_iterate(ctx, ki_first + q, norms);
+    set_ki(c, ki_first);
+    int rc = run_iterations(c, n);
     CK(cudaEventRecord(e1, c->stream));
     CK(cudaEventSynchronize(e1));
     float t = 0;
@@ -119,7 +119,15 @@ int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norm
     *ms = t;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (norms) std::copy(c->cases[0]->norms.begin(), c->cases[0]->norms.end(), norms);
     return rc;
+}
+
+int trans_prepare(void* ctx, int ki) {
+    Ctx* c = as_ctx(ctx);
+    if (!c || c->cases.empty()) return TRANS_E_ARG;
+    set_ki(c, ki);
+    return prepare(c);
 }
 
 int trans_get_norms(void* ctx, trans_norms* norms) {

@@ -59,20 +59,9 @@ int trans_batch_get_field(void* ctx, int case_id, int ib, int field, double* a) 
 int trans_batch_iterate(void* ctx, int n) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c || n < 0) return TRANS_E_ARG;
-    if (c->cases.empty()) return TRANS_OK;
-    for (int q = 0; q < n; ++q) {
-        for (CaseRec* cs : c->cases) cs->KI = cs->p.KI_ini + cs->iters + 1;
-        int rc = run_iteration(c);
-        if (rc == TRANS_E_NAN) {              // norms are final; the caller retires the case(s)
-            for (CaseRec* cs : c->cases) {
-                if (cs->iters == 0) cs->first_norms = cs->norms;
-                cs->iters++;
-            }
-            return rc;
-        }
-        if (rc) return rc;
-    }
-    return TRANS_OK;
+    if (c->cases.empty() || n == 0) return TRANS_OK;
+    for (CaseRec* cs : c->cases) cs->KI = cs->p.KI_ini + cs->iters + 1;
+    return run_iterations(c, n);         // TRANS_E_NAN: norms are final; the caller retires the case(s)
 }
 
 int trans_batch_case_norms(void* ctx, int case_id, int* iterations, trans_norms* first, trans_norms* last) {

@@ -128,6 +128,9 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     CK(cudaMalloc(&c->d_sync, sizeof(SweepSync)));
     CK(cudaMallocHost(&c->h_sync, sizeof(SweepSync)));
     std::memset(c->h_sync, 0, sizeof(SweepSync));
+    // TRANS_GRAPHS=0 turns the whole-iteration graphs off (every iteration launched directly)
+    const char* gr = std::getenv("TRANS_GRAPHS");
+    if (gr && std::string(gr) == "0") c->graphs = false;
     // sweep schedule: TRANS_SWEEP=planes | coop | flow forces one (for tests); default: tuned
     const char* m = std::getenv("TRANS_SWEEP");
     std::string ms = m ? m : "";
@@ -148,7 +151,10 @@ void free_worklists(Ctx* c) {
     for (int d = 0; d < 3; ++d) dfree(c->d_face[d]);
     dfree(c->d_bc); dfree(c->d_outlet); dfree(c->d_lines); dfree(c->d_sweep); dfree(c->d_plane_off);
     dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq_save); dfree(c->d_parts);
-    dfree(c->d_cdev); dfree(c->d_stage);
+    dfree(c->d_cdev); dfree(c->d_stage); dfree(c->d_tile_first); dfree(c->d_norms);
+    if (c->h_norms) { cudaFreeHost(c->h_norms); c->h_norms = nullptr; }
+    if (c->iter_exec) { cudaGraphExecDestroy(c->iter_exec); c->iter_exec = nullptr; }
+    c->iter_n = 0;
     if (c->h_cdev) { cudaFreeHost(c->h_cdev); c->h_cdev = nullptr; }
     if (c->sweep_exec) { cudaGraphExecDestroy(c->sweep_exec); c->sweep_exec = nullptr; }
     c->built = false;

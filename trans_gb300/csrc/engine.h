@@ -47,6 +47,9 @@ enum KClass { K_SPECRAD, K_BC_STATE, K_BC_OUTLET, K_PRIMS, K_MIRROR, K_GRADIENT,
               K_FACE, K_GATHER, K_SST_FC1, K_PREP, K_SWEEP, K_SCATTER, K_UPDATE, K_UPDATE_U, NKCLASS };
 extern const char* const kclass_name[NKCLASS];
 
+constexpr int GRAPH_ITERS = 8;            // outer iterations per replay of the iteration graph
+constexpr int NORM_HIST = GRAPH_ITERS;    // norm history depth (one entry per replayed iteration)
+
 struct Ctx {
     int precision = TRANS_FP64;
     bool mixed = false;
@@ -82,6 +85,14 @@ struct Ctx {
     void* d_dq_save = nullptr;
     NormPart* d_parts = nullptr;
     std::vector<NormPart> h_parts;
+    int* d_tile_first = nullptr;         // first cell tile of each block (+ end)
+    BlockNorms* d_norms = nullptr;       // per block, NORM_HIST iterations deep
+    BlockNorms* h_norms = nullptr;       // pinned
+    // whole iterations replayed as one CUDA graph (trans_batch_iterate, trans_time_iterations)
+    cudaGraphExec_t iter_exec = nullptr;
+    int iter_n = 0;
+    long long iter_launches = 0;
+    bool graphs = true;
     std::vector<trans_norms> norms;      // per block of the context
     CaseDev* d_cdev = nullptr;           // per case slot
     CaseDev* h_cdev = nullptr;           // pinned
@@ -135,6 +146,13 @@ int upload_cdev(Ctx* c);
 int finalize_geometry(Ctx* c);
 int reduce_norms(Ctx* c);
 int run_iteration(Ctx* c);               // one outer iteration of every case at its KI
+// n outer iterations of every case, the first at each case's KI, KI advancing by one; whole
+// iterations are replayed as one CUDA graph where the cases' switches stay fixed
+int run_iterations(Ctx* c, int n);
+// everything an iteration needs before it runs, without running one: work lists, geometry
+// terms, the sweep schedule (tuned on a right-hand side of the current state) and the
+// iteration graph.  The state (interior cells) is unchanged.
+int prepare(Ctx* c);
 int kernel_times(Ctx* c, double* ms, int* launches);
 
 }  // namespace eng

@@ -26,6 +26,10 @@ void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int 
 void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml) {
     if (total > 0) k_mirror<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off, ml);
 }
+void launch_block_norms(cudaStream_t s, const DevBlock* blks, int nblk, const NormPart* parts, const int* tile_first,
+                        BlockNorms* out) {
+    if (nblk > 0) k_block_norms<<<nblk, 256, 0, s>>>(blks, parts, tile_first, out);
+}
 void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev) {
     if (nt > 0) k_update_u<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev);
 }

@@ -1212,6 +1212,55 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
     }
 }
 
+// Per-block norms from the per-tile partials (Time/TIME_Update_V.F90:116-146, 892-908): one
+// block of threads per solver block, fixed summation order (strided partial sums, then a
+// tree), the maximum of |D1/V1| with the later cell winning ties.
+__global__ void k_block_norms(const DevBlock* __restrict__ blks, const NormPart* __restrict__ parts,
+                              const int* __restrict__ tile_first, BlockNorms* __restrict__ out) {
+    const int bi = blockIdx.x, tid = threadIdx.x;
+    __shared__ double s_sum[3][256];
+    __shared__ double s_max[3][256];
+    __shared__ long long s_idx[256];
+    __shared__ int s_nan[256];
+    double sa = 0, sk = 0, so = 0, ma = -1, mk = 0, mo = 0;
+    long long ia = 0;
+    int nan = 0;
+    for (int t = tile_first[bi] + tid; t < tile_first[bi + 1]; t += blockDim.x) {
+        const NormPart P = parts[t];
+        sa += P.sa; sk += P.sk; so += P.so;
+        if (P.ma > ma || (P.ma == ma && P.ia > ia)) { ma = P.ma; ia = P.ia; }
+        mk = dmax(mk, P.mk); mo = dmax(mo, P.mo);
+        nan |= P.nan;
+    }
+    s_sum[0][tid] = sa; s_sum[1][tid] = sk; s_sum[2][tid] = so;
+    s_max[0][tid] = ma; s_max[1][tid] = mk; s_max[2][tid] = mo;
+    s_idx[tid] = ia; s_nan[tid] = nan;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (tid < w) {
+            for (int q = 0; q < 3; ++q) s_sum[q][tid] += s_sum[q][tid + w];
+            double a = s_max[0][tid], bb = s_max[0][tid + w];
+            if (bb > a || (bb == a && s_idx[tid + w] > s_idx[tid])) { s_max[0][tid] = bb; s_idx[tid] = s_idx[tid + w]; }
+            s_max[1][tid] = dmax(s_max[1][tid], s_max[1][tid + w]);
+            s_max[2][tid] = dmax(s_max[2][tid], s_max[2][tid + w]);
+            s_nan[tid] |= s_nan[tid + w];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const DevBlock B = blks[bi];
+        BlockNorms N;
+        N.DRSa = sqrt(s_sum[0][0] / B.NI1 / B.NJ1 / B.NK1);
+        N.DRSk = sqrt(s_sum[1][0] / B.NI1 / B.NJ1 / B.NK1);
+        N.DRSo = sqrt(s_sum[2][0] / B.NI1 / B.NJ1 / B.NK1);
+        N.DUa = s_max[0][0]; N.DUk = s_max[1][0]; N.DUo = s_max[2][0];
+        const long long i0 = s_idx[0];
+        N.Ima = (int)(i0 % B.NI1) + 1; N.Jma = (int)((i0 / B.NI1) % B.NJ1) + 1; N.Kma = (int)(i0 / ((long long)B.NI1 * B.NJ1)) + 1;
+        N.nan_flag = s_nan[0];
+        out[bi] = N;
+    }
+}
+
 // Time/TIME_Update_U.F90:16-44
 __global__ void k_update_u(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];

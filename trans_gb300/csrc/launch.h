@@ -10,6 +10,7 @@ struct SweepCell;
 struct NormPart;
 struct SweepSync;
 struct SweepView;
+struct BlockNorms;
 
 // FP64 kernels shared by both precision modes
 void launch_specrad(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev);
@@ -19,6 +20,8 @@ void launch_bc_outlet(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, 
 void launch_prims(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
 void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts,
                    int d_fp32);
+void launch_block_norms(cudaStream_t s, const DevBlock* blks, int nblk, const NormPart* parts, const int* tile_first,
+                        BlockNorms* out);
 void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml);
 void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev);
 void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, int lb, int is_sd, double* stage, int to_slots);

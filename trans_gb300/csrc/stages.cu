@@ -141,6 +141,19 @@ int reduce_norms(Ctx* c) {
     return TRANS_OK;
 }
 
+// Norms of every block (from k_block_norms, BlockNorms = trans_norms layout) into the context
+// and its cases.
+static_assert(sizeof(BlockNorms) == sizeof(trans_norms), "BlockNorms mirrors trans_norms");
+int collect_norms(Ctx* c, const BlockNorms* hn) {
+    std::memcpy(c->norms.data(), hn, sizeof(trans_norms) * c->norms.size());
+    int nan = 0;
+    for (const trans_norms& N : c->norms) nan |= N.nan_flag;
+    for (CaseRec* cs : c->cases)
+        std::copy(c->norms.begin() + cs->blk0, c->norms.begin() + cs->blk0 + cs->blk.size(), cs->norms.begin());
+    if (nan) return fail(c, TRANS_E_NAN, "NaN in the density increment");
+    return TRANS_OK;
+}
+
 int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
     if (!c || !cs || ib < 0 || ib >= (int)cs->blk.size() || !host) return TRANS_E_ARG;
     if (!c->built) {
@@ -190,7 +203,7 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
 // ---------------------------------------------------------------------------------------
 namespace {
 
-int sweep_once(Ctx* c, int mode, int grid, int block) {
+int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     cudaStream_t s = c->stream;
     const int nh = (int)c->plane_off.size() - 1;
     if (mode == 2) {
@@ -209,7 +222,19 @@ int sweep_once(Ctx* c, int mode, int grid, int block) {
         c->launches++;
         return TRANS_OK;
     }
-    // one launch per hyperplane, L ascending then U descending, replayed as one graph
+    // one launch per hyperplane, L ascending then U descending, replayed as one graph (or
+    // captured directly into the caller's graph)
+    if (capture) {
+        for (int h = 0; h < nh; ++h) {
+            int cnt = c->plane_off[h + 1] - c->plane_off[h];
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, 1);
+        }
+        for (int h = nh - 1; h >= 0; --h) {
+            int cnt = c->plane_off[h + 1] - c->plane_off[h];
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, 1);
+        }
+        return TRANS_OK;
+    }
     if (!c->sweep_exec) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -307,30 +332,36 @@ bool wants_dual(const CaseRec* cs) { return cs->p.Kind_Dual != 0; }
 // ---------------------------------------------------------------------------------------
 // One hot-path subroutine over every block of every case (trans_run_stage)
 // ---------------------------------------------------------------------------------------
-int run_stage(Ctx* c, int stage, int itr) {
+namespace {
+
+// One stage.  capture: inside a CUDA-graph capture (no host synchronisation, no parameter
+// upload, the norms go to history slot `slot`).
+int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
     (void)itr;
     if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
     int rc;
-    if (!c->built && (rc = rebuild(c))) return rc;
-    if ((rc = finalize_geometry(c))) return rc;
+    if (!capture) {
+        if (!c->built && (rc = rebuild(c))) return rc;
+        if ((rc = finalize_geometry(c))) return rc;
+    }
     cudaStream_t s = c->stream;
     const int nct = (int)c->cell_tiles.size();
     switch (stage) {
         case TRANS_STAGE_SPECRAD: {
-            if ((rc = upload_cdev(c))) return rc;
+            if (!capture && (rc = upload_cdev(c))) return rc;
             KScope t(c, K_SPECRAD);
             launch_specrad(s, c->d_blk, c->d_cell, nct, c->d_cdev);
             c->launches++;
             break;
         }
         case TRANS_STAGE_BC_STATE:
-            if ((rc = upload_cdev(c))) return rc;
+            if (!capture && (rc = upload_cdev(c))) return rc;
             { KScope t(c, K_BC_STATE); launch_bc_state(s, c->d_blk, c->d_bc, (int)c->bc.size(), c->d_cdev); }
             { KScope t(c, K_BC_OUTLET); launch_bc_outlet(s, c->d_blk, c->d_outlet, c->d_lines, (int)c->lines.size(), c->d_cdev); }
             c->launches += 1 + (c->lines.empty() ? 0 : 1);
             break;
         case TRANS_STAGE_GRADIENT:
-            if ((rc = upload_cdev(c))) return rc;
+            if (!capture && (rc = upload_cdev(c))) return rc;
             { KScope t(c, K_PRIMS); launch_prims(s, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off); }
             // the FP32 kernels read FP32 copies of this sub-iteration's state, primitives and radii
             if (c->mixed) { KScope t(c, K_MIRROR); mirror(c, {{S_V, 10}, {S_RDS, 4}, {S_PRIM, 5}, {S_RINV, 4}}); }
@@ -343,7 +374,7 @@ int run_stage(Ctx* c, int stage, int itr) {
             c->launches++;
             break;
         case TRANS_STAGE_RESIDUAL:
-            if ((rc = upload_cdev(c))) return rc;
+            if (!capture && (rc = upload_cdev(c))) return rc;
             for (int d = 0; d < 3; ++d) {
                 KScope t(c, K_FACE);
                 c->fl->face_flux[d](s, c->d_blk, c->d_face[d], (int)c->face_tiles[d].size(), c->d_cdev);
@@ -352,7 +383,7 @@ int run_stage(Ctx* c, int stage, int itr) {
             c->launches += 4;
             break;
         case TRANS_STAGE_LUSGS: {
-            if ((rc = upload_cdev(c))) return rc;
+            if (!capture && (rc = upload_cdev(c))) return rc;
             if (any_case(c, wants_des)) {
                 KScope t(c, K_SST_FC1);
                 c->fl->sst_fc1(s, c->d_blk, c->d_cell, nct, c->d_cdev);
@@ -364,24 +395,32 @@ int run_stage(Ctx* c, int stage, int itr) {
                 int nh = (int)c->plane_off.size() - 1, nl = 0;
                 for (int h = 0; h < nh; ++h) nl += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
                 KScope t(c, K_SWEEP, c->sweep_mode >= 1 ? 1 : nl);
-                if ((rc = run_sweeps(c))) return rc;
+                if (capture) rc = sweep_once(c, c->sweep_mode, c->sweep_grid, c->sweep_block, true);
+                else rc = run_sweeps(c);
+                if (rc) return rc;
             }
             { KScope t(c, K_SCATTER); c->fl->scatter(s, c->d_blk, c->sv); }
             c->launches++;
             break;
         }
         case TRANS_STAGE_UPDATE: {
-            if ((rc = upload_cdev(c))) return rc;
-            { KScope t(c, K_UPDATE); launch_update(s, c->d_blk, c->d_cell, nct, c->d_cdev, c->d_parts, c->mixed ? 1 : 0); }
-            c->launches++;
-            CK(cudaMemcpyAsync(c->h_parts.data(), c->d_parts, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, s));
+            if (!capture && (rc = upload_cdev(c))) return rc;
+            const int nblk = (int)c->blk.size();
+            {
+                KScope t(c, K_UPDATE);
+                launch_update(s, c->d_blk, c->d_cell, nct, c->d_cdev, c->d_parts, c->mixed ? 1 : 0);
+                launch_block_norms(s, c->d_blk, nblk, c->d_parts, c->d_tile_first, c->d_norms + (size_t)slot * nblk);
+            }
+            c->launches += 2;
+            if (capture) break;
+            CK(cudaMemcpyAsync(c->h_norms, c->d_norms, sizeof(BlockNorms) * nblk, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
-            if ((rc = reduce_norms(c))) return rc;
+            if ((rc = collect_norms(c, c->h_norms))) return rc;
             break;
         }
         case TRANS_STAGE_UPDATE_U:
-            if ((rc = upload_cdev(c))) return rc;
+            if (!capture && (rc = upload_cdev(c))) return rc;
             if (any_case(c, wants_dual)) {
                 KScope t(c, K_UPDATE_U);
                 launch_update_u(s, c->d_blk, c->d_cell, nct, c->d_cdev);
@@ -391,23 +430,144 @@ int run_stage(Ctx* c, int stage, int itr) {
         default:
             return fail(c, TRANS_E_ARG, "bad stage");
     }
-    CK(cudaGetLastError());
+    if (!capture) CK(cudaGetLastError());
     return TRANS_OK;
 }
+
+}  // namespace
+
+int run_stage(Ctx* c, int stage, int itr) { return stage_exec(c, stage, itr, false, 0); }
 
 // One outer iteration (main.F90:54-171 + :192-197) of every case at its current KI.
 int run_iteration(Ctx* c) {
     if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
     const CaseRec* c0 = c->cases[0];
     const int nsub = c0->p.Kind_Dual != 0 ? c0->p.Kchld : 1;
-    int rc;
-    for (int it = 1; it <= nsub; ++it)
-        for (int st = TRANS_STAGE_SPECRAD; st <= TRANS_STAGE_UPDATE; ++st)
-            if ((rc = run_stage(c, st, it))) return rc;
-    if ((rc = run_stage(c, TRANS_STAGE_UPDATE_U, nsub))) return rc;
-    for (CaseRec* cs : c->cases) {
+    int rc = TRANS_OK;
+    for (int it = 1; it <= nsub && rc == TRANS_OK; ++it)
+        for (int st = TRANS_STAGE_SPECRAD; st <= TRANS_STAGE_UPDATE && rc == TRANS_OK; ++st)
+            rc = run_stage(c, st, it);
+    if (rc == TRANS_OK) rc = run_stage(c, TRANS_STAGE_UPDATE_U, nsub);
+    if (rc != TRANS_OK && rc != TRANS_E_NAN) return rc;
+    for (CaseRec* cs : c->cases) {               // a NaN iteration still has its norms
         if (cs->iters == 0) cs->first_norms = cs->norms;
         cs->iters++;
+    }
+    return rc;
+}
+
+namespace {
+
+// the cases' switches are the same for their next n KI values (graphs replay fixed parameters)
+bool switches_fixed(Ctx* c, int n) {
+    for (CaseRec* cs : c->cases) {
+        const int ki = cs->KI;
+        const CaseDev a = case_dev(cs);
+        cs->KI = ki + n - 1;
+        const CaseDev b = case_dev(cs);
+        cs->KI = ki;
+        if (a.CFL_sub != b.CFL_sub || a.turb != b.turb || a.turb_upd != b.turb_upd) return false;
+        if (cs->p.CFL_Sub_end != cs->p.CFL_Sub_start && ki - cs->p.KI_ini < cs->p.CFL_Sub_step) return false;
+    }
+    return true;
+}
+
+int capture_iterations(Ctx* c, int n) {
+    if (c->iter_exec) { cudaGraphExecDestroy(c->iter_exec); c->iter_exec = nullptr; c->iter_n = 0; }
+    const CaseRec* c0 = c->cases[0];
+    const int nsub = c0->p.Kind_Dual != 0 ? c0->p.Kchld : 1;
+    const int nblk = (int)c->blk.size();
+    cudaStream_t s = c->stream;
+    cudaGraph_t g = nullptr;
+    const long long launches0 = c->launches;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = TRANS_OK;
+    for (int q = 0; q < n && rc == TRANS_OK; ++q) {
+        for (int it = 1; it <= nsub && rc == TRANS_OK; ++it)
+            for (int st = TRANS_STAGE_SPECRAD; st <= TRANS_STAGE_UPDATE && rc == TRANS_OK; ++st)
+                rc = stage_exec(c, st, it, true, q);
+        if (rc == TRANS_OK) rc = stage_exec(c, TRANS_STAGE_UPDATE_U, nsub, true, q);
+    }
+    if (rc == TRANS_OK) {
+        cudaMemcpyAsync(c->h_norms, c->d_norms, sizeof(BlockNorms) * (size_t)nblk * n, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s);
+    }
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, TRANS_E_CUDA, std::string("iteration graph capture: ") + cudaGetErrorString(e));
+    }
+    e = cudaGraphInstantiate(&c->iter_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, TRANS_E_CUDA, std::string("iteration graph instantiate: ") + cudaGetErrorString(e));
+    }
+    c->iter_n = n;
+    c->iter_launches = c->launches - launches0;       // kernels per replay
+    c->launches = launches0;
+    return TRANS_OK;
+}
+
+}  // namespace
+
+int run_iterations(Ctx* c, int n) {
+    if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
+    int rc, done = 0;
+    bool first = true;
+    auto advance = [&]() {
+        for (CaseRec* cs : c->cases) cs->KI++;
+    };
+    while (done < n) {
+        if (!first) advance();                  // KI of this iteration
+        first = false;
+        // an ordinary iteration builds the work lists and the geometry terms and tunes the
+        // sweeps; graphs replay iterations whose switches (CFL ramp, turbulence) are fixed
+        const bool graph = c->graphs && c->built && c->sweep_mode >= 0 && n - done >= GRAPH_ITERS &&
+                           switches_fixed(c, GRAPH_ITERS);
+        if (!graph) {
+            if ((rc = run_iteration(c))) return rc;
+            ++done;
+            continue;
+        }
+        const int m = GRAPH_ITERS;
+        if ((rc = finalize_geometry(c)) || (rc = upload_cdev(c))) return rc;
+        if ((!c->iter_exec || c->iter_n != m) && capture_iterations(c, m) != TRANS_OK) {
+            c->graphs = false;                  // not capturable here: launch directly from now on
+            if ((rc = run_iteration(c))) return rc;
+            ++done;
+            continue;
+        }
+        CK(cudaGraphLaunch(c->iter_exec, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->launches += c->iter_launches;
+        const int nblk = (int)c->blk.size();
+        int nan = 0;
+        for (int q = 0; q < m; ++q) {
+            nan |= collect_norms(c, c->h_norms + (size_t)q * nblk) == TRANS_E_NAN;
+            for (CaseRec* cs : c->cases) {
+                if (cs->iters == 0) cs->first_norms = cs->norms;
+                cs->iters++;
+            }
+        }
+        for (int q = 1; q < m; ++q) advance();  // KI of the last replayed iteration
+        done += m;
+        if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
+        if (nan) return fail(c, TRANS_E_NAN, "NaN in the density increment");
+    }
+    return TRANS_OK;
+}
+
+int prepare(Ctx* c) {
+    if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
+    int rc;
+    for (int st = TRANS_STAGE_SPECRAD; st <= TRANS_STAGE_LUSGS; ++st)
+        if ((rc = run_stage(c, st, 1))) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->graphs && switches_fixed(c, GRAPH_ITERS) && (!c->iter_exec || c->iter_n != GRAPH_ITERS)) {
+        if ((rc = upload_cdev(c))) return rc;
+        if (capture_iterations(c, GRAPH_ITERS) != TRANS_OK) c->graphs = false;
     }
     return TRANS_OK;
 }

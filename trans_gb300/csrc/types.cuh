@@ -35,6 +35,11 @@ struct NormPart {         // per-tile partial residual norms (Time/TIME_Update_V
     int nan, pad_;
 };
 
+struct BlockNorms {       // per-block norms, the layout of trans_norms (include/trans_gpu.h)
+    double DRSa, DUa, DRSk, DUk, DRSo, DUo;
+    int Ima, Jma, Kma, nan_flag;
+};
+
 struct SweepSync {        // grid barrier state of the persistent sweep kernel
     unsigned count, gen;
     int err, pad_;

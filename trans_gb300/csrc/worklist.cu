@@ -251,6 +251,14 @@ int rebuild(Ctx* c) {
         c->stage_doubles = mx;
         CK(cudaMalloc(&c->d_stage, mx * sizeof(double)));
     }
+    {   // first cell tile of every block (tiles are made block by block)
+        std::vector<int> tf(nblk + 1, 0);
+        for (size_t t = 0; t < c->cell_tile_blk.size(); ++t) tf[c->cell_tile_blk[t] + 1]++;
+        for (int n = 0; n < nblk; ++n) tf[n + 1] += tf[n];
+        if ((rc = upload_vec(c, tf.data(), sizeof(int) * tf.size(), (void**)&c->d_tile_first))) return rc;
+        CK(cudaMalloc(&c->d_norms, sizeof(BlockNorms) * (size_t)nblk * NORM_HIST));
+        CK(cudaMallocHost(&c->h_norms, sizeof(BlockNorms) * (size_t)nblk * NORM_HIST));
+    }
     c->h_parts.assign(c->cell_tiles.size(), NormPart{});
     CK(cudaMalloc(&c->d_parts, sizeof(NormPart) * std::max<size_t>(1, c->h_parts.size())));
     c->norms.assign(nblk, trans_norms{});
