@@ -233,10 +233,68 @@ def reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": c.name, "cells": ncell, "blocks": len(c.blocks)},
+            "config": {"workload": c.name, "cells": ncell, "blocks": len(c.blocks), "precision": "fp64",
+                       "implementation": "C++ FP64 restatement of the reference (oracle/), OpenMP over blocks"},
             "cpu_baseline": {"value": v, "unit": "Mcell-iter/s", "cores": min(threads, len(c.blocks)),
                              "kind": "port", "sample": f"{args.steps} iterations of {c.name}"},
             "e2e": {"value": v, "unit": "Mcell-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def batched_leg(c, conns, geo, st, args):
+    """N copies of the workload with back-pressure ratios spread over [0.80, 0.92] in one
+    batch context (every kernel one launch for all of them): aggregate cell-iterations/s,
+    timed like the single case (CUDA events, iteration graphs replayed)."""
+    import copy
+    from trans_gb300.solver import Batch
+    prec = abi.TRANS_MIXED if args.precision == "mixed" else abi.TRANS_FP64
+    bt = Batch(prec)
+    ratio0 = c.meta.get("p_ratio", 0.85)
+    n = args.batch
+    for q in range(n):
+        cq = copy.copy(c)
+        cq.params = CS.params_copy(c.params)
+        ratio = 0.80 + 0.12 * q / max(n - 1, 1)
+        cq.params.Pouthub = c.params.Pouthub * ratio / ratio0
+        if bt.add(cq, conns, geo, st) is None:
+            raise RuntimeError("batch does not fit")
+    bt.iterate(max(args.warmup, 1))
+    if bt.lib.trans_prepare(bt.ctx, -1) != 0:
+        raise RuntimeError(bt.lib.trans_last_error(bt.ctx).decode())
+    ms = C.c_double()
+    rc = bt.lib.trans_batch_time_iterations(bt.ctx, args.steps, C.byref(ms))
+    if rc != 0:
+        raise RuntimeError(f"batched timing failed {rc}")
+    ncell = interior_cells(c) * n
+    out = {"cases": n, "cells": ncell, "value": ncell * args.steps / (ms.value * 1e-3) / 1e6,
+           "unit": "Mcell-iter/s", "ms_per_step": ms.value / args.steps,
+           "sweep_schedule": bt.lib.trans_tuning(bt.ctx).decode()[:40]}
+    bt.close()
+    return out
+
+
+def serve_arm(args):
+    """Serving stream: seeded Poisson arrivals of cascade solves (grid level coarse 60% /
+    medium 30% / fine 10%, back-pressure ratio U[0.80,0.92], inlet Mach U[0.5,0.7]) admitted
+    into one batch context under a device-memory budget, each retired at its residual drop."""
+    from trans_gb300 import serving
+    prec = abi.TRANS_MIXED if args.precision == "mixed" else abi.TRANS_FP64
+    reqs = serving.poisson_requests(rate=args.rate, duration=args.duration, seed=0)
+    rep = serving.serve(reqs, precision=prec, budget_bytes=int(args.budget_gb * 1e9), drop=args.drop,
+                        max_iters=20000)
+    recs = rep.pop("records")
+    by_level = {}
+    for r in recs:
+        by_level.setdefault(r.level, []).append(r.iterations)
+    line = {"metric": "p50/p99 solve latency", "value": rep["latency_p50_s"], "unit": "s",
+            "p99": rep["latency_p99_s"], "throughput_mcell_iter_s": rep["throughput_mcell_iter_s"],
+            "higher_is_better": False, "n_gpus": 1, "dtype": "f64" if prec == abi.TRANS_FP64 else "f32-flux/f64-update",
+            "data": "synthetic",
+            "config": {"workload": "serving stream", "rate_per_s": args.rate, "duration_s": args.duration,
+                       "retire_at_drop": args.drop, "budget_gb": args.budget_gb,
+                       "mix": "coarse 0.6 / medium 0.3 / fine 0.1", "requests": rep["requests"]},
+            "completed": rep["completed"], "converged": rep["converged"], "wall_s": rep["wall_s"],
+            "iterations_by_level": {k: [min(v), int(np.median(v)), max(v)] for k, v in by_level.items()}}
     print(json.dumps(line))
 
 
@@ -250,7 +308,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nk", type=int, default=64, help="spanwise cells of the cascade (64 = full size)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="also time N copies of the workload (back-pressure ratios 0.80..0.92) in one batch context")
+    ap.add_argument("--serve", action="store_true", help="run the serving stream instead (p50/p99 latency)")
+    ap.add_argument("--rate", type=float, default=1.0, help="serving: Poisson arrivals per second")
+    ap.add_argument("--duration", type=float, default=20.0, help="serving: seconds of arrivals")
+    ap.add_argument("--drop", type=float, default=1e-3, help="serving: residual drop at which a request retires")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device-memory budget")
     args = ap.parse_args()
+    if args.serve:
+        return serve_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     if args.case == "cascade" and not hasattr(cases, "cascade"):
@@ -338,6 +405,8 @@ def main():
         "stage_ms": st_ms,
         "kernel_ms": {k: round(v[0], 4) for k, v in sorted(kt.items(), key=lambda x: -x[1][0])},
     }
+    if args.batch > 1:
+        line["batched"] = batched_leg(c, conns, geo, st, args)
     if rank == 0 and not args.no_cpu:
         v, n, dt2 = cpu_sample(c, conns, geo, st)
         line["cpu_baseline"] = {"value": v, "unit": "Mcell-iter/s", "cores": 1, "kind": "port",

@@ -156,7 +156,8 @@ int trans_iterate(void* ctx, int ki, trans_norms* norms);
 /* One stage of one sub-iteration for all blocks; itr_chld is the sub-iteration index (1-based). */
 int trans_run_stage(void* ctx, int stage, int ki, int itr_chld);
 int trans_get_norms(void* ctx, trans_norms* norms);
-/* Prepares the context for iteration KI without running it (no reference counterpart): builds
+/* Prepares the context for iteration KI (KI < 0: each case's next iteration) without running it
+ * (no reference counterpart): builds
  * the work lists and geometry terms, tunes the LU-SGS sweep schedule on a right-hand side of
  * the current state and captures the iteration graph that trans_time_iterations and
  * trans_batch_iterate replay (8 outer iterations per replay).  The interior state is unchanged. */
@@ -196,6 +197,8 @@ int trans_batch_get_field(void* ctx, int case_id, int ib, int field, double* for
 /* n outer iterations of every case.  TRANS_E_NAN: some case produced a NaN (its norms carry
  * nan_flag); the iteration is complete and the caller removes that case. */
 int trans_batch_iterate(void* ctx, int n);
+/* trans_batch_iterate timed with CUDA events on the context's stream (ms: total). */
+int trans_batch_time_iterations(void* ctx, int n, double* ms);
 /* Iterations done by a case, its per-block norms of its first and of its last iteration
  * (arrays of nblocks entries, either may be NULL). */
 int trans_batch_case_norms(void* ctx, int case_id, int* iterations, trans_norms* first, trans_norms* last);

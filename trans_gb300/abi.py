@@ -149,6 +149,7 @@ def bind_common(lib):
     lib.trans_batch_bytes_in_use.restype = C.c_longlong
     lib.trans_batch_cases.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
     lib.trans_prepare.argtypes = [vp, C.c_int]
+    lib.trans_batch_time_iterations.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
     lib.trans_tuning.argtypes = [vp]
     lib.trans_tuning.restype = C.c_char_p
     lib.trans_last_error.argtypes = [vp]
@@ -162,5 +163,6 @@ EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field
             "trans_time_iterations", "trans_update_static_scratch", "trans_tuning", "trans_kernel_times",
             "trans_kernel_class", "trans_batch_create", "trans_batch_case_bytes", "trans_batch_add",
             "trans_batch_remove", "trans_batch_set_field", "trans_batch_get_field", "trans_batch_iterate",
-            "trans_batch_case_norms", "trans_batch_bytes_in_use", "trans_batch_cases", "trans_prepare"]
+            "trans_batch_case_norms", "trans_batch_bytes_in_use", "trans_batch_cases", "trans_prepare",
+            "trans_batch_time_iterations"]
 TRANS_NKCLASS = 16

@@ -269,4 +269,5 @@ def cascade(nle=8, nte=4, ns=120, npitch=16, nr=48, nh=64, nk=64, Re_c=1.0e6, XM
               Block(5, Xp2, p2_segs, walls=end)]
     surfaces = [Xo[:, 0, :, :]] + [X[:, :, kk, :] for X in blocks_xyz for kk in (0, -1)]
     name = "cascade_5blk_%dcells" % sum(int(np.prod([d - 1 for d in b.dims])) for b in blocks)
-    return Case(name, p, blocks, surfaces, ph, dict(Q_dst=0.02 / alscale, chord=scale, pitch=pitch * scale))
+    return Case(name, p, blocks, surfaces, ph, dict(Q_dst=0.02 / alscale, chord=scale, pitch=pitch * scale,
+                                                    p_ratio=p_ratio))

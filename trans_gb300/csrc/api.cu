@@ -126,7 +126,9 @@ int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norm
 int trans_prepare(void* ctx, int ki) {
     Ctx* c = as_ctx(ctx);
     if (!c || c->cases.empty()) return TRANS_E_ARG;
-    set_ki(c, ki);
+    if (ki >= 0) set_ki(c, ki);
+    else
+        for (CaseRec* cs : c->cases) cs->KI = cs->p.KI_ini + cs->iters + 1;
     return prepare(c);
 }
 
@@ -180,7 +182,7 @@ const char* trans_tuning(void* ctx) {
     static thread_local std::string out;
     out = "sweep=" + std::string(c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : "flow ") + std::to_string(c->sweep_grid)
                                                       + "x" + std::to_string(c->sweep_block)
-                                 : c->sweep_mode == 0 ? "planes" : "untuned")
+                                 : c->sweep_mode == 0 ? (c->pdl ? "planes-chained" : "planes") : "untuned")
           + "; measured: " + c->sweep_tuning;
     return out.c_str();
 }

@@ -64,6 +64,24 @@ int trans_batch_iterate(void* ctx, int n) {
     return run_iterations(c, n);         // TRANS_E_NAN: norms are final; the caller retires the case(s)
 }
 
+int trans_batch_time_iterations(void* ctx, int n, double* ms) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || n < 0 || !ms) return TRANS_E_ARG;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->stream));
+    int rc = trans_batch_iterate(ctx, n);
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
 int trans_batch_case_norms(void* ctx, int case_id, int* iterations, trans_norms* first, trans_norms* last) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c) return TRANS_E_ARG;

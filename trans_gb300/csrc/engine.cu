@@ -131,6 +131,9 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     // TRANS_GRAPHS=0 turns the whole-iteration graphs off (every iteration launched directly)
     const char* gr = std::getenv("TRANS_GRAPHS");
     if (gr && std::string(gr) == "0") c->graphs = false;
+    // TRANS_PDL=0 launches the hyperplanes without programmatic dependent launch
+    const char* pd = std::getenv("TRANS_PDL");
+    if (pd && std::string(pd) == "0") c->pdl = c->pdl_allowed = 0;
     // sweep schedule: TRANS_SWEEP=planes | coop | flow forces one (for tests); default: tuned
     const char* m = std::getenv("TRANS_SWEEP");
     std::string ms = m ? m : "";

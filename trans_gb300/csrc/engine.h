@@ -106,6 +106,9 @@ struct Ctx {
     // 2 = dataflow over ready flags; -1 = pick the fastest on first use (all bit-identical)
     int sweep_mode = -1, sweep_grid = 0, sweep_block = 0;
     bool sweep_forced = false;
+    int pdl = 1;                         // chain hyperplane launches (programmatic dependent launch)
+    int pdl_allowed = 1;                 // chaining may be picked by the tuner (TRANS_PDL=0 forbids it)
+    int sweep_exec_pdl = -1;             // chaining the sweep graph was captured with
     SweepSync* d_sync = nullptr;
     SweepSync* h_sync = nullptr;         // pinned
     std::string sweep_tuning;

@@ -33,16 +33,29 @@ void jac(cudaStream_t s, const DevBlock* b, const SweepView& v) {
     if (v.n > 0)
         k_lusgs_jac<TG_R><<<(unsigned)((v.n + 31) / 32), 6 * 32, 0, s>>>(b, v.cells, v.nbp, (TG_R*)v.rec, v.n);
 }
-void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb) {
-    if (count > 0)
-        k_sweep<TG_R, true><<<(count * SWEEP_LANES + SWEEP_CTA - 1) / SWEEP_CTA, SWEEP_CTA, 0, s>>>(
-            v.nbp, (const TG_R*)v.rec, (TG_R*)v.dq, v.n, first, count, turb);
+// one hyperplane; chained = launched with programmatic stream serialisation, so that this
+// hyperplane's independent loads overlap the previous one (the kernel waits before its
+// dependent part)
+template <bool LOWER>
+void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained) {
+    if (count <= 0) return;
+    const int* nbp = v.nbp;
+    const TG_R* rec = (const TG_R*)v.rec;
+    TG_R* dq = (TG_R*)v.dq;
+    long long n = v.n;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((count * SWEEP_LANES + SWEEP_CTA - 1) / SWEEP_CTA);
+    cfg.blockDim = dim3(SWEEP_CTA);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = chained ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k_sweep<TG_R, LOWER>, nbp, rec, dq, n, first, count, turb, chained);
 }
-void swu(cudaStream_t s, const SweepView& v, int first, int count, int turb) {
-    if (count > 0)
-        k_sweep<TG_R, false><<<(count * SWEEP_LANES + SWEEP_CTA - 1) / SWEEP_CTA, SWEEP_CTA, 0, s>>>(
-            v.nbp, (const TG_R*)v.rec, (TG_R*)v.dq, v.n, first, count, turb);
-}
+void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained) { swp<true>(s, v, first, count, turb, chained); }
+void swu(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained) { swp<false>(s, v, first, count, turb, chained); }
 cudaError_t swa(cudaStream_t s, const SweepView& v, const int* po, int nplanes, int turb, SweepSync* sy, int grid, int block) {
     unsigned limit = SWEEP_SPIN_LIMIT;
     const int* nbp = v.nbp;

@@ -915,23 +915,47 @@ __global__ void __launch_bounds__(6 * 32) k_lusgs_jac(const DevBlock* __restrict
 // ---------------------------------------------------------------------------------------
 template <typename R, bool LOWER>
 __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
-                                  int L, int turb) {
-    if (L >= 7 || (L >= 5 && !turb)) return;
+                                  int L, int turb, bool chained = false) {
+    if (L >= 7 || (L >= 5 && !turb)) {
+        if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+        return;
+    }
     const int side = LOWER ? 0 : 3;
     const R sgn = LOWER ? R(1.0) : R(-1.0);
     auto REC = [&](int m) { return rec[sw_at(q, m, NREC)]; };
-    // all loads of the three neighbours are issued together: a missing neighbour (nbp < 0)
-    // reads this cell's own entries instead and its term is replaced by 0 afterwards
+    // Everything that does not depend on the previous hyperplane first: neighbour positions,
+    // this lane's Jacobian terms and radii, the diagonal.  A missing neighbour (nbp < 0) reads
+    // this cell's own entries instead and its term is replaced by 0 afterwards.
     long long npv[3];
+    R k[3][7];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) npv[d] = nbp[sw_at(q, side + d, 6)];
+    for (int d = 0; d < 3; ++d) {
+        npv[d] = nbp[sw_at(q, side + d, 6)];
+        const int jd = NBREC * (side + d);
+        k[d][6] = REC(jd + NJAC);                                   // spectral radius
+        if (L == 0) {
+            for (int m = 0; m < 3; ++m) k[d][m] = REC(jd + JC_R0 + m);
+        } else if (L < 4) {
+            for (int m = 0; m < 5; ++m) k[d][m] = REC(jd + JC_R1 + 5 * (L - 1) + m);
+        } else if (L == 4) {
+            for (int m = 0; m < 4; ++m) k[d][m] = REC(jd + JC_R4 + m);
+            k[d][4] = REC(jd + JC_VP);
+            k[d][5] = REC(jd + JC_GET1);
+        } else {
+            k[d][0] = REC(jd + JC_VPT);
+        }
+    }
+    const R stept = REC(REC_STEPT), cvs = REC(REC_CVS);
+    const R den = L < 5 ? REC(REC_FM) : REC(REC_FT);
+    // one launch per hyperplane chained with programmatic dependent launch: wait for the
+    // previous hyperplane to complete, then let the next one start its loads
+    if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
     R acc[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const bool has = npv[d] >= 0;
         const long long np = has ? npv[d] : q;
-        const int jd = NBREC * (side + d);
-        const R RDSt = REC(jd + NJAC);
+        const R RDSt = k[d][6];
         R val;
         // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1 line)
         if (L < 5) {
@@ -941,27 +965,21 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
             R Dif;
             if (L == 0) {
                 const R aSDt = R(0.0);
-                Dif = AinRo * aSDt + AinRx * REC(jd + JC_R0) + AinRy * REC(jd + JC_R0 + 1) + AinRz * REC(jd + JC_R0 + 2)
-                      + AinRe * R(0.0);
+                Dif = AinRo * aSDt + AinRx * k[d][0] + AinRy * k[d][1] + AinRz * k[d][2] + AinRe * R(0.0);
             } else if (L < 4) {
-                const int r = jd + JC_R1 + 5 * (L - 1);
-                Dif = AinRo * REC(r) + AinRx * REC(r + 1) + AinRy * REC(r + 2) + AinRz * REC(r + 3) + AinRe * REC(r + 4);
+                Dif = AinRo * k[d][0] + AinRx * k[d][1] + AinRy * k[d][2] + AinRz * k[d][3] + AinRe * k[d][4];
             } else {
-                const int r = jd + JC_R4;
-                Dif = AinRo * REC(jd + JC_VP) * REC(jd + JC_GET1) + AinRx * REC(r) + AinRy * REC(r + 1) + AinRz * REC(r + 2)
-                      + AinRe * REC(r + 3);
+                Dif = AinRo * k[d][4] * k[d][5] + AinRx * k[d][0] + AinRy * k[d][1] + AinRz * k[d][2] + AinRe * k[d][3];
             }
             const R Din = L == 0 ? AinRo : L == 1 ? AinRx : L == 2 ? AinRy : L == 3 ? AinRz : AinRe;
             val = R(0.5) * (Dif + sgn * (RDSt * Din));
         } else {
-            const R VP = REC(jd + JC_VPT);
+            const R VP = k[d][0];
             const R Dq = __ldcg(dq + sw_at(np, L, DQ_STRIDE));
             val = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
         }
         acc[d] = has ? val : R(0.0);
     }
-    const R stept = REC(REC_STEPT), cvs = REC(REC_CVS);
-    const R den = L < 5 ? REC(REC_FM) : REC(REC_FT);
     R* D = dq + sw_at(q, L, DQ_STRIDE);
     const R own = __ldcg(D);
     const R sum = acc[0] + acc[1] + acc[2];
@@ -969,13 +987,18 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
     else *D = own - sum * cvs / den;
 }
 
-// one hyperplane [first, first+count) per launch
+// one hyperplane [first, first+count) per launch (chained: launched with programmatic
+// stream serialisation, see sweep_item)
 template <typename R, bool LOWER>
-__global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int first, int count, int turb) {
+__global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int first, int count, int turb,
+                        int chained) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const int e = g / SWEEP_LANES, L = g % SWEEP_LANES;
-    if (e >= count) return;
-    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, turb);
+    if (e >= count) {
+        if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+        return;
+    }
+    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, turb, chained != 0);
 }
 
 // Grid-wide barrier of a co-resident (cooperative) grid.  The wait is bounded: after `limit`

@@ -39,8 +39,8 @@ struct FluxLaunchers {
     // LU-SGS right-hand sides + neighbour Jacobian terms into the sweep-order arrays
     void (*prep)(cudaStream_t, const DevBlock*, const SweepView&, const CaseDev*);
     void (*jac)(cudaStream_t, const DevBlock*, const SweepView&);     // neighbours' Jacobian terms
-    void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int turb);
-    void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int turb);
+    void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int turb, int chained);
+    void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int turb, int chained);
     // both sweeps in one cooperative launch (grid must be co-resident: grid <= SMs x occupancy)
     cudaError_t (*sweep_all)(cudaStream_t, const SweepView&, const int* plane_off, int nplanes, int turb, SweepSync*,
                              int grid, int block);

@@ -204,6 +204,10 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
 namespace {
 
 int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
+    if (mode == 0 && c->sweep_exec && c->sweep_exec_pdl != c->pdl) {       // chaining changed
+        cudaGraphExecDestroy(c->sweep_exec);
+        c->sweep_exec = nullptr;
+    }
     cudaStream_t s = c->stream;
     const int nh = (int)c->plane_off.size() - 1;
     if (mode == 2) {
@@ -227,11 +231,11 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     if (capture) {
         for (int h = 0; h < nh; ++h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, 1);
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, 1, c->pdl);
         }
         for (int h = nh - 1; h >= 0; --h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, 1);
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, 1, c->pdl);
         }
         return TRANS_OK;
     }
@@ -240,17 +244,18 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         for (int h = 0; h < nh; ++h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, 1);
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, 1, c->pdl);
         }
         for (int h = nh - 1; h >= 0; --h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, 1);
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, 1, c->pdl);
         }
         cudaError_t e = cudaStreamEndCapture(s, &g);
         if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph capture: ") + cudaGetErrorString(e));
         e = cudaGraphInstantiate(&c->sweep_exec, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph instantiate: ") + cudaGetErrorString(e));
+        c->sweep_exec_pdl = c->pdl;
     }
     CK(cudaGraphLaunch(c->sweep_exec, s));
     for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
@@ -272,15 +277,16 @@ int tune_sweeps(Ctx* c) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    struct Cand { int mode, grid, block; };
-    std::vector<Cand> cands = {{0, 0, 0}};
+    struct Cand { int mode, grid, block, pdl; };
+    std::vector<Cand> cands = {{0, 0, 0, 1}, {0, 0, 0, 0}};
     for (int block : {128, 256, 512}) {
         int occ = c->fl->sweep_all_occupancy(block);
         for (int per : {1, 2, 4})
-            if (per <= occ) cands.push_back({1, per * nsm, block});
+            if (per <= occ) cands.push_back({1, per * nsm, block, 0});
         int occf = c->fl->sweep_flow_occupancy(block);
-        if (block == 256 && occf >= 4) cands.push_back({2, 4 * nsm, block});
+        if (block == 256 && occf >= 4) cands.push_back({2, 4 * nsm, block, 0});
     }
+    const int pdl0 = c->pdl_allowed;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -289,6 +295,7 @@ int tune_sweeps(Ctx* c) {
     c->sweep_tuning.clear();
     int rc = save_dq(c, false);
     for (const Cand& k : cands) {
+        if (k.mode == 0) c->pdl = pdl0 ? k.pdl : 0;
         for (int rep = 0; rep < 2 && rc == TRANS_OK; ++rep) {      // first run warms up (graph build)
             if ((rc = save_dq(c, true))) break;
             CK(cudaEventRecord(e0, c->stream));
@@ -300,7 +307,8 @@ int tune_sweeps(Ctx* c) {
             CK(cudaEventElapsedTime(&ms, e0, e1));
             if (rep == 1) {
                 c->sweep_tuning += (k.mode ? std::string(k.mode == 1 ? "coop " : "flow ") + std::to_string(k.grid) + "x"
-                                                 + std::to_string(k.block) : std::string("planes"))
+                                                 + std::to_string(k.block)
+                                           : std::string(c->pdl ? "planes-chained" : "planes"))
                                    + ":" + std::to_string(ms) + "ms ";
                 if (ms < best) { best = ms; pick = k; }
             }
@@ -313,6 +321,7 @@ int tune_sweeps(Ctx* c) {
     if (rc) return rc;
     if ((rc = save_dq(c, true))) return rc;
     c->sweep_mode = pick.mode; c->sweep_grid = pick.grid; c->sweep_block = pick.block;
+    c->pdl = pick.mode == 0 ? (pdl0 ? pick.pdl : 0) : 0;
     return TRANS_OK;
 }
 
