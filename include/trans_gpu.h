@@ -131,10 +131,17 @@ enum trans_field {
     TRANS_DTM = 20,   /* Dtm(NIp2,NJp2,NKp2)                   local time step                */
     TRANS_DQDXYZ = 21,/* DQdxyz(18,-1:NIp2,-1:NJp2,-1:NKp2)    cell gradients                 */
     TRANS_SHOCK = 22, /* shock(-2:NIp2,-2:NJp2,-2:NKp2)        shock sensor                   */
-    TRANS_NFIELDS = 23
+    TRANS_WT2 = 23,   /* Wt2(7,NIp2,NJp2,NKp2)                 Runge-Kutta stage-1 state      */
+                      /*   (IF_RK = 1 cases only; Time/TIME_RK_Save.F90:16-28)                */
+    TRANS_NFIELDS = 24
 };
 
-/* Hot-path stages for trans_run_stage (each acts on all blocks, as main.F90 does). */
+/* Hot-path stages for trans_run_stage (each acts on all blocks, as main.F90 does).  With
+ * IF_RK = 1 an outer iteration has 3 sub-iterations (the SSP-RK3 stages, main.F90:54-56) and
+ * two stages change meaning (main.F90:152-161):
+ *   TRANS_STAGE_LUSGS  = TIME_RK_Save (stage 1) + TIME_RK + TURBTWO_TIME_LUSGS_SST
+ *   TRANS_STAGE_UPDATE = TIME_RK_V_Update_New
+ * (Time/TIME_RK_Save.F90:16-28, Time/TIME_RK.F90:27-86, Time/TIME_RK_V_Update_New.F90:66-320). */
 enum trans_stage {
     TRANS_STAGE_SPECRAD = 0,   /* TIME_SpectralRadius                         main.F90:66-69   */
     TRANS_STAGE_BC_STATE = 1,  /* BC_Boundarys(-1) (+ PARALLEL_BCs(-1))       main.F90:72-73   */
@@ -182,7 +189,8 @@ long long trans_kernel_launches(void* ctx);
  * that are advanced together: every kernel launch covers the blocks of all cases.  Cases are
  * added and removed while the context runs (continuous batching); a case is admitted only if
  * its device bytes fit the context's budget (TRANS_E_MEMORY otherwise, nothing allocated).
- * All cases of one context share the precision mode and the sub-iteration count (Kchld).
+ * All cases of one context share the precision mode, the time integrator (IF_RK) and the
+ * sub-iteration count (Kchld).
  * A case's KI starts at its KI_ini and advances by one per trans_batch_iterate step, so its
  * results do not depend on which other cases share the context.
  */
@@ -218,7 +226,8 @@ int trans_batch_cases(void* ctx, int* ids, int max);
  * The first call on a device looks the buffer up (cudaGetSymbolAddress) and should come
  * before any stream capture.  The buffer is shared by every context and call on a device and
  * keeps the last call's contents; concurrent calls race on it and must be serialised by the
- * caller.  norms: nblocks entries, may be NULL.
+ * caller.  norms: nblocks entries, may be NULL.  Runge-Kutta contexts (IF_RK = 1), whose
+ * update is TIME_RK_V_Update_New, get TRANS_E_ARG.
  */
 int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms);
 /* One outer iteration KI with CUDA events around every kernel launch on the context's stream:

@@ -1630,6 +1630,113 @@ void time_update_u(Ctx& c, Blk& b) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Runge-Kutta marching (IF_RK = 1, main.F90:152-161)
+// ---------------------------------------------------------------------------------------
+// Time/TIME_RK_Save.F90:16-28: the stage-1 state, all ML = 7 components
+void time_rk_save(Ctx& c, Blk& b) {
+    if (c.Itr_Chld != 1) return;
+    for (int L = 1; L <= 7; ++L)
+    for (int J = 1; J <= b.NJ1; ++J)
+    for (int K = 1; K <= b.NK1; ++K)
+    for (int I = 1; I <= b.NI1; ++I) b.Wt2(L, I, J, K) = b.V(L, I, J, K);
+}
+
+// Time/TIME_RK.F90:27-86: norms of |D1/V1| on the residual, then the SSP-RK3 stage on V(1:5)
+void time_rk(Ctx& c, Blk& b) {
+    b.nrm.nan_flag = 0;
+    double DRSa = 0.0, DUa = 0.0;
+    int Ima = 0, Jma = 0, Kma = 0;
+    for (int K = 1; K <= b.NK1; ++K)
+    for (int J = 1; J <= b.NJ1; ++J)
+    for (int I = 1; I <= b.NI1; ++I) {
+        double DR = std::fabs(b.D(1, I, J, K) / b.V(1, I, J, K));
+        if (std::isnan(b.D(1, I, J, K))) b.nrm.nan_flag = 1;
+        if (DUa <= DR) { DUa = DR; Ima = I; Jma = J; Kma = K; }
+        DRSa = DRSa + DR * DR;
+    }
+    DRSa = std::sqrt(DRSa / b.NI1 / b.NJ1 / b.NK1);
+    for (int K = 1; K <= b.NK1; ++K)
+    for (int J = 1; J <= b.NJ1; ++J)
+    for (int I = 1; I <= b.NI1; ++I)
+        for (int L = 1; L <= 5; ++L) {
+            const double dtm = b.Dtm(I, J, K), d = b.D(L, I, J, K), vol = b.Vol(I, J, K);
+            if (c.Itr_Chld == 1)
+                b.V(L, I, J, K) = b.V(L, I, J, K) + dtm * d / vol;
+            else if (c.Itr_Chld == 2)
+                b.V(L, I, J, K) = 0.75 * b.Wt2(L, I, J, K) + 0.25 * b.V(L, I, J, K) + 0.25 * dtm * d / vol;
+            else if (c.Itr_Chld == 3)
+                b.V(L, I, J, K) = 1.0 / 3.0 * b.Wt2(L, I, J, K) + 2.0 / 3.0 * b.V(L, I, J, K) + 2.0 / 3.0 * dtm * d / vol;
+        }
+    b.nrm.DRSa = DRSa; b.nrm.DUa = DUa; b.nrm.Ima = Ima; b.nrm.Jma = Jma; b.nrm.Kma = Kma;
+}
+
+// Time/TIME_RK_V_Update_New.F90:66-320: p and T from the new V (no rotation term), the SST
+// update of k and omega from the k-omega LU-SGS increments (Sutherland without Csth1), then
+// the k and omega norms on the updated density
+void time_rk_v_update(Ctx& c, Blk& b) {
+    const trans_params& p = c.p;
+    bool turb_upd = (p.IF_Euler == 0 && c.IF_turb == 1 && c.KI >= p.KItm);
+    for (int K = 1; K <= b.NK1; ++K)
+    for (int J = 1; J <= b.NJ1; ++J)
+    for (int I = 1; I <= b.NI1; ++I) {
+        double VV = b.V(2, I, J, K) * b.V(2, I, J, K) + b.V(3, I, J, K) * b.V(3, I, J, K) + b.V(4, I, J, K) * b.V(4, I, J, K);
+        b.PP(I, J, K) = (1.4 - 1.0) * b.V(5, I, J, K) - 0.5 * (1.4 - 1.0) * VV / b.V(1, I, J, K);
+        b.T(I, J, K) = p.RXM2 * b.PP(I, J, K) / b.V(1, I, J, K);
+        if (!turb_upd) continue;
+        double AinRTk = b.D(6, I, J, K), AinRTO = b.D(7, I, J, K);
+        double ARTk = b.V(6, I, J, K), ARTO = b.V(7, I, J, K);
+        if (AinRTk >= 0.0) ARTk = ARTk + AinRTk;
+        else ARTk = ARTk * otm::exp_(AinRTk / (ARTk + 1.e-10));
+        ARTk = std::max(ARTk, 1.0e-10);
+        if (AinRTO >= 0.0) ARTO = ARTO + AinRTO;
+        else ARTO = ARTO * otm::exp_(AinRTO / (ARTO + 1.e-10));
+        ARTO = std::max(ARTO, 1.0e-10);
+        double pRo = b.V(1, I, J, K);
+        VV = sq(b.V(2, I, J, K)) + sq(b.V(3, I, J, K)) + sq(b.V(4, I, J, K));
+        double PPP = 0.4 * b.V(5, I, J, K) - 0.2 * VV / pRo;
+        double TT = p.RXM2 * PPP / pRo;
+        double RmiuL = (1.0 + p.Csthlnd) / (TT + p.Csthlnd) * p15(TT);
+        double DistN = b.Dst(I, J, K);
+        double Dudx = b.DQ(1, I, J, K), Dudy = b.DQ(2, I, J, K), Dudz = b.DQ(3, I, J, K);
+        double Dvdx = b.DQ(4, I, J, K), Dvdy = b.DQ(5, I, J, K), Dvdz = b.DQ(6, I, J, K);
+        double Dwdx = b.DQ(7, I, J, K), Dwdy = b.DQ(8, I, J, K), Dwdz = b.DQ(9, I, J, K);
+        double Div = Dudx + Dvdy + Dwdz;
+        double prod = (2.0 * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy) + sq(Dwdx + Dudz)
+                       - 2.0 / 3.0 * Div * Div);
+        double arg2 = 2.0 * std::sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
+        arg2 = std::max(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
+        arg2 = otm::tanh_(arg2 * arg2);
+        double Sii = Dudx, Sjj = Dvdy, Skk = Dwdz;
+        double Sij = (Dudy + Dvdx) / 2.0, Sik = (Dudz + Dwdx) / 2.0, Sjk = (Dvdz + Dwdy) / 2.0;
+        double Skl = std::sqrt(2.0 * (1.0 * Sii * Sii + 1.0 * Sjj * Sjj + 1.0 * Skk * Skk + 2.0 * Sij * Sij + 2.0 * Sik * Sik + 2.0 * Sjk * Sjk));
+        double Cmua = std::min(1.0, p.A1 * ARTO / pRo / ((Skl) * arg2 + 1.e-10) * p.Ref);
+        ARTO = std::max(ARTO, std::sqrt(pRo * Cmua * std::fabs(prod) / (p.Prod_Lmt * p.Beta_star)) / p.Ref);
+        ARTk = std::min(ARTk, 100000.0 * RmiuL * ARTO / pRo / Cmua);
+        b.V(6, I, J, K) = ARTk;
+        b.V(7, I, J, K) = ARTO;
+        b.Rmiu(I, J, K) = Cmua * ARTk / ARTO * pRo;
+    }
+    double DRSk = 0, DUk = 0, DRSo = 0, DUo = 0;
+    for (int K = 1; K <= b.NK1; ++K)
+    for (int J = 1; J <= b.NJ1; ++J)
+    for (int I = 1; I <= b.NI1; ++I) {
+        double DRk = std::fabs(b.D(6, I, J, K) / b.V(1, I, J, K));
+        if (DUk <= DRk) DUk = DRk;
+        DRSk = DRSk + DRk * DRk;
+    }
+    DRSk = std::sqrt(DRSk / b.NI1 / b.NJ1 / b.NK1);
+    for (int K = 1; K <= b.NK1; ++K)
+    for (int J = 1; J <= b.NJ1; ++J)
+    for (int I = 1; I <= b.NI1; ++I) {
+        double DRo = std::fabs(b.D(7, I, J, K) / b.V(1, I, J, K));
+        if (DUo <= DRo) DUo = DRo;
+        DRSo = DRSo + DRo * DRo;
+    }
+    DRSo = std::sqrt(DRSo / b.NI1 / b.NJ1 / b.NK1);
+    b.nrm.DRSk = DRSk; b.nrm.DUk = DUk; b.nrm.DRSo = DRSo; b.nrm.DUo = DUo;
+}
+
+// ---------------------------------------------------------------------------------------
 // main.F90:54-171 stage by stage
 // ---------------------------------------------------------------------------------------
 void set_turb(Ctx& c) {
@@ -1674,13 +1781,21 @@ int run_stage(Ctx& c, int stage) {
         case TRANS_STAGE_LUSGS:
 #pragma omp parallel for schedule(dynamic)
             for (size_t n = 0; n < c.B.size(); ++n) {
-                time_lusgs(c, c.B[n]);
+                if (c.p.IF_RK == 1) {
+                    time_rk_save(c, c.B[n]);
+                    time_rk(c, c.B[n]);
+                } else {
+                    time_lusgs(c, c.B[n]);
+                }
                 if (c.IF_turb) turbtwo_lusgs_sst(c, c.B[n]);
             }
             break;
         case TRANS_STAGE_UPDATE:
 #pragma omp parallel for schedule(dynamic)
-            for (size_t n = 0; n < c.B.size(); ++n) time_update_v(c, c.B[n]);
+            for (size_t n = 0; n < c.B.size(); ++n) {
+                if (c.p.IF_RK == 1) time_rk_v_update(c, c.B[n]);
+                else time_update_v(c, c.B[n]);
+            }
             for (auto& b : c.B) c.nan_flag |= b.nrm.nan_flag;
             break;
         case TRANS_STAGE_UPDATE_U:
@@ -1722,6 +1837,7 @@ FieldDesc field_desc(int f) {
         case TRANS_DTM: return {&Blk::Dtm, 1, 1};
         case TRANS_DQDXYZ: return {&Blk::DQ, 18, -1};
         case TRANS_SHOCK: return {&Blk::shock, 1, -2};
+        case TRANS_WT2: return {&Blk::Wt2, 7, 1};
         default: return {nullptr, 0, 0};
     }
 }
@@ -1738,6 +1854,7 @@ int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks,
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return TRANS_E_ARG;
     if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 3)) return TRANS_E_ARG;
     if (p->omega[0] != 0.0 || p->omega[1] != 0.0 || p->omega[2] != 0.0) return TRANS_E_ARG;
+    if (p->IF_RK != 0 && p->IF_RK != 1) return TRANS_E_ARG;
     Ctx* c = new Ctx();
     c->p = *p;
     c->B.resize(nblocks);
@@ -1814,8 +1931,7 @@ int oracle_iterate(void* ctx, int ki, trans_norms* norms) {
     Ctx* c = static_cast<Ctx*>(ctx);
     c->KI = ki;
     set_turb(*c);
-    if (c->p.IF_RK != 0) return TRANS_E_ARG;
-    int nsub = c->p.Kind_Dual != 0 ? c->p.Kchld : 1;
+    int nsub = c->p.IF_RK == 1 ? 3 : (c->p.Kind_Dual != 0 ? c->p.Kchld : 1);      // main.F90:54-56
     c->nan_flag = 0;
     for (int it = 1; it <= nsub; ++it) {
         c->Itr_Chld = it;

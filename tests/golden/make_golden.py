@@ -26,6 +26,8 @@ CASES = {
     "channel_small_mdcd_ausmpw": ("channel", dict(Kind_Spatial=3, Kind_Roe=3)),
     "channel_small_muscl_roe": ("channel", dict(Kind_Spatial=2, Kind_Roe=1)),
     "cascade_small_mdcd_ausmpw": ("cascade", dict(Kind_Spatial=3, Kind_Roe=3)),
+    "channel_small_rk3_mdcd_ausmpw": ("channel", dict(Kind_Spatial=3, Kind_Roe=3, IF_RK=1, CFL_Sub_start=1.0,
+                                                      CFL_Sub_end=1.0)),
 }
 
 

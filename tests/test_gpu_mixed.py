@@ -1,7 +1,8 @@
 """Mixed-precision path (FP32 reconstruction, fluxes, SST sources and sweeps; FP64 update,
 metrics, time step and norms) against the FP64 path, through the C ABI.
 
-Tolerances (normwise relative, max|mixed - fp64| / max|fp64| per component):
+Tolerances (normwise relative, max|mixed - fp64| / max|fp64| per component, per equation group
+for the momentum):
   conserved variables, p, T after 20 iterations   5e-5
   residual-norm history (DRSa per iteration)       1e-2 (observed 2.8e-3 on the cascade)
 FP32 carries 24 bits (6e-8); the residual subtracts fluxes of similar size, so the FP32 error
@@ -33,8 +34,10 @@ def _run(case, precision, n):
 
 @pytest.mark.parametrize("make,scheme", [(small_channel, dict(Kind_Spatial=3, Kind_Roe=3)),
                                          (small_channel, dict(Kind_Spatial=2, Kind_Roe=1)),
-                                         (small_cascade, dict(Kind_Spatial=3, Kind_Roe=3))],
-                         ids=["channel_mdcd_ausmpw", "channel_muscl_roe", "cascade_mdcd_ausmpw"])
+                                         (small_cascade, dict(Kind_Spatial=3, Kind_Roe=3)),
+                                         (small_channel, dict(Kind_Spatial=3, Kind_Roe=3, IF_RK=1, CFL_Sub_start=1.0,
+                                                              CFL_Sub_end=1.0))],
+                         ids=["channel_mdcd_ausmpw", "channel_muscl_roe", "cascade_mdcd_ausmpw", "channel_rk3_mdcd_ausmpw"])
 def test_mixed_tracks_fp64(gpu_lib, make, scheme):
     case = make(**scheme)
     h64, f64 = _run(case, "fp64", 20)
@@ -44,9 +47,17 @@ def test_mixed_tracks_fp64(gpu_lib, make, scheme):
     assert herr <= TOL_HIST, f"residual history differs by {herr:.3e}"
     for ib, b in enumerate(case[0].blocks):
         m = interior(b.dims)
-        for name in ("V", "PP", "T"):
+        for name in ("PP", "T"):
             err = np.max(rel_err(f32[ib][name], f64[ib][name], m))
             assert err <= TOL_STATE, f"block {b.id} {name}: {err:.3e}"
+        # conserved variables, normwise per equation group: density, momentum (the spanwise
+        # component of these nearly two-dimensional flows is tiny on its own), energy, k, omega
+        for grp in ((0,), (1, 2, 3), (4,), (5,), (6,)):
+            scale = max(np.max(np.abs(f64[ib]["V"][q][m])) for q in grp)
+            if scale == 0.0:
+                continue
+            err = max(np.max(np.abs(f32[ib]["V"][q][m] - f64[ib]["V"][q][m])) for q in grp) / scale
+            assert err <= TOL_STATE, f"block {b.id} V{grp}: {err:.3e}"
 
 
 def test_mixed_residual_field_readback(gpu_lib):

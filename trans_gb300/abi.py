@@ -88,7 +88,7 @@ class TransNorms(C.Structure):
 
 # field ids (enum trans_field)
 FIELDS = ["V", "PP", "T", "RMIU", "WT0", "WT1", "SD", "GRAD", "VOL", "ALAGM", "DST", "ALENG",
-          "ASENG", "XC", "YC", "ZC", "RAD", "THTC", "D", "RDS", "DTM", "DQDXYZ", "SHOCK"]
+          "ASENG", "XC", "YC", "ZC", "RAD", "THTC", "D", "RDS", "DTM", "DQDXYZ", "SHOCK", "WT2"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 
 # Fortran allocation of each field: (leading components, lower bound, upper-bound offset from
@@ -100,6 +100,7 @@ FIELD_LAYOUT = {
     "DST": ((), -2), "ALENG": ((), -2), "ASENG": ((), 1),
     "XC": ((), 0), "YC": ((), 0), "ZC": ((), 0), "RAD": ((), -2), "THTC": ((), -2),
     "D": ((7,), 0), "RDS": ((3,), 0), "DTM": ((), 1), "DQDXYZ": ((18,), -1), "SHOCK": ((), -2),
+    "WT2": ((7,), 1),
 }
 
 STAGES = ["SPECRAD", "BC_STATE", "GRADIENT", "BC_GRAD", "RESIDUAL", "LUSGS", "UPDATE", "UPDATE_U"]

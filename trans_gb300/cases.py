@@ -50,12 +50,13 @@ def _flow(XM, Tinf=288.15, p_out_ratio=None, FSTI=0.01, VisRatio=1.0):
                     FSTI=FSTI, VisRatio=VisRatio)
 
 
-def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, **switches):
+def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, top=2, **switches):
     """Channel with a sinusoidal bump on the lower wall (single block, spanwise periodic).
 
     x in [-L, 2L], bump y = h sin^2(pi x / L) on [0, L], top at y = L, span `span` L.
     BCs: i-min inlet (kind 5), i-max outlet (kind 7), j-min no-slip wall (kind 1),
-    j-max far field (kind 2), k faces 1-to-1 onto each other (kind 9, periodic span).
+    j-max far field (kind 2; `top`=1 makes it a second no-slip wall), k faces 1-to-1 onto each
+    other (kind 9, periodic span).
     """
     ph = _flow(XM)
     sw = dict(Kind_Spatial=2, Kind_Roe=1, CFL_Sub_start=5.0, CFL_Sub_end=5.0, CFL_Sub_step=1,
@@ -78,10 +79,13 @@ def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, **
         X[:, j, :, 1] = (yw + (1.0 - yw) * s[j])[:, None]
     X[:, :, :, 2] = z[None, None, :]
     X /= alscale
-    segs = [Segment(1, kind=5), Segment(2, kind=7), Segment(3, kind=1), Segment(4, kind=2),
+    if top not in (1, 2):
+        raise ValueError("top boundary: kind 2 (far field) or 1 (wall)")
+    segs = [Segment(1, kind=5), Segment(2, kind=7), Segment(3, kind=1), Segment(4, kind=top),
             Segment(5, kind=9, blk_ex=1, blkbd_ex=6), Segment(6, kind=9, blk_ex=1, blkbd_ex=5)]
-    b = Block(1, X, segs, walls=[(3, 0, 0, 0, 0)])
-    return Case("channel_bump_%dx%dx%d" % (ni, nj, nk), p, [b], [X[:, 0, :, :]], ph,
+    b = Block(1, X, segs, walls=[(3, 0, 0, 0, 0)] + ([(4, 0, 0, 0, 0)] if top == 1 else []))
+    walls = [X[:, 0, :, :]] + ([X[:, -1, :, :]] if top == 1 else [])
+    return Case("channel_bump_%dx%dx%d" % (ni, nj, nk) + ("" if top == 2 else "_walls"), p, [b], walls, ph,
                 dict(Q_dst=0.05 / alscale, iterations=300))
 
 

@@ -84,7 +84,7 @@ int trans_stage_times(void* ctx, int ki, double* ms) {
     for (int q = 0; q <= TRANS_NSTAGES; ++q) CK(cudaEventCreate(&ev[q]));
     for (int q = 0; q < TRANS_NSTAGES; ++q) ms[q] = 0.0;
     const CaseRec* c0 = c->cases[0];
-    int nsub = c0->p.Kind_Dual != 0 ? c0->p.Kchld : 1;
+    int nsub = sub_iterations(c0->p);
     int rc = TRANS_OK;
     for (int it = 1; it <= nsub && rc == TRANS_OK; ++it)
         for (int st = TRANS_STAGE_SPECRAD; st <= TRANS_STAGE_UPDATE_U && rc == TRANS_OK; ++st) {

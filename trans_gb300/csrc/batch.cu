@@ -21,7 +21,7 @@ int trans_batch_create(int precision, long long device_budget_bytes, void** out)
 
 long long trans_batch_case_bytes(const trans_params* p, int nblocks, const trans_block* blocks) {
     if (validate_case(p, nblocks, blocks) != TRANS_OK) return -1;
-    return case_bytes(p->precision, nblocks, blocks);
+    return case_bytes(p, nblocks, blocks);
 }
 
 int trans_batch_add(void* ctx, const trans_params* p, int nblocks, const trans_block* blocks, int* case_id) {

@@ -44,7 +44,10 @@ enum Slot {
     S_FC1 = 146,        // SST F1 per cell (for the DES length scale of the next cell)
     S_RINV = 147,       // 1/rho
     S_SVEL = 148,       // 3: rho*u * (1/rho) etc., the velocities of the LU-SGS Jacobians
-    NSLOT = 151
+    NSLOT = 151,
+    // Runge-Kutta cases (IF_RK = 1) only: their blocks are allocated with NSLOT_RK slots
+    S_WT2 = 151,        // 7: the stage-1 state of the SSP-RK3 stages
+    NSLOT_RK = 158
 };
 
 // The DeltaQ-independent parts of A(Q)*DeltaQ (Time/TIME_LUSGS.F90:696-768) of one cell and

@@ -52,7 +52,8 @@ Params make_params(const trans_params& p) {
 
 // options outside the configurations of this hot path are rejected, never approximated
 bool params_supported(const trans_params* p) {
-    if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || p->Kind_Model != 1 || p->IF_Euler != 0 || p->IF_RK != 0) return false;
+    if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || p->Kind_Model != 1 || p->IF_Euler != 0) return false;
+    if (p->IF_RK != 0 && p->IF_RK != 1) return false;
     if ((p->Kind_Spatial != 2 && p->Kind_Spatial != 3) || (p->Kind_Roe != 1 && p->Kind_Roe != 3)) return false;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return false;
     if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 3)) return false;
@@ -106,14 +107,15 @@ int upload_walls(Ctx* c, const HostBlock& h, const DevBlock& b) {
 
 // Device bytes one case takes: its slot arena (+ FP32 copies in the mixed path) and its share
 // of the sweep-order arrays and work lists.
-long long case_bytes(int precision, int nblocks, const trans_block* blocks) {
+long long case_bytes(const trans_params* p, int nblocks, const trans_block* blocks) {
+    const int precision = p->precision;
     long long padded = 0, interior = 0;
     for (int n = 0; n < nblocks; ++n) {
         padded += (long long)(blocks[n].ni + 5) * (blocks[n].nj + 5) * (blocks[n].nk + 5);
         interior += (long long)(blocks[n].ni - 1) * (blocks[n].nj - 1) * (blocks[n].nk - 1);
     }
     const long long elem = precision == TRANS_MIXED ? 4 : 8;
-    long long b = padded * NSLOT * (8 + (precision == TRANS_MIXED ? 4 : 0));
+    long long b = padded * case_slots(*p) * (8 + (precision == TRANS_MIXED ? 4 : 0));
     b += interior * ((NREC + 2LL * DQ_STRIDE) * elem + 8LL * 4 + (long long)sizeof(SweepCell));
     b += interior / 16 + 4096;           // tiles, norm partials, boundary tables (rounded up)
     return b;
@@ -188,13 +190,14 @@ int case_add(Ctx* c, const trans_params* p, int nblocks, const trans_block* bloc
     if (!params_supported(p)) return fail(c, TRANS_E_ARG, "option outside the supported configurations");
     if (p->precision != c->precision) return fail(c, TRANS_E_ARG, "a context holds cases of one precision mode");
     for (CaseRec* o : c->cases) {
-        const int ns_o = o->p.Kind_Dual != 0 ? o->p.Kchld : 1, ns_p = p->Kind_Dual != 0 ? p->Kchld : 1;
-        if (ns_o != ns_p || (o->p.Kind_Dual != 0) != (p->Kind_Dual != 0))
+        if (o->p.IF_RK != p->IF_RK) return fail(c, TRANS_E_ARG, "cases of one context share the time integrator");
+        if (sub_iterations(o->p) != sub_iterations(*p) || (o->p.Kind_Dual != 0) != (p->Kind_Dual != 0))
             return fail(c, TRANS_E_ARG, "cases of one context share the sub-iteration count");
     }
     for (int n = 0; n < nblocks; ++n)
         if (!block_ok(blocks[n])) return fail(c, TRANS_E_ARG, "bad block dimensions or connectivity");
-    const long long need = case_bytes(p->precision, nblocks, blocks);
+    const long long need = case_bytes(p, nblocks, blocks);
+    const int nslot = case_slots(*p);
     if (c->budget > 0 && c->in_use + need > c->budget) return fail(c, TRANS_E_MEMORY, "case does not fit the device budget");
     CaseRec* cs = new CaseRec();
     cs->p = *p;
@@ -219,7 +222,7 @@ int case_add(Ctx* c, const trans_params* p, int nblocks, const trans_block* bloc
         b.PI = b.NI + 5; b.PJ = b.NJ + 5; b.PK = b.NK + 5;
         b.ncell = b.PI * b.PJ * b.PK;
         b.nint = b.NI1 * b.NJ1 * b.NK1;
-        total += (size_t)NSLOT * (size_t)b.ncell;
+        total += (size_t)nslot * (size_t)b.ncell;
     }
     cs->arena_doubles = total;
     auto bail = [&](int code, const char* what) {
@@ -238,7 +241,7 @@ int case_add(Ctx* c, const trans_params* p, int nblocks, const trans_block* bloc
     for (int n = 0; n < nblocks; ++n) {
         cs->blk[n].base = cs->arena + pos;
         cs->blk[n].fbase = cs->farena ? cs->farena + pos : nullptr;
-        pos += (size_t)NSLOT * (size_t)cs->blk[n].ncell;
+        pos += (size_t)nslot * (size_t)cs->blk[n].ncell;
         if (upload_walls(c, cs->hb[n], cs->blk[n])) return bail(TRANS_E_CUDA, "wall flags");
     }
     cs->norms.assign(nblocks, trans_norms{});

@@ -109,6 +109,7 @@ struct Ctx {
     int pdl = 1;                         // chain hyperplane launches (programmatic dependent launch)
     int pdl_allowed = 1;                 // chaining may be picked by the tuner (TRANS_PDL=0 forbids it)
     int sweep_exec_pdl = -1;             // chaining the sweep graph was captured with
+    int sweep_lanes = 1;                 // DeltaQ components swept: 1 = all, 2 = k and omega only (Runge-Kutta)
     SweepSync* d_sync = nullptr;
     SweepSync* h_sync = nullptr;         // pinned
     std::string sweep_tuning;
@@ -137,7 +138,11 @@ bool params_supported(const trans_params* p);
 int validate_case(const trans_params* p, int nblocks, const trans_block* blocks);
 int ctx_init(Ctx* c, int precision, long long budget);
 void ctx_free(Ctx* c);
-long long case_bytes(int precision, int nblocks, const trans_block* blocks);
+long long case_bytes(const trans_params* p, int nblocks, const trans_block* blocks);
+// sub-iterations of one outer iteration: 3 SSP-RK3 stages, Kchld dual-time steps or 1 (main.F90:54-56)
+inline int sub_iterations(const trans_params& p) { return p.IF_RK == 1 ? 3 : (p.Kind_Dual != 0 ? p.Kchld : 1); }
+// slots per padded cell of a case's blocks (Runge-Kutta cases keep the stage-1 state as well)
+inline int case_slots(const trans_params& p) { return p.IF_RK == 1 ? NSLOT_RK : NSLOT; }
 int case_add(Ctx* c, const trans_params* p, int nblocks, const trans_block* blocks, CaseRec** out);
 int case_remove(Ctx* c, int id);
 CaseRec* case_find(Ctx* c, int id);

@@ -71,13 +71,14 @@ int swa_occ(int block) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_all<TG_R>, block, 0) != cudaSuccess) return 0;
     return n;
 }
-cudaError_t swf(cudaStream_t s, const SweepView& v, int* flagL, int* flagU, SweepSync* sy, int grid, int block) {
+cudaError_t swf(cudaStream_t s, const SweepView& v, int* flagL, int* flagU, int turb, SweepSync* sy, int grid, int block) {
     unsigned limit = SWEEP_SPIN_LIMIT;
     const int* nbp = v.nbp;
     const TG_R* rec = (const TG_R*)v.rec;
     TG_R* dq = (TG_R*)v.dq;
     long long n = v.n;
-    void* args[] = {(void*)&nbp, (void*)&rec, (void*)&dq, (void*)&n, (void*)&flagL, (void*)&flagU, (void*)&sy, (void*)&limit};
+    void* args[] = {(void*)&nbp, (void*)&rec, (void*)&dq, (void*)&n, (void*)&flagL, (void*)&flagU, (void*)&turb, (void*)&sy,
+                    (void*)&limit};
     return cudaLaunchCooperativeKernel((const void*)k_sweep_flow<TG_R>, dim3(grid), dim3(block), args, 0, s);
 }
 int swf_occ(int block) {
@@ -85,9 +86,10 @@ int swf_occ(int block) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_flow<TG_R>, block, 0) != cudaSuccess) return 0;
     return n;
 }
-void scat(cudaStream_t s, const DevBlock* b, const SweepView& v) {
+void scat(cudaStream_t s, const DevBlock* b, const SweepView& v, int l0) {
     if (v.n > 0)
-        k_sweep_scatter<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(b, v.cells, (const TG_R*)v.dq, v.n);
+        k_sweep_scatter<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(b, v.cells, (const TG_R*)v.dq, v.n,
+                                                                                                  l0);
 }
 }  // namespace
 

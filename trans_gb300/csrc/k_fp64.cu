@@ -23,6 +23,13 @@ void launch_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int 
                    int d_fp32) {
     if (nt > 0) k_update<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev, parts, d_fp32);
 }
+void launch_rk_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, NormPart* parts, int d_fp32, int itr) {
+    if (nt > 0) k_rk_update<<<nt, CELL_TILE, 0, s>>>(blks, tiles, parts, d_fp32, itr);
+}
+void launch_rk_vupdate(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts,
+                       int d_fp32) {
+    if (nt > 0) k_rk_vupdate<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev, parts, d_fp32);
+}
 void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml) {
     if (total > 0) k_mirror<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off, ml);
 }

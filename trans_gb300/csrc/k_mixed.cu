@@ -3,6 +3,16 @@
 #define TG_R float
 #define TG_NAME flux_launchers_f32
 #include "flux_inst.cuh"
+#include "kernels_mixed.cuh"
+
+namespace tg {
+void launch_specrad_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev) {
+    if (nt > 0) k_specrad_mixed<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev);
+}
+void launch_update_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts) {
+    if (nt > 0) k_update_mixed<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev, parts);
+}
+}  // namespace tg
 
 // Throughput probes of the FP64 and FP32 pipes (independent fused multiply-add chains in
 // every thread of a grid covering all SMs); used to state the compute roof of the kernels.

@@ -770,29 +770,44 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell*
     const int c = cidx(b, I, J, K);
     auto REC = [&](int m) -> R& { return rec[sw_at(q, m, NREC)]; };
     auto DQ = [&](int L) -> R& { return dq[sw_at(q, L, DQ_STRIDE)]; };
-    // BDF2 right-hand side and the mean-flow diagonal, in FP64 in both paths
+    // BDF2 right-hand side and the mean-flow diagonal (TIME_LUSGS.F90:73-108).  FP64 path: the
+    // reference's operations.  Mixed path: the time-level difference 3V - 4Wt0 + Wt1 in FP64
+    // (it cancels), everything else in FP32 with one reciprocal of the volume.
     const double DT = pd.DT_LUSGS_Main;
-    double Dtm = slot(b, S_DTM)[c];
-    double vol = slot(b, S_VOL)[c];
-    double stept = 2.0 * Dtm / (3.0 * Dtm / DT + 2.0);
-    double cvs = stept / vol;
-    REC(REC_STEPT) = R(stept);
-    REC(REC_CVS) = R(cvs);
-    for (int L = 0; L < 5; ++L)
-        DQ(L) = R((double)rs<R>(b, S_D + L)[c] / vol
-                  - (3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c]) * 0.5 / DT);
-    double rsum = slot(b, S_RDS)[c] + slot(b, S_RDS + 1)[c] + slot(b, S_RDS + 2)[c];
-    double fm = 1.0 + rsum * cvs;
-    REC(REC_FM) = R(fm);
+    constexpr bool MIXED = sizeof(R) == 4;
+    R stept, cvs, fm;
+    auto rhs = [&](int L) {
+        const double bdf = 3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c];
+        if constexpr (MIXED) {
+            const R rvol = R(1.0) / rs<R>(b, S_VOL)[c];
+            return rs<R>(b, S_D + L)[c] * rvol - R(bdf) * (R(0.5) / R(DT));
+        } else {
+            return R((double)rs<R>(b, S_D + L)[c] / slot(b, S_VOL)[c] - bdf * 0.5 / DT);
+        }
+    };
+    if constexpr (MIXED) {
+        const R Dtm = rs<R>(b, S_DTM)[c], vol = rs<R>(b, S_VOL)[c];
+        stept = R(2.0) * Dtm / (R(3.0) * Dtm / R(DT) + R(2.0));
+        cvs = stept / vol;
+        fm = R(1.0) + (rs<R>(b, S_RDS)[c] + rs<R>(b, S_RDS + 1)[c] + rs<R>(b, S_RDS + 2)[c]) * cvs;
+    } else {
+        const double Dtm = slot(b, S_DTM)[c], vol = slot(b, S_VOL)[c];
+        const double st = 2.0 * Dtm / (3.0 * Dtm / DT + 2.0);
+        const double cv = st / vol;
+        const double rsum = slot(b, S_RDS)[c] + slot(b, S_RDS + 1)[c] + slot(b, S_RDS + 2)[c];
+        stept = R(st); cvs = R(cv); fm = R(1.0 + rsum * cv);
+    }
+    REC(REC_STEPT) = stept;
+    REC(REC_CVS) = cvs;
+    for (int L = 0; L < 5; ++L) DQ(L) = rhs(L);
+    REC(REC_FM) = fm;
     if (!turb) {            // the k-omega lanes of the sweeps then produce zeros
         DQ(5) = rs<R>(b, S_D + 5)[c];
         DQ(6) = rs<R>(b, S_D + 6)[c];
         REC(REC_FT) = R(1.0);
         return;
     }
-    for (int L = 5; L < 7; ++L)
-        DQ(L) = R((double)rs<R>(b, S_D + L)[c] / vol
-                  - (3.0 * slot(b, S_V + L)[c] - 4.0 * slot(b, S_WT0 + L)[c] + slot(b, S_WT1 + L)[c]) * 0.5 / DT);
+    for (int L = 5; L < 7; ++L) DQ(L) = rhs(L);
     auto G = [&](int q) { return rs<R>(b, S_DQ + q)[c]; };
     R dudx = G(0), dudy = G(1), dudz = G(2), dvdx = G(3), dvdy = G(4), dvdz = G(5), dwdx = G(6), dwdy = G(7), dwdz = G(8);
     R dtkdx = G(12), dtkdy = G(13), dtkdz = G(14), dtodx = G(15), dtody = G(16), dtodz = G(17);
@@ -912,11 +927,13 @@ __global__ void __launch_bounds__(6 * 32) k_lusgs_jac(const DevBlock* __restrict
 // SWEEP_LANES lanes per cell, lane L = component L of DeltaQ (0..4 mean flow, 5..6 k and
 // omega, the rest idle), so that the few FP64 operations left on the critical path (the
 // products with the neighbours' DeltaQ and one division) spread over many SM sub-partitions.
+// turb selects the components swept: 0 mean flow, 1 all, 2 k and omega only (the Runge-Kutta
+// path, whose mean flow is explicit).
 // ---------------------------------------------------------------------------------------
 template <typename R, bool LOWER>
 __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
                                   int L, int turb, bool chained = false) {
-    if (L >= 7 || (L >= 5 && !turb)) {
+    if (L >= 7 || (L >= 5 && turb == 0) || (L < 5 && turb == 2)) {
         if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
         return;
     }
@@ -1070,7 +1087,7 @@ __device__ inline bool flow_wait(const int* flag, long long q, int want, SweepSy
 
 template <typename R>
 __global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int* flagL, int* flagU,
-                             SweepSync* sy, unsigned limit) {
+                             int turb, SweepSync* sy, unsigned limit) {
     const long long T = (long long)gridDim.x * blockDim.x;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long items = N * SWEEP_LANES;
@@ -1084,7 +1101,7 @@ __global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ 
             if (np >= 0) ok = flow_wait<R>(flagL, np, 7, sy, limit);
         }
         if (!ok) return;
-        sweep_item<R, true>(nbp, rec, dq, N, q, L, 1);
+        sweep_item<R, true>(nbp, rec, dq, N, q, L, turb);
         __threadfence();
         atomicAdd(flagL + q, 1);
     }
@@ -1098,25 +1115,63 @@ __global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ 
             if (np >= 0) ok = flow_wait<R>(flagU, np, 7, sy, limit);
         }
         if (!ok) return;
-        sweep_item<R, false>(nbp, rec, dq, N, q, L, 1);
+        sweep_item<R, false>(nbp, rec, dq, N, q, L, turb);
         __threadfence();
         atomicAdd(flagU + q, 1);
     }
 }
 
 // DeltaQ back to the cells (the update and trans_get_field read it there)
+// (components l0..6: the Runge-Kutta path sweeps and returns only k and omega, l0 = 5)
 template <typename R>
 __global__ void k_sweep_scatter(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, const R* __restrict__ dq,
-                                long long N) {
+                                long long N, int l0) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= N) return;
     const SweepCell sc = cells[q];
     const DevBlock b = blks[sc.blk];
     const int c = cidx(b, sc.i, sc.j, sc.k);
-    for (int L = 0; L < 7; ++L) rs<R>(b, S_D + L)[c] = dq[sw_at(q, L, DQ_STRIDE)];
+    for (int L = l0; L < 7; ++L) rs<R>(b, S_D + L)[c] = dq[sw_at(q, L, DQ_STRIDE)];
 }
 
 #ifdef TG_COMMON_KERNELS
+// ---------------------------------------------------------------------------------------
+// SST update of k and omega at the end of an iteration (Time/TIME_Update_V.F90:709-816,
+// Time/TIME_RK_V_Update_New.F90:97-187, Kind_Model = 1): exp-positivity increments, the
+// F2-limited Cmu, the omega and k realizability limits and the eddy viscosity.  RmiuL is the
+// caller's laminar viscosity (the two routines evaluate Sutherland differently).
+// ---------------------------------------------------------------------------------------
+__device__ inline void sst_update(const Params& p, const DevBlock& b, int c, int d_fp32, double d6, double d7, double pRo,
+                                  double RmiuL) {
+    double* V5 = slot(b, S_V + 5);
+    double* V6 = slot(b, S_V + 6);
+    double ARTk = V5[c], ARTO = V6[c];
+    if (d6 >= 0.0) ARTk = ARTk + d6;
+    else ARTk = ARTk * tmx::exp_(d6 / (ARTk + 1.e-10));
+    ARTk = dmax(ARTk, 1.0e-10);
+    if (d7 >= 0.0) ARTO = ARTO + d7;
+    else ARTO = ARTO * tmx::exp_(d7 / (ARTO + 1.e-10));
+    ARTO = dmax(ARTO, 1.0e-10);
+    double DistN = slot(b, S_DST)[c];
+    auto G = [&](int q) { return d_fp32 ? (double)fslot(b, S_DQ + q)[c] : slot(b, S_DQ + q)[c]; };
+    double Dudx = G(0), Dudy = G(1), Dudz = G(2), Dvdx = G(3), Dvdy = G(4), Dvdz = G(5), Dwdx = G(6), Dwdy = G(7), Dwdz = G(8);
+    double Div = Dudx + Dvdy + Dwdz;
+    double prod = (2.0 * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy) + sq(Dwdx + Dudz)
+                   - 2.0 / 3.0 * Div * Div);
+    double arg2 = 2.0 * sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
+    arg2 = dmax(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
+    arg2 = tmx::tanh_(arg2 * arg2);
+    double Sii = Dudx, Sjj = Dvdy, Skk = Dwdz;
+    double Sij = (Dudy + Dvdx) / 2.0, Sik = (Dudz + Dwdx) / 2.0, Sjk = (Dvdz + Dwdy) / 2.0;
+    double Skl = sqrt(2.0 * (1.0 * Sii * Sii + 1.0 * Sjj * Sjj + 1.0 * Skk * Skk + 2.0 * Sij * Sij + 2.0 * Sik * Sik + 2.0 * Sjk * Sjk));
+    double Cmua = dmin(1.0, p.A1 * ARTO / pRo / ((Skl) * arg2 + 1.e-10) * p.Ref);
+    ARTO = dmax(ARTO, sqrt(pRo * Cmua * fabs(prod) / (p.Prod_Lmt * p.Beta_star)) / p.Ref);
+    ARTk = dmin(ARTk, 100000.0 * RmiuL * ARTO / pRo / Cmua);
+    V5[c] = ARTk;
+    V6[c] = ARTO;
+    slot(b, S_RMIU)[c] = Cmua * ARTk / ARTO * pRo;
+}
+
 // ---------------------------------------------------------------------------------------
 // Time/TIME_Update_V.F90:106-294 (norms) and :502-859 (update), FP64 in both paths
 // ---------------------------------------------------------------------------------------
@@ -1179,35 +1234,10 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
         double rr = p.omega0 * slot(b, S_RAD)[c];
         V[4][c] = pp / (1.4 - 1.0) + DV * pRo - 0.5 * sq(rr) * pRo;
         if (turb_upd) {   // TIME_Update_V.F90:709-816
-            double ARTk = V[5][c], ARTO = V[6][c];
-            if (d6 >= 0.0) ARTk = ARTk + d6;
-            else ARTk = ARTk * tmx::exp_(d6 / (ARTk + 1.e-10));
-            ARTk = dmax(ARTk, 1.0e-10);
-            if (d7 >= 0.0) ARTO = ARTO + d7;
-            else ARTO = ARTO * tmx::exp_(d7 / (ARTO + 1.e-10));
-            ARTO = dmax(ARTO, 1.0e-10);
             double VV = sq(V[1][c]) + sq(V[2][c]) + sq(V[3][c]);
             double PPP = (1.4 - 1.0) * V[4][c] - 0.5 * (1.4 - 1.0) * (VV / pRo - sq(rr) * pRo);
             double TT = p.RXM2 * PPP / pRo;
-            double RmiuL = mu_suth<double>(p, TT);
-            double DistN = slot(b, S_DST)[c];
-            auto G = [&](int q) { return d_fp32 ? (double)fslot(b, S_DQ + q)[c] : slot(b, S_DQ + q)[c]; };
-            double Dudx = G(0), Dudy = G(1), Dudz = G(2), Dvdx = G(3), Dvdy = G(4), Dvdz = G(5), Dwdx = G(6), Dwdy = G(7), Dwdz = G(8);
-            double Div = Dudx + Dvdy + Dwdz;
-            double prod = (2.0 * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy) + sq(Dwdx + Dudz)
-                           - 2.0 / 3.0 * Div * Div);
-            double arg2 = 2.0 * sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
-            arg2 = dmax(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
-            arg2 = tmx::tanh_(arg2 * arg2);
-            double Sii = Dudx, Sjj = Dvdy, Skk = Dwdz;
-            double Sij = (Dudy + Dvdx) / 2.0, Sik = (Dudz + Dwdx) / 2.0, Sjk = (Dvdz + Dwdy) / 2.0;
-            double Skl = sqrt(2.0 * (1.0 * Sii * Sii + 1.0 * Sjj * Sjj + 1.0 * Skk * Skk + 2.0 * Sij * Sij + 2.0 * Sik * Sik + 2.0 * Sjk * Sjk));
-            double Cmua = dmin(1.0, p.A1 * ARTO / pRo / ((Skl) * arg2 + 1.e-10) * p.Ref);
-            ARTO = dmax(ARTO, sqrt(pRo * Cmua * fabs(prod) / (p.Prod_Lmt * p.Beta_star)) / p.Ref);
-            ARTk = dmin(ARTk, 100000.0 * RmiuL * ARTO / pRo / Cmua);
-            V[5][c] = ARTk;
-            V[6][c] = ARTO;
-            slot(b, S_RMIU)[c] = Cmua * ARTk / ARTO * pRo;
+            sst_update(p, b, c, d_fp32, d6, d7, pRo, mu_suth<double>(p, TT));
         }
     }
     s_sum[0][tid] = sa; s_sum[1][tid] = sk; s_sum[2][tid] = so;
@@ -1232,6 +1262,128 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
         P.ma = s_max[0][0]; P.mk = s_max[1][0]; P.mo = s_max[2][0];
         P.ia = s_idx[0]; P.nan = s_nan[0]; P.pad_ = 0;
         parts[blockIdx.x] = P;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Runge-Kutta marching (IF_RK = 1), FP64 in both paths.
+// Time/TIME_RK_Save.F90:16-28 (Wt2 <- V at stage 1) and Time/TIME_RK.F90:27-86: the norms of
+// |D1/V1| on the residual before the update, then the SSP-RK3 stage on V(1:5).  Also leaves
+// 1/rho and the velocities of the new state for the k-omega sweep Jacobians (FP32 copies of
+// them and of V(1:5) in the mixed path), which TURBTWO_TIME_LUSGS_SST evaluates on it.
+// ---------------------------------------------------------------------------------------
+__global__ void k_rk_update(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, NormPart* __restrict__ parts,
+                            int d_fp32, int itr) {
+    const Tile t = tiles[blockIdx.x];
+    const DevBlock b = blks[t.blk];
+    __shared__ double s_sum[256];
+    __shared__ double s_max[256];
+    __shared__ long long s_idx[256];
+    __shared__ int s_nan[256];
+    const int tid = threadIdx.x;
+    double sa = 0, ma = -1;
+    long long ia = -1;
+    int nanf = 0;
+    if (tid < t.count) {
+        const int n = t.start + tid;
+        const int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+        const int c = cidx(b, I, J, K);
+        if (itr == 1)
+            for (int L = 0; L < 7; ++L) slot(b, S_WT2 + L)[c] = slot(b, S_V + L)[c];
+        auto Dq = [&](int L) { return d_fp32 ? (double)fslot(b, S_D + L)[c] : slot(b, S_D + L)[c]; };
+        const double d1 = Dq(0);
+        const double DR = fabs(d1 / slot(b, S_V)[c]);
+        nanf = isnan(d1) ? 1 : 0;
+        sa = DR * DR; ma = DR; ia = n;
+        const double dtm = slot(b, S_DTM)[c], vol = slot(b, S_VOL)[c];
+        double v[5];
+        for (int L = 0; L < 5; ++L) {
+            const double d = Dq(L), w = slot(b, S_WT2 + L)[c];
+            double x = slot(b, S_V + L)[c];
+            if (itr == 1) x = x + dtm * d / vol;
+            else if (itr == 2) x = 0.75 * w + 0.25 * x + 0.25 * dtm * d / vol;
+            else x = 1.0 / 3.0 * w + 2.0 / 3.0 * x + 2.0 / 3.0 * dtm * d / vol;
+            slot(b, S_V + L)[c] = x;
+            v[L] = x;
+        }
+        const double ri = 1.0 / v[0];
+        const double u = v[1] * ri, vv = v[2] * ri, w = v[3] * ri;
+        slot(b, S_RINV)[c] = ri;
+        slot(b, S_SVEL)[c] = u;
+        slot(b, S_SVEL + 1)[c] = vv;
+        slot(b, S_SVEL + 2)[c] = w;
+        if (d_fp32) {
+            for (int L = 0; L < 5; ++L) fslot(b, S_V + L)[c] = (float)v[L];
+            fslot(b, S_RINV)[c] = (float)ri;
+            fslot(b, S_SVEL)[c] = (float)u;
+            fslot(b, S_SVEL + 1)[c] = (float)vv;
+            fslot(b, S_SVEL + 2)[c] = (float)w;
+        }
+    }
+    s_sum[tid] = sa; s_max[tid] = ma; s_idx[tid] = ia; s_nan[tid] = nanf;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (tid < w) {
+            s_sum[tid] += s_sum[tid + w];
+            const double a = s_max[tid], bb = s_max[tid + w];      // the later cell wins ties (IF(DUa<=DR))
+            if (bb > a || (bb == a && s_idx[tid + w] > s_idx[tid])) { s_max[tid] = bb; s_idx[tid] = s_idx[tid + w]; }
+            s_nan[tid] |= s_nan[tid + w];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        NormPart& P = parts[blockIdx.x];
+        P.sa = s_sum[0]; P.ma = s_max[0]; P.ia = s_idx[0]; P.nan = s_nan[0]; P.pad_ = 0;
+    }
+}
+
+// Time/TIME_RK_V_Update_New.F90:66-320: p and T from the new V (no rotation term), the SST
+// update from the k-omega increments (Sutherland without Csth1), then the k and omega norms
+// on the updated density.
+__global__ void k_rk_vupdate(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const CaseDev* __restrict__ cdev,
+                             NormPart* __restrict__ parts, int d_fp32) {
+    const Tile t = tiles[blockIdx.x];
+    const DevBlock b = blks[t.blk];
+    const Params p = cdev[b.cs].p;
+    const int turb_upd = cdev[b.cs].turb_upd;
+    __shared__ double s_sum[2][256];
+    __shared__ double s_max[2][256];
+    const int tid = threadIdx.x;
+    double sk = 0, mk = 0, so = 0, mo = 0;
+    if (tid < t.count) {
+        const int n = t.start + tid;
+        const int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+        const int c = cidx(b, I, J, K);
+        const double v1 = slot(b, S_V)[c], v2 = slot(b, S_V + 1)[c], v3 = slot(b, S_V + 2)[c];
+        const double v4 = slot(b, S_V + 3)[c], v5 = slot(b, S_V + 4)[c];
+        double VV = v2 * v2 + v3 * v3 + v4 * v4;
+        const double pp = (1.4 - 1.0) * v5 - 0.5 * (1.4 - 1.0) * VV / v1;
+        slot(b, S_PP)[c] = pp;
+        slot(b, S_T)[c] = p.RXM2 * pp / v1;
+        auto Dq = [&](int L) { return d_fp32 ? (double)fslot(b, S_D + L)[c] : slot(b, S_D + L)[c]; };
+        const double d6 = Dq(5), d7 = Dq(6);
+        if (turb_upd) {
+            VV = sq(v2) + sq(v3) + sq(v4);
+            const double PPP = 0.4 * v5 - 0.2 * VV / v1;
+            const double TT = p.RXM2 * PPP / v1;
+            sst_update(p, b, c, d_fp32, d6, d7, v1, mu_suth_nocs<double>(p, TT));
+        }
+        const double DRk = fabs(d6 / v1), DRo = fabs(d7 / v1);
+        sk = DRk * DRk; mk = DRk; so = DRo * DRo; mo = DRo;
+    }
+    s_sum[0][tid] = sk; s_sum[1][tid] = so; s_max[0][tid] = mk; s_max[1][tid] = mo;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (tid < w)
+            for (int q = 0; q < 2; ++q) {
+                s_sum[q][tid] += s_sum[q][tid + w];
+                s_max[q][tid] = dmax(s_max[q][tid], s_max[q][tid + w]);
+            }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        NormPart& P = parts[blockIdx.x];
+        P.sk = s_sum[0][0]; P.so = s_sum[1][0]; P.mk = s_max[0][0]; P.mo = s_max[1][0];
     }
 }
 

@@ -1,0 +1,178 @@
+// kernels_mixed.cuh -- the FP64-state kernels of the mixed-precision path in a reduced-operation
+// form (included by k_mixed.cu only).
+//
+// On GB300 every FP64 instruction issues at 1/64 of the FP32 rate, and a double division or
+// square root is ~10 of them.  The FP64 path evaluates Time/SpectralRadius.F90 and
+// Time/TIME_Update_V.F90 operation by operation (bit-identical to the reference's arithmetic);
+// these mixed-path versions keep the same quantities in FP64 -- the conserved-variable update,
+// the local time step and the residual norms -- but
+//   - divide once per cell (a reciprocal) where the reference divides by the same value
+//     several times,
+//   - evaluate the increments of the positivity-preserving update, p*exp(dp/p) = p + p*expm1(dp/p),
+//     as an FP32 expm1 added to the FP64 value (the FP32 error scales with the increment, so it
+//     vanishes as the iteration converges),
+//   - evaluate the SST model algebra of the update (the F2-limited C_mu and the realizability
+//     limits of omega and k) and the spectral radii's square roots and Sutherland law in FP32,
+//     like the other SST and sweep arithmetic of the mixed path.
+#pragma once
+
+namespace tg {
+
+// ---------------------------------------------------------------------------------------
+// Time/SpectralRadius.F90:47-180, mixed path: spectral radii with FP32 square roots and
+// Sutherland law, accumulated in FP64; the local time step divides in FP64.
+// ---------------------------------------------------------------------------------------
+__global__ void k_specrad_mixed(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
+                                const CaseDev* __restrict__ cdev) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    const CaseDev& cd = cdev[b.cs];
+    const Params& p = cd.p;
+    const double CFL_sub = cd.CFL_sub;
+    const int n = t.start + threadIdx.x;
+    const int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+    const int c = cidx(b, I, J, K);
+    const double Den = slot(b, S_V)[c];
+    const double rden = 1.0 / Den;
+    const double Vxi = slot(b, S_V + 1)[c] * rden, Vyi = slot(b, S_V + 2)[c] * rden, Vzi = slot(b, S_V + 3)[c] * rden;
+    const double AAc = (double)sqrtf((float)(1.4 * slot(b, S_PP)[c] * rden));
+    const double RmiuL = (double)mu_suth<float>(cd.pf, (float)slot(b, S_T)[c]);
+    const double RmiuTL = slot(b, S_RMIU)[c];
+    const double uvmu = (RmiuL + RmiuTL + 1.0e-20) * (4.0 / 3.0);
+    const double uvmupr = (RmiuL * (1.0 / 0.72) + RmiuTL * (1.0 / 0.9) + 1.0e-20) * 1.4;
+    const double vol = slot(b, S_VOL)[c];
+    const double visc = 2.0 * dmax(uvmu, uvmupr) * rden / (vol * p.Ref);
+    double rs = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const double ARX = slot(b, S_ASD + 3 * d)[c], ARY = slot(b, S_ASD + 3 * d + 1)[c], ARZ = slot(b, S_ASD + 3 * d + 2)[c];
+        const double STsq = ARX * ARX + ARY * ARY + ARZ * ARZ;
+        const double UU = Vxi * ARX + Vyi * ARY + Vzi * ARZ;
+        const double Rd = fabs(UU) + (double)sqrtf((float)STsq) * AAc + STsq * visc;
+        slot(b, S_RDS + d)[c] = Rd;
+        rs += Rd;
+    }
+    const double Dtm_local = vol / rs;
+    double dtm = p.IF_Local_Main == 1 ? p.CFL_Main * Dtm_local : p.DT_LUSGS_Main;
+    if (p.Kind_Dual != 0) dtm = p.IF_Local_Sub == 1 ? CFL_sub * Dtm_local : p.DT_LUSGS_Sub;
+    slot(b, S_DTM)[c] = dtm;
+}
+
+// p + p*expm1(dp/(p+1e-10)) for dp < 0, p + dp otherwise (Time/TIME_Update_V.F90:660-675)
+__device__ inline double positive_add(double p, double dp) {
+    if (dp >= 0.0) return p + dp;
+    const float x = (float)dp / ((float)p + 1.0e-10f);
+    return p + p * (double)expm1f(x);
+}
+
+// ---------------------------------------------------------------------------------------
+// Time/TIME_Update_V.F90:106-294 (norms) and :621-816 (update), mixed path.  DeltaQ and the
+// gradients come from the FP32 copies.
+// ---------------------------------------------------------------------------------------
+__global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
+                               const CaseDev* __restrict__ cdev, NormPart* __restrict__ parts) {
+    const Tile t = tiles[blockIdx.x];
+    const DevBlock b = blks[t.blk];
+    const CaseDev& cd = cdev[b.cs];
+    const int turb_upd = cd.turb_upd;
+    __shared__ double s_sum[3][256];
+    __shared__ double s_max[3][256];
+    __shared__ long long s_idx[256];
+    __shared__ int s_nan[256];
+    const int tid = threadIdx.x;
+    double sa = 0, ma = -1, sk = 0, mk = 0, so = 0, mo = 0;
+    long long ia = -1;
+    int nanf = 0;
+    if (tid < t.count) {
+        const int n = t.start + tid;
+        const int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+        const int c = cidx(b, I, J, K);
+        double* V0 = slot(b, S_V);
+        double* V1 = slot(b, S_V + 1);
+        double* V2 = slot(b, S_V + 2);
+        double* V3 = slot(b, S_V + 3);
+        double* V4 = slot(b, S_V + 4);
+        auto Dq = [&](int L) { return (double)fslot(b, S_D + L)[c]; };
+        const double AinRo = Dq(0), AinRx = Dq(1), AinRy = Dq(2), AinRz = Dq(3), AinRe = Dq(4);
+        const double d6 = Dq(5), d7 = Dq(6);
+        double pRo = V0[c];
+        const double roinv = 1.0 / pRo;
+        nanf = isnan(AinRo) ? 1 : 0;
+        const double DR = fabs(AinRo) * roinv, DRk = fabs(d6) * roinv, DRo = fabs(d7) * roinv;
+        sa = DR * DR; ma = DR; ia = n;
+        sk = DRk * DRk; mk = DRk; so = DRo * DRo; mo = DRo;
+        double pVx = V1[c] * roinv, pVy = V2[c] * roinv, pVz = V3[c] * roinv;
+        const double AinX = (AinRx - pVx * AinRo) * roinv;
+        const double AinY = (AinRy - pVy * AinRo) * roinv;
+        const double AinZ = (AinRz - pVz * AinRo) * roinv;
+        const double AinP = (1.4 - 1.0) * (AinRe - 0.5 * AinRo * (pVx * pVx + pVy * pVy + pVz * pVz)
+                                           - pRo * (AinX * pVx + AinY * pVy + AinZ * pVz));
+        pRo = fabs(positive_add(pRo, AinRo));
+        double* PP = slot(b, S_PP);
+        const double pp = fabs(positive_add(PP[c], AinP));
+        PP[c] = pp;
+        const double T = cd.p.RXM2 * pp / pRo;
+        slot(b, S_T)[c] = T;
+        pVx += AinX; pVy += AinY; pVz += AinZ;
+        V0[c] = pRo;
+        V1[c] = pRo * pVx;
+        V2[c] = pRo * pVy;
+        V3[c] = pRo * pVz;
+        const double rr = cd.p.omega0 * slot(b, S_RAD)[c];
+        V4[c] = pp * (1.0 / (1.4 - 1.0)) + (0.5 * (pVx * pVx + pVy * pVy + pVz * pVz) - 0.5 * rr * rr) * pRo;
+        if (turb_upd) {   // TIME_Update_V.F90:709-816
+            double* V5 = slot(b, S_V + 5);
+            double* V6 = slot(b, S_V + 6);
+            double ARTk = dmax(positive_add(V5[c], d6), 1.0e-10);
+            double ARTO = dmax(positive_add(V6[c], d7), 1.0e-10);
+            const ParamsT<float>& p = cd.pf;
+            const float ro = (float)pRo, kf = (float)ARTk;
+            float of = (float)ARTO;
+            const float RmiuL = mu_suth<float>(p, (float)T);
+            const float DistN = fslot(b, S_DST)[c];
+            auto G = [&](int q) { return fslot(b, S_DQ + q)[c]; };
+            const float Dudx = G(0), Dudy = G(1), Dudz = G(2), Dvdx = G(3), Dvdy = G(4), Dvdz = G(5);
+            const float Dwdx = G(6), Dwdy = G(7), Dwdz = G(8);
+            const float Div = Dudx + Dvdy + Dwdz;
+            const float prod = 2.0f * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy)
+                               + sq(Dwdx + Dudz) - (2.0f / 3.0f) * Div * Div;
+            const float Ref = p.Ref, Bs = p.Beta_star;
+            float arg2 = 2.0f * sqrtf(kf / ro) / Bs / (of / ro) / DistN / Ref;
+            arg2 = fmaxf(arg2, 500.0f * RmiuL / DistN / DistN / of / Ref / Ref);
+            arg2 = tanhf(arg2 * arg2);
+            const float Sij = 0.5f * (Dudy + Dvdx), Sik = 0.5f * (Dudz + Dwdx), Sjk = 0.5f * (Dvdz + Dwdy);
+            const float Skl = sqrtf(2.0f * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz + 2.0f * (Sij * Sij + Sik * Sik + Sjk * Sjk)));
+            const float Cmua = fminf(1.0f, p.A1 * of / ro / (Skl * arg2 + 1.e-10f) * Ref);
+            ARTO = dmax(ARTO, (double)(sqrtf(ro * Cmua * fabsf(prod) / (p.Prod_Lmt * Bs)) / Ref));
+            of = (float)ARTO;
+            ARTk = dmin(ARTk, (double)(100000.0f * RmiuL * of / ro / Cmua));
+            V5[c] = ARTk;
+            V6[c] = ARTO;
+            slot(b, S_RMIU)[c] = (double)(Cmua * (float)ARTk / of * ro);
+        }
+    }
+    s_sum[0][tid] = sa; s_sum[1][tid] = sk; s_sum[2][tid] = so;
+    s_max[0][tid] = ma; s_max[1][tid] = mk; s_max[2][tid] = mo;
+    s_idx[tid] = ia; s_nan[tid] = nanf;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (tid < w) {
+            for (int q = 0; q < 3; ++q) s_sum[q][tid] += s_sum[q][tid + w];
+            const double a = s_max[0][tid], bb = s_max[0][tid + w];
+            if (bb > a || (bb == a && s_idx[tid + w] > s_idx[tid])) { s_max[0][tid] = bb; s_idx[tid] = s_idx[tid + w]; }
+            s_max[1][tid] = dmax(s_max[1][tid], s_max[1][tid + w]);
+            s_max[2][tid] = dmax(s_max[2][tid], s_max[2][tid + w]);
+            s_nan[tid] |= s_nan[tid + w];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        NormPart P;
+        P.sa = s_sum[0][0]; P.sk = s_sum[1][0]; P.so = s_sum[2][0];
+        P.ma = s_max[0][0]; P.mk = s_max[1][0]; P.mo = s_max[2][0];
+        P.ia = s_idx[0]; P.nan = s_nan[0]; P.pad_ = 0;
+        parts[blockIdx.x] = P;
+    }
+}
+
+}  // namespace tg

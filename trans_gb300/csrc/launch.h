@@ -24,6 +24,14 @@ void launch_block_norms(cudaStream_t s, const DevBlock* blks, int nblk, const No
                         BlockNorms* out);
 void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml);
 void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev);
+// the mixed path's reduced-operation forms of the spectral radius and the update (k_mixed.cu)
+void launch_specrad_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev);
+void launch_update_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts);
+// Runge-Kutta marching: stage update of V(1:5) with the |D1/V1| norm partials (itr = stage 1..3),
+// then p, T and the SST update with the k and omega norm partials
+void launch_rk_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, NormPart* parts, int d_fp32, int itr);
+void launch_rk_vupdate(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts,
+                       int d_fp32);
 void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, int lb, int is_sd, double* stage, int to_slots);
 double probe_fma_gflops(int fp64);
 void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
@@ -46,9 +54,9 @@ struct FluxLaunchers {
                              int grid, int block);
     int (*sweep_all_occupancy)(int block);          // resident blocks per SM
     // both sweeps as a dataflow over per-position ready flags (one cooperative launch)
-    cudaError_t (*sweep_flow)(cudaStream_t, const SweepView&, int* flagL, int* flagU, SweepSync*, int grid, int block);
+    cudaError_t (*sweep_flow)(cudaStream_t, const SweepView&, int* flagL, int* flagU, int turb, SweepSync*, int grid, int block);
     int (*sweep_flow_occupancy)(int block);
-    void (*scatter)(cudaStream_t, const DevBlock*, const SweepView&);     // DeltaQ back to cell order
+    void (*scatter)(cudaStream_t, const DevBlock*, const SweepView&, int l0);   // DeltaQ l0..6 back to cell order
     size_t elem;                                    // bytes of the sweep arithmetic type
 };
 const FluxLaunchers& flux_launchers_f64();

@@ -43,6 +43,7 @@ int static_norm_scratch(Ctx* c, NormPart** out) {
 extern "C" int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c || c->cases.empty()) return TRANS_E_ARG;
+    if (c->cases[0]->p.IF_RK == 1) return fail(c, TRANS_E_ARG, "trans_update_static_scratch is TIME_Update_V: LU-SGS cases only");
     int rc;
     if (!c->built && (rc = rebuild(c))) return rc;
     if (c->cell_tiles.size() > (size_t)kStaticNormTiles)
@@ -53,7 +54,8 @@ extern "C" int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms
     for (CaseRec* cs : c->cases) cs->KI = ki;
     if ((rc = finalize_geometry(c))) return rc;
     if ((rc = upload_cdev(c))) return rc;
-    launch_update(c->stream, c->d_blk, c->d_cell, (int)c->cell_tiles.size(), c->d_cdev, scratch, c->mixed ? 1 : 0);
+    if (c->mixed) launch_update_mixed(c->stream, c->d_blk, c->d_cell, (int)c->cell_tiles.size(), c->d_cdev, scratch);
+    else launch_update(c->stream, c->d_blk, c->d_cell, (int)c->cell_tiles.size(), c->d_cdev, scratch, 0);
     c->launches++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c->h_parts.data(), scratch, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, c->stream));

@@ -39,6 +39,7 @@ FieldMap field_map(int f) {
         case TRANS_DTM: return {S_DTM, 1, 1};
         case TRANS_DQDXYZ: return {S_DQ, 18, -1};
         case TRANS_SHOCK: return {S_SHOCK, 1, -2};
+        case TRANS_WT2: return {S_WT2, 7, 1};
         default: return {-1, 0, 0};
     }
 }
@@ -162,6 +163,7 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
     }
     FieldMap fm = field_map(f);
     if (fm.slot < 0) return fail(c, TRANS_E_ARG, "bad field id");
+    if (f == TRANS_WT2 && cs->p.IF_RK != 1) return fail(c, TRANS_E_ARG, "Wt2 exists in Runge-Kutta cases only");
     const DevBlock& b = c->blk[cs->blk0 + ib];
     size_t ncells = (size_t)(b.NI + 3 - fm.lb) * (b.NJ + 3 - fm.lb) * (b.NK + 3 - fm.lb);
     size_t bytes = ncells * fm.ncomp * sizeof(double);
@@ -214,14 +216,14 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         const size_t np = (size_t)((c->sv.n + 31) / 32 * 32);
         CK(cudaMemsetAsync(c->d_flags, 0, 2 * np * sizeof(int), s));
         CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
-        CK(c->fl->sweep_flow(s, c->sv, c->d_flags, c->d_flags + np, c->d_sync, grid, block));
+        CK(c->fl->sweep_flow(s, c->sv, c->d_flags, c->d_flags + np, c->sweep_lanes, c->d_sync, grid, block));
         CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
         c->launches++;
         return TRANS_OK;
     }
     if (mode == 1) {
         CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
-        CK(c->fl->sweep_all(s, c->sv, c->d_plane_off, nh, 1, c->d_sync, grid, block));
+        CK(c->fl->sweep_all(s, c->sv, c->d_plane_off, nh, c->sweep_lanes, c->d_sync, grid, block));
         CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
         c->launches++;
         return TRANS_OK;
@@ -231,11 +233,11 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     if (capture) {
         for (int h = 0; h < nh; ++h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, 1, c->pdl);
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, c->sweep_lanes, c->pdl);
         }
         for (int h = nh - 1; h >= 0; --h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, 1, c->pdl);
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, c->sweep_lanes, c->pdl);
         }
         return TRANS_OK;
     }
@@ -244,11 +246,11 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         for (int h = 0; h < nh; ++h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, 1, c->pdl);
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, c->sweep_lanes, c->pdl);
         }
         for (int h = nh - 1; h >= 0; --h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, 1, c->pdl);
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, c->sweep_lanes, c->pdl);
         }
         cudaError_t e = cudaStreamEndCapture(s, &g);
         if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph capture: ") + cudaGetErrorString(e));
@@ -346,7 +348,6 @@ namespace {
 // One stage.  capture: inside a CUDA-graph capture (no host synchronisation, no parameter
 // upload, the norms go to history slot `slot`).
 int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
-    (void)itr;
     if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
     int rc;
     if (!capture) {
@@ -359,7 +360,8 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
         case TRANS_STAGE_SPECRAD: {
             if (!capture && (rc = upload_cdev(c))) return rc;
             KScope t(c, K_SPECRAD);
-            launch_specrad(s, c->d_blk, c->d_cell, nct, c->d_cdev);
+            if (c->mixed) launch_specrad_mixed(s, c->d_blk, c->d_cell, nct, c->d_cdev);
+            else launch_specrad(s, c->d_blk, c->d_cell, nct, c->d_cdev);
             c->launches++;
             break;
         }
@@ -393,6 +395,13 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             break;
         case TRANS_STAGE_LUSGS: {
             if (!capture && (rc = upload_cdev(c))) return rc;
+            if (c->sweep_lanes == 2) {
+                // Runge-Kutta: TIME_RK_Save + TIME_RK on the mean flow, then the k-omega LU-SGS
+                // of TURBTWO_TIME_LUSGS_SST on the new state (main.F90:152-158)
+                KScope t(c, K_UPDATE);
+                launch_rk_update(s, c->d_blk, c->d_cell, nct, c->d_parts, c->mixed ? 1 : 0, itr);
+                c->launches++;
+            }
             if (any_case(c, wants_des)) {
                 KScope t(c, K_SST_FC1);
                 c->fl->sst_fc1(s, c->d_blk, c->d_cell, nct, c->d_cdev);
@@ -408,7 +417,7 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
                 else rc = run_sweeps(c);
                 if (rc) return rc;
             }
-            { KScope t(c, K_SCATTER); c->fl->scatter(s, c->d_blk, c->sv); }
+            { KScope t(c, K_SCATTER); c->fl->scatter(s, c->d_blk, c->sv, c->sweep_lanes == 2 ? 5 : 0); }
             c->launches++;
             break;
         }
@@ -417,7 +426,9 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             const int nblk = (int)c->blk.size();
             {
                 KScope t(c, K_UPDATE);
-                launch_update(s, c->d_blk, c->d_cell, nct, c->d_cdev, c->d_parts, c->mixed ? 1 : 0);
+                if (c->sweep_lanes == 2) launch_rk_vupdate(s, c->d_blk, c->d_cell, nct, c->d_cdev, c->d_parts, c->mixed ? 1 : 0);
+                else if (c->mixed) launch_update_mixed(s, c->d_blk, c->d_cell, nct, c->d_cdev, c->d_parts);
+                else launch_update(s, c->d_blk, c->d_cell, nct, c->d_cdev, c->d_parts, 0);
                 launch_block_norms(s, c->d_blk, nblk, c->d_parts, c->d_tile_first, c->d_norms + (size_t)slot * nblk);
             }
             c->launches += 2;
@@ -451,7 +462,7 @@ int run_stage(Ctx* c, int stage, int itr) { return stage_exec(c, stage, itr, fal
 int run_iteration(Ctx* c) {
     if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
     const CaseRec* c0 = c->cases[0];
-    const int nsub = c0->p.Kind_Dual != 0 ? c0->p.Kchld : 1;
+    const int nsub = sub_iterations(c0->p);
     int rc = TRANS_OK;
     for (int it = 1; it <= nsub && rc == TRANS_OK; ++it)
         for (int st = TRANS_STAGE_SPECRAD; st <= TRANS_STAGE_UPDATE && rc == TRANS_OK; ++st)
@@ -484,7 +495,7 @@ bool switches_fixed(Ctx* c, int n) {
 int capture_iterations(Ctx* c, int n) {
     if (c->iter_exec) { cudaGraphExecDestroy(c->iter_exec); c->iter_exec = nullptr; c->iter_n = 0; }
     const CaseRec* c0 = c->cases[0];
-    const int nsub = c0->p.Kind_Dual != 0 ? c0->p.Kchld : 1;
+    const int nsub = sub_iterations(c0->p);
     const int nblk = (int)c->blk.size();
     cudaStream_t s = c->stream;
     cudaGraph_t g = nullptr;

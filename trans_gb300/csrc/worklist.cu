@@ -157,6 +157,8 @@ int rebuild(Ctx* c) {
     c->bc.clear(); c->outlet.clear(); c->lines.clear(); c->sweep.clear(); c->plane_off.clear();
     c->cdev_last.clear();
     if (c->cases.empty()) return TRANS_OK;
+    // Runge-Kutta cases sweep only k and omega (TURBTWO_TIME_LUSGS_SST; the mean flow is explicit)
+    c->sweep_lanes = c->cases[0]->p.IF_RK == 1 ? 2 : 1;
     // blocks of all cases, in case order
     for (size_t k = 0; k < c->cases.size(); ++k) {
         CaseRec* cs = c->cases[k];
