@@ -79,3 +79,21 @@ def test_parameters_follow_parameterset():
     assert p.Rof == pytest.approx(1.2 * p.Rkf / p.Rmiuf)
     # static inflow pressure 1/(1.4 M^2) with rho = 1: the total-pressure ratio of M = 0.5
     assert p.P0in / p.PPF == pytest.approx((1 + 0.2 * 0.25) ** 3.5, rel=1e-12)
+
+
+def test_square_cylinder_grid():
+    """The square-cylinder O-block: positive volumes, the wrap cut and the periodic span found
+    as 1-to-1 connections, the seeded velocity perturbation applied to the interior only."""
+    import numpy as np
+    from trans_gb300 import cases
+    from trans_gb300 import case as CS
+    c = cases.square_cylinder(ni=33, nj=17, nk=9)
+    assert c.params.Kind_Hybrid == 3 and c.params.Kchld == 10 and c.params.Kind_Dual == 2
+    conns, geo = CS.compute_geometry(c)
+    g = geo[c.blocks[0].id]
+    vol = g["VOL"][3:3 + 32, 3:3 + 16, 3:3 + 8]
+    assert (vol > 0).all()
+    st = CS.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
+    V = st[c.blocks[0].id]["V"]
+    u = V[1][3:3 + 32, 8:3 + 16, 3:3 + 8] / V[0][3:3 + 32, 8:3 + 16, 3:3 + 8]
+    assert 0.002 < np.std(u) < 0.05

@@ -688,7 +688,14 @@ def standard_normal(rng, shape):
     return z.reshape(shape)
 
 
-def initial_state(case, geo, Q_dst=0.01, If_NS_uniform=0, noise=1.0e-4, seed=0):
+def initial_state(case, geo, Q_dst=0.01, If_NS_uniform=0, noise=1.0e-4, seed=0, velocity_noise=None):
+    """The reference's KR=0 initialisation (Input/Init.F90:94-169) plus seeded perturbations:
+    `noise` relative Gaussian on the density (drawn from `seed`) and, if the case asks for it
+    (meta "velocity_noise"), a relative Gaussian perturbation of the streamwise velocity drawn
+    from seed+1 (the density stream is unchanged by it)."""
+    if velocity_noise is None:
+        velocity_noise = case.meta.get("velocity_noise", 0.0)
+    vrng = np.random.default_rng(seed + 1)
     p = case.params
     rng = np.random.default_rng(seed)
     st = {}
@@ -710,6 +717,8 @@ def initial_state(case, geo, Q_dst=0.01, If_NS_uniform=0, noise=1.0e-4, seed=0):
         if If_NS_uniform == 0:
             Rat = 1.0 - dm.exp(-Coff_dst * Dst)
             V2 = np.where(Dst < Q_dst, V2 * Rat, V2)
+        if velocity_noise:
+            V2 = V2 * (1.0 + velocity_noise * standard_normal(vrng, Dst.shape))
         V5 = P / 0.4 + 0.5 * (V2 * V2 + V3 * V3 + V4 * V4) - 0.5 * ((om * rad) * (om * rad))
         C1, C2 = 45.8, 1.68
         Smax = C2 / (2.0 * C1)

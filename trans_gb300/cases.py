@@ -275,3 +275,89 @@ def cascade(nle=8, nte=4, ns=120, npitch=16, nr=48, nh=64, nk=64, Re_c=1.0e6, XM
     name = "cascade_5blk_%dcells" % sum(int(np.prod([d - 1 for d in b.dims])) for b in blocks)
     return Case(name, p, blocks, surfaces, ph, dict(Q_dst=0.02 / alscale, chord=scale, pitch=pitch * scale,
                                                     p_ratio=p_ratio))
+
+
+# --------------------------------------------------------------------------------------------
+# Square cylinder, one O-block, time-accurate DES (dual time stepping).
+# --------------------------------------------------------------------------------------------
+def _square_loop(n_side, half):
+    """Nodes around a square of half-width `half` (closed loop, counterclockwise from the
+    middle of the rear face), `n_side` cells per side: 4*n_side + 1 nodes, last = first."""
+    corners = [(half, half), (-half, half), (-half, -half), (half, -half)]
+    pts = []
+    # rear face upper half: (half, 0) -> (half, half)
+    h = n_side // 2
+    t = np.linspace(0.0, 1.0, h + 1)
+    pts.append(np.stack([np.full(h + 1, half), t * half], axis=1))
+    prev = corners[0]
+    for cnr in corners[1:]:
+        t = np.linspace(0.0, 1.0, n_side + 1)[1:]
+        pts.append(np.stack([prev[0] + (cnr[0] - prev[0]) * t, prev[1] + (cnr[1] - prev[1]) * t], axis=1))
+        prev = cnr
+    t = np.linspace(0.0, 1.0, n_side - h + 1)[1:]
+    pts.append(np.stack([np.full(n_side - h, half), -half + t * half], axis=1))
+    return np.concatenate(pts, axis=0)
+
+
+def _rect_loop(n_side, x0, x1, y0, y1, xc=0.0):
+    """The same node count around the rectangle [x0,x1]x[y0,y1], side by side with
+    _square_loop (rear face <-> outflow side, etc.)."""
+    h = n_side // 2
+    pts = []
+    t = np.linspace(0.0, 1.0, h + 1)
+    pts.append(np.stack([np.full(h + 1, x1), t * y1], axis=1))
+    corners = [(x1, y1), (x0, y1), (x0, y0), (x1, y0)]
+    prev = corners[0]
+    for cnr in corners[1:]:
+        t = np.linspace(0.0, 1.0, n_side + 1)[1:]
+        pts.append(np.stack([prev[0] + (cnr[0] - prev[0]) * t, prev[1] + (cnr[1] - prev[1]) * t], axis=1))
+        prev = cnr
+    t = np.linspace(0.0, 1.0, n_side - h + 1)[1:]
+    pts.append(np.stack([np.full(n_side - h, x1), y0 + t * (0.0 - y0)], axis=1))
+    return np.concatenate(pts, axis=0)
+
+
+def square_cylinder(ni=385, nj=257, nk=129, Re_D=2.0e4, XM=0.2, span=4.0, box=(-10.0, 20.0, -10.0, 10.0),
+                    dt_UD=0.005, perturbation=0.01, **switches):
+    """Wake of a square cylinder (side D = 1): one O-block around it, i around the section
+    (wrapping through a self 1-to-1 cut: i-min onto i-max), j from the wall (kind 1) to a
+    rectangular outer boundary `box` (far field, kind 2), k spanwise over `span` D (periodic
+    1-to-1).  DES (Kind_Hybrid = 3, Kind_SubHY = 0) with dual time stepping: Kchld
+    sub-iterations per physical step dt*U/D = dt_UD.  The initial field is the freestream with
+    a seeded `perturbation` relative Gaussian perturbation of the velocity."""
+    if (ni - 1) % 4:
+        raise ValueError("ni - 1 must be a multiple of 4 (cells per side of the square)")
+    ph = _flow(XM)
+    sw = dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3, Kind_SubHY=0, CFL_Sub_start=5.0, CFL_Sub_end=5.0,
+              CFL_Sub_step=1, Kind_Dual=2, Kchld=10, DT_LUSGS_Main=1.0, gama_max=0.0463783, gama_min=0.0)
+    sw.update(switches)
+    p0 = make_params(ph, **sw)
+    alscale = p0.Ref / (Re_D * mu_laminar_nd(p0, 1.0))
+    sw["Alscale"] = alscale
+    # the physical time step in the reference's units (length 1/alscale = D, velocity Vref)
+    if "DT_LUSGS_Main" not in switches:
+        sw["DT_LUSGS_Main"] = dt_UD / alscale
+    p = make_params(ph, **sw)
+    n_side = (ni - 1) // 4
+    inner = _square_loop(n_side, 0.5)
+    outer = _rect_loop(n_side, *box)
+    # wall-normal distribution: geometric from y+ ~ 1 at the wall, the same parameter on
+    # every i-line (transfinite interpolation between the square and the rectangle)
+    cf = 0.0576 * dm.pow(Re_D, -0.2)
+    dy1 = 1.0 / (Re_D * math.sqrt(0.5 * cf))
+    reach = float(np.mean(np.hypot(outer[:, 0] - inner[:, 0], outer[:, 1] - inner[:, 1])))
+    eta = geometric_spacing(nj - 1, dy1 / reach, 1.0)
+    z = np.linspace(0.0, span, nk)
+    X = np.empty((ni, nj, nk, 3))
+    for j in range(nj):
+        X[:, j, :, 0] = (inner[:, 0] + eta[j] * (outer[:, 0] - inner[:, 0]))[:, None]
+        X[:, j, :, 1] = (inner[:, 1] + eta[j] * (outer[:, 1] - inner[:, 1]))[:, None]
+    X[:, :, :, 2] = z[None, None, :]
+    X /= alscale
+    segs = [Segment(1, kind=9, blk_ex=1, blkbd_ex=2), Segment(2, kind=9, blk_ex=1, blkbd_ex=1),
+            Segment(3, kind=1), Segment(4, kind=2),
+            Segment(5, kind=9, blk_ex=1, blkbd_ex=6), Segment(6, kind=9, blk_ex=1, blkbd_ex=5)]
+    b = Block(1, X, segs, walls=[(3, 0, 0, 0, 0)])
+    return Case("square_cylinder_%dx%dx%d" % (ni, nj, nk), p, [b], [X[:, 0, :, :]], ph,
+                dict(Q_dst=0.05 / alscale, velocity_noise=perturbation, D=1.0 / alscale, dt_UD=dt_UD,
+                     steps=2000))
