@@ -2,6 +2,8 @@
 iteration count, the throughput and the integrated quantities (trans_gb300.integrals).
 
     python -m trans_gb300.converge --case cascade --precision mixed --drop 1e-6 --max-iters 20000
+    python -m trans_gb300.converge --case cascade --level coarse --scheme muscl_roe --compare
+    python -m trans_gb300.converge --case channel_walls --laminar --Re 1e4 --compare
 
 With --compare both precisions run on the same case and the relative differences of the
 mixed-precision results from the FP64 ones are reported (mass flow, total-pressure loss, blade
@@ -20,9 +22,15 @@ from . import integrals
 from .solver import Batch, global_residual
 
 
+SCHEMES = {"mdcd_ausmpw": dict(Kind_Spatial=3, Kind_Roe=3), "muscl_roe": dict(Kind_Spatial=2, Kind_Roe=1)}
+LEVELS = {"coarse": dict(ns=60, nh=32, nk=32), "medium": dict(nk=32), "full": dict()}
+
+
 def make(name, precision, **kw):
     if name == "channel":
         c = cases.channel_bump(precision=precision, **kw)
+    elif name == "channel_walls":          # no-slip walls on both sides instead of a far field
+        c = cases.channel_bump(precision=precision, top=1, **kw)
     elif name == "cascade":
         c = cases.cascade(precision=precision, **kw)
     else:
@@ -78,8 +86,20 @@ def main():
     ap.add_argument("--chunk", type=int, default=50)
     ap.add_argument("--compare", action="store_true", help="run FP64 and mixed and report their differences")
     ap.add_argument("--nk", type=int, default=None, help="spanwise cells of the cascade")
+    ap.add_argument("--level", default=None, choices=sorted(LEVELS), help="cascade grid level")
+    ap.add_argument("--scheme", default=None, choices=sorted(SCHEMES), help="reconstruction + flux")
+    ap.add_argument("--laminar", action="store_true", help="laminar (IF_Turb_org = 0)")
+    ap.add_argument("--Re", type=float, default=None, help="channel Reynolds number Re_L")
     args = ap.parse_args()
-    kw = {} if args.nk is None else {"nk": args.nk}
+    kw = dict(LEVELS[args.level]) if args.level else {}
+    if args.nk is not None:
+        kw["nk"] = args.nk
+    if args.scheme:
+        kw.update(SCHEMES[args.scheme])
+    if args.laminar:
+        kw["IF_Turb_org"] = 0
+    if args.Re is not None:
+        kw["Re_L"] = args.Re
     if args.compare:
         r64, s64 = run(args.case, abi.TRANS_FP64, args.drop, args.max_iters, args.chunk, **kw)
         r32, s32 = run(args.case, abi.TRANS_MIXED, args.drop, args.max_iters, args.chunk, **kw)
