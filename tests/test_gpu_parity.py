@@ -220,15 +220,21 @@ def test_gpu_against_golden_vectors(gpu_lib, name):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
     """The hyperplane-per-launch schedule, the single cooperative launch with grid barriers, the
-    dataflow schedule (and the tuner's pick) compute every DeltaQ with the same operations:
-    states after 6 iterations are bit-identical."""
+    dataflow schedule, the tiled wavefront (two tile shapes), each with the lane-major and the
+    warp-per-component thread mapping, and the tuner's pick compute every DeltaQ with the same
+    operations: states after 6 iterations are bit-identical."""
     from helpers import small_cascade
     from trans_gb300 import abi
     from trans_gb300.solver import Solver
     out = {}
-    for mode in ("planes", "planes_unchained", "coop", "flow", "auto"):
-        monkeypatch.setenv("TRANS_SWEEP", mode.split("_")[0])
-        monkeypatch.setenv("TRANS_PDL", "0" if mode.endswith("unchained") else "1")
+    modes = ("planes", "planes_unchained", "coop", "flow", "tiles", "tiles_4x2x3", "planes_wpc", "planes_unchained_wpc",
+             "coop_wpc", "tiles_4x2x3_wpc", "auto")
+    for mode in modes:
+        parts = mode.split("_")
+        monkeypatch.setenv("TRANS_SWEEP", parts[0])
+        monkeypatch.setenv("TRANS_PDL", "0" if "unchained" in parts else "1")
+        monkeypatch.setenv("TRANS_TILE", next((x for x in parts if "x" in x), "8x8x8"))
+        monkeypatch.setenv("TRANS_SWEEP_MAP", "wpc" if "wpc" in parts else "lane")
         c, conns, geo, st = small_cascade(Kind_Spatial=3, Kind_Roe=3)
         c.params.precision = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
         s = Solver(c, conns, geo, st)
@@ -236,7 +242,7 @@ def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
             s.iterate(ki)
         out[mode] = [s.get_field(ib, "V") for ib in range(len(c.blocks))]
         s.close()
-    for mode in ("planes_unchained", "coop", "flow", "auto"):
+    for mode in modes[1:]:
         for ib in range(len(out["planes"])):
             m = interior(c.blocks[ib].dims)
             assert bit_equal_fraction(out[mode][ib], out["planes"][ib], m) == 1.0, (mode, ib)

@@ -180,10 +180,12 @@ const char* trans_tuning(void* ctx) {
     Ctx* c = as_ctx(ctx);
     if (!c) return "no context";
     static thread_local std::string out;
-    out = "sweep=" + std::string(c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : "flow ") + std::to_string(c->sweep_grid)
-                                                      + "x" + std::to_string(c->sweep_block)
+    const std::string tiles = c->sweep_mode == 3 ? std::to_string(c->tile_shape[0]) + "x" + std::to_string(c->tile_shape[1]) + "x"
+                                                       + std::to_string(c->tile_shape[2]) + "/" : std::string();
+    out = "sweep=" + std::string(c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : c->sweep_mode == 2 ? "flow " : "tiles ")
+                                                      + tiles + std::to_string(c->sweep_grid) + "x" + std::to_string(c->sweep_block)
                                  : c->sweep_mode == 0 ? (c->pdl ? "planes-chained" : "planes") : "untuned")
-          + "; measured: " + c->sweep_tuning;
+          + (c->sweep_wpc ? "/wpc" : "") + "; measured: " + c->sweep_tuning;
     return out.c_str();
 }
 

@@ -84,7 +84,13 @@ struct DevBlock {
     float* fbase;         // FP32 copies of the slots read by the FP32 kernels (mixed mode only)
 };
 
+constexpr int CELL_TILE = 256;   // interior cells per cell tile (and threads per CTA of the cell kernels)
 constexpr int SWEEP_LANES = 8;   // threads per cell in the LU-SGS sweeps (one per DeltaQ component)
+constexpr int SWEEP_WPC = 16;    // `lanes` bit of the sweep kernels: warp-per-component thread mapping
+// threads a sweep launch needs for n positions
+__host__ __device__ inline int sweep_items(int n, int lanes) {
+    return (lanes & SWEEP_WPC) ? ((n + 31) / 32) * (32 * SWEEP_LANES) : n * SWEEP_LANES;
+}
 
 struct MirrorList {       // slot ranges [first, first+count) copied FP64 -> FP32 (or back if to_fp64)
     int n, to_fp64, first[6], count[6];

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 
 #include "engine.h"
@@ -136,10 +137,13 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     // TRANS_PDL=0 launches the hyperplanes without programmatic dependent launch
     const char* pd = std::getenv("TRANS_PDL");
     if (pd && std::string(pd) == "0") c->pdl = c->pdl_allowed = 0;
-    // sweep schedule: TRANS_SWEEP=planes | coop | flow forces one (for tests); default: tuned
+    // TRANS_SWEEP_MAP=wpc forces the warp-per-component thread mapping of the sweeps (for tests)
+    const char* wm = std::getenv("TRANS_SWEEP_MAP");
+    if (wm && std::string(wm) == "wpc") c->sweep_wpc = SWEEP_WPC;
+    // sweep schedule: TRANS_SWEEP=planes | coop | flow | tiles forces one (for tests); default: tuned
     const char* m = std::getenv("TRANS_SWEEP");
     std::string ms = m ? m : "";
-    if (ms == "planes" || ms == "coop" || ms == "flow") {
+    if (ms == "planes" || ms == "coop" || ms == "flow" || ms == "tiles") {
         int dev = 0, nsm = 0;
         CK(cudaGetDevice(&dev));
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -147,6 +151,14 @@ int ctx_init(Ctx* c, int precision, long long budget) {
         if (ms == "planes") c->sweep_mode = 0;
         if (ms == "coop") { c->sweep_mode = 1; c->sweep_block = 256; c->sweep_grid = nsm * std::max(1, std::min(2, c->fl->sweep_all_occupancy(256))); }
         if (ms == "flow") { c->sweep_mode = 2; c->sweep_block = 256; c->sweep_grid = nsm * std::max(1, std::min(4, c->fl->sweep_flow_occupancy(256))); }
+        if (ms == "tiles") {
+            c->sweep_mode = 3; c->sweep_block = 256; c->sweep_grid = nsm * std::max(1, c->fl->sweep_tiles_occupancy(256));
+            const char* ts = std::getenv("TRANS_TILE");
+            int a = 0, b = 0, d = 0;
+            if (ts && std::sscanf(ts, "%dx%dx%d", &a, &b, &d) == 3 && a > 0 && b > 0 && d > 0) {
+                c->tile_default[0] = a; c->tile_default[1] = b; c->tile_default[2] = d;
+            }
+        }
     }
     return TRANS_OK;
 }
@@ -157,6 +169,9 @@ void free_worklists(Ctx* c) {
     dfree(c->d_bc); dfree(c->d_outlet); dfree(c->d_lines); dfree(c->d_sweep); dfree(c->d_plane_off);
     dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq_save); dfree(c->d_parts);
     dfree(c->d_cdev); dfree(c->d_stage); dfree(c->d_tile_first); dfree(c->d_norms);
+    dfree(c->d_tiles); dfree(c->d_tflags); dfree(c->d_qpos);
+    c->tv = TileView{};
+    c->tile_shape[0] = c->tile_shape[1] = c->tile_shape[2] = 0;
     if (c->h_norms) { cudaFreeHost(c->h_norms); c->h_norms = nullptr; }
     if (c->iter_exec) { cudaGraphExecDestroy(c->iter_exec); c->iter_exec = nullptr; }
     c->iter_n = 0;

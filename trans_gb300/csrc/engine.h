@@ -79,6 +79,7 @@ struct Ctx {
     int* d_plane_off = nullptr;
     SweepView sv{};
     int* d_nbp = nullptr;
+    int* d_qpos = nullptr;               // sweep position of every cell-tile slot (-1: past the tile's end)
     int* d_flags = nullptr;
     void* d_rec = nullptr;
     void* d_dqs = nullptr;
@@ -103,12 +104,20 @@ struct Ctx {
     // ---- sweep schedule ----
     cudaGraphExec_t sweep_exec = nullptr;
     // 0 = one launch per hyperplane (graph), 1 = one cooperative launch with grid barriers,
-    // 2 = dataflow over ready flags; -1 = pick the fastest on first use (all bit-identical)
+    // 2 = dataflow over ready flags, 3 = tiled wavefront; -1 = pick the fastest on first use
+    // (all bit-identical)
     int sweep_mode = -1, sweep_grid = 0, sweep_block = 0;
+    int tile_shape[3] = {0, 0, 0};       // tiles of the tiled wavefront (built for this shape)
+    int tile_default[3] = {8, 8, 8};     // shape when the schedule is forced (TRANS_TILE=AxBxC)
+    int* d_tiles = nullptr;              // plane0 | pitem | item | dep arrays of the TileView
+    int* d_tflags = nullptr;             // 2 x ntiles publish flags + the tile counter
+    TileView tv{};
     bool sweep_forced = false;
     int pdl = 1;                         // chain hyperplane launches (programmatic dependent launch)
     int pdl_allowed = 1;                 // chaining may be picked by the tuner (TRANS_PDL=0 forbids it)
     int sweep_exec_pdl = -1;             // chaining the sweep graph was captured with
+    int sweep_wpc = 0;                   // SWEEP_WPC: warp-per-component thread mapping (0: lane-major)
+    int sweep_exec_wpc = -1;             // mapping the sweep graph was captured with
     int sweep_lanes = 1;                 // DeltaQ components swept: 1 = all, 2 = k and omega only (Runge-Kutta)
     SweepSync* d_sync = nullptr;
     SweepSync* h_sync = nullptr;         // pinned
@@ -147,6 +156,7 @@ int case_add(Ctx* c, const trans_params* p, int nblocks, const trans_block* bloc
 int case_remove(Ctx* c, int id);
 CaseRec* case_find(Ctx* c, int id);
 int rebuild(Ctx* c);
+int build_tiles(Ctx* c, int TI, int TJ, int TK);   // tiles of the tiled-wavefront sweep schedule
 void free_worklists(Ctx* c);
 int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload);
 int run_stage(Ctx* c, int stage, int itr);

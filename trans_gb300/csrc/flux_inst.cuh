@@ -24,14 +24,11 @@ void ga(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev*
 void fc(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
     if (nt > 0) k_sst_fc1<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, cd);
 }
-void prep(cudaStream_t s, const DevBlock* b, const SweepView& v, const CaseDev* cd) {
-    if (v.n > 0)
-        k_lusgs_prep<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(
-            b, v.cells, v.nbp, (TG_R*)v.rec, (TG_R*)v.dq, v.n, cd);
+void prep(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const int* qpos, const SweepView& v, const CaseDev* cd) {
+    if (nt > 0) k_lusgs_prep<TG_R><<<nt, CELL_TILE, 0, s>>>(b, tiles, qpos, (TG_R*)v.rec, (TG_R*)v.dq, cd);
 }
-void jac(cudaStream_t s, const DevBlock* b, const SweepView& v) {
-    if (v.n > 0)
-        k_lusgs_jac<TG_R><<<(unsigned)((v.n + 31) / 32), 6 * 32, 0, s>>>(b, v.cells, v.nbp, (TG_R*)v.rec, v.n);
+void jac(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const int* qpos, const int* tile_first, const SweepView& v) {
+    if (nt > 0) k_lusgs_jac<TG_R><<<nt, CELL_TILE, 0, s>>>(b, tiles, qpos, tile_first, (TG_R*)v.rec);
 }
 // one hyperplane; chained = launched with programmatic stream serialisation, so that this
 // hyperplane's independent loads overlap the previous one (the kernel waits before its
@@ -44,7 +41,7 @@ void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int
     TG_R* dq = (TG_R*)v.dq;
     long long n = v.n;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((count * SWEEP_LANES + SWEEP_CTA - 1) / SWEEP_CTA);
+    cfg.gridDim = dim3((sweep_items(count, turb) + SWEEP_CTA - 1) / SWEEP_CTA);
     cfg.blockDim = dim3(SWEEP_CTA);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -86,6 +83,25 @@ int swf_occ(int block) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_flow<TG_R>, block, 0) != cudaSuccess) return 0;
     return n;
 }
+cudaError_t swt(cudaStream_t s, const SweepView& v, const TileView& tv, int lanes, int* flags, int* counter, SweepSync* sy,
+                int grid, int block) {
+    if (v.n <= 0 || tv.ntiles <= 0) return cudaSuccess;
+    // cooperative: the CTAs wait on one another, so the whole grid must be resident
+    unsigned limit = SWEEP_SPIN_LIMIT;
+    const int* nbp = v.nbp;
+    const TG_R* rec = (const TG_R*)v.rec;
+    TG_R* dq = (TG_R*)v.dq;
+    long long n = v.n;
+    TileView t = tv;
+    void* args[] = {(void*)&nbp, (void*)&rec, (void*)&dq, (void*)&n, (void*)&t, (void*)&lanes, (void*)&flags, (void*)&counter,
+                    (void*)&sy, (void*)&limit};
+    return cudaLaunchCooperativeKernel((const void*)k_sweep_tiles<TG_R>, dim3(grid), dim3(block), args, 0, s);
+}
+int swt_occ(int block) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tiles<TG_R>, block, 0) != cudaSuccess) return 0;
+    return n;
+}
 void scat(cudaStream_t s, const DevBlock* b, const SweepView& v, int l0) {
     if (v.n > 0)
         k_sweep_scatter<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(b, v.cells, (const TG_R*)v.dq, v.n,
@@ -94,7 +110,8 @@ void scat(cudaStream_t s, const DevBlock* b, const SweepView& v, int l0) {
 }  // namespace
 
 const FluxLaunchers& TG_NAME() {
-    static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, prep, jac, swl, swu, swa, swa_occ, swf, swf_occ, scat, sizeof(TG_R)};
+    static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, prep, jac, swl, swu, swa, swa_occ, swf, swf_occ,
+                                    swt, swt_occ, scat, sizeof(TG_R)};
     return L;
 }
 }  // namespace tg

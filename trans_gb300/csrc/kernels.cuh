@@ -752,21 +752,22 @@ __global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restr
 
 // ---------------------------------------------------------------------------------------
 // Time/TIME_LUSGS.F90:60-108 and Time/TURBTWO_TIME_LUSGS_SST.F90:118-411: right-hand sides,
-// SST sources and the two diagonals, one thread per sweep position; the results go to the
-// sweep-order arrays together with the neighbours' Jacobian terms and spectral radii.
+// SST sources and the two diagonals, one thread per interior cell in cell order (coalesced
+// reads of the cell's slots); the results go to the cell's sweep position q (qpos) together
+// with the neighbours' Jacobian terms and spectral radii (k_lusgs_jac).
 // ---------------------------------------------------------------------------------------
 template <typename R>
-__global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, const int* __restrict__ nbp,
-                             R* __restrict__ rec, R* __restrict__ dq, long long N, const CaseDev* __restrict__ cdev) {
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= N) return;
-    const SweepCell sc = cells[q];
-    const DevBlock b = blks[sc.blk];
+__global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
+                             R* __restrict__ rec, R* __restrict__ dq, const CaseDev* __restrict__ cdev) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
     const Params pd = cdev[b.cs].p;
     const ParamsT<R> p = cparams<R>(cdev[b.cs]);
     const int turb = cdev[b.cs].turb;
-    const int I = sc.i, J = sc.j, K = sc.k;
-    const int nlex = (I - 1) + b.NI1 * ((J - 1) + b.NJ1 * (K - 1));     // lexicographic interior index
+    const int nlex = t.start + threadIdx.x;                              // lexicographic interior index
+    const int I = nlex % b.NI1 + 1, J = (nlex / b.NI1) % b.NJ1 + 1, K = nlex / (b.NI1 * b.NJ1) + 1;
+    const long long q = qpos[(size_t)blockIdx.x * CELL_TILE + threadIdx.x];
     const int c = cidx(b, I, J, K);
     auto REC = [&](int m) -> R& { return rec[sw_at(q, m, NREC)]; };
     auto DQ = [&](int L) -> R& { return dq[sw_at(q, L, DQ_STRIDE)]; };
@@ -883,38 +884,46 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const SweepCell*
     REC(REC_FT) = R(fm) + (CnegTk + CnegTO) * R(stept);
 }
 
-// The neighbours' Jacobian terms and spectral radii of the sweep records: 6 threads per
-// position (one per neighbour) compute into shared memory, then the block writes its 32
-// consecutive records as one contiguous, coalesced range (the diagonal entries excepted,
-// which k_lusgs_prep writes).  A missing neighbour (nbp < 0) leaves its entries unused.
+// The Jacobian terms and spectral radii of the sweep records, one thread per interior cell in
+// cell order: the terms of a cell in direction d depend on that cell alone, and the cell is
+// the lower neighbour (record entry d) of the cell at +1 and the upper neighbour (entry 3+d)
+// of the cell at -1 in that direction, so each is computed once and written to both records.
+// An absent neighbour's entries are never written; the sweeps do not use them.
 template <typename R>
-__global__ void __launch_bounds__(6 * 32) k_lusgs_jac(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells,
-                                                      const int* __restrict__ nbp, R* __restrict__ rec, long long N) {
-    __shared__ R stage[32][6 * NBREC];
-    const long long q0 = (long long)blockIdx.x * 32;
-    const int t = threadIdx.x, r = t / 6, k = t % 6;
-    const long long q = q0 + r;
-    if (q < N && nbp[sw_at(q, k, 6)] >= 0) {
-        const SweepCell sc = cells[q];
-        const DevBlock b = blks[sc.blk];
-        const int c = cidx(b, sc.i, sc.j, sc.k);
-        const size_t nc = (size_t)b.ncell;
-        const int d = k % 3;
-        const int st = d == 0 ? 1 : (d == 1 ? b.PI : b.PI * b.PJ);
-        const int nb = k < 3 ? c - st : c + st;
-        const R* sv = rs<R>(b, S_SVEL);
+__global__ void k_lusgs_jac(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
+                            const int* __restrict__ tile_first, R* __restrict__ rec) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const int bi = t.blk;
+    const DevBlock b = blks[bi];
+    const int n = t.start + threadIdx.x;
+    const int ijk[3] = {n % b.NI1 + 1, (n / b.NI1) % b.NJ1 + 1, n / (b.NI1 * b.NJ1) + 1};
+    const int hi[3] = {b.NI1, b.NJ1, b.NK1};
+    const int lstride[3] = {1, b.NI1, b.NI1 * b.NJ1};
+    const int c = cidx(b, ijk[0], ijk[1], ijk[2]);
+    const size_t nc = (size_t)b.ncell;
+    const R* sv = rs<R>(b, S_SVEL);
+    const R pp = rs<R>(b, S_PP)[c], rinv = rs<R>(b, S_RINV)[c];
+    const R u = sv[c], v = sv[c + nc], w = sv[c + 2 * nc];
+    const int tf = tile_first[bi];
+    auto pos_of = [&](int m) { return (long long)qpos[((size_t)tf + m / CELL_TILE) * CELL_TILE + m % CELL_TILE]; };
+    for (int d = 0; d < 3; ++d) {
+        const bool up = ijk[d] < hi[d], dn = ijk[d] > 1;
+        if (!up && !dn) continue;
         const R* asd = rs<R>(b, S_ASD + 3 * d);
         R Jt[NJAC];
-        jac_terms<R>(sv[nb], sv[nb + nc], sv[nb + 2 * nc], asd[nb], asd[nb + nc], asd[nb + 2 * nc], rs<R>(b, S_PP)[nb],
-                     rs<R>(b, S_RINV)[nb], Jt);
-        for (int m = 0; m < NJAC; ++m) stage[r][NBREC * k + m] = Jt[m];
-        stage[r][NBREC * k + NJAC] = rs<R>(b, S_RDS + d)[nb];
-    }
-    __syncthreads();
-    const long long nq = N - q0 < 32 ? N - q0 : 32;
-    for (int e = t; e < nq * NREC; e += blockDim.x) {
-        const int rr = e / NREC, m = e % NREC;
-        if (m < 6 * NBREC) rec[sw_at(q0 + rr, m, NREC)] = stage[rr][m];
+        jac_terms<R>(u, v, w, asd[c], asd[c + nc], asd[c + 2 * nc], pp, rinv, Jt);
+        const R rds = rs<R>(b, S_RDS + d)[c];
+        if (up) {           // lower neighbour of the cell at +1
+            R* r = rec + sw_at(pos_of(n + lstride[d]), NBREC * d, NREC);
+            for (int m = 0; m < NJAC; ++m) r[m] = Jt[m];
+            r[NJAC] = rds;
+        }
+        if (dn) {           // upper neighbour of the cell at -1
+            R* r = rec + sw_at(pos_of(n - lstride[d]), NBREC * (3 + d), NREC);
+            for (int m = 0; m < NJAC; ++m) r[m] = Jt[m];
+            r[NJAC] = rds;
+        }
     }
 }
 
@@ -930,6 +939,18 @@ __global__ void __launch_bounds__(6 * 32) k_lusgs_jac(const DevBlock* __restrict
 // turb selects the components swept: 0 mean flow, 1 all, 2 k and omega only (the Runge-Kutta
 // path, whose mean flow is explicit).
 // ---------------------------------------------------------------------------------------
+// The sweep kernels' `lanes` argument: bits 0-1 select the components swept (0 mean flow,
+// 1 all, 2 k and omega only), bit SWEEP_WPC the thread mapping.  Lane-major (bit clear): the
+// 8 threads of a position are adjacent lanes of one warp (component = lane % 8).  Warp per
+// component (bit set): a warp holds one component of 32 consecutive positions, so its lanes
+// take one code path -- on GB300 a warp's FP64 instruction occupies the FP64 unit of its
+// sub-partition for ~64 cycles whatever its active lanes, and the lane-major warp's four
+// divergent component paths issue ~5x the FP64 instructions per position.
+__device__ inline void sweep_map(int g, int lanes, int& e, int& L) {
+    if (lanes & SWEEP_WPC) { e = (g / (32 * SWEEP_LANES)) * 32 + (g & 31); L = (g >> 5) % SWEEP_LANES; }
+    else { e = g / SWEEP_LANES; L = g % SWEEP_LANES; }
+}
+
 template <typename R, bool LOWER>
 __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
                                   int L, int turb, bool chained = false) {
@@ -1007,15 +1028,16 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
 // one hyperplane [first, first+count) per launch (chained: launched with programmatic
 // stream serialisation, see sweep_item)
 template <typename R, bool LOWER>
-__global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int first, int count, int turb,
+__global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int first, int count, int lanes,
                         int chained) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const int e = g / SWEEP_LANES, L = g % SWEEP_LANES;
+    int e, L;
+    sweep_map(g, lanes, e, L);
     if (e >= count) {
         if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
         return;
     }
-    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, turb, chained != 0);
+    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, chained != 0);
 }
 
 // Grid-wide barrier of a co-resident (cooperative) grid.  The wait is bounded: after `limit`
@@ -1048,19 +1070,25 @@ __device__ inline bool grid_barrier(SweepSync* sy, unsigned nblocks, unsigned li
 // spread over the whole grid, then a grid barrier; U runs the hyperplanes in reverse.
 template <typename R>
 __global__ void k_sweep_all(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N,
-                            const int* __restrict__ plane_off, int nplanes, int turb, SweepSync* sy, unsigned limit) {
+                            const int* __restrict__ plane_off, int nplanes, int lanes, SweepSync* sy, unsigned limit) {
     const int stride = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     for (int h = 0; h < nplanes; ++h) {
-        const int first = plane_off[h], items = (plane_off[h + 1] - first) * SWEEP_LANES;
-        for (int g = tid; g < items; g += stride)
-            sweep_item<R, true>(nbp, rec, dq, N, (long long)first + g / SWEEP_LANES, g % SWEEP_LANES, turb);
+        const int first = plane_off[h], n = plane_off[h + 1] - first, items = sweep_items(n, lanes);
+        for (int g = tid; g < items; g += stride) {
+            int e, L;
+            sweep_map(g, lanes, e, L);
+            if (e < n) sweep_item<R, true>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3);
+        }
         if (!grid_barrier(sy, gridDim.x, limit)) return;
     }
     for (int h = nplanes - 1; h >= 0; --h) {
-        const int first = plane_off[h], items = (plane_off[h + 1] - first) * SWEEP_LANES;
-        for (int g = tid; g < items; g += stride)
-            sweep_item<R, false>(nbp, rec, dq, N, (long long)first + g / SWEEP_LANES, g % SWEEP_LANES, turb);
+        const int first = plane_off[h], n = plane_off[h + 1] - first, items = sweep_items(n, lanes);
+        for (int g = tid; g < items; g += stride) {
+            int e, L;
+            sweep_map(g, lanes, e, L);
+            if (e < n) sweep_item<R, false>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3);
+        }
         if (h > 0 && !grid_barrier(sy, gridDim.x, limit)) return;
     }
 }
@@ -1101,7 +1129,7 @@ __global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ 
             if (np >= 0) ok = flow_wait<R>(flagL, np, 7, sy, limit);
         }
         if (!ok) return;
-        sweep_item<R, true>(nbp, rec, dq, N, q, L, turb);
+        sweep_item<R, true>(nbp, rec, dq, N, q, L, turb & 3);
         __threadfence();
         atomicAdd(flagL + q, 1);
     }
@@ -1115,9 +1143,71 @@ __global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ 
             if (np >= 0) ok = flow_wait<R>(flagU, np, 7, sy, limit);
         }
         if (!ok) return;
-        sweep_item<R, false>(nbp, rec, dq, N, q, L, turb);
+        sweep_item<R, false>(nbp, rec, dq, N, q, L, turb & 3);
         __threadfence();
         atomicAdd(flagU + q, 1);
+    }
+}
+
+// Both sweeps as a tiled wavefront (one cooperative launch): every CTA takes the next tile of
+// the topological order from a counter (L sweep tiles first, then the U sweep tiles in
+// reverse), waits until the tiles holding its lower (upper) neighbours have published, sweeps
+// the tile's own planes with a CTA barrier between them, and publishes the tile.  A CTA only
+// waits on tiles taken before its own by CTAs that are running, so the smallest unfinished
+// tile can always proceed.  Waits are bounded: on expiry the kernel records an error and
+// every CTA leaves at its next check.
+__device__ inline bool tile_wait(const int* flag, SweepSync* sy, unsigned limit) {
+    const volatile int* f = flag;
+    unsigned it = 0;
+    while (*f == 0) {
+        if ((++it & 255) == 0 && *((volatile int*)&sy->err)) return false;
+        if (it > limit) { atomicExch(&sy->err, 3); return false; }
+        __nanosleep(64);
+    }
+    __threadfence();
+    return true;
+}
+
+template <typename R>
+__global__ void k_sweep_tiles(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, TileView tv,
+                              int lanes, int* flags, int* counter, SweepSync* sy, unsigned limit) {
+    __shared__ int s_t, s_ok;
+    const int nt = tv.ntiles;
+    for (;;) {
+        if (threadIdx.x == 0) s_t = *((volatile int*)&sy->err) ? 2 * nt : atomicAdd(counter, 1);
+        __syncthreads();
+        const int t = s_t;
+        if (t >= 2 * nt) return;
+        const bool lower = t < nt;
+        const int T = lower ? t : 2 * nt - 1 - t;
+        if (threadIdx.x == 0) {
+            bool ok = true;
+            for (int d = 0; d < 3 && ok; ++d) {
+                const int dep = tv.dep[6 * T + (lower ? 0 : 3) + d];
+                if (dep >= 0) ok = tile_wait(flags + (lower ? 0 : nt) + dep, sy, limit);
+            }
+            if (ok && !lower) ok = tile_wait(flags + T, sy, limit);      // the tile's own L result
+            s_ok = ok ? 1 : 0;
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        const int p0 = tv.plane0[T], np = tv.plane0[T + 1] - p0;
+        for (int pp = 0; pp < np; ++pp) {
+            const int p = lower ? p0 + pp : p0 + np - 1 - pp;
+            const int a = tv.pitem[p], n = tv.pitem[p + 1] - a, items = sweep_items(n, lanes);
+            for (int g = threadIdx.x; g < items; g += blockDim.x) {
+                int e, L;
+                sweep_map(g, lanes, e, L);
+                if (e >= n) continue;
+                const long long q = tv.item[a + e];
+                if (lower) sweep_item<R, true>(nbp, rec, dq, N, q, L, lanes & 3);
+                else sweep_item<R, false>(nbp, rec, dq, N, q, L, lanes & 3);
+            }
+            __syncthreads();
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) atomicExch(flags + (lower ? 0 : nt) + T, 1);
     }
 }
 

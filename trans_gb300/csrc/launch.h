@@ -10,6 +10,7 @@ struct SweepCell;
 struct NormPart;
 struct SweepSync;
 struct SweepView;
+struct TileView;
 struct BlockNorms;
 
 // FP64 kernels shared by both precision modes
@@ -45,24 +46,30 @@ struct FluxLaunchers {
     void (*gather)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
     void (*sst_fc1)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
     // LU-SGS right-hand sides + neighbour Jacobian terms into the sweep-order arrays
-    void (*prep)(cudaStream_t, const DevBlock*, const SweepView&, const CaseDev*);
-    void (*jac)(cudaStream_t, const DevBlock*, const SweepView&);     // neighbours' Jacobian terms
-    void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int turb, int chained);
-    void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int turb, int chained);
+    // (cell order over the cell tiles; qpos = sweep position of each tile slot)
+    void (*prep)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const SweepView&, const CaseDev*);
+    void (*jac)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const int* tile_first,
+                const SweepView&);     // the cells' Jacobian terms into their neighbours' records
+    // lanes: components swept (bits 0-1: 0 mean flow, 1 all, 2 k-omega) | SWEEP_WPC thread mapping
+    void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained);
+    void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained);
     // both sweeps in one cooperative launch (grid must be co-resident: grid <= SMs x occupancy)
-    cudaError_t (*sweep_all)(cudaStream_t, const SweepView&, const int* plane_off, int nplanes, int turb, SweepSync*,
+    cudaError_t (*sweep_all)(cudaStream_t, const SweepView&, const int* plane_off, int nplanes, int lanes, SweepSync*,
                              int grid, int block);
     int (*sweep_all_occupancy)(int block);          // resident blocks per SM
     // both sweeps as a dataflow over per-position ready flags (one cooperative launch)
     cudaError_t (*sweep_flow)(cudaStream_t, const SweepView&, int* flagL, int* flagU, int turb, SweepSync*, int grid, int block);
     int (*sweep_flow_occupancy)(int block);
+    // both sweeps as a tiled wavefront (one cooperative launch, tiles taken from a counter)
+    cudaError_t (*sweep_tiles)(cudaStream_t, const SweepView&, const TileView&, int lanes, int* flags, int* counter, SweepSync*,
+                               int grid, int block);
+    int (*sweep_tiles_occupancy)(int block);
     void (*scatter)(cudaStream_t, const DevBlock*, const SweepView&, int l0);   // DeltaQ l0..6 back to cell order
     size_t elem;                                    // bytes of the sweep arithmetic type
 };
 const FluxLaunchers& flux_launchers_f64();
 const FluxLaunchers& flux_launchers_f32();
 
-constexpr int CELL_TILE = 256;
 constexpr int FACE_TILE = 128;
 constexpr int SWEEP_CTA = 128;
 constexpr unsigned SWEEP_SPIN_LIMIT = 1u << 22;     // polls of one wait before it gives up (~1 s)

@@ -206,12 +206,27 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
 namespace {
 
 int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
-    if (mode == 0 && c->sweep_exec && c->sweep_exec_pdl != c->pdl) {       // chaining changed
+    const int lanes = c->sweep_lanes | c->sweep_wpc;
+    if (mode == 0 && c->sweep_exec && (c->sweep_exec_pdl != c->pdl || c->sweep_exec_wpc != c->sweep_wpc)) {   // changed
         cudaGraphExecDestroy(c->sweep_exec);
         c->sweep_exec = nullptr;
     }
     cudaStream_t s = c->stream;
     const int nh = (int)c->plane_off.size() - 1;
+    if (mode == 3) {
+        if (!c->d_tiles) {
+            if (capture) return fail(c, TRANS_E_CUDA, "tiled sweep captured before its tiles were built");
+            int rc = build_tiles(c, c->tile_default[0], c->tile_default[1], c->tile_default[2]);
+            if (rc) return rc;
+        }
+        const int nt = c->tv.ntiles;
+        CK(cudaMemsetAsync(c->d_tflags, 0, sizeof(int) * ((size_t)2 * nt + 1), s));
+        CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
+        CK(c->fl->sweep_tiles(s, c->sv, c->tv, lanes, c->d_tflags, c->d_tflags + 2 * nt, c->d_sync, grid, block));
+        CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
+        c->launches++;
+        return TRANS_OK;
+    }
     if (mode == 2) {
         const size_t np = (size_t)((c->sv.n + 31) / 32 * 32);
         CK(cudaMemsetAsync(c->d_flags, 0, 2 * np * sizeof(int), s));
@@ -223,7 +238,7 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     }
     if (mode == 1) {
         CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
-        CK(c->fl->sweep_all(s, c->sv, c->d_plane_off, nh, c->sweep_lanes, c->d_sync, grid, block));
+        CK(c->fl->sweep_all(s, c->sv, c->d_plane_off, nh, lanes, c->d_sync, grid, block));
         CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
         c->launches++;
         return TRANS_OK;
@@ -233,11 +248,11 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     if (capture) {
         for (int h = 0; h < nh; ++h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, c->sweep_lanes, c->pdl);
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, lanes, c->pdl);
         }
         for (int h = nh - 1; h >= 0; --h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, c->sweep_lanes, c->pdl);
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, lanes, c->pdl);
         }
         return TRANS_OK;
     }
@@ -246,11 +261,11 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         for (int h = 0; h < nh; ++h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, c->sweep_lanes, c->pdl);
+            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, lanes, c->pdl);
         }
         for (int h = nh - 1; h >= 0; --h) {
             int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, c->sweep_lanes, c->pdl);
+            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, lanes, c->pdl);
         }
         cudaError_t e = cudaStreamEndCapture(s, &g);
         if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph capture: ") + cudaGetErrorString(e));
@@ -258,6 +273,7 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph instantiate: ") + cudaGetErrorString(e));
         c->sweep_exec_pdl = c->pdl;
+        c->sweep_exec_wpc = c->sweep_wpc;
     }
     CK(cudaGraphLaunch(c->sweep_exec, s));
     for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
@@ -279,15 +295,25 @@ int tune_sweeps(Ctx* c) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    struct Cand { int mode, grid, block, pdl; };
-    std::vector<Cand> cands = {{0, 0, 0, 1}, {0, 0, 0, 0}};
-    for (int block : {128, 256, 512}) {
-        int occ = c->fl->sweep_all_occupancy(block);
-        for (int per : {1, 2, 4})
-            if (per <= occ) cands.push_back({1, per * nsm, block, 0});
-        int occf = c->fl->sweep_flow_occupancy(block);
-        if (block == 256 && occf >= 4) cands.push_back({2, 4 * nsm, block, 0});
+    struct Cand { int mode, grid, block, pdl, ti, tj, tk, wpc; };
+    std::vector<Cand> cands;
+    for (int wpc : {0, SWEEP_WPC}) {
+        cands.push_back({0, 0, 0, 1, 0, 0, 0, wpc});
+        cands.push_back({0, 0, 0, 0, 0, 0, 0, wpc});
+        for (int block : {128, 256, 512}) {
+            int occ = c->fl->sweep_all_occupancy(block);
+            for (int per : {1, 2, 4})
+                if (per <= occ) cands.push_back({1, per * nsm, block, 0, 0, 0, 0, wpc});
+        }
+        // tiled wavefront: tile shapes x CTA sizes, one resident wave of CTAs
+        const int shapes[][3] = {{8, 8, 8}, {16, 4, 4}, {8, 4, 4}, {16, 8, 4}, {4, 4, 4}, {32, 4, 2}};
+        for (const auto& sh : shapes)
+            for (int block : {128, 256, 512}) {
+                const int occ = c->fl->sweep_tiles_occupancy(block);
+                if (occ >= 1) cands.push_back({3, occ * nsm, block, 0, sh[0], sh[1], sh[2], wpc});
+            }
     }
+    if (c->fl->sweep_flow_occupancy(256) >= 4) cands.push_back({2, 4 * nsm, 256, 0, 0, 0, 0, 0});
     const int pdl0 = c->pdl_allowed;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -298,6 +324,8 @@ int tune_sweeps(Ctx* c) {
     int rc = save_dq(c, false);
     for (const Cand& k : cands) {
         if (k.mode == 0) c->pdl = pdl0 ? k.pdl : 0;
+        c->sweep_wpc = k.wpc;
+        if (k.mode == 3 && (rc = build_tiles(c, k.ti, k.tj, k.tk))) break;
         for (int rep = 0; rep < 2 && rc == TRANS_OK; ++rep) {      // first run warms up (graph build)
             if ((rc = save_dq(c, true))) break;
             CK(cudaEventRecord(e0, c->stream));
@@ -308,9 +336,12 @@ int tune_sweeps(Ctx* c) {
             float ms = 0;
             CK(cudaEventElapsedTime(&ms, e0, e1));
             if (rep == 1) {
-                c->sweep_tuning += (k.mode ? std::string(k.mode == 1 ? "coop " : "flow ") + std::to_string(k.grid) + "x"
-                                                 + std::to_string(k.block)
+                c->sweep_tuning += (k.mode ? std::string(k.mode == 1 ? "coop " : k.mode == 2 ? "flow " : "tiles ")
+                                                 + (k.mode == 3 ? std::to_string(k.ti) + "x" + std::to_string(k.tj) + "x"
+                                                                      + std::to_string(k.tk) + "/" : std::string())
+                                                 + std::to_string(k.grid) + "x" + std::to_string(k.block)
                                            : std::string(c->pdl ? "planes-chained" : "planes"))
+                                   + (k.wpc ? "/wpc" : "")
                                    + ":" + std::to_string(ms) + "ms ";
                 if (ms < best) { best = ms; pick = k; }
             }
@@ -322,7 +353,9 @@ int tune_sweeps(Ctx* c) {
     cudaEventDestroy(e1);
     if (rc) return rc;
     if ((rc = save_dq(c, true))) return rc;
+    if (pick.mode == 3 && (rc = build_tiles(c, pick.ti, pick.tj, pick.tk))) return rc;
     c->sweep_mode = pick.mode; c->sweep_grid = pick.grid; c->sweep_block = pick.block;
+    c->sweep_wpc = pick.wpc;
     c->pdl = pick.mode == 0 ? (pdl0 ? pick.pdl : 0) : 0;
     return TRANS_OK;
 }
@@ -407,7 +440,11 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
                 c->fl->sst_fc1(s, c->d_blk, c->d_cell, nct, c->d_cdev);
                 c->launches++;
             }
-            { KScope t(c, K_PREP); c->fl->prep(s, c->d_blk, c->sv, c->d_cdev); c->fl->jac(s, c->d_blk, c->sv); }
+            {
+                KScope t(c, K_PREP);
+                c->fl->prep(s, c->d_blk, c->d_cell, nct, c->d_qpos, c->sv, c->d_cdev);
+                c->fl->jac(s, c->d_blk, c->d_cell, nct, c->d_qpos, c->d_tile_first, c->sv);
+            }
             c->launches += 2;
             {
                 int nh = (int)c->plane_off.size() - 1, nl = 0;
@@ -494,6 +531,10 @@ bool switches_fixed(Ctx* c, int n) {
 
 int capture_iterations(Ctx* c, int n) {
     if (c->iter_exec) { cudaGraphExecDestroy(c->iter_exec); c->iter_exec = nullptr; c->iter_n = 0; }
+    if (c->sweep_mode == 3 && !c->d_tiles) {          // allocations cannot happen inside the capture
+        int rc = build_tiles(c, c->tile_default[0], c->tile_default[1], c->tile_default[2]);
+        if (rc) return rc;
+    }
     const CaseRec* c0 = c->cases[0];
     const int nsub = sub_iterations(c0->p);
     const int nblk = (int)c->blk.size();

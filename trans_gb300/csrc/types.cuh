@@ -29,6 +29,20 @@ struct SweepView {
     long long n;
 };
 
+// Tiled wavefront of the sweeps: the interior of every block cut into tiles of TIxTJxTK
+// cells.  Tiles are numbered in a topological order of their (ti-1, tj-1, tk-1) dependencies
+// (tile hyperplanes ti+tj+tk ascending); the cells of a tile are listed by the tile's own
+// i+j+k planes.  Tile t owns planes plane0[t] .. plane0[t+1]-1; plane p lists the sweep
+// positions item[pitem[p] .. pitem[p+1]-1]; dep[6t .. 6t+5] are the tiles holding the lower
+// (0..2) and upper (3..5) neighbours, -1 = none.
+struct TileView {
+    int ntiles;
+    const int* plane0;
+    const int* pitem;
+    const int* item;
+    const int* dep;
+};
+
 struct NormPart {         // per-tile partial residual norms (Time/TIME_Update_V.F90:106-294)
     double sa, ma, sk, mk, so, mo;
     long long ia;                   // lexicographic index of the max of |D1/V1|

@@ -242,6 +242,13 @@ int rebuild(Ctx* c) {
                 }
         }
         if ((rc = upload_vec(c, nbp.data(), sizeof(int) * nbp.size(), (void**)&c->d_nbp))) return rc;
+        // sweep position of every slot of every cell tile (tiles hold consecutive interior cells)
+        std::vector<int> qpos(c->cell_tiles.size() * (size_t)CELL_TILE, -1);
+        for (size_t t = 0; t < c->cell_tiles.size(); ++t) {
+            const Tile& tl = c->cell_tiles[t];
+            for (int r = 0; r < tl.count; ++r) qpos[t * CELL_TILE + r] = pos[tl.blk][(size_t)tl.start + r];
+        }
+        if ((rc = upload_vec(c, qpos.data(), sizeof(int) * qpos.size(), (void**)&c->d_qpos))) return rc;
         CK(cudaMalloc(&c->d_rec, (size_t)NREC * Np * c->fl->elem));
         CK(cudaMalloc(&c->d_dqs, (size_t)DQ_STRIDE * Np * c->fl->elem));
         CK(cudaMalloc(&c->d_flags, (size_t)2 * Np * sizeof(int)));
@@ -268,6 +275,94 @@ int rebuild(Ctx* c) {
     CK(cudaMallocHost(&c->h_cdev, sizeof(CaseDev) * c->cases.size()));
     if (!c->sweep_forced) c->sweep_mode = -1;     // re-tune the sweep schedule for the new work
     c->built = true;
+    return TRANS_OK;
+}
+
+// Tiles of TIxTJxTK cells for the tiled-wavefront sweep schedule (TileView, types.cuh):
+// numbered by tile hyperplane ti+tj+tk (then block, tk, tj, ti), cells of a tile listed by
+// the tile's own i+j+k planes.
+int build_tiles(Ctx* c, int TI, int TJ, int TK) {
+    if (c->tile_shape[0] == TI && c->tile_shape[1] == TJ && c->tile_shape[2] == TK && c->d_tiles) return TRANS_OK;
+    if (c->d_tiles) { cudaFree(c->d_tiles); c->d_tiles = nullptr; }
+    if (c->d_tflags) { cudaFree(c->d_tflags); c->d_tflags = nullptr; }
+    c->tv = TileView{};
+    c->tile_shape[0] = c->tile_shape[1] = c->tile_shape[2] = 0;
+    const int nblk = (int)c->blk.size();
+    std::vector<std::vector<int>> pos(nblk);
+    for (int n = 0; n < nblk; ++n) pos[n].assign((size_t)c->blk[n].nint, -1);
+    for (size_t q = 0; q < c->sweep.size(); ++q) {
+        const SweepCell& sc = c->sweep[q];
+        const DevBlock& b = c->blk[sc.blk];
+        pos[sc.blk][(size_t)(sc.i - 1) + (size_t)b.NI1 * ((sc.j - 1) + (size_t)b.NJ1 * (sc.k - 1))] = (int)q;
+    }
+    struct TileKey { int h, n, tk, tj, ti; };
+    std::vector<TileKey> keys;
+    std::vector<int> nti(nblk), ntj(nblk), ntk(nblk);
+    for (int n = 0; n < nblk; ++n) {
+        const DevBlock& b = c->blk[n];
+        nti[n] = (b.NI1 + TI - 1) / TI; ntj[n] = (b.NJ1 + TJ - 1) / TJ; ntk[n] = (b.NK1 + TK - 1) / TK;
+        for (int tk = 0; tk < ntk[n]; ++tk)
+            for (int tj = 0; tj < ntj[n]; ++tj)
+                for (int ti = 0; ti < nti[n]; ++ti) keys.push_back(TileKey{ti + tj + tk, n, tk, tj, ti});
+    }
+    std::stable_sort(keys.begin(), keys.end(), [](const TileKey& a, const TileKey& b) {
+        if (a.h != b.h) return a.h < b.h;
+        if (a.n != b.n) return a.n < b.n;
+        if (a.tk != b.tk) return a.tk < b.tk;
+        if (a.tj != b.tj) return a.tj < b.tj;
+        return a.ti < b.ti;
+    });
+    const int nt = (int)keys.size();
+    std::vector<std::vector<int>> tid(nblk);           // tile number of (block, ti, tj, tk)
+    for (int n = 0; n < nblk; ++n) tid[n].assign((size_t)nti[n] * ntj[n] * ntk[n], -1);
+    for (int t = 0; t < nt; ++t) {
+        const TileKey& k = keys[t];
+        tid[k.n][(size_t)k.ti + (size_t)nti[k.n] * ((size_t)k.tj + (size_t)ntj[k.n] * k.tk)] = t;
+    }
+    std::vector<int> plane0, pitem, item, dep((size_t)6 * nt, -1);
+    item.reserve(c->sweep.size());
+    for (int t = 0; t < nt; ++t) {
+        const TileKey& k = keys[t];
+        const DevBlock& b = c->blk[k.n];
+        const int i0 = k.ti * TI + 1, j0 = k.tj * TJ + 1, k0 = k.tk * TK + 1;
+        const int i1 = std::min(i0 + TI - 1, b.NI1), j1 = std::min(j0 + TJ - 1, b.NJ1), k1 = std::min(k0 + TK - 1, b.NK1);
+        plane0.push_back((int)pitem.size());
+        for (int h = 0; h <= (i1 - i0) + (j1 - j0) + (k1 - k0); ++h) {
+            pitem.push_back((int)item.size());
+            for (int kk = k0; kk <= k1; ++kk)
+                for (int jj = j0; jj <= j1; ++jj) {
+                    const int ii = i0 + h - (jj - j0) - (kk - k0);
+                    if (ii >= i0 && ii <= i1)
+                        item.push_back(pos[k.n][(size_t)(ii - 1) + (size_t)b.NI1 * ((jj - 1) + (size_t)b.NJ1 * (kk - 1))]);
+                }
+        }
+        const int tc[3] = {k.ti, k.tj, k.tk}, tn[3] = {nti[k.n], ntj[k.n], ntk[k.n]};
+        for (int side = 0; side < 2; ++side)
+            for (int d = 0; d < 3; ++d) {
+                int x[3] = {tc[0], tc[1], tc[2]};
+                x[d] += side == 0 ? -1 : 1;
+                if (x[d] < 0 || x[d] >= tn[d]) continue;
+                dep[(size_t)6 * t + 3 * side + d] = tid[k.n][(size_t)x[0] + (size_t)nti[k.n] * ((size_t)x[1] + (size_t)ntj[k.n] * x[2])];
+            }
+    }
+    plane0.push_back((int)pitem.size());
+    pitem.push_back((int)item.size());
+    if (item.size() != c->sweep.size()) return fail(c, TRANS_E_CUDA, "tile lists do not cover the sweep positions");
+    std::vector<int> all;                               // one device array: plane0 | pitem | item | dep
+    all.reserve(plane0.size() + pitem.size() + item.size() + dep.size());
+    all.insert(all.end(), plane0.begin(), plane0.end());
+    all.insert(all.end(), pitem.begin(), pitem.end());
+    all.insert(all.end(), item.begin(), item.end());
+    all.insert(all.end(), dep.begin(), dep.end());
+    int rc;
+    if ((rc = upload_vec(c, all.data(), sizeof(int) * all.size(), (void**)&c->d_tiles))) return rc;
+    CK(cudaMalloc(&c->d_tflags, sizeof(int) * ((size_t)2 * nt + 1)));
+    c->tv.ntiles = nt;
+    c->tv.plane0 = c->d_tiles;
+    c->tv.pitem = c->d_tiles + plane0.size();
+    c->tv.item = c->tv.pitem + pitem.size();
+    c->tv.dep = c->tv.item + item.size();
+    c->tile_shape[0] = TI; c->tile_shape[1] = TJ; c->tile_shape[2] = TK;
     return TRANS_OK;
 }
 
