@@ -27,8 +27,9 @@ void fc(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev*
 void prep(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const int* qpos, const SweepView& v, const CaseDev* cd) {
     if (nt > 0) k_lusgs_prep<TG_R><<<nt, CELL_TILE, 0, s>>>(b, tiles, qpos, (TG_R*)v.rec, (TG_R*)v.dq, cd);
 }
-void jac(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const int* qpos, const int* tile_first, const SweepView& v) {
-    if (nt > 0) k_lusgs_jac<TG_R><<<nt, CELL_TILE, 0, s>>>(b, tiles, qpos, tile_first, (TG_R*)v.rec);
+void jac(cudaStream_t s, const DevBlock* b, const SweepView& v) {
+    if (v.n > 0)
+        k_lusgs_jac<TG_R><<<(unsigned)((v.n + 31) / 32), 6 * 32, 0, s>>>(b, v.cells, v.nbp, (TG_R*)v.rec, v.n);
 }
 // one hyperplane; chained = launched with programmatic stream serialisation, so that this
 // hyperplane's independent loads overlap the previous one (the kernel waits before its

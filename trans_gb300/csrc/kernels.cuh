@@ -884,48 +884,41 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
     REC(REC_FT) = R(fm) + (CnegTk + CnegTO) * R(stept);
 }
 
-// The Jacobian terms and spectral radii of the sweep records, one thread per interior cell in
-// cell order: the terms of a cell in direction d depend on that cell alone, and the cell is
-// the lower neighbour (record entry d) of the cell at +1 and the upper neighbour (entry 3+d)
-// of the cell at -1 in that direction, so each is computed once and written to both records.
-// An absent neighbour's entries are never written; the sweeps do not use them.
+// The neighbours' Jacobian terms and spectral radii of the sweep records: 6 threads per
+// position (one per neighbour) compute into shared memory, then the block writes its 32
+// consecutive records as one contiguous, coalesced range (the diagonal entries excepted,
+// which k_lusgs_prep writes).  A missing neighbour (nbp < 0) leaves its entries unused.
 template <typename R>
-__global__ void k_lusgs_jac(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
-                            const int* __restrict__ tile_first, R* __restrict__ rec) {
-    const Tile t = tiles[blockIdx.x];
-    if ((int)threadIdx.x >= t.count) return;
-    const int bi = t.blk;
-    const DevBlock b = blks[bi];
-    const int n = t.start + threadIdx.x;
-    const int ijk[3] = {n % b.NI1 + 1, (n / b.NI1) % b.NJ1 + 1, n / (b.NI1 * b.NJ1) + 1};
-    const int hi[3] = {b.NI1, b.NJ1, b.NK1};
-    const int lstride[3] = {1, b.NI1, b.NI1 * b.NJ1};
-    const int c = cidx(b, ijk[0], ijk[1], ijk[2]);
-    const size_t nc = (size_t)b.ncell;
-    const R* sv = rs<R>(b, S_SVEL);
-    const R pp = rs<R>(b, S_PP)[c], rinv = rs<R>(b, S_RINV)[c];
-    const R u = sv[c], v = sv[c + nc], w = sv[c + 2 * nc];
-    const int tf = tile_first[bi];
-    auto pos_of = [&](int m) { return (long long)qpos[((size_t)tf + m / CELL_TILE) * CELL_TILE + m % CELL_TILE]; };
-    for (int d = 0; d < 3; ++d) {
-        const bool up = ijk[d] < hi[d], dn = ijk[d] > 1;
-        if (!up && !dn) continue;
+__global__ void __launch_bounds__(6 * 32) k_lusgs_jac(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells,
+                                                      const int* __restrict__ nbp, R* __restrict__ rec, long long N) {
+    __shared__ R stage[32][6 * NBREC];
+    const long long q0 = (long long)blockIdx.x * 32;
+    const int t = threadIdx.x, r = t / 6, k = t % 6;
+    const long long q = q0 + r;
+    if (q < N && nbp[sw_at(q, k, 6)] >= 0) {
+        const SweepCell sc = cells[q];
+        const DevBlock b = blks[sc.blk];
+        const int c = cidx(b, sc.i, sc.j, sc.k);
+        const size_t nc = (size_t)b.ncell;
+        const int d = k % 3;
+        const int st = d == 0 ? 1 : (d == 1 ? b.PI : b.PI * b.PJ);
+        const int nb = k < 3 ? c - st : c + st;
+        const R* sv = rs<R>(b, S_SVEL);
         const R* asd = rs<R>(b, S_ASD + 3 * d);
         R Jt[NJAC];
-        jac_terms<R>(u, v, w, asd[c], asd[c + nc], asd[c + 2 * nc], pp, rinv, Jt);
-        const R rds = rs<R>(b, S_RDS + d)[c];
-        if (up) {           // lower neighbour of the cell at +1
-            R* r = rec + sw_at(pos_of(n + lstride[d]), NBREC * d, NREC);
-            for (int m = 0; m < NJAC; ++m) r[m] = Jt[m];
-            r[NJAC] = rds;
-        }
-        if (dn) {           // upper neighbour of the cell at -1
-            R* r = rec + sw_at(pos_of(n - lstride[d]), NBREC * (3 + d), NREC);
-            for (int m = 0; m < NJAC; ++m) r[m] = Jt[m];
-            r[NJAC] = rds;
-        }
+        jac_terms<R>(sv[nb], sv[nb + nc], sv[nb + 2 * nc], asd[nb], asd[nb + nc], asd[nb + 2 * nc], rs<R>(b, S_PP)[nb],
+                     rs<R>(b, S_RINV)[nb], Jt);
+        for (int m = 0; m < NJAC; ++m) stage[r][NBREC * k + m] = Jt[m];
+        stage[r][NBREC * k + NJAC] = rs<R>(b, S_RDS + d)[nb];
+    }
+    __syncthreads();
+    const long long nq = N - q0 < 32 ? N - q0 : 32;
+    for (int e = t; e < nq * NREC; e += blockDim.x) {
+        const int rr = e / NREC, m = e % NREC;
+        if (m < 6 * NBREC) rec[sw_at(q0 + rr, m, NREC)] = stage[rr][m];
     }
 }
+
 
 // ---------------------------------------------------------------------------------------
 // LU-SGS sweeps (Time/TIME_LUSGS.F90:172-675, Time/TURBTWO_TIME_LUSGS_SST.F90:562-766) on the

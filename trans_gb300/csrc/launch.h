@@ -48,8 +48,7 @@ struct FluxLaunchers {
     // LU-SGS right-hand sides + neighbour Jacobian terms into the sweep-order arrays
     // (cell order over the cell tiles; qpos = sweep position of each tile slot)
     void (*prep)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const SweepView&, const CaseDev*);
-    void (*jac)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const int* tile_first,
-                const SweepView&);     // the cells' Jacobian terms into their neighbours' records
+    void (*jac)(cudaStream_t, const DevBlock*, const SweepView&);     // neighbours' Jacobian terms (sweep order)
     // lanes: components swept (bits 0-1: 0 mean flow, 1 all, 2 k-omega) | SWEEP_WPC thread mapping
     void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained);
     void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained);

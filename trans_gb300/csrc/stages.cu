@@ -306,9 +306,9 @@ int tune_sweeps(Ctx* c) {
                 if (per <= occ) cands.push_back({1, per * nsm, block, 0, 0, 0, 0, wpc});
         }
         // tiled wavefront: tile shapes x CTA sizes, one resident wave of CTAs
-        const int shapes[][3] = {{8, 8, 8}, {16, 4, 4}, {8, 4, 4}, {16, 8, 4}, {4, 4, 4}, {32, 4, 2}};
+        const int shapes[][3] = {{16, 4, 4}, {8, 4, 4}, {4, 4, 4}};
         for (const auto& sh : shapes)
-            for (int block : {128, 256, 512}) {
+            for (int block : {256, 512}) {
                 const int occ = c->fl->sweep_tiles_occupancy(block);
                 if (occ >= 1) cands.push_back({3, occ * nsm, block, 0, sh[0], sh[1], sh[2], wpc});
             }
@@ -443,7 +443,7 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             {
                 KScope t(c, K_PREP);
                 c->fl->prep(s, c->d_blk, c->d_cell, nct, c->d_qpos, c->sv, c->d_cdev);
-                c->fl->jac(s, c->d_blk, c->d_cell, nct, c->d_qpos, c->d_tile_first, c->sv);
+                c->fl->jac(s, c->d_blk, c->sv);
             }
             c->launches += 2;
             {
