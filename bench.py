@@ -400,7 +400,17 @@ def main():
         roof["traffic"] = FACE_DRAM_BYTES * nunit / dom_n
         roof["traffic_source"] = "ncu dram__bytes_read+write per face on the 339,968-cell cascade, scaled by faces"
     elif dom == "k_sweep":
+        # the sweeps are bound by one dependent step per i+j+k hyperplane: report the measured
+        # step against the floor of a dependent launch chain of the same width (graph replay)
+        sched = lib.trans_tuning(s.ctx).decode()
         roof["binding"] = "latency (one dependent step per i+j+k hyperplane)"
+        if sched.startswith("sweep=planes"):
+            cells_per_plane = ncell * nsub / dom_n
+            grid = max(1, int(round(cells_per_plane * 8 / 128)))
+            floor_us = lib.trans_probe_chain_us(1 if "chained" in sched else 0, grid)
+            roof["latency"] = {"us_per_step": per_launch_ms * 1e3, "floor_us_per_step": floor_us,
+                               "frac": floor_us / (per_launch_ms * 1e3) if floor_us > 0 else None,
+                               "floor": f"dependent launch chain, {grid} CTAs x 128 threads, one L2 round trip per step"}
     line = {
         "metric": "Mcell-iter/s", "value": value, "unit": "Mcell-iter/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

@@ -175,6 +175,11 @@ int trans_stage_times(void* ctx, int ki, double* ms);
 /* Measured fused multiply-add throughput of the FP64 (fp64=1) or FP32 pipe in GFLOP/s (no
  * reference counterpart: the compute roof the FP64 kernels are reported against). */
 double trans_probe_fma_gflops(int fp64);
+/* Measured time in microseconds of one dependent step of a chain of launches of `grid` CTAs (each
+ * thread reads through L2 what the previous launch wrote, then writes), replayed as a CUDA
+ * graph, with programmatic dependent launch when `chained` (no reference counterpart: the
+ * latency floor the per-hyperplane sweep launches are reported against). */
+double trans_probe_chain_us(int chained, int grid);
 /* n outer iterations KI = ki_first.. timed with CUDA events on the context's stream (ms: total).
  * norms as for trans_iterate (last iteration).  No reference counterpart: benchmarking. */
 int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norms* norms);

@@ -132,6 +132,8 @@ def bind_common(lib):
     lib.trans_stage_times.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
     lib.trans_probe_fma_gflops.argtypes = [C.c_int]
     lib.trans_probe_fma_gflops.restype = C.c_double
+    lib.trans_probe_chain_us.argtypes = [C.c_int, C.c_int]
+    lib.trans_probe_chain_us.restype = C.c_double
     lib.trans_time_iterations.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(TransNorms)]
     lib.trans_update_static_scratch.argtypes = [vp, C.c_int, C.POINTER(TransNorms)]
     lib.trans_kernel_times.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int]
@@ -160,7 +162,7 @@ def bind_common(lib):
 
 EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field", "trans_iterate",
             "trans_run_stage", "trans_get_norms", "trans_sync", "trans_device_bytes",
-            "trans_kernel_launches", "trans_last_error", "trans_stage_times", "trans_probe_fma_gflops",
+            "trans_kernel_launches", "trans_last_error", "trans_stage_times", "trans_probe_fma_gflops", "trans_probe_chain_us",
             "trans_time_iterations", "trans_update_static_scratch", "trans_tuning", "trans_kernel_times",
             "trans_kernel_class", "trans_batch_create", "trans_batch_case_bytes", "trans_batch_add",
             "trans_batch_remove", "trans_batch_set_field", "trans_batch_get_field", "trans_batch_iterate",

@@ -103,6 +103,8 @@ int trans_stage_times(void* ctx, int ki, double* ms) {
 
 double trans_probe_fma_gflops(int fp64) { return probe_fma_gflops(fp64); }
 
+double trans_probe_chain_us(int chained, int grid) { return probe_chain_us(chained, grid); }
+
 int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norms* norms) {
     Ctx* c = as_ctx(ctx);
     if (!c || !ms || n < 0 || c->cases.empty()) return TRANS_E_ARG;

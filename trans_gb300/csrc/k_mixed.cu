@@ -54,4 +54,64 @@ double probe_fma_gflops(int fp64) {
     double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
     return flops / (best * 1e-3) / 1e9;
 }
+
+// Floor of one dependent step of the hyperplane sweeps: a chain of launches of `grid` CTAs of
+// SWEEP_CTA threads where each thread reads, after the previous launch completed, a value the
+// previous launch wrote (through L2) and writes it back incremented -- the kernel boundary,
+// one dependent L2 round trip and the launch, without the sweep arithmetic.  Replayed as a
+// CUDA graph like the sweeps, with programmatic dependent launch when `chained`.
+__global__ void k_chain_probe(int* buf, int chained) {
+    if (chained) asm volatile("griddepcontrol.wait;" ::: "memory");
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int x = __ldcg(buf + t);
+    if (chained) asm volatile("griddepcontrol.launch_dependents;");
+    buf[t] = x + 1;
+}
+
+double probe_chain_us(int chained, int grid) {
+    const int n = 512;
+    if (grid < 1) grid = 1;
+    int* buf = nullptr;
+    if (cudaMalloc(&buf, sizeof(int) * (size_t)grid * SWEEP_CTA) != cudaSuccess) return -1.0;
+    cudaMemset(buf, 0, sizeof(int) * (size_t)grid * SWEEP_CTA);
+    cudaStream_t s;
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    double us = -1.0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(SWEEP_CTA);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = chained ? 1 : 0;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        for (int q = 0; q < n; ++q) cudaLaunchKernelEx(&cfg, k_chain_probe, buf, chained);
+        if (cudaStreamEndCapture(s, &g) == cudaSuccess && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) {
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0); cudaEventCreate(&e1);
+            float best = 1e30f;
+            for (int rep = 0; rep < 4; ++rep) {
+                cudaEventRecord(e0, s);
+                cudaGraphLaunch(ge, s);
+                cudaEventRecord(e1, s);
+                cudaEventSynchronize(e1);
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) best = ms < best ? ms : best;
+            }
+            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            us = best * 1e3 / n;
+        }
+    }
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    cudaStreamDestroy(s);
+    cudaFree(buf);
+    return us;
+}
 }  // namespace tg

@@ -24,6 +24,10 @@ from .solver import Batch, global_residual
 
 # grid levels of the cascade topology: (ns, nr, nh, nk) for about 0.35 M, 1.36 M and 5.4 M cells
 LEVELS = {"coarse": dict(ns=60, nh=32, nk=32), "medium": dict(), "fine": dict(ns=240, nh=128, nk=128)}
+# CFL ramp of every request (Time/SpectralRadius.F90:159-160: CFL_sub grows linearly from
+# CFL_Sub_start to CFL_Sub_end over CFL_Sub_step iterations); an impulsive start at CFL 10
+# diverged on the fine level
+RAMP = dict(CFL_Sub_start=2.0, CFL_Sub_end=10.0, CFL_Sub_step=200)
 
 
 @dataclass
@@ -65,6 +69,7 @@ def poisson_requests(rate=4.0, duration=60.0, seed=0, mix=(("coarse", 0.6), ("me
 def build_case(req, precision):
     """Host set-up of one request: grid, connectivity, geometry and initial field."""
     kw = dict(LEVELS.get(req.level, {}))
+    kw.update(RAMP)
     kw.update(req.grid)
     c = cases.cascade(XM=req.mach, p_ratio=req.p_ratio, precision=precision, **kw)
     conns, geo = CS.compute_geometry(c)
