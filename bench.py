@@ -209,7 +209,8 @@ def run_e2e(s, c, st, ki0, steps):
 
 def cpu_sample(c, conns, geo, st, seconds=15.0):
     """The oracle on the host cores for a bounded number of iterations of the same workload."""
-    from oracle.oracle import OracleSolver
+    from oracle.oracle import OracleSolver, load
+    load().oracle_set_threads(1)
     o = OracleSolver(c, conns, geo, st)
     o.iterate(1)
     n, t0 = 0, time.perf_counter()
@@ -228,9 +229,8 @@ def reference_arm(args):
     if rank != 0:
         return
     c, conns, geo, st = make_case(args.case, "fp64", args.nk)
-    from oracle.oracle import OracleSolver
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    from oracle.oracle import OracleSolver, load
+    threads = load().oracle_set_threads(os.cpu_count() or 1)
     o = OracleSolver(c, conns, geo, st)
     for w in range(args.warmup):
         o.iterate(1 + w)
@@ -247,7 +247,9 @@ def reference_arm(args):
             "config": {"workload": c.name, "cells": ncell, "blocks": len(c.blocks), "precision": "fp64",
                        "implementation": "C++ FP64 restatement of the reference (oracle/), OpenMP over blocks"},
             "cpu_baseline": {"value": v, "unit": "Mcell-iter/s", "cores": min(threads, len(c.blocks)),
-                             "kind": "port", "sample": f"{args.steps} iterations of {c.name}"},
+                             "kind": "port",
+                             "sample": f"{args.steps} iterations of {c.name}, OpenMP over its {len(c.blocks)} blocks "
+                                       f"({threads} threads available)"},
             "e2e": {"value": v, "unit": "Mcell-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

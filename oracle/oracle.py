@@ -37,6 +37,8 @@ def load():
         lib.oracle_iterate.argtypes = [vp, C.c_int, C.POINTER(abi.TransNorms)]
         lib.oracle_run_stage.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         lib.oracle_get_norms.argtypes = [vp, C.POINTER(abi.TransNorms)]
+        lib.oracle_set_threads.argtypes = [C.c_int]
+        lib.oracle_set_threads.restype = C.c_int
         lib.oracle_alimiter.argtypes = [C.c_double, C.c_double]
         lib.oracle_alimiter.restype = C.c_double
         dp = C.POINTER(C.c_double)

@@ -28,6 +28,9 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "../include/trans_gpu.h"
 #include "tmath.h"
@@ -1941,6 +1944,18 @@ int oracle_iterate(void* ctx, int ki, trans_norms* norms) {
     if (norms)
         for (size_t n = 0; n < c->B.size(); ++n) norms[n] = c->B[n].nrm;
     return c->nan_flag ? TRANS_E_NAN : TRANS_OK;
+}
+
+// host threads of the per-block loops (the reference runs one MPI rank per block); returns the
+// number in use after the call
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
 }
 
 int oracle_get_norms(void* ctx, trans_norms* norms) {
