@@ -118,6 +118,8 @@ struct Ctx {
     int sweep_exec_pdl = -1;             // chaining the sweep graph was captured with
     int sweep_wpc = 0;                   // SWEEP_WPC: warp-per-component thread mapping (0: lane-major)
     int sweep_exec_wpc = -1;             // mapping the sweep graph was captured with
+    int sweep_pf = 0;                    // L2 prefetch distance of the hyperplane launches (0 = none)
+    int sweep_exec_pf = -1;              // prefetch distance the sweep graph was captured with
     int sweep_lanes = 1;                 // DeltaQ components swept: 1 = all, 2 = k and omega only (Runge-Kutta)
     SweepSync* d_sync = nullptr;
     SweepSync* h_sync = nullptr;         // pinned

@@ -35,7 +35,7 @@ void jac(cudaStream_t s, const DevBlock* b, const SweepView& v) {
 // hyperplane's independent loads overlap the previous one (the kernel waits before its
 // dependent part)
 template <bool LOWER>
-void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained) {
+void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count) {
     if (count <= 0) return;
     const int* nbp = v.nbp;
     const TG_R* rec = (const TG_R*)v.rec;
@@ -50,10 +50,14 @@ void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = chained ? 1 : 0;
-    cudaLaunchKernelEx(&cfg, k_sweep<TG_R, LOWER>, nbp, rec, dq, n, first, count, turb, chained);
+    cudaLaunchKernelEx(&cfg, k_sweep<TG_R, LOWER>, nbp, rec, dq, n, first, count, turb, chained, pf_first, pf_count);
 }
-void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained) { swp<true>(s, v, first, count, turb, chained); }
-void swu(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained) { swp<false>(s, v, first, count, turb, chained); }
+void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count) {
+    swp<true>(s, v, first, count, turb, chained, pf_first, pf_count);
+}
+void swu(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count) {
+    swp<false>(s, v, first, count, turb, chained, pf_first, pf_count);
+}
 cudaError_t swa(cudaStream_t s, const SweepView& v, const int* po, int nplanes, int turb, SweepSync* sy, int grid, int block) {
     unsigned limit = SWEEP_SPIN_LIMIT;
     const int* nbp = v.nbp;

@@ -1020,10 +1020,24 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
 
 // one hyperplane [first, first+count) per launch (chained: launched with programmatic
 // stream serialisation, see sweep_item)
+__device__ inline void prefetch_l2_range(const void* p, size_t bytes, size_t t, size_t stride) {
+    const char* a = (const char*)p;
+    const char* a0 = (const char*)((uintptr_t)a & ~(uintptr_t)127);     // allocations are 256-byte aligned
+    const size_t lines = (size_t)(a + bytes - a0 + 127) / 128;
+    for (size_t l = t; l < lines; l += stride) asm volatile("prefetch.global.L2 [%0];" ::"l"(a0 + l * 128));
+}
+
+// pf_first/pf_count: a later hyperplane whose records and neighbour positions this launch
+// pulls into L2 (otherwise they come from DRAM on the path between two dependent steps)
 template <typename R, bool LOWER>
 __global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int first, int count, int lanes,
-                        int chained) {
+                        int chained, int pf_first, int pf_count) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pf_count > 0) {
+        const size_t T = (size_t)gridDim.x * blockDim.x;
+        prefetch_l2_range(rec + sw_at(pf_first, 0, NREC), (size_t)pf_count * NREC * sizeof(R), g, T);
+        prefetch_l2_range(nbp + sw_at(pf_first, 0, 6), (size_t)pf_count * 6 * sizeof(int), g, T);
+    }
     int e, L;
     sweep_map(g, lanes, e, L);
     if (e >= count) {

@@ -51,8 +51,9 @@ struct FluxLaunchers {
     void (*prep)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const SweepView&, const CaseDev*);
     void (*jac)(cudaStream_t, const DevBlock*, const SweepView&);     // neighbours' Jacobian terms (sweep order)
     // lanes: components swept (bits 0-1: 0 mean flow, 1 all, 2 k-omega) | SWEEP_WPC thread mapping
-    void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained);
-    void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained);
+    // (pf_first, pf_count: a later hyperplane prefetched into L2, count 0 = none)
+    void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained, int pf_first, int pf_count);
+    void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained, int pf_first, int pf_count);
     // both sweeps in one cooperative launch (grid must be co-resident: grid <= SMs x occupancy)
     cudaError_t (*sweep_all)(cudaStream_t, const SweepView&, const int* plane_off, int nplanes, int lanes, SweepSync*,
                              int grid, int block);

@@ -207,7 +207,8 @@ namespace {
 
 int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     const int lanes = c->sweep_lanes | c->sweep_wpc;
-    if (mode == 0 && c->sweep_exec && (c->sweep_exec_pdl != c->pdl || c->sweep_exec_wpc != c->sweep_wpc)) {   // changed
+    if (mode == 0 && c->sweep_exec &&
+        (c->sweep_exec_pdl != c->pdl || c->sweep_exec_wpc != c->sweep_wpc || c->sweep_exec_pf != c->sweep_pf)) {   // changed
         cudaGraphExecDestroy(c->sweep_exec);
         c->sweep_exec = nullptr;
     }
@@ -245,28 +246,27 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     }
     // one launch per hyperplane, L ascending then U descending, replayed as one graph (or
     // captured directly into the caller's graph)
+    // hyperplane h of the L sweep prefetches hyperplane h + sweep_pf into L2, the U sweep h - sweep_pf
+    auto planes = [&]() {
+        const int d = c->sweep_pf;
+        auto cnt = [&](int h) { return (h >= 0 && h < nh) ? c->plane_off[h + 1] - c->plane_off[h] : 0; };
+        for (int h = 0; h < nh; ++h)
+            if (cnt(h))
+                c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt(h), lanes, c->pdl, d && h + d < nh ? c->plane_off[h + d] : 0,
+                                   d ? cnt(h + d) : 0);
+        for (int h = nh - 1; h >= 0; --h)
+            if (cnt(h))
+                c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt(h), lanes, c->pdl, d && h - d >= 0 ? c->plane_off[h - d] : 0,
+                                   d ? cnt(h - d) : 0);
+    };
     if (capture) {
-        for (int h = 0; h < nh; ++h) {
-            int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, lanes, c->pdl);
-        }
-        for (int h = nh - 1; h >= 0; --h) {
-            int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, lanes, c->pdl);
-        }
+        planes();
         return TRANS_OK;
     }
     if (!c->sweep_exec) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int h = 0; h < nh; ++h) {
-            int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt, lanes, c->pdl);
-        }
-        for (int h = nh - 1; h >= 0; --h) {
-            int cnt = c->plane_off[h + 1] - c->plane_off[h];
-            if (cnt) c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt, lanes, c->pdl);
-        }
+        planes();
         cudaError_t e = cudaStreamEndCapture(s, &g);
         if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph capture: ") + cudaGetErrorString(e));
         e = cudaGraphInstantiate(&c->sweep_exec, g, 0);
@@ -274,6 +274,7 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph instantiate: ") + cudaGetErrorString(e));
         c->sweep_exec_pdl = c->pdl;
         c->sweep_exec_wpc = c->sweep_wpc;
+        c->sweep_exec_pf = c->sweep_pf;
     }
     CK(cudaGraphLaunch(c->sweep_exec, s));
     for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
@@ -295,25 +296,27 @@ int tune_sweeps(Ctx* c) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    struct Cand { int mode, grid, block, pdl, ti, tj, tk, wpc; };
+    struct Cand { int mode, grid, block, pdl, ti, tj, tk, wpc, pf; };
     std::vector<Cand> cands;
     for (int wpc : {0, SWEEP_WPC}) {
-        cands.push_back({0, 0, 0, 1, 0, 0, 0, wpc});
-        cands.push_back({0, 0, 0, 0, 0, 0, 0, wpc});
+        for (int pf : {0, 1, 2, 4}) {             // prefetch distance (hyperplanes) of the plane launches
+            cands.push_back({0, 0, 0, 1, 0, 0, 0, wpc, pf});
+            cands.push_back({0, 0, 0, 0, 0, 0, 0, wpc, pf});
+        }
         for (int block : {128, 256, 512}) {
             int occ = c->fl->sweep_all_occupancy(block);
             for (int per : {1, 2, 4})
-                if (per <= occ) cands.push_back({1, per * nsm, block, 0, 0, 0, 0, wpc});
+                if (per <= occ) cands.push_back({1, per * nsm, block, 0, 0, 0, 0, wpc, 0});
         }
         // tiled wavefront: tile shapes x CTA sizes, one resident wave of CTAs
         const int shapes[][3] = {{16, 4, 4}, {8, 4, 4}, {4, 4, 4}};
         for (const auto& sh : shapes)
             for (int block : {256, 512}) {
                 const int occ = c->fl->sweep_tiles_occupancy(block);
-                if (occ >= 1) cands.push_back({3, occ * nsm, block, 0, sh[0], sh[1], sh[2], wpc});
+                if (occ >= 1) cands.push_back({3, occ * nsm, block, 0, sh[0], sh[1], sh[2], wpc, 0});
             }
     }
-    if (c->fl->sweep_flow_occupancy(256) >= 4) cands.push_back({2, 4 * nsm, 256, 0, 0, 0, 0, 0});
+    if (c->fl->sweep_flow_occupancy(256) >= 4) cands.push_back({2, 4 * nsm, 256, 0, 0, 0, 0, 0, 0});
     const int pdl0 = c->pdl_allowed;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -325,6 +328,7 @@ int tune_sweeps(Ctx* c) {
     for (const Cand& k : cands) {
         if (k.mode == 0) c->pdl = pdl0 ? k.pdl : 0;
         c->sweep_wpc = k.wpc;
+        c->sweep_pf = k.pf;
         if (k.mode == 3 && (rc = build_tiles(c, k.ti, k.tj, k.tk))) break;
         for (int rep = 0; rep < 2 && rc == TRANS_OK; ++rep) {      // first run warms up (graph build)
             if ((rc = save_dq(c, true))) break;
@@ -341,7 +345,7 @@ int tune_sweeps(Ctx* c) {
                                                                       + std::to_string(k.tk) + "/" : std::string())
                                                  + std::to_string(k.grid) + "x" + std::to_string(k.block)
                                            : std::string(c->pdl ? "planes-chained" : "planes"))
-                                   + (k.wpc ? "/wpc" : "")
+                                   + (k.wpc ? "/wpc" : "") + (k.pf ? "/pf" + std::to_string(k.pf) : "")
                                    + ":" + std::to_string(ms) + "ms ";
                 if (ms < best) { best = ms; pick = k; }
             }
@@ -356,6 +360,7 @@ int tune_sweeps(Ctx* c) {
     if (pick.mode == 3 && (rc = build_tiles(c, pick.ti, pick.tj, pick.tk))) return rc;
     c->sweep_mode = pick.mode; c->sweep_grid = pick.grid; c->sweep_block = pick.block;
     c->sweep_wpc = pick.wpc;
+    c->sweep_pf = pick.pf;
     c->pdl = pick.mode == 0 ? (pdl0 ? pick.pdl : 0) : 0;
     return TRANS_OK;
 }
