@@ -407,7 +407,7 @@ def main():
         sched = lib.trans_tuning(s.ctx).decode()
         roof["binding"] = "latency (one dependent step per i+j+k hyperplane)"
         if sched.startswith("sweep=planes"):
-            cells_per_plane = ncell * nsub / dom_n
+            cells_per_plane = ncell * nsub * 2 / dom_n      # dom_n counts both sweeps' hyperplanes
             grid = max(1, int(round(cells_per_plane * 8 / 128)))
             floor_us = lib.trans_probe_chain_us(1 if "chained" in sched else 0, grid)
             roof["latency"] = {"us_per_step": per_launch_ms * 1e3, "floor_us_per_step": floor_us,

@@ -981,18 +981,27 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
     // one launch per hyperplane chained with programmatic dependent launch: wait for the
     // previous hyperplane to complete, then let the next one start its loads
     if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+    // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1
+    // line).  Every lane loads in converged code, before the per-component branches, so that a
+    // warp waits for one dependent L2 round trip instead of one per divergent branch.
+    R nq[3][5], nt[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const long long np = npv[d] >= 0 ? npv[d] : q;
+#pragma unroll
+        for (int m = 0; m < 5; ++m) nq[d][m] = __ldcg(dq + sw_at(np, m, DQ_STRIDE));
+        nt[d] = __ldcg(dq + sw_at(np, L < 5 ? 0 : L, DQ_STRIDE));
+    }
+    R* D = dq + sw_at(q, L, DQ_STRIDE);
+    const R own = __ldcg(D);
     R acc[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const bool has = npv[d] >= 0;
-        const long long np = has ? npv[d] : q;
         const R RDSt = k[d][6];
         R val;
-        // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1 line)
         if (L < 5) {
-            R AinRo = __ldcg(dq + sw_at(np, 0, DQ_STRIDE)), AinRx = __ldcg(dq + sw_at(np, 1, DQ_STRIDE));
-            R AinRy = __ldcg(dq + sw_at(np, 2, DQ_STRIDE)), AinRz = __ldcg(dq + sw_at(np, 3, DQ_STRIDE));
-            R AinRe = __ldcg(dq + sw_at(np, 4, DQ_STRIDE));
+            const R AinRo = nq[d][0], AinRx = nq[d][1], AinRy = nq[d][2], AinRz = nq[d][3], AinRe = nq[d][4];
             R Dif;
             if (L == 0) {
                 const R aSDt = R(0.0);
@@ -1006,13 +1015,11 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
             val = R(0.5) * (Dif + sgn * (RDSt * Din));
         } else {
             const R VP = k[d][0];
-            const R Dq = __ldcg(dq + sw_at(np, L, DQ_STRIDE));
+            const R Dq = nt[d];
             val = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
         }
         acc[d] = has ? val : R(0.0);
     }
-    R* D = dq + sw_at(q, L, DQ_STRIDE);
-    const R own = __ldcg(D);
     const R sum = acc[0] + acc[1] + acc[2];
     if (LOWER) *D = (own * stept + sum * cvs) / den;
     else *D = own - sum * cvs / den;
