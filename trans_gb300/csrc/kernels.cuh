@@ -946,7 +946,7 @@ __device__ inline void sweep_map(int g, int lanes, int& e, int& L) {
 
 template <typename R, bool LOWER>
 __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
-                                  int L, int turb, bool chained = false) {
+                                  int L, int turb, bool chained = false, bool hoist = true) {
     if (L >= 7 || (L >= 5 && turb == 0) || (L < 5 && turb == 2)) {
         if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
         return;
@@ -984,13 +984,16 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
     // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1
     // line).  Every lane loads in converged code, before the per-component branches, so that a
     // warp waits for one dependent L2 round trip instead of one per divergent branch.
+    // (A warp of the warp-per-component mapping takes one branch: it loads inside it.)
     R nq[3][5], nt[3];
+    if (hoist) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const long long np = npv[d] >= 0 ? npv[d] : q;
+        for (int d = 0; d < 3; ++d) {
+            const long long np = npv[d] >= 0 ? npv[d] : q;
 #pragma unroll
-        for (int m = 0; m < 5; ++m) nq[d][m] = __ldcg(dq + sw_at(np, m, DQ_STRIDE));
-        nt[d] = __ldcg(dq + sw_at(np, L < 5 ? 0 : L, DQ_STRIDE));
+            for (int m = 0; m < 5; ++m) nq[d][m] = __ldcg(dq + sw_at(np, m, DQ_STRIDE));
+            nt[d] = __ldcg(dq + sw_at(np, L < 5 ? 0 : L, DQ_STRIDE));
+        }
     }
     R* D = dq + sw_at(q, L, DQ_STRIDE);
     const R own = __ldcg(D);
@@ -998,9 +1001,13 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const bool has = npv[d] >= 0;
+        const long long np = has ? npv[d] : q;
         const R RDSt = k[d][6];
         R val;
         if (L < 5) {
+            if (!hoist)
+#pragma unroll
+                for (int m = 0; m < 5; ++m) nq[d][m] = __ldcg(dq + sw_at(np, m, DQ_STRIDE));
             const R AinRo = nq[d][0], AinRx = nq[d][1], AinRy = nq[d][2], AinRz = nq[d][3], AinRe = nq[d][4];
             R Dif;
             if (L == 0) {
@@ -1015,7 +1022,7 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
             val = R(0.5) * (Dif + sgn * (RDSt * Din));
         } else {
             const R VP = k[d][0];
-            const R Dq = nt[d];
+            const R Dq = hoist ? nt[d] : __ldcg(dq + sw_at(np, L, DQ_STRIDE));
             val = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
         }
         acc[d] = has ? val : R(0.0);
@@ -1051,7 +1058,7 @@ __global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, 
         if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
         return;
     }
-    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, chained != 0);
+    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, chained != 0, !(lanes & SWEEP_WPC));
 }
 
 // Grid-wide barrier of a co-resident (cooperative) grid.  The wait is bounded: after `limit`
@@ -1092,7 +1099,7 @@ __global__ void k_sweep_all(const int* __restrict__ nbp, const R* __restrict__ r
         for (int g = tid; g < items; g += stride) {
             int e, L;
             sweep_map(g, lanes, e, L);
-            if (e < n) sweep_item<R, true>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3);
+            if (e < n) sweep_item<R, true>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, false, !(lanes & SWEEP_WPC));
         }
         if (!grid_barrier(sy, gridDim.x, limit)) return;
     }
@@ -1101,7 +1108,7 @@ __global__ void k_sweep_all(const int* __restrict__ nbp, const R* __restrict__ r
         for (int g = tid; g < items; g += stride) {
             int e, L;
             sweep_map(g, lanes, e, L);
-            if (e < n) sweep_item<R, false>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3);
+            if (e < n) sweep_item<R, false>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, false, !(lanes & SWEEP_WPC));
         }
         if (h > 0 && !grid_barrier(sy, gridDim.x, limit)) return;
     }
@@ -1214,8 +1221,8 @@ __global__ void k_sweep_tiles(const int* __restrict__ nbp, const R* __restrict__
                 sweep_map(g, lanes, e, L);
                 if (e >= n) continue;
                 const long long q = tv.item[a + e];
-                if (lower) sweep_item<R, true>(nbp, rec, dq, N, q, L, lanes & 3);
-                else sweep_item<R, false>(nbp, rec, dq, N, q, L, lanes & 3);
+                if (lower) sweep_item<R, true>(nbp, rec, dq, N, q, L, lanes & 3, false, !(lanes & SWEEP_WPC));
+                else sweep_item<R, false>(nbp, rec, dq, N, q, L, lanes & 3, false, !(lanes & SWEEP_WPC));
             }
             __syncthreads();
         }
