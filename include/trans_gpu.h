@@ -156,6 +156,8 @@ enum trans_stage {
 
 int trans_create(const trans_params* p, int nblocks, const trans_block* blocks, void** ctx);
 int trans_destroy(void* ctx);         /* NULL is a no-op returning TRANS_OK */
+/* trans_set_field returns once the caller's array has been copied (it may be reused at once); the
+ * transpose into the device layout completes in order before any later call's device work. */
 int trans_set_field(void* ctx, int ib, int field, const double* fortran_array);
 int trans_get_field(void* ctx, int ib, int field, double* fortran_array);
 /* One outer iteration KI (main.F90:48-197).  norms: array of nblocks entries, may be NULL. */

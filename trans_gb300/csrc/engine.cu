@@ -194,6 +194,7 @@ void ctx_free(Ctx* c) {
     c->cases.clear();
     dfree(c->d_sync);
     if (c->h_sync) { cudaFreeHost(c->h_sync); c->h_sync = nullptr; }
+    if (c->copy_done) { cudaEventDestroy(c->copy_done); c->copy_done = nullptr; }
     if (c->stream) { cudaStreamDestroy(c->stream); c->stream = nullptr; }
 }
 

@@ -99,6 +99,7 @@ struct Ctx {
     CaseDev* h_cdev = nullptr;           // pinned
     std::vector<CaseDev> cdev_last;      // what was last uploaded
     double* d_stage = nullptr;           // Fortran-layout staging buffer of trans_set/get_field
+    cudaEvent_t copy_done = nullptr;     // the last upload's host-to-device copy
     size_t stage_doubles = 0;
     bool built = false;
     // ---- sweep schedule ----

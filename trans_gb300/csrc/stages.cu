@@ -171,6 +171,8 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
     int is_sd = f == TRANS_SD ? 1 : 0;
     if (upload) {
         CK(cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, s));
+        if (!c->copy_done) CK(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
+        CK(cudaEventRecord(c->copy_done, s));
         launch_field_xfer(s, b, fm.slot, fm.ncomp, fm.lb, is_sd, c->d_stage, 1);
         c->launches++;
         if (f == TRANS_THTC) {      // sin/cos of the outlet recurrence, evaluated once on the host
@@ -186,6 +188,11 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
         if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}});
         if (c->mixed && f == TRANS_DQDXYZ) mirror(c, {{S_DQ, 18}});
         if (c->mixed && f == TRANS_SHOCK) mirror(c, {{S_SHOCK, 1}});
+        // the caller's buffer is free once the copy is done; the transpose into the slots runs
+        // on in stream order (later copies into the staging buffer queue behind it)
+        CK(cudaGetLastError());
+        CK(cudaEventSynchronize(c->copy_done));
+        return TRANS_OK;
     } else {
         // the mixed path keeps DeltaQ, the gradients and the shock sensor in FP32
         if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}}, 1);
