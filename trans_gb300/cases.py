@@ -134,7 +134,7 @@ def _two_sided(n, first):
 
 
 def cascade(nle=8, nte=4, ns=120, npitch=16, nr=48, nh=64, nk=64, Re_c=1.0e6, XM=0.6, inflow_deg=40.0,
-            p_ratio=0.85, pitch=0.8, span=1.0, radius=10.0, **switches):
+            p_ratio=0.85, pitch=0.8, span=1.0, radius=10.0, cluster=1.0, **switches):
     """Linear compressor cascade passage with the block structure of a turbomachinery mesh:
     O-block (2*nte+2*ns+nle around x nr x nk) on a circular-arc blade (8% thick, 40 deg camber,
     30 deg stagger), inlet/outlet H-blocks (nh x (2*npitch+nle) x nk) and two passage blocks
@@ -154,7 +154,10 @@ def cascade(nle=8, nte=4, ns=120, npitch=16, nr=48, nh=64, nk=64, Re_c=1.0e6, XM
     surf, mean = _blade(rot_deg=-inflow_deg)
     # chord-fraction parameters of the blade loop segments
     xi_l, xi_t = 0.02, 0.98
-    u = 0.5 * (1.0 - dm.cos(dm.pi * np.linspace(0.0, 1.0, ns + 1)))
+    t = np.linspace(0.0, 1.0, ns + 1)
+    u = 0.5 * (1.0 - dm.cos(dm.pi * t))
+    if cluster != 1.0:          # blend the cosine clustering with uniform spacing
+        u = cluster * u + (1.0 - cluster) * t
     xi_side = xi_l + (xi_t - xi_l) * u                   # LE -> TE
     # mean line of the passage: camber line on the blade, continued with the end slopes
     xm_le, ym_le = mean(np.array(0.0))
