@@ -23,7 +23,12 @@ from . import cases
 from .solver import Batch, global_residual
 
 # grid levels of the cascade topology: (ns, nr, nh, nk) for about 0.35 M, 1.36 M and 5.4 M cells
-LEVELS = {"coarse": dict(ns=60, nh=32, nk=32), "medium": dict(), "fine": dict(ns=240, nh=128, nk=128)}
+# grid levels: coarse ~0.35 M, medium 1.36 M, fine ~5.5 M cells.  The fine level also doubles the
+# leading/trailing-edge caps and blends the side clustering with uniform spacing: with the
+# medium level's cosine clustering at 240 side cells, the side cell next to the trailing-edge
+# cap is 1/60 of the cap cell and the solve diverged at the trailing-edge/endwall corner
+LEVELS = {"coarse": dict(ns=60, nh=32, nk=32), "medium": dict(),
+          "fine": dict(ns=240, nh=128, nk=128, nle=16, nte=8, cluster=0.6)}
 # CFL ramp of every request (Time/SpectralRadius.F90:159-160: CFL_sub grows linearly from
 # CFL_Sub_start to CFL_Sub_end over CFL_Sub_step iterations); an impulsive start at CFL 10
 # diverged on the fine level
