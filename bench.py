@@ -286,6 +286,59 @@ def batched_leg(c, conns, geo, st, args):
     return out
 
 
+def batch_levels_arm(args):
+    """Batched steady solves of uneven size: cascades at three grid levels (counts
+    `--batch-levels C,M,F` of coarse ~0.35 M / medium 1.36 M / fine ~5.5 M cells), back-pressure
+    ratios U[0.80, 0.92] and inlet angles from {36, 40, 44} deg (seeded; the angle rotates the
+    grid, so each level's geometry is computed once per angle), all in one batch context under
+    the device budget; aggregate cell-iterations/s timed like the single case."""
+    from trans_gb300 import serving
+    from trans_gb300.solver import Batch
+    prec = abi.TRANS_MIXED if args.precision == "mixed" else abi.TRANS_FP64
+    counts = [int(x) for x in args.batch_levels.split(",")]
+    rng = np.random.default_rng(0)
+    bt = Batch(prec, budget_bytes=int(args.budget_gb * 1e9))
+    geoms, admitted, refused, cells = {}, 0, 0, 0
+    t0 = time.perf_counter()
+    for level, n in zip(("coarse", "medium", "fine"), counts):
+        for q in range(n):
+            ratio = float(rng.uniform(0.80, 0.92))
+            angle = float(rng.choice([36.0, 40.0, 44.0]))
+            kw = dict(serving.LEVELS[level])
+            kw.update(serving.RAMP)
+            key = (level, angle)
+            c = cases.cascade(inflow_deg=angle, p_ratio=ratio, precision=prec, **kw)
+            if key not in geoms:
+                conns, geo = CS.compute_geometry(c)
+                geoms[key] = (conns, geo, CS.initial_state(c, geo, Q_dst=c.meta.get("Q_dst", 0.01)))
+            conns, geo, st = geoms[key]
+            if bt.add(c, conns, geo, st) is None:
+                refused += 1
+                continue
+            admitted += 1
+            cells += interior_cells(c)
+    setup_s = time.perf_counter() - t0
+    geoms.clear()
+    bt.iterate(max(args.warmup, 1))
+    if bt.lib.trans_prepare(bt.ctx, -1) != 0:
+        raise RuntimeError(bt.lib.trans_last_error(bt.ctx).decode())
+    ms = C.c_double()
+    rc = bt.lib.trans_batch_time_iterations(bt.ctx, args.steps, C.byref(ms))
+    if rc not in (0, abi.TRANS_E_NAN):
+        raise RuntimeError(f"batched timing failed {rc}")
+    value = cells * args.steps / (ms.value * 1e-3) / 1e6
+    line = {"metric": "Mcell-iter/s", "value": value, "unit": "Mcell-iter/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms.value / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == abi.TRANS_FP64 else "f32-flux/f64-update", "data": "synthetic",
+            "config": {"workload": "batched cascades at three grid levels", "requested": counts, "admitted": admitted,
+                       "refused_over_budget": refused, "cells": cells, "budget_gb": args.budget_gb,
+                       "device_gb_in_use": bt.bytes_in_use() / 1e9, "host_setup_s": setup_s,
+                       "sweep_schedule": bt.lib.trans_tuning(bt.ctx).decode()[:60]},
+            "nan_in_timed_steps": rc == abi.TRANS_E_NAN}
+    bt.close()
+    print(json.dumps(line))
+
+
 def serve_arm(args):
     """Serving stream: seeded Poisson arrivals of cascade solves (grid level coarse 60% /
     medium 30% / fine 10%, back-pressure ratio U[0.80,0.92], inlet Mach U[0.5,0.7]) admitted
@@ -321,6 +374,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nk", type=int, default=64, help="spanwise cells of the cascade (64 = full size)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--batch-levels", default=None,
+                    help="batched cascades at three grid levels: counts C,M,F (e.g. 32,24,8)")
     ap.add_argument("--batch", type=int, default=0,
                     help="also time N copies of the workload (back-pressure ratios 0.80..0.92) in one batch context")
     ap.add_argument("--serve", action="store_true", help="run the serving stream instead (p50/p99 latency)")
@@ -329,6 +384,8 @@ def main():
     ap.add_argument("--drop", type=float, default=1e-3, help="serving: residual drop at which a request retires")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device-memory budget")
     args = ap.parse_args()
+    if args.batch_levels:
+        return batch_levels_arm(args)
     if args.serve:
         return serve_arm(args)
     if args.impl == "reference":

@@ -157,17 +157,30 @@ int collect_norms(Ctx* c, const BlockNorms* hn) {
 
 int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
     if (!c || !cs || ib < 0 || ib >= (int)cs->blk.size() || !host) return TRANS_E_ARG;
-    if (!c->built) {
-        int rc = rebuild(c);
-        if (rc) return rc;
-    }
     FieldMap fm = field_map(f);
     if (fm.slot < 0) return fail(c, TRANS_E_ARG, "bad field id");
     if (f == TRANS_WT2 && cs->p.IF_RK != 1) return fail(c, TRANS_E_ARG, "Wt2 exists in Runge-Kutta cases only");
-    const DevBlock& b = c->blk[cs->blk0 + ib];
+    // the FP32 copies of D, DQdxyz and shock go through the work lists; every other field only
+    // needs the case's own block (so adding a case and filling it does not rebuild the lists)
+    const bool mirrored = c->mixed && (f == TRANS_D || f == TRANS_DQDXYZ || f == TRANS_SHOCK);
+    if (mirrored && !c->built) {
+        int rc = rebuild(c);
+        if (rc) return rc;
+    }
+    const DevBlock& b = cs->blk[ib];
     size_t ncells = (size_t)(b.NI + 3 - fm.lb) * (b.NJ + 3 - fm.lb) * (b.NK + 3 - fm.lb);
     size_t bytes = ncells * fm.ncomp * sizeof(double);
     cudaStream_t s = c->stream;
+    if (!c->d_stage || c->stage_doubles < ncells * fm.ncomp) {          // staging for the largest field so far
+        CK(cudaStreamSynchronize(s));
+        if (c->d_stage) cudaFree(c->d_stage);
+        c->d_stage = nullptr;
+        c->stage_doubles = 0;
+        size_t mx = (size_t)(b.NI + 4) * (b.NJ + 4) * (b.NK + 4) * 18;  // DQdxyz of this block
+        mx = std::max(mx, ncells * fm.ncomp);
+        CK(cudaMalloc(&c->d_stage, mx * sizeof(double)));
+        c->stage_doubles = mx;
+    }
     int is_sd = f == TRANS_SD ? 1 : 0;
     if (upload) {
         CK(cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, s));
