@@ -9,6 +9,9 @@ namespace tg {
 void launch_specrad_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev) {
     if (nt > 0) k_specrad_mixed<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev);
 }
+void launch_prims_mixed(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off) {
+    if (total > 0) k_prims_mixed<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off);
+}
 void launch_update_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts) {
     if (nt > 0) k_update_mixed<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev, parts);
 }

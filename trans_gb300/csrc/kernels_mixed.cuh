@@ -58,6 +58,40 @@ __global__ void k_specrad_mixed(const DevBlock* __restrict__ blks, const Tile* _
     slot(b, S_DTM)[c] = dtm;
 }
 
+// ---------------------------------------------------------------------------------------
+// Mixed path: the FP32 copies the FP32 kernels read, in one pass over every padded cell: the
+// state V(7), p, T, mu_t, the spectral radii and time step, and the primitives u, v, w,
+// k/rho, omega/rho, 1/rho and the LU-SGS velocities from one FP64 reciprocal of rho (the FP64
+// path's k_prims divides per component and keeps FP64 primitives, which nothing in the mixed
+// path reads).
+// ---------------------------------------------------------------------------------------
+__global__ void k_prims_mixed(const DevBlock* __restrict__ blks, int nblk, long long total, const long long* __restrict__ off) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = nblk - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (off[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DevBlock b = blks[lo];
+    const int c = (int)(g - off[lo]);
+    double v[7];
+    for (int L = 0; L < 7; ++L) {
+        v[L] = slot(b, S_V + L)[c];
+        fslot(b, S_V + L)[c] = (float)v[L];
+    }
+    for (int q = S_PP; q <= S_RMIU; ++q) fslot(b, q)[c] = (float)slot(b, q)[c];
+    for (int q = S_RDS; q <= S_DTM; ++q) fslot(b, q)[c] = (float)slot(b, q)[c];
+    const double ri = 1.0 / v[0];
+    const float u = (float)(v[1] * ri), vv = (float)(v[2] * ri), w = (float)(v[3] * ri);
+    fslot(b, S_PRIM)[c] = u;
+    fslot(b, S_PRIM + 1)[c] = vv;
+    fslot(b, S_PRIM + 2)[c] = w;
+    fslot(b, S_PRIM + 3)[c] = (float)(v[5] * ri);
+    fslot(b, S_PRIM + 4)[c] = (float)(v[6] * ri);
+    fslot(b, S_RINV)[c] = (float)ri;
+    fslot(b, S_SVEL)[c] = u;
+    fslot(b, S_SVEL + 1)[c] = vv;
+    fslot(b, S_SVEL + 2)[c] = w;
+}
+
 // p + p*expm1(dp/(p+1e-10)) for dp < 0, p + dp otherwise (Time/TIME_Update_V.F90:660-675)
 __device__ inline double positive_add(double p, double dp) {
     if (dp >= 0.0) return p + dp;

@@ -431,9 +431,14 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             break;
         case TRANS_STAGE_GRADIENT:
             if (!capture && (rc = upload_cdev(c))) return rc;
-            { KScope t(c, K_PRIMS); launch_prims(s, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off); }
-            // the FP32 kernels read FP32 copies of this sub-iteration's state, primitives and radii
-            if (c->mixed) { KScope t(c, K_MIRROR); mirror(c, {{S_V, 10}, {S_RDS, 4}, {S_PRIM, 5}, {S_RINV, 4}}); }
+            if (c->mixed) {
+                // the FP32 kernels read FP32 copies of this sub-iteration's state, primitives and radii
+                KScope t(c, K_PRIMS);
+                launch_prims_mixed(s, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off);
+            } else {
+                KScope t(c, K_PRIMS);
+                launch_prims(s, c->d_blk, (int)c->blk.size(), c->total_cells, c->d_off);
+            }
             { KScope t(c, K_GRADIENT); c->fl->gradient(s, c->d_blk, c->d_cell, nct, c->d_cdev); }
             { KScope t(c, K_SHOCK_GHOST); c->fl->shock_ghost(s, c->d_blk, c->d_ghost, (int)c->ghost_tiles.size()); }
             c->launches += 3;
