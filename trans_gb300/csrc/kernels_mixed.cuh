@@ -92,6 +92,69 @@ __global__ void k_prims_mixed(const DevBlock* __restrict__ blks, int nblk, long 
     fslot(b, S_SVEL + 2)[c] = w;
 }
 
+// ---------------------------------------------------------------------------------------
+// BC/BC_Outlet.F90:37-107, mixed path: the radial-equilibrium recurrence along j with the
+// divisions moved off the dependent chain.  The velocities of the previous j enter as
+// V(3:4)/V(1) of its interior cell (equal to the ghost's rho*v / rho, which the FP64 path
+// divides out), 1/(r + tiny), RXM2/T and 1/V(1) do not depend on the recurrence, so one step
+// of the chain is p_j = p_{j-1} + |dr * rho_{j-1} * (..)^2| * 1/(r + tiny), rho_j = p_j * RXM2/T.
+// ---------------------------------------------------------------------------------------
+__global__ void k_bc_outlet_mixed(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent,
+                                  const OutletLine* __restrict__ lines, int nl, const CaseDev* __restrict__ cdev) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nl) return;
+    const OutletLine Ln = lines[q];
+    const DevBlock b = blks[Ln.blk];
+    const Params& p = cdev[b.cs].p;
+    const int turb = cdev[b.cs].turb;
+    double* V[7];
+    for (int m = 0; m < 7; ++m) V[m] = slot(b, S_V + m);
+    double* PP = slot(b, S_PP);
+    double* T = slot(b, S_T);
+    double* Rm = slot(b, S_RMIU);
+    const double* rad = slot(b, S_RAD);
+    const double* sint = slot(b, S_SINT);
+    const double* cost = slot(b, S_COST);
+    double pp_prev = 0.0, den_prev = 1.0, vy_prev = 0.0, vz_prev = 0.0;
+    for (int e = Ln.first; e < Ln.first + Ln.n; ++e) {
+        const BCEntry E = ent[e];
+        const int s0 = E.s[0], l0 = E.l[0];
+        const double Tl = T[s0];
+        const double rv1 = 1.0 / V[0][s0];
+        const double vy = V[2][s0] * rv1, vz = V[3][s0] * rv1;
+        double pp;
+        if (E.sub == 1) {                              // j == Jbgn
+            pp = p.Pouthub;
+        } else {
+            const int lm = l0 - b.PI;                   // (il, jl-1, kl)
+            const double rcs1 = rad[l0], rcs2 = rad[lm];
+            const double RoVr2 = sq(vz_prev * cost[lm] - sint[lm] * vy_prev + p.omega0 * rcs2);
+            pp = pp_prev + fabs((rcs1 - rcs2) * den_prev * RoVr2) * (1.0 / (rcs2 + p.Tiny));
+        }
+        const double den = pp * (p.RXM2 / Tl);
+        const double den_ratio = den * rv1;
+        const double v2 = V[1][s0] * den_ratio, v3 = V[2][s0] * den_ratio, v4 = V[3][s0] * den_ratio;
+        T[l0] = Tl;
+        PP[l0] = pp;
+        V[0][l0] = den; V[1][l0] = v2; V[2][l0] = v3; V[3][l0] = v4;
+        for (int L = 1; L < 3; ++L) {
+            const int ig = E.l[L];
+            V[0][ig] = den; V[1][ig] = v2; V[2][ig] = v3; V[3][ig] = v4;
+            PP[ig] = pp;
+            T[ig] = Tl;
+        }
+        if (turb) {
+            const double k6 = V[5][s0], k7 = V[6][s0], rm = Rm[s0];
+            V[5][l0] = k6; V[6][l0] = k7; Rm[l0] = rm;
+            for (int L = 1; L < 3; ++L) {
+                const int ig = E.l[L];
+                V[5][ig] = k6; V[6][ig] = k7; Rm[ig] = rm;
+            }
+        }
+        pp_prev = pp; den_prev = den; vy_prev = vy; vz_prev = vz;
+    }
+}
+
 // p + p*expm1(dp/(p+1e-10)) for dp < 0, p + dp otherwise (Time/TIME_Update_V.F90:660-675)
 __device__ inline double positive_add(double p, double dp) {
     if (dp >= 0.0) return p + dp;

@@ -26,6 +26,8 @@ void launch_block_norms(cudaStream_t s, const DevBlock* blks, int nblk, const No
 void launch_mirror(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off, const MirrorList& ml);
 void launch_update_u(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev);
 // the mixed path's reduced-operation forms of the spectral radius and the update (k_mixed.cu)
+void launch_bc_outlet_mixed(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const OutletLine* lines, int nl,
+                            const CaseDev* cdev);
 void launch_prims_mixed(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
 void launch_specrad_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev);
 void launch_update_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts);

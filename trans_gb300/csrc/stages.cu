@@ -426,7 +426,11 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
         case TRANS_STAGE_BC_STATE:
             if (!capture && (rc = upload_cdev(c))) return rc;
             { KScope t(c, K_BC_STATE); launch_bc_state(s, c->d_blk, c->d_bc, (int)c->bc.size(), c->d_cdev); }
-            { KScope t(c, K_BC_OUTLET); launch_bc_outlet(s, c->d_blk, c->d_outlet, c->d_lines, (int)c->lines.size(), c->d_cdev); }
+            {
+                KScope t(c, K_BC_OUTLET);
+                if (c->mixed) launch_bc_outlet_mixed(s, c->d_blk, c->d_outlet, c->d_lines, (int)c->lines.size(), c->d_cdev);
+                else launch_bc_outlet(s, c->d_blk, c->d_outlet, c->d_lines, (int)c->lines.size(), c->d_cdev);
+            }
             c->launches += 1 + (c->lines.empty() ? 0 : 1);
             break;
         case TRANS_STAGE_GRADIENT:
