@@ -11,7 +11,7 @@ void launch_specrad_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tile
 }
 void launch_bc_outlet_mixed(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const OutletLine* lines, int nl,
                             const CaseDev* cdev) {
-    if (nl > 0) k_bc_outlet_mixed<<<(nl + 63) / 64, 64, 0, s>>>(blks, ent, lines, nl, cdev);
+    if (nl > 0) k_bc_outlet_mixed<<<(nl + 3) / 4, 128, 0, s>>>(blks, ent, lines, nl, cdev);     // a warp per line
 }
 void launch_prims_mixed(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off) {
     if (total > 0) k_prims_mixed<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off);

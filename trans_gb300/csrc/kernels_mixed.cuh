@@ -93,65 +93,91 @@ __global__ void k_prims_mixed(const DevBlock* __restrict__ blks, int nblk, long 
 }
 
 // ---------------------------------------------------------------------------------------
-// BC/BC_Outlet.F90:37-107, mixed path: the radial-equilibrium recurrence along j with the
-// divisions moved off the dependent chain.  The velocities of the previous j enter as
-// V(3:4)/V(1) of its interior cell (equal to the ghost's rho*v / rho, which the FP64 path
-// divides out), 1/(r + tiny), RXM2/T and 1/V(1) do not depend on the recurrence, so one step
-// of the chain is p_j = p_{j-1} + |dr * rho_{j-1} * (..)^2| * 1/(r + tiny), rho_j = p_j * RXM2/T.
+// BC/BC_Outlet.F90:37-107, mixed path: one warp per outlet line.  The radial-equilibrium
+// recurrence along j,
+//     p_j = p_{j-1} + |dr_j * rho_{j-1} * (w_{j-1} cos - sin v_{j-1} + omega r)^2| / (r_j + tiny),
+//     rho_j = p_j * RXM2 / T_j,
+// has coefficients that depend only on interior values (the previous j's velocities enter as
+// V(3:4)/V(1) of its interior cell, equal to the ghost's rho*v / rho), so the lanes load and
+// prepare 32 entries at a time in parallel and only the multiply-add chain runs lane by lane
+// (through shuffles); the ghost writes are again parallel.
 // ---------------------------------------------------------------------------------------
 __global__ void k_bc_outlet_mixed(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent,
                                   const OutletLine* __restrict__ lines, int nl, const CaseDev* __restrict__ cdev) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nl) return;
-    const OutletLine Ln = lines[q];
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nl) return;                                   // whole warps leave together
+    const OutletLine Ln = lines[w];
     const DevBlock b = blks[Ln.blk];
     const Params& p = cdev[b.cs].p;
     const int turb = cdev[b.cs].turb;
-    double* V[7];
-    for (int m = 0; m < 7; ++m) V[m] = slot(b, S_V + m);
+    double* V0 = slot(b, S_V);
     double* PP = slot(b, S_PP);
     double* T = slot(b, S_T);
     double* Rm = slot(b, S_RMIU);
     const double* rad = slot(b, S_RAD);
     const double* sint = slot(b, S_SINT);
     const double* cost = slot(b, S_COST);
-    double pp_prev = 0.0, den_prev = 1.0, vy_prev = 0.0, vz_prev = 0.0;
-    for (int e = Ln.first; e < Ln.first + Ln.n; ++e) {
-        const BCEntry E = ent[e];
-        const int s0 = E.s[0], l0 = E.l[0];
-        const double Tl = T[s0];
-        const double rv1 = 1.0 / V[0][s0];
-        const double vy = V[2][s0] * rv1, vz = V[3][s0] * rv1;
-        double pp;
-        if (E.sub == 1) {                              // j == Jbgn
-            pp = p.Pouthub;
-        } else {
-            const int lm = l0 - b.PI;                   // (il, jl-1, kl)
-            const double rcs1 = rad[l0], rcs2 = rad[lm];
-            const double RoVr2 = sq(vz_prev * cost[lm] - sint[lm] * vy_prev + p.omega0 * rcs2);
-            pp = pp_prev + fabs((rcs1 - rcs2) * den_prev * RoVr2) * (1.0 / (rcs2 + p.Tiny));
+    double pp_carry = 0.0, den_carry = 1.0, vy_carry = 0.0, vz_carry = 0.0;
+    for (int j0 = 0; j0 < Ln.n; j0 += 32) {
+        const int e = Ln.first + j0 + lane;
+        const bool act = j0 + lane < Ln.n;
+        BCEntry E;
+        double Tl = 1.0, rv1 = 0.0, vy = 0.0, vz = 0.0, a = 0.0, k1 = 0.0;
+        bool first = false;
+        if (act) {
+            E = ent[e];
+            Tl = T[E.s[0]];
+            rv1 = 1.0 / V0[E.s[0]];
+            vy = slot(b, S_V + 2)[E.s[0]] * rv1;
+            vz = slot(b, S_V + 3)[E.s[0]] * rv1;
+            k1 = p.RXM2 / Tl;
+            first = E.sub == 1;
         }
-        const double den = pp * (p.RXM2 / Tl);
+        // velocities of the previous entry (lane - 1, or the previous chunk's last)
+        double vy_p = __shfl_up_sync(0xffffffffu, vy, 1), vz_p = __shfl_up_sync(0xffffffffu, vz, 1);
+        if (lane == 0) { vy_p = vy_carry; vz_p = vz_carry; }
+        if (act && !first) {
+            const int lm = E.l[0] - b.PI;              // (il, jl-1, kl)
+            const double rcs1 = rad[E.l[0]], rcs2 = rad[lm];
+            const double RoVr2 = sq(vz_p * cost[lm] - sint[lm] * vy_p + p.omega0 * rcs2);
+            a = fabs((rcs1 - rcs2) * RoVr2) * (1.0 / (rcs2 + p.Tiny));
+        }
+        // the chain, lane by lane
+        double pp = 0.0, den = 0.0, pp_c = pp_carry, den_c = den_carry;
+        for (int i = 0; i < 32; ++i) {
+            const double ai = __shfl_sync(0xffffffffu, a, i), ki = __shfl_sync(0xffffffffu, k1, i);
+            const int fi = __shfl_sync(0xffffffffu, first ? 1 : 0, i);
+            const double ppi = fi ? p.Pouthub : pp_c + ai * den_c;
+            const double deni = ppi * ki;
+            if (lane == i) { pp = ppi; den = deni; }
+            if (j0 + i < Ln.n) { pp_c = ppi; den_c = deni; }
+        }
+        pp_carry = pp_c; den_carry = den_c;
+        vy_carry = __shfl_sync(0xffffffffu, vy, 31);
+        vz_carry = __shfl_sync(0xffffffffu, vz, 31);
+        if (Ln.n - j0 < 32) {                          // a partial chunk: its last entry's values
+            const int last = Ln.n - j0 - 1;
+            vy_carry = __shfl_sync(0xffffffffu, vy, last);
+            vz_carry = __shfl_sync(0xffffffffu, vz, last);
+        }
+        if (!act) continue;
+        const int s0 = E.s[0];
         const double den_ratio = den * rv1;
-        const double v2 = V[1][s0] * den_ratio, v3 = V[2][s0] * den_ratio, v4 = V[3][s0] * den_ratio;
-        T[l0] = Tl;
-        PP[l0] = pp;
-        V[0][l0] = den; V[1][l0] = v2; V[2][l0] = v3; V[3][l0] = v4;
-        for (int L = 1; L < 3; ++L) {
+        const double v2 = slot(b, S_V + 1)[s0] * den_ratio, v3 = slot(b, S_V + 2)[s0] * den_ratio;
+        const double v4 = slot(b, S_V + 3)[s0] * den_ratio;
+        for (int L = 0; L < 3; ++L) {
             const int ig = E.l[L];
-            V[0][ig] = den; V[1][ig] = v2; V[2][ig] = v3; V[3][ig] = v4;
+            V0[ig] = den; slot(b, S_V + 1)[ig] = v2; slot(b, S_V + 2)[ig] = v3; slot(b, S_V + 3)[ig] = v4;
             PP[ig] = pp;
             T[ig] = Tl;
         }
         if (turb) {
-            const double k6 = V[5][s0], k7 = V[6][s0], rm = Rm[s0];
-            V[5][l0] = k6; V[6][l0] = k7; Rm[l0] = rm;
-            for (int L = 1; L < 3; ++L) {
+            const double k6 = slot(b, S_V + 5)[s0], k7 = slot(b, S_V + 6)[s0], rm = Rm[s0];
+            for (int L = 0; L < 3; ++L) {
                 const int ig = E.l[L];
-                V[5][ig] = k6; V[6][ig] = k7; Rm[ig] = rm;
+                slot(b, S_V + 5)[ig] = k6; slot(b, S_V + 6)[ig] = k7; Rm[ig] = rm;
             }
         }
-        pp_prev = pp; den_prev = den; vy_prev = vy; vz_prev = vz;
     }
 }
 
