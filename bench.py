@@ -35,6 +35,40 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
 
 
+def init_replicas():
+    """One process per GPU (torchrun sets RANK / WORLD_SIZE / LOCAL_RANK): every rank runs an
+    independent replica of the workload -- the path does not shard, blocks of one case are
+    coupled every sub-iteration -- and the ranks only meet for the barrier and the maximum of
+    the timings.  NCCL between GPUs, gloo where no GPU is present."""
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    return rank, world
+
+
+def max_over_ranks(x, world):
+    """The maximum of x over the ranks (the slowest replica sets the time)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank, seconds, world):
+    """Whole-job rate in millions of units per second: every rank processed units_per_rank."""
+    return units_per_rank * world / seconds / 1e6
+
+
 def make_case(name, precision, nk=64):
     prec = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
     if name == "channel":
@@ -392,13 +426,7 @@ def main():
         return reference_arm(args)
     if args.case == "cascade" and not hasattr(cases, "cascade"):
         args.case = "channel"
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    import torch
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    rank, world = init_replicas()
     c, conns, geo, st = make_case(args.case, args.precision, args.nk)
     ncell = interior_cells(c)
     nsub = sub_iterations(c)
@@ -417,20 +445,18 @@ def main():
     clk = ClockSampler()
     clk.start()
     if world > 1:
-        torch.distributed.barrier()
+        import torch.distributed as dist
+        dist.barrier()
     ms = time_resident(s, ki, args.steps)
     ki += args.steps
     launches = lib.trans_kernel_launches(s.ctx) - launches0
     clocks = clk.stop()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ncell * nsub * args.steps / (ms * 1e-3) / 1e6 * world
+    ms = max_over_ranks(ms, world)
+    value = replica_rate(ncell * nsub * args.steps, ms * 1e-3, world)
     # end-to-end through the C ABI with pinned host buffers
     e2e_steps = max(2, min(args.steps, 10))
     dt, h2d, d2h = run_e2e(s, c, st, ki, e2e_steps)
-    e2e = ncell * nsub * e2e_steps / dt / 1e6 * world
+    e2e = replica_rate(ncell * nsub * e2e_steps, max_over_ranks(dt, world), world)
     # roofline of the dominant kernel, from per-launch CUDA events of one more iteration
     kt = kernel_times(s, ki)
     ki += 1
@@ -497,7 +523,8 @@ def main():
         print(json.dumps(line))
     s.close()
     if world > 1:
-        torch.distributed.destroy_process_group()
+        import torch.distributed as dist
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":
