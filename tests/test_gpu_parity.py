@@ -228,13 +228,13 @@ def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
     from trans_gb300.solver import Solver
     out = {}
     modes = ("planes", "planes_unchained", "coop", "flow", "tiles", "tiles_4x2x3", "planes_wpc", "planes_unchained_wpc",
-             "coop_wpc", "tiles_4x2x3_wpc", "planes_pf2", "planes_wpc_pf1", "planes_ppt", "planes_unchained_ppt_pf2", "auto")
+             "coop_wpc", "tiles_4x2x3_wpc", "planes_pf2", "planes_wpc_pf1", "auto")
     for mode in modes:
         parts = mode.split("_")
         monkeypatch.setenv("TRANS_SWEEP", parts[0])
         monkeypatch.setenv("TRANS_PDL", "0" if "unchained" in parts else "1")
         monkeypatch.setenv("TRANS_TILE", next((x for x in parts if "x" in x), "8x8x8"))
-        monkeypatch.setenv("TRANS_SWEEP_MAP", "wpc" if "wpc" in parts else "ppt" if "ppt" in parts else "lane")
+        monkeypatch.setenv("TRANS_SWEEP_MAP", "wpc" if "wpc" in parts else "lane")
         monkeypatch.setenv("TRANS_SWEEP_PF", next((x[2:] for x in parts if x.startswith("pf")), "0"))
         c, conns, geo, st = small_cascade(Kind_Spatial=3, Kind_Roe=3)
         c.params.precision = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64

@@ -187,7 +187,7 @@ const char* trans_tuning(void* ctx) {
     out = "sweep=" + std::string(c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : c->sweep_mode == 2 ? "flow " : "tiles ")
                                                       + tiles + std::to_string(c->sweep_grid) + "x" + std::to_string(c->sweep_block)
                                  : c->sweep_mode == 0 ? (c->pdl ? "planes-chained" : "planes") : "untuned")
-          + (c->sweep_wpc == SWEEP_WPC ? "/wpc" : c->sweep_wpc == SWEEP_PPT ? "/ppt" : "") + (c->sweep_pf && c->sweep_mode == 0 ? "/pf" + std::to_string(c->sweep_pf) : "")
+          + (c->sweep_wpc ? "/wpc" : "") + (c->sweep_pf && c->sweep_mode == 0 ? "/pf" + std::to_string(c->sweep_pf) : "")
           + "; measured: " + c->sweep_tuning;
     return out.c_str();
 }

@@ -87,10 +87,8 @@ struct DevBlock {
 constexpr int CELL_TILE = 256;   // interior cells per cell tile (and threads per CTA of the cell kernels)
 constexpr int SWEEP_LANES = 8;   // threads per cell in the LU-SGS sweeps (one per DeltaQ component)
 constexpr int SWEEP_WPC = 16;    // `lanes` bit of the sweep kernels: warp-per-component thread mapping
-constexpr int SWEEP_PPT = 32;    // `lanes` bit: one thread per position, all components (plane launches only)
 // threads a sweep launch needs for n positions
 __host__ __device__ inline int sweep_items(int n, int lanes) {
-    if (lanes & SWEEP_PPT) return n;
     return (lanes & SWEEP_WPC) ? ((n + 31) / 32) * (32 * SWEEP_LANES) : n * SWEEP_LANES;
 }
 

@@ -140,7 +140,6 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     // TRANS_SWEEP_MAP=wpc forces the warp-per-component thread mapping of the sweeps (for tests)
     const char* wm = std::getenv("TRANS_SWEEP_MAP");
     if (wm && std::string(wm) == "wpc") c->sweep_wpc = SWEEP_WPC;
-    if (wm && std::string(wm) == "ppt") c->sweep_wpc = SWEEP_PPT;       // hyperplane launches only
     // TRANS_SWEEP_PF=n forces an L2 prefetch distance of n hyperplanes (for tests)
     const char* pf = std::getenv("TRANS_SWEEP_PF");
     if (pf) c->sweep_pf = std::max(0, std::atoi(pf));

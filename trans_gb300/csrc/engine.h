@@ -117,8 +117,7 @@ struct Ctx {
     int pdl = 1;                         // chain hyperplane launches (programmatic dependent launch)
     int pdl_allowed = 1;                 // chaining may be picked by the tuner (TRANS_PDL=0 forbids it)
     int sweep_exec_pdl = -1;             // chaining the sweep graph was captured with
-    int sweep_wpc = 0;                   // thread mapping: 0 lane-major, SWEEP_WPC warp per component,
-                                         // SWEEP_PPT position per thread (hyperplane launches only)
+    int sweep_wpc = 0;                   // SWEEP_WPC: warp-per-component thread mapping (0: lane-major)
     int sweep_exec_wpc = -1;             // mapping the sweep graph was captured with
     int sweep_pf = 0;                    // L2 prefetch distance of the hyperplane launches (0 = none)
     int sweep_exec_pf = -1;              // prefetch distance the sweep graph was captured with

@@ -50,8 +50,7 @@ void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = chained ? 1 : 0;
-    if (turb & SWEEP_PPT) cudaLaunchKernelEx(&cfg, k_sweep_ppt<TG_R, LOWER>, nbp, rec, dq, first, count, turb, chained, pf_first, pf_count);
-    else cudaLaunchKernelEx(&cfg, k_sweep<TG_R, LOWER>, nbp, rec, dq, n, first, count, turb, chained, pf_first, pf_count);
+    cudaLaunchKernelEx(&cfg, k_sweep<TG_R, LOWER>, nbp, rec, dq, n, first, count, turb, chained, pf_first, pf_count);
 }
 void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count) {
     swp<true>(s, v, first, count, turb, chained, pf_first, pf_count);

@@ -944,15 +944,24 @@ __device__ inline void sweep_map(int g, int lanes, int& e, int& L) {
     else { e = g / SWEEP_LANES; L = g % SWEEP_LANES; }
 }
 
-// This lane's terms of the three neighbours (lower for the L sweep, upper for U) from the
-// position's record: k[d][6] is the spectral radius, k[d][0..5] the Jacobian terms component L
-// multiplies with the neighbour's DeltaQ.
 template <typename R, bool LOWER>
-__device__ __forceinline__ void sweep_terms(const R* __restrict__ rec, long long q, int L, R (&k)[3][7]) {
+__device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
+                                  int L, int turb, bool chained = false, bool hoist = true) {
+    if (L >= 7 || (L >= 5 && turb == 0) || (L < 5 && turb == 2)) {
+        if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+        return;
+    }
     const int side = LOWER ? 0 : 3;
+    const R sgn = LOWER ? R(1.0) : R(-1.0);
     auto REC = [&](int m) { return rec[sw_at(q, m, NREC)]; };
+    // Everything that does not depend on the previous hyperplane first: neighbour positions,
+    // this lane's Jacobian terms and radii, the diagonal.  A missing neighbour (nbp < 0) reads
+    // this cell's own entries instead and its term is replaced by 0 afterwards.
+    long long npv[3];
+    R k[3][7];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
+        npv[d] = nbp[sw_at(q, side + d, 6)];
         const int jd = NBREC * (side + d);
         k[d][6] = REC(jd + NJAC);                                   // spectral radius
         if (L == 0) {
@@ -967,22 +976,38 @@ __device__ __forceinline__ void sweep_terms(const R* __restrict__ rec, long long
             k[d][0] = REC(jd + JC_VPT);
         }
     }
-}
-
-// New DeltaQ of component L at one position from its neighbours' terms k, their DeltaQ (nq:
-// components 0..4; ntL: component L for a k or omega lane), which neighbours exist, the
-// position's own right-hand side and diagonal terms (Time/TIME_LUSGS.F90:172-675,
-// Time/TURBTWO_TIME_LUSGS_SST.F90:562-766).  Every thread mapping calls this one function.
-template <typename R, bool LOWER>
-__device__ __forceinline__ R sweep_value(int L, const R (&k)[3][7], const R (&nq)[3][5], const R (&ntL)[3],
-                                         const bool (&has)[3], R own, R stept, R cvs, R den) {
-    const R sgn = LOWER ? R(1.0) : R(-1.0);
+    const R stept = REC(REC_STEPT), cvs = REC(REC_CVS);
+    const R den = L < 5 ? REC(REC_FM) : REC(REC_FT);
+    // one launch per hyperplane chained with programmatic dependent launch: wait for the
+    // previous hyperplane to complete, then let the next one start its loads
+    if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+    // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1
+    // line).  Every lane loads in converged code, before the per-component branches, so that a
+    // warp waits for one dependent L2 round trip instead of one per divergent branch.
+    // (A warp of the warp-per-component mapping takes one branch: it loads inside it.)
+    R nq[3][5], nt[3];
+    if (hoist) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const long long np = npv[d] >= 0 ? npv[d] : q;
+#pragma unroll
+            for (int m = 0; m < 5; ++m) nq[d][m] = __ldcg(dq + sw_at(np, m, DQ_STRIDE));
+            nt[d] = __ldcg(dq + sw_at(np, L < 5 ? 0 : L, DQ_STRIDE));
+        }
+    }
+    R* D = dq + sw_at(q, L, DQ_STRIDE);
+    const R own = __ldcg(D);
     R acc[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
+        const bool has = npv[d] >= 0;
+        const long long np = has ? npv[d] : q;
         const R RDSt = k[d][6];
         R val;
         if (L < 5) {
+            if (!hoist)
+#pragma unroll
+                for (int m = 0; m < 5; ++m) nq[d][m] = __ldcg(dq + sw_at(np, m, DQ_STRIDE));
             const R AinRo = nq[d][0], AinRx = nq[d][1], AinRy = nq[d][2], AinRz = nq[d][3], AinRe = nq[d][4];
             R Dif;
             if (L == 0) {
@@ -997,102 +1022,14 @@ __device__ __forceinline__ R sweep_value(int L, const R (&k)[3][7], const R (&nq
             val = R(0.5) * (Dif + sgn * (RDSt * Din));
         } else {
             const R VP = k[d][0];
-            const R Dq = ntL[d];
+            const R Dq = hoist ? nt[d] : __ldcg(dq + sw_at(np, L, DQ_STRIDE));
             val = R(0.5) * (Dq * VP + sgn * (RDSt * Dq));
         }
-        acc[d] = has[d] ? val : R(0.0);
+        acc[d] = has ? val : R(0.0);
     }
     const R sum = acc[0] + acc[1] + acc[2];
-    if (LOWER) return (own * stept + sum * cvs) / den;
-    return own - sum * cvs / den;
-}
-
-// One (position, component) item of a sweep.
-template <typename R, bool LOWER>
-__device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
-                                  int L, int turb, bool chained = false, bool hoist = true) {
-    if (L >= 7 || (L >= 5 && turb == 0) || (L < 5 && turb == 2)) {
-        if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
-        return;
-    }
-    const int side = LOWER ? 0 : 3;
-    // Everything that does not depend on the previous hyperplane first: neighbour positions,
-    // this lane's Jacobian terms and radii, the diagonal.  A missing neighbour (nbp < 0) reads
-    // this cell's own entries instead and its term is replaced by 0 afterwards.
-    long long npv[3];
-    bool has[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        npv[d] = nbp[sw_at(q, side + d, 6)];
-        has[d] = npv[d] >= 0;
-    }
-    R k[3][7];
-    sweep_terms<R, LOWER>(rec, q, L, k);
-    const R stept = rec[sw_at(q, REC_STEPT, NREC)], cvs = rec[sw_at(q, REC_CVS, NREC)];
-    const R den = L < 5 ? rec[sw_at(q, REC_FM, NREC)] : rec[sw_at(q, REC_FT, NREC)];
-    // one launch per hyperplane chained with programmatic dependent launch: wait for the
-    // previous hyperplane to complete, then let the next one start its loads
-    if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
-    // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1
-    // line).  In the lane-major mapping every lane loads in converged code, before the
-    // per-component branches, so that a warp waits for one dependent L2 round trip instead of
-    // one per divergent branch; a warp of the warp-per-component mapping takes one branch and
-    // loads only what it needs.
-    R nq[3][5], nt[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const long long np = has[d] ? npv[d] : q;
-        if (hoist || L < 5)
-#pragma unroll
-            for (int m = 0; m < 5; ++m) nq[d][m] = __ldcg(dq + sw_at(np, m, DQ_STRIDE));
-        if (hoist || L >= 5) nt[d] = __ldcg(dq + sw_at(np, L < 5 ? 0 : L, DQ_STRIDE));
-    }
-    R* D = dq + sw_at(q, L, DQ_STRIDE);
-    const R own = __ldcg(D);
-    *D = sweep_value<R, LOWER>(L, k, nq, nt, has, own, stept, cvs, den);
-}
-
-// One position, all its components, in one thread (the position-per-thread mapping): the
-// records' terms of all components are loaded before the wait, the seven DeltaQ of each
-// neighbour after it, then every component goes through sweep_value.
-template <typename R, bool LOWER>
-__device__ inline void sweep_pos(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long q, int turb,
-                                 bool chained) {
-    const int side = LOWER ? 0 : 3;
-    const int Lo = turb == 2 ? 5 : 0, Hi = turb == 0 ? 5 : 7;
-    long long npv[3];
-    bool has[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        npv[d] = nbp[sw_at(q, side + d, 6)];
-        has[d] = npv[d] >= 0;
-    }
-    R kall[7][3][7];
-#pragma unroll
-    for (int L = 0; L < 7; ++L)
-        if (L >= Lo && L < Hi) sweep_terms<R, LOWER>(rec, q, L, kall[L]);
-    const R stept = rec[sw_at(q, REC_STEPT, NREC)], cvs = rec[sw_at(q, REC_CVS, NREC)];
-    const R fm = rec[sw_at(q, REC_FM, NREC)], ft = rec[sw_at(q, REC_FT, NREC)];
-    if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
-    R nq[3][5], n7[3][2];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const long long np = has[d] ? npv[d] : q;
-#pragma unroll
-        for (int m = 0; m < 5; ++m) nq[d][m] = __ldcg(dq + sw_at(np, m, DQ_STRIDE));
-        n7[d][0] = __ldcg(dq + sw_at(np, 5, DQ_STRIDE));
-        n7[d][1] = __ldcg(dq + sw_at(np, 6, DQ_STRIDE));
-    }
-    R own[7];
-#pragma unroll
-    for (int L = 0; L < 7; ++L) own[L] = __ldcg(dq + sw_at(q, L, DQ_STRIDE));
-#pragma unroll
-    for (int L = 0; L < 7; ++L) {
-        if (L < Lo || L >= Hi) continue;
-        R ntL[3];
-        for (int d = 0; d < 3; ++d) ntL[d] = L < 5 ? nq[d][0] : n7[d][L - 5];
-        dq[sw_at(q, L, DQ_STRIDE)] = sweep_value<R, LOWER>(L, kall[L], nq, ntL, has, own[L], stept, cvs, L < 5 ? fm : ft);
-    }
+    if (LOWER) *D = (own * stept + sum * cvs) / den;
+    else *D = own - sum * cvs / den;
 }
 
 // one hyperplane [first, first+count) per launch (chained: launched with programmatic
@@ -1122,23 +1059,6 @@ __global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, 
         return;
     }
     sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, chained != 0, !(lanes & SWEEP_WPC));
-}
-
-// the same hyperplane with one thread per position (all components in the thread)
-template <typename R, bool LOWER>
-__global__ void k_sweep_ppt(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, int first, int count, int lanes,
-                            int chained, int pf_first, int pf_count) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pf_count > 0) {
-        const size_t T = (size_t)gridDim.x * blockDim.x;
-        prefetch_l2_range(rec + sw_at(pf_first, 0, NREC), (size_t)pf_count * NREC * sizeof(R), g, T);
-        prefetch_l2_range(nbp + sw_at(pf_first, 0, 6), (size_t)pf_count * 6 * sizeof(int), g, T);
-    }
-    if (g >= count) {
-        if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
-        return;
-    }
-    sweep_pos<R, LOWER>(nbp, rec, dq, (long long)first + g, lanes & 3, chained != 0);
 }
 
 // Grid-wide barrier of a co-resident (cooperative) grid.  The wait is bounded: after `limit`

@@ -226,8 +226,7 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
 namespace {
 
 int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
-    // the position-per-thread mapping exists for the hyperplane launches only
-    const int lanes = c->sweep_lanes | (mode == 0 ? c->sweep_wpc : (c->sweep_wpc & SWEEP_WPC));
+    const int lanes = c->sweep_lanes | c->sweep_wpc;
     if (mode == 0 && c->sweep_exec &&
         (c->sweep_exec_pdl != c->pdl || c->sweep_exec_wpc != c->sweep_wpc || c->sweep_exec_pf != c->sweep_pf)) {   // changed
         cudaGraphExecDestroy(c->sweep_exec);
@@ -319,10 +318,6 @@ int tune_sweeps(Ctx* c) {
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     struct Cand { int mode, grid, block, pdl, ti, tj, tk, wpc, pf; };
     std::vector<Cand> cands;
-    for (int pf : {0, 2}) {                      // position per thread: hyperplane launches only
-        cands.push_back({0, 0, 0, 1, 0, 0, 0, SWEEP_PPT, pf});
-        cands.push_back({0, 0, 0, 0, 0, 0, 0, SWEEP_PPT, pf});
-    }
     for (int wpc : {0, SWEEP_WPC}) {
         for (int pf : {0, 1, 2, 4}) {             // prefetch distance (hyperplanes) of the plane launches
             cands.push_back({0, 0, 0, 1, 0, 0, 0, wpc, pf});
@@ -370,8 +365,7 @@ int tune_sweeps(Ctx* c) {
                                                                       + std::to_string(k.tk) + "/" : std::string())
                                                  + std::to_string(k.grid) + "x" + std::to_string(k.block)
                                            : std::string(c->pdl ? "planes-chained" : "planes"))
-                                   + (k.wpc == SWEEP_WPC ? "/wpc" : k.wpc == SWEEP_PPT ? "/ppt" : "")
-                                   + (k.pf ? "/pf" + std::to_string(k.pf) : "")
+                                   + (k.wpc ? "/wpc" : "") + (k.pf ? "/pf" + std::to_string(k.pf) : "")
                                    + ":" + std::to_string(ms) + "ms ";
                 if (ms < best) { best = ms; pick = k; }
             }
