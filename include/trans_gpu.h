@@ -103,6 +103,22 @@ typedef struct trans_norms {
 } trans_norms;
 
 /*
+ * Integrated quantities of one case's current state (trans_get_integrals), summed on the device
+ * over every face of its inlet (kind 5), outlet (kind 7) and wall (kind 1) segments.  Mass flow
+ * and momentum follow Output/OUTPUT_Residual_NS.F90:37-75 (face value = volume-weighted average
+ * of the two cells with the weights crossed, dotted with SD of the face); total pressure
+ * p (1 + 0.2 M^2)^3.5 follows Output/Average_Field.F90:66,157; the wall forces follow
+ * Output/OUTPUT_ClCdCm.F90:114-264 before its 2/Area_Ref scaling.  Nondimensional units.
+ */
+typedef struct trans_integrals {
+    double mass_in, p0_in, p_in;     /* inlet faces: mass flow into the domain; mass-averaged p0 and p */
+    double mass_out, p0_out, p_out;  /* outlet faces: mass flow out of the domain; mass-averaged p0 and p */
+    double loss;                     /* (p0_in - p0_out) / (p0_in - p_in); 0 when p0_in == p_in */
+    double force_p[3];               /* wall faces: sum of (PP - PPF) SD Sgn, Sgn = -1 on min faces   */
+    double force_v[3];               /* wall faces: sum of mu_w/(Dst Ref) (u |S| - (u.S) S/|S|)       */
+} trans_integrals;
+
+/*
  * Field ids for trans_set_field / trans_get_field, with the Fortran allocation each pointer
  * must have (Input/Read_BlockDimensions.F90:306-478; NIp2 = NI+2):
  */
@@ -186,6 +202,13 @@ double trans_probe_chain_us(int chained, int grid);
  * norms as for trans_iterate (last iteration).  No reference counterpart: benchmarking. */
 int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norms* norms);
 int trans_sync(void* ctx);
+/* Integrated quantities of the current state (after the last iteration's update; ghost cells
+ * as the last boundary pass left them, as the reference's output routines see them). */
+int trans_get_integrals(void* ctx, trans_integrals* out);
+/* Pressure coefficient 2 (PP - PPF) of the wall cells of wall segment iconn (1-based, a kind-1
+ * connection) of block ib (Output/OUTPUT_Surfaces.F90:303-305): one value per face of the
+ * segment, I fastest, then J, then K, over pointStart..pointEnd of the segment's face indices. */
+int trans_get_wall_cp(void* ctx, int ib, int iconn, double* cp);
 /* Device bytes held by the context. */
 long long trans_device_bytes(void* ctx);
 /* Kernel launches issued since the context was created (all kernels of this library). */
@@ -218,6 +241,12 @@ int trans_batch_time_iterations(void* ctx, int n, double* ms);
  * (arrays of nblocks entries, either may be NULL). */
 int trans_batch_case_norms(void* ctx, int case_id, int* iterations, trans_norms* first, trans_norms* last);
 long long trans_batch_bytes_in_use(void* ctx);
+/* As trans_get_integrals / trans_get_wall_cp for one case; one launch covers all cases, so a
+ * serving loop reads every case's integrals at once with trans_batch_integrals (ids[k] and
+ * out[k] for the first n cases in trans_batch_cases order; returns the number written). */
+int trans_batch_get_integrals(void* ctx, int case_id, trans_integrals* out);
+int trans_batch_integrals(void* ctx, int* ids, trans_integrals* out, int n);
+int trans_batch_get_wall_cp(void* ctx, int case_id, int ib, int iconn, double* cp);
 /* Number of cases; their ids in ids[0..max-1]. */
 int trans_batch_cases(void* ctx, int* ids, int max);
 

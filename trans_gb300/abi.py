@@ -86,6 +86,19 @@ class TransNorms(C.Structure):
     ]
 
 
+class TransIntegrals(C.Structure):
+    _fields_ = [
+        ("mass_in", C.c_double), ("p0_in", C.c_double), ("p_in", C.c_double),
+        ("mass_out", C.c_double), ("p0_out", C.c_double), ("p_out", C.c_double),
+        ("loss", C.c_double), ("force_p", C.c_double * 3), ("force_v", C.c_double * 3),
+    ]
+
+    def as_dict(self):
+        return {"mass_in": self.mass_in, "p0_in": self.p0_in, "p_in": self.p_in,
+                "mass_out": self.mass_out, "p0_out": self.p0_out, "p_out": self.p_out,
+                "loss": self.loss, "force_p": list(self.force_p), "force_v": list(self.force_v)}
+
+
 # field ids (enum trans_field)
 FIELDS = ["V", "PP", "T", "RMIU", "WT0", "WT1", "SD", "GRAD", "VOL", "ALAGM", "DST", "ALENG",
           "ASENG", "XC", "YC", "ZC", "RAD", "THTC", "D", "RDS", "DTM", "DQDXYZ", "SHOCK", "WT2"]
@@ -153,6 +166,11 @@ def bind_common(lib):
     lib.trans_batch_cases.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
     lib.trans_prepare.argtypes = [vp, C.c_int]
     lib.trans_batch_time_iterations.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+    lib.trans_get_integrals.argtypes = [vp, C.POINTER(TransIntegrals)]
+    lib.trans_get_wall_cp.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    lib.trans_batch_get_integrals.argtypes = [vp, C.c_int, C.POINTER(TransIntegrals)]
+    lib.trans_batch_integrals.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(TransIntegrals), C.c_int]
+    lib.trans_batch_get_wall_cp.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
     lib.trans_tuning.argtypes = [vp]
     lib.trans_tuning.restype = C.c_char_p
     lib.trans_last_error.argtypes = [vp]
@@ -167,5 +185,6 @@ EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field
             "trans_kernel_class", "trans_batch_create", "trans_batch_case_bytes", "trans_batch_add",
             "trans_batch_remove", "trans_batch_set_field", "trans_batch_get_field", "trans_batch_iterate",
             "trans_batch_case_norms", "trans_batch_bytes_in_use", "trans_batch_cases", "trans_prepare",
-            "trans_batch_time_iterations"]
+            "trans_batch_time_iterations", "trans_get_integrals", "trans_get_wall_cp",
+            "trans_batch_get_integrals", "trans_batch_integrals", "trans_batch_get_wall_cp"]
 TRANS_NKCLASS = 16

@@ -23,6 +23,7 @@ UNITS = {
     "noalloc.cu": ["-fmad=false"],
     "batch.cu": ["-fmad=false"],
     "k_fp64.cu": ["-fmad=false"],
+    "k_integrals.cu": ["-fmad=false"],
     "k_mixed.cu": ["-fmad=true"],
 }
 

@@ -141,6 +141,16 @@ int trans_get_norms(void* ctx, trans_norms* norms) {
     return TRANS_OK;
 }
 
+int trans_get_integrals(void* ctx, trans_integrals* out) {
+    Ctx* c = as_ctx(ctx);
+    return c ? integrals(c, first_case(c), out) : TRANS_E_ARG;
+}
+
+int trans_get_wall_cp(void* ctx, int ib, int iconn, double* cp) {
+    Ctx* c = as_ctx(ctx);
+    return c ? wall_cp(c, first_case(c), ib, iconn, cp) : TRANS_E_ARG;
+}
+
 int trans_sync(void* ctx) {
     Ctx* c = as_ctx(ctx);
     if (!c) return TRANS_E_ARG;

@@ -98,6 +98,34 @@ long long trans_batch_bytes_in_use(void* ctx) {
     return c ? c->in_use : 0;
 }
 
+int trans_batch_get_integrals(void* ctx, int case_id, trans_integrals* out) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return TRANS_E_ARG;
+    CaseRec* cs = case_find(c, case_id);
+    if (!cs) return fail(c, TRANS_E_ARG, "no such case");
+    return integrals(c, cs, out);
+}
+
+int trans_batch_integrals(void* ctx, int* ids, trans_integrals* out, int n) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || n < 0 || (n > 0 && (!ids || !out))) return TRANS_E_ARG;
+    if (c->cases.empty() || n == 0) return 0;
+    std::vector<trans_integrals> all;
+    int rc = all_integrals(c, all);
+    if (rc) return rc;
+    int m = std::min(n, (int)all.size());
+    for (int q = 0; q < m; ++q) { ids[q] = c->cases[q]->id; out[q] = all[q]; }
+    return m;
+}
+
+int trans_batch_get_wall_cp(void* ctx, int case_id, int ib, int iconn, double* cp) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return TRANS_E_ARG;
+    CaseRec* cs = case_find(c, case_id);
+    if (!cs) return fail(c, TRANS_E_ARG, "no such case");
+    return wall_cp(c, cs, ib, iconn, cp);
+}
+
 int trans_batch_cases(void* ctx, int* ids, int max) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c) return TRANS_E_ARG;

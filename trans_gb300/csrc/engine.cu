@@ -172,7 +172,7 @@ void free_worklists(Ctx* c) {
     dfree(c->d_bc); dfree(c->d_outlet); dfree(c->d_lines); dfree(c->d_sweep); dfree(c->d_plane_off);
     dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq_save); dfree(c->d_parts);
     dfree(c->d_cdev); dfree(c->d_stage); dfree(c->d_tile_first); dfree(c->d_norms);
-    dfree(c->d_tiles); dfree(c->d_tflags); dfree(c->d_qpos);
+    dfree(c->d_tiles); dfree(c->d_tflags); dfree(c->d_qpos); dfree(c->d_bc_first); dfree(c->d_intg);
     c->tv = TileView{};
     c->tile_shape[0] = c->tile_shape[1] = c->tile_shape[2] = 0;
     if (c->h_norms) { cudaFreeHost(c->h_norms); c->h_norms = nullptr; }

@@ -72,6 +72,9 @@ struct Ctx {
     std::vector<BCEntry> bc, outlet;
     std::vector<OutletLine> lines;
     BCEntry *d_bc = nullptr, *d_outlet = nullptr;
+    std::vector<int> bc_first;           // entries of case k in bc: [bc_first[k], bc_first[k+1])
+    int* d_bc_first = nullptr;
+    double* d_intg = nullptr;            // NINTG integrated-quantity sums per case
     OutletLine* d_lines = nullptr;
     std::vector<SweepCell> sweep;
     std::vector<int> plane_off;          // sweep positions of hyperplane h: [plane_off[h], plane_off[h+1])
@@ -164,6 +167,10 @@ void free_worklists(Ctx* c);
 int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload);
 int run_stage(Ctx* c, int stage, int itr);
 int upload_cdev(Ctx* c);
+// integrated quantities of one case from its current state (k_integrals.cu kernels)
+int integrals(Ctx* c, CaseRec* cs, trans_integrals* out);
+int all_integrals(Ctx* c, std::vector<trans_integrals>& out);     // every case, in c->cases order
+int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp);
 int finalize_geometry(Ctx* c);
 int reduce_norms(Ctx* c);
 int run_iteration(Ctx* c);               // one outer iteration of every case at its KI

@@ -482,8 +482,11 @@ __global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __re
 //   Space/CONVECT_MUSCL.F90 | Space/CONVECT_MDCD.F90, Space/TURBTWO_CONVECT_MUSCL.F90,
 //   Space/CONVECT_Roe_Original.F90 | Space/CONVECT_AUSMPW_Plus.F90, Space/TURBTWO_CONVECT_Upwind.F90
 // ---------------------------------------------------------------------------------------
+#ifndef TG_FACE_MINB
+#define TG_FACE_MINB 5      // resident CTAs per SM asked of the FP32 face-flux kernels (96 registers)
+#endif
 template <typename R, int DIR>
-__global__ void __launch_bounds__(128) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
                                                           const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;

@@ -40,6 +40,12 @@ void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, 
 double probe_fma_gflops(int fp64);
 double probe_chain_us(int chained, int grid);   // floor of one dependent sweep step (k_mixed.cu)
 void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);
+// integrated quantities (k_integrals.cu): NINTG sums per case, Cp of one wall segment
+constexpr int NINTG = 12;    // inlet m, m p0, m p | outlet m, m p0, m p | pressure force xyz | viscous force xyz
+void launch_integrals(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const int* first, int ncase,
+                      const CaseDev* cdev, double* out);
+void launch_wall_cp(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int e0, int n, const CaseDev* cdev,
+                    double* cp);
 
 // flux, source and sweep kernels, instantiated per arithmetic type
 struct FluxLaunchers {

@@ -684,5 +684,77 @@ int kernel_times(Ctx* c, double* ms, int* launches) {
     return rc;
 }
 
+
+// ---- integrated quantities (trans_get_integrals, trans_get_wall_cp) ----
+int all_integrals(Ctx* c, std::vector<trans_integrals>& out) {
+    if (c->cases.empty()) return fail(c, TRANS_E_ARG, "no case");
+    int rc;
+    if (!c->built && (rc = rebuild(c))) return rc;
+    if ((rc = upload_cdev(c))) return rc;
+    const int nc = (int)c->cases.size();
+    launch_integrals(c->stream, c->d_blk, c->d_bc, c->d_bc_first, nc, c->d_cdev, c->d_intg);
+    c->launches++;
+    CK(cudaGetLastError());
+    std::vector<double> h((size_t)NINTG * nc);
+    CK(cudaMemcpyAsync(h.data(), c->d_intg, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    out.assign(nc, trans_integrals{});
+    for (int k = 0; k < nc; ++k) {
+        const double* q = &h[(size_t)NINTG * k];
+        trans_integrals& r = out[k];
+        r.mass_in = q[0];
+        r.p0_in = q[0] != 0.0 ? q[1] / q[0] : 0.0;
+        r.p_in = q[0] != 0.0 ? q[2] / q[0] : 0.0;
+        r.mass_out = q[3];
+        r.p0_out = q[3] != 0.0 ? q[4] / q[3] : 0.0;
+        r.p_out = q[3] != 0.0 ? q[5] / q[3] : 0.0;
+        r.loss = r.p0_in != r.p_in ? (r.p0_in - r.p0_out) / (r.p0_in - r.p_in) : 0.0;
+        for (int d = 0; d < 3; ++d) { r.force_p[d] = q[6 + d]; r.force_v[d] = q[9 + d]; }
+    }
+    return TRANS_OK;
+}
+
+int integrals(Ctx* c, CaseRec* cs, trans_integrals* out) {
+    if (!c || !cs || !out) return TRANS_E_ARG;
+    std::vector<trans_integrals> all;
+    int rc = all_integrals(c, all);
+    if (rc) return rc;
+    for (size_t k = 0; k < c->cases.size(); ++k)
+        if (c->cases[k] == cs) { *out = all[k]; return TRANS_OK; }
+    return fail(c, TRANS_E_ARG, "case not in the context");
+}
+
+int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp) {
+    if (!c || !cs || !cp) return TRANS_E_ARG;
+    if (ib < 0 || ib >= (int)cs->hb.size()) return fail(c, TRANS_E_ARG, "bad block index");
+    const HostBlock& h = cs->hb[ib];
+    if (iconn < 1 || iconn > (int)h.conn.size()) return fail(c, TRANS_E_ARG, "bad connection index");
+    if (h.conn[iconn - 1].BCType != 1) return fail(c, TRANS_E_ARG, "connection is not a wall (kind 1)");
+    int rc;
+    if (!c->built && (rc = rebuild(c))) return rc;
+    if ((rc = upload_cdev(c))) return rc;
+    // entries of the segment in the context's table: cases, blocks and connections in order
+    size_t k = 0;
+    while (k < c->cases.size() && c->cases[k] != cs) ++k;
+    if (k == c->cases.size()) return fail(c, TRANS_E_ARG, "case not in the context");
+    long long e0 = c->bc_first[k], n = 0;
+    for (int nb = 0; nb <= ib; ++nb)
+        for (int ic = 0; ic < (int)cs->hb[nb].conn.size(); ++ic) {
+            const trans_conn& a = cs->hb[nb].conn[ic];
+            long long cnt = 1;
+            for (int q = 0; q < 3; ++q) cnt *= (long long)(a.pointEnd[q] - a.pointStart[q] + 1);
+            if (nb == ib && ic == iconn - 1) { n = cnt; break; }
+            e0 += cnt;
+        }
+    if (e0 + n > c->bc_first[k + 1]) return fail(c, TRANS_E_ARG, "wall segment outside the boundary table");
+    if (!c->d_stage || c->stage_doubles < (size_t)n) return fail(c, TRANS_E_ARG, "staging buffer too small");
+    launch_wall_cp(c->stream, c->d_blk, c->d_bc, (int)e0, (int)n, c->d_cdev, c->d_stage);
+    c->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(cp, c->d_stage, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return TRANS_OK;
+}
+
 }  // namespace eng
 }  // namespace tg

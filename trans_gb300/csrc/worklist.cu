@@ -154,7 +154,7 @@ int rebuild(Ctx* c) {
     free_worklists(c);
     c->blk.clear(); c->cell_tiles.clear(); c->cell_tile_blk.clear(); c->ghost_tiles.clear();
     for (int d = 0; d < 3; ++d) c->face_tiles[d].clear();
-    c->bc.clear(); c->outlet.clear(); c->lines.clear(); c->sweep.clear(); c->plane_off.clear();
+    c->bc.clear(); c->bc_first.clear(); c->outlet.clear(); c->lines.clear(); c->sweep.clear(); c->plane_off.clear();
     c->cdev_last.clear();
     if (c->cases.empty()) return TRANS_OK;
     // Runge-Kutta cases sweep only k and omega (TURBTWO_TIME_LUSGS_SST; the mean flow is explicit)
@@ -195,8 +195,14 @@ int rebuild(Ctx* c) {
         if ((rc = upload_vec(c, c->face_tiles[d].data(), sizeof(Tile) * c->face_tiles[d].size(), (void**)&c->d_face[d]))) return rc;
     if ((rc = upload_vec(c, c->ghost_tiles.data(), sizeof(Tile) * c->ghost_tiles.size(), (void**)&c->d_ghost))) return rc;
     // boundary tables
-    for (CaseRec* cs : c->cases)
+    c->bc_first.clear();
+    for (CaseRec* cs : c->cases) {
+        c->bc_first.push_back((int)c->bc.size());
         if ((rc = build_bc(c, cs))) return rc;
+    }
+    c->bc_first.push_back((int)c->bc.size());
+    if ((rc = upload_vec(c, c->bc_first.data(), sizeof(int) * c->bc_first.size(), (void**)&c->d_bc_first))) return rc;
+    CK(cudaMalloc(&c->d_intg, sizeof(double) * NINTG * c->cases.size()));
     if ((rc = upload_vec(c, c->bc.data(), sizeof(BCEntry) * c->bc.size(), (void**)&c->d_bc))) return rc;
     if ((rc = upload_vec(c, c->outlet.data(), sizeof(BCEntry) * c->outlet.size(), (void**)&c->d_outlet))) return rc;
     if ((rc = upload_vec(c, c->lines.data(), sizeof(OutletLine) * c->lines.size(), (void**)&c->d_lines))) return rc;

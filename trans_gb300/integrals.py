@@ -1,13 +1,17 @@
 """Integrated quantities of a solution, for the precision error table and for retirement
 decisions: mass flow through every inlet and outlet, mass-averaged total pressure and the
 total-pressure loss coefficient, blade loading (pressure coefficient on the blade wall),
-pressure force on the walls, and field L-inf differences.
+pressure and viscous force on the walls, and field L-inf differences.
 
 Semantics follow the reference's output routines, generalised to every inlet/outlet face:
   mass flow       Output/OUTPUT_Residual_NS.F90:37-75 (face momentum from the two cells'
                   volume-weighted average, dotted with SD of the face; nondimensional units)
   pressure coeff. Output/OUTPUT_Surfaces.F90:303-305 (Cp = 2 (p - PPF) at the wall cell)
-  total pressure  Output/Average_Field.F90:112,210 (p (1 + 0.2 M^2)^3.5, mass averaged)
+  total pressure  Output/Average_Field.F90:66,157 (p (1 + 0.2 M^2)^3.5, mass averaged)
+  wall force      Output/OUTPUT_ClCdCm.F90:114-264 (pressure part (p - PPF) S Sgn, viscous part
+                  mu_w/(Dst Ref) times the tangential velocity times |S|; before 2/Area_Ref)
+This is a host (numpy) evaluation from downloaded fields; the library computes the same sums
+on the device (trans_get_integrals), and the tests hold the two against each other.
 Inputs are the full-extent (-2..N+2) arrays of trans_gb300.solver / oracle get_field.
 """
 import numpy as np
@@ -93,21 +97,59 @@ def wall_cp(case, conns, geo, fields, block_index=0, surf_dir=2, k_index=None):
     return 2.0 * (p - case.params.PPF)
 
 
-def wall_force(case, conns, geo, fields):
-    """Pressure force sum(p_wall * S) over every wall face (kind 1), nondimensional."""
-    F = np.zeros(3)
+def wall_forces(case, conns, geo, fields):
+    """Pressure and viscous force summed over every wall face (kind 1), nondimensional, before
+    the reference's 2/Area_Ref scaling (Output/OUTPUT_ClCdCm.F90:199-248)."""
+    P = case.params
+    Fp, Fv = np.zeros(3), np.zeros(3)
     for ib, b in enumerate(case.blocks):
         g = geo[b.id]
-        PP = fields[ib]["PP"]
+        V, PP, T = fields[ib]["V"], fields[ib]["PP"], fields[ib]["T"]
         for cn in conns[b.id]:
             if cn.BCType != 1:
                 continue
             d, ci, cg, cf, is_min = _face_pairs(cn)
-            p = _at(PP, ci)
-            sgn = -1.0 if is_min else 1.0          # outward normal of the fluid domain
+            Sl = _at(g["GRAD"], cf, d)
+            S = [_at(g["SD"], cf, (d, q)) / Sl for q in range(3)]
+            sgn = -1.0 if is_min else 1.0
+            P2 = _at(PP, ci) - P.PPF
             for q in range(3):
-                F[q] += float(np.sum(sgn * p * _at(g["SD"], cf, (d, q))))
-    return F
+                Fp[q] += float(np.sum(P2 * S[q] * Sl * sgn))
+            TT = _at(T, ci)
+            mu_w = (1.0 + P.Csthlnd) / (TT * P.Csth1 + P.Csthlnd) * (P.Csth1 * TT) ** 1.5
+            den = _at(V, ci, 0)
+            u = [_at(V, ci, q + 1) / den for q in range(3)]
+            vcon = u[0] * S[0] * Sl + u[1] * S[1] * Sl + u[2] * S[2] * Sl
+            tau = 1.0 * mu_w / _at(geo[b.id]["DST"], ci) / P.Ref
+            for q in range(3):
+                Fv[q] += float(np.sum(tau * (u[q] * Sl - vcon * S[q])))
+    return Fp, Fv
+
+
+def wall_force(case, conns, geo, fields):
+    """Total (pressure + viscous) wall force."""
+    Fp, Fv = wall_forces(case, conns, geo, fields)
+    return Fp + Fv
+
+
+def segment_cp(case, conns, fields, ib, iconn):
+    """Cp = 2 (p - PPF) at the wall cells of wall segment iconn (1-based) of block ib, shaped
+    over the segment's face index ranges (I, J, K)."""
+    cn = conns[case.blocks[ib].id][iconn - 1]
+    d, ci, cg, cf, is_min = _face_pairs(cn)
+    p = _at(fields[ib]["PP"], ci)
+    shape = tuple(cn.pointEnd[q] - cn.pointStart[q] + 1 for q in range(3))
+    return (2.0 * (p - case.params.PPF)).reshape(shape, order="F")      # face cells run I fastest
+
+
+def face_integrals(case, conns, geo, fields):
+    """The quantities of trans_get_integrals (struct trans_integrals), from host arrays."""
+    m_in, p0i, pi = boundary_flux(case, conns, geo, fields, 5)
+    m_out, p0o, po = boundary_flux(case, conns, geo, fields, 7)
+    Fp, Fv = wall_forces(case, conns, geo, fields)
+    return {"mass_in": m_in, "p0_in": p0i, "p_in": pi, "mass_out": m_out, "p0_out": p0o,
+            "p_out": po, "loss": (p0i - p0o) / (p0i - pi) if p0i != pi else 0.0,
+            "force_p": Fp.tolist(), "force_v": Fv.tolist()}
 
 
 def summary(case, conns, geo, fields):

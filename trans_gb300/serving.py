@@ -51,6 +51,7 @@ class Request:
     status: str = "queued"
     cells: int = 0
     result: dict = None
+    integrals: dict = None             # mass flow, loss, wall forces at retirement (on the device)
 
 
 def poisson_requests(rate=4.0, duration=60.0, seed=0, mix=(("coarse", 0.6), ("medium", 0.3), ("fine", 0.1)),
@@ -107,6 +108,8 @@ def serve(requests, precision=abi.TRANS_MIXED, budget_bytes=0, drop=1.0e-6, max_
         r.iterations = it
         g0, g1 = global_residual(first, c.blocks), global_residual(last, c.blocks)
         r.drop = g1 / g0 if g0 > 0 else math.nan
+        if status != "nan":
+            r.integrals = bt.integrals(cid)
         if keep_fields:
             r.result = {ib: {f: bt.get_field(cid, ib, f) for f in ("V", "PP", "T", "RMIU")} for ib in range(len(c.blocks))}
         bt.remove(cid)

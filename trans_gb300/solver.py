@@ -54,6 +54,7 @@ class Solver:
         self.case = case
         self.params = params if params is not None else case.params
         self.blocks = case.blocks
+        self._conns = conns
         self._keep = []
         nb = len(self.blocks)
         tb = block_table(case, conns, self._keep)
@@ -106,6 +107,22 @@ class Solver:
         sid = abi.STAGE_ID[stage] if isinstance(stage, str) else stage
         self._check(self._fn("run_stage")(self.ctx, sid, ki, itr), "run_stage")
 
+    def integrals(self):
+        """Integrated quantities of the current state, summed on the device (trans_get_integrals)."""
+        out = abi.TransIntegrals()
+        self._check(self.lib.trans_get_integrals(self.ctx, C.byref(out)), "get_integrals")
+        return out.as_dict()
+
+    def wall_cp(self, ib, iconn):
+        """Cp of the wall cells of wall segment iconn (1-based) of block ib, shaped (nI, nJ, nK)
+        over the segment's face index ranges (Fortran order)."""
+        cn = self._conns[self.blocks[ib].id][iconn - 1]
+        shape = tuple(cn.pointEnd[q] - cn.pointStart[q] + 1 for q in range(3))
+        cp = np.zeros(shape, order="F")
+        self._check(self.lib.trans_get_wall_cp(self.ctx, ib, iconn, cp.ctypes.data_as(C.POINTER(C.c_double))),
+                    "get_wall_cp")
+        return cp
+
     def norms(self):
         nb = len(self.blocks)
         norms = (abi.TransNorms * nb)()
@@ -140,6 +157,7 @@ class Batch:
         self.ctx = ctx
         self.precision = precision
         self.cases = {}                     # id -> (case, keep)
+        self.conns = {}                     # id -> connections of the case's blocks
 
     def _check(self, rc, what):
         if rc != 0:
@@ -165,6 +183,7 @@ class Batch:
             return None
         self._check(rc, "add")
         self.cases[cid.value] = (case, keep)
+        self.conns[cid.value] = conns
         for n, b in enumerate(case.blocks):
             for name in GEOMETRY_FIELDS:
                 self.set_field(cid.value, n, name, geo[b.id][name])
@@ -175,6 +194,7 @@ class Batch:
     def remove(self, cid):
         self._check(self.lib.trans_batch_remove(self.ctx, cid), "remove")
         del self.cases[cid]
+        self.conns.pop(cid, None)
 
     def set_field(self, cid, ib, name, full):
         ni, nj, nk = self.cases[cid][0].blocks[ib].dims
@@ -204,6 +224,30 @@ class Batch:
         it = C.c_int()
         self._check(self.lib.trans_batch_case_norms(self.ctx, cid, C.byref(it), first, last), "case_norms")
         return it.value, _norm_dicts(first), _norm_dicts(last)
+
+    def integrals(self, cid=None):
+        """Integrated quantities of one case, or of every case ({id: dict}) from one launch."""
+        if cid is not None:
+            out = abi.TransIntegrals()
+            self._check(self.lib.trans_batch_get_integrals(self.ctx, cid, C.byref(out)), "get_integrals")
+            return out.as_dict()
+        n = len(self.cases)
+        if n == 0:
+            return {}
+        ids, out = (C.c_int * n)(), (abi.TransIntegrals * n)()
+        m = self.lib.trans_batch_integrals(self.ctx, ids, out, n)
+        if m < 0:
+            self._check(m, "integrals")
+        return {ids[q]: out[q].as_dict() for q in range(m)}
+
+    def wall_cp(self, cid, ib, iconn):
+        case, keep = self.cases[cid]
+        cn = self.conns[cid][case.blocks[ib].id][iconn - 1]
+        shape = tuple(cn.pointEnd[q] - cn.pointStart[q] + 1 for q in range(3))
+        cp = np.zeros(shape, order="F")
+        self._check(self.lib.trans_batch_get_wall_cp(self.ctx, cid, ib, iconn, cp.ctypes.data_as(C.POINTER(C.c_double))),
+                    "get_wall_cp")
+        return cp
 
     def bytes_in_use(self):
         return int(self.lib.trans_batch_bytes_in_use(self.ctx))
