@@ -69,7 +69,7 @@ def replica_rate(units_per_rank, seconds, world):
     return units_per_rank * world / seconds / 1e6
 
 
-def make_case(name, precision, nk=64):
+def make_case(name, precision, nk=64, dst_fn=None):
     prec = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
     if name == "channel":
         c = cases.channel_bump(precision=prec)
@@ -79,7 +79,7 @@ def make_case(name, precision, nk=64):
         c = cases.square_cylinder(precision=prec)
     else:
         raise SystemExit(f"unknown case {name}")
-    conns, geo = CS.compute_geometry(c)
+    conns, geo = CS.compute_geometry(c, dst_fn=dst_fn)
     st = CS.initial_state(c, geo, Q_dst=c.meta.get("Q_dst", 0.01))
     return c, conns, geo, st
 
@@ -327,7 +327,7 @@ def batch_levels_arm(args):
     grid, so each level's geometry is computed once per angle), all in one batch context under
     the device budget; aggregate cell-iterations/s timed like the single case."""
     from trans_gb300 import serving
-    from trans_gb300.solver import Batch
+    from trans_gb300.solver import Batch, device_wall_distance
     prec = abi.TRANS_MIXED if args.precision == "mixed" else abi.TRANS_FP64
     counts = [int(x) for x in args.batch_levels.split(",")]
     rng = np.random.default_rng(0)
@@ -343,7 +343,7 @@ def batch_levels_arm(args):
             key = (level, angle)
             c = cases.cascade(inflow_deg=angle, p_ratio=ratio, precision=prec, **kw)
             if key not in geoms:
-                conns, geo = CS.compute_geometry(c)
+                conns, geo = CS.compute_geometry(c, dst_fn=device_wall_distance(bt.lib))
                 geoms[key] = (conns, geo, CS.initial_state(c, geo, Q_dst=c.meta.get("Q_dst", 0.01)))
             conns, geo, st = geoms[key]
             if bt.add(c, conns, geo, st) is None:
@@ -394,7 +394,10 @@ def serve_arm(args):
                        "retire_at_drop": args.drop, "budget_gb": args.budget_gb,
                        "mix": "coarse 0.6 / medium 0.3 / fine 0.1", "requests": rep["requests"]},
             "completed": rep["completed"], "converged": rep["converged"], "wall_s": rep["wall_s"],
-            "iterations_by_level": {k: [min(v), int(np.median(v)), max(v)] for k, v in by_level.items()}}
+            "iterations_by_level": {k: [min(v), int(np.median(v)), max(v)] for k, v in by_level.items()},
+            "setup_s_median_by_level": rep["setup_s_by_level"],
+            "loss_by_level": {lv: [round(r.integrals["loss"], 5) for r in recs if r.level == lv and r.integrals]
+                              for lv in by_level}}
     print(json.dumps(line))
 
 
@@ -427,7 +430,8 @@ def main():
     if args.case == "cascade" and not hasattr(cases, "cascade"):
         args.case = "channel"
     rank, world = init_replicas()
-    c, conns, geo, st = make_case(args.case, args.precision, args.nk)
+    from trans_gb300.solver import device_wall_distance
+    c, conns, geo, st = make_case(args.case, args.precision, args.nk, dst_fn=device_wall_distance())
     ncell = interior_cells(c)
     nsub = sub_iterations(c)
     s = Solver(c, conns, geo, st)

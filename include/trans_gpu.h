@@ -209,6 +209,19 @@ int trans_get_integrals(void* ctx, trans_integrals* out);
  * connection) of block ib (Output/OUTPUT_Surfaces.F90:303-305): one value per face of the
  * segment, I fastest, then J, then K, over pointStart..pointEnd of the segment's face indices. */
 int trans_get_wall_cp(void* ctx, int ib, int iconn, double* cp);
+/*
+ * Wall distance of GEOM_CalcDST (Geom/CalcDst.F90:127-164) on the device, for any set of points
+ * (no context).  xyz: n points, x y z interleaved (the cell centres Xc, Yc, Zc of the interior
+ * cells).  nsurf wall surfaces (AllSurfs): dims[2s], dims[2s+1] = NSur, MSur nodes of surface s;
+ * nodes: for each surface in turn, its X(NSur,MSur), then Y, then Z, Fortran order.  dst[q] =
+ * sqrt of the minimum over the panels of the reference's DDD, the surfaces combined in order
+ * with the reference's tiny floor: bit-identical to the reference's loop.  Allocates and frees
+ * its own device memory and stream; call with the wanted device current.  Errors:
+ * TRANS_E_ARG (non-finite coordinates, bad sizes), TRANS_E_CUDA; message in
+ * trans_last_error(NULL).
+ */
+int trans_wall_distance(long long n, const double* xyz, int nsurf, const int* dims, const double* nodes,
+                        double tiny, double* dst);
 /* Device bytes held by the context. */
 long long trans_device_bytes(void* ctx);
 /* Kernel launches issued since the context was created (all kernels of this library). */
@@ -275,6 +288,8 @@ const char* trans_kernel_class(int k);
 /* The schedule the context's tuner picked for the LU-SGS sweeps and what it measured (no
  * reference counterpart).  The string lives until the next call on this thread. */
 const char* trans_tuning(void* ctx);
+/* Message of the last failed call on ctx; with ctx = NULL, of the last failed context-free call
+ * (trans_wall_distance) on this thread. */
 const char* trans_last_error(void* ctx);
 
 #ifdef __cplusplus

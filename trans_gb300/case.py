@@ -361,8 +361,10 @@ def wall_distance(xc, yc, zc, surfaces, tiny=1.0e-20):
     return np.sqrt(dmin).reshape(xc.shape)
 
 
-def block_metrics(b, surfaces, tiny=1.0e-20):
-    """GEOM_CalcDST for one block (Geom/CalcDst.F90:28-719)."""
+def block_metrics(b, surfaces, tiny=1.0e-20, dst_fn=None):
+    """GEOM_CalcDST for one block (Geom/CalcDst.F90:28-719).  dst_fn: the wall-distance
+    function (default: `wall_distance` on the host; trans_gb300.solver.device_wall_distance
+    evaluates the same minimum on the GPU)."""
     NI, NJ, NK = b.dims
     NI1, NJ1, NK1 = NI - 1, NJ - 1, NK - 1
     XX, YY, ZZ = (np.asfortranarray(b.xyz[..., q]) for q in range(3))
@@ -384,7 +386,7 @@ def block_metrics(b, surfaces, tiny=1.0e-20):
     g["THTC"][ci, cj, ck] = dm.atan2(Zc[ci, cj, ck], Yc[ci, cj, ck])
     g["RAD"][ci, cj, ck] = np.sqrt(Yc[ci, cj, ck] * Yc[ci, cj, ck] + Zc[ci, cj, ck] * Zc[ci, cj, ck])
     # wall distance
-    g["DST"][ci, cj, ck] = wall_distance(Xc[ci, cj, ck], Yc[ci, cj, ck], Zc[ci, cj, ck], surfaces, tiny)
+    g["DST"][ci, cj, ck] = (dst_fn or wall_distance)(Xc[ci, cj, ck], Yc[ci, cj, ck], Zc[ci, cj, ck], surfaces, tiny)
     # SD & Grad
     SD, Gr = g["SD"], g["GRAD"]
     dl = 1.0
@@ -661,12 +663,13 @@ def geom_transform1(blocks, conns, geo):
                     SD[(d, q) + lf] = 2.0 * SD[(d, q) + f0] - SD[(d, q) + sf]
 
 
-def compute_geometry(case):
-    """All metrics of a case: CalcDst per block, then GeomTransform and GeomTransform1."""
+def compute_geometry(case, dst_fn=None):
+    """All metrics of a case: CalcDst per block, then GeomTransform and GeomTransform1.
+    dst_fn: wall-distance function (see block_metrics)."""
     conns = derive_connectivity(case.blocks)
     ph = case.physical
     set_rotate_angles(conns, case.blocks, ph.nblade if ph else 1, ph.npassage if ph else 1)
-    geo = {b.id: block_metrics(b, case.surfaces, case.params.Tiny) for b in case.blocks}
+    geo = {b.id: block_metrics(b, case.surfaces, case.params.Tiny, dst_fn) for b in case.blocks}
     geom_transform(case.blocks, conns, geo)
     geom_transform1(case.blocks, conns, geo)
     return conns, geo

@@ -204,7 +204,7 @@ const char* trans_tuning(void* ctx) {
 
 const char* trans_last_error(void* ctx) {
     Ctx* c = as_ctx(ctx);
-    return c ? c->err.c_str() : "no context";
+    return c ? c->err.c_str() : stateless_error();
 }
 
 }  // extern "C"

@@ -135,6 +135,7 @@ struct Ctx {
 };
 
 int fail(Ctx* c, int code, const std::string& msg);
+const char* stateless_error();          // message of the last failed context-free call on this thread
 
 #define CK(call)                                                                                  \
     do {                                                                                          \

@@ -20,7 +20,7 @@ import numpy as np
 from . import abi
 from . import case as CS
 from . import cases
-from .solver import Batch, global_residual
+from .solver import Batch, device_wall_distance, global_residual
 
 # grid levels of the cascade topology: (ns, nr, nh, nk) for about 0.35 M, 1.36 M and 5.4 M cells
 # grid levels: coarse ~0.35 M, medium 1.36 M, fine ~5.5 M cells.  The fine level also doubles the
@@ -52,6 +52,7 @@ class Request:
     cells: int = 0
     result: dict = None
     integrals: dict = None             # mass flow, loss, wall forces at retirement (on the device)
+    setup_s: float = math.nan          # host set-up (grid, geometry, initial field)
 
 
 def poisson_requests(rate=4.0, duration=60.0, seed=0, mix=(("coarse", 0.6), ("medium", 0.3), ("fine", 0.1)),
@@ -72,19 +73,22 @@ def poisson_requests(rate=4.0, duration=60.0, seed=0, mix=(("coarse", 0.6), ("me
     return out
 
 
-def build_case(req, precision):
-    """Host set-up of one request: grid, connectivity, geometry and initial field."""
+def build_case(req, precision, dst_fn=None):
+    """Set-up of one request: grid, connectivity, geometry (wall distance by dst_fn: on the
+    GPU when given, else on the host) and initial field; records its duration in req.setup_s."""
+    t0 = time.perf_counter()
     kw = dict(LEVELS.get(req.level, {}))
     kw.update(RAMP)
     kw.update(req.grid)
     c = cases.cascade(XM=req.mach, p_ratio=req.p_ratio, precision=precision, **kw)
-    conns, geo = CS.compute_geometry(c)
+    conns, geo = CS.compute_geometry(c, dst_fn=dst_fn)
     st = CS.initial_state(c, geo, Q_dst=c.meta.get("Q_dst", 0.01))
+    req.setup_s = time.perf_counter() - t0
     return c, conns, geo, st
 
 
 def serve(requests, precision=abi.TRANS_MIXED, budget_bytes=0, drop=1.0e-6, max_iters=20000, prep_workers=2,
-          keep_fields=False, lib=None, time_limit=None):
+          keep_fields=False, lib=None, time_limit=None, device_setup=True):
     """Run the request stream to completion (or until `time_limit` seconds); returns a report
     with p50/p99 latency, throughput and the per-request records.
 
@@ -93,6 +97,7 @@ def serve(requests, precision=abi.TRANS_MIXED, budget_bytes=0, drop=1.0e-6, max_
     when its global residual (block RMS norms of TIME_Update_V aggregated over blocks) has
     dropped by `drop` from its first iteration, after `max_iters` iterations, or on a NaN."""
     bt = Batch(precision, budget_bytes, lib)
+    dst_fn = device_wall_distance(bt.lib) if device_setup else None
     pending = sorted(requests, key=lambda r: r.arrival)
     prepping, ready, active = {}, [], {}
     done = []
@@ -124,7 +129,7 @@ def serve(requests, precision=abi.TRANS_MIXED, budget_bytes=0, drop=1.0e-6, max_
             t = now()
             while pending and pending[0].arrival <= t:
                 r = pending.pop(0)
-                prepping[r.rid] = (r, ex.submit(build_case, r, precision))
+                prepping[r.rid] = (r, ex.submit(build_case, r, precision, dst_fn))
             for rid in sorted(prepping):
                 r, f = prepping[rid]
                 if f.done():
@@ -172,6 +177,8 @@ def serve(requests, precision=abi.TRANS_MIXED, budget_bytes=0, drop=1.0e-6, max_
         "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
         "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
         "latency_mean_s": float(lat.mean()) if lat.size else None,
+        "setup_s_by_level": {lv: float(np.median([r.setup_s for r in done if r.level == lv]))
+                             for lv in sorted({r.level for r in done}) if any(r.level == lv for r in done)},
         "wall_s": wall, "cell_iters": int(cell_iters),
         "throughput_mcell_iter_s": cell_iters / wall / 1e6 if wall > 0 else 0.0,
         "records": done,

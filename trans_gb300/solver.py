@@ -273,3 +273,30 @@ def global_residual(norms, blocks):
         num += n * nrm["DRSa"] ** 2
         den += n
     return float(np.sqrt(num / den))
+
+
+def wall_distance_gpu(lib, xc, yc, zc, surfaces, tiny):
+    """trans_wall_distance: the reference's brute-force wall distance (Geom/CalcDst.F90:127-164)
+    of the points (xc, yc, zc) to the panel centres of `surfaces` (node grids (NSur, MSur, 3)),
+    on the GPU; same signature and result as trans_gb300.case.wall_distance."""
+    pts = np.ascontiguousarray(np.stack([xc.ravel(), yc.ravel(), zc.ravel()], axis=1), dtype=np.float64)
+    dims = np.array([d for S in surfaces for d in S.shape[:2]], dtype=np.int32)
+    nodes = np.concatenate([S[..., q].ravel(order="F") for S in surfaces for q in range(3)]) if surfaces else np.zeros(1)
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    out = np.zeros(pts.shape[0])
+    rc = lib.trans_wall_distance(pts.shape[0], pts.ctypes.data_as(C.POINTER(C.c_double)), len(surfaces),
+                                 dims.ctypes.data_as(C.POINTER(C.c_int)), nodes.ctypes.data_as(C.POINTER(C.c_double)),
+                                 float(tiny), out.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        m = lib.trans_last_error(None)
+        raise SolverError(f"trans_wall_distance failed ({rc}: {abi.ERRORS.get(rc, '?')}) {m.decode() if m else ''}")
+    return out.reshape(xc.shape)
+
+
+def device_wall_distance(lib=None):
+    """A dst_fn for trans_gb300.case.compute_geometry that runs the wall distance on the GPU."""
+    if lib is None:
+        from . import native
+        lib = native.load()
+    return lambda xc, yc, zc, surfaces, tiny: wall_distance_gpu(lib, xc, yc, zc, surfaces, tiny)
+
