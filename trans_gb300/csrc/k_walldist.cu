@@ -37,6 +37,14 @@ namespace {
 constexpr int WD_THREADS = 256;
 constexpr int WD_TILE = 2048;             // panels per shared-memory tile (float4: 32 KB)
 
+constexpr int WD_CAND = 8;                // candidates per surface held for the converged FP64 pass
+
+// the reference's DDD (Geom/CalcDst.F90:150-155), in its order
+__device__ __forceinline__ double ddd64(double px, double py, double pz, const double* __restrict__ q) {
+    const double Dx = px - q[0], Dy = py - q[1], Dz = pz - q[2];
+    return Dx * Dx + Dy * Dy + Dz * Dz;
+}
+
 __device__ __forceinline__ float d2f(float fx, float fy, float fz, float4 q) {
     const float dx = fx - q.x, dy = fy - q.y, dz = fz - q.z;
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
@@ -55,20 +63,31 @@ k_wall_distance(long long n, const double* __restrict__ pts, const float4* __res
     for (int s = 0; s < nsurf; ++s) {
         const long long p0 = soff[s], p1 = soff[s + 1];
         // pass A: FP32 minimum over the surface
-        float m = INFINITY;
+        float m = INFINITY, m1 = INFINITY;     // two chains of minima
         for (long long t0 = p0; t0 < p1; t0 += WD_TILE) {
             const int cnt = (int)min((long long)WD_TILE, p1 - t0);
             __syncthreads();
             for (int r = threadIdx.x; r < cnt; r += WD_THREADS) tile[r] = pan32[t0 + r];
             __syncthreads();
-#pragma unroll 8
-            for (int r = 0; r < cnt; ++r) m = fminf(m, d2f(fx, fy, fz, tile[r]));
+            int r = 0;
+#pragma unroll 4
+            for (; r + 1 < cnt; r += 2) {
+                m = fminf(m, d2f(fx, fy, fz, tile[r]));
+                m1 = fminf(m1, d2f(fx, fy, fz, tile[r + 1]));
+            }
+            if (r < cnt) m = fminf(m, d2f(fx, fy, fz, tile[r]));
         }
+        m = fminf(m, m1);
         const float sm = sqrtf(m);
         const float bd = __fmaf_rn(sm, 1.0e-5f, sm) + 2.0f * eabs;
         const float thr = bd * bd * (1.0f + 1.0e-5f);
-        // pass B: the reference's FP64 expression for the candidates
+        // pass B: collect the candidates, then evaluate the reference's FP64 expression for them
+        // with the warp's lanes together (a candidate found by one lane alone would otherwise
+        // cost the whole warp's FP64 issue slots); a lane with more than WD_CAND candidates
+        // evaluates the extra ones at once
         double a = 1.0e20;
+        long long cand[WD_CAND];
+        int nc = 0;
         for (long long t0 = p0; t0 < p1; t0 += WD_TILE) {
             const int cnt = (int)min((long long)WD_TILE, p1 - t0);
             __syncthreads();
@@ -76,11 +95,20 @@ k_wall_distance(long long n, const double* __restrict__ pts, const float4* __res
             __syncthreads();
             for (int r = 0; r < cnt; ++r) {
                 if (d2f(fx, fy, fz, tile[r]) <= thr) {
-                    const double* q = pan64 + 3 * (t0 + r);
-                    const double Dx = px - q[0], Dy = py - q[1], Dz = pz - q[2];
-                    const double DDD = Dx * Dx + Dy * Dy + Dz * Dz;
-                    if (DDD < a) a = DDD;
+                    if (nc < WD_CAND) {
+                        cand[nc++] = t0 + r;
+                    } else {
+                        const double DDD = ddd64(px, py, pz, pan64 + 3 * (t0 + r));
+                        if (DDD < a) a = DDD;
+                    }
                 }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < WD_CAND; ++j) {
+            if (j < nc) {
+                const double DDD = ddd64(px, py, pz, pan64 + 3 * cand[j]);
+                if (DDD < a) a = DDD;
             }
         }
         if (d < tiny) d = tiny;          // amax1(dst_minimum, tiny)
