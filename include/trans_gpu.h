@@ -56,7 +56,7 @@ typedef struct trans_params {
     double VisRatio, FSTI, Rkf, Rof, Rmiuf;
     double A1, Beta_star, Sigk1, Sigo1, Beta1, Gama1, Sigk2, Sigo2, Beta2, Gama2;
     double Prod_Lmt;
-    double F_limiter1, gama_max, gama_min;
+    double F_limiter1, F_limiter2, gama_max, gama_min;
     double DT_LUSGS_Main, DT_LUSGS_Sub, CFL_Main, CFL_Sub_start, CFL_Sub_end;
     double Trans_location, Alscale;
     int CFL_Sub_step, IF_Local_Main, IF_Local_Sub;

@@ -41,6 +41,8 @@ def load():
         lib.oracle_set_threads.restype = C.c_int
         lib.oracle_alimiter.argtypes = [C.c_double, C.c_double]
         lib.oracle_alimiter.restype = C.c_double
+        lib.oracle_muscl2_limiter.argtypes = [C.c_double, C.c_double]
+        lib.oracle_muscl2_limiter.restype = C.c_double
         dp = C.POINTER(C.c_double)
         lib.oracle_ausmpw.argtypes = [C.POINTER(abi.TransParams), dp, dp]
         lib.oracle_roe.argtypes = [C.POINTER(abi.TransParams), dp, dp]

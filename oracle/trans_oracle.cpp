@@ -925,7 +925,17 @@ double alimiter(double var1, double var2) {
            std::fabs(sgn1(var1) * one + sgn1(var2) * one);
 }
 
+// Space/UTIL_MUSCL.F90:21-35 (MUSCL2, the limiter of CONVECT_MUSCL2, Kind_Spatial = 1)
+double muscl2_limiter(double var1, double var2) {
+    const double epsm = 1.0e-6;
+    double smooth = (2.0 * var1 * var2 + epsm) / (var1 * var1 + var2 * var2 + epsm);
+    return ((1.0 + smooth) * var1 + (1.0 - smooth) * var2) * smooth / 2.0;
+}
+
+// CONVECT_MUSCL (Kind_Spatial = 2, limiter alimiter) and CONVECT_MUSCL2
+// (Space/CONVECT_MUSCL2.F90:29-291, Kind_Spatial = 1: the same loops with muscl2_limiter)
 void convect_muscl(Ctx& c, Blk& b) {
+    double (*lim)(double, double) = c.p.Kind_Spatial == 1 ? muscl2_limiter : alimiter;
     for (int i = 0; i <= b.NI + 1; ++i)
     for (int j = 0; j <= b.NJ + 1; ++j)
     for (int k = 0; k <= b.NK + 1; ++k)
@@ -950,14 +960,14 @@ void convect_muscl(Ctx& c, Blk& b) {
             for (int L = 1; L <= 5; ++L) {
                 double DR = b.VL(d, L, ip, jp, kp) - q[L - 1];
                 double DL = q[L - 1] - b.VR(d, L, i, j, k);
-                b.VL(d, L, ip, jp, kp) = q[L - 1] + alimiter(DR, DL);
-                b.VR(d, L, i, j, k) = q[L - 1] - alimiter(DL, DR);
+                b.VL(d, L, ip, jp, kp) = q[L - 1] + lim(DR, DL);
+                b.VR(d, L, i, j, k) = q[L - 1] - lim(DL, DR);
             }
             double rrr = b.rad(i, j, k);
             double DR = b.rccl(d, ip, jp, kp) - rrr;
             double DL = rrr - b.rccr(d, i, j, k);
-            b.rccl(d, ip, jp, kp) = rrr + alimiter(DR, DL);
-            b.rccr(d, i, j, k) = rrr - alimiter(DL, DR);
+            b.rccl(d, ip, jp, kp) = rrr + lim(DR, DL);
+            b.rccr(d, i, j, k) = rrr - lim(DL, DR);
         }
     }
 }
@@ -1035,8 +1045,13 @@ void mdcd_pair(const double* s6, double gama, double& ql, double& qr) {
     }
 }
 
+// CONVECT_MDCD (Kind_Spatial = 3) and CONVECT_MDCDHYB (Space/CONVECT_MDCDHYB.F90:1-477,
+// Kind_Spatial = 4): the same MDCD states, replaced by MUSCL states v0 +- alimiter/2 where the
+// sensor reaches F_limiter2 (:118-120, :175-177 and the J, K twins); MDCDHYB has neither the rcc
+// reconstruction nor the K-direction clamp of the sensor at 0
 void convect_mdcd(Ctx& c, Blk& b) {
     const trans_params& p = c.p;
+    const bool hyb = p.Kind_Spatial == 4;
     for (int d = 1; d <= 3; ++d) {
         const int e[3] = {d == 1, d == 2, d == 3};
         int nI = d == 1 ? b.NI : b.NI1, nJ = d == 2 ? b.NJ : b.NJ1, nK = d == 3 ? b.NK : b.NK1;
@@ -1056,15 +1071,20 @@ void convect_mdcd(Ctx& c, Blk& b) {
                 sh[npt - 1] = b.shock(ii, jj, kk);
             }
             double sensor = std::max(std::max(std::max(std::max(std::max(sh[0], sh[1]), sh[2]), sh[3]), sh[4]), sh[5]);
-            if (d == 3) sensor = std::max(sensor, 0.0);
+            if (d == 3 && !hyb) sensor = std::max(sensor, 0.0);
             double gama = p.gama_min + sensor * (p.gama_max - p.gama_min);
             for (int L = 1; L <= 5; ++L) {
                 double ql, qr;
-                mdcd_pair(s6[L - 1], gama, ql, qr);
+                const double* v = s6[L - 1];
+                mdcd_pair(v, gama, ql, qr);
+                if (hyb && sensor >= p.F_limiter2) {
+                    ql = v[2] + 0.5 * alimiter(v[3] - v[2], v[2] - v[1]);
+                    qr = v[3] - 0.5 * alimiter(v[3] - v[2], v[4] - v[3]);
+                }
                 b.VL(d, L, i, j, k) = ql;
                 b.VR(d, L, i, j, k) = qr;
             }
-            if (d == 3) continue;   // K-direction rcc is left at the face average (stray block, :450-521)
+            if (d == 3 || hyb) continue;   // K-direction rcc is left at the face average (stray block, :450-521)
             double r6[6];
             for (int npt = 1; npt <= 6; ++npt) {
                 int o = -4 + npt;
@@ -1774,7 +1794,7 @@ int run_stage(Ctx& c, int stage) {
                 std::fill(b.D.v.begin(), b.D.v.end(), 0.0);
                 if (c.p.IF_Euler == 0) diffusion_centered(c, b);
                 if (c.IF_turb) turbtwo_diffusion(c, b);
-                if (c.p.Kind_Spatial == 2) convect_muscl(c, b);
+                if (c.p.Kind_Spatial <= 2) convect_muscl(c, b);
                 else convect_mdcd(c, b);
                 if (c.IF_turb) turbtwo_convect_muscl(c, b);
                 convect_inviscid(c, b);
@@ -1852,7 +1872,7 @@ extern "C" {
 int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks, void** out) {
     if (!p || !blocks || nblocks <= 0 || !out) return TRANS_E_ARG;
     if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || p->Kind_Model != 1) return TRANS_E_ARG;
-    if (p->Kind_Spatial != 2 && p->Kind_Spatial != 3) return TRANS_E_ARG;
+    if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4) return TRANS_E_ARG;
     if (p->Kind_Roe != 1 && p->Kind_Roe != 3) return TRANS_E_ARG;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return TRANS_E_ARG;
     if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 3)) return TRANS_E_ARG;
@@ -1966,6 +1986,7 @@ int oracle_get_norms(void* ctx, trans_norms* norms) {
 
 // scalar entry points for known-answer tests of the flux and limiter formulas
 double oracle_alimiter(double a, double b) { return alimiter(a, b); }
+double oracle_muscl2_limiter(double a, double b) { return muscl2_limiter(a, b); }
 void oracle_ausmpw(const trans_params* p, const double* in, double* out) {
     ausmpw_common(*p, in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12], in[13], out);
 }

@@ -28,6 +28,8 @@ CASES = {
     "cascade_small_mdcd_ausmpw": ("cascade", dict(Kind_Spatial=3, Kind_Roe=3)),
     "channel_small_rk3_mdcd_ausmpw": ("channel", dict(Kind_Spatial=3, Kind_Roe=3, IF_RK=1, CFL_Sub_start=1.0,
                                                       CFL_Sub_end=1.0)),
+    "channel_small_muscl2_roe": ("channel", dict(Kind_Spatial=1, Kind_Roe=1)),
+    "cascade_small_mdcdhyb_ausmpw": ("cascade", dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05)),
 }
 
 

@@ -38,8 +38,14 @@ def _mask(kind, dims):
     return face_ghosts(dims, 1)
 
 
-@pytest.mark.parametrize("scheme", [dict(Kind_Spatial=2, Kind_Roe=1), dict(Kind_Spatial=3, Kind_Roe=3)],
-                         ids=["muscl_roe", "mdcd_ausmpw"])
+# Kind_Spatial 1 = MUSCL2 limiter, 4 = MDCD/MUSCL hybrid; F_limiter2 = 0.05 puts the hybrid switch
+# inside the sensor's range on these grids (a mix of MDCD and MUSCL faces)
+SCHEMES = [dict(Kind_Spatial=2, Kind_Roe=1), dict(Kind_Spatial=3, Kind_Roe=3), dict(Kind_Spatial=1, Kind_Roe=1),
+           dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05)]
+SCHEME_IDS = ["muscl_roe", "mdcd_ausmpw", "muscl2_roe", "mdcdhyb_ausmpw"]
+
+
+@pytest.mark.parametrize("scheme", SCHEMES, ids=SCHEME_IDS)
 def test_stage_by_stage(gpu_lib, scheme):
     c, conns, geo, st = small_channel(**scheme)
     g, o = _pair(c, conns, geo, st)
@@ -57,8 +63,7 @@ def test_stage_by_stage(gpu_lib, scheme):
         o.run_stage("UPDATE_U", ki)
 
 
-@pytest.mark.parametrize("scheme", [dict(Kind_Spatial=2, Kind_Roe=1), dict(Kind_Spatial=3, Kind_Roe=3)],
-                         ids=["muscl_roe", "mdcd_ausmpw"])
+@pytest.mark.parametrize("scheme", SCHEMES, ids=SCHEME_IDS)
 def test_iterations_and_residual_history(gpu_lib, scheme):
     """100 outer iterations: the state stays bit-identical to the oracle's (the FP64 kernels and
     the oracle round every operation alike), the residual norms agree to summation order."""
@@ -93,8 +98,7 @@ def test_bitwise_agreement_first_residual(gpu_lib):
     assert frac == 1.0, f"only {frac:.6f} of residual values are bit-identical"
 
 
-@pytest.mark.parametrize("scheme", [dict(Kind_Spatial=3, Kind_Roe=3), dict(Kind_Spatial=2, Kind_Roe=1)],
-                         ids=["mdcd_ausmpw", "muscl_roe"])
+@pytest.mark.parametrize("scheme", SCHEMES, ids=SCHEME_IDS)
 def test_cascade_multiblock_bitwise(gpu_lib, scheme):
     """Five blocks with 1-to-1 interfaces (O-cut, pitch periodicity, partial faces with
     reversed index direction), inlet, outlet recurrence and walls: 12 iterations stay

@@ -54,6 +54,27 @@ def test_alimiter_limits(lib):
     assert lib.oracle_alimiter(0.5, 0.2) == pytest.approx(0.25, rel=1e-12)
 
 
+def muscl2_exact(a, b):
+    """Space/UTIL_MUSCL.F90:21-35 in exact rational arithmetic."""
+    fa, fb, e = Fraction(a), Fraction(b), Fraction(1e-6)
+    s = (2 * fa * fb + e) / (fa * fa + fb * fb + e)
+    return ((1 + s) * fa + (1 - s) * fb) * s / 2
+
+
+@pytest.mark.parametrize("a,b", [(0.3, 0.1), (-0.2, -0.5), (0.3, -0.1), (1e-3, 2e-3), (0.0, 0.4), (5.0, 5.0)])
+def test_muscl2_limiter_known_answers(lib, a, b):
+    assert lib.oracle_muscl2_limiter(a, b) == pytest.approx(float(muscl2_exact(a, b)), rel=1e-13, abs=1e-300)
+
+
+def test_muscl2_limiter_limits(lib):
+    # equal slopes: smoothness 1, the slope itself; opposite slopes of equal size: smoothness
+    # (-2a^2 + e)/(2a^2 + e), nearly -1, so the result is about -a * smooth^2 ... of the first slope
+    assert lib.oracle_muscl2_limiter(0.7, 0.7) == pytest.approx(0.7, rel=1e-12)
+    assert lib.oracle_muscl2_limiter(0.0, 0.0) == 0.0
+    s = (-2 * 0.25 + 1e-6) / (0.5 + 1e-6)
+    assert lib.oracle_muscl2_limiter(0.5, -0.5) == pytest.approx(((1 + s) * 0.5 - (1 - s) * 0.5) * s / 2, rel=1e-12)
+
+
 def _flux_in(p, rho, u, v, w, T, n):
     pp = rho * T / p.RXM2
     s = np.array(n, float)

@@ -32,7 +32,7 @@ _PARAM_DOUBLES2 = [
     "VisRatio", "FSTI", "Rkf", "Rof", "Rmiuf",
     "A1", "Beta_star", "Sigk1", "Sigo1", "Beta1", "Gama1", "Sigk2", "Sigo2", "Beta2", "Gama2",
     "Prod_Lmt",
-    "F_limiter1", "gama_max", "gama_min",
+    "F_limiter1", "F_limiter2", "gama_max", "gama_min",
     "DT_LUSGS_Main", "DT_LUSGS_Sub", "CFL_Main", "CFL_Sub_start", "CFL_Sub_end",
     "Trans_location", "Alscale",
 ]

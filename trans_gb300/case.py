@@ -104,7 +104,7 @@ def make_params(ph: Physical, **kw):
     p.FSTI = ph.FSTI
     p.IF_Local_Main, p.IF_Local_Sub, p.CFL_Main = 0, 1, 1.0
     p.DT_LUSGS_Sub = 0.0
-    for k in ("Kind_Spatial", "Kind_Roe", "F_limiter1", "gama_max", "gama_min",
+    for k in ("Kind_Spatial", "Kind_Roe", "F_limiter1", "F_limiter2", "gama_max", "gama_min",
               "DT_LUSGS_Main", "CFL_Sub_start", "CFL_Sub_end", "CFL_Sub_step", "Kind_Dual",
               "Kchld", "IF_RK", "IF_Euler", "IF_Turb_org", "KItm", "Kind_Model", "Prod_Lmt",
               "IF_Comppress", "Kind_Hybrid", "Kind_SubHY", "If_fix_Transition",

@@ -102,7 +102,7 @@ struct Tile {             // a run of consecutive interior cells (or faces) of o
 
 #define TG_PARAM_REALS(X) X(XM) X(RXM2) X(PPF) X(Csthlnd) X(Csth1) X(Ref) X(Tiny) X(VxF) X(VyF) X(VzF) \
     X(omega0) X(P0in) X(T0in) X(Pouthub) X(VisRatio) X(FSTI) X(A1) X(Beta_star) X(Sigk1) X(Sigo1)    \
-    X(Beta1) X(Gama1) X(Sigk2) X(Sigo2) X(Beta2) X(Gama2) X(Prod_Lmt) X(gama_max) X(gama_min)        \
+    X(Beta1) X(Gama1) X(Sigk2) X(Sigo2) X(Beta2) X(Gama2) X(Prod_Lmt) X(gama_max) X(gama_min) X(F_limiter2)        \
     X(DT_LUSGS_Main) X(DT_LUSGS_Sub) X(CFL_Main) X(Trans_location)
 
 template <typename R>
@@ -181,6 +181,13 @@ template <typename R> __device__ inline R alimiter(R var1, R var2) {
     return (var1 * (var2 * var2 + R(2.0) * epsm * epsm) + var2 * (R(2.0) * var1 * var1 + epsm * epsm)) /
            (R(2.0) * var1 * var1 - var1 * var2 + R(2.0) * var2 * var2 + R(3.0) * epsm * epsm) * R(0.5) *
            fabs(sgn1(var1) + sgn1(var2));
+}
+
+// Space/UTIL_MUSCL.F90:21-35: the limiter of CONVECT_MUSCL2 (Kind_Spatial = 1)
+template <typename R> __device__ inline R muscl2_limiter(R var1, R var2) {
+    const R epsm = R(1.0e-6);
+    R smooth = (R(2.0) * var1 * var2 + epsm) / (var1 * var1 + var2 * var2 + epsm);
+    return ((R(1.0) + smooth) * var1 + (R(1.0) - smooth) * var2) * smooth / R(2.0);
 }
 
 // Space/CONVECT_MDCD.F90:62-120: left (ql) and right (qr) face states from six cells

@@ -614,17 +614,19 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
     // ---------------- reconstruction ----------------
     R qL[7], qR[7];
     const R* qc[5] = {pu, pv, pw, PPp, PT};
-    if (p.Kind_Spatial == 2) {
+    if (p.Kind_Spatial <= 2) {     // CONVECT_MUSCL (2) or CONVECT_MUSCL2 (1): the limiter differs
+        const bool m2 = p.Kind_Spatial == 1;
         for (int q = 0; q < 5; ++q) {
             const R* Q = qc[q];
             R fm = (favg<R>(Q, al, ainv, cm, s)), f0 = (favg<R>(Q, al, ainv, c, s)), fp = (favg<R>(Q, al, ainv, cp, s));
             R q1 = R(Q[cm]), q0 = R(Q[c]);
             R DR = f0 - q1, DL = q1 - fm;
-            qL[q] = q1 + alimiter(DR, DL);
+            qL[q] = q1 + (m2 ? muscl2_limiter(DR, DL) : alimiter(DR, DL));
             DR = fp - q0; DL = q0 - f0;
-            qR[q] = q0 - alimiter(DL, DR);
+            qR[q] = q0 - (m2 ? muscl2_limiter(DL, DR) : alimiter(DL, DR));
         }
-    } else {
+    } else {                       // CONVECT_MDCD (3) or CONVECT_MDCDHYB (4)
+        const bool hyb = p.Kind_Spatial == 4;
         const R* sh = rs<R>(b, S_SHOCK);
         R sensor = R(sh[c - 3 * s]);
         sensor = dmax(sensor, R(sh[c - 2 * s]));
@@ -632,13 +634,20 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
         sensor = dmax(sensor, R(sh[c]));
         sensor = dmax(sensor, R(sh[c + s]));
         sensor = dmax(sensor, R(sh[c + 2 * s]));
-        if (DIR == 3) sensor = dmax(sensor, R(0.0));
+        if (DIR == 3 && !hyb) sensor = dmax(sensor, R(0.0));
         R gama = R(p.gama_min) + sensor * (R(p.gama_max) - R(p.gama_min));
+        // MDCDHYB: MUSCL states where the sensor reaches F_limiter2 (Space/CONVECT_MDCDHYB.F90:118-120, 175-177)
+        const bool muscl = hyb && sensor >= R(p.F_limiter2);
         for (int q = 0; q < 5; ++q) {
             const R* Q = qc[q];
             R s6[6];
             for (int o = 0; o < 6; ++o) s6[o] = R(Q[c + (o - 3) * s]);
-            mdcd_pair(s6, gama, qL[q], qR[q]);
+            if (muscl) {
+                qL[q] = s6[2] + R(0.5) * alimiter(s6[3] - s6[2], s6[2] - s6[1]);
+                qR[q] = s6[3] - R(0.5) * alimiter(s6[3] - s6[2], s6[4] - s6[3]);
+            } else {
+                mdcd_pair(s6, gama, qL[q], qR[q]);
+            }
         }
     }
     if (turb) {
