@@ -885,6 +885,11 @@ void turbtwo_diffusion(Ctx& c, Blk& b) {
             double RmiuT = b.Rmiu(I, J, K), RmiuT1 = b.Rmiu(Im, Jm, Km);
             double RmiuTL = all * RmiuT1 + alr * RmiuT;
             if (Iswall0 || Iswallm) RmiuTL = 0.0;
+            double SigkAB, SigoAB;
+            if (p.Kind_Model == 2) {        // WD+2006: constant sigma (TURBTWO_DIFFUSION_Centered.F90:168-170)
+                SigkAB = p.Sigk1;
+                SigoAB = p.Sigo1;
+            } else {
             double DEN0 = b.V(1, I, J, K);
             double TKK0 = b.V(6, I, J, K) / DEN0, TOO0 = b.V(7, I, J, K) / DEN0;
             double DEN1 = b.V(1, Im, Jm, Km);
@@ -900,8 +905,9 @@ void turbtwo_diffusion(Ctx& c, Blk& b) {
             arg1 = std::min(arg1, 4.0 * Den * p.Sigo2 * TKK / CDKO / distfc / distfc);
             double a2 = arg1 * arg1;
             double fc1c = otm::tanh_(a2 * a2);
-            double SigkAB = fc1c * p.Sigk1 + (1.0 - fc1c) * p.Sigk2;
-            double SigoAB = fc1c * p.Sigo1 + (1.0 - fc1c) * p.Sigo2;
+            SigkAB = fc1c * p.Sigk1 + (1.0 - fc1c) * p.Sigk2;
+            SigoAB = fc1c * p.Sigo1 + (1.0 - fc1c) * p.Sigo2;
+            }
             double vmute = RmiuL + RmiuTL * SigkAB;
             double vmuoq = RmiuL + RmiuTL * SigoAB;
             double Dx = b.SD(d, 1, I, J, K), Dy = b.SD(d, 2, I, J, K), Dz = b.SD(d, 3, I, J, K);
@@ -1398,6 +1404,78 @@ double fsst(const trans_params& p, double Den, double vK, double vOmega, double 
     return 0.0;
 }
 
+// Wilcox 2006 k-omega sources and diagonal of one cell (Kind_Model = 2,
+// Time/TURBTWO_TIME_LUSGS_SST.F90:418-547)
+void wd2006_sources(Ctx& c, Blk& b, int I, int J, int K) {
+    const trans_params& p = c.p;
+    double dudx = b.DQ(1, I, J, K), dudy = b.DQ(2, I, J, K), dudz = b.DQ(3, I, J, K);
+    double dvdx = b.DQ(4, I, J, K), dvdy = b.DQ(5, I, J, K), dvdz = b.DQ(6, I, J, K);
+    double dwdx = b.DQ(7, I, J, K), dwdy = b.DQ(8, I, J, K), dwdz = b.DQ(9, I, J, K);
+    double dtkdx = b.DQ(13, I, J, K), dtkdy = b.DQ(14, I, J, K), dtkdz = b.DQ(15, I, J, K);
+    double dtodx = b.DQ(16, I, J, K), dtody = b.DQ(17, I, J, K), dtodz = b.DQ(18, I, J, K);
+    double W[3][3], S[3][3];
+    W[0][0] = 0.; W[1][1] = 0.; W[2][2] = 0.;
+    W[0][1] = 0.5 * (dudy - dvdx); W[0][2] = 0.5 * (dudz - dwdx); W[1][2] = 0.5 * (dvdz - dwdy);
+    W[1][0] = -W[0][1]; W[2][0] = -W[0][2]; W[2][1] = -W[1][2];
+    S[0][0] = 0.5 * (dudx + dudx); S[1][1] = 0.5 * (dvdy + dvdy); S[2][2] = 0.5 * (dwdz + dwdz);
+    S[0][1] = 0.5 * (dudy + dvdx); S[0][2] = 0.5 * (dudz + dwdx); S[1][2] = 0.5 * (dvdz + dwdy);
+    S[1][0] = S[0][1]; S[2][0] = S[0][2]; S[2][1] = S[1][2];
+    double Div = dudx + dvdy + dwdz;
+    double Votg = sq(dudy - dvdx) + sq(dvdz - dwdy) + sq(dwdx - dudz);
+    double prod = (2.0 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz) + sq(dudy + dvdx) + sq(dvdz + dwdy) + sq(dwdx + dudz)
+                   - 2.0 / 3.0 * Div * Div);
+    double tprod = std::min(prod, Votg) * b.Rmiu(I, J, K) / p.Ref;
+    double ARo = b.V(1, I, J, K), ARTk = b.V(6, I, J, K), ARTO = b.V(7, I, J, K);
+    double tprodl1 = p.Prod_Lmt * p.Beta_star * ARTk * ARTO / ARo * p.Ref;
+    tprod = std::min(tprod, tprodl1);
+    double SourceP = tprod - 2.0 / 3.0 * std::min(Div, 0.0) * ARTk;
+    double SourceN1 = -2.0 / 3.0 * std::max(Div, 0.0) - p.Beta_star * ARTO / ARo * p.Ref;
+    double Source = SourceP + SourceN1 * ARTk;
+    double CnegTk = std::fabs(SourceN1);
+    b.D(6, I, J, K) = b.D(6, I, J, K) + Source;
+    tprod = std::min(prod, Votg) / p.Ref;
+    double WWSg = 0.;
+    for (int ii = 0; ii < 3; ++ii)
+        for (int jj = 0; jj < 3; ++jj)
+            for (int kk = 0; kk < 3; ++kk) WWSg = WWSg + W[ii][jj] * W[jj][kk] * S[kk][ii];
+    double aK_omg = std::fabs(WWSg / otm::pow_(0.09 * ARTO / ARo * p.Ref, 3.));
+    double FBeta = (1. + 85. * aK_omg) / (1. + 100. * aK_omg);
+    double Beta_06 = p.Beta1 * FBeta;
+    double cdif = dtkdx * dtodx + dtkdy * dtody + dtkdz * dtodz;
+    double dltCD = cdif <= 0. ? 0. : 0.125;
+    SourceP = p.Gama1 * ARo * tprod - 2.0 / 3.0 * p.Gama1 * std::min(Div, 0.0) * ARTO;
+    SourceN1 = -2.0 / 3.0 * p.Gama1 * std::max(Div, 0.0) - Beta_06 * ARTO / ARo * p.Ref;
+    Source = SourceP + SourceN1 * ARTO;
+    double SourceCross = dltCD * ARo * ARo / ARTO / p.Ref * cdif;
+    Source = Source + SourceCross;
+    double CnegTO = 2.0 * std::fabs(SourceN1);
+    b.D(7, I, J, K) = b.D(7, I, J, K) + Source;
+    double stept = 2.0 * b.Dtm(I, J, K) / (3.0 * b.Dtm(I, J, K) / p.DT_LUSGS_Main + 2.0);
+    b.F(1, I, J, K) = 1. + (b.Rds(1, I, J, K) + b.Rds(2, I, J, K) + b.Rds(3, I, J, K)) * (stept / b.Vol(I, J, K)) + (CnegTk + CnegTO) * stept;
+    b.F(2, I, J, K) = b.F(1, I, J, K);
+}
+
+// Wilcox 2006 limits and eddy viscosity of the k-omega update (Kind_Model = 2,
+// Time/TIME_Update_V.F90:821-858, Time/TIME_RK_V_Update_New.F90:195-232); prod as the caller
+// computed it
+void wd2006_update(const trans_params& p, Blk& b, int I, int J, int K, double ARTk, double ARTO, double pRo,
+                   double RmiuL, double prod) {
+    double Dudx = b.DQ(1, I, J, K), Dudy = b.DQ(2, I, J, K), Dudz = b.DQ(3, I, J, K);
+    double Dvdx = b.DQ(4, I, J, K), Dvdy = b.DQ(5, I, J, K), Dvdz = b.DQ(6, I, J, K);
+    double Dwdx = b.DQ(7, I, J, K), Dwdy = b.DQ(8, I, J, K), Dwdz = b.DQ(9, I, J, K);
+    double Sii = Dudx - (Dudx + Dvdy + Dwdz) / 3.;
+    double Sjj = Dvdy - (Dudx + Dvdy + Dwdz) / 3.;
+    double Skk = Dwdz - (Dudx + Dvdy + Dwdz) / 3.;
+    double Sij = (Dudy + Dvdx) / 2.0, Sik = (Dudz + Dwdx) / 2.0, Sjk = (Dvdz + Dwdy) / 2.0;
+    double Skl = std::sqrt(1.0 * Sii * Sii + 1.0 * Sjj * Sjj + 1.0 * Skk * Skk + 2.0 * Sij * Sij + 2.0 * Sik * Sik + 2.0 * Sjk * Sjk);
+    ARTO = std::max(ARTO, std::sqrt(pRo * std::fabs(prod) / (p.Prod_Lmt * p.Beta_star)) / p.Ref);
+    ARTk = std::min(ARTk, 100000.0 * RmiuL * ARTO / pRo);
+    b.V(6, I, J, K) = ARTk;
+    b.V(7, I, J, K) = ARTO;
+    ARTO = std::max(ARTO, 7. / 8. * pRo * std::sqrt(Skl * Skl * 2. / 0.09) / p.Ref);
+    b.Rmiu(I, J, K) = ARTk / ARTO * pRo;
+}
+
 void turbtwo_lusgs_sst(Ctx& c, Blk& b) {
     const trans_params& p = c.p;
     for (int K = 1; K <= b.NK1; ++K)
@@ -1412,6 +1490,7 @@ void turbtwo_lusgs_sst(Ctx& c, Blk& b) {
     for (int K = 1; K <= b.NK1; ++K)
     for (int J = 1; J <= b.NJ1; ++J)
     for (int I = 1; I <= b.NI1; ++I) {
+        if (p.Kind_Model == 2) { wd2006_sources(c, b, I, J, K); continue; }
         double dudx = b.DQ(1, I, J, K), dudy = b.DQ(2, I, J, K), dudz = b.DQ(3, I, J, K);
         double dvdx = b.DQ(4, I, J, K), dvdy = b.DQ(5, I, J, K), dvdz = b.DQ(6, I, J, K);
         double dwdx = b.DQ(7, I, J, K), dwdy = b.DQ(8, I, J, K), dwdz = b.DQ(9, I, J, K);
@@ -1621,6 +1700,7 @@ void time_update_v(Ctx& c, Blk& b) {
         double Div = Dudx + Dvdy + Dwdz;
         double prod = (2.0 * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy) + sq(Dwdx + Dudz)
                        - 2.0 / 3.0 * Div * Div);
+        if (p.Kind_Model == 2) { wd2006_update(p, b, I, J, K, ARTk, ARTO, pRo, RmiuL, prod); continue; }
         double arg2 = 2.0 * std::sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
         arg2 = std::max(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
         arg2 = otm::tanh_(arg2 * arg2);
@@ -1726,6 +1806,7 @@ void time_rk_v_update(Ctx& c, Blk& b) {
         double Div = Dudx + Dvdy + Dwdz;
         double prod = (2.0 * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy) + sq(Dwdx + Dudz)
                        - 2.0 / 3.0 * Div * Div);
+        if (p.Kind_Model == 2) { wd2006_update(p, b, I, J, K, ARTk, ARTO, pRo, RmiuL, prod); continue; }
         double arg2 = 2.0 * std::sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
         arg2 = std::max(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
         arg2 = otm::tanh_(arg2 * arg2);
@@ -1871,7 +1952,7 @@ extern "C" {
 
 int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks, void** out) {
     if (!p || !blocks || nblocks <= 0 || !out) return TRANS_E_ARG;
-    if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || p->Kind_Model != 1) return TRANS_E_ARG;
+    if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2)) return TRANS_E_ARG;
     if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4) return TRANS_E_ARG;
     if (p->Kind_Roe != 1 && p->Kind_Roe != 3) return TRANS_E_ARG;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return TRANS_E_ARG;

@@ -40,9 +40,10 @@ def _mask(kind, dims):
 
 # Kind_Spatial 1 = MUSCL2 limiter, 4 = MDCD/MUSCL hybrid; F_limiter2 = 0.05 puts the hybrid switch
 # inside the sensor's range on these grids (a mix of MDCD and MUSCL faces)
+# Kind_Model 2 = the WD+2006 k-omega model in place of SST
 SCHEMES = [dict(Kind_Spatial=2, Kind_Roe=1), dict(Kind_Spatial=3, Kind_Roe=3), dict(Kind_Spatial=1, Kind_Roe=1),
-           dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05)]
-SCHEME_IDS = ["muscl_roe", "mdcd_ausmpw", "muscl2_roe", "mdcdhyb_ausmpw"]
+           dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05), dict(Kind_Spatial=3, Kind_Roe=3, Kind_Model=2)]
+SCHEME_IDS = ["muscl_roe", "mdcd_ausmpw", "muscl2_roe", "mdcdhyb_ausmpw", "mdcd_ausmpw_wd2006"]
 
 
 @pytest.mark.parametrize("scheme", SCHEMES, ids=SCHEME_IDS)
@@ -150,14 +151,17 @@ def test_runge_kutta_stages_bitwise(gpu_lib):
         o.run_stage("UPDATE_U", ki, 3)
 
 
-@pytest.mark.parametrize("kind", ["channel", "cascade"])
+@pytest.mark.parametrize("kind", ["channel", "cascade", "channel_wd2006"])
 def test_runge_kutta_iterations_bitwise(gpu_lib, kind):
     """Runge-Kutta outer iterations through trans_iterate (3 stages each): the state stays
     bit-identical to the oracle's, the norms of every block agree to summation order."""
     from helpers import small_cascade
-    c, conns, geo, st = small_channel(**RK3) if kind == "channel" else small_cascade(**RK3)
+    if kind == "channel_wd2006":
+        c, conns, geo, st = small_channel(**RK3, Kind_Model=2)
+    else:
+        c, conns, geo, st = small_channel(**RK3) if kind == "channel" else small_cascade(**RK3)
     g, o = _pair(c, conns, geo, st)
-    n = 30 if kind == "channel" else 8
+    n = 8 if kind == "cascade" else 30
     for ki in range(1, n + 1):
         ng = g.iterate(ki)
         no = o.iterate(ki)

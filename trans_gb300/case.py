@@ -77,10 +77,14 @@ def make_params(ph: Physical, **kw):
     p.Tiny = 1.0e-20                                   # main.F90:12
     if sw["IF_Turb_org"]:
         p.A1, Akapa, p.Beta_star = 0.31, 0.41, 0.09
-        if sw["Kind_Model"] != 1:
-            raise ValueError("only SST (Kind_Model=1) is supported")
-        p.Sigk1, p.Sigo1, p.Beta1, p.Gama1 = 0.85, 0.500, 0.0750, 5.0 / 9.0
-        p.Sigk2, p.Sigo2, p.Beta2, p.Gama2 = 1.00, 0.856, 0.0828, 0.440
+        if sw["Kind_Model"] == 1:                      # SST (Input/ParameterSet.F90:34-37)
+            p.Sigk1, p.Sigo1, p.Beta1, p.Gama1 = 0.85, 0.500, 0.0750, 5.0 / 9.0
+            p.Sigk2, p.Sigo2, p.Beta2, p.Gama2 = 1.00, 0.856, 0.0828, 0.440
+        elif sw["Kind_Model"] == 2:                    # WD+2006 (Input/ParameterSet.F90:39-43)
+            p.Sigk1, p.Sigo1, p.Beta1, p.Gama1 = 0.6, 0.5, 0.0708, 0.52
+            p.Sigk2, p.Sigo2, p.Beta2, p.Gama2 = 0.6, 0.5, 0.0708, 0.52
+        else:
+            raise ValueError("Kind_Model must be 1 (SST) or 2 (WD+2006)")
         p.Rmiuf = 1.8e-5 / 1.2
         p.Rkf = 1.5 * ph.FSTI * ph.FSTI
         p.Rof = 1.2 * p.Rkf / p.Rmiuf

@@ -111,7 +111,7 @@ struct ParamsT {          // module globals the kernels read (trans_params + der
     TG_PARAM_REALS(TG_DECL)
 #undef TG_DECL
     int Kind_Spatial, Kind_Roe, Kind_Hybrid, Kind_SubHY, Kind_Dual, IF_Local_Main, IF_Local_Sub;
-    int IF_Comppress, If_fix_Transition, pad_;
+    int IF_Comppress, If_fix_Transition, Kind_Model;
 };
 using Params = ParamsT<double>;
 
@@ -124,7 +124,7 @@ inline ParamsT<R> params_as(const Params& p) {
     q.Kind_Spatial = p.Kind_Spatial; q.Kind_Roe = p.Kind_Roe; q.Kind_Hybrid = p.Kind_Hybrid;
     q.Kind_SubHY = p.Kind_SubHY; q.Kind_Dual = p.Kind_Dual; q.IF_Local_Main = p.IF_Local_Main;
     q.IF_Local_Sub = p.IF_Local_Sub; q.IF_Comppress = p.IF_Comppress; q.If_fix_Transition = p.If_fix_Transition;
-    q.pad_ = 0;
+    q.Kind_Model = p.Kind_Model;
     return q;
 }
 
@@ -174,6 +174,11 @@ template <typename R> __device__ inline R mu_suth(const ParamsT<R>& p, R TT) {
 template <typename R> __device__ inline R mu_suth_nocs(const ParamsT<R>& p, R TT) {
     return (R(1.0) + R(p.Csthlnd)) / (TT + R(p.Csthlnd)) * p15(TT);
 }
+
+// x**3. of a Fortran real exponent: the pow of tmath in FP64 (as the oracle), x*x*x in FP32
+template <typename R> __device__ inline R cube_pow(R x);
+template <> __device__ inline double cube_pow<double>(double x) { return tmx::pow_(x, 3.0); }
+template <> __device__ inline float cube_pow<float>(float x) { return x * x * x; }
 
 // Space/UTIL_MUSCL.F90:2-18
 template <typename R> __device__ inline R alimiter(R var1, R var2) {

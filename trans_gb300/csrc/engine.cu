@@ -46,6 +46,7 @@ Params make_params(const trans_params& p) {
     d.Kind_Spatial = p.Kind_Spatial; d.Kind_Roe = p.Kind_Roe; d.Kind_Hybrid = p.Kind_Hybrid;
     d.Kind_SubHY = p.Kind_SubHY; d.Kind_Dual = p.Kind_Dual; d.IF_Local_Main = p.IF_Local_Main;
     d.IF_Local_Sub = p.IF_Local_Sub; d.IF_Comppress = p.IF_Comppress; d.If_fix_Transition = p.If_fix_Transition;
+    d.Kind_Model = p.Kind_Model;
     return d;
 }
 
@@ -53,7 +54,8 @@ Params make_params(const trans_params& p) {
 
 // options outside the configurations of this hot path are rejected, never approximated
 bool params_supported(const trans_params* p) {
-    if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || p->Kind_Model != 1 || p->IF_Euler != 0) return false;
+    if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2) || p->IF_Euler != 0)
+        return false;
     if (p->IF_RK != 0 && p->IF_RK != 1) return false;
     if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4 || (p->Kind_Roe != 1 && p->Kind_Roe != 3)) return false;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return false;

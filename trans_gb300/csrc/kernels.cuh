@@ -588,23 +588,30 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
         }
         R TTLt = all * R(PT[cm]) + alr * R(PT[c]);
         R RmiuLt = mu_suth_nocs<R>(p, TTLt);
-        const R* V1 = rs<R>(b, S_V);
-        R DEN0 = R(V1[c]), TKK0 = R(pk[c]), TOO0 = R(po[c]);
-        R DEN1 = R(V1[cm]), TKK1 = R(pk[cm]), TOO1 = R(po[cm]);
-        R Den = all * DEN1 + alr * DEN0;
-        R TKK = all * TKK1 + alr * TKK0;
-        R TOO = all * TOO1 + alr * TOO0;
-        R dTKO = gt[0][0] * gt[1][0] + gt[0][1] * gt[1][1] + gt[0][2] * gt[1][2];
-        R Sigo2 = R(p.Sigo2), Bs = R(p.Beta_star), Ref = R(p.Ref);
-        R CDKO = dmax(R(2.0) * Den * Sigo2 / TOO * (dTKO), R(1.0e-10));
-        const R* Dst = rs<R>(b, S_DST);
-        R distfc = alr * R(Dst[c]) + all * R(Dst[cm]);
-        R arg1 = dmax(sqrt(TKK) / Bs / TOO / distfc / Ref, R(500.0) * RmiuLt / Den / distfc / distfc / TOO / Ref / Ref);
-        arg1 = dmin(arg1, R(4.0) * Den * Sigo2 * TKK / CDKO / distfc / distfc);
-        R a2 = arg1 * arg1;
-        R fc1c = ttanh(a2 * a2);
-        R SigkAB = fc1c * R(p.Sigk1) + (R(1.0) - fc1c) * R(p.Sigk2);
-        R SigoAB = fc1c * R(p.Sigo1) + (R(1.0) - fc1c) * Sigo2;
+        const R Ref = R(p.Ref);
+        R SigkAB, SigoAB;
+        if (p.Kind_Model == 2) {         // WD+2006: constant sigma (TURBTWO_DIFFUSION_Centered.F90:168-170)
+            SigkAB = R(p.Sigk1);
+            SigoAB = R(p.Sigo1);
+        } else {
+            const R* V1 = rs<R>(b, S_V);
+            R DEN0 = R(V1[c]), TKK0 = R(pk[c]), TOO0 = R(po[c]);
+            R DEN1 = R(V1[cm]), TKK1 = R(pk[cm]), TOO1 = R(po[cm]);
+            R Den = all * DEN1 + alr * DEN0;
+            R TKK = all * TKK1 + alr * TKK0;
+            R TOO = all * TOO1 + alr * TOO0;
+            R dTKO = gt[0][0] * gt[1][0] + gt[0][1] * gt[1][1] + gt[0][2] * gt[1][2];
+            R Sigo2 = R(p.Sigo2), Bs = R(p.Beta_star);
+            R CDKO = dmax(R(2.0) * Den * Sigo2 / TOO * (dTKO), R(1.0e-10));
+            const R* Dst = rs<R>(b, S_DST);
+            R distfc = alr * R(Dst[c]) + all * R(Dst[cm]);
+            R arg1 = dmax(sqrt(TKK) / Bs / TOO / distfc / Ref, R(500.0) * RmiuLt / Den / distfc / distfc / TOO / Ref / Ref);
+            arg1 = dmin(arg1, R(4.0) * Den * Sigo2 * TKK / CDKO / distfc / distfc);
+            R a2 = arg1 * arg1;
+            R fc1c = ttanh(a2 * a2);
+            SigkAB = fc1c * R(p.Sigk1) + (R(1.0) - fc1c) * R(p.Sigk2);
+            SigoAB = fc1c * R(p.Sigo1) + (R(1.0) - fc1c) * Sigo2;
+        }
         R vmute = RmiuLt + RmiuTL * SigkAB;
         R vmuoq = RmiuLt + RmiuTL * SigoAB;
         R Dx = R(SDd[c]), Dy = R(SDd[c + nc]), Dz = R(SDd[c + 2 * nc]);
@@ -834,6 +841,37 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
     R ARo = (rs<R>(b, S_V)[c]), ARTk = (rs<R>(b, S_V + 5)[c]), ARTO = (rs<R>(b, S_V + 6)[c]);
     R tprodl1 = R(p.Prod_Lmt) * Bs * ARTk * ARTO / ARo * Ref;
     tprod = dmin(tprod, tprodl1);
+    if (p.Kind_Model == 2) {    // Wilcox 2006 k-omega (TURBTWO_TIME_LUSGS_SST.F90:418-547)
+        const R c23 = R(2.0 / 3.0);
+        R SourceN1 = -(c23 * dmax(Div, R(0.0))) - Bs * ARTO / ARo * Ref;
+        DQ(5) = DQ(5) + ((tprod - c23 * dmin(Div, R(0.0)) * ARTk) + SourceN1 * ARTk);
+        const R CnegTk = fabs(SourceN1);
+        tprod = dmin(prod, Votg) / Ref;
+        const R h = R(0.5);
+        const R W[3][3] = {{R(0.), h * (dudy - dvdx), h * (dudz - dwdx)},
+                           {-(h * (dudy - dvdx)), R(0.), h * (dvdz - dwdy)},
+                           {-(h * (dudz - dwdx)), -(h * (dvdz - dwdy)), R(0.)}};
+        const R Sxy = h * (dudy + dvdx), Sxz = h * (dudz + dwdx), Syz = h * (dvdz + dwdy);
+        const R S[3][3] = {{h * (dudx + dudx), Sxy, Sxz}, {Sxy, h * (dvdy + dvdy), Syz}, {Sxz, Syz, h * (dwdz + dwdz)}};
+        R WWSg = R(0.);
+#pragma unroll
+        for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+            for (int jj = 0; jj < 3; ++jj)
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) WWSg = WWSg + W[ii][jj] * W[jj][kk] * S[kk][ii];
+        R aK_omg = fabs(WWSg / cube_pow(R(0.09) * ARTO / ARo * Ref));
+        R Beta_06 = R(p.Beta1) * ((R(1.) + R(85.) * aK_omg) / (R(1.) + R(100.) * aK_omg));
+        const R G1 = R(p.Gama1);
+        R SourceP = G1 * ARo * tprod - c23 * G1 * dmin(Div, R(0.0)) * ARTO;
+        SourceN1 = -(c23 * G1 * dmax(Div, R(0.0))) - Beta_06 * ARTO / ARo * Ref;
+        R Source = SourceP + SourceN1 * ARTO;
+        R dltCD = cdif <= R(0.) ? R(0.) : R(0.125);
+        Source = Source + dltCD * ARo * ARo / ARTO / Ref * cdif;
+        DQ(6) = DQ(6) + Source;
+        REC(REC_FT) = R(fm) + (CnegTk + R(2.0) * fabs(SourceN1)) * R(stept);
+        return;
+    }
     R TT = (rs<R>(b, S_T)[c]);
     R RmiuL = mu_suth<R>(p, TT);
     R Fdes = R(1.0);
@@ -1281,6 +1319,20 @@ __device__ inline void sst_update(const Params& p, const DevBlock& b, int c, int
     double Div = Dudx + Dvdy + Dwdz;
     double prod = (2.0 * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy) + sq(Dwdx + Dudz)
                    - 2.0 / 3.0 * Div * Div);
+    if (p.Kind_Model == 2) {    // Wilcox 2006 (TIME_Update_V.F90:821-858, TIME_RK_V_Update_New.F90:195-232)
+        double Sii = Dudx - (Dudx + Dvdy + Dwdz) / 3.;
+        double Sjj = Dvdy - (Dudx + Dvdy + Dwdz) / 3.;
+        double Skk = Dwdz - (Dudx + Dvdy + Dwdz) / 3.;
+        double Sij = (Dudy + Dvdx) / 2.0, Sik = (Dudz + Dwdx) / 2.0, Sjk = (Dvdz + Dwdy) / 2.0;
+        double Skl = sqrt(1.0 * Sii * Sii + 1.0 * Sjj * Sjj + 1.0 * Skk * Skk + 2.0 * Sij * Sij + 2.0 * Sik * Sik + 2.0 * Sjk * Sjk);
+        ARTO = dmax(ARTO, sqrt(pRo * fabs(prod) / (p.Prod_Lmt * p.Beta_star)) / p.Ref);
+        ARTk = dmin(ARTk, 100000.0 * RmiuL * ARTO / pRo);
+        V5[c] = ARTk;
+        V6[c] = ARTO;
+        ARTO = dmax(ARTO, 7. / 8. * pRo * sqrt(Skl * Skl * 2. / 0.09) / p.Ref);
+        slot(b, S_RMIU)[c] = ARTk / ARTO * pRo;
+        return;
+    }
     double arg2 = 2.0 * sqrt(ARTk / pRo) / p.Beta_star / (ARTO / pRo) / DistN / p.Ref;
     arg2 = dmax(arg2, 500.0 * RmiuL / DistN / DistN / ARTO / p.Ref / p.Ref);
     arg2 = tmx::tanh_(arg2 * arg2);

@@ -260,6 +260,19 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
             const float prod = 2.0f * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy)
                                + sq(Dwdx + Dudz) - (2.0f / 3.0f) * Div * Div;
             const float Ref = p.Ref, Bs = p.Beta_star;
+            if (p.Kind_Model == 2) {    // Wilcox 2006 (TIME_Update_V.F90:821-858), in FP32
+                const float t3 = Div / 3.0f;
+                const float Sii = Dudx - t3, Sjj = Dvdy - t3, Skk = Dwdz - t3;
+                const float Sij = 0.5f * (Dudy + Dvdx), Sik = 0.5f * (Dudz + Dwdx), Sjk = 0.5f * (Dvdz + Dwdy);
+                const float Skl = sqrtf(Sii * Sii + Sjj * Sjj + Skk * Skk + 2.0f * (Sij * Sij + Sik * Sik + Sjk * Sjk));
+                ARTO = dmax(ARTO, (double)(sqrtf(ro * fabsf(prod) / (p.Prod_Lmt * Bs)) / Ref));
+                of = (float)ARTO;
+                ARTk = dmin(ARTk, (double)(100000.0f * RmiuL * of / ro));
+                V5[c] = ARTk;
+                V6[c] = ARTO;
+                const float om = fmaxf(of, 0.875f * ro * sqrtf(Skl * Skl * (2.0f / 0.09f)) / Ref);
+                slot(b, S_RMIU)[c] = (double)((float)ARTk / om * ro);
+            } else {
             float arg2 = 2.0f * sqrtf(kf / ro) / Bs / (of / ro) / DistN / Ref;
             arg2 = fmaxf(arg2, 500.0f * RmiuL / DistN / DistN / of / Ref / Ref);
             arg2 = tanhf(arg2 * arg2);
@@ -272,6 +285,7 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
             V5[c] = ARTk;
             V6[c] = ARTO;
             slot(b, S_RMIU)[c] = (double)(Cmua * (float)ARTk / of * ro);
+            }
         }
     }
     s_sum[0][tid] = sa; s_sum[1][tid] = sk; s_sum[2][tid] = so;
