@@ -205,7 +205,8 @@ def pinned_copy(arr):
 
 def run_e2e(s, c, st, ki0, steps):
     """Per step through the C ABI with host buffers: upload the state (V, PP, T, Rmiu, Wt0,
-    Wt1 as the Fortran caller holds them), iterate, download V, PP, T, Rmiu and the norms."""
+    Wt1 as the Fortran caller holds them, page-locked) with trans_set_fields, iterate, download
+    V, PP, T, Rmiu and the norms with trans_get_fields."""
     lib = s.lib
     keep = []
     up, down = [], []
@@ -226,16 +227,24 @@ def run_e2e(s, c, st, ki0, steps):
     norms = (abi.TransNorms * nb)()
     d2h += C.sizeof(norms)
     dp = C.POINTER(C.c_double)
+
+    def table(lst):      # the (block, field, array) lists as the arrays of trans_set/get_fields
+        n = len(lst)
+        ib, fid, ptr = (C.c_int * n)(), (C.c_int * n)(), (dp * n)()
+        for q, (b, f, a) in enumerate(lst):
+            ib[q], fid[q], ptr[q] = b, f, a.ctypes.data_as(dp)
+        return n, ib, fid, ptr
+    tu, td = table(up), table(down)
     lib.trans_sync(s.ctx)
     t0 = time.perf_counter()
     for q in range(steps):
-        for ib, fid, a in up:
-            lib.trans_set_field(s.ctx, ib, fid, a.ctypes.data_as(dp))
+        if lib.trans_set_fields(s.ctx, *tu) != 0:
+            raise RuntimeError("trans_set_fields failed")
         rc = lib.trans_iterate(s.ctx, ki0 + q, norms)
         if rc != 0:
             raise RuntimeError(f"iterate failed {rc}")
-        for ib, fid, a in down:
-            lib.trans_get_field(s.ctx, ib, fid, a.ctypes.data_as(dp))
+        if lib.trans_get_fields(s.ctx, *td) != 0:
+            raise RuntimeError("trans_get_fields failed")
     lib.trans_sync(s.ctx)
     dt = time.perf_counter() - t0
     return dt, h2d, d2h

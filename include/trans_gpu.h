@@ -175,6 +175,13 @@ int trans_destroy(void* ctx);         /* NULL is a no-op returning TRANS_OK */
 /* trans_set_field returns once the caller's array has been copied (it may be reused at once); the
  * transpose into the device layout completes in order before any later call's device work. */
 int trans_set_field(void* ctx, int ib, int field, const double* fortran_array);
+/* n trans_set_field / trans_get_field calls in one, (ib[q], field[q], arrays[q]) for q < n,
+ * with one synchronisation at the end: trans_set_fields returns once every array is copied,
+ * trans_get_fields once every array is filled.  Page-locked arrays (cudaHostAlloc,
+ * cudaHostRegister) are transposed in place over the host link, others through a device
+ * staging buffer; either way the layout is the Fortran one above. */
+int trans_set_fields(void* ctx, int n, const int* ib, const int* field, const double* const* arrays);
+int trans_get_fields(void* ctx, int n, const int* ib, const int* field, double* const* arrays);
 int trans_get_field(void* ctx, int ib, int field, double* fortran_array);
 /* One outer iteration KI (main.F90:48-197).  norms: array of nblocks entries, may be NULL. */
 int trans_iterate(void* ctx, int ki, trans_norms* norms);
@@ -245,6 +252,8 @@ int trans_batch_remove(void* ctx, int case_id);
 /* As trans_set_field / trans_get_field for block ib of one case. */
 int trans_batch_set_field(void* ctx, int case_id, int ib, int field, const double* fortran_array);
 int trans_batch_get_field(void* ctx, int case_id, int ib, int field, double* fortran_array);
+int trans_batch_set_fields(void* ctx, int case_id, int n, const int* ib, const int* field, const double* const* arrays);
+int trans_batch_get_fields(void* ctx, int case_id, int n, const int* ib, const int* field, double* const* arrays);
 /* n outer iterations of every case.  TRANS_E_NAN: some case produced a NaN (its norms carry
  * nan_flag); the iteration is complete and the caller removes that case. */
 int trans_batch_iterate(void* ctx, int n);

@@ -173,6 +173,12 @@ def bind_common(lib):
     lib.trans_batch_get_wall_cp.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
     lib.trans_wall_distance.argtypes = [C.c_longlong, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int),
                                         C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double)]
+    PP = C.POINTER(C.POINTER(C.c_double))
+    IP = C.POINTER(C.c_int)
+    lib.trans_set_fields.argtypes = [vp, C.c_int, IP, IP, PP]
+    lib.trans_get_fields.argtypes = [vp, C.c_int, IP, IP, PP]
+    lib.trans_batch_set_fields.argtypes = [vp, C.c_int, C.c_int, IP, IP, PP]
+    lib.trans_batch_get_fields.argtypes = [vp, C.c_int, C.c_int, IP, IP, PP]
     lib.trans_tuning.argtypes = [vp]
     lib.trans_tuning.restype = C.c_char_p
     lib.trans_last_error.argtypes = [vp]
@@ -188,5 +194,6 @@ EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field
             "trans_batch_remove", "trans_batch_set_field", "trans_batch_get_field", "trans_batch_iterate",
             "trans_batch_case_norms", "trans_batch_bytes_in_use", "trans_batch_cases", "trans_prepare",
             "trans_batch_time_iterations", "trans_get_integrals", "trans_get_wall_cp",
-            "trans_batch_get_integrals", "trans_batch_integrals", "trans_batch_get_wall_cp", "trans_wall_distance"]
+            "trans_batch_get_integrals", "trans_batch_integrals", "trans_batch_get_wall_cp", "trans_wall_distance",
+            "trans_set_fields", "trans_get_fields", "trans_batch_set_fields", "trans_batch_get_fields"]
 TRANS_NKCLASS = 16

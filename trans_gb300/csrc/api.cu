@@ -59,6 +59,16 @@ int trans_get_field(void* ctx, int ib, int f, double* a) {
     return c ? field_io(c, first_case(c), ib, f, a, false) : TRANS_E_ARG;
 }
 
+int trans_set_fields(void* ctx, int n, const int* ib, const int* field, const double* const* arrays) {
+    Ctx* c = as_ctx(ctx);
+    return c ? fields_io(c, first_case(c), n, ib, field, const_cast<double* const*>(arrays), true) : TRANS_E_ARG;
+}
+
+int trans_get_fields(void* ctx, int n, const int* ib, const int* field, double* const* arrays) {
+    Ctx* c = as_ctx(ctx);
+    return c ? fields_io(c, first_case(c), n, ib, field, arrays, false) : TRANS_E_ARG;
+}
+
 int trans_run_stage(void* ctx, int stage, int ki, int itr_chld) {
     Ctx* c = as_ctx(ctx);
     if (!c) return TRANS_E_ARG;

@@ -56,6 +56,22 @@ int trans_batch_get_field(void* ctx, int case_id, int ib, int field, double* a) 
     return field_io(c, cs, ib, field, a, false);
 }
 
+int trans_batch_set_fields(void* ctx, int case_id, int n, const int* ib, const int* field, const double* const* arrays) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return TRANS_E_ARG;
+    CaseRec* cs = case_find(c, case_id);
+    if (!cs) return fail(c, TRANS_E_ARG, "no such case");
+    return fields_io(c, cs, n, ib, field, const_cast<double* const*>(arrays), true);
+}
+
+int trans_batch_get_fields(void* ctx, int case_id, int n, const int* ib, const int* field, double* const* arrays) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return TRANS_E_ARG;
+    CaseRec* cs = case_find(c, case_id);
+    if (!cs) return fail(c, TRANS_E_ARG, "no such case");
+    return fields_io(c, cs, n, ib, field, arrays, false);
+}
+
 int trans_batch_iterate(void* ctx, int n) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c || n < 0) return TRANS_E_ARG;

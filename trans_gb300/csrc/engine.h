@@ -165,7 +165,11 @@ CaseRec* case_find(Ctx* c, int id);
 int rebuild(Ctx* c);
 int build_tiles(Ctx* c, int TI, int TJ, int TK);   // tiles of the tiled-wavefront sweep schedule
 void free_worklists(Ctx* c);
-int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload);
+// one Fortran array in or out; sync = false leaves the copy in flight (the caller synchronises
+// the stream before it reuses the array)
+int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload, bool sync = true);
+// n arrays in or out with one synchronisation at the end
+int fields_io(Ctx* c, CaseRec* cs, int n, const int* ib, const int* f, double* const* host, bool upload);
 int run_stage(Ctx* c, int stage, int itr);
 int upload_cdev(Ctx* c);
 // integrated quantities of one case from its current state (k_integrals.cu kernels)

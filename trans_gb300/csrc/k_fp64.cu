@@ -47,7 +47,7 @@ void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long lon
 
 namespace tg {
 void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, int lb, int is_sd, double* stage, int to_slots) {
-    long long n = (long long)(b.NI + 3 - lb) * (b.NJ + 3 - lb) * (b.NK + 3 - lb);
+    long long n = (long long)(b.NI + 3 - lb) * (b.NJ + 3 - lb) * (b.NK + 3 - lb) * ncomp;
     if (n > 0) k_field_xfer<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, slot0, ncomp, lb, is_sd, stage, to_slots);
 }
 }  // namespace tg

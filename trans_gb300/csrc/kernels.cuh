@@ -1661,18 +1661,21 @@ __global__ void k_geom_static(const DevBlock* __restrict__ blks, int nblk, long 
 namespace tg {
 #ifdef TG_COMMON_KERNELS
 // Fortran-layout (component fastest, lower bound lb) <-> slots, one thread per Fortran cell
+// one thread per element of the Fortran array (component fastest), so that the array side --
+// a staging buffer, or the caller's page-locked array over the host link -- is read and written
+// in whole consecutive lines
 __global__ void k_field_xfer(DevBlock b, int slot0, int ncomp, int lb, int is_sd, double* __restrict__ stage, int to_slots) {
     int ei = b.NI + 2 - lb + 1, ej = b.NJ + 2 - lb + 1, ek = b.NK + 2 - lb + 1;
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= (long long)ei * ej * ek) return;
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)ei * ej * ek * ncomp) return;
+    long long n = e / ncomp;
+    int m = (int)(e - n * ncomp);
     int i = (int)(n % ei), j = (int)((n / ei) % ej), k = (int)(n / ((long long)ei * ej));
     int c = cidx(b, i + lb, j + lb, k + lb);
-    for (int m = 0; m < ncomp; ++m) {
-        int so = is_sd ? 3 * (m % 3) + m / 3 : m;
-        double* sl = slot(b, slot0 + so);
-        if (to_slots) sl[c] = stage[n * ncomp + m];
-        else stage[n * ncomp + m] = sl[c];
-    }
+    int so = is_sd ? 3 * (m % 3) + m / 3 : m;
+    double* sl = slot(b, slot0 + so);
+    if (to_slots) sl[c] = stage[e];
+    else stage[e] = sl[c];
 }
 #endif  // TG_COMMON_KERNELS
 }  // namespace tg

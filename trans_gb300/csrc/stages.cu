@@ -2,6 +2,7 @@
 // main.F90:54-197, with the LU-SGS sweep schedules, the residual norms and field transfer.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <initializer_list>
 #include <utility>
@@ -155,7 +156,31 @@ int collect_norms(Ctx* c, const BlockNorms* hn) {
     return TRANS_OK;
 }
 
-int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
+namespace {
+
+// The device address of a page-locked host array of `bytes` bytes registered with this
+// device (cudaHostAlloc, cudaHostRegister), or null: the transpose kernel then reads or writes
+// the caller's array in place over the host link, with no staging copy.  Both ends of the
+// array must be page-locked host memory at a linear device mapping.
+double* mapped_host(const double* host, size_t bytes) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    cudaPointerAttributes a0{}, a1{};
+    const char* last = (const char*)host + bytes - 1;
+    if (cudaPointerGetAttributes(&a0, host) != cudaSuccess || cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+        return nullptr;
+    if (a0.device != dev || a1.device != dev) return nullptr;
+    if ((const char*)a1.devicePointer - (const char*)a0.devicePointer != (std::ptrdiff_t)(bytes - 1)) return nullptr;
+    return (double*)a0.devicePointer;
+}
+
+}  // namespace
+
+int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload, bool sync) {
     if (!c || !cs || ib < 0 || ib >= (int)cs->blk.size() || !host) return TRANS_E_ARG;
     FieldMap fm = field_map(f);
     if (fm.slot < 0) return fail(c, TRANS_E_ARG, "bad field id");
@@ -171,6 +196,26 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
     size_t ncells = (size_t)(b.NI + 3 - fm.lb) * (b.NJ + 3 - fm.lb) * (b.NK + 3 - fm.lb);
     size_t bytes = ncells * fm.ncomp * sizeof(double);
     cudaStream_t s = c->stream;
+    int is_sd = f == TRANS_SD ? 1 : 0;
+    double* mapped = f == TRANS_THTC ? nullptr : mapped_host(host, bytes);
+    if (mapped) {       // page-locked caller array: transpose in place over the host link
+        if (!upload) {
+            if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}}, 1);
+            if (c->mixed && f == TRANS_DQDXYZ) mirror(c, {{S_DQ, 18}}, 1);
+            if (c->mixed && f == TRANS_SHOCK) mirror(c, {{S_SHOCK, 1}}, 1);
+        }
+        launch_field_xfer(s, b, fm.slot, fm.ncomp, fm.lb, is_sd, mapped, upload ? 1 : 0);
+        c->launches++;
+        if (upload) {
+            if (is_geometry(f)) cs->geom_dirty = true;
+            if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}});
+            if (c->mixed && f == TRANS_DQDXYZ) mirror(c, {{S_DQ, 18}});
+            if (c->mixed && f == TRANS_SHOCK) mirror(c, {{S_SHOCK, 1}});
+        }
+        CK(cudaGetLastError());
+        if (sync) CK(cudaStreamSynchronize(s));
+        return TRANS_OK;
+    }
     if (!c->d_stage || c->stage_doubles < ncells * fm.ncomp) {          // staging for the largest field so far
         CK(cudaStreamSynchronize(s));
         if (c->d_stage) cudaFree(c->d_stage);
@@ -181,7 +226,6 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
         CK(cudaMalloc(&c->d_stage, mx * sizeof(double)));
         c->stage_doubles = mx;
     }
-    int is_sd = f == TRANS_SD ? 1 : 0;
     if (upload) {
         CK(cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, s));
         if (!c->copy_done) CK(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
@@ -204,7 +248,7 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
         // the caller's buffer is free once the copy is done; the transpose into the slots runs
         // on in stream order (later copies into the staging buffer queue behind it)
         CK(cudaGetLastError());
-        CK(cudaEventSynchronize(c->copy_done));
+        if (sync) CK(cudaEventSynchronize(c->copy_done));
         return TRANS_OK;
     } else {
         // the mixed path keeps DeltaQ, the gradients and the shock sensor in FP32
@@ -216,7 +260,7 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload) {
         CK(cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, s));
     }
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(s));
+    if (sync) CK(cudaStreamSynchronize(s));
     return TRANS_OK;
 }
 
@@ -752,6 +796,19 @@ int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp) {
     c->launches++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(cp, c->d_stage, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return TRANS_OK;
+}
+
+int fields_io(Ctx* c, CaseRec* cs, int n, const int* ib, const int* f, double* const* host, bool upload) {
+    if (!c || !cs || n < 0 || (n > 0 && (!ib || !f || !host))) return TRANS_E_ARG;
+    for (int q = 0; q < n; ++q) {
+        int rc = field_io(c, cs, ib[q], f[q], host[q], upload, false);
+        if (rc) {
+            cudaStreamSynchronize(c->stream);    // the arrays already queued are settled either way
+            return rc;
+        }
+    }
     CK(cudaStreamSynchronize(c->stream));
     return TRANS_OK;
 }
