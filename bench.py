@@ -69,7 +69,7 @@ def replica_rate(units_per_rank, seconds, world):
     return units_per_rank * world / seconds / 1e6
 
 
-def make_case(name, precision, nk=64, dst_fn=None):
+def make_case(name, precision, nk=64, metrics_fn=None):
     prec = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
     if name == "channel":
         c = cases.channel_bump(precision=prec)
@@ -79,7 +79,7 @@ def make_case(name, precision, nk=64, dst_fn=None):
         c = cases.square_cylinder(precision=prec)
     else:
         raise SystemExit(f"unknown case {name}")
-    conns, geo = CS.compute_geometry(c, dst_fn=dst_fn)
+    conns, geo = CS.compute_geometry(c, metrics_fn=metrics_fn)
     st = CS.initial_state(c, geo, Q_dst=c.meta.get("Q_dst", 0.01))
     return c, conns, geo, st
 
@@ -336,7 +336,7 @@ def batch_levels_arm(args):
     grid, so each level's geometry is computed once per angle), all in one batch context under
     the device budget; aggregate cell-iterations/s timed like the single case."""
     from trans_gb300 import serving
-    from trans_gb300.solver import Batch, device_wall_distance
+    from trans_gb300.solver import Batch, device_block_metrics
     prec = abi.TRANS_MIXED if args.precision == "mixed" else abi.TRANS_FP64
     counts = [int(x) for x in args.batch_levels.split(",")]
     rng = np.random.default_rng(0)
@@ -352,7 +352,7 @@ def batch_levels_arm(args):
             key = (level, angle)
             c = cases.cascade(inflow_deg=angle, p_ratio=ratio, precision=prec, **kw)
             if key not in geoms:
-                conns, geo = CS.compute_geometry(c, dst_fn=device_wall_distance(bt.lib))
+                conns, geo = CS.compute_geometry(c, metrics_fn=device_block_metrics(bt.lib))
                 geoms[key] = (conns, geo, CS.initial_state(c, geo, Q_dst=c.meta.get("Q_dst", 0.01)))
             conns, geo, st = geoms[key]
             if bt.add(c, conns, geo, st) is None:
@@ -439,8 +439,8 @@ def main():
     if args.case == "cascade" and not hasattr(cases, "cascade"):
         args.case = "channel"
     rank, world = init_replicas()
-    from trans_gb300.solver import device_wall_distance
-    c, conns, geo, st = make_case(args.case, args.precision, args.nk, dst_fn=device_wall_distance())
+    from trans_gb300.solver import device_block_metrics
+    c, conns, geo, st = make_case(args.case, args.precision, args.nk, metrics_fn=device_block_metrics())
     ncell = interior_cells(c)
     nsub = sub_iterations(c)
     s = Solver(c, conns, geo, st)

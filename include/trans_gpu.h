@@ -229,6 +229,20 @@ int trans_get_wall_cp(void* ctx, int ib, int iconn, double* cp);
  */
 int trans_wall_distance(long long n, const double* xyz, int nsurf, const int* dims, const double* nodes,
                         double tiny, double* dst);
+/*
+ * GEOM_CalcDST (Geom/CalcDst.F90:95-521) of one block on the device (no context): from the
+ * block's nodes (xyz: X(ni,nj,nk), then Y, then Z, Fortran order) and the wall surfaces (as for
+ * trans_wall_distance), the cell centres Xc/Yc/Zc with the boundary face centres in the first
+ * ghost layer, thtc and rad, the wall distance Dst, SD and Grad of every face (face 0 = face 1),
+ * Alagm, aLeng/aSeng and Vol of every interior cell.  out: 24 arrays of (ni+5)(nj+5)(nk+5)
+ * doubles (index -2..n+2 per direction, i fastest), zero where not computed, in the order Xc,
+ * Yc, Zc, Dst, aLeng, aSeng, Vol, rad, thtc, SD(dir 1..3, comp 1..3), Grad(1..3),
+ * Alagm(1..3).  The corner centres and ghost copies of :530-640 are left to the caller.  Every
+ * value equals a CPU evaluation of the reference's expressions (no contraction).
+ * TRANS_E_ARG for a negative volume (message in trans_last_error(NULL)).
+ */
+int trans_block_metrics(int ni, int nj, int nk, const double* xyz, int nsurf, const int* dims, const double* nodes,
+                        double tiny, double* out);
 /* Device bytes held by the context. */
 long long trans_device_bytes(void* ctx);
 /* Kernel launches issued since the context was created (all kernels of this library). */

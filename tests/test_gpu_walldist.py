@@ -51,3 +51,31 @@ def test_geometry_with_device_wall_distance_equals_host(gpu_lib):
     for b in c.blocks:
         for name in geo_h[b.id]:
             assert np.array_equal(geo_h[b.id][name], geo_d[b.id][name]), (b.id, name)
+
+
+@pytest.mark.parametrize("which", ["channel", "cascade", "cylinder", "serving_coarse"])
+def test_block_metrics_on_device_equal_host(gpu_lib, which):
+    """trans_block_metrics (centres, thtc, rad, Dst, SD/Grad, Alagm, boundary face centres,
+    aLeng/aSeng, Vol) plus the host's corner and ghost fill-in: every geometry array of the
+    set-up bit-identical to the host code."""
+    from trans_gb300 import case as CS
+    from trans_gb300 import cases
+    from trans_gb300.serving import LEVELS
+    from trans_gb300.solver import device_block_metrics
+    if which == "channel":
+        c = cases.channel_bump(25, 17, 6)
+    elif which == "cascade":
+        from helpers import SMALL_CASCADE
+        c = cases.cascade(**SMALL_CASCADE)
+    elif which == "cylinder":
+        c = cases.square_cylinder(ni=49, nj=33, nk=9)
+    else:
+        c = cases.cascade(**LEVELS["coarse"])
+    conns_h, geo_h = CS.compute_geometry(c)
+    conns_d, geo_d = CS.compute_geometry(c, metrics_fn=device_block_metrics(gpu_lib))
+    for b in c.blocks:
+        assert set(geo_h[b.id]) == set(geo_d[b.id])
+        for name in geo_h[b.id]:
+            a, d = geo_h[b.id][name], geo_d[b.id][name]
+            assert a.shape == d.shape, (b.id, name)
+            assert np.array_equal(a.view(np.int64), d.view(np.int64)), (b.id, name)

@@ -92,3 +92,16 @@ def test_wall_distance_rejects_bad_input_before_device_work(lib):
                                  nodes.ctypes.data_as(P), 1e-20, out.ctypes.data_as(P))
     assert rc == abi.TRANS_E_ARG
     assert lib.trans_wall_distance(0, None, 0, None, None, 1e-20, None) == abi.TRANS_OK
+
+
+def test_block_metrics_rejects_bad_input_before_device_work(lib):
+    from trans_gb300 import abi
+    P = C.POINTER(C.c_double)
+    nodes = np.zeros(3 * 4 * 4 * 4)
+    nodes[5] = np.inf
+    out = np.zeros(24 * 9 * 9 * 9)
+    rc = lib.trans_block_metrics(4, 4, 4, nodes.ctypes.data_as(P), 0, None, None, 1e-20, out.ctypes.data_as(P))
+    assert rc == abi.TRANS_E_ARG
+    assert b"not finite" in lib.trans_last_error(None)
+    rc = lib.trans_block_metrics(2, 4, 4, nodes.ctypes.data_as(P), 0, None, None, 1e-20, out.ctypes.data_as(P))
+    assert rc == abi.TRANS_E_ARG

@@ -24,7 +24,7 @@ UNITS = {
     "batch.cu": ["-fmad=false"],
     "k_fp64.cu": ["-fmad=false"],
     "k_integrals.cu": ["-fmad=false"],
-    "k_walldist.cu": ["-fmad=false"],
+    "k_geometry.cu": ["-fmad=false"],
     "k_mixed.cu": ["-fmad=true"],
 }
 

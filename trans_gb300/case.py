@@ -365,10 +365,19 @@ def wall_distance(xc, yc, zc, surfaces, tiny=1.0e-20):
     return np.sqrt(dmin).reshape(xc.shape)
 
 
-def block_metrics(b, surfaces, tiny=1.0e-20, dst_fn=None):
+def block_metrics(b, surfaces, tiny=1.0e-20, dst_fn=None, metrics_fn=None):
     """GEOM_CalcDST for one block (Geom/CalcDst.F90:28-719).  dst_fn: the wall-distance
     function (default: `wall_distance` on the host; trans_gb300.solver.device_wall_distance
-    evaluates the same minimum on the GPU)."""
+    evaluates the same minimum on the GPU).  metrics_fn: centres, wall distance, SD/Grad,
+    Alagm, boundary face centres, aLeng/aSeng and Vol of the block in one call
+    (trans_gb300.solver.device_block_metrics runs them on the GPU; default: the host code
+    below); the corner centres and ghost copies follow on the host either way."""
+    NI, NJ, NK = b.dims
+    g = metrics_fn(b, surfaces, tiny) if metrics_fn is not None else _block_metrics_host(b, surfaces, tiny, dst_fn)
+    return _corners_and_ghosts(g, NI, NJ, NK)
+
+
+def _block_metrics_host(b, surfaces, tiny, dst_fn):
     NI, NJ, NK = b.dims
     NI1, NJ1, NK1 = NI - 1, NJ - 1, NK - 1
     XX, YY, ZZ = (np.asfortranarray(b.xyz[..., q]) for q in range(3))
@@ -511,6 +520,13 @@ def block_metrics(b, surfaces, tiny=1.0e-20, dst_fn=None):
     g["VOL"][c0] = C13 * OMG
     if np.any(g["VOL"][c0] < tiny):
         raise ValueError(f"block {b.id}: negative volume")
+    return g
+
+
+def _corners_and_ghosts(g, NI, NJ, NK):
+    NI1, NJ1, NK1 = NI - 1, NJ - 1, NK - 1
+    ci, cj, ck = slice(G + 1, G + NI), slice(G + 1, G + NJ), slice(G + 1, G + NK)
+    Xc, Yc, Zc, SD, Al = g["XC"], g["YC"], g["ZC"], g["SD"], g["ALAGM"]
     # corner centres (Geom/CalcDst.F90:530-581)
     for Cc in (Xc, Yc, Zc):
         for j in range(1, NJ1 + 1):
@@ -667,13 +683,13 @@ def geom_transform1(blocks, conns, geo):
                     SD[(d, q) + lf] = 2.0 * SD[(d, q) + f0] - SD[(d, q) + sf]
 
 
-def compute_geometry(case, dst_fn=None):
+def compute_geometry(case, dst_fn=None, metrics_fn=None):
     """All metrics of a case: CalcDst per block, then GeomTransform and GeomTransform1.
-    dst_fn: wall-distance function (see block_metrics)."""
+    dst_fn, metrics_fn: see block_metrics."""
     conns = derive_connectivity(case.blocks)
     ph = case.physical
     set_rotate_angles(conns, case.blocks, ph.nblade if ph else 1, ph.npassage if ph else 1)
-    geo = {b.id: block_metrics(b, case.surfaces, case.params.Tiny, dst_fn) for b in case.blocks}
+    geo = {b.id: block_metrics(b, case.surfaces, case.params.Tiny, dst_fn, metrics_fn) for b in case.blocks}
     geom_transform(case.blocks, conns, geo)
     geom_transform1(case.blocks, conns, geo)
     return conns, geo

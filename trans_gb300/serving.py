@@ -20,7 +20,7 @@ import numpy as np
 from . import abi
 from . import case as CS
 from . import cases
-from .solver import Batch, device_wall_distance, global_residual
+from .solver import Batch, device_block_metrics, global_residual
 
 # grid levels of the cascade topology: (ns, nr, nh, nk) for about 0.35 M, 1.36 M and 5.4 M cells
 # grid levels: coarse ~0.35 M, medium 1.36 M, fine ~5.5 M cells.  The fine level also doubles the
@@ -73,15 +73,16 @@ def poisson_requests(rate=4.0, duration=60.0, seed=0, mix=(("coarse", 0.6), ("me
     return out
 
 
-def build_case(req, precision, dst_fn=None):
-    """Set-up of one request: grid, connectivity, geometry (wall distance by dst_fn: on the
-    GPU when given, else on the host) and initial field; records its duration in req.setup_s."""
+def build_case(req, precision, metrics_fn=None):
+    """Set-up of one request: grid, connectivity, geometry (the block metrics and wall
+    distance by metrics_fn: on the GPU when given, else on the host) and initial field; records
+    its duration in req.setup_s."""
     t0 = time.perf_counter()
     kw = dict(LEVELS.get(req.level, {}))
     kw.update(RAMP)
     kw.update(req.grid)
     c = cases.cascade(XM=req.mach, p_ratio=req.p_ratio, precision=precision, **kw)
-    conns, geo = CS.compute_geometry(c, dst_fn=dst_fn)
+    conns, geo = CS.compute_geometry(c, metrics_fn=metrics_fn)
     st = CS.initial_state(c, geo, Q_dst=c.meta.get("Q_dst", 0.01))
     req.setup_s = time.perf_counter() - t0
     return c, conns, geo, st
@@ -97,7 +98,7 @@ def serve(requests, precision=abi.TRANS_MIXED, budget_bytes=0, drop=1.0e-6, max_
     when its global residual (block RMS norms of TIME_Update_V aggregated over blocks) has
     dropped by `drop` from its first iteration, after `max_iters` iterations, or on a NaN."""
     bt = Batch(precision, budget_bytes, lib)
-    dst_fn = device_wall_distance(bt.lib) if device_setup else None
+    metrics_fn = device_block_metrics(bt.lib) if device_setup else None
     pending = sorted(requests, key=lambda r: r.arrival)
     prepping, ready, active = {}, [], {}
     done = []
@@ -129,7 +130,7 @@ def serve(requests, precision=abi.TRANS_MIXED, budget_bytes=0, drop=1.0e-6, max_
             t = now()
             while pending and pending[0].arrival <= t:
                 r = pending.pop(0)
-                prepping[r.rid] = (r, ex.submit(build_case, r, precision, dst_fn))
+                prepping[r.rid] = (r, ex.submit(build_case, r, precision, metrics_fn))
             for rid in sorted(prepping):
                 r, f = prepping[rid]
                 if f.done():

@@ -300,3 +300,51 @@ def device_wall_distance(lib=None):
         lib = native.load()
     return lambda xc, yc, zc, surfaces, tiny: wall_distance_gpu(lib, xc, yc, zc, surfaces, tiny)
 
+
+
+_GEO_SCALARS = ("XC", "YC", "ZC", "DST", "ALENG", "ASENG", "VOL", "RAD", "THTC")
+
+
+def block_metrics_gpu(lib, b, surfaces, tiny):
+    """trans_block_metrics: cell centres, thtc/rad, wall distance, SD/Grad, Alagm, boundary face
+    centres, aLeng/aSeng and Vol of one block (Geom/CalcDst.F90:95-521) on the GPU, as the
+    arrays of trans_gb300.case.block_metrics before its corner and ghost fill-in."""
+    ni, nj, nk = b.dims
+    nodes = np.concatenate([np.asfortranarray(b.xyz[..., q]).ravel(order="F") for q in range(3)])
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    dims = np.array([d for S in surfaces for d in S.shape[:2]], dtype=np.int32)
+    snodes = np.concatenate([S[..., q].ravel(order="F") for S in surfaces for q in range(3)]) if surfaces else np.zeros(1)
+    snodes = np.ascontiguousarray(snodes, dtype=np.float64)
+    shape = (ni + 5, nj + 5, nk + 5)
+    P = int(np.prod(shape))
+    out = np.zeros(24 * P)
+    dp = C.POINTER(C.c_double)
+    rc = lib.trans_block_metrics(ni, nj, nk, nodes.ctypes.data_as(dp), len(surfaces),
+                                 dims.ctypes.data_as(C.POINTER(C.c_int)), snodes.ctypes.data_as(dp), float(tiny),
+                                 out.ctypes.data_as(dp))
+    if rc != 0:
+        m = lib.trans_last_error(None)
+        msg = m.decode() if m else ""
+        if "negative volume" in msg:
+            raise ValueError(f"block {b.id}: negative volume")
+        raise SolverError(f"trans_block_metrics failed ({rc}: {abi.ERRORS.get(rc, '?')}) {msg}")
+    f = lambda q: out[q * P:(q + 1) * P].reshape(shape, order="F")
+    g = {n: np.asfortranarray(f(q)) for q, n in enumerate(_GEO_SCALARS)}
+    g["SD"] = np.zeros((3, 3) + shape, order="F")
+    for d in range(3):
+        for c in range(3):
+            g["SD"][d, c] = f(9 + 3 * d + c)
+    g["GRAD"] = np.zeros((3,) + shape, order="F")
+    g["ALAGM"] = np.zeros((3,) + shape, order="F")
+    for d in range(3):
+        g["GRAD"][d] = f(18 + d)
+        g["ALAGM"][d] = f(21 + d)
+    return g
+
+
+def device_block_metrics(lib=None):
+    """A metrics_fn for trans_gb300.case.compute_geometry that runs the block metrics on the GPU."""
+    if lib is None:
+        from . import native
+        lib = native.load()
+    return lambda b, surfaces, tiny: block_metrics_gpu(lib, b, surfaces, tiny)
