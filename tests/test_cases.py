@@ -97,3 +97,19 @@ def test_square_cylinder_grid():
     V = st[c.blocks[0].id]["V"]
     u = V[1][3:3 + 32, 8:3 + 16, 3:3 + 8] / V[0][3:3 + 32, 8:3 + 16, 3:3 + 8]
     assert 0.002 < np.std(u) < 0.05
+
+
+def test_annular_sector_rotational_periodicity():
+    """The annular sector's periodic faces carry rotateAngle = +-sector and the oracle runs it."""
+    import numpy as np
+    from oracle.oracle import OracleSolver
+    from trans_gb300 import case as C
+    from trans_gb300 import cases
+    c = cases.annular_sector(ni=13, nj=9, nk=6)
+    conns, geo = C.compute_geometry(c)
+    angles = sorted(cn.rotateAngle for cn in conns[1] if cn.BCType == 9)
+    assert np.allclose(angles, [-np.pi / 18, np.pi / 18], rtol=1e-12)
+    st = C.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
+    o = OracleSolver(c, conns, geo, st)
+    h = [o.iterate(k)[0]["DRSa"] for k in range(1, 6)]
+    assert np.all(np.isfinite(h))
