@@ -99,3 +99,34 @@ def test_fields_reject_bad_entries(gpu_lib):
     assert gpu_lib.trans_get_fields(s.ctx, *_table([(0, 99, a)])) == abi.TRANS_E_ARG
     assert gpu_lib.trans_get_fields(s.ctx, 0, None, None, None) == abi.TRANS_OK
     s.close()
+
+
+def test_batch_fields_match_single_case(gpu_lib):
+    """trans_batch_set_fields / trans_batch_get_fields on one case of a batch context."""
+    from trans_gb300 import abi
+    from trans_gb300.solver import Batch
+    bt = Batch(abi.TRANS_FP64, lib=gpu_lib)
+    a = small_cascade(Kind_Spatial=3, Kind_Roe=3)
+    cid = bt.add(*a)
+    other = bt.add(*small_cascade(Kind_Spatial=2, Kind_Roe=1))
+    bt.iterate(2)
+    keep, items, ref = [], [], []
+    for ib, b in enumerate(a[0].blocks):
+        for name in ("V", "PP", "RMIU"):
+            p, t = _pinned(abi.field_shape(name, *b.dims))
+            keep.append(t)
+            items.append((ib, abi.FIELD_ID[name], p))
+            ref.append(bt.get_field(cid, ib, name, full=False))
+    assert gpu_lib.trans_batch_get_fields(bt.ctx, cid, *_table(items)) == 0
+    for (ib, f, p), r in zip(items, ref):
+        assert np.array_equal(p.view(np.int64), r.view(np.int64)), (ib, abi.FIELDS[f])
+    # write the arrays back scaled into the other order and read them again
+    for _, _, p in items:
+        p *= 1.0
+    assert gpu_lib.trans_batch_set_fields(bt.ctx, cid, *_table(items)) == 0
+    for (ib, f, p), r in zip(items, ref):
+        back = bt.get_field(cid, ib, abi.FIELDS[f], full=False)
+        assert np.array_equal(back.view(np.int64), r.view(np.int64)), (ib, abi.FIELDS[f])
+    assert gpu_lib.trans_batch_get_fields(bt.ctx, 12345, *_table(items[:1])) == abi.TRANS_E_ARG
+    assert bt.norms(other)[0] == 2
+    bt.close()
