@@ -81,6 +81,9 @@ const FluxLaunchers& flux_launchers_f64();
 const FluxLaunchers& flux_launchers_f32();
 
 constexpr int FACE_TILE = 128;
-constexpr int SWEEP_CTA = 128;
+#ifndef TG_SWEEP_CTA
+#define TG_SWEEP_CTA 128
+#endif
+constexpr int SWEEP_CTA = TG_SWEEP_CTA;    // threads per CTA of the hyperplane sweep launches
 constexpr unsigned SWEEP_SPIN_LIMIT = 1u << 22;     // polls of one wait before it gives up (~1 s)
 }  // namespace tg
