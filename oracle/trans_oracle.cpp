@@ -65,7 +65,7 @@ struct Blk {
     std::vector<int> mw[6];     // MARKWALL arrays, Fortran (n1,n2) column-major
     int mwn1[6];
     Arr V, PP, T, Rmiu, Wt0, Wt1, Wt2, SD, Grad, Vol, Alagm, Dst, ALeng, ASeng, Xc, Yc, Zc, rad, thtc;
-    Arr D, Rds, Dtm, DQ, shock, F, VL, VR, rccl, rccr, FunDES;
+    Arr D, Rds, Dtm, DQ, shock, F, VL, VR, rccl, rccr, FunDES, Fsch;
     trans_norms nrm;
     int markwall(int face, int a, int b) const {
         if (mw[face].empty()) return 0;
@@ -670,6 +670,37 @@ void spaceinterp(Ctx& c, Blk& b) {
 // extrapolation; the first-ghost-layer gradients of :77-230 are overwritten by
 // BC_Boundarys(0) on every boundary face cell and are not restated)
 // ---------------------------------------------------------------------------------------
+// The hybrid blend Fscheme of one interior cell (Space/DIFF_DqDxyz.F90:311-380), read only by
+// the rotated Roe scheme: CH1 = 3, CH2 = 1, CH3 = 2, cmu = 0.09, tau = 1
+// (Module_Global.F90:64,105-106,124); real exponents 2 and 3 are products, 0.5 a square root
+double fscheme(const trans_params& p, Blk& b, int I, int J, int K, double W12, double W13, double W23, double Vort) {
+    (void)W12; (void)W13; (void)W23;
+    double DuDx = b.DQ(1, I, J, K), DuDy = b.DQ(2, I, J, K), DuDz = b.DQ(3, I, J, K);
+    double DvDx = b.DQ(4, I, J, K), DvDy = b.DQ(5, I, J, K), DvDz = b.DQ(6, I, J, K);
+    double DwDx = b.DQ(7, I, J, K), DwDy = b.DQ(8, I, J, K), DwDz = b.DQ(9, I, J, K);
+    double S11 = (DuDx + DuDx) / 2., S22 = (DvDy + DvDy) / 2., S33 = (DwDz + DwDz) / 2.;
+    double S12 = (DuDy + DvDx) / 2., S13 = (DuDz + DwDx) / 2., S23 = (DwDy + DvDz) / 2.;
+    double Skl = std::sqrt(2. * (1. * S11 * S11 + 1. * S22 * S22 + 1. * S33 * S33 + 2. * S12 * S12 + 2. * S13 * S13 + 2. * S23 * S23));
+    double Den = b.V(1, I, J, K), RmiuT = b.Rmiu(I, J, K), TT = b.T(I, J, K);
+    double RMIUL = (1. + p.Csthlnd) / (TT * p.Csth1 + p.Csthlnd) * p15(p.Csth1 * TT);
+    double vK = b.V(6, I, J, K) / Den, vOmega = b.V(7, I, J, K) / Den;
+    double DLTxyz = b.ALeng(I, J, K);
+    double dTKO = b.DQ(13, I, J, K) * b.DQ(16, I, J, K) + b.DQ(14, I, J, K) * b.DQ(17, I, J, K) + b.DQ(15, I, J, K) * b.DQ(18, I, J, K);
+    double Dist = b.Dst(I, J, K);
+    double CDKO = std::max(2.0 * Den * p.Sigo2 / vOmega * (dTKO), 1.0e-10);
+    double arg1 = std::max(std::sqrt(vK) / p.Beta_star / vOmega / Dist / p.Ref, 500.0 * RMIUL / Den / Dist / Dist / vOmega / p.Ref / p.Ref);
+    arg1 = std::min(arg1, 4.0 * Den * p.Sigo2 * vK / CDKO / Dist / Dist);
+    double a2 = arg1 * arg1;
+    double FunC1 = otm::tanh_(a2 * a2);
+    double aLgrd = ((1. - FunC1) * 0.61 + FunC1 * 0.78) * DLTxyz;
+    double B0 = 2. * Vort * std::max(Vort, Skl) / std::max((Vort * Vort + Skl * Skl) / 2., p.Alscale * 0.1);
+    double g0 = otm::tanh_(B0 * B0 * B0 * B0);
+    double sok = std::max(std::sqrt((Vort * Vort + Skl * Skl) / 2.), 0.1 / 1.0);
+    double alturb = std::sqrt((RmiuT + RMIUL) / Den / (p.Ref * sok * p15(0.09)));
+    double A0 = 1. * std::max(((aLgrd / alturb / g0) - 0.1), 0.0);
+    return std::max(1. * otm::tanh_(A0 * A0 * A0), p.F_limiter1);
+}
+
 void diff_dqdxyz(Ctx& c, Blk& b) {
     for (int k = 1; k <= b.NK1; ++k)
     for (int j = 1; j <= b.NJ1; ++j)
@@ -712,6 +743,18 @@ void diff_dqdxyz(Ctx& c, Blk& b) {
         double Vort = std::sqrt(2.0 * (2.0 * W12 * W12 + 2.0 * W13 * W13 + 2.0 * W23 * W23));
         double DivU = std::sqrt(DuDx * DuDx + DvDy * DvDy + DwDz * DwDz);
         b.shock(I, J, K) = DivU * DivU / std::max(DivU * DivU + Vort * Vort, 1.0);
+        if (c.p.Kind_Roe == 2) b.Fsch(I, J, K) = fscheme(c.p, b, I, J, K, W12, W13, W23, Vort);
+    }
+    if (c.p.Kind_Roe == 2) {    // the face-adjacent ghosts of Fscheme (:399-404)
+        for (int k = 1; k <= b.NK1; ++k) for (int j = 1; j <= b.NJ1; ++j) {
+            b.Fsch(0, j, k) = b.Fsch(1, j, k); b.Fsch(b.NI, j, k) = b.Fsch(b.NI1, j, k);
+        }
+        for (int k = 1; k <= b.NK1; ++k) for (int i = 1; i <= b.NI1; ++i) {
+            b.Fsch(i, 0, k) = b.Fsch(i, 1, k); b.Fsch(i, b.NJ, k) = b.Fsch(i, b.NJ1, k);
+        }
+        for (int j = 1; j <= b.NJ1; ++j) for (int i = 1; i <= b.NI1; ++i) {
+            b.Fsch(i, j, 0) = b.Fsch(i, j, 1); b.Fsch(i, j, b.NK) = b.Fsch(i, j, b.NK1);
+        }
     }
     // shock extrapolation into three ghost layers, whole planes in the reference's order
     int lo = -2, hi_i = b.NI + 2, hi_j = b.NJ + 2, hi_k = b.NK + 2;
@@ -1226,6 +1269,88 @@ void ausmpw_common(const trans_params& p, double PLo, double PRo, double TLo, do
     out[4] = (-1) * MMaL_plus * Acc * DENLo * HLo - MMaR_neg * Acc * DENRo * HRo;
 }
 
+// Roe_Common of the rotated scheme (Space/CONVECT_Roe_Rotated.F90:597-752), non-preconditioned:
+// adds 0.5 |A| dQ along (sav1..3)/sav, times sav and the face blend Funscheme, to dr[0..4]
+void roe_rot_common(const trans_params& p, double PLo, double PRo, double TLo, double TRo, double ULo, double URo,
+                    double VLo, double VRo, double WLo, double WRo, double sav1, double sav2, double sav3, double sav,
+                    double Funscheme, double* dr) {
+    double rcpcv = p.PPF;
+    double DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
+    const double ga = 1.4, ga1 = 0.4;
+    double VAMLo = ULo * ULo + VLo * VLo + WLo * WLo, VAMRo = URo * URo + VRo * VRo + WRo * WRo;
+    const double rLo = 0.0, rRo = 0.0;          // rccl/rccr * omega, omega = 0
+    double HLo = PLo * ga / (DENLo * ga1) + 0.5 * VAMLo - 0.5 * (rLo * rLo);
+    double HRo = PRo * ga / (DENRo * ga1) + 0.5 * VAMRo - 0.5 * (rRo * rRo);
+    double rrorl = std::sqrt(DENRo / DENLo), rrorlp1 = 1.0 + rrorl;
+    double rm = std::sqrt(DENRo * DENLo);
+    double um = (ULo + URo * rrorl) / rrorlp1, vm = (VLo + VRo * rrorl) / rrorlp1, wm = (WLo + WRo * rrorl) / rrorlp1;
+    double hm = (HLo + HRo * rrorl) / rrorlp1;
+    double vm2 = um * um + vm * vm + wm * wm;
+    double rccm = (rLo + rRo * rrorl) / rrorlp1;
+    double am2 = ga1 * std::fabs(hm - 0.5 * vm2 + 0.5 * (rccm * rccm));
+    double am = std::sqrt(am2);
+    double sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
+    double unormaln = (sav1n * um + sav2n * vm + sav3n * wm);
+    double anormaln = am;
+    double eig1 = std::fabs(unormaln), eig2 = std::fabs(unormaln + anormaln), eig3 = std::fabs(unormaln - anormaln);
+    const double alf = 0.0, ubetac2 = 1.0;
+    double amrev = am;
+    double dunormaln = (sav1n * (URo - ULo) + sav2n * (VRo - VLo) + sav3n * (WRo - WLo));
+    double astar = (eig2 + eig3) / 2.0;
+    double Mstar = (eig2 - eig3) / 2.0 / amrev;
+    double dW1 = DENRo - DENLo, dU1 = URo - ULo, dU2 = VRo - VLo, dU3 = WRo - WLo, dP1 = PRo - PLo;
+    double dW2 = rm * dU1 + dW1 * um, dW3 = rm * dU2 + dW1 * vm, dW4 = rm * dU3 + dW1 * wm;
+    double dW5 = dP1 / ga1 + 0.5 * vm2 * dW1 + rm * um * dU1 + rm * vm * dU2 + rm * wm * dU3;
+    double dUroe = Mstar * dunormaln + (astar - (1 - 2.0 * alf) * eig1 - alf * unormaln * Mstar) * (PRo - PLo) / rm / (ubetac2 * am2);
+    double dProe = Mstar * (PRo - PLo) + (astar - eig1 + alf * unormaln * Mstar) * rm * dunormaln;
+    double d1[5] = {eig1 * dW1 + dUroe * rm, eig1 * dW2 + dUroe * rm * um + dProe * sav1n,
+                    eig1 * dW3 + dUroe * rm * vm + dProe * sav2n, eig1 * dW4 + dUroe * rm * wm + dProe * sav3n,
+                    eig1 * dW5 + dUroe * rm * hm + dProe * unormaln};
+    for (int L = 0; L < 5; ++L) dr[L] = dr[L] + 0.5 * d1[L] * sav * Funscheme;
+}
+
+// CONVECT_Roe_Rotated (Space/CONVECT_Roe_Rotated.F90:59-591): central flux along the face
+// normal, then Roe dissipation along the velocity-jump direction n1 and along the rest of the
+// face vector (one direction when the jump is below Tiny).  The grid velocities vibc, vjbc,
+// vkbc that the reference reads uninitialised (:169, :332, :510) are taken as 0.
+void roe_rotated(const trans_params& p, double PLo, double PRo, double TLo, double TRo, double ULo, double URo,
+                 double VLo, double VRo, double WLo, double WRo, double sav1, double sav2, double sav3, double sav,
+                 double Funscheme, double* dr) {
+    double rcpcv = p.PPF;
+    double DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
+    const double ga = 1.4, ga1 = 0.4;
+    double VAMLo = ULo * ULo + VLo * VLo + WLo * WLo, VAMRo = URo * URo + VRo * VRo + WRo * WRo;
+    const double rLo = 0.0, rRo = 0.0;
+    double HLo = PLo * ga / (DENLo * ga1) + 0.5 * VAMLo - 0.5 * (rLo * rLo);
+    double HRo = PRo * ga / (DENRo * ga1) + 0.5 * VAMRo - 0.5 * (rRo * rRo);
+    double sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
+    const double vbc = 0.0;
+    double ulnormaln = (sav1n * ULo + sav2n * VLo + sav3n * WLo);
+    double urnormaln = (sav1n * URo + sav2n * VRo + sav3n * WRo);
+    double rulnormaln = DENLo * ulnormaln, rurnormaln = DENRo * urnormaln;
+    dr[0] = -0.5 * (rulnormaln + rurnormaln) * sav;
+    dr[1] = -0.5 * (rulnormaln * ULo + rurnormaln * URo + sav1n * (PLo + PRo)) * sav;
+    dr[2] = -0.5 * (rulnormaln * VLo + rurnormaln * VRo + sav2n * (PLo + PRo)) * sav;
+    dr[3] = -0.5 * (rulnormaln * WLo + rurnormaln * WRo + sav3n * (PLo + PRo)) * sav;
+    dr[4] = -0.5 * (rulnormaln * HLo + rurnormaln * HRo - vbc * (PLo + PRo)) * sav;
+    double DeltaU = std::sqrt((URo - ULo) * (URo - ULo) + (VRo - VLo) * (VRo - VLo) + (WRo - WLo) * (WRo - WLo));
+    if (DeltaU <= p.Tiny) {
+        roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, Funscheme, dr);
+        return;
+    }
+    double n1 = (URo - ULo) / DeltaU, n2 = (VRo - VLo) / DeltaU, n3 = (WRo - WLo) / DeltaU;
+    double s = n1 * sav1 + n2 * sav2 + n3 * sav3;
+    double sg = sgn1(s);
+    n1 = sg * n1; n2 = sg * n2; n3 = sg * n3;
+    s = std::fabs(s);
+    double a1 = n1 * s, a2 = n2 * s, a3 = n3 * s;
+    double b1 = sav1 - a1, b2 = sav2 - a2, b3 = sav3 - a3;
+    double sa = std::max(std::sqrt(a1 * a1 + a2 * a2 + a3 * a3), p.Tiny);
+    roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, a1, a2, a3, sa, Funscheme, dr);
+    double sb = std::max(std::sqrt(b1 * b1 + b2 * b2 + b3 * b3), p.Tiny);
+    roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, b1, b2, b3, sb, Funscheme, dr);
+}
+
 void convect_inviscid(Ctx& c, Blk& b) {
     const trans_params& p = c.p;
     for (int d = 1; d <= 3; ++d) {
@@ -1242,6 +1367,17 @@ void convect_inviscid(Ctx& c, Blk& b) {
             double sav1 = b.SD(d, 1, i, j, k), sav2 = b.SD(d, 2, i, j, k), sav3 = b.SD(d, 3, i, j, k);
             double sav = b.Grad(d, i, j, k);
             double f[5];
+            if (p.Kind_Roe == 2) {          // dr = the face's flux contribution, already times |S|
+                int im = i - e[0], jm = j - e[1], km = k - e[2];
+                double Funscheme = (b.Fsch(im, jm, km) + b.Fsch(i, j, k)) / 2.;
+                double dr[5];
+                roe_rotated(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, Funscheme, dr);
+                for (int L = 1; L <= 5; ++L) {
+                    b.D(L, i, j, k) = b.D(L, i, j, k) - dr[L - 1];
+                    b.D(L, im, jm, km) = b.D(L, im, jm, km) + dr[L - 1];
+                }
+                continue;
+            }
             if (p.Kind_Roe == 1) {
                 double rLo = b.rccl(d, i, j, k) * p.omega[0], rRo = b.rccr(d, i, j, k) * p.omega[0];
                 roe_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, rLo, rRo, f);
@@ -1954,7 +2090,7 @@ int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks,
     if (!p || !blocks || nblocks <= 0 || !out) return TRANS_E_ARG;
     if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2)) return TRANS_E_ARG;
     if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4) return TRANS_E_ARG;
-    if (p->Kind_Roe != 1 && p->Kind_Roe != 3) return TRANS_E_ARG;
+    if (p->Kind_Roe < 1 || p->Kind_Roe > 3) return TRANS_E_ARG;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return TRANS_E_ARG;
     if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 3)) return TRANS_E_ARG;
     if (p->omega[0] != 0.0 || p->omega[1] != 0.0 || p->omega[2] != 0.0) return TRANS_E_ARG;
@@ -1986,6 +2122,7 @@ int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks,
         b.DQ.alloc(18, 1, ni, nj, nk); b.shock.alloc(1, 1, ni, nj, nk); b.F.alloc(2, 1, ni, nj, nk);
         b.VL.alloc(3, 8, ni, nj, nk); b.VR.alloc(3, 8, ni, nj, nk);
         b.rccl.alloc(3, 1, ni, nj, nk); b.rccr.alloc(3, 1, ni, nj, nk); b.FunDES.alloc(1, 1, ni, nj, nk);
+        b.Fsch.alloc(1, 1, ni, nj, nk);
         std::memset(&b.nrm, 0, sizeof(b.nrm));
     }
     *out = c;

@@ -31,6 +31,7 @@ CASES = {
     "channel_small_muscl2_roe": ("channel", dict(Kind_Spatial=1, Kind_Roe=1)),
     "cascade_small_mdcdhyb_ausmpw": ("cascade", dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05)),
     "channel_small_mdcd_ausmpw_wd2006": ("channel", dict(Kind_Spatial=3, Kind_Roe=3, Kind_Model=2)),
+    "cascade_small_mdcd_roerot": ("cascade", dict(Kind_Spatial=3, Kind_Roe=2)),
 }
 
 

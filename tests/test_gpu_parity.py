@@ -42,8 +42,10 @@ def _mask(kind, dims):
 # inside the sensor's range on these grids (a mix of MDCD and MUSCL faces)
 # Kind_Model 2 = the WD+2006 k-omega model in place of SST
 SCHEMES = [dict(Kind_Spatial=2, Kind_Roe=1), dict(Kind_Spatial=3, Kind_Roe=3), dict(Kind_Spatial=1, Kind_Roe=1),
-           dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05), dict(Kind_Spatial=3, Kind_Roe=3, Kind_Model=2)]
-SCHEME_IDS = ["muscl_roe", "mdcd_ausmpw", "muscl2_roe", "mdcdhyb_ausmpw", "mdcd_ausmpw_wd2006"]
+           dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05), dict(Kind_Spatial=3, Kind_Roe=3, Kind_Model=2),
+           dict(Kind_Spatial=2, Kind_Roe=2), dict(Kind_Spatial=3, Kind_Roe=2)]
+SCHEME_IDS = ["muscl_roe", "mdcd_ausmpw", "muscl2_roe", "mdcdhyb_ausmpw", "mdcd_ausmpw_wd2006", "muscl_roerot",
+              "mdcd_roerot"]
 
 
 @pytest.mark.parametrize("scheme", SCHEMES, ids=SCHEME_IDS)

@@ -24,7 +24,8 @@ from .solver import Batch, global_residual
 
 SCHEMES = {"mdcd_ausmpw": dict(Kind_Spatial=3, Kind_Roe=3), "muscl_roe": dict(Kind_Spatial=2, Kind_Roe=1),
            "muscl2_roe": dict(Kind_Spatial=1, Kind_Roe=1),
-           "muscl_roe_wd2006": dict(Kind_Spatial=2, Kind_Roe=1, Kind_Model=2)}
+           "muscl_roe_wd2006": dict(Kind_Spatial=2, Kind_Roe=1, Kind_Model=2),
+           "muscl_roerot": dict(Kind_Spatial=2, Kind_Roe=2)}
 LEVELS = {"coarse": dict(ns=60, nh=32, nk=32), "medium": dict(nk=32), "full": dict()}
 
 

@@ -44,10 +44,11 @@ enum Slot {
     S_FC1 = 146,        // SST F1 per cell (for the DES length scale of the next cell)
     S_RINV = 147,       // 1/rho
     S_SVEL = 148,       // 3: rho*u * (1/rho) etc., the velocities of the LU-SGS Jacobians
-    NSLOT = 151,
+    S_FSCH = 151,       // hybrid blend Fscheme of the rotated Roe scheme (Kind_Roe = 2)
+    NSLOT = 152,
     // Runge-Kutta cases (IF_RK = 1) only: their blocks are allocated with NSLOT_RK slots
-    S_WT2 = 151,        // 7: the stage-1 state of the SSP-RK3 stages
-    NSLOT_RK = 158
+    S_WT2 = 152,        // 7: the stage-1 state of the SSP-RK3 stages
+    NSLOT_RK = 159
 };
 
 // The DeltaQ-independent parts of A(Q)*DeltaQ (Time/TIME_LUSGS.F90:696-768) of one cell and
@@ -102,7 +103,7 @@ struct Tile {             // a run of consecutive interior cells (or faces) of o
 
 #define TG_PARAM_REALS(X) X(XM) X(RXM2) X(PPF) X(Csthlnd) X(Csth1) X(Ref) X(Tiny) X(VxF) X(VyF) X(VzF) \
     X(omega0) X(P0in) X(T0in) X(Pouthub) X(VisRatio) X(FSTI) X(A1) X(Beta_star) X(Sigk1) X(Sigo1)    \
-    X(Beta1) X(Gama1) X(Sigk2) X(Sigo2) X(Beta2) X(Gama2) X(Prod_Lmt) X(gama_max) X(gama_min) X(F_limiter2)        \
+    X(Beta1) X(Gama1) X(Sigk2) X(Sigo2) X(Beta2) X(Gama2) X(Prod_Lmt) X(gama_max) X(gama_min) X(F_limiter1) X(F_limiter2) X(Alscale)        \
     X(DT_LUSGS_Main) X(DT_LUSGS_Sub) X(CFL_Main) X(Trans_location)
 
 template <typename R>
@@ -236,6 +237,86 @@ template <typename R> __device__ inline void mdcd_pair(const R* s6, R gama, R& q
         R qq3 = c116 * v_1 - c76 * v_2 + c13 * v_3;
         qr = w0 * qq0 + w1 * qq1 + w2 * qq2 + w3 * qq3;
     }
+}
+
+// Roe_Common of the rotated scheme (Space/CONVECT_Roe_Rotated.F90:597-752), non-preconditioned,
+// rcc * omega = 0: adds 0.5 |A| dQ along (sav1..3)/sav, times sav and Funscheme, to dr
+template <typename R>
+__device__ inline void roe_rot_common(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo,
+                                      R WRo, R sav1, R sav2, R sav3, R sav, R Funscheme, R* dr) {
+    const R rcpcv = R(p.PPF);
+    const R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
+    const R ga = R(1.4), ga1 = R(0.4);
+    const R VAMLo = ULo * ULo + VLo * VLo + WLo * WLo, VAMRo = URo * URo + VRo * VRo + WRo * WRo;
+    const R rLo = R(0.0), rRo = R(0.0);
+    const R HLo = PLo * ga / (DENLo * ga1) + R(0.5) * VAMLo - R(0.5) * (rLo * rLo);
+    const R HRo = PRo * ga / (DENRo * ga1) + R(0.5) * VAMRo - R(0.5) * (rRo * rRo);
+    const R rrorl = sqrt(DENRo / DENLo), rrorlp1 = R(1.0) + rrorl;
+    const R rm = sqrt(DENRo * DENLo);
+    const R um = (ULo + URo * rrorl) / rrorlp1, vm = (VLo + VRo * rrorl) / rrorlp1, wm = (WLo + WRo * rrorl) / rrorlp1;
+    const R hm = (HLo + HRo * rrorl) / rrorlp1;
+    const R vm2 = um * um + vm * vm + wm * wm;
+    const R rccm = (rLo + rRo * rrorl) / rrorlp1;
+    const R am2 = ga1 * fabs(hm - R(0.5) * vm2 + R(0.5) * (rccm * rccm));
+    const R am = sqrt(am2);
+    const R sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
+    const R unormaln = (sav1n * um + sav2n * vm + sav3n * wm);
+    const R eig1 = fabs(unormaln), eig2 = fabs(unormaln + am), eig3 = fabs(unormaln - am);
+    const R alf = R(0.0), ubetac2 = R(1.0);
+    const R dunormaln = (sav1n * (URo - ULo) + sav2n * (VRo - VLo) + sav3n * (WRo - WLo));
+    const R astar = (eig2 + eig3) / R(2.0);
+    const R Mstar = (eig2 - eig3) / R(2.0) / am;
+    const R dW1 = DENRo - DENLo, dU1 = URo - ULo, dU2 = VRo - VLo, dU3 = WRo - WLo, dP1 = PRo - PLo;
+    const R dW2 = rm * dU1 + dW1 * um, dW3 = rm * dU2 + dW1 * vm, dW4 = rm * dU3 + dW1 * wm;
+    const R dW5 = dP1 / ga1 + R(0.5) * vm2 * dW1 + rm * um * dU1 + rm * vm * dU2 + rm * wm * dU3;
+    const R dUroe = Mstar * dunormaln + (astar - (R(1) - R(2.0) * alf) * eig1 - alf * unormaln * Mstar) * (PRo - PLo) / rm / (ubetac2 * am2);
+    const R dProe = Mstar * (PRo - PLo) + (astar - eig1 + alf * unormaln * Mstar) * rm * dunormaln;
+    const R d1[5] = {eig1 * dW1 + dUroe * rm, eig1 * dW2 + dUroe * rm * um + dProe * sav1n,
+                     eig1 * dW3 + dUroe * rm * vm + dProe * sav2n, eig1 * dW4 + dUroe * rm * wm + dProe * sav3n,
+                     eig1 * dW5 + dUroe * rm * hm + dProe * unormaln};
+    for (int L = 0; L < 5; ++L) dr[L] = dr[L] + R(0.5) * d1[L] * sav * Funscheme;
+}
+
+// CONVECT_Roe_Rotated (Space/CONVECT_Roe_Rotated.F90:59-591): central flux along the face
+// normal, then the dissipation along the velocity-jump direction and along the rest of the face
+// vector (one direction when the jump is below Tiny); dr = the face's contribution (times |S|).
+// The grid velocities the reference reads uninitialised (:169, :332, :510) are taken as 0.
+template <typename R>
+__device__ inline void roe_rotated(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo,
+                                   R WRo, R sav1, R sav2, R sav3, R sav, R Funscheme, R* dr) {
+    const R rcpcv = R(p.PPF);
+    const R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
+    const R ga = R(1.4), ga1 = R(0.4);
+    const R VAMLo = ULo * ULo + VLo * VLo + WLo * WLo, VAMRo = URo * URo + VRo * VRo + WRo * WRo;
+    const R rLo = R(0.0), rRo = R(0.0);
+    const R HLo = PLo * ga / (DENLo * ga1) + R(0.5) * VAMLo - R(0.5) * (rLo * rLo);
+    const R HRo = PRo * ga / (DENRo * ga1) + R(0.5) * VAMRo - R(0.5) * (rRo * rRo);
+    const R sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
+    const R vbc = R(0.0);
+    const R ulnormaln = (sav1n * ULo + sav2n * VLo + sav3n * WLo);
+    const R urnormaln = (sav1n * URo + sav2n * VRo + sav3n * WRo);
+    const R rulnormaln = DENLo * ulnormaln, rurnormaln = DENRo * urnormaln;
+    dr[0] = R(-0.5) * (rulnormaln + rurnormaln) * sav;
+    dr[1] = R(-0.5) * (rulnormaln * ULo + rurnormaln * URo + sav1n * (PLo + PRo)) * sav;
+    dr[2] = R(-0.5) * (rulnormaln * VLo + rurnormaln * VRo + sav2n * (PLo + PRo)) * sav;
+    dr[3] = R(-0.5) * (rulnormaln * WLo + rurnormaln * WRo + sav3n * (PLo + PRo)) * sav;
+    dr[4] = R(-0.5) * (rulnormaln * HLo + rurnormaln * HRo - vbc * (PLo + PRo)) * sav;
+    const R DeltaU = sqrt((URo - ULo) * (URo - ULo) + (VRo - VLo) * (VRo - VLo) + (WRo - WLo) * (WRo - WLo));
+    if (DeltaU <= R(p.Tiny)) {
+        roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, Funscheme, dr);
+        return;
+    }
+    R n1 = (URo - ULo) / DeltaU, n2 = (VRo - VLo) / DeltaU, n3 = (WRo - WLo) / DeltaU;
+    R s = n1 * sav1 + n2 * sav2 + n3 * sav3;
+    const R sg = sgn1(s);
+    n1 = sg * n1; n2 = sg * n2; n3 = sg * n3;
+    s = fabs(s);
+    const R a1 = n1 * s, a2 = n2 * s, a3 = n3 * s;
+    const R b1 = sav1 - a1, b2 = sav2 - a2, b3 = sav3 - a3;
+    const R sa = dmax(sqrt(a1 * a1 + a2 * a2 + a3 * a3), R(p.Tiny));
+    roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, a1, a2, a3, sa, Funscheme, dr);
+    const R sb = dmax(sqrt(b1 * b1 + b2 * b2 + b3 * b3), R(p.Tiny));
+    roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, b1, b2, b3, sb, Funscheme, dr);
 }
 
 // Space/CONVECT_Roe_Original.F90:242-407 (non-preconditioned, no rotation); out = flux / |S|

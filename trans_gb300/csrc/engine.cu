@@ -40,7 +40,7 @@ Params make_params(const trans_params& p) {
     d.P0in = p.P0in; d.T0in = p.T0in; d.Pouthub = p.Pouthub; d.VisRatio = p.VisRatio; d.FSTI = p.FSTI;
     d.A1 = p.A1; d.Beta_star = p.Beta_star; d.Sigk1 = p.Sigk1; d.Sigo1 = p.Sigo1; d.Beta1 = p.Beta1;
     d.Gama1 = p.Gama1; d.Sigk2 = p.Sigk2; d.Sigo2 = p.Sigo2; d.Beta2 = p.Beta2; d.Gama2 = p.Gama2;
-    d.Prod_Lmt = p.Prod_Lmt; d.gama_max = p.gama_max; d.gama_min = p.gama_min; d.F_limiter2 = p.F_limiter2;
+    d.Prod_Lmt = p.Prod_Lmt; d.gama_max = p.gama_max; d.gama_min = p.gama_min; d.F_limiter1 = p.F_limiter1; d.F_limiter2 = p.F_limiter2; d.Alscale = p.Alscale;
     d.DT_LUSGS_Main = p.DT_LUSGS_Main; d.DT_LUSGS_Sub = p.DT_LUSGS_Sub; d.CFL_Main = p.CFL_Main;
     d.Trans_location = p.Trans_location;
     d.Kind_Spatial = p.Kind_Spatial; d.Kind_Roe = p.Kind_Roe; d.Kind_Hybrid = p.Kind_Hybrid;
@@ -57,7 +57,7 @@ bool params_supported(const trans_params* p) {
     if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2) || p->IF_Euler != 0)
         return false;
     if (p->IF_RK != 0 && p->IF_RK != 1) return false;
-    if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4 || (p->Kind_Roe != 1 && p->Kind_Roe != 3)) return false;
+    if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4 || p->Kind_Roe < 1 || p->Kind_Roe > 3) return false;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return false;
     if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 3)) return false;
     if (p->omega[0] != 0.0 || p->omega[1] != 0.0 || p->omega[2] != 0.0) return false;

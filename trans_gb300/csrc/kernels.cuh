@@ -414,6 +414,36 @@ __global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __rest
     R Vort = sqrt(R(2.0) * (R(2.0) * W12 * W12 + R(2.0) * W13 * W13 + R(2.0) * W23 * W23));
     R DivU = sqrt(DuDx * DuDx + DvDy * DvDy + DwDz * DwDz);
     rs<R>(b, S_SHOCK)[c] = DivU * DivU / dmax(DivU * DivU + Vort * Vort, R(1.0));
+    const ParamsT<R>& p = cparams<R>(cdev[b.cs]);
+    if (p.Kind_Roe == 2) {
+        // the hybrid blend Fscheme (Space/DIFF_DqDxyz.F90:311-380), read only by the rotated Roe
+        // scheme: CH1 = 3, CH2 = 1, CH3 = 2, cmu = 0.09, tau = 1; real exponents 2 and 3 as
+        // products, 0.5 as a square root
+        R S11 = (DuDx + DuDx) / R(2.), S22 = (DvDy + DvDy) / R(2.), S33 = (DwDz + DwDz) / R(2.);
+        R S12 = (DuDy + DvDx) / R(2.), S13 = (DuDz + DwDx) / R(2.), S23 = (DwDy + DvDz) / R(2.);
+        R Skl = sqrt(R(2.) * (R(1.) * S11 * S11 + R(1.) * S22 * S22 + R(1.) * S33 * S33 + R(2.) * S12 * S12 +
+                              R(2.) * S13 * S13 + R(2.) * S23 * S23));
+        R Den = rs<R>(b, S_V)[c], RmiuT = rs<R>(b, S_RMIU)[c], TT = rs<R>(b, S_T)[c];
+        R RMIUL = mu_suth<R>(p, TT);
+        R vK = rs<R>(b, S_V + 5)[c] / Den, vOmega = rs<R>(b, S_V + 6)[c] / Den;
+        R DLTxyz = rs<R>(b, S_ALENG)[c];
+        auto G = [&](int q) { return rs<R>(b, S_DQ + q)[c]; };
+        R dTKO = G(12) * G(15) + G(13) * G(16) + G(14) * G(17);
+        R Dist = rs<R>(b, S_DST)[c];
+        const R Sigo2 = R(p.Sigo2), Bs = R(p.Beta_star), Ref = R(p.Ref);
+        R CDKO = dmax(R(2.0) * Den * Sigo2 / vOmega * (dTKO), R(1.0e-10));
+        R arg1 = dmax(sqrt(vK) / Bs / vOmega / Dist / Ref, R(500.0) * RMIUL / Den / Dist / Dist / vOmega / Ref / Ref);
+        arg1 = dmin(arg1, R(4.0) * Den * Sigo2 * vK / CDKO / Dist / Dist);
+        R a2 = arg1 * arg1;
+        R FunC1 = ttanh(a2 * a2);
+        R aLgrd = ((R(1.) - FunC1) * R(0.61) + FunC1 * R(0.78)) * DLTxyz;
+        R B0 = R(2.) * Vort * dmax(Vort, Skl) / dmax((Vort * Vort + Skl * Skl) / R(2.), R(p.Alscale) * R(0.1));
+        R g0 = ttanh(B0 * B0 * B0 * B0);
+        R sok = dmax(sqrt((Vort * Vort + Skl * Skl) / R(2.)), R(0.1) / R(1.0));
+        R alturb = sqrt((RmiuT + RMIUL) / Den / (Ref * sok * p15(R(0.09))));
+        R A0 = R(1.) * dmax(((aLgrd / alturb / g0) - R(0.1)), R(0.0));
+        rs<R>(b, S_FSCH)[c] = dmax(R(1.) * ttanh(A0 * A0 * A0), R(p.F_limiter1));
+    }
 }
 
 // shock of the three ghost layers of every face = shock of the adjacent interior cell
@@ -436,6 +466,10 @@ __global__ void k_shock_ghost(const DevBlock* __restrict__ blks, const Tile* __r
     else { i = n % b.NI1 + 1; j = n / b.NI1 + 1; k = side ? b.NK1 + L : 1 - L; kk = side ? b.NK1 : 1; ii = i; jj = j; }
     R* sh = rs<R>(b, S_SHOCK);
     sh[cidx(b, i, j, k)] = sh[cidx(b, ii, jj, kk)];
+    if (L == 1) {       // Fscheme's face-adjacent ghosts (Space/DIFF_DqDxyz.F90:399-404)
+        R* fs = rs<R>(b, S_FSCH);
+        fs[cidx(b, i, j, k)] = fs[cidx(b, ii, jj, kk)];
+    }
 }
 
 // BC_Boundarys(0): gradients of the first ghost layer (BC/*.F90 sweep 0, BC/BC_P2P.F90:140-184)
@@ -673,11 +707,19 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
     R sav1 = R(SDd[c]), sav2 = R(SDd[c + nc]), sav3 = R(SDd[c + 2 * nc]);
     R sav = R(rs<R>(b, S_GRAD + d)[c]);
     R f[5];
-    if (p.Kind_Roe == 1)
-        roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
-    else
-        ausmpw_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
-    for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = (f[L] * sav);
+    if (p.Kind_Roe == 2) {          // rotated Roe: the contribution already carries |S|
+        const R* fs = rs<R>(b, S_FSCH);
+        const R Funscheme = (R(fs[cm]) + R(fs[c])) / R(2.);
+        roe_rotated<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav,
+                       Funscheme, f);
+        for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = f[L];
+    } else {
+        if (p.Kind_Roe == 1)
+            roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
+        else
+            ausmpw_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
+        for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = (f[L] * sav);
+    }
     if (turb) {
         R rcpcv = R(p.PPF);
         R DENL = qL[3] / (rcpcv * qL[4]), DENR = qR[3] / (rcpcv * qR[4]);
