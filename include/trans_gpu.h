@@ -41,7 +41,8 @@ extern "C" {
 
 /* Precision modes */
 #define TRANS_FP64 0            /* all-FP64 path, drop-in for the reference subroutines    */
-#define TRANS_MIXED 1           /* FP32 reconstruction/flux/SST/sweeps, FP64 update/metrics */
+#define TRANS_MIXED 1           /* FP32 reconstruction/flux/SST/sweeps, FP64 update/metrics
+                                   (not with Kind_Roe = 2, the rotated Roe scheme)          */
 
 /*
  * Module globals read by the hot path (Module_Global.F90:39-148), with the values they hold

@@ -105,3 +105,12 @@ def test_null_arguments_are_rejected(lib):
     assert lib.trans_create(None, 1, None, C.byref(ctx)) == abi.TRANS_E_ARG
     assert lib.trans_iterate(None, 1, None) == abi.TRANS_E_ARG
     assert lib.trans_destroy(None) == abi.TRANS_OK      # like free(NULL)
+
+
+def test_rotated_roe_is_fp64_only(lib):
+    """The rotated Roe scheme (Kind_Roe = 2) runs in the FP64 path; the mixed path refuses it."""
+    p = _params(Kind_Roe=2, precision=abi.TRANS_MIXED)
+    blk = (abi.TransBlock * 1)()
+    blk[0].ni = blk[0].nj = blk[0].nk = 8
+    ctx = C.c_void_p()
+    assert lib.trans_create(C.byref(p), 1, blk, C.byref(ctx)) == abi.TRANS_E_ARG
