@@ -5,7 +5,7 @@
  * subroutines that act on the block selected by GLOBAL_SetPointers(iBlock)
  * (Module_Global.F90:274-392) and read module globals.  This header replaces that driver loop
  * body (main.F90:54-197) and the subroutine calls inside it with plain C entry points that a
- * Fortran caller binds through ISO_C_BINDING:
+ * Fortran caller binds through ISO_C_BINDING (BIND(C) interfaces over these prototypes):
  *
  *   trans_create            replaces the per-block allocation of Input/Read_BlockDimensions.F90:306-478
  *                           and takes the connectivity built by Input/PLOT3DReadInit.F90:123-348
@@ -293,13 +293,18 @@ int trans_batch_cases(void* ctx, int* ids, int max);
  * 4 MiB buffer that is part of the library image instead of the context's own buffer.  No
  * counterpart in the reference.  It is for callers that cannot allocate device memory at this
  * point -- for instance a serving loop that has committed its whole device-memory budget to
- * resident solves -- and it allocates nothing: no cudaMalloc, no allocating library routine.
+ * resident solves -- and it allocates nothing: no cudaMalloc, no page-locked host memory, no
+ * allocating library routine.  The context must already be built (by trans_prepare,
+ * trans_run_stage or trans_iterate), because building it allocates its work lists: an
+ * unbuilt context gets TRANS_E_ARG and nothing is allocated.
  * Limit: 65536 cell tiles (16,777,216 interior cells per context); larger contexts get
  * TRANS_E_ARG with a message in trans_last_error.  Call it with the context's device current.
- * The first call on a device looks the buffer up (cudaGetSymbolAddress) and should come
- * before any stream capture.  The buffer is shared by every context and call on a device and
- * keeps the last call's contents; concurrent calls race on it and must be serialised by the
- * caller.  norms: nblocks entries, may be NULL.  Runge-Kutta contexts (IF_RK = 1), whose
+ * The first call on a device looks the buffer up (cudaGetSymbolAddress, which may load the
+ * library's device code on that device) and should come before any stream capture.  The
+ * buffer is shared by every context and call on a device and keeps the last call's contents;
+ * concurrent calls race on it and must be serialised by the caller.  norms: nblocks entries,
+ * may be NULL.  TRANS_E_TIMEOUT when the LU-SGS sweep of this iteration gave up on a bounded
+ * device-side wait, as the UPDATE stage reports it.  Runge-Kutta contexts (IF_RK = 1), whose
  * update is TIME_RK_V_Update_New, get TRANS_E_ARG.
  */
 int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms);

@@ -1,52 +1,142 @@
 """trans_update_static_scratch: TIME_Update_V with its norm partials in the library's fixed
 device buffer, against the regular update stage (trans_run_stage UPDATE), through the C ABI.
 
-Two contexts start from the same state and run the same stages; one finishes each iteration
-with the regular update, the other with the static-scratch entry point.  Two calls in a row
-must give the same norms and the same updated state (tolerance 1e-11 relative, the FP64
-path's bar; both run the same kernel, so they agree bit for bit in practice).
+The entry point is for callers that cannot allocate device memory when they update, such as a
+serving loop that has committed its whole device-memory budget to resident solves.  Two
+contexts start from the same state and run the same stages; one finishes each iteration with
+the regular update, the other with the static-scratch entry point.  Two calls in a row must
+give the same norms and the same updated state (tolerance 1e-11 relative, the FP64 path's bar;
+in the mixed path both run the same FP64 update kernel on the same FP32 increments, so the
+same bar holds), and the device memory the context holds must not change across the calls.
+An unbuilt context is refused without allocating anything.
+
+This file is collected last on purpose, so a run that stops at its first failure has run every
+other test already; it passes alone in a fresh process too.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
-from helpers import interior, rel_err, small_channel
+from helpers import interior, rel_err, small_cascade, small_channel
 
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-11
 PRE_UPDATE = ("SPECRAD", "BC_STATE", "GRADIENT", "BC_GRAD", "RESIDUAL", "LUSGS")
+NORM_VALUES = ("DRSa", "DUa", "DRSk", "DUk", "DRSo", "DUo")
+NORM_INDICES = ("Ima", "Jma", "Kma", "nan_flag")
 
 
-def test_static_scratch_update_matches_regular_update(gpu_lib):
+def _device_free_bytes():
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    return free
+
+
+def _compare(regular, static, ki, nblk, mask_of):
+    from trans_gb300 import abi
+    lib = static.lib
+    want = regular.norms()
+    out = (abi.TransNorms * nblk)()
+    held = lib.trans_device_bytes(static.ctx)
+    rc = lib.trans_update_static_scratch(static.ctx, ki, out)
+    assert rc == abi.TRANS_OK, lib.trans_last_error(static.ctx)
+    assert lib.trans_device_bytes(static.ctx) == held, "the context's device memory changed"
+    for ib in range(nblk):
+        got = {f: getattr(out[ib], f) for f, _ in abi.TransNorms._fields_}
+        for f in NORM_VALUES:
+            assert abs(got[f] - want[ib][f]) <= TOL * abs(want[ib][f]), (ki, ib, f, got[f], want[ib][f])
+        for f in NORM_INDICES:
+            assert got[f] == want[ib][f], (ki, ib, f)
+        for name in ("V", "PP", "T", "RMIU"):
+            err = np.max(rel_err(static.get_field(ib, name), regular.get_field(ib, name), mask_of(ib)))
+            assert err <= TOL, (ki, ib, name, err)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("which", ["channel", "cascade"])
+def test_static_scratch_update_matches_regular_update(gpu_lib, precision, which):
     from trans_gb300 import abi
     from trans_gb300.solver import Solver
-    c, conns, geo, st = small_channel(Kind_Spatial=3, Kind_Roe=3)
+    make = small_channel if which == "channel" else small_cascade
+    c, conns, geo, st = make(Kind_Spatial=3, Kind_Roe=3)
+    c.params.precision = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
     regular, static = Solver(c, conns, geo, st), Solver(c, conns, geo, st)
-    lib = static.lib
-    m = interior(c.blocks[0].dims)
+    nblk = len(c.blocks)
+    masks = [interior(b.dims) for b in c.blocks]
+    free0 = None
     for ki in (1, 2):                       # two calls in a row
         for s in PRE_UPDATE:
             regular.run_stage(s, ki)
             static.run_stage(s, ki)
         regular.run_stage("UPDATE", ki)
-        want = regular.norms()[0]
-        out = (abi.TransNorms * 1)()
-        rc = lib.trans_update_static_scratch(static.ctx, ki, out)
-        assert rc == abi.TRANS_OK, lib.trans_last_error(static.ctx)
-        got = {f: getattr(out[0], f) for f, _ in abi.TransNorms._fields_}
-        for f in ("DRSa", "DUa", "DRSk", "DUk", "DRSo", "DUo"):
-            assert abs(got[f] - want[f]) <= TOL * abs(want[f]), (ki, f, got[f], want[f])
-        for f in ("Ima", "Jma", "Kma", "nan_flag"):
-            assert got[f] == want[f], (ki, f)
-        for name in ("V", "PP", "T", "RMIU"):
-            err = np.max(rel_err(static.get_field(0, name), regular.get_field(0, name), m))
-            assert err <= TOL, (ki, name, err)
+        if free0 is None:
+            import torch
+            torch.cuda.synchronize()
+            free0 = _device_free_bytes()
+        _compare(regular, static, ki, nblk, lambda ib: masks[ib])
         regular.run_stage("UPDATE_U", ki)
         static.run_stage("UPDATE_U", ki)
+    assert _device_free_bytes() == free0, "device memory was allocated or freed across the calls"
     regular.close()
     static.close()
+
+
+def test_static_scratch_batch_context(gpu_lib):
+    """Two cases of uneven size in one batch context: the per-block norms of every case match
+    the regular update's."""
+    from trans_gb300 import abi
+    from trans_gb300.solver import Batch
+    lib = gpu_lib
+    cases = [small_channel(Kind_Spatial=3, Kind_Roe=3), small_cascade(Kind_Spatial=3, Kind_Roe=3)]
+    regular, static = Batch(abi.TRANS_FP64), Batch(abi.TRANS_FP64)
+    ids = []
+    for c, conns, geo, st in cases:
+        ids.append((regular.add(c, conns, geo, st), static.add(c, conns, geo, st), len(c.blocks)))
+    for ki in (1, 2):
+        for s in PRE_UPDATE + ("UPDATE",):
+            assert lib.trans_run_stage(regular.ctx, abi.STAGE_ID[s], ki, 1) == abi.TRANS_OK
+        for s in PRE_UPDATE:
+            assert lib.trans_run_stage(static.ctx, abi.STAGE_ID[s], ki, 1) == abi.TRANS_OK
+        held = lib.trans_device_bytes(static.ctx)
+        rc = lib.trans_update_static_scratch(static.ctx, ki, C.cast(None, C.POINTER(abi.TransNorms)))
+        assert rc == abi.TRANS_OK, lib.trans_last_error(static.ctx)
+        assert lib.trans_device_bytes(static.ctx) == held
+        for rid, sid, nb in ids:
+            a, b = (abi.TransNorms * nb)(), (abi.TransNorms * nb)()
+            it = C.c_int()
+            assert lib.trans_batch_case_norms(regular.ctx, rid, C.byref(it), None, a) == abi.TRANS_OK
+            assert lib.trans_batch_case_norms(static.ctx, sid, C.byref(it), None, b) == abi.TRANS_OK
+            for ib in range(nb):
+                for f in NORM_VALUES:
+                    x, y = getattr(b[ib], f), getattr(a[ib], f)
+                    assert abs(x - y) <= TOL * abs(y), (ki, rid, ib, f, x, y)
+        for s in ("UPDATE_U",):
+            assert lib.trans_run_stage(regular.ctx, abi.STAGE_ID[s], ki, 1) == abi.TRANS_OK
+            assert lib.trans_run_stage(static.ctx, abi.STAGE_ID[s], ki, 1) == abi.TRANS_OK
+    regular.close()
+    static.close()
+
+
+def test_static_scratch_refuses_unbuilt_context(gpu_lib):
+    """A context whose work lists are not built yet would have to allocate them: the call
+    returns TRANS_E_ARG and the context holds the same device memory afterwards."""
+    from trans_gb300 import abi
+    from trans_gb300.solver import Solver
+    c, conns, geo, st = small_channel(Kind_Spatial=3, Kind_Roe=3)
+    s = Solver(c, conns, geo, st)
+    lib = s.lib
+    held = lib.trans_device_bytes(s.ctx)
+    rc = lib.trans_update_static_scratch(s.ctx, 1, C.cast(None, C.POINTER(abi.TransNorms)))
+    assert rc == abi.TRANS_E_ARG
+    assert b"not built" in lib.trans_last_error(s.ctx)
+    assert lib.trans_device_bytes(s.ctx) == held
+    s.iterate(1)                            # the context still works, and the entry point then does
+    for st_name in PRE_UPDATE:
+        s.run_stage(st_name, 2)
+    assert lib.trans_update_static_scratch(s.ctx, 2, C.cast(None, C.POINTER(abi.TransNorms))) == abi.TRANS_OK
+    s.close()
 
 
 def test_static_scratch_rejects_null_context(gpu_lib):

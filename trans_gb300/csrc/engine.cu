@@ -148,6 +148,10 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     // TRANS_SWEEP_PF=n forces an L2 prefetch distance of n hyperplanes (for tests)
     const char* pf = std::getenv("TRANS_SWEEP_PF");
     if (pf) c->sweep_pf = std::max(0, std::atoi(pf));
+    // TRANS_SWEEP_SPIN=n bounds every device-side wait of the cooperative sweep schedules at n
+    // polls (for tests of the timeout path: a small n makes the waits run out)
+    const char* sp = std::getenv("TRANS_SWEEP_SPIN");
+    if (sp) c->spin_limit = (unsigned)std::max(0L, std::strtol(sp, nullptr, 10));
     // sweep schedule: TRANS_SWEEP=planes | coop | flow | tiles forces one (for tests); default: tuned
     const char* m = std::getenv("TRANS_SWEEP");
     std::string ms = m ? m : "";

@@ -127,6 +127,7 @@ struct Ctx {
     int sweep_lanes = 1;                 // DeltaQ components swept: 1 = all, 2 = k and omega only (Runge-Kutta)
     SweepSync* d_sync = nullptr;
     SweepSync* h_sync = nullptr;         // pinned
+    unsigned spin_limit = SWEEP_SPIN_LIMIT;   // polls of one device-side wait before it gives up
     std::string sweep_tuning;
     // ---- instrumentation ----
     bool ktime_on = false;

@@ -62,8 +62,8 @@ void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb, int
 void swu(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count) {
     swp<false>(s, v, first, count, turb, chained, pf_first, pf_count);
 }
-cudaError_t swa(cudaStream_t s, const SweepView& v, const int* po, int nplanes, int turb, SweepSync* sy, int grid, int block) {
-    unsigned limit = SWEEP_SPIN_LIMIT;
+cudaError_t swa(cudaStream_t s, const SweepView& v, const int* po, int nplanes, int turb, SweepSync* sy, int grid, int block,
+                unsigned limit) {
     const int* nbp = v.nbp;
     const TG_R* rec = (const TG_R*)v.rec;
     TG_R* dq = (TG_R*)v.dq;
@@ -77,8 +77,8 @@ int swa_occ(int block) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_all<TG_R>, block, 0) != cudaSuccess) return 0;
     return n;
 }
-cudaError_t swf(cudaStream_t s, const SweepView& v, int* flagL, int* flagU, int turb, SweepSync* sy, int grid, int block) {
-    unsigned limit = SWEEP_SPIN_LIMIT;
+cudaError_t swf(cudaStream_t s, const SweepView& v, int* flagL, int* flagU, int turb, SweepSync* sy, int grid, int block,
+                unsigned limit) {
     const int* nbp = v.nbp;
     const TG_R* rec = (const TG_R*)v.rec;
     TG_R* dq = (TG_R*)v.dq;
@@ -93,10 +93,9 @@ int swf_occ(int block) {
     return n;
 }
 cudaError_t swt(cudaStream_t s, const SweepView& v, const TileView& tv, int lanes, int* flags, int* counter, SweepSync* sy,
-                int grid, int block) {
+                int grid, int block, unsigned limit) {
     if (v.n <= 0 || tv.ntiles <= 0) return cudaSuccess;
     // cooperative: the CTAs wait on one another, so the whole grid must be resident
-    unsigned limit = SWEEP_SPIN_LIMIT;
     const int* nbp = v.nbp;
     const TG_R* rec = (const TG_R*)v.rec;
     TG_R* dq = (TG_R*)v.dq;

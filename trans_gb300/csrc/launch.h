@@ -64,15 +64,17 @@ struct FluxLaunchers {
     void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained, int pf_first, int pf_count);
     void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained, int pf_first, int pf_count);
     // both sweeps in one cooperative launch (grid must be co-resident: grid <= SMs x occupancy)
+    // (limit: polls of one wait before the kernel gives up, records the error and returns)
     cudaError_t (*sweep_all)(cudaStream_t, const SweepView&, const int* plane_off, int nplanes, int lanes, SweepSync*,
-                             int grid, int block);
+                             int grid, int block, unsigned limit);
     int (*sweep_all_occupancy)(int block);          // resident blocks per SM
     // both sweeps as a dataflow over per-position ready flags (one cooperative launch)
-    cudaError_t (*sweep_flow)(cudaStream_t, const SweepView&, int* flagL, int* flagU, int turb, SweepSync*, int grid, int block);
+    cudaError_t (*sweep_flow)(cudaStream_t, const SweepView&, int* flagL, int* flagU, int turb, SweepSync*, int grid, int block,
+                              unsigned limit);
     int (*sweep_flow_occupancy)(int block);
     // both sweeps as a tiled wavefront (one cooperative launch, tiles taken from a counter)
     cudaError_t (*sweep_tiles)(cudaStream_t, const SweepView&, const TileView&, int lanes, int* flags, int* counter, SweepSync*,
-                               int grid, int block);
+                               int grid, int block, unsigned limit);
     int (*sweep_tiles_occupancy)(int block);
     void (*scatter)(cudaStream_t, const DevBlock*, const SweepView&, int l0);   // DeltaQ l0..6 back to cell order
     size_t elem;                                    // bytes of the sweep arithmetic type
@@ -85,5 +87,5 @@ constexpr int FACE_TILE = 128;
 #define TG_SWEEP_CTA 128
 #endif
 constexpr int SWEEP_CTA = TG_SWEEP_CTA;    // threads per CTA of the hyperplane sweep launches
-constexpr unsigned SWEEP_SPIN_LIMIT = 1u << 22;     // polls of one wait before it gives up (~1 s)
+constexpr unsigned SWEEP_SPIN_LIMIT = 1u << 22;     // default polls of one wait before it gives up (~1 s)
 }  // namespace tg

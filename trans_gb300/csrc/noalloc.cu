@@ -1,12 +1,15 @@
 // noalloc.cu -- TIME_Update_V with its per-tile norm partials in a fixed device buffer.
 //
 // The buffer is a file-scope __device__ array, part of the loaded library image: the call
-// makes no device allocation of any kind.  Its address is taken once per device with
-// cudaGetSymbolAddress, with that device current, on the first call made on it (so that first
-// call should come before any stream capture), and handed to the kernel as a plain pointer.
-// All contexts and calls share the array and it keeps the last call's contents; every entry a
-// call reads is written earlier in the same call, so nothing needs clearing.  Calls that
-// overlap (two host threads, or two contexts whose streams run concurrently) race on it.
+// makes no device or page-locked host allocation of any kind.  Its address is taken once per
+// device with cudaGetSymbolAddress, with that device current, on the first call made on it
+// (that lookup may load the library's device code on the device if nothing has yet, so the
+// first call should come before any stream capture), and handed to the kernel as a plain
+// pointer.  All contexts and calls share the array and it keeps the last call's contents;
+// every entry a call reads is written earlier in the same call, so nothing needs clearing.
+// Calls that overlap (two host threads, or two contexts whose streams run concurrently) race
+// on it.  The context must already be built (by trans_prepare, a stage or an iteration):
+// building it allocates its work lists, so an unbuilt context is refused, not built here.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -45,7 +48,9 @@ extern "C" int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms
     if (!c || c->cases.empty()) return TRANS_E_ARG;
     if (c->cases[0]->p.IF_RK == 1) return fail(c, TRANS_E_ARG, "trans_update_static_scratch is TIME_Update_V: LU-SGS cases only");
     int rc;
-    if (!c->built && (rc = rebuild(c))) return rc;
+    if (!c->built)      // building the work lists would allocate device memory
+        return fail(c, TRANS_E_ARG, "trans_update_static_scratch: the context is not built yet; call trans_prepare, "
+                                    "trans_run_stage or trans_iterate first");
     if (c->cell_tiles.size() > (size_t)kStaticNormTiles)
         return fail(c, TRANS_E_ARG, "trans_update_static_scratch: " + std::to_string(c->cell_tiles.size()) +
                     " cell tiles exceed the static scratch of 65536 tiles (16,777,216 interior cells)");
@@ -60,6 +65,8 @@ extern "C" int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c->h_parts.data(), scratch, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    // a cooperative sweep of this iteration that gave up on a bounded wait left DeltaQ partial
+    if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
     rc = reduce_norms(c);
     if (norms) std::copy(c->cases[0]->norms.begin(), c->cases[0]->norms.end(), norms);
     return rc;

@@ -287,7 +287,8 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         const int nt = c->tv.ntiles;
         CK(cudaMemsetAsync(c->d_tflags, 0, sizeof(int) * ((size_t)2 * nt + 1), s));
         CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
-        CK(c->fl->sweep_tiles(s, c->sv, c->tv, lanes, c->d_tflags, c->d_tflags + 2 * nt, c->d_sync, grid, block));
+        CK(c->fl->sweep_tiles(s, c->sv, c->tv, lanes, c->d_tflags, c->d_tflags + 2 * nt, c->d_sync, grid, block,
+                                   c->spin_limit));
         CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
         c->launches++;
         return TRANS_OK;
@@ -296,14 +297,14 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         const size_t np = (size_t)((c->sv.n + 31) / 32 * 32);
         CK(cudaMemsetAsync(c->d_flags, 0, 2 * np * sizeof(int), s));
         CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
-        CK(c->fl->sweep_flow(s, c->sv, c->d_flags, c->d_flags + np, c->sweep_lanes, c->d_sync, grid, block));
+        CK(c->fl->sweep_flow(s, c->sv, c->d_flags, c->d_flags + np, c->sweep_lanes, c->d_sync, grid, block, c->spin_limit));
         CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
         c->launches++;
         return TRANS_OK;
     }
     if (mode == 1) {
         CK(cudaMemsetAsync(c->d_sync, 0, sizeof(SweepSync), s));
-        CK(c->fl->sweep_all(s, c->sv, c->d_plane_off, nh, lanes, c->d_sync, grid, block));
+        CK(c->fl->sweep_all(s, c->sv, c->d_plane_off, nh, lanes, c->d_sync, grid, block, c->spin_limit));
         CK(cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s));
         c->launches++;
         return TRANS_OK;
@@ -323,8 +324,12 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
                 c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt(h), lanes, c->pdl, d && h - d >= 0 ? c->plane_off[h - d] : 0,
                                    d ? cnt(h - d) : 0);
     };
-    if (capture) {
+    auto count_planes = [&]() {
+        for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
+    };
+    if (capture) {              // captured into the caller's graph: every hyperplane launch counts per replay
         planes();
+        count_planes();
         return TRANS_OK;
     }
     if (!c->sweep_exec) {
@@ -341,7 +346,7 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         c->sweep_exec_pf = c->sweep_pf;
     }
     CK(cudaGraphLaunch(c->sweep_exec, s));
-    for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
+    count_planes();
     return TRANS_OK;
 }
 
