@@ -5,8 +5,13 @@ path for the steady cases (Kchld = 1), Kchld dual-time sub-iterations for the sq
 DES case.  The metric is cell-iterations per second (Mcell-iter/s), each sub-iteration of each
 interior cell counting once.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--case cascade|channel|cylinder]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--case cascade|cascade_medium|channel|cylinder]
                   [--precision fp64|mixed] [--impl gb300|reference]
+
+The default line is the FP64 path on the five-block cascade at the benchmark's block sizes
+(1,966,080 cells) with sub-objects for the same workload in mixed precision (`mixed`), eight
+copies of it in one mixed-precision batch context (`batched`), and a bounded serving stream at
+4 requests/s (`serving`, p50/p99 latency).
 
 --impl reference times the reference's algorithm on the host cores: the C++ FP64 restatement
 in oracle/ (the Fortran reference cannot be built here), parallel over blocks with OpenMP as
@@ -70,10 +75,15 @@ def replica_rate(units_per_rank, seconds, world):
 
 
 def make_case(name, precision, nk=64, metrics_fn=None):
+    """The benchmark workloads: `cascade` is the five-block cascade at the benchmark's block
+    sizes (O 257x49x65, H 65x97x65, passage 97x33x65: 1,966,080 cells), `cascade_medium` the
+    1,359,872-cell layout of the serving medium level."""
     prec = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
     if name == "channel":
         c = cases.channel_bump(precision=prec)
     elif name == "cascade":
+        c = cases.cascade(precision=prec, **dict(cases.CASCADE_CONFIG2, nk=nk))
+    elif name == "cascade_medium":
         c = cases.cascade(nk=nk, precision=prec)
     elif name == "cylinder":
         c = cases.square_cylinder(precision=prec)
@@ -172,6 +182,13 @@ ALG_WORDS = {
 # bytes per face from the same capture (profiles/k_face_flux_fp64_cascade_339968cells.md)
 FACE_FP64_INST = 2541.0
 FACE_DRAM_BYTES = 391.3
+FACE_DRAM_SOURCE = "ncu dram__bytes_read+write per face on the 339,968-cell cascade, scaled by faces"
+# kernel classes that run in FP32 in the mixed path (their algorithmic words are 4 bytes there)
+FP32_KERNELS = ("k_face_flux", "k_gather", "k_sweep", "k_gradient")
+# bounded serving leg of the default line (4 requests/s as the serving configuration states)
+SERVE_DURATION = 10.0
+SERVE_DROP = 1e-1
+SERVE_MAX_ITERS = 2000
 
 
 def units(c, kernel):
@@ -299,11 +316,11 @@ def reference_arm(args):
 
 def batched_leg(c, conns, geo, st, args):
     """N copies of the workload with back-pressure ratios spread over [0.80, 0.92] in one
-    batch context (every kernel one launch for all of them): aggregate cell-iterations/s,
-    timed like the single case (CUDA events, iteration graphs replayed)."""
+    mixed-precision batch context (every kernel one launch for all of them): aggregate
+    cell-iterations/s, timed like the single case (CUDA events, iteration graphs replayed)."""
     import copy
     from trans_gb300.solver import Batch
-    prec = abi.TRANS_MIXED if args.precision == "mixed" else abi.TRANS_FP64
+    prec = abi.TRANS_MIXED
     bt = Batch(prec)
     ratio0 = c.meta.get("p_ratio", 0.85)
     n = args.batch
@@ -323,8 +340,8 @@ def batched_leg(c, conns, geo, st, args):
         raise RuntimeError(f"batched timing failed {rc}")
     ncell = interior_cells(c) * n
     out = {"cases": n, "cells": ncell, "value": ncell * sub_iterations(c) * args.steps / (ms.value * 1e-3) / 1e6,
-           "unit": "Mcell-iter/s", "ms_per_step": ms.value / args.steps,
-           "sweep_schedule": bt.lib.trans_tuning(bt.ctx).decode()[:40]}
+           "unit": "Mcell-iter/s", "ms_per_step": ms.value / args.steps, "precision": "mixed",
+           "device_gb": bt.bytes_in_use() / 1e9, "sweep_schedule": bt.lib.trans_tuning(bt.ctx).decode()[:40]}
     bt.close()
     return out
 
@@ -410,48 +427,65 @@ def serve_arm(args):
     print(json.dumps(line))
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--case", default=os.environ.get("TRANS_BENCH_CASE", "cascade"))
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--nk", type=int, default=64, help="spanwise cells of the cascade (64 = full size)")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
-    ap.add_argument("--batch-levels", default=None,
-                    help="batched cascades at three grid levels: counts C,M,F (e.g. 32,24,8)")
-    ap.add_argument("--batch", type=int, default=0,
-                    help="also time N copies of the workload (back-pressure ratios 0.80..0.92) in one batch context")
-    ap.add_argument("--serve", action="store_true", help="run the serving stream instead (p50/p99 latency)")
-    ap.add_argument("--rate", type=float, default=1.0, help="serving: Poisson arrivals per second")
-    ap.add_argument("--duration", type=float, default=20.0, help="serving: seconds of arrivals")
-    ap.add_argument("--drop", type=float, default=1e-3, help="serving: residual drop at which a request retires")
-    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device-memory budget")
-    args = ap.parse_args()
-    if args.batch_levels:
-        return batch_levels_arm(args)
-    if args.serve:
-        return serve_arm(args)
-    if args.impl == "reference":
-        return reference_arm(args)
-    if args.case == "cascade" and not hasattr(cases, "cascade"):
-        args.case = "channel"
-    rank, world = init_replicas()
-    from trans_gb300.solver import device_block_metrics
-    c, conns, geo, st = make_case(args.case, args.precision, args.nk, metrics_fn=device_block_metrics())
-    ncell = interior_cells(c)
-    nsub = sub_iterations(c)
-    s = Solver(c, conns, geo, st)
+def roofline(lib, c, kt, nsub, precision, sched):
+    """Roofline of the dominant kernel class from per-launch CUDA-event times of one iteration:
+    algorithmic bytes per launch / launch time against the measured HBM copy bandwidth, and the
+    binding roof where it is not HBM (the FP64 pipe of the FP64 face fluxes, the dependent-step
+    latency of the hyperplane sweeps)."""
+    pk = peaks()
+    hbm = pk.get("hbm_gbs", FALLBACK_HBM)
+    fp64 = lib.trans_probe_fma_gflops(1)
+    fp32 = lib.trans_probe_fma_gflops(0)
+    dom = max(kt, key=lambda k: kt[k][0])
+    dom_ms, dom_n = kt[dom]
+    per_launch_ms = dom_ms / dom_n
+    nunit = units(c, dom) * nsub
+    word = 4.0 if precision == "mixed" and dom in FP32_KERNELS else 8.0
+    alg_bytes = ALG_WORDS.get(dom, 0) * word * nunit / dom_n
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "kernel": dom, "launches_per_step": dom_n, "ms_per_launch": per_launch_ms,
+            "alg_bytes_per_launch": alg_bytes,
+            "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
+            "fp64_pipe_gflops_peak_measured": fp64, "fp32_pipe_gflops_peak_measured": fp32}
+    if dom == "k_face_flux" and precision == "fp64":
+        # the binding roof of the FP64 residual is the FP64 pipe: thread-instructions per second
+        # against the probe's FMA rate (one FMA = one FP64 thread-instruction)
+        inst = FACE_FP64_INST * nunit / dom_n / (per_launch_ms * 1e-3)
+        roof["binding"] = "fp64_pipe"
+        roof["fp64_inst_per_s"] = inst
+        roof["fp64_pipe_frac"] = inst / (fp64 * 1e9 / 2.0)
+        roof["traffic"] = FACE_DRAM_BYTES * nunit / dom_n
+        roof["traffic_source"] = FACE_DRAM_SOURCE
+    elif dom == "k_sweep":
+        # the sweeps are bound by one dependent step per i+j+k hyperplane: report the measured
+        # step against the floor of a dependent launch chain of the same width (graph replay)
+        roof["binding"] = "latency (one dependent step per i+j+k hyperplane)"
+        if sched.startswith("sweep=planes"):
+            cells_per_plane = interior_cells(c) * nsub * 2 / dom_n      # dom_n counts both sweeps' hyperplanes
+            grid = max(1, int(round(cells_per_plane * 8 / 128)))
+            floor_us = lib.trans_probe_chain_us(1 if "chained" in sched else 0, grid)
+            roof["latency"] = {"us_per_step": per_launch_ms * 1e3, "floor_us_per_step": floor_us,
+                               "frac": floor_us / (per_launch_ms * 1e3) if floor_us > 0 else None,
+                               "floor": f"dependent launch chain, {grid} CTAs x 128 threads, one L2 round trip per step"}
+    return roof
+
+
+def measure(c, conns, geo, st, precision, args, world):
+    """One context of the workload in `precision`: W warm-up steps (the last with CUDA events
+    around every stage), trans_prepare (untimed tuning and graph capture), K steps timed with
+    CUDA events on the context's stream, clocks sampled meanwhile; then the end-to-end leg
+    through the C ABI with page-locked host buffers and the per-kernel times of one more step."""
+    p = CS.params_copy(c.params)
+    p.precision = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
+    s = Solver(c, conns, geo, st, params=p)
     lib = s.lib
+    ncell, nsub = interior_cells(c), sub_iterations(c)
     ki = 1
-    # W warm-up steps, the last one with CUDA events around every stage (stage_ms)
     for _ in range(max(args.warmup - 1, 0)):
         s.iterate(ki); ki += 1
     stage_ms = (C.c_double * len(abi.STAGES))()
     lib.trans_stage_times(s.ctx, ki, stage_ms); ki += 1
-    # untimed set-up: sweep schedule tuning and capture of the iteration graph (no iteration runs)
     if lib.trans_prepare(s.ctx, ki) != 0:
         raise RuntimeError(f"trans_prepare failed: {lib.trans_last_error(s.ctx)}")
     launches0 = lib.trans_kernel_launches(s.ctx)
@@ -466,75 +500,114 @@ def main():
     clocks = clk.stop()
     ms = max_over_ranks(ms, world)
     value = replica_rate(ncell * nsub * args.steps, ms * 1e-3, world)
-    # end-to-end through the C ABI with pinned host buffers
     e2e_steps = max(2, min(args.steps, 10))
     dt, h2d, d2h = run_e2e(s, c, st, ki, e2e_steps)
+    ki += e2e_steps
     e2e = replica_rate(ncell * nsub * e2e_steps, max_over_ranks(dt, world), world)
-    # roofline of the dominant kernel, from per-launch CUDA events of one more iteration
     kt = kernel_times(s, ki)
-    ki += 1
-    pk = peaks()
-    hbm = pk.get("hbm_gbs", FALLBACK_HBM)
-    fp64 = lib.trans_probe_fma_gflops(1)
-    fp32 = lib.trans_probe_fma_gflops(0)
-    st_ms = {n: stage_ms[i] for i, n in enumerate(abi.STAGES)}
-    dom = max(kt, key=lambda k: kt[k][0])
-    dom_ms, dom_n = kt[dom]
-    per_launch_ms = dom_ms / dom_n
-    nunit = units(c, dom) * nsub
-    alg_bytes = ALG_WORDS.get(dom, 0) * 8.0 * nunit / dom_n
-    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9
-    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "kernel": dom, "launches_per_step": dom_n, "ms_per_launch": per_launch_ms,
-            "peak_source": "measured" if "hbm_gbs" in pk else "fallback",
-            "fp64_pipe_gflops_peak_measured": fp64, "fp32_pipe_gflops_peak_measured": fp32}
-    if dom == "k_face_flux" and args.precision == "fp64":
-        # the binding roof of the FP64 residual is the FP64 pipe: thread-instructions per second
-        # against the probe's FMA rate (one FMA = one FP64 thread-instruction)
-        inst = FACE_FP64_INST * nunit / dom_n / (per_launch_ms * 1e-3)
-        roof["binding"] = "fp64_pipe"
-        roof["fp64_inst_per_s"] = inst
-        roof["fp64_pipe_frac"] = inst / (fp64 * 1e9 / 2.0)
-        roof["traffic"] = FACE_DRAM_BYTES * nunit / dom_n
-        roof["traffic_source"] = "ncu dram__bytes_read+write per face on the 339,968-cell cascade, scaled by faces"
-    elif dom == "k_sweep":
-        # the sweeps are bound by one dependent step per i+j+k hyperplane: report the measured
-        # step against the floor of a dependent launch chain of the same width (graph replay)
-        sched = lib.trans_tuning(s.ctx).decode()
-        roof["binding"] = "latency (one dependent step per i+j+k hyperplane)"
-        if sched.startswith("sweep=planes"):
-            cells_per_plane = ncell * nsub * 2 / dom_n      # dom_n counts both sweeps' hyperplanes
-            grid = max(1, int(round(cells_per_plane * 8 / 128)))
-            floor_us = lib.trans_probe_chain_us(1 if "chained" in sched else 0, grid)
-            roof["latency"] = {"us_per_step": per_launch_ms * 1e3, "floor_us_per_step": floor_us,
-                               "frac": floor_us / (per_launch_ms * 1e3) if floor_us > 0 else None,
-                               "floor": f"dependent launch chain, {grid} CTAs x 128 threads, one L2 round trip per step"}
+    sched = lib.trans_tuning(s.ctx).decode()
+    out = {"value": value, "unit": "Mcell-iter/s", "ms_per_step": ms / args.steps,
+           "e2e": {"value": e2e, "unit": "Mcell-iter/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "gpu_launches": int(launches), "clocks": clocks,
+           "roofline": roofline(lib, c, kt, nsub, precision, sched),
+           "stage_ms": {n: stage_ms[i] for i, n in enumerate(abi.STAGES)},
+           "kernel_ms": {k: round(v[0], 4) for k, v in sorted(kt.items(), key=lambda x: -x[1][0])},
+           "device_gb": lib.trans_device_bytes(s.ctx) / 1e9, "sweep_schedule": sched}
+    s.close()
+    return out
+
+
+def serving_leg(args):
+    """Bounded serving stream (mixed precision): seeded Poisson arrivals at `--rate` per second
+    for `--duration` seconds, grid level coarse 60% / medium 30% / fine 10%, back-pressure ratio
+    U[0.80, 0.92], inlet Mach U[0.5, 0.7], admission under a `--budget-gb` device budget, each
+    request retired at a `--drop` residual drop or after `--max-iters` iterations."""
+    from trans_gb300 import serving
+    reqs = serving.poisson_requests(rate=args.rate, duration=args.duration, seed=0)
+    rep = serving.serve(reqs, precision=abi.TRANS_MIXED, budget_bytes=int(args.budget_gb * 1e9), drop=args.drop,
+                        max_iters=args.max_iters, prep_workers=args.prep_workers)
+    recs = rep.pop("records")
+    by_level = {}
+    for r in recs:
+        by_level.setdefault(r.level, []).append(r.iterations)
+    return {"p50_s": rep["latency_p50_s"], "p99_s": rep["latency_p99_s"], "unit": "s",
+            "throughput_mcell_iter_s": rep["throughput_mcell_iter_s"], "precision": "mixed",
+            "rate_per_s": args.rate, "duration_s": args.duration, "retire_at_drop": args.drop,
+            "max_iters": args.max_iters, "budget_gb": args.budget_gb, "mix": "coarse 0.6 / medium 0.3 / fine 0.1",
+            "requests": rep["requests"], "completed": rep["completed"], "converged": rep["converged"],
+            "hit_iteration_cap": sum(r.status == "max_iters" for r in recs),
+            "nan": sum(r.status == "nan" for r in recs), "wall_s": rep["wall_s"],
+            "iterations_by_level": {k: [min(v), int(np.median(v)), max(v)] for k, v in by_level.items()},
+            "setup_s_median_by_level": rep["setup_s_by_level"]}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--case", default=os.environ.get("TRANS_BENCH_CASE", "cascade"))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"], help="precision of the headline value")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nk", type=int, default=64, help="spanwise cells of the cascade (64 = full size)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
+    ap.add_argument("--batch-levels", default=None,
+                    help="batched cascades at three grid levels: counts C,M,F (e.g. 32,24,8)")
+    ap.add_argument("--batch", type=int, default=8,
+                    help="copies of the workload (back-pressure ratios 0.80..0.92) in one mixed batch context (0: none)")
+    ap.add_argument("--serve", action="store_true", help="run only the serving stream (p50/p99 latency)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--rate", type=float, default=4.0, help="serving: Poisson arrivals per second")
+    ap.add_argument("--duration", type=float, default=SERVE_DURATION, help="serving: seconds of arrivals")
+    ap.add_argument("--drop", type=float, default=SERVE_DROP, help="serving: residual drop at which a request retires")
+    ap.add_argument("--max-iters", type=int, default=SERVE_MAX_ITERS, help="serving: iteration cap of a request")
+    ap.add_argument("--prep-workers", type=int, default=4, help="serving: host set-up threads")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: device-memory budget")
+    args = ap.parse_args()
+    if args.batch_levels:
+        return batch_levels_arm(args)
+    if args.serve:
+        return serve_arm(args)
+    if args.impl == "reference":
+        return reference_arm(args)
+    rank, world = init_replicas()
+    from trans_gb300.solver import device_block_metrics
+    c, conns, geo, st = make_case(args.case, "fp64", args.nk, metrics_fn=device_block_metrics())
+    ncell = interior_cells(c)
+    nsub = sub_iterations(c)
+    head = measure(c, conns, geo, st, args.precision, args, world)
     line = {
-        "metric": "Mcell-iter/s", "value": value, "unit": "Mcell-iter/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "metric": "Mcell-iter/s", "value": head["value"], "unit": "Mcell-iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32-flux/f64-update",
         "data": "synthetic",
-        "config": {"workload": c.name, "cells": ncell, "blocks": len(c.blocks), "precision": args.precision,
+        "config": {"workload": c.name, "cells": ncell, "blocks": len(c.blocks),
+                   "block_nodes": [list(b.dims) for b in c.blocks], "precision": args.precision,
                    "sub_iterations_per_step": nsub,
-                   "l2": f"working set {lib.trans_device_bytes(s.ctx) / 1e9:.2f} GB > L2 (no flush needed)",
-                   "sweep_schedule": lib.trans_tuning(s.ctx).decode()},
-        "e2e": {"value": e2e, "unit": "Mcell-iter/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": int(launches),
-        "clocks": clocks,
-        "roofline": roof,
-        "stage_ms": st_ms,
-        "kernel_ms": {k: round(v[0], 4) for k, v in sorted(kt.items(), key=lambda x: -x[1][0])},
+                   "l2": f"working set {head['device_gb']:.2f} GB > L2 (no flush needed)",
+                   "sweep_schedule": head["sweep_schedule"]},
+        "e2e": head["e2e"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
+        "roofline": head["roofline"], "stage_ms": head["stage_ms"], "kernel_ms": head["kernel_ms"],
     }
+    if not args.no_mixed and args.precision == "fp64":
+        m = measure(c, conns, geo, st, "mixed", args, world)
+        m["vs_fp64"] = m["value"] / head["value"]
+        m["e2e_vs_fp64"] = m["e2e"]["value"] / head["e2e"]["value"]
+        line["mixed"] = m
     if args.batch > 1:
-        line["batched"] = batched_leg(c, conns, geo, st, args)
+        b = batched_leg(c, conns, geo, st, args)
+        b["vs_fp64"] = b["value"] / head["value"]
+        line["batched"] = b
+    if rank == 0 and not args.no_serve and world == 1:
+        line["serving"] = serving_leg(args)
     if rank == 0 and not args.no_cpu:
         v, n, dt2 = cpu_sample(c, conns, geo, st)
         line["cpu_baseline"] = {"value": v, "unit": "Mcell-iter/s", "cores": 1, "kind": "port",
                                 "sample": f"{n} iterations of {c.name} on one core ({dt2:.1f} s)"}
     if rank == 0:
         print(json.dumps(line))
-    s.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

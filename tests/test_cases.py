@@ -24,8 +24,9 @@ def _face_centre(X, c, i, j, k):
     return np.mean([X[q[0] - 1, q[1] - 1, q[2] - 1] for q in ids], axis=0)
 
 
-@pytest.mark.parametrize("make", [lambda: cases.cascade(**SMALL_CASCADE), lambda: cases.channel_bump(25, 17, 6)],
-                         ids=["cascade", "channel"])
+@pytest.mark.parametrize("make", [lambda: cases.cascade(**SMALL_CASCADE), lambda: cases.channel_bump(25, 17, 6),
+                                  lambda: cases.cascade(**dict(cases.CASCADE_CONFIG2, nk=4))],
+                         ids=["cascade", "channel", "cascade_config2_layout"])
 def test_interfaces_match_node_for_node(make):
     c = make()
     conns = C.derive_connectivity(c.blocks)
@@ -58,6 +59,18 @@ def test_cascade_block_sizes():
     assert (257, 49, 65) in dims
     assert dims.count((65, 41, 65)) == 2
     assert dims.count((121, 17, 65)) == 2
+
+
+def test_cascade_config2_block_sizes():
+    """The benchmark cascade: O-block 257x49x65 and passage blocks 97x33x65 as stated; the
+    H-blocks take the 97 pitchwise nodes the 1-to-1 interfaces force; at least the stated
+    1,507,328 interior cells."""
+    c = cases.cascade(**cases.CASCADE_CONFIG2)
+    dims = [b.dims for b in c.blocks]
+    assert dims[0] == (257, 49, 65)
+    assert dims.count((97, 33, 65)) == 2 and dims.count((65, 97, 65)) == 2
+    cells = sum((a - 1) * (b - 1) * (d - 1) for a, b, d in dims)
+    assert cells == 1966080 >= 1507328
 
 
 def test_cascade_metrics_positive():

@@ -1,0 +1,151 @@
+"""GPU FP64 path against the CPU oracle on the configurations and switches the scheme-set tests
+do not reach, through the C ABI:
+
+- the channel bump at its benchmark size (97x49x9 nodes, 36,864 cells) for 100 iterations;
+- the five-block cascade at the benchmark's block sizes (1,966,080 cells) for 3 iterations;
+- the DDES shielding functions of Time/Hybrid_function.F90:1-38 (Kind_SubHY = 1, 2, 3) under
+  the DES length scale of Time/TURBTWO_TIME_LUSGS_SST.F90:192-213;
+- Suzen's compressibility correction (IF_Comppress = 1, Time/TURBTWO_TIME_LUSGS_SST.F90:339-397);
+- the fixed-transition switch (If_fix_Transition = 1: no k source upstream of Trans_location,
+  Time/TURBTWO_TIME_LUSGS_SST.F90:291-293);
+- a symmetry plane (kind 3, BC/BC_Symm.F90:42-121), stage by stage and over iterations.
+
+Bar: bit-identical states (the FP64 kernels and the oracle round every operation alike) and
+the residual history within 1e-11 relative (summation order).
+"""
+import numpy as np
+import pytest
+
+from helpers import G, bit_equal_fraction, face_ghosts, interior, rel_err, small_channel
+
+TOL = 1e-11
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(c, conns, geo, st, threads=None):
+    from oracle.oracle import OracleSolver, load
+    from trans_gb300.solver import Solver
+    if threads:
+        load().oracle_set_threads(threads)
+    return Solver(c, conns, geo, st), OracleSolver(c, conns, geo, st)
+
+
+def _run_bitwise(c, conns, geo, st, iters, fields=("V", "PP", "T", "RMIU"), threads=None):
+    g, o = _pair(c, conns, geo, st, threads)
+    hg, ho = [], []
+    for ki in range(1, iters + 1):
+        ng, no = g.iterate(ki), o.iterate(ki)
+        hg.append([n["DRSa"] for n in ng]); ho.append([n["DRSa"] for n in no])
+    hg, ho = np.array(hg), np.array(ho)
+    hist = np.max(np.abs(hg - ho) / np.abs(ho))
+    assert hist <= TOL, f"residual history differs by {hist:.3e}"
+    for ib, b in enumerate(c.blocks):
+        m = interior(b.dims)
+        for name in fields:
+            a, r = g.get_field(ib, name), o.get_field(ib, name)
+            frac = bit_equal_fraction(a, r, m)
+            assert frac == 1.0, f"block {b.id} {name}: {frac:.6f} bit-identical, rel err {np.max(rel_err(a, r, m)):.3e}"
+    g.close(); o.close()
+    return hg
+
+
+def test_channel_benchmark_size_100_iterations(gpu_lib):
+    """The channel bump as the benchmark states it: 97x49x9 nodes, MUSCL + Roe, SST, CFL 5."""
+    from trans_gb300 import case as CS
+    from trans_gb300 import cases
+    c = cases.channel_bump()
+    assert c.blocks[0].dims == (97, 49, 9)
+    conns, geo = CS.compute_geometry(c)
+    st = CS.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
+    hist = _run_bitwise(c, conns, geo, st, 100)
+    assert np.all(np.isfinite(hist))
+
+
+def test_cascade_benchmark_size_3_iterations(gpu_lib):
+    """The benchmarked cascade at full size (O 257x49x65, H 65x97x65, passage 97x33x65;
+    MDCD + AUSMPW+, SST, CFL 10): 3 iterations bit-identical in every block."""
+    from trans_gb300 import case as CS
+    from trans_gb300 import cases
+    from trans_gb300.solver import device_block_metrics
+    c = cases.cascade(**cases.CASCADE_CONFIG2)
+    conns, geo = CS.compute_geometry(c, metrics_fn=device_block_metrics())
+    st = CS.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
+    _run_bitwise(c, conns, geo, st, 3, threads=8)
+
+
+DES = dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3)
+
+
+@pytest.mark.parametrize("subhy", [1, 2, 3])
+def test_ddes_shielding_functions(gpu_lib, subhy):
+    """Kind_Hybrid = 3 with Menter's F1 (1), Menter's F2 (2) and Spalart's F1 (3) shielding."""
+    c, conns, geo, st = small_channel(Kind_SubHY=subhy, **DES)
+    _run_bitwise(c, conns, geo, st, 20)
+
+
+@pytest.mark.parametrize("hybrid", [0, 3], ids=["rans", "des"])
+def test_suzen_compressibility_correction(gpu_lib, hybrid):
+    c, conns, geo, st = small_channel(Kind_Spatial=3, Kind_Roe=3, IF_Comppress=1, Kind_Hybrid=hybrid)
+    _run_bitwise(c, conns, geo, st, 20)
+
+
+def test_fixed_transition(gpu_lib):
+    """If_fix_Transition = 1 with Trans_location halfway along the channel: the k source is
+    zero in the cells whose centre lies upstream of it."""
+    from trans_gb300 import case as CS
+    from trans_gb300 import cases
+    probe = cases.channel_bump(ni=25, nj=17, nk=6)
+    c = cases.channel_bump(ni=25, nj=17, nk=6, Kind_Spatial=3, Kind_Roe=3, If_fix_Transition=1,
+                           Trans_location=0.5 / probe.params.Alscale)
+    conns, geo = CS.compute_geometry(c)
+    xc = geo[c.blocks[0].id]["XC"][interior(c.blocks[0].dims)]
+    assert np.any(xc < c.params.Trans_location) and np.any(xc > c.params.Trans_location)
+    st = CS.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
+    _run_bitwise(c, conns, geo, st, 20)
+
+
+def _symmetry_case():
+    """The channel with a symmetry plane on top.  BC_Symm sets every ghost value of the three
+    layers except the density of layer 2 (BC/BC_Symm.F90:70-79), which keeps what the restart
+    held: the ghost density is filled with the free-stream value, as in a restart of a run."""
+    c, conns, geo, st = small_channel(Kind_Spatial=2, Kind_Roe=1, top=3)
+    for b in c.blocks:
+        V = st[b.id]["V"]
+        m = ~interior(b.dims)
+        V[0][m] = 1.0
+    return c, conns, geo, st
+
+
+def test_symmetry_plane_bc_state_stage(gpu_lib):
+    """BC_STATE on the three ghost layers of every face (the symmetry plane among them), then
+    the gradients and their ghost copies, against the oracle."""
+    c, conns, geo, st = _symmetry_case()
+    g, o = _pair(c, conns, geo, st)
+    dims = c.blocks[0].dims
+    ni, nj, nk = dims
+    top = np.zeros((ni + 5, nj + 5, nk + 5), bool, order="F")
+    top[G + 1:G + ni, G + nj:G + nj + 3, G + 1:G + nk] = True
+    for ki in (1, 2):
+        for stage in ("SPECRAD", "BC_STATE", "GRADIENT", "BC_GRAD", "RESIDUAL", "LUSGS", "UPDATE", "UPDATE_U"):
+            g.run_stage(stage, ki)
+            o.run_stage(stage, ki)
+            if stage == "BC_STATE":
+                for name in ("V", "PP", "T", "RMIU"):
+                    a, b = g.get_field(0, name), o.get_field(0, name)
+                    assert bit_equal_fraction(a, b, top) == 1.0, (ki, name)
+                    assert bit_equal_fraction(a, b, face_ghosts(dims, 3)) == 1.0, (ki, name)
+            if stage == "BC_GRAD":
+                a, b = g.get_field(0, "DQDXYZ"), o.get_field(0, "DQDXYZ")
+                assert bit_equal_fraction(a, b, face_ghosts(dims, 1)) == 1.0, ki
+    # the mirrored normal velocity: the layer-1 ghost's normal momentum is the negative of the
+    # first interior cell's (flat top, normal along +y)
+    V = g.get_field(0, "V")
+    assert np.allclose(V[2][G + 1:G + ni, G + nj, G + 1:G + nk], -V[2][G + 1:G + ni, G + nj - 1, G + 1:G + nk],
+                       rtol=1e-12, atol=1e-14)
+    g.close(); o.close()
+
+
+def test_symmetry_plane_iterations(gpu_lib):
+    c, conns, geo, st = _symmetry_case()
+    _run_bitwise(c, conns, geo, st, 30)

@@ -55,8 +55,8 @@ def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, to
 
     x in [-L, 2L], bump y = h sin^2(pi x / L) on [0, L], top at y = L, span `span` L.
     BCs: i-min inlet (kind 5), i-max outlet (kind 7), j-min no-slip wall (kind 1),
-    j-max far field (kind 2; `top`=1 makes it a second no-slip wall), k faces 1-to-1 onto each
-    other (kind 9, periodic span).
+    j-max far field (kind 2; `top`=1 makes it a second no-slip wall, `top`=3 a symmetry plane),
+    k faces 1-to-1 onto each other (kind 9, periodic span).
     """
     ph = _flow(XM)
     sw = dict(Kind_Spatial=2, Kind_Roe=1, CFL_Sub_start=5.0, CFL_Sub_end=5.0, CFL_Sub_step=1,
@@ -79,13 +79,13 @@ def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, to
         X[:, j, :, 1] = (yw + (1.0 - yw) * s[j])[:, None]
     X[:, :, :, 2] = z[None, None, :]
     X /= alscale
-    if top not in (1, 2):
-        raise ValueError("top boundary: kind 2 (far field) or 1 (wall)")
+    if top not in (1, 2, 3):
+        raise ValueError("top boundary: kind 2 (far field), 1 (wall) or 3 (symmetry)")
     segs = [Segment(1, kind=5), Segment(2, kind=7), Segment(3, kind=1), Segment(4, kind=top),
             Segment(5, kind=9, blk_ex=1, blkbd_ex=6), Segment(6, kind=9, blk_ex=1, blkbd_ex=5)]
     b = Block(1, X, segs, walls=[(3, 0, 0, 0, 0)] + ([(4, 0, 0, 0, 0)] if top == 1 else []))
     walls = [X[:, 0, :, :]] + ([X[:, -1, :, :]] if top == 1 else [])
-    return Case("channel_bump_%dx%dx%d" % (ni, nj, nk) + ("" if top == 2 else "_walls"), p, [b], walls, ph,
+    return Case("channel_bump_%dx%dx%d" % (ni, nj, nk) + {1: "_walls", 2: "", 3: "_symm"}[top], p, [b], walls, ph,
                 dict(Q_dst=0.05 / alscale, iterations=300))
 
 
@@ -167,6 +167,16 @@ def _two_sided(n, first):
     """n cells on [0,1] clustered at both ends with first spacing `first` (n even)."""
     h = geometric_spacing(n // 2, first, 0.5)
     return np.concatenate([h, 1.0 - h[::-1][1:]])
+
+
+# The five-block cascade at the sizes of the benchmark configuration: O-block 257x49x65 and
+# passage blocks 97x33x65 as stated.  With 1-to-1 interfaces the H-blocks' pitchwise node count
+# is forced: their face towards the blade is the two passage blocks' pitch edges plus the
+# O-block's leading-edge (or trailing-edge) cap, 2*npitch + nle = 2*32 + 32 = 96 cells, and the
+# O-block loop is 2*ns + 2*nte + nle = 2*96 + 2*16 + 32 = 256 cells.  (H-blocks of 41 pitchwise
+# nodes would force passage blocks of at most 121x17 nodes, 10% fewer cells in all.)  Interior
+# cells: 786,432 + 2 x 393,216 + 2 x 196,608 = 1,966,080.
+CASCADE_CONFIG2 = dict(ns=96, npitch=32, nle=32, nte=16, nr=48, nh=64, nk=64)
 
 
 def cascade(nle=8, nte=4, ns=120, npitch=16, nr=48, nh=64, nk=64, Re_c=1.0e6, XM=0.6, inflow_deg=40.0,
