@@ -1540,6 +1540,42 @@ double fsst(const trans_params& p, double Den, double vK, double vOmega, double 
     return 0.0;
 }
 
+// IDDES functions of Time/Hybrid_function.F90:43-105 (Kind_SubHY = 5).  The constants
+// akapa_iddes, Cw, Ct, Cl are Module_Global.F90:126; their squares are constant expressions
+// (0.41**2. folds to 0.41*0.41); the real exponents of variables (aDst**2., (Cl**2.*rdl)**10.)
+// are evaluated by the pow of tmath, as every real-exponent power of this restatement.
+// g: the nine velocity gradients dudx, dudy, dudz, dvdx, ..., dwdz.
+constexpr double KAPPA_IDDES2 = 0.41 * 0.41, CT_IDDES2 = 1.87 * 1.87, CL_IDDES2 = 5.00 * 5.00, CW_IDDES = 0.15;
+
+double sij_norm(const double* g) {
+    double s = g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + g[3] * g[3] + g[4] * g[4] + g[5] * g[5] + g[6] * g[6] +
+               g[7] * g[7] + g[8] * g[8];
+    s = std::sqrt(s);
+    return std::max(s, 1.0e-10);
+}
+
+double fd_function(const trans_params& p, double Den1, double RmiuT1, double aDst1, double aLmax1, const double* g) {
+    double alpha1 = 0.25 - aDst1 / aLmax1;
+    double fb = std::min(2. * otm::exp_(-9.0 * alpha1 * alpha1), 1.);
+    double Sij = sij_norm(g);
+    double rdt = (RmiuT1 / Den1) / (KAPPA_IDDES2 * otm::pow_(aDst1, 2.) * Sij * p.Ref);
+    double fdt = 1. - otm::tanh_((8. * rdt) * (8. * rdt) * (8. * rdt));
+    return std::max((1. - fdt), fb);
+}
+
+double fe_function(const trans_params& p, double Den2, double RmiuT2, double RmiuL2, double aDst2, double aLmax2,
+                   const double* g) {
+    double alpha2 = 0.25 - aDst2 / aLmax2;
+    double fe1 = alpha2 >= 0. ? 2. * otm::exp_(-11.09 * alpha2 * alpha2) : 2. * otm::exp_(-9. * alpha2 * alpha2);
+    double Sij = sij_norm(g);
+    double rdt = (RmiuT2 / Den2) / (KAPPA_IDDES2 * otm::pow_(aDst2, 2.) * Sij * p.Ref);
+    double ft = otm::tanh_((CT_IDDES2 * rdt) * (CT_IDDES2 * rdt) * (CT_IDDES2 * rdt));
+    double rdl = (RmiuL2 / Den2) / (KAPPA_IDDES2 * otm::pow_(aDst2, 2.) * Sij * p.Ref);
+    double fl = otm::tanh_(otm::pow_(CL_IDDES2 * rdl, 10.));
+    double fe2 = 1. - std::max(ft, fl);
+    return fe2 * std::max((fe1 - 1.), 0.);
+}
+
 // Wilcox 2006 k-omega sources and diagonal of one cell (Kind_Model = 2,
 // Time/TURBTWO_TIME_LUSGS_SST.F90:418-547)
 void wd2006_sources(Ctx& c, Blk& b, int I, int J, int K) {
@@ -1644,6 +1680,8 @@ void turbtwo_lusgs_sst(Ctx& c, Blk& b) {
         double TT = b.T(I, J, K);
         double RmiuL = (1.0 + p.Csthlnd) / (TT * p.Csth1 + p.Csthlnd) * p15(p.Csth1 * TT);
         double Fdes = 1.0;
+        double alIDDES = 1.0;
+        const bool iddes = p.Kind_Hybrid == 3 && p.Kind_SubHY == 5;
         if (p.Kind_Hybrid == 3) {
             double aLt = std::sqrt(ARTk / ARo) / (p.Beta_star * ARTO / ARo * p.Ref);
             double Cdiff_DDES_S = (2. * 0.856 / Vomega_prev) / p.Ref * cdif;
@@ -1651,10 +1689,24 @@ void turbtwo_lusgs_sst(Ctx& c, Blk& b) {
             double vOmega = ARTO / ARo;
             Vomega_prev = vOmega;
             double aDst = b.Dst(I, J, K);
+            // FSST has no branch for Kind_SubHY = 5 (its result is undefined there); with IDDES the
+            // Fdes it feeds is overwritten below before it is used, so 0 stands in for it
             double Fsst_DES = fsst(p, Den, vk, vOmega, aDst, RmiuL, Cdiff_DDES_S);
             double aLgrd = ((1. - arg1_prev) * 0.61 + arg1_prev * 0.78) * b.ALeng(I, J, K);
             Fdes = std::max(aLt * (1. - Fsst_DES) / aLgrd, 1.0);
             b.FunDES(I, J, K) = aLt * (1. - Fsst_DES) / aLgrd;
+            if (iddes) {            // Time/TURBTWO_TIME_LUSGS_SST.F90:218-252
+                double aLmax = b.ALeng(I, J, K), aLmin = b.ASeng(I, J, K);
+                double Cdes = (1. - arg1_prev) * 0.61 + arg1_prev * 0.78;     // Ciddes_epsi, Ciddes_omeg
+                double dlt_IDDES = std::min(std::max(std::max(CW_IDDES * aLmax, CW_IDDES * aDst), aLmin), aLmax);
+                aLgrd = Cdes * dlt_IDDES;
+                const double g[9] = {dudx, dudy, dudz, dvdx, dvdy, dvdz, dwdx, dwdy, dwdz};
+                double RmiuT = b.Rmiu(I, J, K);
+                double fd = fd_function(p, Den, RmiuT, aDst, aLmax, g);
+                double fe = fe_function(p, Den, RmiuT, RmiuL, aDst, aLmax, g);
+                alIDDES = (1. + fe) * fd * aLt + (1. - fd) * aLgrd;
+                b.FunDES(I, J, K) = aLt / alIDDES;
+            }
         }
         double DistN = b.Dst(I, J, K);
         double CDKO = std::max(2.0 * ARo * p.Sigo2 / (ARTO / ARo) * cdif, 1.0e-10);
@@ -1686,6 +1738,15 @@ void turbtwo_lusgs_sst(Ctx& c, Blk& b) {
             CnegTk = std::fabs(SourceN1);
         }
         if (fixsrc != 0.0) Source = 0.0;
+        if (iddes) {        // the IDDES destruction (TURBTWO_TIME_LUSGS_SST.F90:299-310, 354-366)
+            if (p.IF_Comppress == 0)
+                SourceN1 = -2.0 / 3.0 * std::max(Div, 0.0) - std::sqrt(ARTk / ARo) / alIDDES;
+            else
+                SourceN1 = -2.0 / 3.0 * std::max(Div, 0.0) - (1. + (1. - arg1) * (Alf1 - Alf3) * Mt * Mt) * std::sqrt(ARTk / ARo) / alIDDES;
+            Source = SourceP + SourceN1 * ARTk;
+            CnegTk = std::fabs(-2.0 / 3.0 * std::max(Div, 0.0) - 1.5 * std::sqrt(ARTk / ARo) / alIDDES);
+            if (fixsrc != 0.0) Source = 0.0;
+        }
         b.D(6, I, J, K) = b.D(6, I, J, K) + Source;
         tprod = std::min(prod, Votg) / p.Ref;
         double GamaAB = p.Gama1 * arg1 + p.Gama2 * (1.0 - arg1);
@@ -2092,7 +2153,8 @@ int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks,
     if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4) return TRANS_E_ARG;
     if (p->Kind_Roe < 1 || p->Kind_Roe > 3) return TRANS_E_ARG;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return TRANS_E_ARG;
-    if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 3)) return TRANS_E_ARG;
+    // DES (0), the DDES shielding functions (1-3) and IDDES (5); FSST is undefined for 4
+    if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 5 || p->Kind_SubHY == 4)) return TRANS_E_ARG;
     if (p->omega[0] != 0.0 || p->omega[1] != 0.0 || p->omega[2] != 0.0) return TRANS_E_ARG;
     if (p->IF_RK != 0 && p->IF_RK != 1) return TRANS_E_ARG;
     Ctx* c = new Ctx();

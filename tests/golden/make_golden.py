@@ -6,7 +6,7 @@ seeded synthetic cases of trans_gb300/cases.py.  They pin the oracle across mach
 compilers, and the GPU tests compare the CUDA path with them; they are not an independent
 check of the oracle against the reference.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name ...]     (default: every case)
 """
 import json
 import os
@@ -32,6 +32,7 @@ CASES = {
     "cascade_small_mdcdhyb_ausmpw": ("cascade", dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05)),
     "channel_small_mdcd_ausmpw_wd2006": ("channel", dict(Kind_Spatial=3, Kind_Roe=3, Kind_Model=2)),
     "cascade_small_mdcd_roerot": ("cascade", dict(Kind_Spatial=3, Kind_Roe=2)),
+    "channel_small_mdcd_ausmpw_iddes": ("channel", dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3, Kind_SubHY=5)),
 }
 
 
@@ -78,7 +79,9 @@ def record(kind, sw):
 
 
 def main():
-    for name, (kind, sw) in CASES.items():
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        kind, sw = CASES[name]
         g = record(kind, sw)
         g["generator"] = "tests/golden/make_golden.py (oracle, %d iterations)" % NITER
         with open(os.path.join(HERE, name + ".json"), "w") as f:

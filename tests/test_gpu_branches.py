@@ -4,7 +4,7 @@ do not reach, through the C ABI:
 - the channel bump at its benchmark size (97x49x9 nodes, 36,864 cells) for 100 iterations;
 - the five-block cascade at the benchmark's block sizes (1,966,080 cells) for 3 iterations;
 - the DDES shielding functions of Time/Hybrid_function.F90:1-38 (Kind_SubHY = 1, 2, 3) under
-  the DES length scale of Time/TURBTWO_TIME_LUSGS_SST.F90:192-213;
+  the DES length scale of Time/TURBTWO_TIME_LUSGS_SST.F90:192-213, and IDDES (Kind_SubHY = 5);
 - Suzen's compressibility correction (IF_Comppress = 1, Time/TURBTWO_TIME_LUSGS_SST.F90:339-397);
 - the fixed-transition switch (If_fix_Transition = 1: no k source upstream of Trans_location,
   Time/TURBTWO_TIME_LUSGS_SST.F90:291-293);
@@ -77,11 +77,35 @@ def test_cascade_benchmark_size_3_iterations(gpu_lib):
 DES = dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3)
 
 
-@pytest.mark.parametrize("subhy", [1, 2, 3])
+@pytest.mark.parametrize("subhy", [1, 2, 3, 5])
 def test_ddes_shielding_functions(gpu_lib, subhy):
-    """Kind_Hybrid = 3 with Menter's F1 (1), Menter's F2 (2) and Spalart's F1 (3) shielding."""
+    """Kind_Hybrid = 3 with Menter's F1 (1), Menter's F2 (2) and Spalart's F1 (3) shielding, and
+    IDDES (5): its length scale from fd/fe (Time/Hybrid_function.F90:43-105) and its own k
+    destruction and diagonal (Time/TURBTWO_TIME_LUSGS_SST.F90:218-252, 299-310)."""
     c, conns, geo, st = small_channel(Kind_SubHY=subhy, **DES)
     _run_bitwise(c, conns, geo, st, 20)
+
+
+def test_iddes_with_compressibility_and_transition(gpu_lib):
+    """IDDES with Suzen's correction of its destruction (:354-366) and the fixed-transition
+    switch inside the IDDES branch."""
+    from trans_gb300 import case as CS
+    from trans_gb300 import cases
+    probe = cases.channel_bump(ni=25, nj=17, nk=6)
+    c = cases.channel_bump(ni=25, nj=17, nk=6, Kind_SubHY=5, IF_Comppress=1, If_fix_Transition=1,
+                           Trans_location=0.5 / probe.params.Alscale, **DES)
+    conns, geo = CS.compute_geometry(c)
+    st = CS.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
+    _run_bitwise(c, conns, geo, st, 20)
+
+
+def test_undefined_shielding_switch_rejected(gpu_lib):
+    """Kind_SubHY = 4 has no branch in FSST (its result would be undefined): refused."""
+    from trans_gb300 import abi
+    from trans_gb300.solver import Solver, SolverError
+    c, conns, geo, st = small_channel(Kind_SubHY=4, **DES)
+    with pytest.raises(SolverError, match=str(abi.TRANS_E_ARG)):
+        Solver(c, conns, geo, st)
 
 
 @pytest.mark.parametrize("hybrid", [0, 3], ids=["rans", "des"])

@@ -167,6 +167,22 @@ template <typename R> __device__ inline R ttanh(R x);
 template <> __device__ inline double ttanh<double>(double x) { return tmx::tanh_(x); }
 template <> __device__ inline float ttanh<float>(float x) { return tanhf(x); }
 
+// exp: the bit-reproducible FP64 restatement, or the CUDA single-precision function
+template <typename R> __device__ inline R texp(R x);
+template <> __device__ inline double texp<double>(double x) { return tmx::exp_(x); }
+template <> __device__ inline float texp<float>(float x) { return expf(x); }
+// x**2. and x**10. of a Fortran real exponent: the pow of tmath in FP64 (as the oracle),
+// products in FP32
+template <typename R> __device__ inline R pow2_real(R x);
+template <> __device__ inline double pow2_real<double>(double x) { return tmx::pow_(x, 2.0); }
+template <> __device__ inline float pow2_real<float>(float x) { return x * x; }
+template <typename R> __device__ inline R pow10_real(R x);
+template <> __device__ inline double pow10_real<double>(double x) { return tmx::pow_(x, 10.0); }
+template <> __device__ inline float pow10_real<float>(float x) {
+    const float x2 = x * x, x4 = x2 * x2;
+    return x4 * x4 * x2;
+}
+
 // Sutherland viscosity (Time/SpectralRadius.F90:59 and every copy of it)
 template <typename R> __device__ inline R mu_suth(const ParamsT<R>& p, R TT) {
     return (R(1.0) + R(p.Csthlnd)) / (TT * R(p.Csth1) + R(p.Csthlnd)) * p15(R(p.Csth1) * TT);
@@ -500,7 +516,42 @@ __device__ inline R fsst(const ParamsT<R>& p, R Den, R vK, R vOmega, R Dist, R R
         R arg = dmax(arg1, arg2);
         return ttanh(arg * arg);
     }
-    return R(0.0);
+    return R(0.0);      // DES (0); no branch for IDDES (5), whose destruction does not use it
+}
+
+// IDDES functions of Time/Hybrid_function.F90:43-105 (Kind_SubHY = 5), constants of
+// Module_Global.F90:126 (akapa_iddes 0.41, Cw 0.15, Ct 1.87, Cl 5.00; their squares folded as
+// products); g = the nine velocity gradients dudx, dudy, dudz, dvdx, ..., dwdz
+template <typename R> __device__ inline R sij_norm(const R* g) {
+    R s = g[0] * g[0] + g[1] * g[1] + g[2] * g[2] + g[3] * g[3] + g[4] * g[4] + g[5] * g[5] + g[6] * g[6] + g[7] * g[7] +
+          g[8] * g[8];
+    s = sqrt(s);
+    return dmax(s, R(1.0e-10));
+}
+
+template <typename R>
+__device__ inline R fd_function(const ParamsT<R>& p, R Den1, R RmiuT1, R aDst1, R aLmax1, const R* g) {
+    const R K2 = R(0.41 * 0.41);
+    R alpha1 = R(0.25) - aDst1 / aLmax1;
+    R fb = dmin(R(2.) * texp(R(-9.0) * alpha1 * alpha1), R(1.));
+    R Sij = sij_norm(g);
+    R rdt = (RmiuT1 / Den1) / (K2 * pow2_real(aDst1) * Sij * R(p.Ref));
+    R fdt = R(1.) - ttanh((R(8.) * rdt) * (R(8.) * rdt) * (R(8.) * rdt));
+    return dmax((R(1.) - fdt), fb);
+}
+
+template <typename R>
+__device__ inline R fe_function(const ParamsT<R>& p, R Den2, R RmiuT2, R RmiuL2, R aDst2, R aLmax2, const R* g) {
+    const R K2 = R(0.41 * 0.41), CT2 = R(1.87 * 1.87), CL2 = R(5.00 * 5.00);
+    R alpha2 = R(0.25) - aDst2 / aLmax2;
+    R fe1 = alpha2 >= R(0.) ? R(2.) * texp(R(-11.09) * alpha2 * alpha2) : R(2.) * texp(R(-9.) * alpha2 * alpha2);
+    R Sij = sij_norm(g);
+    R rdt = (RmiuT2 / Den2) / (K2 * pow2_real(aDst2) * Sij * R(p.Ref));
+    R ft = ttanh((CT2 * rdt) * (CT2 * rdt) * (CT2 * rdt));
+    R rdl = (RmiuL2 / Den2) / (K2 * pow2_real(aDst2) * Sij * R(p.Ref));
+    R fl = ttanh(pow10_real(CL2 * rdl));
+    R fe2 = R(1.) - dmax(ft, fl);
+    return fe2 * dmax((fe1 - R(1.)), R(0.));
 }
 
 }  // namespace tg

@@ -59,7 +59,8 @@ bool params_supported(const trans_params* p) {
     if (p->IF_RK != 0 && p->IF_RK != 1) return false;
     if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4 || p->Kind_Roe < 1 || p->Kind_Roe > 3) return false;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return false;
-    if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 3)) return false;
+    // DES (0), the DDES shielding functions (1-3) and IDDES (5); FSST is undefined for 4
+    if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 5 || p->Kind_SubHY == 4)) return false;
     if (p->omega[0] != 0.0 || p->omega[1] != 0.0 || p->omega[2] != 0.0) return false;
     if (p->precision != TRANS_FP64 && p->precision != TRANS_MIXED) return false;
     // the rotated Roe scheme splits its dissipation along the direction of the velocity jump,

@@ -917,6 +917,8 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
     R TT = (rs<R>(b, S_T)[c]);
     R RmiuL = mu_suth<R>(p, TT);
     R Fdes = R(1.0);
+    R alIDDES = R(1.0);
+    const bool iddes = p.Kind_Hybrid == 3 && p.Kind_SubHY == 5;
     if (p.Kind_Hybrid == 3) {
         // DES length scale with the loop-carried F1 and omega of the previous interior cell
         // (TURBTWO_TIME_LUSGS_SST.F90:192-213); the first cell uses F1 = 0 and its own omega
@@ -934,6 +936,18 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
         R Fsst = fsst<R>(p, ARo, ARTk / ARo, vOmega, (rs<R>(b, S_DST)[c]), RmiuL, Cdiff);
         R aLgrd = ((R(1.) - arg1p) * R(0.61) + arg1p * R(0.78)) * (rs<R>(b, S_ALENG)[c]);
         Fdes = dmax(aLt * (R(1.) - Fsst) / aLgrd, R(1.0));
+        if (iddes) {        // IDDES length scale (TURBTWO_TIME_LUSGS_SST.F90:218-252)
+            const R aLmax = rs<R>(b, S_ALENG)[c], aDst = rs<R>(b, S_DST)[c], aLmin = rs<R>(b, S_ASENG)[c];
+            const R Cw = R(0.15);
+            R Cdes = (R(1.) - arg1p) * R(0.61) + arg1p * R(0.78);
+            R dlt = dmin(dmax(dmax(Cw * aLmax, Cw * aDst), aLmin), aLmax);
+            aLgrd = Cdes * dlt;
+            const R g[9] = {dudx, dudy, dudz, dvdx, dvdy, dvdz, dwdx, dwdy, dwdz};
+            const R RmiuT = rs<R>(b, S_RMIU)[c];
+            R fd = fd_function<R>(p, ARo, RmiuT, aDst, aLmax, g);
+            R fe = fe_function<R>(p, ARo, RmiuT, RmiuL, aDst, aLmax, g);
+            alIDDES = (R(1.) + fe) * fd * aLt + (R(1.) - fd) * aLgrd;
+        }
     }
     R DistN = (rs<R>(b, S_DST)[c]);
     R CDKO = dmax(R(2.0) * ARo * Sigo2 / (ARTO / ARo) * cdif, R(1.0e-10));
@@ -956,6 +970,13 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
     Source = SourceP + SourceN1 * ARTk;
     CnegTk = fabs(SourceN1);
     if (p.If_fix_Transition && rs<R>(b, S_XC)[c] < p.Trans_location) Source = R(0.0);
+    if (iddes) {            // the IDDES destruction (TURBTWO_TIME_LUSGS_SST.F90:299-310, 354-366)
+        if (p.IF_Comppress == 0) SourceN1 = -(c23 * dmax(Div, R(0.0))) - sqrt(ARTk / ARo) / alIDDES;
+        else SourceN1 = -(c23 * dmax(Div, R(0.0))) - (R(1.) + (R(1.) - arg1) * (Alf1 - Alf3) * Mt * Mt) * sqrt(ARTk / ARo) / alIDDES;
+        Source = SourceP + SourceN1 * ARTk;
+        CnegTk = fabs(-(c23 * dmax(Div, R(0.0))) - R(1.5) * sqrt(ARTk / ARo) / alIDDES);
+        if (p.If_fix_Transition && rs<R>(b, S_XC)[c] < p.Trans_location) Source = R(0.0);
+    }
     DQ(5) = DQ(5) + Source;
     tprod = dmin(prod, Votg) / Ref;
     R GamaAB = R(p.Gama1) * arg1 + R(p.Gama2) * (R(1.0) - arg1);
