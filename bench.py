@@ -185,10 +185,13 @@ FACE_DRAM_BYTES = 391.3
 FACE_DRAM_SOURCE = "ncu dram__bytes_read+write per face on the 339,968-cell cascade, scaled by faces"
 # kernel classes that run in FP32 in the mixed path (their algorithmic words are 4 bytes there)
 FP32_KERNELS = ("k_face_flux", "k_gather", "k_sweep", "k_gradient")
-# bounded serving leg of the default line (4 requests/s as the serving configuration states)
-SERVE_DURATION = 10.0
-SERVE_DROP = 1e-1
-SERVE_MAX_ITERS = 2000
+# bounded serving leg of the default line: 4 requests/s as the serving configuration states,
+# for 5 s of arrivals; each request retires at a 0.3 drop of its residual (coarse grids take
+# ~580 iterations to it, medium ~690 with the CFL ramp) or after 1,500 iterations, so the leg
+# ends within about a minute on one GPU
+SERVE_DURATION = 5.0
+SERVE_DROP = 0.3
+SERVE_MAX_ITERS = 1500
 
 
 def units(c, kernel):

@@ -141,6 +141,27 @@ def _symmetry_case():
     return c, conns, geo, st
 
 
+def _ghost_mismatches(a, b, dims):
+    """(face, layer, component, count, sample gpu, sample oracle) of the face ghosts that differ
+    bit for bit (face 0..5 = i-min, i-max, j-min, j-max, k-min, k-max)."""
+    ni, nj, nk = dims
+    out = []
+    a2 = a.reshape((-1,) + a.shape[-3:])
+    b2 = b.reshape((-1,) + b.shape[-3:])
+    I, J, K = slice(G + 1, G + ni), slice(G + 1, G + nj), slice(G + 1, G + nk)
+    for L in range(1, 4):
+        sl = [(G + 1 - L, J, K), (G + ni - 1 + L, J, K), (I, G + 1 - L, K), (I, G + nj - 1 + L, K),
+              (I, J, G + 1 - L), (I, J, G + nk - 1 + L)]
+        for f, s in enumerate(sl):
+            for q in range(a2.shape[0]):
+                x, y = a2[q][s].ravel(), b2[q][s].ravel()
+                bad = x.view(np.int64) != y.view(np.int64)
+                if np.any(bad):
+                    k = int(np.argmax(bad))
+                    out.append((f, L, q, int(bad.sum()), float(x[k]), float(y[k])))
+    return out
+
+
 def test_symmetry_plane_bc_state_stage(gpu_lib):
     """BC_STATE on the three ghost layers of every face (the symmetry plane among them), then
     the gradients and their ghost copies, against the oracle."""
@@ -158,7 +179,8 @@ def test_symmetry_plane_bc_state_stage(gpu_lib):
                 for name in ("V", "PP", "T", "RMIU"):
                     a, b = g.get_field(0, name), o.get_field(0, name)
                     assert bit_equal_fraction(a, b, top) == 1.0, (ki, name)
-                    assert bit_equal_fraction(a, b, face_ghosts(dims, 3)) == 1.0, (ki, name)
+                    bad = _ghost_mismatches(a, b, dims)
+                    assert not bad, (ki, name, bad[:12])
             if stage == "BC_GRAD":
                 a, b = g.get_field(0, "DQDXYZ"), o.get_field(0, "DQDXYZ")
                 assert bit_equal_fraction(a, b, face_ghosts(dims, 1)) == 1.0, ki

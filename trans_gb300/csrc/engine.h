@@ -117,6 +117,7 @@ struct Ctx {
     int* d_tflags = nullptr;             // 2 x ntiles publish flags + the tile counter
     TileView tv{};
     bool sweep_forced = false;
+    long long tuned_positions = 0;       // sweep positions the schedule was tuned on (0: never tuned)
     int pdl = 1;                         // chain hyperplane launches (programmatic dependent launch)
     int pdl_allowed = 1;                 // chaining may be picked by the tuner (TRANS_PDL=0 forbids it)
     int sweep_exec_pdl = -1;             // chaining the sweep graph was captured with

@@ -426,7 +426,11 @@ int tune_sweeps(Ctx* c) {
     cudaEventDestroy(e1);
     if (rc) return rc;
     if ((rc = save_dq(c, true))) return rc;
-    if (pick.mode == 3 && (rc = build_tiles(c, pick.ti, pick.tj, pick.tk))) return rc;
+    if (pick.mode == 3) {
+        if ((rc = build_tiles(c, pick.ti, pick.tj, pick.tk))) return rc;
+        c->tile_default[0] = pick.ti; c->tile_default[1] = pick.tj; c->tile_default[2] = pick.tk;   // kept over rebuilds
+    }
+    c->tuned_positions = c->sv.n;
     c->sweep_mode = pick.mode; c->sweep_grid = pick.grid; c->sweep_block = pick.block;
     c->sweep_wpc = pick.wpc;
     c->sweep_pf = pick.pf;

@@ -279,7 +279,12 @@ int rebuild(Ctx* c) {
     c->norms.assign(nblk, trans_norms{});
     CK(cudaMalloc(&c->d_cdev, sizeof(CaseDev) * c->cases.size()));
     CK(cudaMallocHost(&c->h_cdev, sizeof(CaseDev) * c->cases.size()));
-    if (!c->sweep_forced) c->sweep_mode = -1;     // re-tune the sweep schedule for the new work
+    // re-tune the sweep schedule when the sweep work has changed by more than a factor 2 since
+    // it was tuned (a serving loop adds and removes cases every few iterations, and a tuning run
+    // times ~40 candidate sweeps); the schedule kept is re-captured for the new work lists
+    const long long npos = (long long)c->sweep.size();
+    if (!c->sweep_forced && (c->tuned_positions <= 0 || npos > 2 * c->tuned_positions || 2 * npos < c->tuned_positions))
+        c->sweep_mode = -1;
     c->built = true;
     return TRANS_OK;
 }
