@@ -466,8 +466,11 @@ def roofline(lib, c, kt, nsub, precision, sched):
         roof["binding"] = "latency (one dependent step per i+j+k hyperplane)"
         if sched.startswith("sweep=planes"):
             cells_per_plane = interior_cells(c) * nsub * 2 / dom_n      # dom_n counts both sweeps' hyperplanes
-            grid = max(1, int(round(cells_per_plane * 8 / 128)))
-            floor_us = lib.trans_probe_chain_us(1 if "chained" in sched else 0, grid)
+            # threads per hyperplane: 8 per position in the FP64 path, 1 in the mixed path
+            threads = cells_per_plane * (8 if precision == "fp64" else 1)
+            grid = max(1, int(round(threads / 128)))
+            chained = "chained" in sched.split(";")[0] or "early" in sched.split(";")[0]
+            floor_us = lib.trans_probe_chain_us(1 if chained else 0, grid)
             roof["latency"] = {"us_per_step": per_launch_ms * 1e3, "floor_us_per_step": floor_us,
                                "frac": floor_us / (per_launch_ms * 1e3) if floor_us > 0 else None,
                                "floor": f"dependent launch chain, {grid} CTAs x 128 threads, one L2 round trip per step"}

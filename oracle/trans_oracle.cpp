@@ -2264,6 +2264,116 @@ int oracle_get_norms(void* ctx, trans_norms* norms) {
     return TRANS_OK;
 }
 
+// Cross-rank 1-to-1 interfaces (BC/PARALLEL_BC_P2P.F90:1-257).  A kind-9 connection whose
+// target block is not in this context is left out of BC_Boundarys (bc_boundarys finds no
+// target) and exchanged by the caller between BC_STATE / BC_GRAD and the next stage:
+// oracle_halo_pack fills the segment's send buffer from this block's interior layers, face
+// cells in the segment's K, J, I order, in the reference's buffer layout (sweep -1: 36 words
+// per face cell -- layer 0: V(1:7), PP, T, Rmiu, Rds(1:3), shock; layers 1 and 2: V(1:7), PP,
+// T, Rmiu, shock; sweep 0: DqDxyz(1:18) of layer 0), at full precision (the reference sends
+// FP32).  oracle_halo_unpack fills this segment's ghost layers from the partner segment's
+// buffer through the same index transform and rotation as the same-rank copy (bc_p2p), and
+// applies what that copy applies (Rds and shock travel but are not written: the ghost shock is
+// overwritten by the extrapolation of DIFF_DqDxyz, the ghost Rds is not read by the path).
+int halo_words(int sweep) { return sweep == -1 ? 36 : 18; }
+
+int oracle_halo_pack(void* ctx, int sweep, int ib, int iconn, double* buf) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || ib < 0 || ib >= (int)c->B.size() || !buf || (sweep != -1 && sweep != 0)) return TRANS_E_ARG;
+    Blk& b = c->B[ib];
+    if (iconn < 1 || iconn > (int)b.conn.size() || b.conn[iconn - 1].BCType != 9) return TRANS_E_ARG;
+    SegIdx s(b.conn[iconn - 1]);
+    const int S[3][3] = {{s.iadd, s.jadd, s.kadd}, {s.iadd1, s.jadd1, s.kadd1}, {s.iadd2, s.jadd2, s.kadd2}};
+    size_t n = 0;
+    for (int K = s.Kbgn; K <= s.Kend; ++K)
+    for (int J = s.Jbgn; J <= s.Jend; ++J)
+    for (int I = s.Ibgn; I <= s.Iend; ++I) {
+        if (sweep == -1) {
+            for (int L = 0; L < 3; ++L) {
+                int is = I + S[L][0], js = J + S[L][1], ks = K + S[L][2];
+                for (int m = 1; m <= 7; ++m) buf[n++] = b.V(m, is, js, ks);
+                buf[n++] = b.PP(is, js, ks);
+                buf[n++] = b.T(is, js, ks);
+                buf[n++] = b.Rmiu(is, js, ks);
+                if (L == 0)
+                    for (int d = 1; d <= 3; ++d) buf[n++] = b.Rds(d, is, js, ks);
+                buf[n++] = b.shock(is, js, ks);
+            }
+        } else {
+            int is = I + s.iadd, js = J + s.jadd, ks = K + s.kadd;
+            for (int m = 1; m <= 18; ++m) buf[n++] = b.DQ(m, is, js, ks);
+        }
+    }
+    return TRANS_OK;
+}
+
+int oracle_halo_unpack(void* ctx, int sweep, int ib, int iconn, const trans_conn* partner, const double* buf) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || ib < 0 || ib >= (int)c->B.size() || !buf || !partner || (sweep != -1 && sweep != 0)) return TRANS_E_ARG;
+    Blk& b = c->B[ib];
+    if (iconn < 1 || iconn > (int)b.conn.size() || b.conn[iconn - 1].BCType != 9) return TRANS_E_ARG;
+    const trans_conn& a = b.conn[iconn - 1];
+    SegIdx s(a), t(*partner);
+    const int ti = t.Iend - t.Ibgn + 1, tj = t.Jend - t.Jbgn + 1, tk = t.Kend - t.Kbgn + 1;
+    int IIadd = s.Iend - s.Ibgn + 2, JJadd = s.Jend - s.Jbgn + 2, KKadd = s.Kend - s.Kbgn + 2;
+    double dstage = a.rotateAngle;
+    double sint = std::sin(dstage), cost = std::cos(dstage);
+    double cos2t = cost * cost, sin2t = sint * sint, sct = sint * cost;
+    const int W = halo_words(sweep);
+    for (int K = s.Kbgn; K <= s.Kend; ++K)
+    for (int J = s.Jbgn; J <= s.Jend; ++J)
+    for (int I = s.Ibgn; I <= s.Iend; ++I) {
+        int iL = I - s.Ibgn + 1, jL = J - s.Jbgn + 1, kL = K - s.Kbgn + 1;
+        iL = a.revMatrix[0] * IIadd + (1 - 2 * a.revMatrix[0]) * iL;
+        jL = a.revMatrix[1] * JJadd + (1 - 2 * a.revMatrix[1]) * jL;
+        kL = a.revMatrix[2] * KKadd + (1 - 2 * a.revMatrix[2]) * kL;
+        int pb, pj, pk;
+        ijk_start_end(iL, jL, kL, pb, pj, pk, a.Transform, a.TransformT, a.lcross);     // partner face cell
+        pb -= 1; pj -= 1; pk -= 1;
+        if (pb < 0 || pb >= ti || pj < 0 || pj >= tj || pk < 0 || pk >= tk) return TRANS_E_ARG;
+        const double* w = buf + ((size_t)pb + (size_t)ti * ((size_t)pj + (size_t)tj * (size_t)pk)) * W;
+        if (sweep == -1) {
+            const int E[3][3] = {{s.Eiadd, s.Ejadd, s.Ekadd}, {s.Eiadd1, s.Ejadd1, s.Ekadd1}, {s.Eiadd2, s.Ejadd2, s.Ekadd2}};
+            const int off[3] = {0, 14, 25};
+            for (int L = 0; L < 3; ++L) {
+                const double* x = w + off[L];
+                int il = I + E[L][0], jl = J + E[L][1], kl = K + E[L][2];
+                b.V(1, il, jl, kl) = x[0];
+                b.V(2, il, jl, kl) = x[1];
+                double txy = x[2], txz = x[3];
+                b.V(3, il, jl, kl) = cost * txy + sint * txz;
+                b.V(4, il, jl, kl) = -sint * txy + cost * txz;
+                for (int m = 5; m <= 7; ++m) b.V(m, il, jl, kl) = x[m - 1];
+                b.PP(il, jl, kl) = x[7];
+                b.T(il, jl, kl) = x[8];
+                b.Rmiu(il, jl, kl) = x[9];
+            }
+        } else {
+            int il = I + s.Eiadd, jl = J + s.Ejadd, kl = K + s.Ekadd;
+            double ugx = w[0], ugy = w[1], ugz = w[2];
+            double vgx = w[3], vgy = w[4], vgz = w[5];
+            double wgx = w[6], wgy = w[7], wgz = w[8];
+            b.DQ(1, il, jl, kl) = ugx;
+            b.DQ(2, il, jl, kl) = cost * ugy + sint * ugz;
+            b.DQ(3, il, jl, kl) = -sint * ugy + cost * ugz;
+            b.DQ(4, il, jl, kl) = cost * vgx + sint * wgx;
+            b.DQ(5, il, jl, kl) = cos2t * vgy + sct * (vgz + wgy) + sin2t * wgz;
+            b.DQ(6, il, jl, kl) = cos2t * vgz + sct * (-vgy + wgz) - sin2t * wgy;
+            b.DQ(7, il, jl, kl) = -sint * vgx + cost * wgx;
+            b.DQ(8, il, jl, kl) = -sin2t * vgz + sct * (-vgy + wgz) + cos2t * wgy;
+            b.DQ(9, il, jl, kl) = sin2t * vgy + sct * (vgz + wgy) + cos2t * wgz;
+            for (int LL = 4; LL <= 6; ++LL) {
+                int L = (LL - 1) * 3 + 1;
+                b.DQ(L, il, jl, kl) = w[L - 1];
+                double gy = w[L], gz = w[L + 1];
+                b.DQ(L + 1, il, jl, kl) = cost * gy + sint * gz;
+                b.DQ(L + 2, il, jl, kl) = -sint * gy + cost * gz;
+            }
+        }
+    }
+    return TRANS_OK;
+}
+
 // scalar entry points for known-answer tests of the flux and limiter formulas
 double oracle_alimiter(double a, double b) { return alimiter(a, b); }
 double oracle_muscl2_limiter(double a, double b) { return muscl2_limiter(a, b); }

@@ -231,18 +231,21 @@ def test_gpu_against_golden_vectors(gpu_lib, name):
 def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
     """The hyperplane-per-launch schedule, the single cooperative launch with grid barriers, the
     dataflow schedule, the tiled wavefront (two tile shapes), each with the lane-major and the
-    warp-per-component thread mapping, and the tuner's pick compute every DeltaQ with the same
-    operations: states after 6 iterations are bit-identical."""
+    warp-per-component thread mapping (FP64), the chaining, prefetch and CTA-size variants of the
+    hyperplane launches, and the tuner's pick compute every DeltaQ with the same operations:
+    states after 6 iterations are bit-identical."""
     from helpers import small_cascade
     from trans_gb300 import abi
     from trans_gb300.solver import Solver
     out = {}
     modes = ("planes", "planes_unchained", "coop", "flow", "tiles", "tiles_4x2x3", "planes_wpc", "planes_unchained_wpc",
-             "coop_wpc", "tiles_4x2x3_wpc", "planes_pf2", "planes_wpc_pf1", "auto")
+             "coop_wpc", "tiles_4x2x3_wpc", "planes_pf2", "planes_wpc_pf1", "planes_early_cta32", "planes_early_pf2_cta64",
+             "auto")
     for mode in modes:
         parts = mode.split("_")
         monkeypatch.setenv("TRANS_SWEEP", parts[0])
-        monkeypatch.setenv("TRANS_PDL", "0" if "unchained" in parts else "1")
+        monkeypatch.setenv("TRANS_PDL", "0" if "unchained" in parts else ("2" if "early" in parts else "1"))
+        monkeypatch.setenv("TRANS_SWEEP_CTA", next((x[3:] for x in parts if x.startswith("cta")), "0"))
         monkeypatch.setenv("TRANS_TILE", next((x for x in parts if "x" in x), "8x8x8"))
         monkeypatch.setenv("TRANS_SWEEP_MAP", "wpc" if "wpc" in parts else "lane")
         monkeypatch.setenv("TRANS_SWEEP_PF", next((x[2:] for x in parts if x.startswith("pf")), "0"))

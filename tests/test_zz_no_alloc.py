@@ -120,23 +120,25 @@ def test_static_scratch_batch_context(gpu_lib):
 
 
 def test_static_scratch_refuses_unbuilt_context(gpu_lib):
-    """A context whose work lists are not built yet would have to allocate them: the call
-    returns TRANS_E_ARG and the context holds the same device memory afterwards."""
+    """A batch context whose work lists are not built yet (a case was just added) would have to
+    allocate them: the call returns TRANS_E_ARG and the context holds the same device memory
+    afterwards; once an iteration has built it, the call works."""
     from trans_gb300 import abi
-    from trans_gb300.solver import Solver
+    from trans_gb300.solver import Batch
+    lib = gpu_lib
+    bt = Batch(abi.TRANS_FP64)
     c, conns, geo, st = small_channel(Kind_Spatial=3, Kind_Roe=3)
-    s = Solver(c, conns, geo, st)
-    lib = s.lib
-    held = lib.trans_device_bytes(s.ctx)
-    rc = lib.trans_update_static_scratch(s.ctx, 1, C.cast(None, C.POINTER(abi.TransNorms)))
+    bt.add(c, conns, geo, st)
+    held = lib.trans_device_bytes(bt.ctx)
+    rc = lib.trans_update_static_scratch(bt.ctx, 1, C.cast(None, C.POINTER(abi.TransNorms)))
     assert rc == abi.TRANS_E_ARG
-    assert b"not built" in lib.trans_last_error(s.ctx)
-    assert lib.trans_device_bytes(s.ctx) == held
-    s.iterate(1)                            # the context still works, and the entry point then does
-    for st_name in PRE_UPDATE:
-        s.run_stage(st_name, 2)
-    assert lib.trans_update_static_scratch(s.ctx, 2, C.cast(None, C.POINTER(abi.TransNorms))) == abi.TRANS_OK
-    s.close()
+    assert b"not built" in lib.trans_last_error(bt.ctx)
+    assert lib.trans_device_bytes(bt.ctx) == held
+    bt.iterate(1)                           # builds the context; the entry point then works
+    for name in PRE_UPDATE:
+        assert lib.trans_run_stage(bt.ctx, abi.STAGE_ID[name], 2, 1) == abi.TRANS_OK
+    assert lib.trans_update_static_scratch(bt.ctx, 2, C.cast(None, C.POINTER(abi.TransNorms))) == abi.TRANS_OK
+    bt.close()
 
 
 def test_static_scratch_rejects_null_context(gpu_lib):

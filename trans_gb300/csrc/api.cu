@@ -174,7 +174,7 @@ long long trans_device_bytes(void* ctx) {
     long long b = 0;
     for (const CaseRec* cs : c->cases)
         b += (long long)(cs->arena_doubles * (sizeof(double) + (cs->farena ? sizeof(float) : 0)));
-    b += (c->sv.n + 31) / 32 * 32 * ((long long)(NREC + DQ_STRIDE) * (long long)c->fl->elem + 8LL * (long long)sizeof(int));
+    b += (c->sv.n + 31) / 32 * 32 * ((long long)(c->fl->rec_width + DQ_STRIDE) * (long long)c->fl->elem + 8LL * (long long)sizeof(int));
     return b;
 }
 
@@ -206,8 +206,9 @@ const char* trans_tuning(void* ctx) {
                                                        + std::to_string(c->tile_shape[2]) + "/" : std::string();
     out = "sweep=" + std::string(c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : c->sweep_mode == 2 ? "flow " : "tiles ")
                                                       + tiles + std::to_string(c->sweep_grid) + "x" + std::to_string(c->sweep_block)
-                                 : c->sweep_mode == 0 ? (c->pdl ? "planes-chained" : "planes") : "untuned")
+                                 : c->sweep_mode == 0 ? (c->pdl ? (c->pdl == 2 ? "planes-early" : "planes-chained") : "planes") : "untuned")
           + (c->sweep_wpc ? "/wpc" : "") + (c->sweep_pf && c->sweep_mode == 0 ? "/pf" + std::to_string(c->sweep_pf) : "")
+          + (c->sweep_cta && c->sweep_mode == 0 ? "/cta" + std::to_string(c->sweep_cta) : "")
           + "; measured: " + c->sweep_tuning;
     return out.c_str();
 }

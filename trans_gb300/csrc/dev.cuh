@@ -65,6 +65,11 @@ enum JacTerm { JC_R0 = 0, JC_R1 = 3, JC_R2 = 8, JC_R3 = 13, JC_VP = 18, JC_GET1 
 // Jacobian terms, then its spectral radius in that direction.
 enum SweepRec { NBREC = NJAC + 1, REC_STEPT = 6 * NBREC, REC_CVS = REC_STEPT + 1, REC_FM = REC_STEPT + 2,
                 REC_FT = REC_STEPT + 3, NREC = REC_STEPT + 4 };
+// The mixed path's (FP32) record is compact: per sweep position the cell's own values from
+// which its neighbours rebuild the Jacobian rows, and its diagonal terms, as float4 groups:
+// direction d (0..2): face-averaged metric s = 0.5 (SD(d,c) + SD(d,c+1)) and Rds(d); then the
+// velocity and total enthalpy H = |v|^2/2 + gamma p/(rho (gamma-1)); then stept, cvs, 1/fm, 1/ft.
+enum CompactRec { CR_DIR = 0, CR_VEL = 12, CR_DIAG = 16, NCREC = 20 };
 constexpr int DQ_STRIDE = 8;     // DeltaQ of one sweep position: 7 components + 1 pad
 // Sweep-order arrays keep the entries of one position together (element m of position q at
 // q*width + m): a hyperplane is one contiguous range, and one cell's record spans a few lines.

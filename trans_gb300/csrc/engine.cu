@@ -123,7 +123,8 @@ long long case_bytes(const trans_params* p, int nblocks, const trans_block* bloc
     }
     const long long elem = precision == TRANS_MIXED ? 4 : 8;
     long long b = padded * case_slots(*p) * (8 + (precision == TRANS_MIXED ? 4 : 0));
-    b += interior * ((NREC + 2LL * DQ_STRIDE) * elem + 8LL * 4 + (long long)sizeof(SweepCell));
+    const long long rec = precision == TRANS_MIXED ? NCREC : NREC;      // sweep record entries per position
+    b += interior * ((rec + 2LL * DQ_STRIDE) * elem + 8LL * 4 + (long long)sizeof(SweepCell));
     b += interior / 16 + 4096;           // tiles, norm partials, boundary tables (rounded up)
     return b;
 }
@@ -140,9 +141,14 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     // TRANS_GRAPHS=0 turns the whole-iteration graphs off (every iteration launched directly)
     const char* gr = std::getenv("TRANS_GRAPHS");
     if (gr && std::string(gr) == "0") c->graphs = false;
-    // TRANS_PDL=0 launches the hyperplanes without programmatic dependent launch
+    // TRANS_PDL=0 launches the hyperplanes without programmatic dependent launch; TRANS_PDL=2
+    // releases the next hyperplane's launch at entry (mixed path)
     const char* pd = std::getenv("TRANS_PDL");
     if (pd && std::string(pd) == "0") c->pdl = c->pdl_allowed = 0;
+    if (pd && std::string(pd) == "2") c->pdl = 2;
+    // TRANS_SWEEP_CTA=n: CTA size of the mixed path's hyperplane launches (for tests and captures)
+    const char* sc = std::getenv("TRANS_SWEEP_CTA");
+    if (sc) c->sweep_cta = std::max(0, std::atoi(sc));
     // TRANS_SWEEP_MAP=wpc forces the warp-per-component thread mapping of the sweeps (for tests)
     const char* wm = std::getenv("TRANS_SWEEP_MAP");
     if (wm && std::string(wm) == "wpc") c->sweep_wpc = SWEEP_WPC;

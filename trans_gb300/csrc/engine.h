@@ -118,13 +118,16 @@ struct Ctx {
     TileView tv{};
     bool sweep_forced = false;
     long long tuned_positions = 0;       // sweep positions the schedule was tuned on (0: never tuned)
-    int pdl = 1;                         // chain hyperplane launches (programmatic dependent launch)
+    int pdl = 1;                         // chain hyperplane launches (programmatic dependent launch;
+                                         // 2 = the mixed path's release of the next launch at entry)
     int pdl_allowed = 1;                 // chaining may be picked by the tuner (TRANS_PDL=0 forbids it)
     int sweep_exec_pdl = -1;             // chaining the sweep graph was captured with
     int sweep_wpc = 0;                   // SWEEP_WPC: warp-per-component thread mapping (0: lane-major)
     int sweep_exec_wpc = -1;             // mapping the sweep graph was captured with
     int sweep_pf = 0;                    // L2 prefetch distance of the hyperplane launches (0 = none)
     int sweep_exec_pf = -1;              // prefetch distance the sweep graph was captured with
+    int sweep_cta = 0;                   // CTA size of the mixed path's hyperplane launches (0 = default)
+    int sweep_exec_cta = -1;             // CTA size the sweep graph was captured with
     int sweep_lanes = 1;                 // DeltaQ components swept: 1 = all, 2 = k and omega only (Runge-Kutta)
     SweepSync* d_sync = nullptr;
     SweepSync* h_sync = nullptr;         // pinned

@@ -27,16 +27,35 @@ void fc(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev*
 void prep(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const int* qpos, const SweepView& v, const CaseDev* cd) {
     if (nt > 0) k_lusgs_prep<TG_R><<<nt, CELL_TILE, 0, s>>>(b, tiles, qpos, (TG_R*)v.rec, (TG_R*)v.dq, cd);
 }
+// the FP64 path's neighbour Jacobian terms; the mixed path rebuilds them in the sweep from the
+// compact records k_lusgs_prep writes, so it has no such pass
 void jac(cudaStream_t s, const DevBlock* b, const SweepView& v) {
-    if (v.n > 0)
-        k_lusgs_jac<TG_R><<<(unsigned)((v.n + 31) / 32), 6 * 32, 0, s>>>(b, v.cells, v.nbp, (TG_R*)v.rec, v.n);
+    if constexpr (sizeof(TG_R) == 8) {
+        if (v.n > 0)
+            k_lusgs_jac<TG_R><<<(unsigned)((v.n + 31) / 32), 6 * 32, 0, s>>>(b, v.cells, v.nbp, (TG_R*)v.rec, v.n);
+    }
 }
 // one hyperplane; chained = launched with programmatic stream serialisation, so that this
 // hyperplane's independent loads overlap the previous one (the kernel waits before its
 // dependent part)
 template <bool LOWER>
-void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count) {
+void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count, int cta) {
     if (count <= 0) return;
+    if constexpr (sizeof(TG_R) == 4) {      // mixed path: one thread per position (k_sweep_c)
+        const int CTA = cta > 0 ? cta : SWEEP_CTA;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((count + CTA - 1) / CTA);
+        cfg.blockDim = dim3(CTA);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = chained ? 1 : 0;
+        cudaLaunchKernelEx(&cfg, k_sweep_c<LOWER>, (const int*)v.nbp, (const float*)v.rec, (float*)v.dq, first, count, turb & 3,
+                           chained, pf_first, pf_count);
+        return;
+    }
     const int* nbp = v.nbp;
     const TG_R* rec = (const TG_R*)v.rec;
     TG_R* dq = (TG_R*)v.dq;
@@ -56,11 +75,11 @@ void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int
     cfg.numAttrs = chained ? 1 : 0;
     cudaLaunchKernelEx(&cfg, k_sweep<TG_R, LOWER>, nbp, rec, dq, n, first, count, turb, chained, pf_first, pf_count);
 }
-void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count) {
-    swp<true>(s, v, first, count, turb, chained, pf_first, pf_count);
+void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count, int cta) {
+    swp<true>(s, v, first, count, turb, chained, pf_first, pf_count, cta);
 }
-void swu(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count) {
-    swp<false>(s, v, first, count, turb, chained, pf_first, pf_count);
+void swu(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count, int cta) {
+    swp<false>(s, v, first, count, turb, chained, pf_first, pf_count, cta);
 }
 cudaError_t swa(cudaStream_t s, const SweepView& v, const int* po, int nplanes, int turb, SweepSync* sy, int grid, int block,
                 unsigned limit) {
@@ -119,7 +138,7 @@ void scat(cudaStream_t s, const DevBlock* b, const SweepView& v, int l0) {
 
 const FluxLaunchers& TG_NAME() {
     static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, prep, jac, swl, swu, swa, swa_occ, swf, swf_occ,
-                                    swt, swt_occ, scat, sizeof(TG_R)};
+                                    swt, swt_occ, scat, sizeof(TG_R), sizeof(TG_R) == 4 ? (int)NCREC : (int)NREC};
     return L;
 }
 }  // namespace tg

@@ -114,7 +114,13 @@ __global__ void k_bc_state(const DevBlock* __restrict__ blks, const BCEntry* __r
     double* Rm = slot(b, S_RMIU);
     const int s0 = E.s[0], l0 = E.l[0];
     if (E.kind == 1) {                              // BC/BC_Wall.F90:42-117
-        double vibc = 0.0, vjbc = 0.0, vkbc = 0.0;   // zero grid speed (omega = 0)
+        // wall velocity of the frame Kindsub_BC * omega (BC_Wall.F90:46-52), as the reference
+        // evaluates it (its sign of zero included)
+        const double ztemp = 0.5 * (slot(b, S_ZC)[s0] + slot(b, S_ZC)[l0]);
+        const double ytemp = 0.5 * (slot(b, S_YC)[s0] + slot(b, S_YC)[l0]);
+        const double vibc = 0.0;
+        const double vjbc = (double)E.kindsub * p.omega0 * ztemp;
+        const double vkbc = -(double)E.kindsub * p.omega0 * ytemp;
         for (int L = 0; L < 3; ++L) {
             int is = E.s[L], il = E.l[L];
             PP[il] = PP[is];
@@ -859,14 +865,32 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
         const double rsum = slot(b, S_RDS)[c] + slot(b, S_RDS + 1)[c] + slot(b, S_RDS + 2)[c];
         stept = R(st); cvs = R(cv); fm = R(1.0 + rsum * cv);
     }
-    REC(REC_STEPT) = stept;
-    REC(REC_CVS) = cvs;
+    // the diagonal terms into the record: FP64 path its four entries; mixed path the compact
+    // record of this position (CompactRec: metric and radius per direction, velocity and total
+    // enthalpy, stept, cvs and the reciprocals of the two diagonals)
+    auto finish = [&](R ft) {
+        if constexpr (MIXED) {
+            float4* R4 = reinterpret_cast<float4*>(rec) + (size_t)q * (NCREC / 4);
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                R4[d] = make_float4(rs<R>(b, S_ASD + 3 * d)[c], rs<R>(b, S_ASD + 3 * d + 1)[c], rs<R>(b, S_ASD + 3 * d + 2)[c],
+                                    rs<R>(b, S_RDS + d)[c]);
+            const float u = rs<R>(b, S_SVEL)[c], v = rs<R>(b, S_SVEL + 1)[c], w = rs<R>(b, S_SVEL + 2)[c];
+            const float H = 0.5f * (u * u + v * v + w * w) + 1.4f * rs<R>(b, S_PP)[c] * rs<R>(b, S_RINV)[c] / 0.4f;
+            R4[CR_VEL / 4] = make_float4(u, v, w, H);
+            R4[CR_DIAG / 4] = make_float4(stept, cvs, 1.0f / fm, 1.0f / ft);
+        } else {
+            REC(REC_STEPT) = stept;
+            REC(REC_CVS) = cvs;
+            REC(REC_FM) = fm;
+            REC(REC_FT) = ft;
+        }
+    };
     for (int L = 0; L < 5; ++L) DQ(L) = rhs(L);
-    REC(REC_FM) = fm;
     if (!turb) {            // the k-omega lanes of the sweeps then produce zeros
         DQ(5) = rs<R>(b, S_D + 5)[c];
         DQ(6) = rs<R>(b, S_D + 6)[c];
-        REC(REC_FT) = R(1.0);
+        finish(R(1.0));
         return;
     }
     for (int L = 5; L < 7; ++L) DQ(L) = rhs(L);
@@ -911,7 +935,7 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
         R dltCD = cdif <= R(0.) ? R(0.) : R(0.125);
         Source = Source + dltCD * ARo * ARo / ARTO / Ref * cdif;
         DQ(6) = DQ(6) + Source;
-        REC(REC_FT) = R(fm) + (CnegTk + R(2.0) * fabs(SourceN1)) * R(stept);
+        finish(R(fm) + (CnegTk + R(2.0) * fabs(SourceN1)) * R(stept));
         return;
     }
     R TT = (rs<R>(b, S_T)[c]);
@@ -994,7 +1018,7 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
     Source = Source + SourceCross;
     DQ(6) = DQ(6) + Source;
     CnegTO = R(2.0) * fabs(SourceN1);
-    REC(REC_FT) = R(fm) + (CnegTk + CnegTO) * R(stept);
+    finish(R(fm) + (CnegTk + CnegTO) * R(stept));
 }
 
 // The neighbours' Jacobian terms and spectral radii of the sweep records: 6 threads per
@@ -1057,11 +1081,100 @@ __device__ inline void sweep_map(int g, int lanes, int& e, int& L) {
     else { e = g / SWEEP_LANES; L = g % SWEEP_LANES; }
 }
 
+// Mixed-path (FP32) sweep step of one position, all seven components, from the compact records
+// (CompactRec).  Each neighbour's Jacobian row is rebuilt from its metric s, velocity v and total
+// enthalpy H: with VP = v.s, th = s.dm - VP dr and ph = (gamma-1)(|v|^2/2 dr - v.dm + dE),
+//   row 0 = s.dm,   rows 1-3 = v_a th + s_a ph + VP dm_a,   row 4 = H th + VP (ph + dE),
+// the rows of A(Q) DeltaQ of TIME_LUSGS.F90:696-768 re-associated (the FP32 path does not keep
+// the reference's operation order); the k and omega rows are VP dq (TURBTWO_TIME_LUSGS_SST.F90:
+// 562-766).  The neighbour terms are 0.5 (row + sgn Rds dq), summed over the three neighbours;
+// then D = (own stept + sum cvs) / diag in the lower sweep, own - sum cvs / diag in the upper.
+// turb: 0 mean flow, 1 all, 2 k and omega only (the others are stored back unchanged).
+// chained: griddepcontrol.wait before the first DeltaQ access.
+template <bool LOWER>
+__device__ inline void sweep_pos_compact(const int* __restrict__ nbp, const float* __restrict__ rec, float* dq, long long q,
+                                         int turb, bool chained) {
+    const int side = LOWER ? 0 : 3;
+    const float sgn = LOWER ? 1.0f : -1.0f;
+    const float4* R4 = reinterpret_cast<const float4*>(rec);
+    int np[3];
+    float4 g[3], h[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        np[d] = nbp[sw_at(q, side + d, 6)];
+        const long long r = np[d] >= 0 ? np[d] : q;
+        g[d] = __ldg(R4 + (size_t)r * (NCREC / 4) + d);               // s of direction d, Rds(d)
+        h[d] = __ldg(R4 + (size_t)r * (NCREC / 4) + CR_VEL / 4);      // u, v, w, H
+    }
+    const float4 dg = __ldg(R4 + (size_t)q * (NCREC / 4) + CR_DIAG / 4);     // stept, cvs, 1/fm, 1/ft
+    float VP[3], q2[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        VP[d] = h[d].x * g[d].x + h[d].y * g[d].y + h[d].z * g[d].z;
+        q2[d] = 0.5f * (h[d].x * h[d].x + h[d].y * h[d].y + h[d].z * h[d].z);
+    }
+    if (chained) asm volatile("griddepcontrol.wait;" ::: "memory");
+    // DeltaQ is written during the sweep by other SMs: read it through L2
+    const float4* D4 = reinterpret_cast<const float4*>(dq);
+    float4 a[3], t[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const long long r = np[d] >= 0 ? np[d] : q;
+        a[d] = __ldcg(D4 + (size_t)r * 2);
+        t[d] = __ldcg(D4 + (size_t)r * 2 + 1);
+    }
+    const float4 o0 = __ldcg(D4 + (size_t)q * 2), o1 = __ldcg(D4 + (size_t)q * 2 + 1);
+    float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const float Gm1 = 0.4f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (np[d] < 0) continue;
+        const float a0 = a[d].x, a1 = a[d].y, a2 = a[d].z, a3 = a[d].w, a4 = t[d].x, a5 = t[d].y, a6 = t[d].z;
+        const float sx = g[d].x, sy = g[d].y, sz = g[d].z, sr = sgn * g[d].w;
+        const float u = h[d].x, v = h[d].y, w = h[d].z, H = h[d].w, vp = VP[d];
+        const float sm = sx * a1 + sy * a2 + sz * a3;
+        const float th = sm - vp * a0;
+        const float ph = Gm1 * (q2[d] * a0 - (u * a1 + v * a2 + w * a3) + a4);
+        acc[0] += sm + sr * a0;
+        acc[1] += u * th + sx * ph + (vp + sr) * a1;
+        acc[2] += v * th + sy * ph + (vp + sr) * a2;
+        acc[3] += w * th + sz * ph + (vp + sr) * a3;
+        acc[4] += H * th + vp * (ph + a4) + sr * a4;
+        acc[5] += (vp + sr) * a5;
+        acc[6] += (vp + sr) * a6;
+    }
+    const float own[7] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z};
+    const float stept = dg.x, hc = 0.5f * dg.y;
+    float out[7];
+#pragma unroll
+    for (int L = 0; L < 7; ++L) {
+        const float iden = L < 5 ? dg.z : dg.w;
+        const bool act = turb == 1 || (turb == 0 ? L < 5 : L >= 5);
+        const float nv = LOWER ? (own[L] * stept + acc[L] * hc) * iden : own[L] - acc[L] * hc * iden;
+        out[L] = act ? nv : own[L];
+    }
+    float4* W4 = reinterpret_cast<float4*>(dq) + (size_t)q * 2;
+    __stcg(W4, make_float4(out[0], out[1], out[2], out[3]));
+    __stcg(W4 + 1, make_float4(out[4], out[5], out[6], o1.w));
+}
+
 template <typename R, bool LOWER>
 __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
-                                  int L, int turb, bool chained = false, bool hoist = true) {
+                                  int L, int turb, bool chained = false, bool hoist = true, bool release = true) {
+    if constexpr (sizeof(R) == 4) {     // mixed path: lane 0 of a position computes all its components
+        if (L != 0) {
+            if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+            return;
+        }
+        sweep_pos_compact<LOWER>(nbp, (const float*)rec, (float*)dq, q, turb, chained);
+        if (chained) asm volatile("griddepcontrol.launch_dependents;");
+        return;
+    }
     if (L >= 7 || (L >= 5 && turb == 0) || (L < 5 && turb == 2)) {
-        if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+        if (chained) {
+            asm volatile("griddepcontrol.wait;" ::: "memory");
+            if (release) asm volatile("griddepcontrol.launch_dependents;");
+        }
         return;
     }
     const int side = LOWER ? 0 : 3;
@@ -1092,8 +1205,12 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
     const R stept = REC(REC_STEPT), cvs = REC(REC_CVS);
     const R den = L < 5 ? REC(REC_FM) : REC(REC_FT);
     // one launch per hyperplane chained with programmatic dependent launch: wait for the
-    // previous hyperplane to complete, then let the next one start its loads
-    if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+    // previous hyperplane to complete, then let the next one start its loads (unless the
+    // kernel released it at entry)
+    if (chained) {
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        if (release) asm volatile("griddepcontrol.launch_dependents;");
+    }
     // DeltaQ is written during the sweep by other SMs: read it through L2 (never a stale L1
     // line).  Every lane loads in converged code, before the per-component branches, so that a
     // warp waits for one dependent L2 round trip instead of one per divergent branch.
@@ -1156,9 +1273,11 @@ __device__ inline void prefetch_l2_range(const void* p, size_t bytes, size_t t, 
 
 // pf_first/pf_count: a later hyperplane whose records and neighbour positions this launch
 // pulls into L2 (otherwise they come from DRAM on the path between two dependent steps)
+// chained: 1 = the next hyperplane's launch is released after this one's wait, 2 = at entry
 template <typename R, bool LOWER>
 __global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int first, int count, int lanes,
                         int chained, int pf_first, int pf_count) {
+    if (chained == 2) asm volatile("griddepcontrol.launch_dependents;");
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (pf_count > 0) {
         const size_t T = (size_t)gridDim.x * blockDim.x;
@@ -1168,10 +1287,36 @@ __global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, 
     int e, L;
     sweep_map(g, lanes, e, L);
     if (e >= count) {
-        if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
+        if (chained) {
+            asm volatile("griddepcontrol.wait;" ::: "memory");
+            if (chained == 1) asm volatile("griddepcontrol.launch_dependents;");
+        }
         return;
     }
-    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, chained != 0, !(lanes & SWEEP_WPC));
+    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, chained != 0, !(lanes & SWEEP_WPC), chained == 1);
+}
+
+// Mixed path: one hyperplane per launch, one thread per position (sweep_pos_compact).
+// chained: 1 = the next hyperplane's launch is released after this one's wait, 2 = at entry,
+// so that its DeltaQ-independent loads (records, neighbour positions) run while this hyperplane
+// still waits for the previous one (every DeltaQ access stays after griddepcontrol.wait).
+template <bool LOWER>
+__global__ void k_sweep_c(const int* __restrict__ nbp, const float* __restrict__ rec, float* dq, int first, int count, int turb,
+                          int chained, int pf_first, int pf_count) {
+    if (chained == 2) asm volatile("griddepcontrol.launch_dependents;");
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pf_count > 0) {
+        const size_t T = (size_t)gridDim.x * blockDim.x;
+        prefetch_l2_range(rec + sw_at(pf_first, 0, NCREC), (size_t)pf_count * NCREC * sizeof(float), g, T);
+        prefetch_l2_range(nbp + sw_at(pf_first, 0, 6), (size_t)pf_count * 6 * sizeof(int), g, T);
+    }
+    if (g >= count) {
+        if (chained) asm volatile("griddepcontrol.wait;" ::: "memory");
+        if (chained == 1) asm volatile("griddepcontrol.launch_dependents;");
+        return;
+    }
+    sweep_pos_compact<LOWER>(nbp, rec, dq, (long long)first + g, turb, chained != 0);
+    if (chained == 1) asm volatile("griddepcontrol.launch_dependents;");
 }
 
 // Grid-wide barrier of a co-resident (cooperative) grid.  The wait is bounded: after `limit`

@@ -60,9 +60,13 @@ struct FluxLaunchers {
     void (*prep)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const SweepView&, const CaseDev*);
     void (*jac)(cudaStream_t, const DevBlock*, const SweepView&);     // neighbours' Jacobian terms (sweep order)
     // lanes: components swept (bits 0-1: 0 mean flow, 1 all, 2 k-omega) | SWEEP_WPC thread mapping
-    // (pf_first, pf_count: a later hyperplane prefetched into L2, count 0 = none)
-    void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained, int pf_first, int pf_count);
-    void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained, int pf_first, int pf_count);
+    // (pf_first, pf_count: a later hyperplane prefetched into L2, count 0 = none; chained: 0 plain
+    // launch, 1 programmatic dependent launch released after the wait, 2 released at entry (mixed
+    // path); cta: threads per CTA of the mixed path's one-thread-per-position launches, 0 = default)
+    void (*sweep_lower)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained, int pf_first, int pf_count,
+                        int cta);
+    void (*sweep_upper)(cudaStream_t, const SweepView&, int first, int count, int lanes, int chained, int pf_first, int pf_count,
+                        int cta);
     // both sweeps in one cooperative launch (grid must be co-resident: grid <= SMs x occupancy)
     // (limit: polls of one wait before the kernel gives up, records the error and returns)
     cudaError_t (*sweep_all)(cudaStream_t, const SweepView&, const int* plane_off, int nplanes, int lanes, SweepSync*,
@@ -78,6 +82,7 @@ struct FluxLaunchers {
     int (*sweep_tiles_occupancy)(int block);
     void (*scatter)(cudaStream_t, const DevBlock*, const SweepView&, int l0);   // DeltaQ l0..6 back to cell order
     size_t elem;                                    // bytes of the sweep arithmetic type
+    int rec_width;                                  // sweep record entries per position (NREC, or NCREC in FP32)
 };
 const FluxLaunchers& flux_launchers_f64();
 const FluxLaunchers& flux_launchers_f32();

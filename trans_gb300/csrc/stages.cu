@@ -272,7 +272,8 @@ namespace {
 int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     const int lanes = c->sweep_lanes | c->sweep_wpc;
     if (mode == 0 && c->sweep_exec &&
-        (c->sweep_exec_pdl != c->pdl || c->sweep_exec_wpc != c->sweep_wpc || c->sweep_exec_pf != c->sweep_pf)) {   // changed
+        (c->sweep_exec_pdl != c->pdl || c->sweep_exec_wpc != c->sweep_wpc || c->sweep_exec_pf != c->sweep_pf ||
+         c->sweep_exec_cta != c->sweep_cta)) {   // changed
         cudaGraphExecDestroy(c->sweep_exec);
         c->sweep_exec = nullptr;
     }
@@ -318,11 +319,11 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         for (int h = 0; h < nh; ++h)
             if (cnt(h))
                 c->fl->sweep_lower(s, c->sv, c->plane_off[h], cnt(h), lanes, c->pdl, d && h + d < nh ? c->plane_off[h + d] : 0,
-                                   d ? cnt(h + d) : 0);
+                                   d ? cnt(h + d) : 0, c->sweep_cta);
         for (int h = nh - 1; h >= 0; --h)
             if (cnt(h))
                 c->fl->sweep_upper(s, c->sv, c->plane_off[h], cnt(h), lanes, c->pdl, d && h - d >= 0 ? c->plane_off[h - d] : 0,
-                                   d ? cnt(h - d) : 0);
+                                   d ? cnt(h - d) : 0, c->sweep_cta);
     };
     auto count_planes = [&]() {
         for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
@@ -344,6 +345,7 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         c->sweep_exec_pdl = c->pdl;
         c->sweep_exec_wpc = c->sweep_wpc;
         c->sweep_exec_pf = c->sweep_pf;
+        c->sweep_exec_cta = c->sweep_cta;
     }
     CK(cudaGraphLaunch(c->sweep_exec, s));
     count_planes();
@@ -365,12 +367,26 @@ int tune_sweeps(Ctx* c) {
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    struct Cand { int mode, grid, block, pdl, ti, tj, tk, wpc, pf; };
+    struct Cand { int mode, grid, block, pdl, ti, tj, tk, wpc, pf, cta = 0; };
     std::vector<Cand> cands;
+    const bool fp32 = c->fl->elem == 4;
+    if (fp32) {
+        // mixed path: one thread per position; plain launches, or chained with the next
+        // hyperplane released after the wait (1) or at entry (2); prefetch distance; CTA size
+        for (int pdl : {0, 1, 2})
+            for (int pf : {0, 2})
+                for (int cta : {32, 64, 128}) cands.push_back({0, 0, 0, pdl, 0, 0, 0, 0, pf, cta});
+        const int occ = c->fl->sweep_all_occupancy(256);
+        if (occ >= 1) cands.push_back({1, nsm, 256, 0, 0, 0, 0, 0, 0});
+        const int tocc = c->fl->sweep_tiles_occupancy(256);
+        if (tocc >= 1) cands.push_back({3, tocc * nsm, 256, 0, 16, 4, 4, 0, 0});
+    }
     for (int wpc : {0, SWEEP_WPC}) {
+        if (fp32) break;
         for (int pf : {0, 1, 2, 4}) {             // prefetch distance (hyperplanes) of the plane launches
             cands.push_back({0, 0, 0, 1, 0, 0, 0, wpc, pf});
             cands.push_back({0, 0, 0, 0, 0, 0, 0, wpc, pf});
+            cands.push_back({0, 0, 0, 2, 0, 0, 0, wpc, pf});     // next launch released at entry
         }
         for (int block : {128, 256, 512}) {
             int occ = c->fl->sweep_all_occupancy(block);
@@ -385,7 +401,7 @@ int tune_sweeps(Ctx* c) {
                 if (occ >= 1) cands.push_back({3, occ * nsm, block, 0, sh[0], sh[1], sh[2], wpc, 0});
             }
     }
-    if (c->fl->sweep_flow_occupancy(256) >= 4) cands.push_back({2, 4 * nsm, 256, 0, 0, 0, 0, 0, 0});
+    if (!fp32 && c->fl->sweep_flow_occupancy(256) >= 4) cands.push_back({2, 4 * nsm, 256, 0, 0, 0, 0, 0, 0});
     const int pdl0 = c->pdl_allowed;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -398,6 +414,7 @@ int tune_sweeps(Ctx* c) {
         if (k.mode == 0) c->pdl = pdl0 ? k.pdl : 0;
         c->sweep_wpc = k.wpc;
         c->sweep_pf = k.pf;
+        c->sweep_cta = k.cta;
         if (k.mode == 3 && (rc = build_tiles(c, k.ti, k.tj, k.tk))) break;
         for (int rep = 0; rep < 2 && rc == TRANS_OK; ++rep) {      // first run warms up (graph build)
             if ((rc = save_dq(c, true))) break;
@@ -413,8 +430,9 @@ int tune_sweeps(Ctx* c) {
                                                  + (k.mode == 3 ? std::to_string(k.ti) + "x" + std::to_string(k.tj) + "x"
                                                                       + std::to_string(k.tk) + "/" : std::string())
                                                  + std::to_string(k.grid) + "x" + std::to_string(k.block)
-                                           : std::string(c->pdl ? "planes-chained" : "planes"))
+                                           : std::string(c->pdl ? (c->pdl == 2 ? "planes-early" : "planes-chained") : "planes"))
                                    + (k.wpc ? "/wpc" : "") + (k.pf ? "/pf" + std::to_string(k.pf) : "")
+                                   + (k.cta ? "/cta" + std::to_string(k.cta) : "")
                                    + ":" + std::to_string(ms) + "ms ";
                 if (ms < best) { best = ms; pick = k; }
             }
@@ -434,6 +452,7 @@ int tune_sweeps(Ctx* c) {
     c->sweep_mode = pick.mode; c->sweep_grid = pick.grid; c->sweep_block = pick.block;
     c->sweep_wpc = pick.wpc;
     c->sweep_pf = pick.pf;
+    c->sweep_cta = pick.cta;
     c->pdl = pick.mode == 0 ? (pdl0 ? pick.pdl : 0) : 0;
     return TRANS_OK;
 }

@@ -10,7 +10,7 @@ struct BCEntry {          // one boundary face cell of one connection (BC/Bounda
     int s[3], l[3];                 // interior source cells (layers 0,1,2) and ghost cells (1,2,3)
     int face;                       // face cell index for SD/Grad (i + IJKAdd)
     int dir;                        // IJKDirect (1..3)
-    int lor, pad_;                  // LeftOrRight
+    int lor, kindsub;               // LeftOrRight, SubBCType (wall: the frame of its grid velocity)
     double cost, sint;              // interface rotation
 };
 

@@ -77,7 +77,7 @@ int build_bc(Ctx* c, const CaseRec* cs) {
                 BCEntry E;
                 std::memset(&E, 0, sizeof(E));
                 E.kind = kind; E.blk = g0 + (int)nb; E.conn = (int)ic; E.i = I; E.j = J; E.k = K;
-                E.dir = a.IJKDirect; E.lor = a.LeftOrRight;
+                E.dir = a.IJKDirect; E.lor = a.LeftOrRight; E.kindsub = a.SubBCType;
                 E.sub = (J == a.pointStart[1]) ? 1 : 0;
                 const int* E3[3] = {a.CEIJKAdd, a.CEIJKAdd1, a.CEIJKAdd2};
                 for (int L = 0; L < 3; ++L) E.l[L] = cidx(b, I + E3[L][0], J + E3[L][1], K + E3[L][2]);
@@ -255,7 +255,7 @@ int rebuild(Ctx* c) {
             for (int r = 0; r < tl.count; ++r) qpos[t * CELL_TILE + r] = pos[tl.blk][(size_t)tl.start + r];
         }
         if ((rc = upload_vec(c, qpos.data(), sizeof(int) * qpos.size(), (void**)&c->d_qpos))) return rc;
-        CK(cudaMalloc(&c->d_rec, (size_t)NREC * Np * c->fl->elem));
+        CK(cudaMalloc(&c->d_rec, (size_t)c->fl->rec_width * Np * c->fl->elem));
         CK(cudaMalloc(&c->d_dqs, (size_t)DQ_STRIDE * Np * c->fl->elem));
         CK(cudaMalloc(&c->d_flags, (size_t)2 * Np * sizeof(int)));
         c->sv.cells = c->d_sweep; c->sv.nbp = c->d_nbp; c->sv.rec = c->d_rec; c->sv.dq = c->d_dqs; c->sv.n = N;
