@@ -40,6 +40,38 @@ namespace {
 inline double p15(double x) { return x * std::sqrt(x); }
 inline double sgn1(double b) { return b >= 0.0 ? 1.0 : -1.0; }
 inline double sq(double x) { return x * x; }
+// x**2.0 with a real exponent: Fortran's power with an even integral exponent, whose base may be
+// negative; the pow of tmath on |x|, as every real-exponent power of this restatement
+inline double pow2r(double x) { return otm::pow_(std::fabs(x), 2.0); }
+
+// Low-Mach preconditioning (IF_Precondition = 1), Common/UTIL_Precond_Funcs.F90.
+// getPrecondPara (:6-32): the preconditioning parameter ubetac2 of one state.
+double get_precond_para(const trans_params& p, double VM2, double AM2, double RR, double TT, double RMIUT, double ALAGMR) {
+    const double K = 3.0, Kc = 1.0;
+    double ubetac2 = std::min(std::max(VM2 / AM2, K * p.XM * p.XM), 1.0);
+    double RmiuL = (1.0 + p.Csthlnd) / (TT * p.Csth1 + p.Csthlnd) * p15(p.Csth1 * TT);
+    double RmiuAll = RmiuL + RMIUT;
+    return std::max(ubetac2, Kc * pow2r(RmiuAll / RR / p.Ref / ALAGMR) / AM2);
+}
+
+// PrecondDW (:90-127): the conservative increment (AinRo..AinRe) mapped through the
+// preconditioning matrix of the state (pRo, pV, pE, AAc, ubetac2, pTT)
+void precond_dw(const trans_params& p, double& AinRo, double& AinRx, double& AinRy, double& AinRz, double& AinRe, double pRo,
+                double pVx, double pVy, double pVz, double pE, double AAc, double ubetac2, double pTT) {
+    double pU2 = pVx * pVx + pVy * pVy + pVz * pVz;
+    double pUAU = pVx * AinRx + pVy * AinRy + pVz * AinRz;
+    AinRe = AinRe - (pUAU) - (pE / 1.4 - 1.2 * (pU2)) * AinRo;
+    double rCp = 1.4 / 0.4 * p.PPF * pRo;
+    double a11 = AAc * AAc * ubetac2;
+    double a15 = -0.4 * ubetac2 / rCp;
+    double b11 = 1.0 * a11 / rCp;
+    double b15 = (1.0 + 0.4 * ubetac2) / rCp;
+    double AinP = a11 * AinRo + a15 * AinRe;
+    double AinT = b11 * AinRo + b15 * AinRe;
+    AinRo = AinP / p.PPF / pTT - pRo * AinT / pTT;
+    AinRe = AinP / 0.4 + (pUAU);
+    (void)AinRx; (void)AinRy; (void)AinRz;
+}
 
 // Fortran-style arrays on the full ghost extent -2..N+2, leading components first.
 struct Arr {
@@ -120,6 +152,20 @@ void spectral_radius(Ctx& c, Blk& b) {
         double WW = Vxi * ARX3 + Vyi * ARY3 + Vzi * ARZ3 + vibc;
         double alfu = 0.0, alfv = 0.0, alfw = 0.0;
         double AAcu = AAc, AAcv = AAc, AAcw = AAc;
+        if (p.IF_Precondition) {            // Time/SpectralRadius.F90:91-127
+            double UVW2 = Vxi * Vxi + Vyi * Vyi + Vzi * Vzi;
+            double ubetac2 = get_precond_para(p, UVW2, AAc * AAc, Den, 0.0, 0.0, 1.0);
+            double RmiuAll = RmiuL + RmiuTL;
+            double ubu = std::max(ubetac2, pow2r(RmiuAll / Den / p.Ref / b.Alagm(1, I, J, K) / AAc));
+            alfu = (1.0 - ubu) / 2.0;
+            AAcu = std::sqrt(alfu * alfu * UVW2 + ubu * AAc * AAc);
+            double ubv = std::max(ubetac2, pow2r(RmiuAll / Den / p.Ref / b.Alagm(2, I, J, K) / AAc));
+            alfv = (1.0 - ubv) / 2.0;
+            AAcv = std::sqrt(alfv * alfv * UVW2 + ubv * AAc * AAc);
+            double ubw = std::max(ubetac2, pow2r(RmiuAll / Den / p.Ref / b.Alagm(3, I, J, K) / AAc));
+            alfw = (1.0 - ubw) / 2.0;
+            AAcw = std::sqrt(alfw * alfw * UVW2 + ubw * AAc * AAc);
+        }
         b.Rds(1, I, J, K) = std::fabs(UU) * (1.0 - alfu) + std::sqrt(ST1sq) * AAcu + 2.0 * ST1sq / b.Vol(I, J, K) * pruvmu / p.Ref;
         b.Rds(2, I, J, K) = std::fabs(VV) * (1.0 - alfv) + std::sqrt(ST2sq) * AAcv + 2.0 * ST2sq / b.Vol(I, J, K) * pruvmu / p.Ref;
         b.Rds(3, I, J, K) = std::fabs(WW) * (1.0 - alfw) + std::sqrt(ST3sq) * AAcw + 2.0 * ST3sq / b.Vol(I, J, K) * pruvmu / p.Ref;
@@ -1152,7 +1198,7 @@ void convect_mdcd(Ctx& c, Blk& b) {
 // ---------------------------------------------------------------------------------------
 void roe_common(const trans_params& p, double PLo, double PRo, double TLo, double TRo, double ULo, double URo,
                 double VLo, double VRo, double WLo, double WRo, double sav1, double sav2, double sav3, double sav,
-                double rLo, double rRo, double* out) {
+                double rLo, double rRo, double* out, double RmiuT = 0.0, double AlagmR = 1.0) {
     double rcpcv = p.PPF;
     double DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
     double ga = 1.4, ga1 = 1.4 - 1.0;
@@ -1177,14 +1223,27 @@ void roe_common(const trans_params& p, double PLo, double PRo, double TLo, doubl
     double anormaln = am;
     double dacou = acr - acl;
     (void)dacou;
-    double eig1 = std::fabs(unormaln);
-    double eig2 = std::fabs(unormaln + anormaln);
-    double eig3 = std::fabs(unormaln - anormaln);
-    if (eig1 < 0.1) eig1 = (eig1 * eig1 + 0.1 * 0.1) / 0.2;
-    if (eig2 < 0.1) eig2 = (eig2 * eig2 + 0.1 * 0.1) / 0.2;
-    if (eig3 < 0.1) eig3 = (eig3 * eig3 + 0.1 * 0.1) / 0.2;
-    double alf = 0.0, ubetac2 = 1.0;
-    double amrev = am;
+    double eig1, eig2, eig3, alf, ubetac2, amrev;
+    if (p.IF_Precondition) {        // Space/CONVECT_Roe_Original.F90:319-331
+        double TTL = am2 / ga / p.PPF;
+        ubetac2 = get_precond_para(p, vm2, am2, rm, TTL, RmiuT, AlagmR);
+        alf = (1.0 - ubetac2) / 2.0;
+        double unrev = unormaln * (1.0 - alf);
+        amrev = std::sqrt(pow2r(alf * unormaln) + ubetac2 * am2);
+        eig1 = std::fabs(unormaln);
+        eig2 = std::fabs(unrev + amrev);
+        eig3 = std::fabs(unrev - amrev);
+    } else {
+        eig1 = std::fabs(unormaln);
+        eig2 = std::fabs(unormaln + anormaln);
+        eig3 = std::fabs(unormaln - anormaln);
+        if (eig1 < 0.1) eig1 = (eig1 * eig1 + 0.1 * 0.1) / 0.2;
+        if (eig2 < 0.1) eig2 = (eig2 * eig2 + 0.1 * 0.1) / 0.2;
+        if (eig3 < 0.1) eig3 = (eig3 * eig3 + 0.1 * 0.1) / 0.2;
+        alf = 0.0;
+        ubetac2 = 1.0;
+        amrev = am;
+    }
     double dunormaln = (sav1n * (URo - ULo) + sav2n * (VRo - VLo) + sav3n * (WRo - WLo));
     double astar = (eig2 + eig3) / 2.0;
     double Mstar = (eig2 - eig3) / 2.0 / amrev;
@@ -1380,7 +1439,10 @@ void convect_inviscid(Ctx& c, Blk& b) {
             }
             if (p.Kind_Roe == 1) {
                 double rLo = b.rccl(d, i, j, k) * p.omega[0], rRo = b.rccr(d, i, j, k) * p.omega[0];
-                roe_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, rLo, rRo, f);
+                // RmiuT = VL(d,8), the face-averaged eddy viscosity (0 while turbulence is off);
+                // AlagmR = Alagm(d,i,j,k) (CONVECT_Roe_Original.F90:86-87)
+                roe_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, rLo, rRo, f,
+                           b.VL(d, 8, i, j, k), b.Alagm(d, i, j, k));
             } else {
                 ausmpw_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, f);
             }
@@ -1454,7 +1516,8 @@ void lusgs_adq(double pGam, double pVx, double pVy, double pVz, double aSDx, dou
 
 // neighbour term of the L (sgn=+1) and U (sgn=-1) sweeps for direction d at neighbour cell (ni,nj,nk);
 // (fi,fj,fk)/(gi,gj,gk) are the two faces of the neighbour cell whose metrics are averaged
-void lusgs_nb(Blk& b, int d, int ni, int nj, int nk, int fi, int fj, int fk, int gi, int gj, int gk, double sgn, double* out) {
+void lusgs_nb(const trans_params& p, Blk& b, int d, int ni, int nj, int nk, int fi, int fj, int fk, int gi, int gj, int gk,
+              double sgn, double* out) {
     double AinRo = b.D(1, ni, nj, nk), AinRx = b.D(2, ni, nj, nk), AinRy = b.D(3, ni, nj, nk);
     double AinRz = b.D(4, ni, nj, nk), AinRe = b.D(5, ni, nj, nk);
     double pRo = b.V(1, ni, nj, nk);
@@ -1467,6 +1530,15 @@ void lusgs_nb(Blk& b, int d, int ni, int nj, int nk, int fi, int fj, int fk, int
     double pPP = b.PP(ni, nj, nk);
     double Dif[5];
     lusgs_adq(1.4, pVx, pVy, pVz, aSDx, aSDy, aSDz, pPP, roinv, AinRo, AinRx, AinRy, AinRz, AinRe, Dif, vbc);
+    if (p.IF_Precondition) {        // TIME_LUSGS.F90:235-248 (and every neighbour of both sweeps)
+        double pE = b.V(5, ni, nj, nk) * roinv;
+        double pTT = b.T(ni, nj, nk);
+        double AAc = std::sqrt(1.4 * pPP * roinv);
+        double UVW2 = pVx * pVx + pVy * pVy + pVz * pVz;
+        double ALL = std::min(std::min(b.Alagm(1, ni, nj, nk), b.Alagm(2, ni, nj, nk)), b.Alagm(3, ni, nj, nk));
+        double ubetac2 = get_precond_para(p, UVW2, AAc * AAc, pRo, pTT, b.Rmiu(ni, nj, nk), ALL);
+        precond_dw(p, Dif[0], Dif[1], Dif[2], Dif[3], Dif[4], pRo, pVx, pVy, pVz, pE, AAc, ubetac2, pTT);
+    }
     double RDSt = b.Rds(d, ni, nj, nk);
     for (int L = 0; L < 5; ++L) {
         if (sgn > 0) out[L] = 0.5 * (Dif[L] + RDSt * b.D(L + 1, ni, nj, nk));
@@ -1488,6 +1560,23 @@ void time_lusgs(Ctx& c, Blk& b) {
         double stept = 2.0 * b.Dtm(I, J, K) / (3.0 * b.Dtm(I, J, K) / p.DT_LUSGS_Main + 2.0);
         b.F(1, I, J, K) = 1.0 + (b.Rds(1, I, J, K) + b.Rds(2, I, J, K) + b.Rds(3, I, J, K)) * (stept / b.Vol(I, J, K));
     }
+    if (p.IF_Precondition) {        // TIME_LUSGS.F90:113-160: the right-hand side preconditioned
+        for (int K = 1; K <= b.NK1; ++K)
+        for (int J = 1; J <= b.NJ1; ++J)
+        for (int I = 1; I <= b.NI1; ++I) {
+            double pRo = b.V(1, I, J, K);
+            double roinv = 1.0 / pRo;
+            double pVx = b.V(2, I, J, K) * roinv, pVy = b.V(3, I, J, K) * roinv, pVz = b.V(4, I, J, K) * roinv;
+            double pE = b.V(5, I, J, K) * roinv;
+            double pPP = b.PP(I, J, K), pTT = b.T(I, J, K);
+            double AAc = std::sqrt(1.4 * pPP * roinv);
+            double UVW2 = pVx * pVx + pVy * pVy + pVz * pVz;
+            double ALL = std::min(std::min(b.Alagm(1, I, J, K), b.Alagm(2, I, J, K)), b.Alagm(3, I, J, K));
+            double ubetac2 = get_precond_para(p, UVW2, AAc * AAc, pRo, pTT, b.Rmiu(I, J, K), ALL);
+            precond_dw(p, b.D(1, I, J, K), b.D(2, I, J, K), b.D(3, I, J, K), b.D(4, I, J, K), b.D(5, I, J, K), pRo, pVx, pVy,
+                       pVz, pE, AAc, ubetac2, pTT);
+        }
+    }
     // L sweep
     for (int K = 1; K <= b.NK1; ++K)
     for (int J = 1; J <= b.NJ1; ++J)
@@ -1495,9 +1584,9 @@ void time_lusgs(Ctx& c, Blk& b) {
         double stept = 2.0 * b.Dtm(I, J, K) / (3.0 * b.Dtm(I, J, K) / p.DT_LUSGS_Main + 2.0);
         double cvs = stept / b.Vol(I, J, K);
         double Di[5] = {0, 0, 0, 0, 0}, Dj[5] = {0, 0, 0, 0, 0}, Dk[5] = {0, 0, 0, 0, 0};
-        if (I != 1) lusgs_nb(b, 1, I - 1, J, K, I, J, K, I - 1, J, K, +1, Di);
-        if (J != 1) lusgs_nb(b, 2, I, J - 1, K, I, J, K, I, J - 1, K, +1, Dj);
-        if (K != 1) lusgs_nb(b, 3, I, J, K - 1, I, J, K, I, J, K - 1, +1, Dk);
+        if (I != 1) lusgs_nb(p, b, 1, I - 1, J, K, I, J, K, I - 1, J, K, +1, Di);
+        if (J != 1) lusgs_nb(p, b, 2, I, J - 1, K, I, J, K, I, J - 1, K, +1, Dj);
+        if (K != 1) lusgs_nb(p, b, 3, I, J, K - 1, I, J, K, I, J, K - 1, +1, Dk);
         stept = 2.0 * b.Dtm(I, J, K) / (3.0 * b.Dtm(I, J, K) / p.DT_LUSGS_Main + 2.0);
         for (int L = 1; L <= 5; ++L)
             b.D(L, I, J, K) = (b.D(L, I, J, K) * stept + (Di[L - 1] + Dj[L - 1] + Dk[L - 1]) * cvs) / b.F(1, I, J, K);
@@ -1509,9 +1598,9 @@ void time_lusgs(Ctx& c, Blk& b) {
         double stept = 2.0 * b.Dtm(I, J, K) / (3.0 * b.Dtm(I, J, K) / p.DT_LUSGS_Main + 2.0);
         double cvs = stept / b.Vol(I, J, K);
         double Di[5] = {0, 0, 0, 0, 0}, Dj[5] = {0, 0, 0, 0, 0}, Dk[5] = {0, 0, 0, 0, 0};
-        if (I != b.NI1) lusgs_nb(b, 1, I + 1, J, K, I + 2, J, K, I + 1, J, K, -1, Di);
-        if (J != b.NJ1) lusgs_nb(b, 2, I, J + 1, K, I, J + 2, K, I, J + 1, K, -1, Dj);
-        if (K != b.NK1) lusgs_nb(b, 3, I, J, K + 1, I, J, K + 2, I, J, K + 1, -1, Dk);
+        if (I != b.NI1) lusgs_nb(p, b, 1, I + 1, J, K, I + 2, J, K, I + 1, J, K, -1, Di);
+        if (J != b.NJ1) lusgs_nb(p, b, 2, I, J + 1, K, I, J + 2, K, I, J + 1, K, -1, Dj);
+        if (K != b.NK1) lusgs_nb(p, b, 3, I, J, K + 1, I, J, K + 2, I, J, K + 1, -1, Dk);
         for (int L = 1; L <= 5; ++L)
             b.D(L, I, J, K) = b.D(L, I, J, K) - (Di[L - 1] + Dj[L - 1] + Dk[L - 1]) * cvs / b.F(1, I, J, K);
     }
@@ -1857,6 +1946,26 @@ void time_update_v(Ctx& c, Blk& b) {
         double AinRz = b.D(4, I, J, K), AinRe = b.D(5, I, J, K);
         double pRo = b.V(1, I, J, K);
         double roinv = 1.0 / pRo;
+        if (p.IF_Precondition) {
+            // TIME_Update_V.F90:580-607: conservative increments; the kinetic energy takes the
+            // new momenta with the old 1/rho, and T the old pressure with the new density
+            double pRx = b.V(2, I, J, K), pRy = b.V(3, I, J, K), pRz = b.V(4, I, J, K), pRe = b.V(5, I, J, K);
+            pRo = pRo + AinRo;
+            pRo = std::fabs(pRo);
+            pRx = pRx + AinRx; pRy = pRy + AinRy; pRz = pRz + AinRz;
+            pRe = pRe + AinRe;
+            pRe = std::fabs(pRe);
+            double DV = 0.5 * (pRx * pRx + pRy * pRy + pRz * pRz) * roinv;
+            double pPP = (pRe - DV) * (1.4 - 1.0);
+            if (pPP <= 0.0) {
+                pPP = std::fabs(pPP);
+                pRe = pPP / (1.4 - 1.0) + DV;
+            }
+            double pTT = p.RXM2 * b.PP(I, J, K) / pRo;
+            b.V(1, I, J, K) = pRo; b.V(2, I, J, K) = pRx; b.V(3, I, J, K) = pRy; b.V(4, I, J, K) = pRz; b.V(5, I, J, K) = pRe;
+            b.PP(I, J, K) = pPP;
+            b.T(I, J, K) = pTT;
+        } else {
         double pVx = b.V(2, I, J, K) * roinv, pVy = b.V(3, I, J, K) * roinv, pVz = b.V(4, I, J, K) * roinv;
         double AinX = (AinRx - pVx * AinRo) * roinv;
         double AinY = (AinRy - pVy * AinRo) * roinv;
@@ -1876,6 +1985,7 @@ void time_update_v(Ctx& c, Blk& b) {
         b.V(4, I, J, K) = pRo * pVz;
         double DV = 0.5 * (pVx * pVx + pVy * pVy + pVz * pVz);
         b.V(5, I, J, K) = b.PP(I, J, K) / (1.4 - 1.0) + DV * pRo - 0.5 * sq(p.omega[0] * b.rad(I, J, K)) * pRo;
+        }
         if (!turb_upd) continue;
         double AinRTk = b.D(6, I, J, K), AinRTO = b.D(7, I, J, K);
         double ARTk = b.V(6, I, J, K), ARTO = b.V(7, I, J, K);
@@ -2149,7 +2259,9 @@ extern "C" {
 
 int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks, void** out) {
     if (!p || !blocks || nblocks <= 0 || !out) return TRANS_E_ARG;
-    if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2)) return TRANS_E_ARG;
+    if ((p->IF_Precondition != 0 && p->IF_Precondition != 1) || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2))
+        return TRANS_E_ARG;
+    if (p->IF_Precondition == 1 && p->IF_RK != 0) return TRANS_E_ARG;     // preconditioning with LU-SGS only
     if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4) return TRANS_E_ARG;
     if (p->Kind_Roe < 1 || p->Kind_Roe > 3) return TRANS_E_ARG;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return TRANS_E_ARG;

@@ -117,7 +117,7 @@ struct ParamsT {          // module globals the kernels read (trans_params + der
     TG_PARAM_REALS(TG_DECL)
 #undef TG_DECL
     int Kind_Spatial, Kind_Roe, Kind_Hybrid, Kind_SubHY, Kind_Dual, IF_Local_Main, IF_Local_Sub;
-    int IF_Comppress, If_fix_Transition, Kind_Model;
+    int IF_Comppress, If_fix_Transition, Kind_Model, IF_Precondition;
 };
 using Params = ParamsT<double>;
 
@@ -130,7 +130,7 @@ inline ParamsT<R> params_as(const Params& p) {
     q.Kind_Spatial = p.Kind_Spatial; q.Kind_Roe = p.Kind_Roe; q.Kind_Hybrid = p.Kind_Hybrid;
     q.Kind_SubHY = p.Kind_SubHY; q.Kind_Dual = p.Kind_Dual; q.IF_Local_Main = p.IF_Local_Main;
     q.IF_Local_Sub = p.IF_Local_Sub; q.IF_Comppress = p.IF_Comppress; q.If_fix_Transition = p.If_fix_Transition;
-    q.Kind_Model = p.Kind_Model;
+    q.Kind_Model = p.Kind_Model; q.IF_Precondition = p.IF_Precondition;
     return q;
 }
 
@@ -201,6 +201,69 @@ template <typename R> __device__ inline R mu_suth_nocs(const ParamsT<R>& p, R TT
 template <typename R> __device__ inline R cube_pow(R x);
 template <> __device__ inline double cube_pow<double>(double x) { return tmx::pow_(x, 3.0); }
 template <> __device__ inline float cube_pow<float>(float x) { return x * x * x; }
+
+// x**2.0 of a Fortran real exponent whose base may be negative (an even integral power): the pow
+// of tmath on |x| in FP64 (as the oracle), the product in FP32
+template <typename R> __device__ inline R pow2r(R x);
+template <> __device__ inline double pow2r<double>(double x) { return tmx::pow_(fabs(x), 2.0); }
+template <> __device__ inline float pow2r<float>(float x) { return x * x; }
+
+// Low-Mach preconditioning (IF_Precondition = 1), Common/UTIL_Precond_Funcs.F90.
+// getPrecondPara (:6-32): the preconditioning parameter ubetac2 of one state
+template <typename R>
+__device__ inline R get_precond_para(const ParamsT<R>& p, R VM2, R AM2, R RR, R TT, R RMIUT, R ALAGMR) {
+    const R K = R(3.0), Kc = R(1.0);
+    R ubetac2 = dmin(dmax(VM2 / AM2, K * R(p.XM) * R(p.XM)), R(1.0));
+    R RmiuL = mu_suth<R>(p, TT);
+    R RmiuAll = RmiuL + RMIUT;
+    return dmax(ubetac2, Kc * pow2r(RmiuAll / RR / R(p.Ref) / ALAGMR) / AM2);
+}
+
+// The coefficients of PrecondDW (:90-127) for one state, each formed as the reference forms it:
+// pVx, pVy, pVz, pE/1.4 - 1.2 |v|^2, a11, a15, b11, b15, pRo, pTT, and PPF
+constexpr int NPC = 11;
+
+template <typename R>
+__device__ inline void precond_terms(const ParamsT<R>& p, R pRo, R pVx, R pVy, R pVz, R pE, R AAc, R ubetac2, R pTT, R* t) {
+    R pU2 = pVx * pVx + pVy * pVy + pVz * pVz;
+    R rCp = R(1.4 / 0.4) * R(p.PPF) * pRo;
+    t[0] = pVx; t[1] = pVy; t[2] = pVz;
+    t[3] = pE / R(1.4) - R(1.2) * (pU2);
+    t[4] = AAc * AAc * ubetac2;
+    t[5] = R(-0.4) * ubetac2 / rCp;
+    t[6] = R(1.0) * t[4] / rCp;
+    t[7] = (R(1.0) + R(0.4) * ubetac2) / rCp;
+    t[8] = pRo;
+    t[9] = pTT;
+    t[10] = R(p.PPF);
+}
+
+// PrecondDW applied to the increment A[0..4] with the coefficients t of precond_terms
+template <typename R>
+__device__ inline void precond_apply(R* A, const R* t) {
+    R pUAU = t[0] * A[1] + t[1] * A[2] + t[2] * A[3];
+    A[4] = A[4] - (pUAU) - (t[3]) * A[0];
+    R AinP = t[4] * A[0] + t[5] * A[4];
+    R AinT = t[6] * A[0] + t[7] * A[4];
+    A[0] = AinP / t[10] / t[9] - t[8] * AinT / t[9];
+    A[4] = AinP / R(0.4) + (pUAU);
+}
+
+// PrecondDW coefficients of the cell at slot index c (FP64 slots; TIME_LUSGS.F90:113-160 and
+// every neighbour of the sweeps, :235-248): ubetac2 from getPrecondPara with the cell's
+// Rmiu and its smallest Alagm
+__device__ inline void precond_terms_at(const Params& p, const DevBlock& b, int c, double* t) {
+    const double pRo = slot(b, S_V)[c];
+    const double roinv = 1.0 / pRo;
+    const double pVx = slot(b, S_V + 1)[c] * roinv, pVy = slot(b, S_V + 2)[c] * roinv, pVz = slot(b, S_V + 3)[c] * roinv;
+    const double pE = slot(b, S_V + 4)[c] * roinv;
+    const double pPP = slot(b, S_PP)[c], pTT = slot(b, S_T)[c];
+    const double AAc = sqrt(1.4 * pPP * roinv);
+    const double UVW2 = pVx * pVx + pVy * pVy + pVz * pVz;
+    const double ALL = dmin(dmin(slot(b, S_ALAGM)[c], slot(b, S_ALAGM + 1)[c]), slot(b, S_ALAGM + 2)[c]);
+    const double ub = get_precond_para<double>(p, UVW2, AAc * AAc, pRo, pTT, slot(b, S_RMIU)[c], ALL);
+    precond_terms<double>(p, pRo, pVx, pVy, pVz, pE, AAc, ub, pTT, t);
+}
 
 // Space/UTIL_MUSCL.F90:2-18
 template <typename R> __device__ inline R alimiter(R var1, R var2) {
@@ -343,7 +406,7 @@ __device__ inline void roe_rotated(const ParamsT<R>& p, R PLo, R PRo, R TLo, R T
 // Space/CONVECT_Roe_Original.F90:242-407 (non-preconditioned, no rotation); out = flux / |S|
 template <typename R>
 __device__ inline void roe_flux(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo, R WRo,
-                                R sav1, R sav2, R sav3, R sav, R* out) {
+                                R sav1, R sav2, R sav3, R sav, R* out, R RmiuT = R(0.0), R AlagmR = R(1.0)) {
     R rcpcv = R(p.PPF);
     R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
     const R ga = R(1.4), ga1 = R(1.4 - 1.0);
@@ -365,15 +428,28 @@ __device__ inline void roe_flux(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo,
     R am = sqrt(am2);
     R sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
     R unormaln = (sav1n * um + sav2n * vm + sav3n * wm);
-    R eig1 = fabs(unormaln);
-    R eig2 = fabs(unormaln + am);
-    R eig3 = fabs(unormaln - am);
-    const R e01 = R(0.1), ee = R(0.1 * 0.1), e02 = R(0.2);
-    if (eig1 < e01) eig1 = (eig1 * eig1 + ee) / e02;
-    if (eig2 < e01) eig2 = (eig2 * eig2 + ee) / e02;
-    if (eig3 < e01) eig3 = (eig3 * eig3 + ee) / e02;
-    const R alf = R(0.0), ubetac2 = R(1.0);
-    R amrev = am;
+    R eig1, eig2, eig3, alf, ubetac2, amrev;
+    if (p.IF_Precondition) {        // Space/CONVECT_Roe_Original.F90:319-331 (RmiuT = VL(d,8), AlagmR = Alagm(d))
+        R TTL = am2 / ga / R(p.PPF);
+        ubetac2 = get_precond_para<R>(p, vm2, am2, rm, TTL, RmiuT, AlagmR);
+        alf = (R(1.0) - ubetac2) / R(2.0);
+        R unrev = unormaln * (R(1.0) - alf);
+        amrev = sqrt(pow2r<R>(alf * unormaln) + ubetac2 * am2);
+        eig1 = fabs(unormaln);
+        eig2 = fabs(unrev + amrev);
+        eig3 = fabs(unrev - amrev);
+    } else {
+        eig1 = fabs(unormaln);
+        eig2 = fabs(unormaln + am);
+        eig3 = fabs(unormaln - am);
+        const R e01 = R(0.1), ee = R(0.1 * 0.1), e02 = R(0.2);
+        if (eig1 < e01) eig1 = (eig1 * eig1 + ee) / e02;
+        if (eig2 < e01) eig2 = (eig2 * eig2 + ee) / e02;
+        if (eig3 < e01) eig3 = (eig3 * eig3 + ee) / e02;
+        alf = R(0.0);
+        ubetac2 = R(1.0);
+        amrev = am;
+    }
     R dunormaln = (sav1n * (URo - ULo) + sav2n * (VRo - VLo) + sav3n * (WRo - WLo));
     R astar = (eig2 + eig3) / R(2.0);
     R Mstar = (eig2 - eig3) / R(2.0) / amrev;

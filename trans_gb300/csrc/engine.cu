@@ -46,7 +46,7 @@ Params make_params(const trans_params& p) {
     d.Kind_Spatial = p.Kind_Spatial; d.Kind_Roe = p.Kind_Roe; d.Kind_Hybrid = p.Kind_Hybrid;
     d.Kind_SubHY = p.Kind_SubHY; d.Kind_Dual = p.Kind_Dual; d.IF_Local_Main = p.IF_Local_Main;
     d.IF_Local_Sub = p.IF_Local_Sub; d.IF_Comppress = p.IF_Comppress; d.If_fix_Transition = p.If_fix_Transition;
-    d.Kind_Model = p.Kind_Model;
+    d.Kind_Model = p.Kind_Model; d.IF_Precondition = p.IF_Precondition;
     return d;
 }
 
@@ -54,8 +54,11 @@ Params make_params(const trans_params& p) {
 
 // options outside the configurations of this hot path are rejected, never approximated
 bool params_supported(const trans_params* p) {
-    if (p->IF_Precondition != 0 || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2) || p->IF_Euler != 0)
+    if ((p->IF_Precondition != 0 && p->IF_Precondition != 1) || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2) ||
+        p->IF_Euler != 0)
         return false;
+    // low-Mach preconditioning: LU-SGS marching, FP64 path
+    if (p->IF_Precondition == 1 && (p->IF_RK != 0 || p->precision != TRANS_FP64)) return false;
     if (p->IF_RK != 0 && p->IF_RK != 1) return false;
     if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4 || p->Kind_Roe < 1 || p->Kind_Roe > 3) return false;
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return false;
@@ -125,6 +128,7 @@ long long case_bytes(const trans_params* p, int nblocks, const trans_block* bloc
     long long b = padded * case_slots(*p) * (8 + (precision == TRANS_MIXED ? 4 : 0));
     const long long rec = precision == TRANS_MIXED ? NCREC : NREC;      // sweep record entries per position
     b += interior * ((rec + 2LL * DQ_STRIDE) * elem + 8LL * 4 + (long long)sizeof(SweepCell));
+    if (p->IF_Precondition == 1) b += interior * 6LL * NPC * 8;          // the neighbours' PrecondDW coefficients
     b += interior / 16 + 4096;           // tiles, norm partials, boundary tables (rounded up)
     return b;
 }
@@ -186,7 +190,7 @@ void free_worklists(Ctx* c) {
     dfree(c->d_blk); dfree(c->d_off); dfree(c->d_cell); dfree(c->d_ghost);
     for (int d = 0; d < 3; ++d) dfree(c->d_face[d]);
     dfree(c->d_bc); dfree(c->d_outlet); dfree(c->d_lines); dfree(c->d_sweep); dfree(c->d_plane_off);
-    dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq_save); dfree(c->d_parts);
+    dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq_save); dfree(c->d_parts); dfree(c->d_pc);
     dfree(c->d_cdev); dfree(c->d_stage); dfree(c->d_tile_first); dfree(c->d_norms);
     dfree(c->d_tiles); dfree(c->d_tflags); dfree(c->d_qpos); dfree(c->d_bc_first); dfree(c->d_intg);
     c->tv = TileView{};
@@ -226,6 +230,8 @@ int case_add(Ctx* c, const trans_params* p, int nblocks, const trans_block* bloc
     if (p->precision != c->precision) return fail(c, TRANS_E_ARG, "a context holds cases of one precision mode");
     for (CaseRec* o : c->cases) {
         if (o->p.IF_RK != p->IF_RK) return fail(c, TRANS_E_ARG, "cases of one context share the time integrator");
+        if (o->p.IF_Precondition != p->IF_Precondition)
+            return fail(c, TRANS_E_ARG, "cases of one context share the preconditioning switch");
         if (sub_iterations(o->p) != sub_iterations(*p) || (o->p.Kind_Dual != 0) != (p->Kind_Dual != 0))
             return fail(c, TRANS_E_ARG, "cases of one context share the sub-iteration count");
     }

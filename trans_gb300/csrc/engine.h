@@ -87,6 +87,7 @@ struct Ctx {
     void* d_rec = nullptr;
     void* d_dqs = nullptr;
     void* d_dq_save = nullptr;
+    double* d_pc = nullptr;              // PrecondDW coefficients of the sweep neighbours (IF_Precondition = 1)
     NormPart* d_parts = nullptr;
     std::vector<NormPart> h_parts;
     int* d_tile_first = nullptr;         // first cell tile of each block (+ end)

@@ -29,10 +29,12 @@ void prep(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const in
 }
 // the FP64 path's neighbour Jacobian terms; the mixed path rebuilds them in the sweep from the
 // compact records k_lusgs_prep writes, so it has no such pass
-void jac(cudaStream_t s, const DevBlock* b, const SweepView& v) {
+void jac(cudaStream_t s, const DevBlock* b, const SweepView& v, const CaseDev* cd) {
     if constexpr (sizeof(TG_R) == 8) {
         if (v.n > 0)
             k_lusgs_jac<TG_R><<<(unsigned)((v.n + 31) / 32), 6 * 32, 0, s>>>(b, v.cells, v.nbp, (TG_R*)v.rec, v.n);
+        if (v.n > 0 && v.pc)        // low-Mach preconditioning: the neighbours' PrecondDW coefficients
+            k_lusgs_jac_pc<<<(unsigned)((6 * v.n + 127) / 128), 128, 0, s>>>(b, v.cells, v.nbp, cd, (double*)v.pc, v.n);
     }
 }
 // one hyperplane; chained = launched with programmatic stream serialisation, so that this
@@ -73,7 +75,8 @@ void swp(cudaStream_t s, const SweepView& v, int first, int count, int turb, int
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = chained ? 1 : 0;
-    cudaLaunchKernelEx(&cfg, k_sweep<TG_R, LOWER>, nbp, rec, dq, n, first, count, turb, chained, pf_first, pf_count);
+    const TG_R* pc = (const TG_R*)v.pc;
+    cudaLaunchKernelEx(&cfg, k_sweep<TG_R, LOWER>, nbp, rec, dq, n, first, count, turb, chained, pf_first, pf_count, pc);
 }
 void swl(cudaStream_t s, const SweepView& v, int first, int count, int turb, int chained, int pf_first, int pf_count, int cta) {
     swp<true>(s, v, first, count, turb, chained, pf_first, pf_count, cta);
@@ -87,8 +90,9 @@ cudaError_t swa(cudaStream_t s, const SweepView& v, const int* po, int nplanes, 
     const TG_R* rec = (const TG_R*)v.rec;
     TG_R* dq = (TG_R*)v.dq;
     long long n = v.n;
+    const TG_R* pc = (const TG_R*)v.pc;
     void* args[] = {(void*)&nbp, (void*)&rec, (void*)&dq, (void*)&n, (void*)&po, (void*)&nplanes, (void*)&turb,
-                    (void*)&sy, (void*)&limit};
+                    (void*)&sy, (void*)&limit, (void*)&pc};
     return cudaLaunchCooperativeKernel((const void*)k_sweep_all<TG_R>, dim3(grid), dim3(block), args, 0, s);
 }
 int swa_occ(int block) {
@@ -102,8 +106,9 @@ cudaError_t swf(cudaStream_t s, const SweepView& v, int* flagL, int* flagU, int 
     const TG_R* rec = (const TG_R*)v.rec;
     TG_R* dq = (TG_R*)v.dq;
     long long n = v.n;
+    const TG_R* pc = (const TG_R*)v.pc;
     void* args[] = {(void*)&nbp, (void*)&rec, (void*)&dq, (void*)&n, (void*)&flagL, (void*)&flagU, (void*)&turb, (void*)&sy,
-                    (void*)&limit};
+                    (void*)&limit, (void*)&pc};
     return cudaLaunchCooperativeKernel((const void*)k_sweep_flow<TG_R>, dim3(grid), dim3(block), args, 0, s);
 }
 int swf_occ(int block) {
@@ -120,8 +125,9 @@ cudaError_t swt(cudaStream_t s, const SweepView& v, const TileView& tv, int lane
     TG_R* dq = (TG_R*)v.dq;
     long long n = v.n;
     TileView t = tv;
+    const TG_R* pc = (const TG_R*)v.pc;
     void* args[] = {(void*)&nbp, (void*)&rec, (void*)&dq, (void*)&n, (void*)&t, (void*)&lanes, (void*)&flags, (void*)&counter,
-                    (void*)&sy, (void*)&limit};
+                    (void*)&sy, (void*)&limit, (void*)&pc};
     return cudaLaunchCooperativeKernel((const void*)k_sweep_tiles<TG_R>, dim3(grid), dim3(block), args, 0, s);
 }
 int swt_occ(int block) {

@@ -40,11 +40,25 @@ __global__ void k_specrad(const DevBlock* __restrict__ blks, const Tile* __restr
     double vol = slot(b, S_VOL)[c];
     double rs = 0.0;
     double Rd[3];
+    // low-Mach preconditioning (Time/SpectralRadius.F90:91-127): the acoustic speed and the
+    // convective weight of each direction from ubetac2 and its viscous limit
+    double UVW2 = 0.0, ubetac2 = 1.0, RmiuAll = 0.0;
+    if (p.IF_Precondition) {
+        UVW2 = Vxi * Vxi + Vyi * Vyi + Vzi * Vzi;
+        ubetac2 = get_precond_para<double>(p, UVW2, AAc * AAc, Den, 0.0, 0.0, 1.0);
+        RmiuAll = RmiuL + RmiuTL;
+    }
     for (int d = 0; d < 3; ++d) {
         double ARX = slot(b, S_ASD + 3 * d)[c], ARY = slot(b, S_ASD + 3 * d + 1)[c], ARZ = slot(b, S_ASD + 3 * d + 2)[c];
         double STsq = ARX * ARX + ARY * ARY + ARZ * ARZ;
         double UU = Vxi * ARX + Vyi * ARY + Vzi * ARZ + 0.0;
-        Rd[d] = fabs(UU) * (1.0 - 0.0) + sqrt(STsq) * AAc + 2.0 * STsq / vol * pruvmu / p.Ref;
+        double alf = 0.0, AAcd = AAc;
+        if (p.IF_Precondition) {
+            double ubd = dmax(ubetac2, pow2r<double>(RmiuAll / Den / p.Ref / slot(b, S_ALAGM + d)[c] / AAc));
+            alf = (1.0 - ubd) / 2.0;
+            AAcd = sqrt(alf * alf * UVW2 + ubd * AAc * AAc);
+        }
+        Rd[d] = fabs(UU) * (1.0 - alf) + sqrt(STsq) * AAcd + 2.0 * STsq / vol * pruvmu / p.Ref;
         slot(b, S_RDS + d)[c] = Rd[d];
     }
     rs = Rd[0] + Rd[1] + Rd[2];
@@ -720,9 +734,13 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
                        Funscheme, f);
         for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = f[L];
     } else {
-        if (p.Kind_Roe == 1)
-            roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
-        else
+        if (p.Kind_Roe == 1) {
+            // preconditioning reads VL(d,8), the face-averaged eddy viscosity (0 while turbulence
+            // is off), and Alagm(d) of the face's cell (Space/CONVECT_Roe_Original.F90:86-87)
+            const R RmiuTf = (p.IF_Precondition && turb) ? favg<R>(rs<R>(b, S_RMIU), al, ainv, c, s) : R(0.0);
+            roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f, RmiuTf,
+                        R(al[c]));
+        } else
             ausmpw_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
         for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = (f[L] * sav);
     }
@@ -887,6 +905,14 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
         }
     };
     for (int L = 0; L < 5; ++L) DQ(L) = rhs(L);
+    if constexpr (!MIXED) {
+        if (pd.IF_Precondition) {     // the right-hand side preconditioned (TIME_LUSGS.F90:113-160)
+            double A[5] = {DQ(0), DQ(1), DQ(2), DQ(3), DQ(4)}, tpc[NPC];
+            precond_terms_at(pd, b, c, tpc);
+            precond_apply<double>(A, tpc);
+            for (int L = 0; L < 5; ++L) DQ(L) = A[L];
+        }
+    }
     if (!turb) {            // the k-omega lanes of the sweeps then produce zeros
         DQ(5) = rs<R>(b, S_D + 5)[c];
         DQ(6) = rs<R>(b, S_D + 6)[c];
@@ -1057,6 +1083,26 @@ __global__ void __launch_bounds__(6 * 32) k_lusgs_jac(const DevBlock* __restrict
 }
 
 
+// The PrecondDW coefficients of the six neighbours of every sweep position (FP64 path, low-Mach
+// preconditioning): one thread per (position, neighbour); a missing neighbour is left unused
+static __global__ void k_lusgs_jac_pc(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, const int* __restrict__ nbp,
+                               const CaseDev* __restrict__ cdev, double* __restrict__ pc, long long N) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= 6 * N) return;
+    const long long q = g / 6;
+    const int k = (int)(g % 6);
+    if (nbp[sw_at(q, k, 6)] < 0) return;
+    const SweepCell sc = cells[q];
+    const DevBlock b = blks[sc.blk];
+    const Params p = cdev[b.cs].p;
+    const int c = cidx(b, sc.i, sc.j, sc.k);
+    const int d = k % 3;
+    const int st = d == 0 ? 1 : (d == 1 ? b.PI : b.PI * b.PJ);
+    double t[NPC];
+    precond_terms_at(p, b, k < 3 ? c - st : c + st, t);
+    for (int m = 0; m < NPC; ++m) pc[sw_at(q, k * NPC + m, 6 * NPC)] = t[m];
+}
+
 // ---------------------------------------------------------------------------------------
 // LU-SGS sweeps (Time/TIME_LUSGS.F90:172-675, Time/TURBTWO_TIME_LUSGS_SST.F90:562-766) on the
 // i+j+k hyperplanes of every block.  Any order of the (i-1,j-1,k-1) dependency graph
@@ -1160,7 +1206,8 @@ __device__ inline void sweep_pos_compact(const int* __restrict__ nbp, const floa
 
 template <typename R, bool LOWER>
 __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, long long q,
-                                  int L, int turb, bool chained = false, bool hoist = true, bool release = true) {
+                                  int L, int turb, bool chained = false, bool hoist = true, bool release = true,
+                                  const R* __restrict__ pc = nullptr) {
     if constexpr (sizeof(R) == 4) {     // mixed path: lane 0 of a position computes all its components
         if (L != 0) {
             if (chained) { asm volatile("griddepcontrol.wait;" ::: "memory"); asm volatile("griddepcontrol.launch_dependents;"); }
@@ -1248,6 +1295,26 @@ __device__ inline void sweep_item(const int* __restrict__ nbp, const R* __restri
             } else {
                 Dif = AinRo * k[d][4] * k[d][5] + AinRx * k[d][0] + AinRy * k[d][1] + AinRz * k[d][2] + AinRe * k[d][3];
             }
+            if constexpr (sizeof(R) == 8) {
+                if (pc && (L == 0 || L == 4)) {
+                    // low-Mach preconditioning: PrecondDW of the neighbour's whole A(Q) DeltaQ
+                    // (TIME_LUSGS.F90:235-248); its rows as the lanes form them, then the map
+                    const int jd = NBREC * (side + d);
+                    R A[5];
+                    A[0] = AinRo * R(0.0) + AinRx * REC(jd + JC_R0) + AinRy * REC(jd + JC_R0 + 1) + AinRz * REC(jd + JC_R0 + 2) +
+                           AinRe * R(0.0);
+                    for (int l = 1; l < 4; ++l) {
+                        const int o = jd + JC_R1 + 5 * (l - 1);
+                        A[l] = AinRo * REC(o) + AinRx * REC(o + 1) + AinRy * REC(o + 2) + AinRz * REC(o + 3) + AinRe * REC(o + 4);
+                    }
+                    A[4] = AinRo * REC(jd + JC_VP) * REC(jd + JC_GET1) + AinRx * REC(jd + JC_R4) + AinRy * REC(jd + JC_R4 + 1) +
+                           AinRz * REC(jd + JC_R4 + 2) + AinRe * REC(jd + JC_R4 + 3);
+                    R tpc[NPC];
+                    for (int m = 0; m < NPC; ++m) tpc[m] = pc[sw_at(q, (side + d) * NPC + m, 6 * NPC)];
+                    precond_apply<R>(A, tpc);
+                    Dif = A[L];
+                }
+            }
             const R Din = L == 0 ? AinRo : L == 1 ? AinRx : L == 2 ? AinRy : L == 3 ? AinRz : AinRe;
             val = R(0.5) * (Dif + sgn * (RDSt * Din));
         } else {
@@ -1276,7 +1343,7 @@ __device__ inline void prefetch_l2_range(const void* p, size_t bytes, size_t t, 
 // chained: 1 = the next hyperplane's launch is released after this one's wait, 2 = at entry
 template <typename R, bool LOWER>
 __global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int first, int count, int lanes,
-                        int chained, int pf_first, int pf_count) {
+                        int chained, int pf_first, int pf_count, const R* __restrict__ pc) {
     if (chained == 2) asm volatile("griddepcontrol.launch_dependents;");
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (pf_count > 0) {
@@ -1293,7 +1360,7 @@ __global__ void k_sweep(const int* __restrict__ nbp, const R* __restrict__ rec, 
         }
         return;
     }
-    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, chained != 0, !(lanes & SWEEP_WPC), chained == 1);
+    sweep_item<R, LOWER>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, chained != 0, !(lanes & SWEEP_WPC), chained == 1, pc);
 }
 
 // Mixed path: one hyperplane per launch, one thread per position (sweep_pos_compact).
@@ -1349,7 +1416,8 @@ __device__ inline bool grid_barrier(SweepSync* sy, unsigned nblocks, unsigned li
 // spread over the whole grid, then a grid barrier; U runs the hyperplanes in reverse.
 template <typename R>
 __global__ void k_sweep_all(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N,
-                            const int* __restrict__ plane_off, int nplanes, int lanes, SweepSync* sy, unsigned limit) {
+                            const int* __restrict__ plane_off, int nplanes, int lanes, SweepSync* sy, unsigned limit,
+                            const R* __restrict__ pc) {
     const int stride = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     for (int h = 0; h < nplanes; ++h) {
@@ -1357,7 +1425,7 @@ __global__ void k_sweep_all(const int* __restrict__ nbp, const R* __restrict__ r
         for (int g = tid; g < items; g += stride) {
             int e, L;
             sweep_map(g, lanes, e, L);
-            if (e < n) sweep_item<R, true>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, false, !(lanes & SWEEP_WPC));
+            if (e < n) sweep_item<R, true>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, false, !(lanes & SWEEP_WPC), true, pc);
         }
         if (!grid_barrier(sy, gridDim.x, limit)) return;
     }
@@ -1366,7 +1434,7 @@ __global__ void k_sweep_all(const int* __restrict__ nbp, const R* __restrict__ r
         for (int g = tid; g < items; g += stride) {
             int e, L;
             sweep_map(g, lanes, e, L);
-            if (e < n) sweep_item<R, false>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, false, !(lanes & SWEEP_WPC));
+            if (e < n) sweep_item<R, false>(nbp, rec, dq, N, (long long)first + e, L, lanes & 3, false, !(lanes & SWEEP_WPC), true, pc);
         }
         if (h > 0 && !grid_barrier(sy, gridDim.x, limit)) return;
     }
@@ -1394,7 +1462,7 @@ __device__ inline bool flow_wait(const int* flag, long long q, int want, SweepSy
 
 template <typename R>
 __global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, int* flagL, int* flagU,
-                             int turb, SweepSync* sy, unsigned limit) {
+                             int turb, SweepSync* sy, unsigned limit, const R* __restrict__ pc) {
     const long long T = (long long)gridDim.x * blockDim.x;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long items = N * SWEEP_LANES;
@@ -1408,7 +1476,7 @@ __global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ 
             if (np >= 0) ok = flow_wait<R>(flagL, np, 7, sy, limit);
         }
         if (!ok) return;
-        sweep_item<R, true>(nbp, rec, dq, N, q, L, turb & 3);
+        sweep_item<R, true>(nbp, rec, dq, N, q, L, turb & 3, false, true, true, pc);
         __threadfence();
         atomicAdd(flagL + q, 1);
     }
@@ -1422,7 +1490,7 @@ __global__ void k_sweep_flow(const int* __restrict__ nbp, const R* __restrict__ 
             if (np >= 0) ok = flow_wait<R>(flagU, np, 7, sy, limit);
         }
         if (!ok) return;
-        sweep_item<R, false>(nbp, rec, dq, N, q, L, turb & 3);
+        sweep_item<R, false>(nbp, rec, dq, N, q, L, turb & 3, false, true, true, pc);
         __threadfence();
         atomicAdd(flagU + q, 1);
     }
@@ -1449,7 +1517,7 @@ __device__ inline bool tile_wait(const int* flag, SweepSync* sy, unsigned limit)
 
 template <typename R>
 __global__ void k_sweep_tiles(const int* __restrict__ nbp, const R* __restrict__ rec, R* dq, long long N, TileView tv,
-                              int lanes, int* flags, int* counter, SweepSync* sy, unsigned limit) {
+                              int lanes, int* flags, int* counter, SweepSync* sy, unsigned limit, const R* __restrict__ pc) {
     __shared__ int s_t, s_ok;
     const int nt = tv.ntiles;
     for (;;) {
@@ -1479,8 +1547,8 @@ __global__ void k_sweep_tiles(const int* __restrict__ nbp, const R* __restrict__
                 sweep_map(g, lanes, e, L);
                 if (e >= n) continue;
                 const long long q = tv.item[a + e];
-                if (lower) sweep_item<R, true>(nbp, rec, dq, N, q, L, lanes & 3, false, !(lanes & SWEEP_WPC));
-                else sweep_item<R, false>(nbp, rec, dq, N, q, L, lanes & 3, false, !(lanes & SWEEP_WPC));
+                if (lower) sweep_item<R, true>(nbp, rec, dq, N, q, L, lanes & 3, false, !(lanes & SWEEP_WPC), true, pc);
+                else sweep_item<R, false>(nbp, rec, dq, N, q, L, lanes & 3, false, !(lanes & SWEEP_WPC), true, pc);
             }
             __syncthreads();
         }
@@ -1594,6 +1662,28 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
         double AinRe = Dq(4);
         double pRo = v1;
         double roinv = 1.0 / pRo;
+        double rr = p.omega0 * slot(b, S_RAD)[c];
+        if (p.IF_Precondition) {
+            // preconditioned (TIME_Update_V.F90:580-607): conservative increments; the kinetic
+            // energy takes the new momenta with the old 1/rho, and T the old pressure with the
+            // new density
+            double pRx = V[1][c], pRy = V[2][c], pRz = V[3][c], pRe = V[4][c];
+            pRo = pRo + AinRo;
+            pRo = fabs(pRo);
+            pRx = pRx + AinRx; pRy = pRy + AinRy; pRz = pRz + AinRz;
+            pRe = pRe + AinRe;
+            pRe = fabs(pRe);
+            double DV = 0.5 * (pRx * pRx + pRy * pRy + pRz * pRz) * roinv;
+            double pPP = (pRe - DV) * (1.4 - 1.0);
+            if (pPP <= 0.0) {
+                pPP = fabs(pPP);
+                pRe = pPP / (1.4 - 1.0) + DV;
+            }
+            double pTT = p.RXM2 * PP[c] / pRo;
+            V[0][c] = pRo; V[1][c] = pRx; V[2][c] = pRy; V[3][c] = pRz; V[4][c] = pRe;
+            PP[c] = pPP;
+            T[c] = pTT;
+        } else {
         double pVx = V[1][c] * roinv, pVy = V[2][c] * roinv, pVz = V[3][c] * roinv;
         double AinX = (AinRx - pVx * AinRo) * roinv;
         double AinY = (AinRy - pVy * AinRo) * roinv;
@@ -1614,8 +1704,8 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
         V[2][c] = pRo * pVy;
         V[3][c] = pRo * pVz;
         double DV = 0.5 * (pVx * pVx + pVy * pVy + pVz * pVz);
-        double rr = p.omega0 * slot(b, S_RAD)[c];
         V[4][c] = pp / (1.4 - 1.0) + DV * pRo - 0.5 * sq(rr) * pRo;
+        }
         if (turb_upd) {   // TIME_Update_V.F90:709-816
             double VV = sq(V[1][c]) + sq(V[2][c]) + sq(V[3][c]);
             double PPP = (1.4 - 1.0) * V[4][c] - 0.5 * (1.4 - 1.0) * (VV / pRo - sq(rr) * pRo);

@@ -58,7 +58,7 @@ struct FluxLaunchers {
     // LU-SGS right-hand sides + neighbour Jacobian terms into the sweep-order arrays
     // (cell order over the cell tiles; qpos = sweep position of each tile slot)
     void (*prep)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const SweepView&, const CaseDev*);
-    void (*jac)(cudaStream_t, const DevBlock*, const SweepView&);     // neighbours' Jacobian terms (sweep order)
+    void (*jac)(cudaStream_t, const DevBlock*, const SweepView&, const CaseDev*);   // neighbours' Jacobian terms (sweep order)
     // lanes: components swept (bits 0-1: 0 mean flow, 1 all, 2 k-omega) | SWEEP_WPC thread mapping
     // (pf_first, pf_count: a later hyperplane prefetched into L2, count 0 = none; chained: 0 plain
     // launch, 1 programmatic dependent launch released after the wait, 2 released at entry (mixed

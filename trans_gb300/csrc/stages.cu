@@ -549,7 +549,7 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             {
                 KScope t(c, K_PREP);
                 c->fl->prep(s, c->d_blk, c->d_cell, nct, c->d_qpos, c->sv, c->d_cdev);
-                c->fl->jac(s, c->d_blk, c->sv);
+                c->fl->jac(s, c->d_blk, c->sv, c->d_cdev);
             }
             c->launches += 2;
             {

@@ -27,6 +27,7 @@ struct SweepView {
     void* rec;                  // n x NREC records
     void* dq;                   // n x DQ_STRIDE DeltaQ
     long long n;
+    void* pc;                   // n x 6 x NPC PrecondDW coefficients of the neighbours (FP64 path, IF_Precondition = 1), else null
 };
 
 // Tiled wavefront of the sweeps: the interior of every block cut into tiles of TIxTJxTK

@@ -259,6 +259,11 @@ int rebuild(Ctx* c) {
         CK(cudaMalloc(&c->d_dqs, (size_t)DQ_STRIDE * Np * c->fl->elem));
         CK(cudaMalloc(&c->d_flags, (size_t)2 * Np * sizeof(int)));
         c->sv.cells = c->d_sweep; c->sv.nbp = c->d_nbp; c->sv.rec = c->d_rec; c->sv.dq = c->d_dqs; c->sv.n = N;
+        c->sv.pc = nullptr;
+        if (c->cases[0]->p.IF_Precondition == 1) {      // the neighbours' PrecondDW coefficients (FP64 path)
+            CK(cudaMalloc(&c->d_pc, (size_t)6 * NPC * Np * sizeof(double)));
+            c->sv.pc = c->d_pc;
+        }
     }
     {   // staging buffer for the largest Fortran field (DQdxyz: 18 components, lower bound -1)
         size_t mx = 0;
