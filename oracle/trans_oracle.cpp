@@ -40,9 +40,9 @@ namespace {
 inline double p15(double x) { return x * std::sqrt(x); }
 inline double sgn1(double b) { return b >= 0.0 ? 1.0 : -1.0; }
 inline double sq(double x) { return x * x; }
-// x**2.0 with a real exponent: Fortran's power with an even integral exponent, whose base may be
-// negative; the pow of tmath on |x|, as every real-exponent power of this restatement
-inline double pow2r(double x) { return otm::pow_(std::fabs(x), 2.0); }
+// x**2.0 with a real exponent: the product x*x, the correctly rounded value of the power (a
+// compiler may emit it for the whole-number exponent without changing the result)
+inline double pow2r(double x) { return x * x; }
 
 // Low-Mach preconditioning (IF_Precondition = 1), Common/UTIL_Precond_Funcs.F90.
 // getPrecondPara (:6-32): the preconditioning parameter ubetac2 of one state.
@@ -1630,9 +1630,8 @@ double fsst(const trans_params& p, double Den, double vK, double vOmega, double 
 }
 
 // IDDES functions of Time/Hybrid_function.F90:43-105 (Kind_SubHY = 5).  The constants
-// akapa_iddes, Cw, Ct, Cl are Module_Global.F90:126; their squares are constant expressions
-// (0.41**2. folds to 0.41*0.41); the real exponents of variables (aDst**2., (Cl**2.*rdl)**10.)
-// are evaluated by the pow of tmath, as every real-exponent power of this restatement.
+// akapa_iddes, Cw, Ct, Cl are Module_Global.F90:126; a square (0.41**2., aDst**2.) is the
+// product, the correctly rounded power; (Cl**2.*rdl)**10. is the pow of tmath.
 // g: the nine velocity gradients dudx, dudy, dudz, dvdx, ..., dwdz.
 constexpr double KAPPA_IDDES2 = 0.41 * 0.41, CT_IDDES2 = 1.87 * 1.87, CL_IDDES2 = 5.00 * 5.00, CW_IDDES = 0.15;
 
@@ -1647,7 +1646,7 @@ double fd_function(const trans_params& p, double Den1, double RmiuT1, double aDs
     double alpha1 = 0.25 - aDst1 / aLmax1;
     double fb = std::min(2. * otm::exp_(-9.0 * alpha1 * alpha1), 1.);
     double Sij = sij_norm(g);
-    double rdt = (RmiuT1 / Den1) / (KAPPA_IDDES2 * otm::pow_(aDst1, 2.) * Sij * p.Ref);
+    double rdt = (RmiuT1 / Den1) / (KAPPA_IDDES2 * (aDst1 * aDst1) * Sij * p.Ref);
     double fdt = 1. - otm::tanh_((8. * rdt) * (8. * rdt) * (8. * rdt));
     return std::max((1. - fdt), fb);
 }
@@ -1657,9 +1656,9 @@ double fe_function(const trans_params& p, double Den2, double RmiuT2, double Rmi
     double alpha2 = 0.25 - aDst2 / aLmax2;
     double fe1 = alpha2 >= 0. ? 2. * otm::exp_(-11.09 * alpha2 * alpha2) : 2. * otm::exp_(-9. * alpha2 * alpha2);
     double Sij = sij_norm(g);
-    double rdt = (RmiuT2 / Den2) / (KAPPA_IDDES2 * otm::pow_(aDst2, 2.) * Sij * p.Ref);
+    double rdt = (RmiuT2 / Den2) / (KAPPA_IDDES2 * (aDst2 * aDst2) * Sij * p.Ref);
     double ft = otm::tanh_((CT_IDDES2 * rdt) * (CT_IDDES2 * rdt) * (CT_IDDES2 * rdt));
-    double rdl = (RmiuL2 / Den2) / (KAPPA_IDDES2 * otm::pow_(aDst2, 2.) * Sij * p.Ref);
+    double rdl = (RmiuL2 / Den2) / (KAPPA_IDDES2 * (aDst2 * aDst2) * Sij * p.Ref);
     double fl = otm::tanh_(otm::pow_(CL_IDDES2 * rdl, 10.));
     double fe2 = 1. - std::max(ft, fl);
     return fe2 * std::max((fe1 - 1.), 0.);

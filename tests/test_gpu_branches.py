@@ -181,13 +181,20 @@ def test_symmetry_plane_bc_state_stage(gpu_lib):
                     assert bit_equal_fraction(a, b, top) == 1.0, (ki, name)
                     bad = _ghost_mismatches(a, b, dims)
                     assert not bad, (ki, name, bad[:12])
-                # the mirrored normal velocity: the layer-1 ghost's normal momentum is the
-                # negative of the first interior cell's (the top plane is flat to the grid
-                # generator's rounding, so the mirror holds to a small part of the momentum)
+                # the mirror: the layer-1 ghost's momentum is the first interior cell's reflected
+                # about the unit normal of the face BC_Symm reads, i + IJKAdd with IJKAdd = -1 on a
+                # max face (Input/PLOT3DReadInit.F90:235): the first interior face, which follows
+                # the bump below the flat top (BC/BC_Symm.F90:46-49, 59-63)
                 V = g.get_field(0, "V")
-                scale = np.max(np.abs(V[1][G + 1:G + ni, G + nj - 1, G + 1:G + nk]))
-                err = np.max(np.abs(V[2][G + 1:G + ni, G + nj, G + 1:G + nk] + V[2][G + 1:G + ni, G + nj - 1, G + 1:G + nk]))
-                assert err <= 1e-6 * scale, (ki, err, scale)
+                gb = geo[c.blocks[0].id]
+                n = np.stack([gb["SD"][1, q, G + 1:G + ni, G + nj - 1, G + 1:G + nk] for q in range(3)])
+                n = n / gb["GRAD"][1, G + 1:G + ni, G + nj - 1, G + 1:G + nk]
+                rho = V[0][G + 1:G + ni, G + nj - 1, G + 1:G + nk]
+                m_in = np.stack([V[q][G + 1:G + ni, G + nj - 1, G + 1:G + nk] for q in (1, 2, 3)])
+                vc = np.sum(n * m_in / rho, axis=0)
+                want = m_in - 2.0 * n * vc * rho
+                got = np.stack([V[q][G + 1:G + ni, G + nj, G + 1:G + nk] for q in (1, 2, 3)])
+                assert np.allclose(got, want, rtol=1e-12, atol=1e-14), (ki, np.max(np.abs(got - want)))
             if stage == "BC_GRAD":
                 a, b = g.get_field(0, "DQDXYZ"), o.get_field(0, "DQDXYZ")
                 assert bit_equal_fraction(a, b, face_ghosts(dims, 1)) == 1.0, ki

@@ -176,11 +176,9 @@ template <> __device__ inline float ttanh<float>(float x) { return tanhf(x); }
 template <typename R> __device__ inline R texp(R x);
 template <> __device__ inline double texp<double>(double x) { return tmx::exp_(x); }
 template <> __device__ inline float texp<float>(float x) { return expf(x); }
-// x**2. and x**10. of a Fortran real exponent: the pow of tmath in FP64 (as the oracle),
-// products in FP32
-template <typename R> __device__ inline R pow2_real(R x);
-template <> __device__ inline double pow2_real<double>(double x) { return tmx::pow_(x, 2.0); }
-template <> __device__ inline float pow2_real<float>(float x) { return x * x; }
+// x**2. of a Fortran real exponent: the product, the correctly rounded power; x**10.: the pow
+// of tmath in FP64 (as the oracle), products in FP32
+template <typename R> __device__ inline R pow2_real(R x) { return x * x; }
 template <typename R> __device__ inline R pow10_real(R x);
 template <> __device__ inline double pow10_real<double>(double x) { return tmx::pow_(x, 10.0); }
 template <> __device__ inline float pow10_real<float>(float x) {
@@ -202,11 +200,9 @@ template <typename R> __device__ inline R cube_pow(R x);
 template <> __device__ inline double cube_pow<double>(double x) { return tmx::pow_(x, 3.0); }
 template <> __device__ inline float cube_pow<float>(float x) { return x * x * x; }
 
-// x**2.0 of a Fortran real exponent whose base may be negative (an even integral power): the pow
-// of tmath on |x| in FP64 (as the oracle), the product in FP32
-template <typename R> __device__ inline R pow2r(R x);
-template <> __device__ inline double pow2r<double>(double x) { return tmx::pow_(fabs(x), 2.0); }
-template <> __device__ inline float pow2r<float>(float x) { return x * x; }
+// x**2.0 of a Fortran real exponent (a base of either sign): the product, the correctly
+// rounded power
+template <typename R> __device__ inline R pow2r(R x) { return x * x; }
 
 // Low-Mach preconditioning (IF_Precondition = 1), Common/UTIL_Precond_Funcs.F90.
 // getPrecondPara (:6-32): the preconditioning parameter ubetac2 of one state
