@@ -47,7 +47,7 @@ def load():
         lib.oracle_ausmpw.argtypes = [C.POINTER(abi.TransParams), dp, dp]
         lib.oracle_roe.argtypes = [C.POINTER(abi.TransParams), dp, dp]
         lib.oracle_mdcd.argtypes = [dp, C.c_double, dp]
-        for f in ("exp", "expm1", "tanh", "log"):
+        for f in ("exp", "expm1", "tanh", "log", "atan"):
             fn = getattr(lib, "oracle_tm_" + f)
             fn.argtypes = [C.c_double]
             fn.restype = C.c_double

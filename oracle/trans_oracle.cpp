@@ -97,7 +97,7 @@ struct Blk {
     std::vector<int> mw[6];     // MARKWALL arrays, Fortran (n1,n2) column-major
     int mwn1[6];
     Arr V, PP, T, Rmiu, Wt0, Wt1, Wt2, SD, Grad, Vol, Alagm, Dst, ALeng, ASeng, Xc, Yc, Zc, rad, thtc;
-    Arr D, Rds, Dtm, DQ, shock, F, VL, VR, rccl, rccr, FunDES, Fsch;
+    Arr D, Rds, Dtm, DQ, shock, F, VL, VR, rccl, rccr, FunDES, Fsch, Fr1;
     trans_norms nrm;
     int markwall(int face, int a, int b) const {
         if (mw[face].empty()) return 0;
@@ -1491,6 +1491,87 @@ void turbtwo_convect_upwind(Ctx& c, Blk& b) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Space/RC_Correction.F90:19-124 (Kind_RotMod = 1): the rotation/curvature factor f_r1 of the
+// SST production, as the reference's build evaluates it (-O2 without -auto: the local arrays
+// St2 and Wij are static, zero at load, and the entries the routine never writes -- St2(3,3)
+// and the diagonal of Wij -- stay 0).  omega(M) (:107; M is never set, the loop variable is
+// MM) multiplies omega, which is 0 in every case this restatement accepts; omega(1) stands in.
+// VL(d,v) is what SPACEINTERP_GetSurfCenterVars wrote in this iteration, 0 where it writes
+// nothing (the reference zeroes VL at allocation, Input/Read_BlockDimensions.F90:418, and no
+// routine writes those entries).  Kind_RotMod = 2 computes f_r2 (:126-171), which no routine
+// of the path reads, so it leaves every result unchanged and is not evaluated.
+// ---------------------------------------------------------------------------------------
+void rc_correction(Ctx& c, Blk& b) {
+    const trans_params& p = c.p;
+    const double cr1 = 1.0, cr2 = 2.0, cr3 = 1.0;
+    for (int K = 1; K <= b.NK1; ++K)
+    for (int J = 1; J <= b.NJ1; ++J)
+    for (int I = 1; I <= b.NI1; ++I) {
+        double St2[4][4] = {}, Wij[4][4] = {};          // 1-based, as the reference indexes them
+        double DuDx = b.DQ(1, I, J, K), DuDy = b.DQ(2, I, J, K), DuDz = b.DQ(3, I, J, K);
+        double DvDx = b.DQ(4, I, J, K), DvDy = b.DQ(5, I, J, K), DvDz = b.DQ(6, I, J, K);
+        double DwDx = b.DQ(7, I, J, K), DwDy = b.DQ(8, I, J, K);
+        St2[1][1] = DuDx;
+        St2[1][2] = 0.5 * (DuDy + DvDx);
+        St2[1][3] = 0.5 * (DuDz + DwDx);
+        St2[2][1] = St2[1][2];
+        St2[2][2] = DvDy;
+        St2[2][3] = 0.5 * (DvDz + DwDy);
+        St2[3][1] = St2[1][3];
+        St2[3][2] = St2[2][3];
+        Wij[1][2] = 0.5 * (DuDy - DvDx);
+        Wij[1][3] = 0.5 * (DuDz - DwDx);
+        Wij[2][3] = 0.5 * (DvDz - DwDy) - p.omega[0];
+        Wij[2][1] = -Wij[1][2];
+        Wij[3][1] = -Wij[1][3];
+        Wij[3][2] = -Wij[2][3];
+        double SSum = 0.0, WSum = 0.0;
+        for (int JJ = 1; JJ <= 3; ++JJ)
+            for (int II = 1; II <= 3; ++II) {
+                SSum = SSum + St2[II][JJ] * St2[II][JJ];
+                WSum = WSum + Wij[II][JJ] * Wij[II][JJ];
+            }
+        SSum = SSum * 2.0;
+        WSum = WSum * 2.0;
+        double r_bar = 0.0;
+        for (int JJ = 1; JJ <= 3; ++JJ)
+            for (int II = 1; II <= 3; ++II) {
+                int LL1 = (II - 1) * 3 + JJ, LL2 = (JJ - 1) * 3 + II;
+                double Sij = b.DQ(LL1, I, J, K) + b.DQ(LL2, I, J, K);
+                auto face = [&](int i, int j, int k) {
+                    double vol1 = b.Vol(i, j, k) / (b.Vol(i, j, k) + b.Vol(I, J, K));
+                    return vol1 * (b.DQ(LL1, i, j, k) + b.DQ(LL2, i, j, k)) + (1.0 - vol1) * Sij;
+                };
+                double Sijf1 = face(I - 1, J, K), Sijf2 = face(I + 1, J, K);
+                double Sijf3 = face(I, J - 1, K), Sijf4 = face(I, J + 1, K);
+                double Sijf5 = face(I, J, K - 1), Sijf6 = face(I, J, K + 1);
+                double volinv = 1.0 / b.Vol(I, J, K);
+                auto U = [&](int v, int i, int j, int k) {     // the VL*SD sum of RC_Correction.F90:95-100
+                    return b.VL(1, v, i, j, k) * b.SD(1, v, i, j, k) + b.VL(2, v, i, j, k) * b.SD(2, v, i, j, k) +
+                           b.VL(3, v, i, j, k) * b.SD(3, v, i, j, k);
+                };
+                double DsijDt = U(1, I + 1, J, K) * Sijf2 - U(1, I, J, K) * Sijf1 + U(2, I, J + 1, K) * Sijf4 -
+                                U(2, I, J, K) * Sijf3 + U(3, I, J, K + 1) * Sijf6 - U(3, I, J, K) * Sijf5;
+                double DsDt = DsijDt * 0.5 * volinv;
+                double DsDt2 = 0.0;
+                for (int MM = 1; MM <= 1; ++MM)
+                    for (int NN = 1; NN <= 3; ++NN) {
+                        double epsIMN = 0.5 * (II - MM) * (MM - NN) * (NN - II);
+                        double epsJMN = 0.5 * (JJ - MM) * (MM - NN) * (NN - JJ);
+                        DsDt2 = DsDt2 + (epsIMN * St2[JJ][NN] + epsJMN * St2[II][NN]) * p.omega[0];
+                    }
+                DsDt = DsDt + DsDt2;
+                for (int KK = 1; KK <= 3; ++KK) r_bar = r_bar + Wij[II][KK] * St2[JJ][KK] * DsDt;
+            }
+        double Dsum = std::max(SSum, 0.09 * sq(b.V(7, I, J, K) / b.V(1, I, J, K)));
+        double r_star = std::sqrt(SSum / WSum);
+        r_bar = 2.0 * r_bar / (std::sqrt(WSum) * p15(Dsum));
+        double f_rot = (1 + cr1) * 2.0 * r_star / (1.0 + r_star) * (1 - cr3 * otm::atan_(cr2 * r_bar)) - cr1;
+        b.Fr1(I, J, K) = std::max(std::min(f_rot, 1.25), 0.0);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // Time/TIME_LUSGS.F90:60-768 (non-preconditioned)
 // ---------------------------------------------------------------------------------------
 void lusgs_adq(double pGam, double pVx, double pVy, double pVz, double aSDx, double aSDy, double aSDz, double pPP,
@@ -1807,7 +1888,7 @@ void turbtwo_lusgs_sst(Ctx& c, Blk& b) {
         double AA = std::sqrt(1.4 * b.PP(I, J, K) / ARo);
         double Mt = std::sqrt(ARTk / ARo) / AA;
         double Alf1 = 1.0, Alf2 = 0.4, Alf3 = 0.2;
-        double f_r1 = 1.0;
+        double f_r1 = b.Fr1(I, J, K);       // 1 unless RCCorrection set it (Kind_RotMod = 1)
         double Source, SourceP, SourceN1, SourceNc, CnegTk, CnegTO;
         double fixsrc = (p.If_fix_Transition && b.Xc(I, J, K) < p.Trans_location) ? 1.0 : 0.0;
         if (p.IF_Comppress == 0) {
@@ -2174,10 +2255,12 @@ int run_stage(Ctx& c, int stage) {
             bc_boundarys(c, 0);
             break;
         case TRANS_STAGE_RESIDUAL:
-            // per block: the three loops of main.F90:92-133 touch only the block's own arrays
+            // per block: RCCorrection (main.F90:89) and the three loops of main.F90:92-133 touch
+            // only the block's own arrays
 #pragma omp parallel for schedule(dynamic)
             for (size_t n = 0; n < c.B.size(); ++n) {
                 Blk& b = c.B[n];
+                if (c.p.Kind_RotMod == 1) rc_correction(c, b);
                 std::fill(b.D.v.begin(), b.D.v.end(), 0.0);
                 if (c.p.IF_Euler == 0) diffusion_centered(c, b);
                 if (c.IF_turb) turbtwo_diffusion(c, b);
@@ -2258,7 +2341,8 @@ extern "C" {
 
 int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks, void** out) {
     if (!p || !blocks || nblocks <= 0 || !out) return TRANS_E_ARG;
-    if ((p->IF_Precondition != 0 && p->IF_Precondition != 1) || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2))
+    if ((p->IF_Precondition != 0 && p->IF_Precondition != 1) || p->Kind_RotMod < 0 || p->Kind_RotMod > 2 ||
+        (p->Kind_Model != 1 && p->Kind_Model != 2))
         return TRANS_E_ARG;
     if (p->IF_Precondition == 1 && p->IF_RK != 0) return TRANS_E_ARG;     // preconditioning with LU-SGS only
     if (p->Kind_Spatial < 1 || p->Kind_Spatial > 4) return TRANS_E_ARG;
@@ -2296,6 +2380,8 @@ int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks,
         b.VL.alloc(3, 8, ni, nj, nk); b.VR.alloc(3, 8, ni, nj, nk);
         b.rccl.alloc(3, 1, ni, nj, nk); b.rccr.alloc(3, 1, ni, nj, nk); b.FunDES.alloc(1, 1, ni, nj, nk);
         b.Fsch.alloc(1, 1, ni, nj, nk);
+        b.Fr1.alloc(1, 1, ni, nj, nk);
+        std::fill(b.Fr1.v.begin(), b.Fr1.v.end(), 1.0);       // f_r1 = 1 (Input/Read_BlockDimensions.F90:426)
         std::memset(&b.nrm, 0, sizeof(b.nrm));
     }
     *out = c;
@@ -2504,4 +2590,5 @@ double oracle_tm_expm1(double x) { return otm::expm1_(x); }
 double oracle_tm_tanh(double x) { return otm::tanh_(x); }
 double oracle_tm_log(double x) { return otm::log_(x); }
 double oracle_tm_pow(double x, double y) { return otm::pow_(x, y); }
+double oracle_tm_atan(double x) { return otm::atan_(x); }
 }

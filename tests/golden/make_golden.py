@@ -34,6 +34,7 @@ CASES = {
     "cascade_small_mdcd_roerot": ("cascade", dict(Kind_Spatial=3, Kind_Roe=2)),
     "channel_small_mdcd_ausmpw_iddes": ("channel", dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3, Kind_SubHY=5)),
     "channel_small_m03_muscl_roe_precond": ("channel", dict(Kind_Spatial=2, Kind_Roe=1, IF_Precondition=1, XM=0.3)),
+    "cascade_small_mdcd_ausmpw_rc": ("cascade", dict(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=1)),
 }
 
 

@@ -87,7 +87,7 @@ def _params(**kw):
 
 
 @pytest.mark.parametrize("bad", [dict(IF_RK=2), dict(IF_Precondition=2), dict(IF_Precondition=1, precision=1),
-                                 dict(IF_Precondition=1, IF_RK=1), dict(Kind_RotMod=1), dict(Kind_Model=3),
+                                 dict(IF_Precondition=1, IF_RK=1), dict(Kind_RotMod=3), dict(Kind_Model=3),
                                  dict(Kind_Spatial=5), dict(Kind_Spatial=0), dict(Kind_Roe=4), dict(Kind_Hybrid=1),
                                  dict(IF_Euler=1),
                                  dict(precision=7)])

@@ -255,3 +255,38 @@ def test_preconditioning_fp64_path_only(gpu_lib):
     c.params.precision = abi.TRANS_MIXED
     with pytest.raises(SolverError, match=str(abi.TRANS_E_ARG)):
         Solver(c, conns, geo, st)
+
+
+RC = dict(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=1)
+
+
+def test_rc_correction_channel(gpu_lib):
+    """RC correction (Kind_RotMod = 1, Space/RC_Correction.F90:19-124): the rotation/curvature
+    factor f_r1 of the SST production (Time/TURBTWO_TIME_LUSGS_SST.F90:286,325), 20 iterations
+    bit-identical, with the compressibility correction as well."""
+    c, conns, geo, st = small_channel(**RC)
+    _run_bitwise(c, conns, geo, st, 20)
+    c, conns, geo, st = small_channel(IF_Comppress=1, **RC)
+    _run_bitwise(c, conns, geo, st, 10)
+
+
+def test_rc_correction_cascade(gpu_lib):
+    """Five blocks: the face averages and gradients RC reads across block interfaces."""
+    from helpers import small_cascade
+    c, conns, geo, st = small_cascade(**RC)
+    _run_bitwise(c, conns, geo, st, 8)
+
+
+def test_rc_mode_2_changes_nothing(gpu_lib):
+    """Kind_RotMod = 2 computes f_r2 (RC_Correction.F90:126-171), which no routine of the path
+    reads: the state is bit-identical to Kind_RotMod = 0."""
+    from trans_gb300.solver import Solver
+    out = []
+    for rot in (0, 2):
+        c, conns, geo, st = small_channel(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=rot)
+        s = Solver(c, conns, geo, st)
+        for ki in range(1, 6):
+            s.iterate(ki)
+        out.append(s.get_field(0, "V"))
+        s.close()
+    assert bit_equal_fraction(out[0], out[1], interior(c.blocks[0].dims)) == 1.0

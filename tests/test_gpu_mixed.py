@@ -40,10 +40,11 @@ def _run(case, precision, n):
                                          (small_channel, dict(Kind_Spatial=1, Kind_Roe=1)),
                                          (small_cascade, dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05)),
                                          (small_cascade, dict(Kind_Spatial=3, Kind_Roe=3, Kind_Model=2)),
-                                         (small_channel, dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3, Kind_SubHY=5))],
+                                         (small_channel, dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3, Kind_SubHY=5)),
+                                         (small_channel, dict(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=1))],
                          ids=["channel_mdcd_ausmpw", "channel_muscl_roe", "cascade_mdcd_ausmpw", "channel_rk3_mdcd_ausmpw",
                               "channel_muscl2_roe", "cascade_mdcdhyb_ausmpw", "cascade_mdcd_ausmpw_wd2006",
-                              "channel_mdcd_ausmpw_iddes"])
+                              "channel_mdcd_ausmpw_iddes", "channel_mdcd_ausmpw_rc"])
 def test_mixed_tracks_fp64(gpu_lib, make, scheme):
     case = make(**scheme)
     h64, f64 = _run(case, "fp64", 20)

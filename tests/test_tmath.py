@@ -1,4 +1,4 @@
-"""Accuracy of the exp/expm1/tanh/log/pow restatements shared (as a method) by the oracle and
+"""Accuracy of the exp/expm1/tanh/log/pow/atan restatements shared (as a method) by the oracle and
 the FP64 GPU path, against the platform libm, in units in the last place."""
 import math
 
@@ -28,6 +28,9 @@ def lib():
     ("tanh", math.tanh, -1e-3, 1e-3, 3),
     ("log", math.log, 1e-300, 1e300, 3),
     ("log", math.log, 0.5, 2.0, 3),
+    ("atan", math.atan, -60.0, 60.0, 3),
+    ("atan", math.atan, -1.0, 1.0, 3),
+    ("atan", math.atan, 1e-12, 1e12, 3),
 ])
 def test_accuracy(lib, fn, ref, lo, hi, tol):
     rng = np.random.default_rng(1)
@@ -55,3 +58,6 @@ def test_special_values(lib):
     assert lib.oracle_tm_tanh(40.0) == 1.0 and lib.oracle_tm_tanh(-40.0) == -1.0
     assert lib.oracle_tm_log(1.0) == 0.0
     assert math.isnan(lib.oracle_tm_tanh(float("nan")))
+    assert lib.oracle_tm_atan(0.0) == 0.0 and math.copysign(1, lib.oracle_tm_atan(-0.0)) < 0
+    assert lib.oracle_tm_atan(float("inf")) == math.pi / 2 and lib.oracle_tm_atan(-float("inf")) == -math.pi / 2
+    assert abs(lib.oracle_tm_atan(1.0) - math.pi / 4) <= math.ulp(math.pi / 4)

@@ -117,7 +117,7 @@ struct ParamsT {          // module globals the kernels read (trans_params + der
     TG_PARAM_REALS(TG_DECL)
 #undef TG_DECL
     int Kind_Spatial, Kind_Roe, Kind_Hybrid, Kind_SubHY, Kind_Dual, IF_Local_Main, IF_Local_Sub;
-    int IF_Comppress, If_fix_Transition, Kind_Model, IF_Precondition;
+    int IF_Comppress, If_fix_Transition, Kind_Model, IF_Precondition, Kind_RotMod;
 };
 using Params = ParamsT<double>;
 
@@ -130,7 +130,7 @@ inline ParamsT<R> params_as(const Params& p) {
     q.Kind_Spatial = p.Kind_Spatial; q.Kind_Roe = p.Kind_Roe; q.Kind_Hybrid = p.Kind_Hybrid;
     q.Kind_SubHY = p.Kind_SubHY; q.Kind_Dual = p.Kind_Dual; q.IF_Local_Main = p.IF_Local_Main;
     q.IF_Local_Sub = p.IF_Local_Sub; q.IF_Comppress = p.IF_Comppress; q.If_fix_Transition = p.If_fix_Transition;
-    q.Kind_Model = p.Kind_Model; q.IF_Precondition = p.IF_Precondition;
+    q.Kind_Model = p.Kind_Model; q.IF_Precondition = p.IF_Precondition; q.Kind_RotMod = p.Kind_RotMod;
     return q;
 }
 
@@ -172,6 +172,10 @@ template <typename R> __device__ inline R ttanh(R x);
 template <> __device__ inline double ttanh<double>(double x) { return tmx::tanh_(x); }
 template <> __device__ inline float ttanh<float>(float x) { return tanhf(x); }
 
+// atan: the bit-reproducible FP64 restatement, or the CUDA single-precision function
+template <typename R> __device__ inline R tatan(R x);
+template <> __device__ inline double tatan<double>(double x) { return tmx::atan_(x); }
+template <> __device__ inline float tatan<float>(float x) { return atanf(x); }
 // exp: the bit-reproducible FP64 restatement, or the CUDA single-precision function
 template <typename R> __device__ inline R texp(R x);
 template <> __device__ inline double texp<double>(double x) { return tmx::exp_(x); }

@@ -46,7 +46,7 @@ Params make_params(const trans_params& p) {
     d.Kind_Spatial = p.Kind_Spatial; d.Kind_Roe = p.Kind_Roe; d.Kind_Hybrid = p.Kind_Hybrid;
     d.Kind_SubHY = p.Kind_SubHY; d.Kind_Dual = p.Kind_Dual; d.IF_Local_Main = p.IF_Local_Main;
     d.IF_Local_Sub = p.IF_Local_Sub; d.IF_Comppress = p.IF_Comppress; d.If_fix_Transition = p.If_fix_Transition;
-    d.Kind_Model = p.Kind_Model; d.IF_Precondition = p.IF_Precondition;
+    d.Kind_Model = p.Kind_Model; d.IF_Precondition = p.IF_Precondition; d.Kind_RotMod = p.Kind_RotMod;
     return d;
 }
 
@@ -54,8 +54,9 @@ Params make_params(const trans_params& p) {
 
 // options outside the configurations of this hot path are rejected, never approximated
 bool params_supported(const trans_params* p) {
-    if ((p->IF_Precondition != 0 && p->IF_Precondition != 1) || p->Kind_RotMod != 0 || (p->Kind_Model != 1 && p->Kind_Model != 2) ||
-        p->IF_Euler != 0)
+    // RC correction (Kind_RotMod 1; 2 computes a factor nothing reads) in a frame at rest
+    if ((p->IF_Precondition != 0 && p->IF_Precondition != 1) || p->Kind_RotMod < 0 || p->Kind_RotMod > 2 ||
+        (p->Kind_Model != 1 && p->Kind_Model != 2) || p->IF_Euler != 0)
         return false;
     // low-Mach preconditioning: LU-SGS marching, FP64 path
     if (p->IF_Precondition == 1 && (p->IF_RK != 0 || p->precision != TRANS_FP64)) return false;

@@ -841,6 +841,85 @@ __global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restr
 // reads of the cell's slots); the results go to the cell's sweep position q (qpos) together
 // with the neighbours' Jacobian terms and spectral radii (k_lusgs_jac).
 // ---------------------------------------------------------------------------------------
+// Space/RC_Correction.F90:19-124 (Kind_RotMod = 1): the rotation/curvature factor f_r1 of the
+// SST production of one interior cell (I,J,K), slot index c, evaluated as the reference's build
+// evaluates it: the static local arrays' entries it never writes (St2(3,3), the diagonal of
+// Wij) are 0; omega(M) multiplies omega = 0; VL(d,v) is the face average of
+// SPACEINTERP_GetSurfCenterVars where that routine writes it and 0 elsewhere.  RCCorrection
+// runs after BC_Boundarys(0) (main.F90:89); its inputs do not change until the update, so the
+// LU-SGS preparation evaluates it.
+template <typename R>
+__device__ inline R rc_fr1(const ParamsT<R>& p, const DevBlock& b, int I, int J, int K, int c) {
+    const int st[3] = {1, b.PI, b.PI * b.PJ};
+    auto DQ = [&](int L, int cc) { return rs<R>(b, S_DQ + L - 1)[cc]; };         // DqDxyz(L), L 1-based
+    R St2[4][4], Wij[4][4];
+    for (int a = 0; a < 4; ++a)
+        for (int e = 0; e < 4; ++e) { St2[a][e] = R(0.0); Wij[a][e] = R(0.0); }
+    const R DuDx = DQ(1, c), DuDy = DQ(2, c), DuDz = DQ(3, c), DvDx = DQ(4, c), DvDy = DQ(5, c), DvDz = DQ(6, c);
+    const R DwDx = DQ(7, c), DwDy = DQ(8, c);
+    const R h = R(0.5), om = R(p.omega0);
+    St2[1][1] = DuDx; St2[1][2] = h * (DuDy + DvDx); St2[1][3] = h * (DuDz + DwDx);
+    St2[2][1] = St2[1][2]; St2[2][2] = DvDy; St2[2][3] = h * (DvDz + DwDy);
+    St2[3][1] = St2[1][3]; St2[3][2] = St2[2][3];
+    Wij[1][2] = h * (DuDy - DvDx); Wij[1][3] = h * (DuDz - DwDx); Wij[2][3] = h * (DvDz - DwDy) - om;
+    Wij[2][1] = -Wij[1][2]; Wij[3][1] = -Wij[1][3]; Wij[3][2] = -Wij[2][3];
+    R SSum = R(0.0), WSum = R(0.0);
+    for (int JJ = 1; JJ <= 3; ++JJ)
+        for (int II = 1; II <= 3; ++II) {
+            SSum = SSum + St2[II][JJ] * St2[II][JJ];
+            WSum = WSum + Wij[II][JJ] * Wij[II][JJ];
+        }
+    SSum = SSum * R(2.0);
+    WSum = WSum * R(2.0);
+    // VL(d,v) at face index (i,j,k) where SPACEINTERP writes it (d = 1: j, k interior; d = 2:
+    // i, k interior; d = 3: i, j interior), 0 elsewhere
+    auto VLf = [&](int d, int v, int i, int j, int k) -> R {
+        const bool in = d == 1 ? (j >= 1 && j <= b.NJ1 && k >= 1 && k <= b.NK1)
+                      : d == 2 ? (i >= 1 && i <= b.NI1 && k >= 1 && k <= b.NK1)
+                               : (i >= 1 && i <= b.NI1 && j >= 1 && j <= b.NJ1);
+        if (!in) return R(0.0);
+        return favg<R>(rs<R>(b, S_PRIM + v - 1), rs<R>(b, S_ALAGM + d - 1), rs<R>(b, S_AINV + d - 1), cidx(b, i, j, k), st[d - 1]);
+    };
+    auto U = [&](int v, int i, int j, int k) {      // the VL*SD sum of RC_Correction.F90:95-100
+        const int cf = cidx(b, i, j, k);
+        return VLf(1, v, i, j, k) * rs<R>(b, S_SD + v - 1)[cf] + VLf(2, v, i, j, k) * rs<R>(b, S_SD + 3 + v - 1)[cf] +
+               VLf(3, v, i, j, k) * rs<R>(b, S_SD + 6 + v - 1)[cf];
+    };
+    const R Ui1 = U(1, I + 1, J, K), Ui0 = U(1, I, J, K), Uj1 = U(2, I, J + 1, K), Uj0 = U(2, I, J, K);
+    const R Uk1 = U(3, I, J, K + 1), Uk0 = U(3, I, J, K);
+    const R* Vol = rs<R>(b, S_VOL);
+    R r_bar = R(0.0);
+    for (int JJ = 1; JJ <= 3; ++JJ)
+        for (int II = 1; II <= 3; ++II) {
+            const int LL1 = (II - 1) * 3 + JJ, LL2 = (JJ - 1) * 3 + II;
+            const R Sij = DQ(LL1, c) + DQ(LL2, c);
+            auto face = [&](int cn) {
+                R vol1 = Vol[cn] / (Vol[cn] + Vol[c]);
+                return vol1 * (DQ(LL1, cn) + DQ(LL2, cn)) + (R(1.0) - vol1) * Sij;
+            };
+            const R Sijf1 = face(c - st[0]), Sijf2 = face(c + st[0]), Sijf3 = face(c - st[1]), Sijf4 = face(c + st[1]);
+            const R Sijf5 = face(c - st[2]), Sijf6 = face(c + st[2]);
+            const R volinv = R(1.0) / Vol[c];
+            R DsijDt = Ui1 * Sijf2 - Ui0 * Sijf1 + Uj1 * Sijf4 - Uj0 * Sijf3 + Uk1 * Sijf6 - Uk0 * Sijf5;
+            R DsDt = DsijDt * R(0.5) * volinv;
+            R DsDt2 = R(0.0);
+            for (int MM = 1; MM <= 1; ++MM)
+                for (int NN = 1; NN <= 3; ++NN) {
+                    const R epsIMN = R(0.5 * (II - MM) * (MM - NN) * (NN - II));
+                    const R epsJMN = R(0.5 * (JJ - MM) * (MM - NN) * (NN - JJ));
+                    DsDt2 = DsDt2 + (epsIMN * St2[JJ][NN] + epsJMN * St2[II][NN]) * om;
+                }
+            DsDt = DsDt + DsDt2;
+            for (int KK = 1; KK <= 3; ++KK) r_bar = r_bar + Wij[II][KK] * St2[JJ][KK] * DsDt;
+        }
+    const R Dsum = dmax(SSum, R(0.09) * sq(rs<R>(b, S_V + 6)[c] / rs<R>(b, S_V)[c]));
+    const R r_star = sqrt(SSum / WSum);
+    r_bar = R(2.0) * r_bar / (sqrt(WSum) * p15(Dsum));
+    const R cr1 = R(1.0), cr2 = R(2.0), cr3 = R(1.0);
+    const R f_rot = (R(1) + cr1) * R(2.0) * r_star / (R(1.0) + r_star) * (R(1) - cr3 * tatan(cr2 * r_bar)) - cr1;
+    return dmax(dmin(f_rot, R(1.25)), R(0.0));
+}
+
 template <typename R>
 __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
                              R* __restrict__ rec, R* __restrict__ dq, const CaseDev* __restrict__ cdev) {
@@ -1010,11 +1089,17 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
     const R Alf1 = R(1.0), Alf2 = R(0.4), Alf3 = R(0.2);
     const R c23 = R(2.0 / 3.0);
     R SourceP, SourceN1, Source, CnegTk, CnegTO;
+    // the rotation/curvature factor of the production (TURBTWO_TIME_LUSGS_SST.F90:286,325,343,384;
+    // 1 unless Kind_RotMod = 1)
+    const bool rc = p.Kind_RotMod == 1;
+    const R f_r1 = rc ? rc_fr1<R>(p, b, I, J, K, c) : R(1.0);
     if (p.IF_Comppress == 0) {
         SourceP = tprod - c23 * dmin(Div, R(0.0)) * ARTk;
+        if (rc) SourceP = SourceP * f_r1;
         SourceN1 = -(c23 * dmax(Div, R(0.0))) - Bs * ARTO / ARo * Ref * Fdes;
     } else {
         SourceP = (R(1.) - (R(1.) - arg1) * Alf2 * Mt * Mt) * tprod - c23 * dmin(Div, R(0.0)) * ARTk;
+        if (rc) SourceP = SourceP * f_r1;
         SourceN1 = -(c23 * dmax(Div, R(0.0))) - (R(1.) + (R(1.) - arg1) * (Alf1 - Alf3) * Mt * Mt) * Bs * ARTO / ARo * Ref * Fdes;
     }
     Source = SourceP + SourceN1 * ARTk;
@@ -1033,9 +1118,11 @@ __global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __re
     R BetaAB = R(p.Beta1) * arg1 + R(p.Beta2) * (R(1.0) - arg1);
     if (p.IF_Comppress == 0) {
         SourceP = GamaAB * ARo * tprod - c23 * GamaAB * dmin(Div, R(0.0)) * ARTO;
+        if (rc) SourceP = SourceP * f_r1;
         SourceN1 = -(c23 * GamaAB * dmax(Div, R(0.0))) - BetaAB * ARTO / ARo * Ref;
     } else {
         SourceP = (GamaAB + (R(1.) - arg1) * Alf2 * Mt * Mt) * ARo * tprod - c23 * GamaAB * dmin(Div, R(0.0)) * ARTO;
+        if (rc) SourceP = SourceP * f_r1;
         SourceN1 = -(c23 * GamaAB * dmax(Div, R(0.0))) - (R(1.) - (R(1.) - arg1) * (Alf1 - Alf3) * Mt * Mt) * BetaAB * ARTO / ARo * Ref;
     }
     Source = SourceP + SourceN1 * ARTO;

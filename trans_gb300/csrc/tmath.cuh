@@ -8,6 +8,7 @@
 //   log:   x = m 2^e with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s), s = (m-1)/(m+1),
 //          atanh by its odd series to s^25 (|s| <= 0.1716); e ln2 with the split constant.
 //   pow:   exp(y log x) for x > 0.
+//   atan:  argument reduction to |t| <= tan(pi/8), then the Taylor series (atan_ below).
 // Their accuracy against the platform libm is checked in the test-suite (a few ulp).
 #pragma once
 #include <math.h>
@@ -110,5 +111,46 @@ TM_HD inline double log_(double x) {
 }
 
 TM_HD inline double pow_(double x, double y) { return exp_(y * log_(x)); }
+
+// atan: |x| > 1 by pi/2 - atan(1/|x|); t > tan(pi/8) by pi/4 + atan((t-1)/(t+1)); then the
+// Taylor series t - t^3/3 + t^5/5 - ... to t^43/43 (|t| <= tan(pi/8): truncation < 1e-18);
+// the sign of x restored
+TM_HD inline double atan_(double x) {
+    if (x != x) return x;
+    const double PI_2 = 1.5707963267948966, PI_4 = 0.7853981633974483;
+    const double TAN_PI_8 = 0.41421356237309503;
+    double ax = fabs(x);
+    bool inv = ax > 1.0;
+    double t = inv ? 1.0 / ax : ax;
+    bool red = t > TAN_PI_8;
+    if (red) t = (t - 1.0) / (t + 1.0);
+    double z = -(t * t);
+    double p = 1.0 / 43.0;
+    p = p * z + 1.0 / 41.0;
+    p = p * z + 1.0 / 39.0;
+    p = p * z + 1.0 / 37.0;
+    p = p * z + 1.0 / 35.0;
+    p = p * z + 1.0 / 33.0;
+    p = p * z + 1.0 / 31.0;
+    p = p * z + 1.0 / 29.0;
+    p = p * z + 1.0 / 27.0;
+    p = p * z + 1.0 / 25.0;
+    p = p * z + 1.0 / 23.0;
+    p = p * z + 1.0 / 21.0;
+    p = p * z + 1.0 / 19.0;
+    p = p * z + 1.0 / 17.0;
+    p = p * z + 1.0 / 15.0;
+    p = p * z + 1.0 / 13.0;
+    p = p * z + 1.0 / 11.0;
+    p = p * z + 1.0 / 9.0;
+    p = p * z + 1.0 / 7.0;
+    p = p * z + 1.0 / 5.0;
+    p = p * z + 1.0 / 3.0;
+    p = p * z + 1.0 / 1.0;
+    double r = t * p;
+    if (red) r = PI_4 + r;
+    if (inv) r = PI_2 - r;
+    return copysign(r, x);
+}
 
 }  // namespace tmx
