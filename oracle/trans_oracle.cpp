@@ -1332,12 +1332,11 @@ void ausmpw_common(const trans_params& p, double PLo, double PRo, double TLo, do
 // adds 0.5 |A| dQ along (sav1..3)/sav, times sav and the face blend Funscheme, to dr[0..4]
 void roe_rot_common(const trans_params& p, double PLo, double PRo, double TLo, double TRo, double ULo, double URo,
                     double VLo, double VRo, double WLo, double WRo, double sav1, double sav2, double sav3, double sav,
-                    double Funscheme, double* dr) {
+                    double rLo, double rRo, double Funscheme, double* dr) {
     double rcpcv = p.PPF;
     double DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
     const double ga = 1.4, ga1 = 0.4;
     double VAMLo = ULo * ULo + VLo * VLo + WLo * WLo, VAMRo = URo * URo + VRo * VRo + WRo * WRo;
-    const double rLo = 0.0, rRo = 0.0;          // rccl/rccr * omega, omega = 0
     double HLo = PLo * ga / (DENLo * ga1) + 0.5 * VAMLo - 0.5 * (rLo * rLo);
     double HRo = PRo * ga / (DENRo * ga1) + 0.5 * VAMRo - 0.5 * (rRo * rRo);
     double rrorl = std::sqrt(DENRo / DENLo), rrorlp1 = 1.0 + rrorl;
@@ -1374,12 +1373,11 @@ void roe_rot_common(const trans_params& p, double PLo, double PRo, double TLo, d
 // vkbc that the reference reads uninitialised (:169, :332, :510) are taken as 0.
 void roe_rotated(const trans_params& p, double PLo, double PRo, double TLo, double TRo, double ULo, double URo,
                  double VLo, double VRo, double WLo, double WRo, double sav1, double sav2, double sav3, double sav,
-                 double Funscheme, double* dr) {
+                 double rLo, double rRo, double Funscheme, double* dr) {
     double rcpcv = p.PPF;
     double DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
     const double ga = 1.4, ga1 = 0.4;
     double VAMLo = ULo * ULo + VLo * VLo + WLo * WLo, VAMRo = URo * URo + VRo * VRo + WRo * WRo;
-    const double rLo = 0.0, rRo = 0.0;
     double HLo = PLo * ga / (DENLo * ga1) + 0.5 * VAMLo - 0.5 * (rLo * rLo);
     double HRo = PRo * ga / (DENRo * ga1) + 0.5 * VAMRo - 0.5 * (rRo * rRo);
     double sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
@@ -1394,7 +1392,7 @@ void roe_rotated(const trans_params& p, double PLo, double PRo, double TLo, doub
     dr[4] = -0.5 * (rulnormaln * HLo + rurnormaln * HRo - vbc * (PLo + PRo)) * sav;
     double DeltaU = std::sqrt((URo - ULo) * (URo - ULo) + (VRo - VLo) * (VRo - VLo) + (WRo - WLo) * (WRo - WLo));
     if (DeltaU <= p.Tiny) {
-        roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, Funscheme, dr);
+        roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, rLo, rRo, Funscheme, dr);
         return;
     }
     double n1 = (URo - ULo) / DeltaU, n2 = (VRo - VLo) / DeltaU, n3 = (WRo - WLo) / DeltaU;
@@ -1405,9 +1403,9 @@ void roe_rotated(const trans_params& p, double PLo, double PRo, double TLo, doub
     double a1 = n1 * s, a2 = n2 * s, a3 = n3 * s;
     double b1 = sav1 - a1, b2 = sav2 - a2, b3 = sav3 - a3;
     double sa = std::max(std::sqrt(a1 * a1 + a2 * a2 + a3 * a3), p.Tiny);
-    roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, a1, a2, a3, sa, Funscheme, dr);
+    roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, a1, a2, a3, sa, rLo, rRo, Funscheme, dr);
     double sb = std::max(std::sqrt(b1 * b1 + b2 * b2 + b3 * b3), p.Tiny);
-    roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, b1, b2, b3, sb, Funscheme, dr);
+    roe_rot_common(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, b1, b2, b3, sb, rLo, rRo, Funscheme, dr);
 }
 
 void convect_inviscid(Ctx& c, Blk& b) {
@@ -1430,7 +1428,9 @@ void convect_inviscid(Ctx& c, Blk& b) {
                 int im = i - e[0], jm = j - e[1], km = k - e[2];
                 double Funscheme = (b.Fsch(im, jm, km) + b.Fsch(i, j, k)) / 2.;
                 double dr[5];
-                roe_rotated(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, Funscheme, dr);
+                // rLo, rRo = rccl, rccr * omega(1) (Space/CONVECT_Roe_Rotated.F90:102-103, 274-275, 446-447)
+                double rLo = b.rccl(d, i, j, k) * p.omega[0], rRo = b.rccr(d, i, j, k) * p.omega[0];
+                roe_rotated(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, rLo, rRo, Funscheme, dr);
                 for (int L = 1; L <= 5; ++L) {
                     b.D(L, i, j, k) = b.D(L, i, j, k) - dr[L - 1];
                     b.D(L, im, jm, km) = b.D(L, im, jm, km) + dr[L - 1];
@@ -1494,8 +1494,10 @@ void turbtwo_convect_upwind(Ctx& c, Blk& b) {
 // Space/RC_Correction.F90:19-124 (Kind_RotMod = 1): the rotation/curvature factor f_r1 of the
 // SST production, as the reference's build evaluates it (-O2 without -auto: the local arrays
 // St2 and Wij are static, zero at load, and the entries the routine never writes -- St2(3,3)
-// and the diagonal of Wij -- stay 0).  omega(M) (:107; M is never set, the loop variable is
-// MM) multiplies omega, which is 0 in every case this restatement accepts; omega(1) stands in.
+// and the diagonal of Wij -- stay 0).  omega(M) (:107) reads an index M that the routine never
+// sets (the loop variable is MM, which runs over 1 only); with the static zero M it would read
+// outside omega(1:3).  The restatement reads omega(1), the loop's evident intent; the term is 0
+// whenever omega(1) is 0.
 // VL(d,v) is what SPACEINTERP_GetSurfCenterVars wrote in this iteration, 0 where it writes
 // nothing (the reference zeroes VL at allocation, Input/Read_BlockDimensions.F90:418, and no
 // routine writes those entries).  Kind_RotMod = 2 computes f_r2 (:126-171), which no routine
@@ -2350,7 +2352,8 @@ int oracle_create(const trans_params* p, int nblocks, const trans_block* blocks,
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return TRANS_E_ARG;
     // DES (0), the DDES shielding functions (1-3) and IDDES (5); FSST is undefined for 4
     if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 5 || p->Kind_SubHY == 4)) return TRANS_E_ARG;
-    if (p->omega[0] != 0.0 || p->omega[1] != 0.0 || p->omega[2] != 0.0) return TRANS_E_ARG;
+    // rotation about the x axis at omega(1); omega(2) and omega(3) are read by no routine of the path
+    if (!std::isfinite(p->omega[0])) return TRANS_E_ARG;
     if (p->IF_RK != 0 && p->IF_RK != 1) return TRANS_E_ARG;
     Ctx* c = new Ctx();
     c->p = *p;

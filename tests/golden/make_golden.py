@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from helpers import inputs_digest, small_cascade, small_channel  # noqa: E402
+from helpers import inputs_digest, small_case  # noqa: E402
 from oracle.oracle import OracleSolver  # noqa: E402
 
 NITER = 10
@@ -35,6 +35,8 @@ CASES = {
     "channel_small_mdcd_ausmpw_iddes": ("channel", dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3, Kind_SubHY=5)),
     "channel_small_m03_muscl_roe_precond": ("channel", dict(Kind_Spatial=2, Kind_Roe=1, IF_Precondition=1, XM=0.3)),
     "cascade_small_mdcd_ausmpw_rc": ("cascade", dict(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=1)),
+    "annular_small_rotating_mdcd_roe": ("annular", dict(Kind_Spatial=3, Kind_Roe=1)),
+    "annular_small_rotating_muscl_roerot": ("annular", dict(Kind_Spatial=2, Kind_Roe=2)),
 }
 
 
@@ -46,7 +48,7 @@ def probe_cells(dims, n=6, seed=1):
 
 
 def make_case(kind, sw):
-    return small_channel(**sw) if kind == "channel" else small_cascade(**sw)
+    return small_case(kind, **sw)
 
 
 def record(kind, sw):

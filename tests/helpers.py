@@ -16,6 +16,23 @@ def small_channel(ni=25, nj=17, nk=6, **sw):
     return c, conns, geo, st
 
 
+# rotating annular sector: 2000 rev/min gives a blade speed omega*r of about 0.27 of the axial
+# velocity at the casing; the casing is at rest in the absolute frame (Kindsub_BC = 1)
+SMALL_ANNULAR = dict(ni=17, nj=11, nk=6, rpm=2000.0, casing_kindsub=1)
+
+
+def small_annular(**sw):
+    c = cases.annular_sector(**SMALL_ANNULAR, **sw)
+    conns, geo = C.compute_geometry(c)
+    st = C.initial_state(c, geo, Q_dst=c.meta["Q_dst"])
+    return c, conns, geo, st
+
+
+def small_case(kind, **sw):
+    """The small case of a golden fixture's kind: channel, cascade or annular."""
+    return {"channel": small_channel, "cascade": small_cascade, "annular": small_annular}[kind](**sw)
+
+
 def interior(dims):
     ni, nj, nk = dims
     m = np.zeros((ni + 5, nj + 5, nk + 5), bool, order="F")

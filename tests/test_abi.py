@@ -101,6 +101,17 @@ def test_unsupported_options_are_rejected(lib, bad):
     assert not ctx.value
 
 
+def test_non_finite_rotation_is_rejected(lib):
+    """omega(1) is the frame's rotation about x; any finite value is accepted, NaN or inf is not."""
+    p = _params()
+    p.omega[0] = float("nan")
+    blk = (abi.TransBlock * 1)()
+    blk[0].ni = blk[0].nj = blk[0].nk = 8
+    ctx = C.c_void_p()
+    assert lib.trans_create(C.byref(p), 1, blk, C.byref(ctx)) == abi.TRANS_E_ARG
+    assert not ctx.value
+
+
 def test_null_arguments_are_rejected(lib):
     ctx = C.c_void_p()
     assert lib.trans_create(None, 1, None, C.byref(ctx)) == abi.TRANS_E_ARG

@@ -12,7 +12,7 @@ beyond a few FP32 ulps per iteration.
 import numpy as np
 import pytest
 
-from helpers import interior, rel_err, small_cascade, small_channel
+from helpers import interior, rel_err, small_annular, small_cascade, small_channel
 
 pytestmark = pytest.mark.gpu
 
@@ -41,10 +41,13 @@ def _run(case, precision, n):
                                          (small_cascade, dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05)),
                                          (small_cascade, dict(Kind_Spatial=3, Kind_Roe=3, Kind_Model=2)),
                                          (small_channel, dict(Kind_Spatial=3, Kind_Roe=3, Kind_Hybrid=3, Kind_SubHY=5)),
-                                         (small_channel, dict(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=1))],
+                                         (small_channel, dict(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=1)),
+                                         (small_annular, dict(Kind_Spatial=3, Kind_Roe=1)),
+                                         (small_annular, dict(Kind_Spatial=2, Kind_Roe=1, Kind_RotMod=1))],
                          ids=["channel_mdcd_ausmpw", "channel_muscl_roe", "cascade_mdcd_ausmpw", "channel_rk3_mdcd_ausmpw",
                               "channel_muscl2_roe", "cascade_mdcdhyb_ausmpw", "cascade_mdcd_ausmpw_wd2006",
-                              "channel_mdcd_ausmpw_iddes", "channel_mdcd_ausmpw_rc"])
+                              "channel_mdcd_ausmpw_iddes", "channel_mdcd_ausmpw_rc", "annular_rotating_mdcd_roe",
+                              "annular_rotating_muscl_roe_rc"])
 def test_mixed_tracks_fp64(gpu_lib, make, scheme):
     case = make(**scheme)
     h64, f64 = _run(case, "fp64", 20)

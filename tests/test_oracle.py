@@ -152,8 +152,8 @@ GOLD_TOL = 1e-12
 
 
 def golden_case(g):
-    from helpers import small_cascade
-    return small_channel(**g["switches"]) if g["case"] == "channel" else small_cascade(**g["switches"])
+    from helpers import small_case
+    return small_case(g["case"], **g["switches"])
 
 
 @pytest.mark.parametrize("name", GOLDEN)

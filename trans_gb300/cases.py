@@ -90,16 +90,21 @@ def channel_bump(ni=97, nj=49, nk=9, Re_L=1.0e6, XM=0.5, bump=0.08, span=0.2, to
 
 
 def annular_sector(ni=25, nj=13, nk=9, sector_deg=10.0, r_hub=1.0, r_tip=1.5, Re_L=1.0e6, XM=0.4,
-                   p_ratio=0.95, **switches):
+                   p_ratio=0.95, rpm=0.0, casing_kindsub=0, **switches):
     """Annular duct sector with rotational periodicity (single block): x in [-1, 2] axial (i),
     r in [r_hub, r_tip] (j), theta in [0, sector] (k) about the x axis.  BCs: i-min inlet
     (kind 5), i-max outlet (kind 7, radial-equilibrium recurrence over r), hub and casing
     no-slip walls (kind 1), k faces 1-to-1 onto each other (kind 9) across the sector, so the
     interface rotates (v, w) and the gradients by rotateAngle = +-sector
-    (Input/PLOT3DReadInit.F90:157-160 with nblade = 360/sector, one passage)."""
+    (Input/PLOT3DReadInit.F90:157-160 with nblade = 360/sector, one passage).
+
+    rpm: the frame's rotation about the x axis (omega(1) of the dimension file, in rev/min);
+    the hub turns with the frame, and the casing does too unless casing_kindsub = 1, which
+    makes it a wall at rest in the absolute frame (BC_Wall.F90:46-52)."""
     nblade = int(round(360.0 / sector_deg))
     ph = _flow(XM, p_out_ratio=p_ratio)
     ph.nblade, ph.npassage = nblade, 1
+    ph.omega_rpm = (float(rpm), 0.0, 0.0)
     sw = dict(Kind_Spatial=3, Kind_Roe=3, CFL_Sub_start=2.0, CFL_Sub_end=2.0, CFL_Sub_step=1,
               Kind_Dual=2, Kchld=1, DT_LUSGS_Main=1.0e8)
     sw.update(switches)
@@ -117,7 +122,7 @@ def annular_sector(ni=25, nj=13, nk=9, sector_deg=10.0, r_hub=1.0, r_tip=1.5, Re
     X /= alscale
     # k-min ghosts take the k-max cells (one sector further round): their (v, w) rotate back by
     # the sector angle, V(3) = cos a vy + sin a vz with a = +sector (BC/BC_P2P.F90:69-94)
-    segs = [Segment(1, kind=5), Segment(2, kind=7), Segment(3, kind=1), Segment(4, kind=1),
+    segs = [Segment(1, kind=5), Segment(2, kind=7), Segment(3, kind=1), Segment(4, kind=1, kindsub=casing_kindsub),
             Segment(5, kind=9, blk_ex=1, blkbd_ex=6, period=1), Segment(6, kind=9, blk_ex=1, blkbd_ex=5, period=-1)]
     b = Block(1, X, segs, walls=[(3, 0, 0, 0, 0), (4, 0, 0, 0, 0)])
     walls = [X[:, 0, :, :], X[:, -1, :, :]]

@@ -323,16 +323,16 @@ template <typename R> __device__ inline void mdcd_pair(const R* s6, R gama, R& q
     }
 }
 
-// Roe_Common of the rotated scheme (Space/CONVECT_Roe_Rotated.F90:597-752), non-preconditioned,
-// rcc * omega = 0: adds 0.5 |A| dQ along (sav1..3)/sav, times sav and Funscheme, to dr
+// Roe_Common of the rotated scheme (Space/CONVECT_Roe_Rotated.F90:597-752), non-preconditioned:
+// adds 0.5 |A| dQ along (sav1..3)/sav, times sav and Funscheme, to dr.  rLo, rRo = rccl, rccr
+// times omega(1), the frame speeds of the two states.
 template <typename R>
 __device__ inline void roe_rot_common(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo,
-                                      R WRo, R sav1, R sav2, R sav3, R sav, R Funscheme, R* dr) {
+                                      R WRo, R sav1, R sav2, R sav3, R sav, R rLo, R rRo, R Funscheme, R* dr) {
     const R rcpcv = R(p.PPF);
     const R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
     const R ga = R(1.4), ga1 = R(0.4);
     const R VAMLo = ULo * ULo + VLo * VLo + WLo * WLo, VAMRo = URo * URo + VRo * VRo + WRo * WRo;
-    const R rLo = R(0.0), rRo = R(0.0);
     const R HLo = PLo * ga / (DENLo * ga1) + R(0.5) * VAMLo - R(0.5) * (rLo * rLo);
     const R HRo = PRo * ga / (DENRo * ga1) + R(0.5) * VAMRo - R(0.5) * (rRo * rRo);
     const R rrorl = sqrt(DENRo / DENLo), rrorlp1 = R(1.0) + rrorl;
@@ -367,12 +367,11 @@ __device__ inline void roe_rot_common(const ParamsT<R>& p, R PLo, R PRo, R TLo, 
 // The grid velocities the reference reads uninitialised (:169, :332, :510) are taken as 0.
 template <typename R>
 __device__ inline void roe_rotated(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo,
-                                   R WRo, R sav1, R sav2, R sav3, R sav, R Funscheme, R* dr) {
+                                   R WRo, R sav1, R sav2, R sav3, R sav, R rLo, R rRo, R Funscheme, R* dr) {
     const R rcpcv = R(p.PPF);
     const R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
     const R ga = R(1.4), ga1 = R(0.4);
     const R VAMLo = ULo * ULo + VLo * VLo + WLo * WLo, VAMRo = URo * URo + VRo * VRo + WRo * WRo;
-    const R rLo = R(0.0), rRo = R(0.0);
     const R HLo = PLo * ga / (DENLo * ga1) + R(0.5) * VAMLo - R(0.5) * (rLo * rLo);
     const R HRo = PRo * ga / (DENRo * ga1) + R(0.5) * VAMRo - R(0.5) * (rRo * rRo);
     const R sav1n = sav1 / sav, sav2n = sav2 / sav, sav3n = sav3 / sav;
@@ -387,7 +386,7 @@ __device__ inline void roe_rotated(const ParamsT<R>& p, R PLo, R PRo, R TLo, R T
     dr[4] = R(-0.5) * (rulnormaln * HLo + rurnormaln * HRo - vbc * (PLo + PRo)) * sav;
     const R DeltaU = sqrt((URo - ULo) * (URo - ULo) + (VRo - VLo) * (VRo - VLo) + (WRo - WLo) * (WRo - WLo));
     if (DeltaU <= R(p.Tiny)) {
-        roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, Funscheme, dr);
+        roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, sav1, sav2, sav3, sav, rLo, rRo, Funscheme, dr);
         return;
     }
     R n1 = (URo - ULo) / DeltaU, n2 = (VRo - VLo) / DeltaU, n3 = (WRo - WLo) / DeltaU;
@@ -398,21 +397,21 @@ __device__ inline void roe_rotated(const ParamsT<R>& p, R PLo, R PRo, R TLo, R T
     const R a1 = n1 * s, a2 = n2 * s, a3 = n3 * s;
     const R b1 = sav1 - a1, b2 = sav2 - a2, b3 = sav3 - a3;
     const R sa = dmax(sqrt(a1 * a1 + a2 * a2 + a3 * a3), R(p.Tiny));
-    roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, a1, a2, a3, sa, Funscheme, dr);
+    roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, a1, a2, a3, sa, rLo, rRo, Funscheme, dr);
     const R sb = dmax(sqrt(b1 * b1 + b2 * b2 + b3 * b3), R(p.Tiny));
-    roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, b1, b2, b3, sb, Funscheme, dr);
+    roe_rot_common<R>(p, PLo, PRo, TLo, TRo, ULo, URo, VLo, VRo, WLo, WRo, b1, b2, b3, sb, rLo, rRo, Funscheme, dr);
 }
 
-// Space/CONVECT_Roe_Original.F90:242-407 (non-preconditioned, no rotation); out = flux / |S|
+// Space/CONVECT_Roe_Original.F90:242-407; out = flux / |S|.  rLo, rRo = rccl, rccr times
+// omega(1) (:79-80, 138-139, 196-197), the frame speeds of the two states.
 template <typename R>
 __device__ inline void roe_flux(const ParamsT<R>& p, R PLo, R PRo, R TLo, R TRo, R ULo, R URo, R VLo, R VRo, R WLo, R WRo,
-                                R sav1, R sav2, R sav3, R sav, R* out, R RmiuT = R(0.0), R AlagmR = R(1.0)) {
+                                R sav1, R sav2, R sav3, R sav, R rLo, R rRo, R* out, R RmiuT = R(0.0), R AlagmR = R(1.0)) {
     R rcpcv = R(p.PPF);
     R DENLo = PLo / (rcpcv * TLo), DENRo = PRo / (rcpcv * TRo);
     const R ga = R(1.4), ga1 = R(1.4 - 1.0);
     R VAMLo = ULo * ULo + VLo * VLo + WLo * WLo;
     R VAMRo = URo * URo + VRo * VRo + WRo * WRo;
-    R rLo = R(0.0), rRo = R(0.0);
     R HLo = PLo * ga / (DENLo * ga1) + R(0.5) * VAMLo - R(0.5) * (rLo * rLo);
     R HRo = PRo * ga / (DENRo * ga1) + R(0.5) * VAMRo - R(0.5) * (rRo * rRo);
     R rrorl = sqrt(DENRo / DENLo);

@@ -54,7 +54,7 @@ Params make_params(const trans_params& p) {
 
 // options outside the configurations of this hot path are rejected, never approximated
 bool params_supported(const trans_params* p) {
-    // RC correction (Kind_RotMod 1; 2 computes a factor nothing reads) in a frame at rest
+    // RC correction (Kind_RotMod 1; 2 computes a factor nothing reads)
     if ((p->IF_Precondition != 0 && p->IF_Precondition != 1) || p->Kind_RotMod < 0 || p->Kind_RotMod > 2 ||
         (p->Kind_Model != 1 && p->Kind_Model != 2) || p->IF_Euler != 0)
         return false;
@@ -65,7 +65,9 @@ bool params_supported(const trans_params* p) {
     if (p->Kind_Hybrid != 0 && p->Kind_Hybrid != 3) return false;
     // DES (0), the DDES shielding functions (1-3) and IDDES (5); FSST is undefined for 4
     if (p->Kind_Hybrid == 3 && (p->Kind_SubHY < 0 || p->Kind_SubHY > 5 || p->Kind_SubHY == 4)) return false;
-    if (p->omega[0] != 0.0 || p->omega[1] != 0.0 || p->omega[2] != 0.0) return false;
+    // a frame rotating about the x axis at omega(1); omega(2) and omega(3) are read by no
+    // routine of the path
+    if (!std::isfinite(p->omega[0])) return false;
     if (p->precision != TRANS_FP64 && p->precision != TRANS_MIXED) return false;
     // the rotated Roe scheme splits its dissipation along the direction of the velocity jump,
     // which FP32 rounding turns into noise where the two states nearly agree: FP64 path only

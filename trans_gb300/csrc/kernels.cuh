@@ -675,6 +675,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
     // ---------------- reconstruction ----------------
     R qL[7], qR[7];
     const R* qc[5] = {pu, pv, pw, PPp, PT};
+    R gama = R(0.0);
     if (p.Kind_Spatial <= 2) {     // CONVECT_MUSCL (2) or CONVECT_MUSCL2 (1): the limiter differs
         const bool m2 = p.Kind_Spatial == 1;
         for (int q = 0; q < 5; ++q) {
@@ -696,7 +697,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
         sensor = dmax(sensor, R(sh[c + s]));
         sensor = dmax(sensor, R(sh[c + 2 * s]));
         if (DIR == 3 && !hyb) sensor = dmax(sensor, R(0.0));
-        R gama = R(p.gama_min) + sensor * (R(p.gama_max) - R(p.gama_min));
+        gama = R(p.gama_min) + sensor * (R(p.gama_max) - R(p.gama_min));
         // MDCDHYB: MUSCL states where the sensor reaches F_limiter2 (Space/CONVECT_MDCDHYB.F90:118-120, 175-177)
         const bool muscl = hyb && sensor >= R(p.F_limiter2);
         for (int q = 0; q < 5; ++q) {
@@ -723,6 +724,36 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
             qR[5 + q] = q0 - alimiter(DL, DR);
         }
     }
+    // ---------------- frame speeds of the two states (rotating frame) ----------------
+    // rLo, rRo = rccl, rccr * omega(1), read by the Roe schemes only.  rccl/rccr start as the
+    // face average of rad (SPACEINTERP_GetSurfCenterVars); CONVECT_MUSCL / CONVECT_MUSCL2 limit
+    // them like the primitives (CONVECT_MUSCL.F90:111-116, CONVECT_MUSCL2.F90:114-118); CONVECT_MDCD
+    // replaces them in I and J by the MDCD states of rad with the cell's weights
+    // (CONVECT_MDCD.F90:51-120, 259-328) and leaves the K faces at the average (its K block sits
+    // outside the face loops, :450-521); CONVECT_MDCDHYB leaves every face at the average.
+    R rLo = R(0.0), rRo = R(0.0);
+    if (p.omega0 != R(0.0) && p.Kind_Roe != 3) {
+        const R* rad = rs<R>(b, S_RAD);
+        R rl, rr;
+        if (p.Kind_Spatial <= 2) {
+            const bool m2 = p.Kind_Spatial == 1;
+            R fm = favg<R>(rad, al, ainv, cm, s), f0 = favg<R>(rad, al, ainv, c, s), fp = favg<R>(rad, al, ainv, cp, s);
+            R q1 = R(rad[cm]), q0 = R(rad[c]);
+            R DR = f0 - q1, DL = q1 - fm;
+            rl = q1 + (m2 ? muscl2_limiter(DR, DL) : alimiter(DR, DL));
+            DR = fp - q0; DL = q0 - f0;
+            rr = q0 - (m2 ? muscl2_limiter(DL, DR) : alimiter(DL, DR));
+        } else if (p.Kind_Spatial == 3 && DIR != 3) {
+            R s6[6];
+            for (int o = 0; o < 6; ++o) s6[o] = R(rad[c + (o - 3) * s]);
+            mdcd_pair(s6, gama, rl, rr);
+        } else {
+            rl = favg<R>(rad, al, ainv, c, s);
+            rr = rl;
+        }
+        rLo = rl * R(p.omega0);
+        rRo = rr * R(p.omega0);
+    }
     // ---------------- inviscid flux ----------------
     R sav1 = R(SDd[c]), sav2 = R(SDd[c + nc]), sav3 = R(SDd[c + 2 * nc]);
     R sav = R(rs<R>(b, S_GRAD + d)[c]);
@@ -731,14 +762,14 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
         const R* fs = rs<R>(b, S_FSCH);
         const R Funscheme = (R(fs[cm]) + R(fs[c])) / R(2.);
         roe_rotated<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav,
-                       Funscheme, f);
+                       rLo, rRo, Funscheme, f);
         for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = f[L];
     } else {
         if (p.Kind_Roe == 1) {
             // preconditioning reads VL(d,8), the face-averaged eddy viscosity (0 while turbulence
             // is off), and Alagm(d) of the face's cell (Space/CONVECT_Roe_Original.F90:86-87)
             const R RmiuTf = (p.IF_Precondition && turb) ? favg<R>(rs<R>(b, S_RMIU), al, ainv, c, s) : R(0.0);
-            roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f, RmiuTf,
+            roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, rLo, rRo, f, RmiuTf,
                         R(al[c]));
         } else
             ausmpw_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
@@ -783,9 +814,20 @@ __global__ void k_gather(const DevBlock* __restrict__ blks, const Tile* __restri
         for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_C0, c); acc = acc + fx(d, FX_C0, c + st[d]); }
         rs<R>(b, S_D)[c] = acc;
     }
+    // rotating-frame source of DIFFUSION_Centered (:812-822), after its viscous terms: Coriolis
+    // and centrifugal force on y and z momentum times the cell volume.  With omega(1) = 0 it adds
+    // a signed zero, which leaves a sum that started at +0 unchanged, so it is skipped.
+    const R om = R(cdev[b.cs].p.omega0);
     for (int L = 1; L < 5; ++L) {
         R acc = R(0.0);
         for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_VX + L - 1, c); acc = acc + fx(d, FX_VX + L - 1, c + st[d]); }
+        if ((L == 2 || L == 3) && om != R(0.0)) {
+            const R* V = rs<R>(b, S_V);
+            const R V1 = R(V[c]);
+            const R ss = L == 2 ? R(2.0) * om * R(V[3 * nc + c]) + om * R(rs<R>(b, S_YC)[c]) * om * V1
+                                : R(-2.0) * om * R(V[2 * nc + c]) + om * R(rs<R>(b, S_ZC)[c]) * om * V1;
+            acc = acc + ss * R(rs<R>(b, S_VOL)[c]);
+        }
         for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_C0 + L, c); acc = acc + fx(d, FX_C0 + L, c + st[d]); }
         rs<R>(b, S_D + L)[c] = acc;
     }
@@ -844,7 +886,8 @@ __global__ void k_sst_fc1(const DevBlock* __restrict__ blks, const Tile* __restr
 // Space/RC_Correction.F90:19-124 (Kind_RotMod = 1): the rotation/curvature factor f_r1 of the
 // SST production of one interior cell (I,J,K), slot index c, evaluated as the reference's build
 // evaluates it: the static local arrays' entries it never writes (St2(3,3), the diagonal of
-// Wij) are 0; omega(M) multiplies omega = 0; VL(d,v) is the face average of
+// Wij) are 0; omega(M), whose index the routine never sets, is read as omega(1) (the term is
+// 0 whenever omega(1) is); VL(d,v) is the face average of
 // SPACEINTERP_GetSurfCenterVars where that routine writes it and 0 elsewhere.  RCCorrection
 // runs after BC_Boundarys(0) (main.F90:89); its inputs do not change until the update, so the
 // LU-SGS preparation evaluates it.
