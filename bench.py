@@ -174,6 +174,7 @@ def time_resident(s, ki0, steps):
 # writes of one unit (interior cell, or face for the face fluxes) with halos excluded.
 ALG_WORDS = {
     "k_face_flux": 51,      # per face: stencil 38 words in, 13 face fluxes out
+    "k_resid_tma": 50,      # per face: stencil 38 words in; D of the face's cell, 7 out and 7 in for 2 of 3 directions
     "k_sweep": 24,          # the L -> U hand-off: DeltaQ 7 + Rds 3 + diagonals 2, written and read once
     "k_update": 37, "k_gradient": 46, "k_specrad": 24, "k_lusgs_prep": 60, "k_gather": 46,
 }
@@ -184,7 +185,7 @@ FACE_FP64_INST = 2541.0
 FACE_DRAM_BYTES = 391.3
 FACE_DRAM_SOURCE = "ncu dram__bytes_read+write per face on the 339,968-cell cascade, scaled by faces"
 # kernel classes that run in FP32 in the mixed path (their algorithmic words are 4 bytes there)
-FP32_KERNELS = ("k_face_flux", "k_gather", "k_sweep", "k_gradient")
+FP32_KERNELS = ("k_face_flux", "k_resid_tma", "k_gather", "k_sweep", "k_gradient")
 # bounded serving leg of the default line: 4 requests/s as the serving configuration states,
 # for 5 s of arrivals; each request retires at a 0.3 drop of its residual (coarse grids take
 # ~580 iterations to it, medium ~690 with the CFL ramp) or after 1,500 iterations, so the leg
@@ -197,7 +198,7 @@ SERVE_MAX_ITERS = 1500
 def units(c, kernel):
     """Units a kernel class processes per iteration: faces of all three directions for the
     face fluxes, interior cells otherwise."""
-    if kernel == "k_face_flux":
+    if kernel in ("k_face_flux", "k_resid_tma"):
         return sum(ni * (nj - 1) * (nk - 1) + (ni - 1) * nj * (nk - 1) + (ni - 1) * (nj - 1) * nk
                    for ni, nj, nk in (b.dims for b in c.blocks))
     return interior_cells(c)

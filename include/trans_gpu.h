@@ -311,7 +311,7 @@ int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms);
 /* One outer iteration KI with CUDA events around every kernel launch on the context's stream:
  * ms[k] and launches[k] per kernel class k (n >= TRANS_NKCLASS entries); names from
  * trans_kernel_class(k).  No reference counterpart: instrumentation. */
-#define TRANS_NKCLASS 16
+#define TRANS_NKCLASS 17
 int trans_kernel_times(void* ctx, int ki, double* ms, int* launches, int n);
 const char* trans_kernel_class(int k);
 /* The schedule the context's tuner picked for the LU-SGS sweeps and what it measured (no

@@ -96,3 +96,63 @@ def test_mixed_residual_field_readback(gpu_lib):
         for q in g:
             err = np.max(np.abs(D32[q][m] - D64[q][m])) / scale
             assert err < 2e-4, (q, err)
+
+
+def _first_residual(case, precision, env="1"):
+    """D after the first iteration's residual stage of a context of the given precision,
+    created with the given TRANS_RESID_TMA setting, and the kernel classes that ran."""
+    import os
+    from trans_gb300 import abi
+    from trans_gb300.solver import Solver
+    c, conns, geo, st = case
+    c.params.precision = abi.TRANS_MIXED if precision == "mixed" else abi.TRANS_FP64
+    old = os.environ.get("TRANS_RESID_TMA")
+    os.environ["TRANS_RESID_TMA"] = env
+    try:
+        s = Solver(c, conns, geo, st)
+    finally:
+        if old is None:
+            del os.environ["TRANS_RESID_TMA"]
+        else:
+            os.environ["TRANS_RESID_TMA"] = old
+    for stage in ("SPECRAD", "BC_STATE", "GRADIENT", "BC_GRAD", "RESIDUAL"):
+        s.run_stage(stage, 1)
+    D = [s.get_field(ib, "D") for ib in range(len(c.blocks))]
+    s.iterate(2)
+    import bench
+    names = set(bench.kernel_times(s, 3))
+    s.close()
+    return D, names
+
+
+@pytest.mark.parametrize("make,scheme", [(small_channel, dict(Kind_Spatial=3, Kind_Roe=3)),
+                                         (small_channel, dict(Kind_Spatial=2, Kind_Roe=1)),
+                                         (small_cascade, dict(Kind_Spatial=3, Kind_Roe=3)),
+                                         (small_cascade, dict(Kind_Spatial=4, Kind_Roe=3, F_limiter2=0.05)),
+                                         (small_annular, dict(Kind_Spatial=3, Kind_Roe=1))],
+                         ids=["channel_mdcd_ausmpw", "channel_muscl_roe", "cascade_mdcd_ausmpw", "cascade_mdcdhyb_ausmpw",
+                              "annular_rotating_mdcd_roe"])
+def test_tma_tiles_match_face_flux_kernels(gpu_lib, make, scheme):
+    """The mixed path's residual from TMA-staged shared-memory tiles (k_resid_tma, the default)
+    against its residual from k_face_flux<float> + k_gather<float> (TRANS_RESID_TMA=0), both
+    against the FP64 residual: the same FP32 face arithmetic, summed per direction instead of in
+    the gather's order.  D is a difference of fluxes many times its size, so FP32 rounding of the
+    fluxes shows in D at up to ~1e-4 of its largest value; the tiled path must be as close to
+    FP64 as the gather path (within 3x its error, plus 1e-6 of the largest |D|), per equation
+    group and block."""
+    D_t, names_t = _first_residual(make(**scheme), "mixed", "1")
+    D_g, names_g = _first_residual(make(**scheme), "mixed", "0")
+    D_64, _ = _first_residual(make(**scheme), "fp64")
+    assert "k_resid_tma" in names_t and "k_face_flux" not in names_t and "k_gather" not in names_t
+    assert "k_face_flux" in names_g and "k_resid_tma" not in names_g
+    case = make(**scheme)
+    for ib, b in enumerate(case[0].blocks):
+        m = interior(b.dims)
+        for grp in ((0,), (1, 2, 3), (4,), (5,), (6,)):
+            scale = max(np.max(np.abs(D_64[ib][q][m])) for q in grp)
+            if scale == 0.0:
+                continue
+            e_t = max(np.max(np.abs(D_t[ib][q][m] - D_64[ib][q][m])) for q in grp) / scale
+            e_g = max(np.max(np.abs(D_g[ib][q][m] - D_64[ib][q][m])) for q in grp) / scale
+            assert e_t <= 3.0 * e_g + 1e-6, f"block {b.id} D{grp}: tiled {e_t:.3e}, gather {e_g:.3e}"
+            assert e_t <= 1e-3, f"block {b.id} D{grp}: tiled {e_t:.3e}"

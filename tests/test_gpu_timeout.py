@@ -41,3 +41,28 @@ def test_sweep_wait_runs_out(gpu_lib, schedule, monkeypatch):
         norms = s.iterate(ki)
         assert all(n["nan_flag"] == 0 and n["DRSa"] > 0 for n in norms)
     s.close()
+
+
+def test_tile_staging_wait_runs_out(gpu_lib, monkeypatch):
+    """The mixed path's residual tiles wait on an mbarrier for their TMA copies.  Allowed no
+    polls (TRANS_RESID_SPIN=0), every CTA records the error, waits for its copies in flight with
+    the default bound (they land; the shared memory they write must outlive them) and returns;
+    the UPDATE stage reports TRANS_E_TIMEOUT, and a context with the default limit iterates."""
+    from trans_gb300 import abi
+    from trans_gb300.solver import Solver
+    monkeypatch.setenv("TRANS_RESID_SPIN", "0")
+    c, conns, geo, st = small_cascade(Kind_Spatial=3, Kind_Roe=3)
+    c.params.precision = abi.TRANS_MIXED
+    s = Solver(c, conns, geo, st)
+    lib = s.lib
+    for name in PRE_UPDATE:
+        s.run_stage(name, 1)
+    assert lib.trans_run_stage(s.ctx, abi.STAGE_ID["UPDATE"], 1, 1) == abi.TRANS_E_TIMEOUT
+    assert b"residual tile" in lib.trans_last_error(s.ctx)
+    s.close()
+    monkeypatch.delenv("TRANS_RESID_SPIN")
+    s = Solver(c, conns, geo, st)
+    for ki in (1, 2):
+        norms = s.iterate(ki)
+        assert all(n["nan_flag"] == 0 and n["DRSa"] > 0 for n in norms)
+    s.close()

@@ -199,4 +199,4 @@ EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field
             "trans_batch_get_integrals", "trans_batch_integrals", "trans_batch_get_wall_cp", "trans_wall_distance",
             "trans_set_fields", "trans_get_fields", "trans_batch_set_fields", "trans_batch_get_fields",
             "trans_block_metrics"]
-TRANS_NKCLASS = 16
+TRANS_NKCLASS = 17

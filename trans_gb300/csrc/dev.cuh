@@ -1,8 +1,11 @@
 // dev.cuh -- device data layout and per-face / per-cell physics of the TRANS hot path.
 //
 // Layout: every block of every case lives in one device arena.  A block owns NSLOT scalar
-// arrays ("slots") of ncell = (NI+5)(NJ+5)(NK+5) doubles each, i fastest, covering the full
-// ghost extent -2..N+2 of the reference's arrays.  Cell-centred and face-centred quantities
+// arrays ("slots") of ncell = PI*PJ*PK doubles each, i fastest, covering the full ghost extent
+// -2..N+2 of the reference's arrays: PJ = NJ+5, PK = NK+5, and PI = NI+5 rounded up to a
+// multiple of 4, so that every row of the FP32 copies starts on a 16-byte boundary and a slot
+// range forms a 4-D tensor (i, j, k, slot) that the tensor-memory-access unit can tile.  The
+// cells i >= NI+5 of a row are padding that no stencil reads.  Cell-centred and face-centred quantities
 // share the index: face i of direction d is stored at cell i (the cell on its +d side).
 //
 // The physics functions below restate the reference's expressions operation by operation
@@ -106,6 +109,10 @@ struct Tile {             // a run of consecutive interior cells (or faces) of o
     int blk, start, count, pad_;
 };
 
+struct ResidTile {        // a brick of cells of one block (array indices of its first cell)
+    int blk, x0, y0, z0;
+};
+
 #define TG_PARAM_REALS(X) X(XM) X(RXM2) X(PPF) X(Csthlnd) X(Csth1) X(Ref) X(Tiny) X(VxF) X(VyF) X(VzF) \
     X(omega0) X(P0in) X(T0in) X(Pouthub) X(VisRatio) X(FSTI) X(A1) X(Beta_star) X(Sigk1) X(Sigo1)    \
     X(Beta1) X(Gama1) X(Sigk2) X(Sigo2) X(Beta2) X(Gama2) X(Prod_Lmt) X(gama_max) X(gama_min) X(F_limiter1) X(F_limiter2) X(Alscale)        \
@@ -150,6 +157,9 @@ __host__ __device__ inline int cidx(const DevBlock& b, int i, int j, int k) {
     return (i + 2) + b.PI * ((j + 2) + b.PJ * (k + 2));
 }
 __device__ inline double* slot(const DevBlock& b, int s) { return b.base + (size_t)s * (size_t)b.ncell; }
+// row pitch of a block of NI nodes in i (the ghost extent NI+5 rounded up to a multiple of 4)
+__host__ __device__ inline int padded_pi(int ni) { return (ni + 5 + 3) & ~3; }
+
 __device__ inline float* fslot(const DevBlock& b, int s) { return b.fbase + (size_t)s * (size_t)b.ncell; }
 // slot s in the arithmetic type R: the FP64 arrays, or their FP32 copies in the mixed path
 template <typename R> __device__ inline R* rs(const DevBlock& b, int s);

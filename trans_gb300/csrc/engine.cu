@@ -13,7 +13,7 @@ namespace eng {
 
 const char* const kclass_name[NKCLASS] = {"k_specrad", "k_bc_state", "k_bc_outlet", "k_prims", "k_mirror", "k_gradient",
     "k_shock_ghost", "k_bc_grad", "k_face_flux", "k_gather", "k_sst_fc1", "k_lusgs_prep", "k_sweep", "k_sweep_scatter",
-    "k_update", "k_update_u"};
+    "k_update", "k_update_u", "k_resid_tma"};
 
 int fail(Ctx* c, int code, const std::string& msg) {
     if (c) c->err = msg;
@@ -78,7 +78,7 @@ bool params_supported(const trans_params* p) {
 
 bool block_ok(const trans_block& tb) {
     if (tb.ni < 4 || tb.nj < 4 || tb.nk < 4 || tb.nconn < 0 || (tb.nconn > 0 && !tb.conn)) return false;
-    return (long long)(tb.ni + 5) * (tb.nj + 5) * (tb.nk + 5) <= (1LL << 30);
+    return (long long)padded_pi(tb.ni) * (tb.nj + 5) * (tb.nk + 5) <= (1LL << 30);
 }
 
 int validate_case(const trans_params* p, int nblocks, const trans_block* blocks) {
@@ -124,7 +124,7 @@ long long case_bytes(const trans_params* p, int nblocks, const trans_block* bloc
     const int precision = p->precision;
     long long padded = 0, interior = 0;
     for (int n = 0; n < nblocks; ++n) {
-        padded += (long long)(blocks[n].ni + 5) * (blocks[n].nj + 5) * (blocks[n].nk + 5);
+        padded += (long long)padded_pi(blocks[n].ni) * (blocks[n].nj + 5) * (blocks[n].nk + 5);
         interior += (long long)(blocks[n].ni - 1) * (blocks[n].nj - 1) * (blocks[n].nk - 1);
     }
     const long long elem = precision == TRANS_MIXED ? 4 : 8;
@@ -145,6 +145,17 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     CK(cudaMalloc(&c->d_sync, sizeof(SweepSync)));
     CK(cudaMallocHost(&c->h_sync, sizeof(SweepSync)));
     std::memset(c->h_sync, 0, sizeof(SweepSync));
+    CK(cudaMalloc(&c->d_kerr, sizeof(int)));
+    CK(cudaMemset(c->d_kerr, 0, sizeof(int)));
+    CK(cudaMallocHost(&c->h_kerr, sizeof(int)));
+    *c->h_kerr = 0;
+    // TRANS_RESID_TMA=0: the mixed path's residual from k_face_flux + k_gather instead of the
+    // TMA-staged tiles (for comparisons)
+    const char* rt = std::getenv("TRANS_RESID_TMA");
+    if (rt && std::string(rt) == "0") c->resid_tma = 0;
+    // TRANS_RESID_SPIN=n: polls of the tile staging wait before it gives up (for tests)
+    const char* rsp = std::getenv("TRANS_RESID_SPIN");
+    if (rsp) c->resid_spin = (unsigned)std::max(0L, std::atol(rsp));
     // TRANS_GRAPHS=0 turns the whole-iteration graphs off (every iteration launched directly)
     const char* gr = std::getenv("TRANS_GRAPHS");
     if (gr && std::string(gr) == "0") c->graphs = false;
@@ -191,7 +202,8 @@ int ctx_init(Ctx* c, int precision, long long budget) {
 
 void free_worklists(Ctx* c) {
     dfree(c->d_blk); dfree(c->d_off); dfree(c->d_cell); dfree(c->d_ghost);
-    for (int d = 0; d < 3; ++d) dfree(c->d_face[d]);
+    for (int d = 0; d < 3; ++d) { dfree(c->d_face[d]); dfree(c->d_rtiles[d]); c->n_rtiles[d] = 0; }
+    dfree(c->d_rmaps);
     dfree(c->d_bc); dfree(c->d_outlet); dfree(c->d_lines); dfree(c->d_sweep); dfree(c->d_plane_off);
     dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq_save); dfree(c->d_parts); dfree(c->d_pc);
     dfree(c->d_cdev); dfree(c->d_stage); dfree(c->d_tile_first); dfree(c->d_norms);
@@ -217,6 +229,8 @@ void ctx_free(Ctx* c) {
     c->cases.clear();
     dfree(c->d_sync);
     if (c->h_sync) { cudaFreeHost(c->h_sync); c->h_sync = nullptr; }
+    dfree(c->d_kerr);
+    if (c->h_kerr) { cudaFreeHost(c->h_kerr); c->h_kerr = nullptr; }
     if (c->copy_done) { cudaEventDestroy(c->copy_done); c->copy_done = nullptr; }
     if (c->stream) { cudaStreamDestroy(c->stream); c->stream = nullptr; }
 }
@@ -263,7 +277,7 @@ int case_add(Ctx* c, const trans_params* p, int nblocks, const trans_block* bloc
         std::memset(&b, 0, sizeof(b));
         b.NI = tb.ni; b.NJ = tb.nj; b.NK = tb.nk;
         b.NI1 = b.NI - 1; b.NJ1 = b.NJ - 1; b.NK1 = b.NK - 1;
-        b.PI = b.NI + 5; b.PJ = b.NJ + 5; b.PK = b.NK + 5;
+        b.PI = padded_pi(b.NI); b.PJ = b.NJ + 5; b.PK = b.NK + 5;
         b.ncell = b.PI * b.PJ * b.PK;
         b.nint = b.NI1 * b.NJ1 * b.NK1;
         total += (size_t)nslot * (size_t)b.ncell;

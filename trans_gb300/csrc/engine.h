@@ -44,7 +44,7 @@ struct CaseRec {
 
 // kernel classes of trans_kernel_times
 enum KClass { K_SPECRAD, K_BC_STATE, K_BC_OUTLET, K_PRIMS, K_MIRROR, K_GRADIENT, K_SHOCK_GHOST, K_BC_GRAD,
-              K_FACE, K_GATHER, K_SST_FC1, K_PREP, K_SWEEP, K_SCATTER, K_UPDATE, K_UPDATE_U, NKCLASS };
+              K_FACE, K_GATHER, K_SST_FC1, K_PREP, K_SWEEP, K_SCATTER, K_UPDATE, K_UPDATE_U, K_RESID_TMA, NKCLASS };
 extern const char* const kclass_name[NKCLASS];
 
 constexpr int GRAPH_ITERS = 8;            // outer iterations per replay of the iteration graph
@@ -69,6 +69,15 @@ struct Ctx {
     std::vector<Tile> cell_tiles, face_tiles[3], ghost_tiles;
     Tile *d_cell = nullptr, *d_face[3] = {nullptr, nullptr, nullptr}, *d_ghost = nullptr;
     std::vector<int> cell_tile_blk;      // block of each cell tile (norm reduction)
+    // mixed path: the residual from TMA-staged tiles (one tile list per face direction, NRMAP
+    // tensor maps per block over its FP32 slots); resid_tma = 0 uses k_face_flux + k_gather
+    int resid_tma = 1;
+    ResidTile* d_rtiles[3] = {nullptr, nullptr, nullptr};
+    int n_rtiles[3] = {0, 0, 0};
+    void* d_rmaps = nullptr;
+    unsigned resid_spin = RT_WAIT_LIMIT; // polls of a tile's staging wait (TRANS_RESID_SPIN overrides)
+    int* d_kerr = nullptr;               // set by a kernel whose bounded wait gave up
+    int* h_kerr = nullptr;               // pinned
     std::vector<BCEntry> bc, outlet;
     std::vector<OutletLine> lines;
     BCEntry *d_bc = nullptr, *d_outlet = nullptr;

@@ -4,8 +4,25 @@
 #define TG_NAME flux_launchers_f32
 #include "flux_inst.cuh"
 #include "kernels_mixed.cuh"
+#include "resid_tma.cuh"
 
 namespace tg {
+cudaError_t prepare_resid_tma() {
+    cudaError_t e = cudaFuncSetAttribute(k_resid_tma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rt_smem_bytes(1));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_resid_tma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rt_smem_bytes(2));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_resid_tma<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rt_smem_bytes(3));
+    return e;
+}
+void launch_resid_tma(int dir, cudaStream_t s, const DevBlock* blks, const ResidTile* tiles, int nt, const CaseDev* cdev,
+                      const void* maps, int* err, unsigned limit) {
+    if (nt <= 0) return;
+    const CUtensorMap* m = (const CUtensorMap*)maps;
+    if (dir == 1) k_resid_tma<1><<<nt, 32 * RT_D, rt_smem_bytes(1), s>>>(blks, tiles, cdev, m, err, limit);
+    else if (dir == 2) k_resid_tma<2><<<nt, RT_FACES, rt_smem_bytes(2), s>>>(blks, tiles, cdev, m, err, limit);
+    else k_resid_tma<3><<<nt, RT_FACES, rt_smem_bytes(3), s>>>(blks, tiles, cdev, m, err, limit);
+}
 void launch_specrad_mixed(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev) {
     if (nt > 0) k_specrad_mixed<<<nt, CELL_TILE, 0, s>>>(blks, tiles, cdev);
 }

@@ -12,6 +12,51 @@
 
 namespace tg {
 
+// ---------------------------------------------------------------------------------------
+// Residual-norm partials (Time/TIME_Update_V.F90:106-146, 892-908): sums of |D/V|^2, maxima of
+// |D/V| and the NaN flag.  A CTA reduces them by warp shuffles -- lane l takes lane l+w for
+// w = 16, 8, 4, 2, 1 -- then warp 0 over the warps' results, a fixed order.  The maximum of
+// |D1/V1| keeps the later cell on ties (IF(DUa<=DR), :135).
+// ---------------------------------------------------------------------------------------
+__device__ inline NormPart norm_identity() {
+    NormPart a;
+    a.sa = 0; a.ma = -1; a.sk = 0; a.mk = 0; a.so = 0; a.mo = 0; a.ia = -1; a.nan = 0; a.pad_ = 0;
+    return a;
+}
+__device__ inline void norm_join(NormPart& a, const NormPart& b) {
+    a.sa += b.sa; a.sk += b.sk; a.so += b.so;
+    if (b.ma > a.ma || (b.ma == a.ma && b.ia > a.ia)) { a.ma = b.ma; a.ia = b.ia; }
+    a.mk = dmax(a.mk, b.mk); a.mo = dmax(a.mo, b.mo);
+    a.nan |= b.nan;
+}
+__device__ inline NormPart norm_shfl_down(const NormPart& a, int w) {
+    const unsigned full = 0xffffffffu;
+    NormPart b;
+    b.sa = __shfl_down_sync(full, a.sa, w); b.ma = __shfl_down_sync(full, a.ma, w);
+    b.sk = __shfl_down_sync(full, a.sk, w); b.mk = __shfl_down_sync(full, a.mk, w);
+    b.so = __shfl_down_sync(full, a.so, w); b.mo = __shfl_down_sync(full, a.mo, w);
+    b.ia = __shfl_down_sync(full, a.ia, w); b.nan = __shfl_down_sync(full, a.nan, w);
+    b.pad_ = 0;
+    return b;
+}
+__device__ inline NormPart norm_reduce_warp(NormPart a) {
+    for (int w = 16; w > 0; w >>= 1) {
+        const NormPart o = norm_shfl_down(a, w);
+        if ((int)(threadIdx.x & 31) + w < 32) norm_join(a, o);
+    }
+    return a;
+}
+// the CTA's reduction, valid in thread 0 (blockDim a multiple of 32); every thread calls it
+__device__ inline NormPart norm_reduce_cta(NormPart a) {
+    __shared__ NormPart s_warp[32];
+    a = norm_reduce_warp(a);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) s_warp[wid] = a;
+    __syncthreads();
+    if (wid == 0) a = norm_reduce_warp(lane < (int)(blockDim.x >> 5) ? s_warp[lane] : norm_identity());
+    return a;
+}
+
 #ifdef TG_COMMON_KERNELS
 // ---------------------------------------------------------------------------------------
 // Time/SpectralRadius.F90:47-180
@@ -535,66 +580,54 @@ __global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __re
 //   Space/DIFFUSION_Centered.F90, Space/TURBTWO_DIFFUSION_Centered.F90,
 //   Space/CONVECT_MUSCL.F90 | Space/CONVECT_MDCD.F90, Space/TURBTWO_CONVECT_MUSCL.F90,
 //   Space/CONVECT_Roe_Original.F90 | Space/CONVECT_AUSMPW_Plus.F90, Space/TURBTWO_CONVECT_Upwind.F90
+//
+// face_flux_body computes the NFX fluxes of one face from an accessor q: q.v(slot, o) is the
+// slot's value at the cell o steps along DIR from the face's cell c (o = -1 is the cell on the
+// face's minus side).  The kernels differ only in where the values come from: FaceGlobal reads
+// the slot arrays (k_face_flux); the shared-memory tiles of the mixed path read a staged copy.
 // ---------------------------------------------------------------------------------------
-#ifndef TG_FACE_MINB
-#define TG_FACE_MINB 5      // resident CTAs per SM asked of the FP32 face-flux kernels (96 registers)
-#endif
-template <typename R, int DIR>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
-                                                          const CaseDev* __restrict__ cdev) {
-    const Tile t = tiles[blockIdx.x];
-    if ((int)threadIdx.x >= t.count) return;
-    const DevBlock b = blks[t.blk];
-    const ParamsT<R> p = cparams<R>(cdev[b.cs]);
-    const int turb = cdev[b.cs].turb;
-    int n = t.start + threadIdx.x;
-    const int ni = DIR == 1 ? b.NI : b.NI1, nj = DIR == 2 ? b.NJ : b.NJ1;
-    int i = n % ni + 1, j = (n / ni) % nj + 1, k = n / (ni * nj) + 1;
-    const int d = DIR - 1;
-    const int s = DIR == 1 ? 1 : (DIR == 2 ? b.PI : b.PI * b.PJ);
-    const int c = cidx(b, i, j, k);
-    const int cm = c - s, cp = c + s;
-    const R* al = rs<R>(b, S_ALAGM + d);
-    const R* ainv = rs<R>(b, S_AINV + d);
-    const R* pu = rs<R>(b, S_PRIM);
-    const R* pv = rs<R>(b, S_PRIM + 1);
-    const R* pw = rs<R>(b, S_PRIM + 2);
-    const R* pk = rs<R>(b, S_PRIM + 3);
-    const R* po = rs<R>(b, S_PRIM + 4);
-    const R* PT = rs<R>(b, S_T);
-    const R* PPp = rs<R>(b, S_PP);
-    const R* SDd = rs<R>(b, S_SD + 3 * d);
-    const size_t nc = (size_t)b.ncell;
-    R* FX = rs<R>(b, S_FX + NFX * d);
+template <typename R>
+struct FaceGlobal {
+    const DevBlock& b;
+    int c, s;
+    __device__ R v(int slot, int o) const { return R(rs<R>(b, slot)[c + o * s]); }
+};
+
+template <typename R, int DIR, class A>
+__device__ __forceinline__ void face_flux_body(const ParamsT<R>& p, int turb, const A& q, R* F) {
+    constexpr int d = DIR - 1;
+    constexpr int AL = S_ALAGM + d, AIN = S_AINV + d, SDD = S_SD + 3 * d;
+    // face average of a slot at the face o steps from this one (SPACEINTERP_GetSurfCenterVars)
+    auto fa = [&](int slot, int o) { return (q.v(AL, o) * q.v(slot, o - 1) + q.v(AL, o - 1) * q.v(slot, o)) * q.v(AIN, o); };
     // ---------------- viscous flux (DIFFUSION_Centered) ----------------
-    const bool wall = rs<R>(b, S_WALL + d)[c] != R(0.0);
-    const R vinv = rs<R>(b, S_VINV + d)[c];
-    const R vall = rs<R>(b, S_VOL)[cm] * vinv;
-    const R valr = rs<R>(b, S_VOL)[c] * vinv;
+    const bool wall = q.v(S_WALL + d, 0) != R(0.0);
+    const R vinv = q.v(S_VINV + d, 0);
+    const R vall = q.v(S_VOL, -1) * vinv;
+    const R valr = q.v(S_VOL, 0) * vinv;
     const R alsinv = wall ? R(0.0) : R(vinv);
-    const R* qv[4] = {pu, pv, pw, PT};
+    constexpr int qv[4] = {S_PRIM, S_PRIM + 1, S_PRIM + 2, S_T};
     R g[4][3];
-    for (int q = 0; q < 4; ++q) {
-        const R* Q = qv[q];
-        R disfpp = (favg<R>(Q, al, ainv, cp, s));
-        R disfnn = (favg<R>(Q, al, ainv, cm, s));
-        R disfp = R(Q[c]), disfn = R(Q[cm]);
-        const R* DQ0 = rs<R>(b, S_DQ + 3 * q);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int Q = qv[k];
+        R disfpp = fa(Q, 1);
+        R disfnn = fa(Q, -1);
+        R disfp = q.v(Q, 0), disfn = q.v(Q, -1);
+#pragma unroll
         for (int m = 0; m < 3; ++m) {
-            const R* G = DQ0 + (size_t)m * nc;
-            R xL = R(vall) * R(G[cm]) + R(valr) * R(G[c]);
-            const R* S = SDd + (size_t)m * nc;
-            R cmv = alsinv * (-R(S[cp]) * (disfpp - disfp) - R(S[cm]) * (disfn - disfnn) + R(S[c]) * (disfp - disfn));
-            g[q][m] = cmv + xL;
+            const int G = S_DQ + 3 * k + m;
+            R xL = vall * q.v(G, -1) + valr * q.v(G, 0);
+            R cmv = alsinv * (-q.v(SDD + m, 1) * (disfpp - disfp) - q.v(SDD + m, -1) * (disfn - disfnn) +
+                              q.v(SDD + m, 0) * (disfp - disfn));
+            g[k][m] = cmv + xL;
         }
     }
-    const R a0 = R(al[c]), a1 = R(al[cm]);
-    const R ai = R(ainv[c]);
+    const R a0 = q.v(AL, 0), a1 = q.v(AL, -1);
+    const R ai = q.v(AIN, 0);
     const R all = a0 * ai, alr = a1 * ai;
-    const R TTL = (favg<R>(PT, al, ainv, c, s));
+    const R TTL = fa(S_T, 0);
     const R RmiuL = mu_suth<R>(p, TTL);
-    const R* Rm = rs<R>(b, S_RMIU);
-    R RmiuTL = all * R(Rm[cm]) + alr * R(Rm[c]);
+    R RmiuTL = all * q.v(S_RMIU, -1) + alr * q.v(S_RMIU, 0);
     if (wall) RmiuTL = R(0.0);
     {
         const R NMD = R(-2.0 / 3.0);
@@ -611,36 +644,36 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
         R Tzx = RmiuL * (DuDzL + DwDxL) + RmiuTL * (DuDzL + DwDxL);
         R cp_ = R(1.4) * R(p.PPF) / R(1.4 - 1.0);
         R akmu = cp_ * (RmiuL / R(0.72) + RmiuTL / R(0.9));
-        R ucc = (favg<R>(pu, al, ainv, c, s)), vcc = (favg<R>(pv, al, ainv, c, s)), wcc = (favg<R>(pw, al, ainv, c, s));
+        R ucc = fa(S_PRIM, 0), vcc = fa(S_PRIM + 1, 0), wcc = fa(S_PRIM + 2, 0);
         R Phix = akmu * DTDxL + ucc * Txx + vcc * Txy + wcc * Tzx;
         R Phiy = akmu * DTDyL + ucc * Txy + vcc * Tyy + wcc * Tyz;
         R Phiz = akmu * DTDzL + ucc * Tzx + vcc * Tyz + wcc * Tzz;
-        R Dx = R(SDd[c]), Dy = R(SDd[c + nc]), Dz = R(SDd[c + 2 * nc]);
+        R Dx = q.v(SDD, 0), Dy = q.v(SDD + 1, 0), Dz = q.v(SDD + 2, 0);
         R Ref = R(p.Ref);
-        FX[(size_t)FX_VX * nc + c] = ((Txx * Dx + Txy * Dy + Tzx * Dz) / Ref);
-        FX[(size_t)FX_VY * nc + c] = ((Txy * Dx + Tyy * Dy + Tyz * Dz) / Ref);
-        FX[(size_t)FX_VZ * nc + c] = ((Tzx * Dx + Tyz * Dy + Tzz * Dz) / Ref);
-        FX[(size_t)FX_VE * nc + c] = ((Phix * Dx + Phiy * Dy + Phiz * Dz) / Ref);
+        F[FX_VX] = (Txx * Dx + Txy * Dy + Tzx * Dz) / Ref;
+        F[FX_VY] = (Txy * Dx + Tyy * Dy + Tyz * Dz) / Ref;
+        F[FX_VZ] = (Tzx * Dx + Tyz * Dy + Tzz * Dz) / Ref;
+        F[FX_VE] = (Phix * Dx + Phiy * Dy + Phiz * Dz) / Ref;
     }
     // ---------------- k-omega diffusion (TURBTWO_DIFFUSION_Centered) ----------------
     if (turb) {
         R gt[2][3];
-        const R* qt[2] = {pk, po};
-        for (int q = 0; q < 2; ++q) {
-            const R* Q = qt[q];
-            R disfpp = (favg<R>(Q, al, ainv, cp, s));
-            R disfnn = (favg<R>(Q, al, ainv, cm, s));
-            R disfp = R(Q[c]), disfn = R(Q[cm]);
-            const R* DQ0 = rs<R>(b, S_DQ + 12 + 3 * q);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int Q = S_PRIM + 3 + k;
+            R disfpp = fa(Q, 1);
+            R disfnn = fa(Q, -1);
+            R disfp = q.v(Q, 0), disfn = q.v(Q, -1);
+#pragma unroll
             for (int m = 0; m < 3; ++m) {
-                const R* G = DQ0 + (size_t)m * nc;
-                R xL = R(vall) * R(G[cm]) + R(valr) * R(G[c]);
-                const R* S = SDd + (size_t)m * nc;
-                R cmv = alsinv * (-R(S[cp]) * (disfpp - disfp) - R(S[cm]) * (disfn - disfnn) + R(S[c]) * (disfp - disfn));
-                gt[q][m] = cmv + xL;
+                const int G = S_DQ + 12 + 3 * k + m;
+                R xL = vall * q.v(G, -1) + valr * q.v(G, 0);
+                R cmv = alsinv * (-q.v(SDD + m, 1) * (disfpp - disfp) - q.v(SDD + m, -1) * (disfn - disfnn) +
+                                  q.v(SDD + m, 0) * (disfp - disfn));
+                gt[k][m] = cmv + xL;
             }
         }
-        R TTLt = all * R(PT[cm]) + alr * R(PT[c]);
+        R TTLt = all * q.v(S_T, -1) + alr * q.v(S_T, 0);
         R RmiuLt = mu_suth_nocs<R>(p, TTLt);
         const R Ref = R(p.Ref);
         R SigkAB, SigoAB;
@@ -648,17 +681,15 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
             SigkAB = R(p.Sigk1);
             SigoAB = R(p.Sigo1);
         } else {
-            const R* V1 = rs<R>(b, S_V);
-            R DEN0 = R(V1[c]), TKK0 = R(pk[c]), TOO0 = R(po[c]);
-            R DEN1 = R(V1[cm]), TKK1 = R(pk[cm]), TOO1 = R(po[cm]);
+            R DEN0 = q.v(S_V, 0), TKK0 = q.v(S_PRIM + 3, 0), TOO0 = q.v(S_PRIM + 4, 0);
+            R DEN1 = q.v(S_V, -1), TKK1 = q.v(S_PRIM + 3, -1), TOO1 = q.v(S_PRIM + 4, -1);
             R Den = all * DEN1 + alr * DEN0;
             R TKK = all * TKK1 + alr * TKK0;
             R TOO = all * TOO1 + alr * TOO0;
             R dTKO = gt[0][0] * gt[1][0] + gt[0][1] * gt[1][1] + gt[0][2] * gt[1][2];
             R Sigo2 = R(p.Sigo2), Bs = R(p.Beta_star);
             R CDKO = dmax(R(2.0) * Den * Sigo2 / TOO * (dTKO), R(1.0e-10));
-            const R* Dst = rs<R>(b, S_DST);
-            R distfc = alr * R(Dst[c]) + all * R(Dst[cm]);
+            R distfc = alr * q.v(S_DST, 0) + all * q.v(S_DST, -1);
             R arg1 = dmax(sqrt(TKK) / Bs / TOO / distfc / Ref, R(500.0) * RmiuLt / Den / distfc / distfc / TOO / Ref / Ref);
             arg1 = dmin(arg1, R(4.0) * Den * Sigo2 * TKK / CDKO / distfc / distfc);
             R a2 = arg1 * arg1;
@@ -668,60 +699,62 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
         }
         R vmute = RmiuLt + RmiuTL * SigkAB;
         R vmuoq = RmiuLt + RmiuTL * SigoAB;
-        R Dx = R(SDd[c]), Dy = R(SDd[c + nc]), Dz = R(SDd[c + 2 * nc]);
-        FX[(size_t)FX_TK * nc + c] = ((vmute * (gt[0][0] * Dx + gt[0][1] * Dy + gt[0][2] * Dz)) / Ref);
-        FX[(size_t)FX_TO * nc + c] = ((vmuoq * (gt[1][0] * Dx + gt[1][1] * Dy + gt[1][2] * Dz)) / Ref);
+        R Dx = q.v(SDD, 0), Dy = q.v(SDD + 1, 0), Dz = q.v(SDD + 2, 0);
+        F[FX_TK] = (vmute * (gt[0][0] * Dx + gt[0][1] * Dy + gt[0][2] * Dz)) / Ref;
+        F[FX_TO] = (vmuoq * (gt[1][0] * Dx + gt[1][1] * Dy + gt[1][2] * Dz)) / Ref;
     }
     // ---------------- reconstruction ----------------
     R qL[7], qR[7];
-    const R* qc[5] = {pu, pv, pw, PPp, PT};
+    constexpr int qc[5] = {S_PRIM, S_PRIM + 1, S_PRIM + 2, S_PP, S_T};
     R gama = R(0.0);
     if (p.Kind_Spatial <= 2) {     // CONVECT_MUSCL (2) or CONVECT_MUSCL2 (1): the limiter differs
         const bool m2 = p.Kind_Spatial == 1;
-        for (int q = 0; q < 5; ++q) {
-            const R* Q = qc[q];
-            R fm = (favg<R>(Q, al, ainv, cm, s)), f0 = (favg<R>(Q, al, ainv, c, s)), fp = (favg<R>(Q, al, ainv, cp, s));
-            R q1 = R(Q[cm]), q0 = R(Q[c]);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int Q = qc[k];
+            R fm = fa(Q, -1), f0 = fa(Q, 0), fp = fa(Q, 1);
+            R q1 = q.v(Q, -1), q0 = q.v(Q, 0);
             R DR = f0 - q1, DL = q1 - fm;
-            qL[q] = q1 + (m2 ? muscl2_limiter(DR, DL) : alimiter(DR, DL));
+            qL[k] = q1 + (m2 ? muscl2_limiter(DR, DL) : alimiter(DR, DL));
             DR = fp - q0; DL = q0 - f0;
-            qR[q] = q0 - (m2 ? muscl2_limiter(DL, DR) : alimiter(DL, DR));
+            qR[k] = q0 - (m2 ? muscl2_limiter(DL, DR) : alimiter(DL, DR));
         }
     } else {                       // CONVECT_MDCD (3) or CONVECT_MDCDHYB (4)
         const bool hyb = p.Kind_Spatial == 4;
-        const R* sh = rs<R>(b, S_SHOCK);
-        R sensor = R(sh[c - 3 * s]);
-        sensor = dmax(sensor, R(sh[c - 2 * s]));
-        sensor = dmax(sensor, R(sh[c - s]));
-        sensor = dmax(sensor, R(sh[c]));
-        sensor = dmax(sensor, R(sh[c + s]));
-        sensor = dmax(sensor, R(sh[c + 2 * s]));
+        R sensor = q.v(S_SHOCK, -3);
+        sensor = dmax(sensor, q.v(S_SHOCK, -2));
+        sensor = dmax(sensor, q.v(S_SHOCK, -1));
+        sensor = dmax(sensor, q.v(S_SHOCK, 0));
+        sensor = dmax(sensor, q.v(S_SHOCK, 1));
+        sensor = dmax(sensor, q.v(S_SHOCK, 2));
         if (DIR == 3 && !hyb) sensor = dmax(sensor, R(0.0));
         gama = R(p.gama_min) + sensor * (R(p.gama_max) - R(p.gama_min));
         // MDCDHYB: MUSCL states where the sensor reaches F_limiter2 (Space/CONVECT_MDCDHYB.F90:118-120, 175-177)
         const bool muscl = hyb && sensor >= R(p.F_limiter2);
-        for (int q = 0; q < 5; ++q) {
-            const R* Q = qc[q];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int Q = qc[k];
             R s6[6];
-            for (int o = 0; o < 6; ++o) s6[o] = R(Q[c + (o - 3) * s]);
+#pragma unroll
+            for (int o = 0; o < 6; ++o) s6[o] = q.v(Q, o - 3);
             if (muscl) {
-                qL[q] = s6[2] + R(0.5) * alimiter(s6[3] - s6[2], s6[2] - s6[1]);
-                qR[q] = s6[3] - R(0.5) * alimiter(s6[3] - s6[2], s6[4] - s6[3]);
+                qL[k] = s6[2] + R(0.5) * alimiter(s6[3] - s6[2], s6[2] - s6[1]);
+                qR[k] = s6[3] - R(0.5) * alimiter(s6[3] - s6[2], s6[4] - s6[3]);
             } else {
-                mdcd_pair(s6, gama, qL[q], qR[q]);
+                mdcd_pair(s6, gama, qL[k], qR[k]);
             }
         }
     }
     if (turb) {
-        const R* qk[2] = {pk, po};
-        for (int q = 0; q < 2; ++q) {
-            const R* Q = qk[q];
-            R fm = (favg<R>(Q, al, ainv, cm, s)), f0 = (favg<R>(Q, al, ainv, c, s)), fp = (favg<R>(Q, al, ainv, cp, s));
-            R q1 = R(Q[cm]), q0 = R(Q[c]);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int Q = S_PRIM + 3 + k;
+            R fm = fa(Q, -1), f0 = fa(Q, 0), fp = fa(Q, 1);
+            R q1 = q.v(Q, -1), q0 = q.v(Q, 0);
             R DR = f0 - q1, DL = q1 - fm;
-            qL[5 + q] = q1 + alimiter(DR, DL);
+            qL[5 + k] = q1 + alimiter(DR, DL);
             DR = fp - q0; DL = q0 - f0;
-            qR[5 + q] = q0 - alimiter(DL, DR);
+            qR[5 + k] = q0 - alimiter(DL, DR);
         }
     }
     // ---------------- frame speeds of the two states (rotating frame) ----------------
@@ -733,47 +766,48 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
     // outside the face loops, :450-521); CONVECT_MDCDHYB leaves every face at the average.
     R rLo = R(0.0), rRo = R(0.0);
     if (p.omega0 != R(0.0) && p.Kind_Roe != 3) {
-        const R* rad = rs<R>(b, S_RAD);
         R rl, rr;
         if (p.Kind_Spatial <= 2) {
             const bool m2 = p.Kind_Spatial == 1;
-            R fm = favg<R>(rad, al, ainv, cm, s), f0 = favg<R>(rad, al, ainv, c, s), fp = favg<R>(rad, al, ainv, cp, s);
-            R q1 = R(rad[cm]), q0 = R(rad[c]);
+            R fm = fa(S_RAD, -1), f0 = fa(S_RAD, 0), fp = fa(S_RAD, 1);
+            R q1 = q.v(S_RAD, -1), q0 = q.v(S_RAD, 0);
             R DR = f0 - q1, DL = q1 - fm;
             rl = q1 + (m2 ? muscl2_limiter(DR, DL) : alimiter(DR, DL));
             DR = fp - q0; DL = q0 - f0;
             rr = q0 - (m2 ? muscl2_limiter(DL, DR) : alimiter(DL, DR));
         } else if (p.Kind_Spatial == 3 && DIR != 3) {
             R s6[6];
-            for (int o = 0; o < 6; ++o) s6[o] = R(rad[c + (o - 3) * s]);
+#pragma unroll
+            for (int o = 0; o < 6; ++o) s6[o] = q.v(S_RAD, o - 3);
             mdcd_pair(s6, gama, rl, rr);
         } else {
-            rl = favg<R>(rad, al, ainv, c, s);
+            rl = fa(S_RAD, 0);
             rr = rl;
         }
         rLo = rl * R(p.omega0);
         rRo = rr * R(p.omega0);
     }
     // ---------------- inviscid flux ----------------
-    R sav1 = R(SDd[c]), sav2 = R(SDd[c + nc]), sav3 = R(SDd[c + 2 * nc]);
-    R sav = R(rs<R>(b, S_GRAD + d)[c]);
+    R sav1 = q.v(SDD, 0), sav2 = q.v(SDD + 1, 0), sav3 = q.v(SDD + 2, 0);
+    R sav = q.v(S_GRAD + d, 0);
     R f[5];
     if (p.Kind_Roe == 2) {          // rotated Roe: the contribution already carries |S|
-        const R* fs = rs<R>(b, S_FSCH);
-        const R Funscheme = (R(fs[cm]) + R(fs[c])) / R(2.);
+        const R Funscheme = (q.v(S_FSCH, -1) + q.v(S_FSCH, 0)) / R(2.);
         roe_rotated<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav,
                        rLo, rRo, Funscheme, f);
-        for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = f[L];
+#pragma unroll
+        for (int L = 0; L < 5; ++L) F[FX_C0 + L] = f[L];
     } else {
         if (p.Kind_Roe == 1) {
             // preconditioning reads VL(d,8), the face-averaged eddy viscosity (0 while turbulence
             // is off), and Alagm(d) of the face's cell (Space/CONVECT_Roe_Original.F90:86-87)
-            const R RmiuTf = (p.IF_Precondition && turb) ? favg<R>(rs<R>(b, S_RMIU), al, ainv, c, s) : R(0.0);
-            roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, rLo, rRo, f, RmiuTf,
-                        R(al[c]));
+            const R RmiuTf = (p.IF_Precondition && turb) ? fa(S_RMIU, 0) : R(0.0);
+            roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, rLo, rRo,
+                        f, RmiuTf, a0);
         } else
             ausmpw_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
-        for (int L = 0; L < 5; ++L) FX[(size_t)(FX_C0 + L) * nc + c] = (f[L] * sav);
+#pragma unroll
+        for (int L = 0; L < 5; ++L) F[FX_C0 + L] = f[L] * sav;
     }
     if (turb) {
         R rcpcv = R(p.PPF);
@@ -784,11 +818,43 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
         const R small = R(1.e-10);
         R eigTKO = R(0.5) * dmax(fabs(ulnormal), fabs(urnormal));
         R TKL = dmax(qL[5], small), TKR = dmax(qR[5], small);
-        R dTK = R(-0.5) * (rulnormal * TKL + rurnormal * TKR - eigTKO * (DENR * TKR - DENL * TKL));
+        F[FX_CK] = R(-0.5) * (rulnormal * TKL + rurnormal * TKR - eigTKO * (DENR * TKR - DENL * TKL));
         R TOL = dmax(qL[6], small), TOR = dmax(qR[6], small);
-        R dTO = R(-0.5) * (rulnormal * TOL + rurnormal * TOR - eigTKO * (DENR * TOR - DENL * TOL));
-        FX[(size_t)FX_CK * nc + c] = dTK;
-        FX[(size_t)FX_CO * nc + c] = dTO;
+        F[FX_CO] = R(-0.5) * (rulnormal * TOL + rurnormal * TOR - eigTKO * (DENR * TOR - DENL * TOL));
+    }
+}
+
+#ifndef TG_FACE_MINB
+#define TG_FACE_MINB 5      // resident CTAs per SM asked of the FP32 face-flux kernels (96 registers)
+#endif
+// one thread per face; the fluxes go to the FX slots, k_gather sums them per cell
+template <typename R, int DIR>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
+                                                          const CaseDev* __restrict__ cdev) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    const ParamsT<R> p = cparams<R>(cdev[b.cs]);
+    const int turb = cdev[b.cs].turb;
+    int n = t.start + threadIdx.x;
+    const int ni = DIR == 1 ? b.NI : b.NI1, nj = DIR == 2 ? b.NJ : b.NJ1;
+    int i = n % ni + 1, j = (n / ni) % nj + 1, k = n / (ni * nj) + 1;
+    const int s = DIR == 1 ? 1 : (DIR == 2 ? b.PI : b.PI * b.PJ);
+    const int c = cidx(b, i, j, k);
+    const FaceGlobal<R> q{b, c, s};
+    R F[NFX];
+    face_flux_body<R, DIR>(p, turb, q, F);
+    const size_t nc = (size_t)b.ncell;
+    R* FX = rs<R>(b, S_FX + NFX * (DIR - 1));
+#pragma unroll
+    for (int m = 0; m < FX_TK; ++m) FX[(size_t)m * nc + c] = F[m];
+#pragma unroll
+    for (int m = FX_C0; m < FX_CK; ++m) FX[(size_t)m * nc + c] = F[m];
+    if (turb) {
+        FX[(size_t)FX_TK * nc + c] = F[FX_TK];
+        FX[(size_t)FX_TO * nc + c] = F[FX_TO];
+        FX[(size_t)FX_CK * nc + c] = F[FX_CK];
+        FX[(size_t)FX_CO * nc + c] = F[FX_CO];
     }
 }
 
@@ -1762,10 +1828,6 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
     const DevBlock b = blks[t.blk];
     const Params p = cdev[b.cs].p;
     const int turb_upd = cdev[b.cs].turb_upd;
-    __shared__ double s_sum[3][256];
-    __shared__ double s_max[3][256];
-    __shared__ long long s_idx[256];
-    __shared__ int s_nan[256];
     int tid = threadIdx.x;
     double sa = 0, ma = -1, sk = 0, mk = 0, so = 0, mo = 0;
     long long ia = -1;
@@ -1843,29 +1905,10 @@ __global__ void k_update(const DevBlock* __restrict__ blks, const Tile* __restri
             sst_update(p, b, c, d_fp32, d6, d7, pRo, mu_suth<double>(p, TT));
         }
     }
-    s_sum[0][tid] = sa; s_sum[1][tid] = sk; s_sum[2][tid] = so;
-    s_max[0][tid] = ma; s_max[1][tid] = mk; s_max[2][tid] = mo;
-    s_idx[tid] = ia; s_nan[tid] = nanf;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (tid < w) {
-            for (int q = 0; q < 3; ++q) s_sum[q][tid] += s_sum[q][tid + w];
-            // max of |D1/V1| with the later cell winning ties (IF(DUa<=DR), TIME_Update_V.F90:135)
-            double a = s_max[0][tid], bb = s_max[0][tid + w];
-            if (bb > a || (bb == a && s_idx[tid + w] > s_idx[tid])) { s_max[0][tid] = bb; s_idx[tid] = s_idx[tid + w]; }
-            s_max[1][tid] = dmax(s_max[1][tid], s_max[1][tid + w]);
-            s_max[2][tid] = dmax(s_max[2][tid], s_max[2][tid + w]);
-            s_nan[tid] |= s_nan[tid + w];
-        }
-        __syncthreads();
-    }
-    if (tid == 0) {
-        NormPart P;
-        P.sa = s_sum[0][0]; P.sk = s_sum[1][0]; P.so = s_sum[2][0];
-        P.ma = s_max[0][0]; P.mk = s_max[1][0]; P.mo = s_max[2][0];
-        P.ia = s_idx[0]; P.nan = s_nan[0]; P.pad_ = 0;
-        parts[blockIdx.x] = P;
-    }
+    NormPart P;
+    P.sa = sa; P.ma = ma; P.sk = sk; P.mk = mk; P.so = so; P.mo = mo; P.ia = ia; P.nan = nanf; P.pad_ = 0;
+    P = norm_reduce_cta(P);
+    if (tid == 0) parts[blockIdx.x] = P;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1879,10 +1922,6 @@ __global__ void k_rk_update(const DevBlock* __restrict__ blks, const Tile* __res
                             int d_fp32, int itr) {
     const Tile t = tiles[blockIdx.x];
     const DevBlock b = blks[t.blk];
-    __shared__ double s_sum[256];
-    __shared__ double s_max[256];
-    __shared__ long long s_idx[256];
-    __shared__ int s_nan[256];
     const int tid = threadIdx.x;
     double sa = 0, ma = -1;
     long long ia = -1;
@@ -1923,20 +1962,12 @@ __global__ void k_rk_update(const DevBlock* __restrict__ blks, const Tile* __res
             fslot(b, S_SVEL + 2)[c] = (float)w;
         }
     }
-    s_sum[tid] = sa; s_max[tid] = ma; s_idx[tid] = ia; s_nan[tid] = nanf;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (tid < w) {
-            s_sum[tid] += s_sum[tid + w];
-            const double a = s_max[tid], bb = s_max[tid + w];      // the later cell wins ties (IF(DUa<=DR))
-            if (bb > a || (bb == a && s_idx[tid + w] > s_idx[tid])) { s_max[tid] = bb; s_idx[tid] = s_idx[tid + w]; }
-            s_nan[tid] |= s_nan[tid + w];
-        }
-        __syncthreads();
-    }
-    if (tid == 0) {
-        NormPart& P = parts[blockIdx.x];
-        P.sa = s_sum[0]; P.ma = s_max[0]; P.ia = s_idx[0]; P.nan = s_nan[0]; P.pad_ = 0;
+    NormPart P = norm_identity();
+    P.sa = sa; P.ma = ma; P.ia = ia; P.nan = nanf;
+    P = norm_reduce_cta(P);
+    if (tid == 0) {      // the k and omega parts are written by k_rk_vupdate
+        NormPart& Q = parts[blockIdx.x];
+        Q.sa = P.sa; Q.ma = P.ma; Q.ia = P.ia; Q.nan = P.nan; Q.pad_ = 0;
     }
 }
 
@@ -1949,8 +1980,6 @@ __global__ void k_rk_vupdate(const DevBlock* __restrict__ blks, const Tile* __re
     const DevBlock b = blks[t.blk];
     const Params p = cdev[b.cs].p;
     const int turb_upd = cdev[b.cs].turb_upd;
-    __shared__ double s_sum[2][256];
-    __shared__ double s_max[2][256];
     const int tid = threadIdx.x;
     double sk = 0, mk = 0, so = 0, mo = 0;
     if (tid < t.count) {
@@ -1974,32 +2003,21 @@ __global__ void k_rk_vupdate(const DevBlock* __restrict__ blks, const Tile* __re
         const double DRk = fabs(d6 / v1), DRo = fabs(d7 / v1);
         sk = DRk * DRk; mk = DRk; so = DRo * DRo; mo = DRo;
     }
-    s_sum[0][tid] = sk; s_sum[1][tid] = so; s_max[0][tid] = mk; s_max[1][tid] = mo;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (tid < w)
-            for (int q = 0; q < 2; ++q) {
-                s_sum[q][tid] += s_sum[q][tid + w];
-                s_max[q][tid] = dmax(s_max[q][tid], s_max[q][tid + w]);
-            }
-        __syncthreads();
-    }
+    NormPart P = norm_identity();
+    P.sk = sk; P.so = so; P.mk = mk; P.mo = mo;
+    P = norm_reduce_cta(P);
     if (tid == 0) {
-        NormPart& P = parts[blockIdx.x];
-        P.sk = s_sum[0][0]; P.so = s_sum[1][0]; P.mk = s_max[0][0]; P.mo = s_max[1][0];
+        NormPart& Q = parts[blockIdx.x];
+        Q.sk = P.sk; Q.so = P.so; Q.mk = P.mk; Q.mo = P.mo;
     }
 }
 
 // Per-block norms from the per-tile partials (Time/TIME_Update_V.F90:116-146, 892-908): one
-// block of threads per solver block, fixed summation order (strided partial sums, then a
-// tree), the maximum of |D1/V1| with the later cell winning ties.
+// block of threads per solver block, fixed summation order (strided partial sums, then the
+// warp-shuffle reduction), the maximum of |D1/V1| with the later cell winning ties.
 __global__ void k_block_norms(const DevBlock* __restrict__ blks, const NormPart* __restrict__ parts,
                               const int* __restrict__ tile_first, BlockNorms* __restrict__ out) {
     const int bi = blockIdx.x, tid = threadIdx.x;
-    __shared__ double s_sum[3][256];
-    __shared__ double s_max[3][256];
-    __shared__ long long s_idx[256];
-    __shared__ int s_nan[256];
     double sa = 0, sk = 0, so = 0, ma = -1, mk = 0, mo = 0;
     long long ia = 0;
     int nan = 0;
@@ -2010,31 +2028,19 @@ __global__ void k_block_norms(const DevBlock* __restrict__ blks, const NormPart*
         mk = dmax(mk, P.mk); mo = dmax(mo, P.mo);
         nan |= P.nan;
     }
-    s_sum[0][tid] = sa; s_sum[1][tid] = sk; s_sum[2][tid] = so;
-    s_max[0][tid] = ma; s_max[1][tid] = mk; s_max[2][tid] = mo;
-    s_idx[tid] = ia; s_nan[tid] = nan;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (tid < w) {
-            for (int q = 0; q < 3; ++q) s_sum[q][tid] += s_sum[q][tid + w];
-            double a = s_max[0][tid], bb = s_max[0][tid + w];
-            if (bb > a || (bb == a && s_idx[tid + w] > s_idx[tid])) { s_max[0][tid] = bb; s_idx[tid] = s_idx[tid + w]; }
-            s_max[1][tid] = dmax(s_max[1][tid], s_max[1][tid + w]);
-            s_max[2][tid] = dmax(s_max[2][tid], s_max[2][tid + w]);
-            s_nan[tid] |= s_nan[tid + w];
-        }
-        __syncthreads();
-    }
+    NormPart P;
+    P.sa = sa; P.ma = ma; P.sk = sk; P.mk = mk; P.so = so; P.mo = mo; P.ia = ia; P.nan = nan; P.pad_ = 0;
+    P = norm_reduce_cta(P);
     if (tid == 0) {
         const DevBlock B = blks[bi];
         BlockNorms N;
-        N.DRSa = sqrt(s_sum[0][0] / B.NI1 / B.NJ1 / B.NK1);
-        N.DRSk = sqrt(s_sum[1][0] / B.NI1 / B.NJ1 / B.NK1);
-        N.DRSo = sqrt(s_sum[2][0] / B.NI1 / B.NJ1 / B.NK1);
-        N.DUa = s_max[0][0]; N.DUk = s_max[1][0]; N.DUo = s_max[2][0];
-        const long long i0 = s_idx[0];
+        N.DRSa = sqrt(P.sa / B.NI1 / B.NJ1 / B.NK1);
+        N.DRSk = sqrt(P.sk / B.NI1 / B.NJ1 / B.NK1);
+        N.DRSo = sqrt(P.so / B.NI1 / B.NJ1 / B.NK1);
+        N.DUa = P.ma; N.DUk = P.mk; N.DUo = P.mo;
+        const long long i0 = P.ia;
         N.Ima = (int)(i0 % B.NI1) + 1; N.Jma = (int)((i0 / B.NI1) % B.NJ1) + 1; N.Kma = (int)(i0 / ((long long)B.NI1 * B.NJ1)) + 1;
-        N.nan_flag = s_nan[0];
+        N.nan_flag = P.nan;
         out[bi] = N;
     }
 }
@@ -2066,7 +2072,7 @@ __global__ void k_geom_static(const DevBlock* __restrict__ blks, int nblk, long 
     int i = c % b.PI, j = (c / b.PI) % b.PJ, k = c / (b.PI * b.PJ);
     const int st[3] = {1, b.PI, b.PI * b.PJ};
     const int pos[3] = {i, j, k};
-    const int ext[3] = {b.PI, b.PJ, b.PK};
+    const int ext[3] = {b.NI + 5, b.PJ, b.PK};       // the ghost extent (row padding excluded)
     for (int d = 0; d < 3; ++d) {
         if (pos[d] >= 1) {
             const double* al = slot(b, S_ALAGM + d);

@@ -198,10 +198,6 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
     const DevBlock b = blks[t.blk];
     const CaseDev& cd = cdev[b.cs];
     const int turb_upd = cd.turb_upd;
-    __shared__ double s_sum[3][256];
-    __shared__ double s_max[3][256];
-    __shared__ long long s_idx[256];
-    __shared__ int s_nan[256];
     const int tid = threadIdx.x;
     double sa = 0, ma = -1, sk = 0, mk = 0, so = 0, mo = 0;
     long long ia = -1;
@@ -288,28 +284,10 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
             }
         }
     }
-    s_sum[0][tid] = sa; s_sum[1][tid] = sk; s_sum[2][tid] = so;
-    s_max[0][tid] = ma; s_max[1][tid] = mk; s_max[2][tid] = mo;
-    s_idx[tid] = ia; s_nan[tid] = nanf;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (tid < w) {
-            for (int q = 0; q < 3; ++q) s_sum[q][tid] += s_sum[q][tid + w];
-            const double a = s_max[0][tid], bb = s_max[0][tid + w];
-            if (bb > a || (bb == a && s_idx[tid + w] > s_idx[tid])) { s_max[0][tid] = bb; s_idx[tid] = s_idx[tid + w]; }
-            s_max[1][tid] = dmax(s_max[1][tid], s_max[1][tid + w]);
-            s_max[2][tid] = dmax(s_max[2][tid], s_max[2][tid + w]);
-            s_nan[tid] |= s_nan[tid + w];
-        }
-        __syncthreads();
-    }
-    if (tid == 0) {
-        NormPart P;
-        P.sa = s_sum[0][0]; P.sk = s_sum[1][0]; P.so = s_sum[2][0];
-        P.ma = s_max[0][0]; P.mk = s_max[1][0]; P.mo = s_max[2][0];
-        P.ia = s_idx[0]; P.nan = s_nan[0]; P.pad_ = 0;
-        parts[blockIdx.x] = P;
-    }
+    NormPart P;
+    P.sa = sa; P.ma = ma; P.sk = sk; P.mk = mk; P.so = so; P.mo = mo; P.ia = ia; P.nan = nanf; P.pad_ = 0;
+    P = norm_reduce_cta(P);
+    if (tid == 0) parts[blockIdx.x] = P;
 }
 
 }  // namespace tg

@@ -47,6 +47,19 @@ void launch_integrals(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, 
 void launch_wall_cp(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int e0, int n, const CaseDev* cdev,
                     double* cp);
 
+// the mixed path's residual from TMA-staged shared-memory tiles (resid_tma.cuh, k_mixed.cu)
+constexpr int RT_X = 32;                  // cells along i of a direction-2/3 tile
+constexpr int RT_X1 = 28;                 // cells along i of a direction-1 tile
+constexpr int RT_D = 8;                   // cells along the direction (2, 3) / rows along j (1)
+constexpr int RT_W1 = RT_X1 + 8;          // staged extent along i, direction 1 (x0-4 .. x0+31)
+constexpr int RT_WIDE = RT_D + 6;         // staged extent along the direction of the stencil fields
+constexpr int RT_NARROW = RT_D + 2;       // ... of the two-point fields
+constexpr int NRMAP = 5;                  // tensor maps per block: direction 1; 2 stencil, two-point; 3 stencil, two-point
+constexpr unsigned RT_WAIT_LIMIT = 1u << 20;   // polls of the tile's mbarrier before the kernel gives up
+cudaError_t prepare_resid_tma();          // the kernels' dynamic shared-memory opt-in
+void launch_resid_tma(int dir, cudaStream_t s, const DevBlock* blks, const ResidTile* tiles, int nt, const CaseDev* cdev,
+                      const void* maps, int* err, unsigned limit);
+
 // flux, source and sweep kernels, instantiated per arithmetic type
 struct FluxLaunchers {
     void (*gradient)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);

@@ -525,6 +525,16 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             break;
         case TRANS_STAGE_RESIDUAL:
             if (!capture && (rc = upload_cdev(c))) return rc;
+            if (c->mixed && c->resid_tma) {
+                // FP32: fluxes from TMA-staged tiles, summed into D per direction
+                for (int d = 0; d < 3; ++d) {
+                    KScope t(c, K_RESID_TMA);
+                    launch_resid_tma(d + 1, s, c->d_blk, c->d_rtiles[d], c->n_rtiles[d], c->d_cdev, c->d_rmaps, c->d_kerr,
+                                     c->resid_spin);
+                }
+                c->launches += 3;
+                break;
+            }
             for (int d = 0; d < 3; ++d) {
                 KScope t(c, K_FACE);
                 c->fl->face_flux[d](s, c->d_blk, c->d_face[d], (int)c->face_tiles[d].size(), c->d_cdev);
@@ -577,8 +587,10 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             c->launches += 2;
             if (capture) break;
             CK(cudaMemcpyAsync(c->h_norms, c->d_norms, sizeof(BlockNorms) * nblk, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(c->h_kerr, c->d_kerr, sizeof(int), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
+            if (*c->h_kerr) return fail(c, TRANS_E_TIMEOUT, "residual tile staging wait timed out");
             if ((rc = collect_norms(c, c->h_norms))) return rc;
             break;
         }
@@ -658,6 +670,7 @@ int capture_iterations(Ctx* c, int n) {
     if (rc == TRANS_OK) {
         cudaMemcpyAsync(c->h_norms, c->d_norms, sizeof(BlockNorms) * (size_t)nblk * n, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(c->h_sync, c->d_sync, sizeof(SweepSync), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(c->h_kerr, c->d_kerr, sizeof(int), cudaMemcpyDeviceToHost, s);
     }
     cudaError_t e = cudaStreamEndCapture(s, &g);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
@@ -721,6 +734,7 @@ int run_iterations(Ctx* c, int n) {
         for (int q = 1; q < m; ++q) advance();  // KI of the last replayed iteration
         done += m;
         if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
+        if (*c->h_kerr) return fail(c, TRANS_E_TIMEOUT, "residual tile staging wait timed out");
         if (nan) return fail(c, TRANS_E_NAN, "NaN in the density increment");
     }
     return TRANS_OK;

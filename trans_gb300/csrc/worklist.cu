@@ -7,6 +7,8 @@
 #include <cstring>
 
 #include "engine.h"
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 namespace tg {
 namespace eng {
@@ -147,6 +149,72 @@ void make_tiles(int nblk, const std::vector<long long>& counts, int tile, std::v
         }
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        looked = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// The mixed path's TMA-staged residual: brick tiles per face direction and NRMAP tensor maps
+// per block over its FP32 slots, a 4-D tensor (i, j, k, slot) with strides PI, PI*PJ, ncell
+// floats (multiples of 16 bytes because PI is a multiple of 4).  Box shapes: direction 1
+// 36 x 8 x 1 x 1; directions 2 and 3 a stencil box of 14 and a two-point box of 10 cells along
+// the direction, 32 along i.  Returns false (the context then uses k_face_flux + k_gather) if
+// the driver cannot encode a map.
+bool build_resid_tma(Ctx* c) {
+    const int nblk = (int)c->blk.size();
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    std::vector<CUtensorMap> maps((size_t)nblk * NRMAP);
+    const cuuint32_t boxes[NRMAP][4] = {{RT_W1, RT_D, 1, 1}, {RT_X, RT_WIDE, 1, 1}, {RT_X, RT_NARROW, 1, 1},
+                                        {RT_X, 1, RT_WIDE, 1}, {RT_X, 1, RT_NARROW, 1}};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    for (int n = 0; n < nblk; ++n) {
+        const DevBlock& b = c->blk[n];
+        if (!b.fbase || (b.PI & 3) || ((uintptr_t)b.fbase & 15)) return false;
+        const cuuint64_t dims[4] = {(cuuint64_t)b.PI, (cuuint64_t)b.PJ, (cuuint64_t)b.PK,
+                                    (cuuint64_t)case_slots(c->cases[b.cs]->p)};
+        const cuuint64_t strides[3] = {(cuuint64_t)b.PI * 4, (cuuint64_t)b.PI * b.PJ * 4, (cuuint64_t)b.ncell * 4};
+        for (int q = 0; q < NRMAP; ++q)
+            if (enc(&maps[(size_t)n * NRMAP + q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void*)b.fbase, dims, strides, boxes[q], estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return false;
+    }
+    // bricks: interior cells are array indices 3..N+1; origins along i are multiples of 32
+    // (directions 2, 3) or 28 (direction 1), so every box starts on a 16-byte boundary
+    std::vector<ResidTile> t[3];
+    for (int n = 0; n < nblk; ++n) {
+        const DevBlock& b = c->blk[n];
+        for (int k = 3; k <= b.NK + 1; ++k)
+            for (int j = 3; j <= b.NJ + 1; j += RT_D)
+                for (int i = 0; i <= b.NI + 1; i += RT_X1) t[0].push_back({n, i, j, k});
+        for (int k = 3; k <= b.NK + 1; ++k)
+            for (int j = 3; j <= b.NJ + 1; j += RT_D)
+                for (int i = 0; i <= b.NI + 1; i += RT_X) t[1].push_back({n, i, j, k});
+        for (int k = 3; k <= b.NK + 1; k += RT_D)
+            for (int j = 3; j <= b.NJ + 1; ++j)
+                for (int i = 0; i <= b.NI + 1; i += RT_X) t[2].push_back({n, i, j, k});
+    }
+    if (upload_vec(c, maps.data(), sizeof(CUtensorMap) * maps.size(), &c->d_rmaps)) return false;
+    for (int d = 0; d < 3; ++d) {
+        if (upload_vec(c, t[d].data(), sizeof(ResidTile) * t[d].size(), (void**)&c->d_rtiles[d])) return false;
+        c->n_rtiles[d] = (int)t[d].size();
+    }
+    return prepare_resid_tma() == cudaSuccess;
+}
+
 }  // namespace
 
 int rebuild(Ctx* c) {
@@ -194,6 +262,7 @@ int rebuild(Ctx* c) {
     for (int d = 0; d < 3; ++d)
         if ((rc = upload_vec(c, c->face_tiles[d].data(), sizeof(Tile) * c->face_tiles[d].size(), (void**)&c->d_face[d]))) return rc;
     if ((rc = upload_vec(c, c->ghost_tiles.data(), sizeof(Tile) * c->ghost_tiles.size(), (void**)&c->d_ghost))) return rc;
+    if (c->mixed && c->resid_tma && !build_resid_tma(c)) c->resid_tma = 0;
     // boundary tables
     c->bc_first.clear();
     for (CaseRec* cs : c->cases) {
