@@ -232,15 +232,16 @@ def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
     """The hyperplane-per-launch schedule, the single cooperative launch with grid barriers, the
     dataflow schedule, the tiled wavefront (two tile shapes), each with the lane-major and the
     warp-per-component thread mapping (FP64), the chaining, prefetch and CTA-size variants of the
-    hyperplane launches, and the tuner's pick compute every DeltaQ with the same operations:
-    states after 6 iterations are bit-identical."""
+    hyperplane launches, the mixed path's cluster-barrier schedule (one thread-block cluster per
+    block; the FP64 path runs planes for it), and the tuner's pick compute every DeltaQ with
+    the same operations: states after 6 iterations are bit-identical."""
     from helpers import small_cascade
     from trans_gb300 import abi
     from trans_gb300.solver import Solver
     out = {}
     modes = ("planes", "planes_unchained", "coop", "flow", "tiles", "tiles_4x2x3", "planes_wpc", "planes_unchained_wpc",
              "coop_wpc", "tiles_4x2x3_wpc", "planes_pf2", "planes_wpc_pf1", "planes_early_cta32", "planes_early_pf2_cta64",
-             "auto")
+             "clusters", "clusters_pf2", "auto")
     for mode in modes:
         parts = mode.split("_")
         monkeypatch.setenv("TRANS_SWEEP", parts[0])

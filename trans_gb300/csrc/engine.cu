@@ -180,6 +180,14 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     // sweep schedule: TRANS_SWEEP=planes | coop | flow | tiles forces one (for tests); default: tuned
     const char* m = std::getenv("TRANS_SWEEP");
     std::string ms = m ? m : "";
+    // clusters: the mixed path's cluster-barrier schedule (the FP64 path takes planes)
+    if (ms == "clusters") ms = c->mixed ? "clusters" : "planes";
+    if (ms == "clusters") {
+        c->sweep_forced = true;
+        c->sweep_mode = 4; c->sweep_grid = 8; c->sweep_block = 256;
+        const char* pfs = std::getenv("TRANS_SWEEP_PF");
+        c->sweep_pf = pfs ? std::max(0, std::atoi(pfs)) : 0;
+    }
     if (ms == "planes" || ms == "coop" || ms == "flow" || ms == "tiles") {
         int dev = 0, nsm = 0;
         CK(cudaGetDevice(&dev));
@@ -204,7 +212,7 @@ void free_worklists(Ctx* c) {
     dfree(c->d_blk); dfree(c->d_off); dfree(c->d_cell); dfree(c->d_ghost);
     for (int d = 0; d < 3; ++d) { dfree(c->d_face[d]); dfree(c->d_rtiles[d]); c->n_rtiles[d] = 0; }
     dfree(c->d_rmaps);
-    dfree(c->d_bc); dfree(c->d_outlet); dfree(c->d_lines); dfree(c->d_sweep); dfree(c->d_plane_off);
+    dfree(c->d_bc); dfree(c->d_outlet); dfree(c->d_lines); dfree(c->d_sweep); dfree(c->d_plane_off); dfree(c->d_pb_off);
     dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq_save); dfree(c->d_parts); dfree(c->d_pc);
     dfree(c->d_cdev); dfree(c->d_stage); dfree(c->d_tile_first); dfree(c->d_norms);
     dfree(c->d_tiles); dfree(c->d_tflags); dfree(c->d_qpos); dfree(c->d_bc_first); dfree(c->d_intg);

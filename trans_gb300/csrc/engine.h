@@ -89,6 +89,7 @@ struct Ctx {
     std::vector<int> plane_off;          // sweep positions of hyperplane h: [plane_off[h], plane_off[h+1])
     SweepCell* d_sweep = nullptr;
     int* d_plane_off = nullptr;
+    int* d_pb_off = nullptr;             // nh x (nblk+1): first position of block b in hyperplane h
     SweepView sv{};
     int* d_nbp = nullptr;
     int* d_qpos = nullptr;               // sweep position of every cell-tile slot (-1: past the tile's end)
@@ -118,7 +119,9 @@ struct Ctx {
     // ---- sweep schedule ----
     cudaGraphExec_t sweep_exec = nullptr;
     // 0 = one launch per hyperplane (graph), 1 = one cooperative launch with grid barriers,
-    // 2 = dataflow over ready flags, 3 = tiled wavefront; -1 = pick the fastest on first use
+    // 2 = dataflow over ready flags, 3 = tiled wavefront, 4 = one thread-block cluster per
+    // block with cluster barriers between hyperplanes (mixed path; sweep_grid = CTAs per
+    // cluster); -1 = pick the fastest on first use
     // (all bit-identical)
     int sweep_mode = -1, sweep_grid = 0, sweep_block = 0;
     int tile_shape[3] = {0, 0, 0};       // tiles of the tiled wavefront (built for this shape)

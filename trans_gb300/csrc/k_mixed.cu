@@ -15,6 +15,42 @@ cudaError_t prepare_resid_tma() {
         e = cudaFuncSetAttribute(k_resid_tma<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rt_smem_bytes(3));
     return e;
 }
+// cluster-barrier sweeps: cs CTAs of bs threads per solver block
+static cudaLaunchConfig_t cluster_cfg(cudaStream_t s, int nblk, int cs, int bs, cudaLaunchAttribute* attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nblk * cs));
+    cfg.blockDim = dim3((unsigned)bs);
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+int sweep_cluster_fits(int cs, int bs) {
+    if (cs > 8 && cudaFuncSetAttribute(k_sweep_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_cfg(nullptr, 1, cs, bs, attr);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_sweep_cluster, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+cudaError_t launch_sweep_cluster(cudaStream_t s, const SweepView& v, const int* pb_off, int nh, int nblk, int turb, int cs, int bs,
+                                 int pf) {
+    if (nblk <= 0 || v.n <= 0) return cudaSuccess;
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_cfg(s, nblk, cs, bs, attr);
+    return cudaLaunchKernelEx(&cfg, k_sweep_cluster, (const int*)v.nbp, (const float*)v.rec, (float*)v.dq, pb_off, nh, nblk,
+                              turb, pf);
+}
 void launch_resid_tma(int dir, cudaStream_t s, const DevBlock* blks, const ResidTile* tiles, int nt, const CaseDev* cdev,
                       const void* maps, int* err, unsigned limit) {
     if (nt <= 0) return;

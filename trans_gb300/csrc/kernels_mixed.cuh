@@ -290,4 +290,53 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
     if (tid == 0) parts[blockIdx.x] = P;
 }
 
+// ---------------------------------------------------------------------------------------
+// Both LU-SGS sweeps of the mixed path with one thread-block cluster per solver block
+// (Time/TIME_LUSGS.F90:73-215 order): the cluster's CTAs take the block's positions of
+// hyperplane h, then meet at a cluster barrier (arrive.release / wait.acquire) before h+1; the
+// lower sweep ascends, the upper descends.  The sweeps stop at block faces, so clusters never
+// wait on one another and need no co-residency beyond their own CTAs, which the hardware
+// schedules together; a cluster barrier is a hardware barrier every thread reaches, not a spin.
+// Every position runs sweep_pos_compact, as in the other schedules (bit-identical results);
+// DeltaQ written by other SMs of the cluster is read through L2.  pb_off[h*(nblk+1) + b] is the
+// first sweep position of block b in hyperplane h; pf > 0 prefetches the block's records of
+// hyperplane h +- pf into L2 while h is swept.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ unsigned cluster_reg(int which) {
+    unsigned r;
+    if (which == 0) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    else if (which == 1) asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    else asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+
+__global__ void k_sweep_cluster(const int* __restrict__ nbp, const float* __restrict__ rec, float* dq,
+                                const int* __restrict__ pb_off, int nh, int nblk, int turb, int pf) {
+    const int rank = (int)cluster_reg(0), ncta = (int)cluster_reg(1), b = (int)cluster_reg(2);
+    const int nt = ncta * blockDim.x, t = rank * blockDim.x + threadIdx.x;
+    auto first = [&](int h) { return pb_off[(size_t)h * (nblk + 1) + b]; };
+    auto last = [&](int h) { return pb_off[(size_t)h * (nblk + 1) + b + 1]; };
+    auto prefetch = [&](int h) {
+        if (pf > 0 && h >= 0 && h < nh && last(h) > first(h))
+            prefetch_l2_range(rec + sw_at(first(h), 0, NCREC), (size_t)(last(h) - first(h)) * NCREC * sizeof(float), t, nt);
+    };
+    for (int h = 0; h < nh; ++h) {
+        const int p0 = first(h), p1 = last(h);
+        if (p0 == p1) continue;             // the same for every thread of the cluster
+        prefetch(h + pf);
+        for (int q = p0 + t; q < p1; q += nt) sweep_pos_compact<true>(nbp, rec, dq, q, turb, false);
+        cluster_barrier();
+    }
+    for (int h = nh - 1; h >= 0; --h) {
+        const int p0 = first(h), p1 = last(h);
+        if (p0 == p1) continue;
+        prefetch(h - pf);
+        for (int q = p0 + t; q < p1; q += nt) sweep_pos_compact<false>(nbp, rec, dq, q, turb, false);
+        cluster_barrier();
+    }
+}
+
 }  // namespace tg

@@ -60,6 +60,14 @@ cudaError_t prepare_resid_tma();          // the kernels' dynamic shared-memory 
 void launch_resid_tma(int dir, cudaStream_t s, const DevBlock* blks, const ResidTile* tiles, int nt, const CaseDev* cdev,
                       const void* maps, int* err, unsigned limit);
 
+// the mixed path's sweeps with one thread-block cluster of cs CTAs x bs threads per solver
+// block and cluster barriers between hyperplanes (k_mixed.cu); pb_off: nh x (nblk+1) first
+// positions of each block in each hyperplane; sweep_cluster_fits: clusters that fit at once
+// (0: this shape cannot launch)
+cudaError_t launch_sweep_cluster(cudaStream_t s, const SweepView& v, const int* pb_off, int nh, int nblk, int turb, int cs, int bs,
+                                 int pf);
+int sweep_cluster_fits(int cs, int bs);
+
 // flux, source and sweep kernels, instantiated per arithmetic type
 struct FluxLaunchers {
     void (*gradient)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);

@@ -294,6 +294,11 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         c->launches++;
         return TRANS_OK;
     }
+    if (mode == 4) {
+        CK(launch_sweep_cluster(s, c->sv, c->d_pb_off, nh, (int)c->blk.size(), c->sweep_lanes, grid, block, c->sweep_pf));
+        c->launches++;
+        return TRANS_OK;
+    }
     if (mode == 2) {
         const size_t np = (size_t)((c->sv.n + 31) / 32 * 32);
         CK(cudaMemsetAsync(c->d_flags, 0, 2 * np * sizeof(int), s));
@@ -380,6 +385,11 @@ int tune_sweeps(Ctx* c) {
         if (occ >= 1) cands.push_back({1, nsm, 256, 0, 0, 0, 0, 0, 0});
         const int tocc = c->fl->sweep_tiles_occupancy(256);
         if (tocc >= 1) cands.push_back({3, tocc * nsm, 256, 0, 16, 4, 4, 0, 0});
+        // one cluster per block: CTAs per cluster x CTA size, records prefetched 0 or 2 ahead
+        for (int cs : {8, 16})
+            for (int bs : {256, 512})
+                if (sweep_cluster_fits(cs, bs) >= 1)
+                    for (int pf : {0, 2}) cands.push_back({4, cs, bs, 0, 0, 0, 0, 0, pf});
     }
     for (int wpc : {0, SWEEP_WPC}) {
         if (fp32) break;
@@ -426,7 +436,7 @@ int tune_sweeps(Ctx* c) {
             float ms = 0;
             CK(cudaEventElapsedTime(&ms, e0, e1));
             if (rep == 1) {
-                c->sweep_tuning += (k.mode ? std::string(k.mode == 1 ? "coop " : k.mode == 2 ? "flow " : "tiles ")
+                c->sweep_tuning += (k.mode ? std::string(k.mode == 1 ? "coop " : k.mode == 2 ? "flow " : k.mode == 4 ? "clusters " : "tiles ")
                                                  + (k.mode == 3 ? std::to_string(k.ti) + "x" + std::to_string(k.tj) + "x"
                                                                       + std::to_string(k.tk) + "/" : std::string())
                                                  + std::to_string(k.grid) + "x" + std::to_string(k.block)

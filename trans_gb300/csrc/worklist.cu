@@ -279,17 +279,21 @@ int rebuild(Ctx* c) {
     int hmax = 3;
     for (auto& b : c->blk) hmax = std::max(hmax, b.NI1 + b.NJ1 + b.NK1);
     c->plane_off.assign(1, 0);
+    std::vector<int> pb_off;
     for (int h = 3; h <= hmax; ++h) {
         for (int n = 0; n < nblk; ++n) {
             const DevBlock& b = c->blk[n];
+            pb_off.push_back((int)c->sweep.size());
             for (int k = 1; k <= b.NK1; ++k)
                 for (int j = 1; j <= b.NJ1; ++j) {
                     int i = h - j - k;
                     if (i >= 1 && i <= b.NI1) c->sweep.push_back(SweepCell{n, i, j, k});
                 }
         }
+        pb_off.push_back((int)c->sweep.size());
         c->plane_off.push_back((int)c->sweep.size());
     }
+    if ((rc = upload_vec(c, pb_off.data(), sizeof(int) * pb_off.size(), (void**)&c->d_pb_off))) return rc;
     if ((rc = upload_vec(c, c->sweep.data(), sizeof(SweepCell) * c->sweep.size(), (void**)&c->d_sweep))) return rc;
     if ((rc = upload_vec(c, c->plane_off.data(), sizeof(int) * c->plane_off.size(), (void**)&c->d_plane_off))) return rc;
     {   // neighbour positions in sweep order: lower i,j,k (0..2) and upper (3..5), -1 = none
