@@ -204,12 +204,15 @@ const char* trans_tuning(void* ctx) {
     static thread_local std::string out;
     const std::string tiles = c->sweep_mode == 3 ? std::to_string(c->tile_shape[0]) + "x" + std::to_string(c->tile_shape[1]) + "x"
                                                        + std::to_string(c->tile_shape[2]) + "/" : std::string();
-    out = "sweep=" + std::string(c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : c->sweep_mode == 2 ? "flow " : "tiles ")
+    out = "sweep=" + std::string(c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : c->sweep_mode == 2 ? "flow " : c->sweep_mode == 4 ? "clusters " : "tiles ")
                                                       + tiles + std::to_string(c->sweep_grid) + "x" + std::to_string(c->sweep_block)
                                  : c->sweep_mode == 0 ? (c->pdl ? (c->pdl == 2 ? "planes-early" : "planes-chained") : "planes") : "untuned")
-          + (c->sweep_wpc ? "/wpc" : "") + (c->sweep_pf && c->sweep_mode == 0 ? "/pf" + std::to_string(c->sweep_pf) : "")
+          + (c->sweep_wpc ? "/wpc" : "") + (c->sweep_pf && (c->sweep_mode == 0 || c->sweep_mode == 4) ? "/pf" + std::to_string(c->sweep_pf) : "")
           + (c->sweep_cta && c->sweep_mode == 0 ? "/cta" + std::to_string(c->sweep_cta) : "")
-          + "; measured: " + c->sweep_tuning;
+          + "; measured: " + c->sweep_tuning
+          + (c->mixed ? std::string("; residual=") + (c->resid_tma == 1 ? "tma" : c->resid_tma == 0 ? "gather" : "untuned")
+                            + (c->resid_tuning.empty() ? std::string() : " (" + c->resid_tuning + ")")
+                      : std::string());
     return out.c_str();
 }
 

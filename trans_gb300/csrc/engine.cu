@@ -149,10 +149,11 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     CK(cudaMemset(c->d_kerr, 0, sizeof(int)));
     CK(cudaMallocHost(&c->h_kerr, sizeof(int)));
     *c->h_kerr = 0;
-    // TRANS_RESID_TMA=0: the mixed path's residual from k_face_flux + k_gather instead of the
-    // TMA-staged tiles (for comparisons)
+    // TRANS_RESID_TMA=0 | 1: the mixed path's residual from k_face_flux + k_gather, or from the
+    // TMA-staged tiles (for comparisons); default: the faster on the context's first residual
     const char* rt = std::getenv("TRANS_RESID_TMA");
     if (rt && std::string(rt) == "0") c->resid_tma = 0;
+    if (rt && std::string(rt) == "1") c->resid_tma = 1;
     // TRANS_RESID_SPIN=n: polls of the tile staging wait before it gives up (for tests)
     const char* rsp = std::getenv("TRANS_RESID_SPIN");
     if (rsp) c->resid_spin = (unsigned)std::max(0L, std::atol(rsp));

@@ -70,8 +70,10 @@ struct Ctx {
     Tile *d_cell = nullptr, *d_face[3] = {nullptr, nullptr, nullptr}, *d_ghost = nullptr;
     std::vector<int> cell_tile_blk;      // block of each cell tile (norm reduction)
     // mixed path: the residual from TMA-staged tiles (one tile list per face direction, NRMAP
-    // tensor maps per block over its FP32 slots); resid_tma = 0 uses k_face_flux + k_gather
-    int resid_tma = 1;
+    // tensor maps per block over its FP32 slots); resid_tma = 0 uses k_face_flux + k_gather,
+    // -1 times both on the first residual and keeps the faster
+    int resid_tma = -1;
+    std::string resid_tuning;
     ResidTile* d_rtiles[3] = {nullptr, nullptr, nullptr};
     int n_rtiles[3] = {0, 0, 0};
     void* d_rmaps = nullptr;

@@ -55,7 +55,7 @@ void launch_resid_tma(int dir, cudaStream_t s, const DevBlock* blks, const Resid
                       const void* maps, int* err, unsigned limit) {
     if (nt <= 0) return;
     const CUtensorMap* m = (const CUtensorMap*)maps;
-    if (dir == 1) k_resid_tma<1><<<nt, 32 * RT_D, rt_smem_bytes(1), s>>>(blks, tiles, cdev, m, err, limit);
+    if (dir == 1) k_resid_tma<1><<<nt, 32 * RT_R1, rt_smem_bytes(1), s>>>(blks, tiles, cdev, m, err, limit);
     else if (dir == 2) k_resid_tma<2><<<nt, RT_FACES, rt_smem_bytes(2), s>>>(blks, tiles, cdev, m, err, limit);
     else k_resid_tma<3><<<nt, RT_FACES, rt_smem_bytes(3), s>>>(blks, tiles, cdev, m, err, limit);
 }

@@ -467,6 +467,42 @@ int tune_sweeps(Ctx* c) {
     return TRANS_OK;
 }
 
+// The mixed path's two residual implementations (TMA-staged tiles, or k_face_flux + k_gather)
+// compute the same FP32 face fluxes: time both on the live state (the residual stage only
+// writes D and the FX slots), keep the faster.
+int tune_resid(Ctx* c) {
+    cudaStream_t s = c->stream;
+    const int nct = (int)c->cell_tiles.size();
+    auto run = [&](int tma) {
+        if (tma) {
+            for (int d = 0; d < 3; ++d)
+                launch_resid_tma(d + 1, s, c->d_blk, c->d_rtiles[d], c->n_rtiles[d], c->d_cdev, c->d_rmaps, c->d_kerr,
+                                 c->resid_spin);
+        } else {
+            for (int d = 0; d < 3; ++d) c->fl->face_flux[d](s, c->d_blk, c->d_face[d], (int)c->face_tiles[d].size(), c->d_cdev);
+            c->fl->gather(s, c->d_blk, c->d_cell, nct, c->d_cdev);
+        }
+    };
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float ms[2] = {0.f, 0.f};
+    for (int v = 0; v < 2; ++v) {
+        run(v);                                  // warm-up
+        CK(cudaEventRecord(e0, s));
+        for (int rep = 0; rep < 3; ++rep) run(v);
+        CK(cudaEventRecord(e1, s));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaEventElapsedTime(&ms[v], e0, e1));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaGetLastError());
+    c->resid_tma = ms[1] < ms[0] ? 1 : 0;
+    c->resid_tuning = "tma:" + std::to_string(ms[1] / 3) + "ms gather:" + std::to_string(ms[0] / 3) + "ms";
+    return TRANS_OK;
+}
+
 int run_sweeps(Ctx* c) {
     if (c->sweep_mode < 0) {
         int rc = tune_sweeps(c);
@@ -535,7 +571,8 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             break;
         case TRANS_STAGE_RESIDUAL:
             if (!capture && (rc = upload_cdev(c))) return rc;
-            if (c->mixed && c->resid_tma) {
+            if (c->mixed && c->resid_tma < 0 && !capture && (rc = tune_resid(c))) return rc;
+            if (c->mixed && c->resid_tma == 1) {
                 // FP32: fluxes from TMA-staged tiles, summed into D per direction
                 for (int d = 0; d < 3; ++d) {
                     KScope t(c, K_RESID_TMA);

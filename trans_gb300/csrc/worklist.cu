@@ -169,7 +169,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 // The mixed path's TMA-staged residual: brick tiles per face direction and NRMAP tensor maps
 // per block over its FP32 slots, a 4-D tensor (i, j, k, slot) with strides PI, PI*PJ, ncell
 // floats (multiples of 16 bytes because PI is a multiple of 4).  Box shapes: direction 1
-// 36 x 8 x 1 x 1; directions 2 and 3 a stencil box of 14 and a two-point box of 10 cells along
+// 36 x 4 x 1 x 1; directions 2 and 3 a stencil box of 10 and a two-point box of 6 cells along
 // the direction, 32 along i.  Returns false (the context then uses k_face_flux + k_gather) if
 // the driver cannot encode a map.
 bool build_resid_tma(Ctx* c) {
@@ -177,7 +177,7 @@ bool build_resid_tma(Ctx* c) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) return false;
     std::vector<CUtensorMap> maps((size_t)nblk * NRMAP);
-    const cuuint32_t boxes[NRMAP][4] = {{RT_W1, RT_D, 1, 1}, {RT_X, RT_WIDE, 1, 1}, {RT_X, RT_NARROW, 1, 1},
+    const cuuint32_t boxes[NRMAP][4] = {{RT_W1, RT_R1, 1, 1}, {RT_X, RT_WIDE, 1, 1}, {RT_X, RT_NARROW, 1, 1},
                                         {RT_X, 1, RT_WIDE, 1}, {RT_X, 1, RT_NARROW, 1}};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     for (int n = 0; n < nblk; ++n) {
@@ -198,7 +198,7 @@ bool build_resid_tma(Ctx* c) {
     for (int n = 0; n < nblk; ++n) {
         const DevBlock& b = c->blk[n];
         for (int k = 3; k <= b.NK + 1; ++k)
-            for (int j = 3; j <= b.NJ + 1; j += RT_D)
+            for (int j = 3; j <= b.NJ + 1; j += RT_R1)
                 for (int i = 0; i <= b.NI + 1; i += RT_X1) t[0].push_back({n, i, j, k});
         for (int k = 3; k <= b.NK + 1; ++k)
             for (int j = 3; j <= b.NJ + 1; j += RT_D)
@@ -262,7 +262,7 @@ int rebuild(Ctx* c) {
     for (int d = 0; d < 3; ++d)
         if ((rc = upload_vec(c, c->face_tiles[d].data(), sizeof(Tile) * c->face_tiles[d].size(), (void**)&c->d_face[d]))) return rc;
     if ((rc = upload_vec(c, c->ghost_tiles.data(), sizeof(Tile) * c->ghost_tiles.size(), (void**)&c->d_ghost))) return rc;
-    if (c->mixed && c->resid_tma && !build_resid_tma(c)) c->resid_tma = 0;
+    if (c->mixed && c->resid_tma != 0 && !build_resid_tma(c)) c->resid_tma = 0;
     // boundary tables
     c->bc_first.clear();
     for (CaseRec* cs : c->cases) {
