@@ -33,10 +33,14 @@ namespace tg {
 // tile geometry (RT_X, RT_X1, RT_D, RT_W1, RT_WIDE, RT_NARROW, NRMAP) is in launch.h
 constexpr int RT_NWIDE = 14, RT_NNARROW = 25, RT_NFIELD = RT_NWIDE + RT_NNARROW;
 constexpr int RT_FACES = RT_X * (RT_D + 1);                       // faces of a direction-2/3 tile
-constexpr int RT_F1 = RT_W1 * RT_R1;                              // floats per field, direction 1
+constexpr int RT_B1 = RT_W1 * RT_R1;                              // floats of a direction-1 box
+constexpr int RT_F1 = (RT_B1 + 31) / 32 * 32;                     // floats per field, direction 1 (128-byte multiple)
 constexpr int RT_FW = RT_X * RT_WIDE, RT_FN = RT_X * RT_NARROW;   // floats per field, directions 2, 3
 constexpr int RT_FIELDS1 = RT_NFIELD * RT_F1;
 constexpr int RT_FIELDS23 = RT_NWIDE * RT_FW + RT_NNARROW * RT_FN;
+// every field starts on a 128-byte boundary: a TMA tensor copy's shared-memory destination must
+static_assert(RT_F1 * 4 % 128 == 0 && RT_FW * 4 % 128 == 0 && RT_FN * 4 % 128 == 0 && RT_NWIDE * RT_FW * 4 % 128 == 0,
+              "TMA destinations must be 128-byte aligned");
 // dynamic shared memory of a CTA: fields, face fluxes (directions 2, 3), mbarrier, alignment slack
 constexpr size_t rt_smem_bytes(int dir) {
     return (size_t)(dir == 1 ? RT_FIELDS1 : RT_FIELDS23 + NFX * RT_FACES) * 4 + 16 + 128;
@@ -188,7 +192,8 @@ __global__ void __launch_bounds__(DIR == 1 ? 32 * RT_R1 : RT_FACES, 4)
         nl[nn++] = S_RMIU; nl[nn++] = S_VOL;
         if (turb) { nl[nn++] = S_V; nl[nn++] = S_DST; }
         nl[nn++] = S_VINV + DIR - 1; nl[nn++] = S_WALL + DIR - 1; nl[nn++] = S_GRAD + DIR - 1;
-        const unsigned wb = (DIR == 1 ? RT_F1 : RT_FW) * 4, nb = (DIR == 1 ? RT_F1 : RT_FN) * 4;
+        // bytes the copies deliver: the boxes' sizes (a direction-1 field is padded beyond its box)
+        const unsigned wb = (DIR == 1 ? RT_B1 : RT_FW) * 4, nb = (DIR == 1 ? RT_B1 : RT_FN) * 4;
         mbar_arrive_expect_tx(bar, nw * wb + nn * nb);
         for (int q = 0; q < nw; ++q) tma_load_4d(sm + rt_offset<DIR>(rt_field<DIR>(wl[q])), mw, wx, wy, wz, wl[q], bar);
         for (int q = 0; q < nn; ++q) tma_load_4d(sm + rt_offset<DIR>(rt_field<DIR>(nl[q])), mn, wx, ny, nz, nl[q], bar);
