@@ -50,8 +50,8 @@ void launch_wall_cp(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, in
 // the mixed path's residual from TMA-staged shared-memory tiles (resid_tma.cuh, k_mixed.cu)
 constexpr int RT_X = 32;                  // cells along i of a direction-2/3 tile
 constexpr int RT_X1 = 28;                 // cells along i of a direction-1 tile
-constexpr int RT_D = 4;                   // cells along the direction of a direction-2/3 tile
-constexpr int RT_R1 = 4;                  // rows along j of a direction-1 tile (one warp each)
+constexpr int RT_D = 8;                   // cells along the direction of a direction-2/3 tile
+constexpr int RT_R1 = 8;                  // rows along j of a direction-1 tile (one warp each)
 constexpr int RT_W1 = RT_X1 + 8;          // staged extent along i, direction 1 (x0-4 .. x0+31)
 constexpr int RT_WIDE = RT_D + 6;         // staged extent along the direction of the stencil fields
 constexpr int RT_NARROW = RT_D + 2;       // ... of the two-point fields

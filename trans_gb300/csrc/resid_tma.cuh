@@ -11,14 +11,14 @@
 //   D = (-Fv1 + Fv1' [+ rotating source] - Fc1 + Fc1') + (-Fv2 + ...) + (-Fv3 + ...).
 //
 // Tiles (array indices, i.e. Fortran index + 2; interior cells 3..N+1):
-//   direction 1: 28 cells along i x 4 rows along j x 1 k; staged box 36 x 4 from x0-4 (29
+//   direction 1: 28 cells along i x 8 rows along j x 1 k; staged box 36 x 8 from x0-4 (29
 //                faces per row, one warp per row; the neighbour face's flux comes from the
 //                next lane by a warp shuffle);
-//   directions 2, 3: 32 cells along i x 4 cells along the direction; staged boxes 32 x 10
-//                (stencil, from y0-3) and 32 x 6 (two-point fields, from y0-1); 5 faces per
+//   directions 2, 3: 32 cells along i x 8 cells along the direction; staged boxes 32 x 14
+//                (stencil, from y0-3) and 32 x 10 (two-point fields, from y0-1); 9 faces per
 //                column, one thread per face, the fluxes exchanged through shared memory.
-// Small bricks keep four CTAs resident per SM, so that one CTA's staging overlaps the others'
-// arithmetic.
+// Two CTAs are resident per SM (registers and shared memory); 4-cell bricks with four CTAs
+// measured slower (more halo faces, more instructions per cell).
 // The x origin of every box is a multiple of 4 cells (16 bytes) and the row pitch PI a
 // multiple of 4, as the TMA unit requires; boxes reaching outside the block read zeros, which
 // no valid face uses.
@@ -121,13 +121,13 @@ __device__ __forceinline__ void tma_load_4d(float* dst, const void* map, int x, 
 
 // flux differences of one cell in the mixed path's order (see the file comment); Fm = the
 // fluxes of the face on the cell's minus side, Fp of the face on its plus side
-// (first: direction 1, which writes D; otherwise Dold holds D of the cell, to which it adds)
+// (first: direction 1, which writes D; directions 2, 3 add to it)
 __device__ __forceinline__ void rt_cell(const DevBlock& b, int c, int turb, const float* Fm, const float* Fp, bool first,
-                                        float om, const float* Dold) {
+                                        float om) {
     const size_t nc = (size_t)b.ncell;
     float* D = fslot(b, S_D);
     float a = 0.f - Fm[FX_C0] + Fp[FX_C0];
-    D[c] = first ? a : Dold[0] + a;
+    D[c] = first ? a : D[c] + a;
 #pragma unroll
     for (int L = 1; L < 5; ++L) {
         a = 0.f - Fm[FX_VX + L - 1] + Fp[FX_VX + L - 1];
@@ -140,13 +140,13 @@ __device__ __forceinline__ void rt_cell(const DevBlock& b, int c, int turb, cons
             a = a + ss * fslot(b, S_VOL)[c];
         }
         a = a - Fm[FX_C0 + L] + Fp[FX_C0 + L];
-        D[L * nc + c] = first ? a : Dold[L] + a;
+        D[L * nc + c] = first ? a : D[L * nc + c] + a;
     }
     if (turb) {
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             a = 0.f - Fm[FX_TK + q] + Fp[FX_TK + q] - Fm[FX_CK + q] + Fp[FX_CK + q];
-            D[(5 + q) * nc + c] = first ? a : Dold[5 + q] + a;
+            D[(5 + q) * nc + c] = first ? a : D[(5 + q) * nc + c] + a;
         }
     } else if (first) {
         D[5 * nc + c] = 0.f;
@@ -155,7 +155,7 @@ __device__ __forceinline__ void rt_cell(const DevBlock& b, int c, int turb, cons
 }
 
 template <int DIR>
-__global__ void __launch_bounds__(DIR == 1 ? 32 * RT_R1 : RT_FACES, 4)
+__global__ void __launch_bounds__(DIR == 1 ? 32 * RT_R1 : RT_FACES, 2)
     k_resid_tma(const DevBlock* __restrict__ blks, const ResidTile* __restrict__ tiles, const CaseDev* __restrict__ cdev,
                 const CUtensorMap* __restrict__ maps, int* __restrict__ err, unsigned limit) {
     extern __shared__ unsigned char rt_raw[];
@@ -198,17 +198,6 @@ __global__ void __launch_bounds__(DIR == 1 ? 32 * RT_R1 : RT_FACES, 4)
         for (int q = 0; q < nw; ++q) tma_load_4d(sm + rt_offset<DIR>(rt_field<DIR>(wl[q])), mw, wx, wy, wz, wl[q], bar);
         for (int q = 0; q < nn; ++q) tma_load_4d(sm + rt_offset<DIR>(rt_field<DIR>(nl[q])), mn, wx, ny, nz, nl[q], bar);
     }
-    // directions 2, 3 add to D: its values (written by the previous launch) load during the wait
-    float Dold[7];
-    if (DIR != 1) {
-        const int x = tid & 31, f = tid >> 5;
-        const int ia = t.x0 + x, ja = DIR == 2 ? t.y0 + f : t.y0, ka = DIR == 3 ? t.z0 + f : t.z0;
-        const bool cell_ok = f < RT_D && ia >= 3 && ia <= b.NI + 1 && ja <= b.NJ + 1 && ka <= b.NK + 1;
-        const size_t nc = (size_t)b.ncell;
-        const int c = ia + b.PI * (ja + b.PJ * ka);
-#pragma unroll
-        for (int L = 0; L < 7; ++L) Dold[L] = cell_ok && (L < 5 || turb) ? fslot(b, S_D)[L * nc + c] : 0.f;
-    }
     // one verdict for the whole CTA, so that no thread is left at a barrier
     if (__syncthreads_or(!mbar_wait(bar, 0, limit))) {
         // the copies did not land in time: record it, give the ones in flight the default
@@ -236,7 +225,7 @@ __global__ void __launch_bounds__(DIR == 1 ? 32 * RT_R1 : RT_FACES, 4)
 #pragma unroll
         for (int m = 0; m < NFX; ++m) Fp[m] = __shfl_down_sync(0xffffffffu, F[m], 1);
         if (l < RT_X1 && ia >= 3 && ia <= b.NI + 1 && ja <= b.NJ + 1 && ka <= b.NK + 1)
-            rt_cell(b, c, turb, F, Fp, true, p.omega0, nullptr);
+            rt_cell(b, c, turb, F, Fp, true, p.omega0);
     } else {
         const int x = tid & 31, f = tid >> 5;
         const int ia = t.x0 + x;
@@ -262,7 +251,7 @@ __global__ void __launch_bounds__(DIR == 1 ? 32 * RT_R1 : RT_FACES, 4)
                 Fm[m] = Fb[m * RT_FACES + tid];
                 Fp[m] = Fb[m * RT_FACES + tid + RT_X];
             }
-            rt_cell(b, c, turb, Fm, Fp, false, 0.f, Dold);
+            rt_cell(b, c, turb, Fm, Fp, false, 0.f);
         }
     }
 }

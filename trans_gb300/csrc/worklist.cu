@@ -169,7 +169,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 // The mixed path's TMA-staged residual: brick tiles per face direction and NRMAP tensor maps
 // per block over its FP32 slots, a 4-D tensor (i, j, k, slot) with strides PI, PI*PJ, ncell
 // floats (multiples of 16 bytes because PI is a multiple of 4).  Box shapes: direction 1
-// 36 x 4 x 1 x 1; directions 2 and 3 a stencil box of 10 and a two-point box of 6 cells along
+// 36 x 8 x 1 x 1; directions 2 and 3 a stencil box of 14 and a two-point box of 10 cells along
 // the direction, 32 along i.  Returns false (the context then uses k_face_flux + k_gather) if
 // the driver cannot encode a map.
 bool build_resid_tma(Ctx* c) {
