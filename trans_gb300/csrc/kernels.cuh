@@ -1029,8 +1029,9 @@ __device__ inline R rc_fr1(const ParamsT<R>& p, const DevBlock& b, int I, int J,
     return dmax(dmin(f_rot, R(1.25)), R(0.0));
 }
 
+// (FP32: two resident CTAs of 256 threads per SM, i.e. at most 128 registers)
 template <typename R>
-__global__ void k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
+__global__ void __launch_bounds__(CELL_TILE, sizeof(R) == 4 ? 2 : 1) k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
                              R* __restrict__ rec, R* __restrict__ dq, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
