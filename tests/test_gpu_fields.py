@@ -128,3 +128,38 @@ def test_batch_fields_match_single_case(gpu_lib):
     assert gpu_lib.trans_batch_get_fields(bt.ctx, 12345, *_table(items[:1])) == abi.TRANS_E_ARG
     assert bt.norms(other)[0] == 2
     bt.close()
+
+
+def test_batched_transfers_keep_call_order(gpu_lib):
+    """Page-locked arrays go over the host link in batches (one launch for up to 60 arrays): a
+    call with more arrays than one batch holds, and one that names the same block and field
+    twice (the later array wins, as with one call per array), give what one-array calls give."""
+    from trans_gb300 import abi
+    from trans_gb300.solver import Solver
+    c, conns, geo, st = small_cascade(Kind_Spatial=3, Kind_Roe=3)
+    s = Solver(c, conns, geo, st, lib=gpu_lib)
+    s.iterate(1)
+    keep, items, ref = [], [], []
+    for rep in range(14):                          # 70 arrays: two batches
+        for ib, b in enumerate(c.blocks):
+            shape = abi.field_shape("PP", *b.dims)
+            a, t = _pinned(shape)
+            a[...] = np.nan
+            keep.append(t)
+            items.append((ib, abi.FIELD_ID["PP"], a))
+    assert gpu_lib.trans_get_fields(s.ctx, *_table(items)) == 0
+    for ib, b in enumerate(c.blocks):
+        ref = s.get_field(ib, "PP")
+        for (jb, _, a) in items:
+            if jb == ib:
+                assert np.array_equal(a.view(np.int64), ref.view(np.int64))
+    # the same block and field twice in one upload: the second array is what the slots hold
+    shape = abi.field_shape("T", *c.blocks[0].dims)
+    first, t1 = _pinned(shape)
+    second, t2 = _pinned(shape)
+    first[...] = 1.0
+    second[...] = 2.0
+    keep += [t1, t2]
+    assert gpu_lib.trans_set_fields(s.ctx, *_table([(0, abi.FIELD_ID["T"], first), (0, abi.FIELD_ID["T"], second)])) == 0
+    assert np.all(s.get_field(0, "T") == 2.0)
+    s.close()

@@ -7,7 +7,9 @@ contexts start from the same state and run the same stages; one finishes each it
 the regular update, the other with the static-scratch entry point.  Two calls in a row must
 give the same norms and the same updated state (tolerance 1e-11 relative, the FP64 path's bar;
 in the mixed path both run the same FP64 update kernel on the same FP32 increments, so the
-same bar holds), and the device memory the context holds must not change across the calls.
+same bar holds), and the device memory the context holds must not change across the calls;
+the device's free memory must not change across the second call (the first call on a device
+looks the fixed buffer up, which may load the library's device code).
 An unbuilt context is refused without allocating anything.
 
 This file is collected last on purpose, so a run that stops at its first failure has run every
@@ -71,14 +73,18 @@ def test_static_scratch_update_matches_regular_update(gpu_lib, precision, which)
             regular.run_stage(s, ki)
             static.run_stage(s, ki)
         regular.run_stage("UPDATE", ki)
+        _compare(regular, static, ki, nblk, lambda ib: masks[ib])
         if free0 is None:
+            # the first call on the device looks the fixed buffer up, which may load the
+            # library's device code (and its buffer) on the device; later calls allocate nothing
             import torch
             torch.cuda.synchronize()
             free0 = _device_free_bytes()
-        _compare(regular, static, ki, nblk, lambda ib: masks[ib])
         regular.run_stage("UPDATE_U", ki)
         static.run_stage("UPDATE_U", ki)
-    assert _device_free_bytes() == free0, "device memory was allocated or freed across the calls"
+    import torch
+    torch.cuda.synchronize()
+    assert _device_free_bytes() == free0, "device memory was allocated or freed across the second call"
     regular.close()
     static.close()
 

@@ -109,6 +109,19 @@ struct Tile {             // a run of consecutive interior cells (or faces) of o
     int blk, start, count, pad_;
 };
 
+// one page-locked Fortran-layout array of a field transfer and its slots (k_fields_xfer)
+struct XferEntry {
+    double* base;                 // the block's slot arena
+    double* host;                 // device address of the page-locked array
+    long long off;                // first element within the batch
+    int ncell, PI, PJ, ei, ej, slot0, ncomp, lb, is_sd, pad_;
+};
+constexpr int XFER_MAX = 60;      // entries per launch (the batch stays under 4 KB of kernel parameters)
+struct XferBatch {
+    XferEntry e[XFER_MAX];
+    int n, pad_;
+};
+
 struct ResidTile {        // a brick of cells of one block (array indices of its first cell)
     int blk, x0, y0, z0;
 };

@@ -154,6 +154,9 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     const char* rt = std::getenv("TRANS_RESID_TMA");
     if (rt && std::string(rt) == "0") c->resid_tma = 0;
     if (rt && std::string(rt) == "1") c->resid_tma = 1;
+    // TRANS_XFER_BATCH=0: trans_set/get_fields transfer the arrays one launch each (for comparisons)
+    const char* xb = std::getenv("TRANS_XFER_BATCH");
+    if (xb && std::string(xb) == "0") c->xfer_batch = false;
     // TRANS_RESID_SPIN=n: polls of the tile staging wait before it gives up (for tests)
     const char* rsp = std::getenv("TRANS_RESID_SPIN");
     if (rsp) c->resid_spin = (unsigned)std::max(0L, std::atol(rsp));

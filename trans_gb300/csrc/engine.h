@@ -73,6 +73,7 @@ struct Ctx {
     // tensor maps per block over its FP32 slots); resid_tma = 0 uses k_face_flux + k_gather,
     // -1 times both on the first residual and keeps the faster
     int resid_tma = -1;
+    bool xfer_batch = true;              // trans_set/get_fields: page-locked arrays in one launch
     std::string resid_tuning;
     ResidTile* d_rtiles[3] = {nullptr, nullptr, nullptr};
     int n_rtiles[3] = {0, 0, 0};

@@ -2112,5 +2112,26 @@ __global__ void k_field_xfer(DevBlock b, int slot0, int ncomp, int lb, int is_sd
     if (to_slots) sl[c] = stage[e];
     else stage[e] = sl[c];
 }
+
+// Several Fortran-layout arrays in page-locked host memory <-> slots in one launch: entry q
+// covers elements [off[q], off[q+1]) of the concatenated arrays, read or written over the
+// host link directly (component fastest, so a warp touches 256 consecutive bytes of host
+// memory); one launch keeps enough reads in flight to fill the link.
+__global__ void k_fields_xfer(XferBatch x, long long total, int to_slots) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    int lo = 0, hi = x.n - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (x.e[mid].off <= e) lo = mid; else hi = mid - 1; }
+    const XferEntry& E = x.e[lo];
+    const long long r = e - E.off;
+    const long long n = r / E.ncomp;
+    const int m = (int)(r - n * E.ncomp);
+    const int i = (int)(n % E.ei), j = (int)((n / E.ei) % E.ej), k = (int)(n / ((long long)E.ei * E.ej));
+    const long long c = (long long)(i + E.lb + 2) + (long long)E.PI * ((j + E.lb + 2) + (long long)E.PJ * (k + E.lb + 2));
+    const int so = E.is_sd ? 3 * (m % 3) + m / 3 : m;
+    double* sl = E.base + (size_t)(E.slot0 + so) * (size_t)E.ncell;
+    if (to_slots) sl[c] = E.host[r];
+    else E.host[r] = sl[c];
+}
 #endif  // TG_COMMON_KERNELS
 }  // namespace tg

@@ -891,13 +891,54 @@ int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp) {
 
 int fields_io(Ctx* c, CaseRec* cs, int n, const int* ib, const int* f, double* const* host, bool upload) {
     if (!c || !cs || n < 0 || (n > 0 && (!ib || !f || !host))) return TRANS_E_ARG;
+    // page-locked arrays of plain fields go in batches, one launch each over the host link; the
+    // rest (pageable arrays, fields with FP32 copies or derived slots) one by one, in the
+    // caller's order (a batch is launched before the next array that is not in it, or that
+    // names a block and field the batch already holds)
+    XferBatch x;
+    std::memset(&x, 0, sizeof(x));
+    long long total = 0;
+    std::vector<std::pair<int, int>> held;
+    auto flush = [&]() {
+        if (x.n == 0) return;
+        launch_fields_xfer(c->stream, x, total, upload ? 1 : 0);
+        c->launches++;
+        std::memset(&x, 0, sizeof(x));
+        total = 0;
+        held.clear();
+    };
     for (int q = 0; q < n; ++q) {
-        int rc = field_io(c, cs, ib[q], f[q], host[q], upload, false);
-        if (rc) {
-            cudaStreamSynchronize(c->stream);    // the arrays already queued are settled either way
-            return rc;
+        const int fq = f[q];
+        const FieldMap fm = field_map(fq);
+        double* mapped = nullptr;
+        long long cnt = 0;
+        if (c->xfer_batch && ib[q] >= 0 && ib[q] < (int)cs->blk.size() && host[q] && fm.slot >= 0 && fq != TRANS_THTC &&
+            fq != TRANS_D && fq != TRANS_DQDXYZ && fq != TRANS_SHOCK && !(fq == TRANS_WT2 && cs->p.IF_RK != 1)) {
+            const DevBlock& bq = cs->blk[ib[q]];
+            cnt = (long long)(bq.NI + 3 - fm.lb) * (bq.NJ + 3 - fm.lb) * (bq.NK + 3 - fm.lb) * fm.ncomp;
+            mapped = mapped_host(host[q], (size_t)cnt * sizeof(double));
         }
+        if (!mapped) {
+            flush();
+            int rc = field_io(c, cs, ib[q], fq, host[q], upload, false);
+            if (rc) {
+                cudaStreamSynchronize(c->stream);    // the arrays already queued are settled either way
+                return rc;
+            }
+            continue;
+        }
+        if (x.n == XFER_MAX || std::find(held.begin(), held.end(), std::make_pair(ib[q], fq)) != held.end()) flush();
+        const DevBlock& b = cs->blk[ib[q]];
+        XferEntry& E = x.e[x.n++];
+        E.base = b.base; E.host = mapped; E.off = total;
+        E.ncell = b.ncell; E.PI = b.PI; E.PJ = b.PJ; E.ei = b.NI + 3 - fm.lb; E.ej = b.NJ + 3 - fm.lb;
+        E.slot0 = fm.slot; E.ncomp = fm.ncomp; E.lb = fm.lb; E.is_sd = fq == TRANS_SD ? 1 : 0;
+        total += cnt;
+        held.emplace_back(ib[q], fq);
+        if (upload && is_geometry(fq)) cs->geom_dirty = true;
     }
+    flush();
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
     return TRANS_OK;
 }
