@@ -157,6 +157,9 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     // TRANS_XFER_BATCH=0: trans_set/get_fields transfer the arrays one launch each (for comparisons)
     const char* xb = std::getenv("TRANS_XFER_BATCH");
     if (xb && std::string(xb) == "0") c->xfer_batch = false;
+    // TRANS_XFER_DMA=1: page-locked arrays too go through the staging buffer by DMA copies
+    const char* xd = std::getenv("TRANS_XFER_DMA");
+    if (xd && std::string(xd) == "1") c->xfer_mapped = false;
     // TRANS_RESID_SPIN=n: polls of the tile staging wait before it gives up (for tests)
     const char* rsp = std::getenv("TRANS_RESID_SPIN");
     if (rsp) c->resid_spin = (unsigned)std::max(0L, std::atol(rsp));

@@ -74,6 +74,7 @@ struct Ctx {
     // -1 times both on the first residual and keeps the faster
     int resid_tma = -1;
     bool xfer_batch = true;              // trans_set/get_fields: page-locked arrays in one launch
+    bool xfer_mapped = true;             // page-locked arrays read in place (false: copied by DMA through the staging buffer)
     std::string resid_tuning;
     ResidTile* d_rtiles[3] = {nullptr, nullptr, nullptr};
     int n_rtiles[3] = {0, 0, 0};

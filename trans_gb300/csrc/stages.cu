@@ -197,7 +197,7 @@ int field_io(Ctx* c, CaseRec* cs, int ib, int f, double* host, bool upload, bool
     size_t bytes = ncells * fm.ncomp * sizeof(double);
     cudaStream_t s = c->stream;
     int is_sd = f == TRANS_SD ? 1 : 0;
-    double* mapped = f == TRANS_THTC ? nullptr : mapped_host(host, bytes);
+    double* mapped = f == TRANS_THTC || !c->xfer_mapped ? nullptr : mapped_host(host, bytes);
     if (mapped) {       // page-locked caller array: transpose in place over the host link
         if (!upload) {
             if (c->mixed && f == TRANS_D) mirror(c, {{S_D, 7}}, 1);
@@ -916,7 +916,7 @@ int fields_io(Ctx* c, CaseRec* cs, int n, const int* ib, const int* f, double* c
             fq != TRANS_D && fq != TRANS_DQDXYZ && fq != TRANS_SHOCK && !(fq == TRANS_WT2 && cs->p.IF_RK != 1)) {
             const DevBlock& bq = cs->blk[ib[q]];
             cnt = (long long)(bq.NI + 3 - fm.lb) * (bq.NJ + 3 - fm.lb) * (bq.NK + 3 - fm.lb) * fm.ncomp;
-            mapped = mapped_host(host[q], (size_t)cnt * sizeof(double));
+            mapped = c->xfer_mapped ? mapped_host(host[q], (size_t)cnt * sizeof(double)) : nullptr;
         }
         if (!mapped) {
             flush();
