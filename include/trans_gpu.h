@@ -217,6 +217,12 @@ int trans_get_integrals(void* ctx, trans_integrals* out);
  * connection) of block ib (Output/OUTPUT_Surfaces.F90:303-305): one value per face of the
  * segment, I fastest, then J, then K, over pointStart..pointEnd of the segment's face indices. */
 int trans_get_wall_cp(void* ctx, int ib, int iconn, double* cp);
+/* Pressure and viscous force of each face of wall segment iconn of block ib, the per-face terms
+ * of the force and moment sums of Output/OUTPUT_ClCdCm.F90:199-264 (before its 2/Area_Ref
+ * scaling): forces[6r .. 6r+5] = pressure x, y, z and viscous x, y, z of face r, the faces in
+ * the order of trans_get_wall_cp.  The moment sums (:250-252) weight them with the face centres,
+ * the mean of the face's four nodes, which the caller holds. */
+int trans_get_wall_forces(void* ctx, int ib, int iconn, double* forces);
 /*
  * Wall distance of GEOM_CalcDST (Geom/CalcDst.F90:127-164) on the device, for any set of points
  * (no context).  xyz: n points, x y z interleaved (the cell centres Xc, Yc, Zc of the interior

@@ -122,3 +122,44 @@ def test_batch_integrals_alone_equal_in_mix(gpu_lib):
     from trans_gb300 import integrals
     assert np.array_equal(cp, integrals.segment_cp(a[0], a[1], host_fields, 0, 3))
     mix.close()
+
+
+def test_wall_forces_per_face_and_moments(gpu_lib):
+    """trans_get_wall_forces: the pressure and viscous force of every face of every wall
+    segment, against the host restatement of the same per-face terms (the same expressions in
+    FP64: 1e-12 of the segment's largest component; in practice bit-identical); summed over the
+    walls they give trans_get_integrals' wall forces; and the moment sums of
+    Output/OUTPUT_ClCdCm.F90:250-252 formed from them with the face centres equal the host
+    moment sums."""
+    from trans_gb300 import integrals
+    from trans_gb300.solver import Solver
+    c, conns, geo, st = small_cascade(Kind_Spatial=3, Kind_Roe=3)
+    s = Solver(c, conns, geo, st, lib=gpu_lib)
+    for ki in range(1, 4):
+        s.iterate(ki)
+    f = _solver_fields(s, c)
+    dev_f, host_f, centres = [], [], []
+    for ib, b in enumerate(c.blocks):
+        for ic, cn in enumerate(conns[b.id], start=1):
+            if cn.BCType != 1:
+                continue
+            dev = s.wall_forces(ib, ic)
+            host = integrals.segment_wall_forces(c, conns, geo, f, ib, ic)
+            assert dev.shape == host.shape
+            scale = np.max(np.abs(host))
+            assert np.max(np.abs(dev - host)) <= TOL * scale, (ib, ic)
+            dev_f.append(dev)
+            host_f.append(host)
+            centres.append(integrals.segment_face_centres(c, conns, ib, ic))
+    total = sum(F.sum(axis=1) for F in dev_f)
+    intg = s.integrals()
+    for q in range(3):
+        assert abs(total[q] - intg["force_p"][q]) <= TOL * max(abs(x) for x in intg["force_p"])
+        assert abs(total[3 + q] - intg["force_v"][q]) <= TOL * max(abs(x) for x in intg["force_v"])
+    ref = (0.25, -0.1, 0.5)
+    m_dev = integrals.wall_moments(dev_f, centres, ref)
+    m_host = integrals.wall_moments(host_f, centres, ref)
+    mscale = max(abs(x) for x in m_host)
+    assert mscale > 0
+    assert max(abs(a - b) for a, b in zip(m_dev, m_host)) <= TOL * mscale
+    s.close()

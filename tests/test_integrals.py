@@ -141,3 +141,41 @@ def test_face_integrals_match_scalar_loops():
     assert scale_p > 0 and scale_v > 0
     assert max(abs(x - y) for x, y in zip(r["force_p"], a[6:9])) <= 1e-13 * scale_p
     assert max(abs(x - y) for x, y in zip(r["force_v"], a[9:12])) <= 1e-13 * scale_v
+
+
+def test_wall_moments_are_minus_r_cross_f():
+    """The moment sums of Output/OUTPUT_ClCdCm.F90:250-252 are minus the sum of r x F, with r
+    from the reference point to the face centre; the face centre is the mean of four nodes at
+    node index 1 on a min face and N-1 on a max face (the reference's Iw = NI1)."""
+    from trans_gb300 import case as CS
+    c, conns, geo, st = small_channel()
+    b = c.blocks[0]
+    X = b.xyz
+    ni, nj, nk = b.dims
+    rng = np.random.default_rng(3)
+    for ic, cn in enumerate(conns[b.id], start=1):
+        if cn.BCType != 1:
+            continue
+        Xc = integrals.segment_face_centres(c, conns, 0, ic)
+        I, J, K = face_cells(cn)
+        d = cn.IJKDirect - 1
+        node = 0 if cn.pointStart[d] == 1 else [ni, nj, nk][d] - 2
+        q = 0
+        idx = [I - 1, J - 1, K - 1]
+        idx[d] = np.full_like(idx[d], node)
+        o = [a for a in range(3) if a != d]
+        ref = np.zeros((3, len(I)))
+        for a in (0, 1):
+            for e in (0, 1):
+                jdx = list(idx)
+                jdx[o[0]] = idx[o[0]] + a
+                jdx[o[1]] = idx[o[1]] + e
+                ref += X[jdx[0], jdx[1], jdx[2]].T
+        np.testing.assert_allclose(Xc, ref / 4.0, rtol=0, atol=1e-14 * np.max(np.abs(X)))
+        F = rng.standard_normal((6, Xc.shape[1]))
+        r0 = (0.3, -0.2, 0.1)
+        Cm = integrals.wall_moments([F], [Xc], r0)
+        r = Xc - np.array(r0)[:, None]
+        cross = np.cross(r.T, (F[:3] + F[3:]).T).sum(axis=0)
+        np.testing.assert_allclose(Cm, -cross, rtol=1e-12, atol=1e-12)
+        q += 1

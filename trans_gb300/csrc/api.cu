@@ -161,6 +161,11 @@ int trans_get_wall_cp(void* ctx, int ib, int iconn, double* cp) {
     return c ? wall_cp(c, first_case(c), ib, iconn, cp) : TRANS_E_ARG;
 }
 
+int trans_get_wall_forces(void* ctx, int ib, int iconn, double* forces) {
+    Ctx* c = as_ctx(ctx);
+    return c ? wall_cp(c, first_case(c), ib, iconn, forces, true) : TRANS_E_ARG;
+}
+
 int trans_sync(void* ctx) {
     Ctx* c = as_ctx(ctx);
     if (!c) return TRANS_E_ARG;

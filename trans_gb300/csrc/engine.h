@@ -197,7 +197,8 @@ int upload_cdev(Ctx* c);
 // integrated quantities of one case from its current state (k_integrals.cu kernels)
 int integrals(Ctx* c, CaseRec* cs, trans_integrals* out);
 int all_integrals(Ctx* c, std::vector<trans_integrals>& out);     // every case, in c->cases order
-int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp);
+// Cp of each face of a wall segment, or (forces) its pressure and viscous force, 6 per face
+int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp, bool forces = false);
 int finalize_geometry(Ctx* c);
 int reduce_norms(Ctx* c);
 int run_iteration(Ctx* c);               // one outer iteration of every case at its KI

@@ -114,7 +114,25 @@ __global__ void k_wall_cp(const DevBlock* __restrict__ blks, const BCEntry* __re
     cp[r] = 2.0 * (slot(b, S_PP)[E.s[0]] - cdev[b.cs].p.PPF);
 }
 
+// pressure and viscous force of each face of one segment: f[6r .. 6r+5] = (pressure x, y, z,
+// viscous x, y, z) of face r, the terms k_integrals sums
+__global__ void k_wall_forces(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int e0, int n,
+                              const CaseDev* __restrict__ cdev, double* __restrict__ f) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const BCEntry E = ent[e0 + r];
+    double q[NINTG];
+    for (int m = 0; m < NINTG; ++m) q[m] = 0.0;
+    face_terms(blks, E, cdev[blks[E.blk].cs], q);
+    for (int m = 0; m < 6; ++m) f[(size_t)6 * r + m] = q[6 + m];
+}
+
 }  // namespace
+
+void launch_wall_forces(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int e0, int n, const CaseDev* cdev,
+                        double* f) {
+    if (n > 0) k_wall_forces<<<(n + 127) / 128, 128, 0, s>>>(blks, ent, e0, n, cdev, f);
+}
 
 void launch_integrals(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const int* first, int ncase,
                       const CaseDev* cdev, double* out) {

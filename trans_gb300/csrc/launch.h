@@ -48,6 +48,8 @@ void launch_integrals(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, 
                       const CaseDev* cdev, double* out);
 void launch_wall_cp(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int e0, int n, const CaseDev* cdev,
                     double* cp);
+void launch_wall_forces(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, int e0, int n, const CaseDev* cdev,
+                        double* f);
 
 // the mixed path's residual from TMA-staged shared-memory tiles (resid_tma.cuh, k_mixed.cu)
 constexpr int RT_X = 32;                  // cells along i of a direction-2/3 tile

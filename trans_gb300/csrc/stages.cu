@@ -857,7 +857,7 @@ int integrals(Ctx* c, CaseRec* cs, trans_integrals* out) {
     return fail(c, TRANS_E_ARG, "case not in the context");
 }
 
-int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp) {
+int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp, bool forces) {
     if (!c || !cs || !cp) return TRANS_E_ARG;
     if (ib < 0 || ib >= (int)cs->hb.size()) return fail(c, TRANS_E_ARG, "bad block index");
     const HostBlock& h = cs->hb[ib];
@@ -880,11 +880,20 @@ int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp) {
             e0 += cnt;
         }
     if (e0 + n > c->bc_first[k + 1]) return fail(c, TRANS_E_ARG, "wall segment outside the boundary table");
-    if (!c->d_stage || c->stage_doubles < (size_t)n) return fail(c, TRANS_E_ARG, "staging buffer too small");
-    launch_wall_cp(c->stream, c->d_blk, c->d_bc, (int)e0, (int)n, c->d_cdev, c->d_stage);
+    const size_t words = (size_t)n * (forces ? 6 : 1);
+    if (!c->d_stage || c->stage_doubles < words) {      // the staging buffer holds the segment's values
+        CK(cudaStreamSynchronize(c->stream));
+        if (c->d_stage) cudaFree(c->d_stage);
+        c->d_stage = nullptr;
+        c->stage_doubles = 0;
+        CK(cudaMalloc(&c->d_stage, words * sizeof(double)));
+        c->stage_doubles = words;
+    }
+    if (forces) launch_wall_forces(c->stream, c->d_blk, c->d_bc, (int)e0, (int)n, c->d_cdev, c->d_stage);
+    else launch_wall_cp(c->stream, c->d_blk, c->d_bc, (int)e0, (int)n, c->d_cdev, c->d_stage);
     c->launches++;
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(cp, c->d_stage, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(cp, c->d_stage, sizeof(double) * words, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return TRANS_OK;
 }

@@ -10,6 +10,8 @@ Semantics follow the reference's output routines, generalised to every inlet/out
   total pressure  Output/Average_Field.F90:66,157 (p (1 + 0.2 M^2)^3.5, mass averaged)
   wall force      Output/OUTPUT_ClCdCm.F90:114-264 (pressure part (p - PPF) S Sgn, viscous part
                   mu_w/(Dst Ref) times the tangential velocity times |S|; before 2/Area_Ref)
+  wall moment     Output/OUTPUT_ClCdCm.F90:250-265 (face force times the arm from the reference
+                  point to the face centre, the mean of the face's four nodes)
 This is a host (numpy) evaluation from downloaded fields; the library computes the same sums
 on the device (trans_get_integrals), and the tests hold the two against each other.
 Inputs are the full-extent (-2..N+2) arrays of trans_gb300.solver / oracle get_field.
@@ -124,6 +126,80 @@ def wall_forces(case, conns, geo, fields):
             for q in range(3):
                 Fv[q] += float(np.sum(tau * (u[q] * Sl - vcon * S[q])))
     return Fp, Fv
+
+
+def segment_wall_forces(case, conns, geo, fields, ib, iconn):
+    """Pressure and viscous force of each face of wall segment iconn (1-based) of block ib, as
+    an array (6, nfaces): rows pressure x, y, z, viscous x, y, z; the faces I fastest, then J,
+    then K (the per-face terms of wall_forces, Output/OUTPUT_ClCdCm.F90:199-248)."""
+    P = case.params
+    b = case.blocks[ib]
+    g = geo[b.id]
+    cn = conns[b.id][iconn - 1]
+    V, PP, T = fields[ib]["V"], fields[ib]["PP"], fields[ib]["T"]
+    d, ci, cg, cf, is_min = _face_pairs(cn)
+    Sl = _at(g["GRAD"], cf, d)
+    S = [_at(g["SD"], cf, (d, q)) / Sl for q in range(3)]
+    sgn = -1.0 if is_min else 1.0
+    P2 = _at(PP, ci) - P.PPF
+    TT = _at(T, ci)
+    mu_w = (1.0 + P.Csthlnd) / (TT * P.Csth1 + P.Csthlnd) * (P.Csth1 * TT) ** 1.5
+    den = _at(V, ci, 0)
+    u = [_at(V, ci, q + 1) / den for q in range(3)]
+    vcon = u[0] * S[0] * Sl + u[1] * S[1] * Sl + u[2] * S[2] * Sl
+    tau = 1.0 * mu_w / _at(g["DST"], ci) / P.Ref
+    out = np.empty((6, len(P2)))
+    for q in range(3):
+        out[q] = P2 * S[q] * Sl * sgn
+        out[3 + q] = tau * (u[q] * Sl - vcon * S[q])
+    return out
+
+
+def segment_face_centres(case, conns, ib, iconn):
+    """Moment arm point of each face of a wall segment, the mean of four nodes
+    (Output/OUTPUT_ClCdCm.F90:152-154, 173-175, 194-196): an array (3, nfaces), faces in the
+    order of segment_wall_forces.  As the reference has it, the nodes lie at node index 1 on a
+    min face and at N-1 (NI1, NJ1, NK1) -- one node layer inside the wall -- on a max face."""
+    b = case.blocks[ib]
+    cn = conns[b.id][iconn - 1]
+    d, ci, cg, cf, is_min = _face_pairs(cn)
+    X = b.xyz
+    lo = [np.asarray(cf[q]) - 1 for q in range(3)]       # 0-based node of the face / of the cell's low corner
+    if not is_min:
+        lo[d] = lo[d] - 1                                 # Iw = NI1 on a max face
+    corners = []
+    for a in (0, 1):
+        for e in (0, 1):
+            idx = list(lo)
+            o = [q for q in range(3) if q != d]
+            idx[o[0]] = lo[o[0]] + a
+            idx[o[1]] = lo[o[1]] + e
+            corners.append(X[idx[0], idx[1], idx[2]])
+    # the reference's order: (a, e) = (0, 0), (1, 0), (0, 1), (1, 1) summed left to right, / 4
+    c = (((corners[0] + corners[2]) + corners[1]) + corners[3]) / 4.0
+    return c.T.copy()
+
+
+def wall_moments(forces, centres, ref):
+    """Moment sums of Output/OUTPUT_ClCdCm.F90:250-252 over the faces of wall segments, before
+    the 2/Area_Ref/B_Ref (or C_Ref) scaling and the sign of :263-265: forces and centres are
+    lists of the (6, n) and (3, n) arrays of each segment; ref = (Xwc, Ywc, Zwc).  Returns
+    (Cmx, Cmy, Cmz)."""
+    Cmx = Cmy = Cmz = 0.0
+    for F, Xc in zip(forces, centres):
+        dCx, dCy, dCz = F[0] + F[3], F[1] + F[4], F[2] + F[5]
+        rx, ry, rz = Xc[0] - ref[0], Xc[1] - ref[1], Xc[2] - ref[2]
+        for q in range(F.shape[1]):
+            Cmx = Cmx + dCy[q] * rz[q] - dCz[q] * ry[q]
+            Cmz = Cmz + dCx[q] * ry[q] - dCy[q] * rx[q]
+            Cmy = Cmy + dCz[q] * rx[q] - dCx[q] * rz[q]
+    return Cmx, Cmy, Cmz
+
+
+def moment_coefficients(Cm, area_ref, b_ref, c_ref):
+    """The scaled moment coefficients of Output/OUTPUT_ClCdCm.F90:263-265."""
+    Cmx, Cmy, Cmz = Cm
+    return -Cmx * 2.0 / area_ref / b_ref, -Cmy * 2.0 / area_ref / b_ref, Cmz * 2.0 / area_ref / c_ref
 
 
 def wall_force(case, conns, geo, fields):

@@ -123,6 +123,17 @@ class Solver:
                     "get_wall_cp")
         return cp
 
+    def wall_forces(self, ib, iconn):
+        """Pressure and viscous force of each face of wall segment iconn (1-based) of block ib:
+        an array (6, nfaces), rows pressure x, y, z and viscous x, y, z, the faces in the order
+        of wall_cp (I fastest, then J, then K)."""
+        cn = self._conns[self.blocks[ib].id][iconn - 1]
+        n = int(np.prod([cn.pointEnd[q] - cn.pointStart[q] + 1 for q in range(3)]))
+        f = np.zeros((6, n), order="F")
+        self._check(self.lib.trans_get_wall_forces(self.ctx, ib, iconn, f.ctypes.data_as(C.POINTER(C.c_double))),
+                    "get_wall_forces")
+        return f
+
     def norms(self):
         nb = len(self.blocks)
         norms = (abi.TransNorms * nb)()
