@@ -113,10 +113,12 @@ struct Tile {             // a run of consecutive interior cells (or faces) of o
 struct XferEntry {
     double* base;                 // the block's slot arena
     double* host;                 // device address of the page-locked array
-    long long off;                // first element within the batch
+    long long off;                // first chunk within the batch
+    long long count;              // elements of the array
     int ncell, PI, PJ, ei, ej, slot0, ncomp, lb, is_sd, pad_;
 };
-constexpr int XFER_MAX = 60;      // entries per launch (the batch stays under 4 KB of kernel parameters)
+constexpr int XFER_CHUNK = 4;     // consecutive elements per thread
+constexpr int XFER_MAX = 56;      // entries per launch (the batch stays under 4 KB of kernel parameters)
 struct XferBatch {
     XferEntry e[XFER_MAX];
     int n, pad_;

@@ -2113,25 +2113,54 @@ __global__ void k_field_xfer(DevBlock b, int slot0, int ncomp, int lb, int is_sd
     else stage[e] = sl[c];
 }
 
-// Several Fortran-layout arrays in page-locked host memory <-> slots in one launch: entry q
-// covers elements [off[q], off[q+1]) of the concatenated arrays, read or written over the
-// host link directly (component fastest, so a warp touches 256 consecutive bytes of host
-// memory); one launch keeps enough reads in flight to fill the link.
+// Several Fortran-layout arrays in page-locked host memory <-> slots in one launch: each thread
+// moves a chunk of XFER_CHUNK consecutive elements of one array (component fastest) with 16-byte
+// accesses of the host side, so a warp keeps 1 KB of the host link in flight per access; entry q
+// owns chunks [off[q], off[q+1]).  The arrays start on 16-byte boundaries (page-locked
+// allocations), and every chunk starts at a multiple of XFER_CHUNK within its array.
 __global__ void k_fields_xfer(XferBatch x, long long total, int to_slots) {
-    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= total) return;
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
     int lo = 0, hi = x.n - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (x.e[mid].off <= e) lo = mid; else hi = mid - 1; }
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (x.e[mid].off <= g) lo = mid; else hi = mid - 1; }
     const XferEntry& E = x.e[lo];
-    const long long r = e - E.off;
-    const long long n = r / E.ncomp;
-    const int m = (int)(r - n * E.ncomp);
-    const int i = (int)(n % E.ei), j = (int)((n / E.ei) % E.ej), k = (int)(n / ((long long)E.ei * E.ej));
-    const long long c = (long long)(i + E.lb + 2) + (long long)E.PI * ((j + E.lb + 2) + (long long)E.PJ * (k + E.lb + 2));
-    const int so = E.is_sd ? 3 * (m % 3) + m / 3 : m;
-    double* sl = E.base + (size_t)(E.slot0 + so) * (size_t)E.ncell;
-    if (to_slots) sl[c] = E.host[r];
-    else E.host[r] = sl[c];
+    const long long r0 = (g - E.off) * XFER_CHUNK;
+    const int m = (int)(E.count - r0 < XFER_CHUNK ? E.count - r0 : XFER_CHUNK);
+    double v[XFER_CHUNK];
+    long long cs[XFER_CHUNK];
+#pragma unroll
+    for (int u = 0; u < XFER_CHUNK; ++u) {
+        const long long r = r0 + u;
+        const long long n = r / E.ncomp;
+        const int mc = (int)(r - n * E.ncomp);
+        const int i = (int)(n % E.ei), j = (int)((n / E.ei) % E.ej), k = (int)(n / ((long long)E.ei * E.ej));
+        const long long c = (long long)(i + E.lb + 2) + (long long)E.PI * ((j + E.lb + 2) + (long long)E.PJ * (k + E.lb + 2));
+        const int so = E.is_sd ? 3 * (mc % 3) + mc / 3 : mc;
+        cs[u] = (long long)(E.slot0 + so) * (long long)E.ncell + c;
+    }
+    if (to_slots) {
+        if (m == XFER_CHUNK) {
+            const double2* h = reinterpret_cast<const double2*>(E.host + r0);
+#pragma unroll
+            for (int u = 0; u < XFER_CHUNK / 2; ++u) {
+                const double2 w = h[u];
+                v[2 * u] = w.x;
+                v[2 * u + 1] = w.y;
+            }
+        } else {
+            for (int u = 0; u < m; ++u) v[u] = E.host[r0 + u];
+        }
+        for (int u = 0; u < m; ++u) E.base[cs[u]] = v[u];
+    } else {
+        for (int u = 0; u < m; ++u) v[u] = E.base[cs[u]];
+        if (m == XFER_CHUNK) {
+            double2* h = reinterpret_cast<double2*>(E.host + r0);
+#pragma unroll
+            for (int u = 0; u < XFER_CHUNK / 2; ++u) h[u] = make_double2(v[2 * u], v[2 * u + 1]);
+        } else {
+            for (int u = 0; u < m; ++u) E.host[r0 + u] = v[u];
+        }
+    }
 }
 #endif  // TG_COMMON_KERNELS
 }  // namespace tg

@@ -936,13 +936,22 @@ int fields_io(Ctx* c, CaseRec* cs, int n, const int* ib, const int* f, double* c
             }
             continue;
         }
+        if ((uintptr_t)mapped & 15) {          // 16-byte host accesses need an aligned array
+            flush();
+            int rc = field_io(c, cs, ib[q], fq, host[q], upload, false);
+            if (rc) {
+                cudaStreamSynchronize(c->stream);
+                return rc;
+            }
+            continue;
+        }
         if (x.n == XFER_MAX || std::find(held.begin(), held.end(), std::make_pair(ib[q], fq)) != held.end()) flush();
         const DevBlock& b = cs->blk[ib[q]];
         XferEntry& E = x.e[x.n++];
-        E.base = b.base; E.host = mapped; E.off = total;
+        E.base = b.base; E.host = mapped; E.off = total; E.count = cnt;
         E.ncell = b.ncell; E.PI = b.PI; E.PJ = b.PJ; E.ei = b.NI + 3 - fm.lb; E.ej = b.NJ + 3 - fm.lb;
         E.slot0 = fm.slot; E.ncomp = fm.ncomp; E.lb = fm.lb; E.is_sd = fq == TRANS_SD ? 1 : 0;
-        total += cnt;
+        total += (cnt + XFER_CHUNK - 1) / XFER_CHUNK;      // chunks
         held.emplace_back(ib[q], fq);
         if (upload && is_geometry(fq)) cs->geom_dirty = true;
     }
