@@ -296,19 +296,22 @@ def test_rc_mode_2_changes_nothing(gpu_lib):
 
 ROTATING = [dict(Kind_Spatial=3, Kind_Roe=1), dict(Kind_Spatial=2, Kind_Roe=1), dict(Kind_Spatial=1, Kind_Roe=1),
             dict(Kind_Spatial=4, Kind_Roe=1, F_limiter2=0.05), dict(Kind_Spatial=3, Kind_Roe=2),
-            dict(Kind_Spatial=3, Kind_Roe=3), dict(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=1)]
+            dict(Kind_Spatial=3, Kind_Roe=3), dict(Kind_Spatial=3, Kind_Roe=3, Kind_RotMod=1),
+            dict(Kind_Spatial=2, Kind_Roe=1, IF_Precondition=1),
+            dict(Kind_Spatial=3, Kind_Roe=1, IF_RK=1, CFL_Sub_start=1.0, CFL_Sub_end=1.0)]
 
 
 @pytest.mark.parametrize("scheme", ROTATING, ids=["mdcd_roe", "muscl_roe", "muscl2_roe", "mdcdhyb_roe", "mdcd_roerot",
-                                                  "mdcd_ausmpw", "mdcd_ausmpw_rc"])
+                                                  "mdcd_ausmpw", "mdcd_ausmpw_rc", "muscl_roe_precond", "mdcd_roe_rk3"])
 def test_rotating_frame(gpu_lib, scheme):
     """A frame rotating about x (omega(1) != 0) on the annular sector, hub turning with the frame
     and casing at rest: the frame speeds rccl/rccr * omega of the Roe schemes (reconstructed as
     each spatial scheme does: limited in MUSCL and MUSCL2, MDCD states in I and J and the face
     average in K for MDCD, the face average for MDCDHYB), the Coriolis and centrifugal source
     of DIFFUSION_Centered.F90:812-822, the rotating wall, inlet and outlet conditions, the
-    rothalpy of the update and, with RC correction, omega in the rotation tensor.  15 iterations
-    bit-identical."""
+    rothalpy of the update and, with RC correction, omega in the rotation tensor; also with
+    low-Mach preconditioning and with the SSP-RK3 stages (whose update has no rotation term, as
+    in the reference).  15 iterations bit-identical."""
     from helpers import small_annular
     c, conns, geo, st = small_annular(**scheme)
     assert c.params.omega[0] > 0.5
