@@ -46,8 +46,8 @@ void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long lon
 }  // namespace tg
 
 namespace tg {
-void launch_fields_xfer(cudaStream_t s, const XferBatch& x, long long total, int to_slots) {
-    if (total > 0) k_fields_xfer<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(x, total, to_slots);
+void launch_fields_xfer(cudaStream_t s, const XferBatch& x, long long total, int to_slots, int chunk) {
+    if (total > 0) k_fields_xfer<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(x, total, to_slots, chunk);
 }
 void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, int lb, int is_sd, double* stage, int to_slots) {
     long long n = (long long)(b.NI + 3 - lb) * (b.NJ + 3 - lb) * (b.NK + 3 - lb) * ncomp;

@@ -2114,22 +2114,25 @@ __global__ void k_field_xfer(DevBlock b, int slot0, int ncomp, int lb, int is_sd
 }
 
 // Several Fortran-layout arrays in page-locked host memory <-> slots in one launch: each thread
-// moves a chunk of XFER_CHUNK consecutive elements of one array (component fastest) with 16-byte
-// accesses of the host side, so a warp keeps 1 KB of the host link in flight per access; entry q
-// owns chunks [off[q], off[q+1]).  The arrays start on 16-byte boundaries (page-locked
-// allocations), and every chunk starts at a multiple of XFER_CHUNK within its array.
-__global__ void k_fields_xfer(XferBatch x, long long total, int to_slots) {
+// moves a chunk of ch consecutive elements of one array (component fastest); uploads take chunks
+// of XFER_CHUNK with 16-byte reads of the host side (a warp keeps 1 KB of the host link in
+// flight per access), downloads one element per thread (measured faster: the writes to the host
+// side stream from many more threads).  Entry q owns chunks [off[q], off[q+1]); the arrays start
+// on 16-byte boundaries (page-locked allocations), and every chunk starts at a multiple of ch
+// within its array.
+__global__ void k_fields_xfer(XferBatch x, long long total, int to_slots, int ch) {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total) return;
     int lo = 0, hi = x.n - 1;
     while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (x.e[mid].off <= g) lo = mid; else hi = mid - 1; }
     const XferEntry& E = x.e[lo];
-    const long long r0 = (g - E.off) * XFER_CHUNK;
-    const int m = (int)(E.count - r0 < XFER_CHUNK ? E.count - r0 : XFER_CHUNK);
+    const long long r0 = (g - E.off) * ch;
+    const int m = (int)(E.count - r0 < ch ? E.count - r0 : ch);
     double v[XFER_CHUNK];
     long long cs[XFER_CHUNK];
 #pragma unroll
     for (int u = 0; u < XFER_CHUNK; ++u) {
+        if (u >= m) break;
         const long long r = r0 + u;
         const long long n = r / E.ncomp;
         const int mc = (int)(r - n * E.ncomp);
@@ -2139,7 +2142,7 @@ __global__ void k_fields_xfer(XferBatch x, long long total, int to_slots) {
         cs[u] = (long long)(E.slot0 + so) * (long long)E.ncell + c;
     }
     if (to_slots) {
-        if (m == XFER_CHUNK) {
+        if (m == XFER_CHUNK && ch == XFER_CHUNK) {
             const double2* h = reinterpret_cast<const double2*>(E.host + r0);
 #pragma unroll
             for (int u = 0; u < XFER_CHUNK / 2; ++u) {
@@ -2153,7 +2156,7 @@ __global__ void k_fields_xfer(XferBatch x, long long total, int to_slots) {
         for (int u = 0; u < m; ++u) E.base[cs[u]] = v[u];
     } else {
         for (int u = 0; u < m; ++u) v[u] = E.base[cs[u]];
-        if (m == XFER_CHUNK) {
+        if (m == XFER_CHUNK && ch == XFER_CHUNK) {
             double2* h = reinterpret_cast<double2*>(E.host + r0);
 #pragma unroll
             for (int u = 0; u < XFER_CHUNK / 2; ++u) h[u] = make_double2(v[2 * u], v[2 * u + 1]);

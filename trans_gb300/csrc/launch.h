@@ -37,8 +37,9 @@ void launch_rk_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, i
 void launch_rk_vupdate(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts,
                        int d_fp32);
 void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, int lb, int is_sd, double* stage, int to_slots);
-// several page-locked Fortran-layout arrays <-> slots in one launch (total = their elements)
-void launch_fields_xfer(cudaStream_t s, const XferBatch& x, long long total, int to_slots);
+// several page-locked Fortran-layout arrays <-> slots in one launch (total = chunks of `chunk`
+// consecutive elements)
+void launch_fields_xfer(cudaStream_t s, const XferBatch& x, long long total, int to_slots, int chunk);
 double probe_fma_gflops(int fp64);
 double probe_chain_us(int chained, int grid);   // floor of one dependent sweep step (k_mixed.cu)
 void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off);

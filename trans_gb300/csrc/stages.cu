@@ -907,10 +907,11 @@ int fields_io(Ctx* c, CaseRec* cs, int n, const int* ib, const int* f, double* c
     XferBatch x;
     std::memset(&x, 0, sizeof(x));
     long long total = 0;
+    const int ch = upload ? XFER_CHUNK : 1;      // elements per thread
     std::vector<std::pair<int, int>> held;
     auto flush = [&]() {
         if (x.n == 0) return;
-        launch_fields_xfer(c->stream, x, total, upload ? 1 : 0);
+        launch_fields_xfer(c->stream, x, total, upload ? 1 : 0, ch);
         c->launches++;
         std::memset(&x, 0, sizeof(x));
         total = 0;
@@ -951,7 +952,7 @@ int fields_io(Ctx* c, CaseRec* cs, int n, const int* ib, const int* f, double* c
         E.base = b.base; E.host = mapped; E.off = total; E.count = cnt;
         E.ncell = b.ncell; E.PI = b.PI; E.PJ = b.PJ; E.ei = b.NI + 3 - fm.lb; E.ej = b.NJ + 3 - fm.lb;
         E.slot0 = fm.slot; E.ncomp = fm.ncomp; E.lb = fm.lb; E.is_sd = fq == TRANS_SD ? 1 : 0;
-        total += (cnt + XFER_CHUNK - 1) / XFER_CHUNK;      // chunks
+        total += (cnt + ch - 1) / ch;      // chunks
         held.emplace_back(ib[q], fq);
         if (upload && is_geometry(fq)) cs->geom_dirty = true;
     }
