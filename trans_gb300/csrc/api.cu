@@ -80,7 +80,7 @@ int trans_iterate(void* ctx, int ki, trans_norms* norms) {
     Ctx* c = as_ctx(ctx);
     if (!c || c->cases.empty()) return TRANS_E_ARG;
     set_ki(c, ki);
-    int rc = run_iteration(c);
+    int rc = run_iterations(c, 1);          // replayed as a one-iteration graph once tuned
     if (rc) return rc;
     if (norms) std::copy(c->cases[0]->norms.begin(), c->cases[0]->norms.end(), norms);
     return TRANS_OK;

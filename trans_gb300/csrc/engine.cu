@@ -227,6 +227,7 @@ void free_worklists(Ctx* c) {
     c->tile_shape[0] = c->tile_shape[1] = c->tile_shape[2] = 0;
     if (c->h_norms) { cudaFreeHost(c->h_norms); c->h_norms = nullptr; }
     if (c->iter_exec) { cudaGraphExecDestroy(c->iter_exec); c->iter_exec = nullptr; }
+    if (c->iter1_exec) { cudaGraphExecDestroy(c->iter1_exec); c->iter1_exec = nullptr; }
     c->iter_n = 0;
     if (c->h_cdev) { cudaFreeHost(c->h_cdev); c->h_cdev = nullptr; }
     if (c->sweep_exec) { cudaGraphExecDestroy(c->sweep_exec); c->sweep_exec = nullptr; }

@@ -111,6 +111,8 @@ struct Ctx {
     cudaGraphExec_t iter_exec = nullptr;
     int iter_n = 0;
     long long iter_launches = 0;
+    cudaGraphExec_t iter1_exec = nullptr;  // one iteration (trans_iterate, and the rest of a run)
+    long long iter1_launches = 0;
     bool graphs = true;
     std::vector<trans_norms> norms;      // per block of the context
     CaseDev* d_cdev = nullptr;           // per case slot

@@ -694,8 +694,11 @@ bool switches_fixed(Ctx* c, int n) {
     return true;
 }
 
+// capture n iterations into c->iter_exec (n = GRAPH_ITERS) or c->iter1_exec (n = 1)
 int capture_iterations(Ctx* c, int n) {
-    if (c->iter_exec) { cudaGraphExecDestroy(c->iter_exec); c->iter_exec = nullptr; c->iter_n = 0; }
+    cudaGraphExec_t& exec = n == 1 ? c->iter1_exec : c->iter_exec;
+    if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+    if (n != 1) c->iter_n = 0;
     if (c->sweep_mode == 3 && !c->d_tiles) {          // allocations cannot happen inside the capture
         int rc = build_tiles(c, c->tile_default[0], c->tile_default[1], c->tile_default[2]);
         if (rc) return rc;
@@ -725,14 +728,18 @@ int capture_iterations(Ctx* c, int n) {
         cudaGetLastError();
         return fail(c, TRANS_E_CUDA, std::string("iteration graph capture: ") + cudaGetErrorString(e));
     }
-    e = cudaGraphInstantiate(&c->iter_exec, g, 0);
+    e = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return fail(c, TRANS_E_CUDA, std::string("iteration graph instantiate: ") + cudaGetErrorString(e));
     }
-    c->iter_n = n;
-    c->iter_launches = c->launches - launches0;       // kernels per replay
+    if (n == 1) {
+        c->iter1_launches = c->launches - launches0;
+    } else {
+        c->iter_n = n;
+        c->iter_launches = c->launches - launches0;       // kernels per replay
+    }
     c->launches = launches0;
     return TRANS_OK;
 }
@@ -751,24 +758,27 @@ int run_iterations(Ctx* c, int n) {
         first = false;
         // an ordinary iteration builds the work lists and the geometry terms and tunes the
         // sweeps; graphs replay iterations whose switches (CFL ramp, turbulence) are fixed
-        const bool graph = c->graphs && c->built && c->sweep_mode >= 0 && n - done >= GRAPH_ITERS &&
-                           switches_fixed(c, GRAPH_ITERS);
-        if (!graph) {
+        // (a single iteration replays a one-iteration graph: its switches are uploaded with it)
+        const bool tuned = c->graphs && c->built && c->sweep_mode >= 0 && !(c->mixed && c->resid_tma < 0);
+        const bool graph = tuned && n - done >= GRAPH_ITERS && switches_fixed(c, GRAPH_ITERS);
+        const bool graph1 = tuned && !graph && n - done < GRAPH_ITERS;
+        if (!graph && !graph1) {
             if ((rc = run_iteration(c))) return rc;
             ++done;
             continue;
         }
-        const int m = GRAPH_ITERS;
+        const int m = graph ? GRAPH_ITERS : 1;
         if ((rc = finalize_geometry(c)) || (rc = upload_cdev(c))) return rc;
-        if ((!c->iter_exec || c->iter_n != m) && capture_iterations(c, m) != TRANS_OK) {
+        const bool have = graph ? (c->iter_exec && c->iter_n == m) : c->iter1_exec != nullptr;
+        if (!have && capture_iterations(c, m) != TRANS_OK) {
             c->graphs = false;                  // not capturable here: launch directly from now on
             if ((rc = run_iteration(c))) return rc;
             ++done;
             continue;
         }
-        CK(cudaGraphLaunch(c->iter_exec, c->stream));
+        CK(cudaGraphLaunch(graph ? c->iter_exec : c->iter1_exec, c->stream));
         CK(cudaStreamSynchronize(c->stream));
-        c->launches += c->iter_launches;
+        c->launches += graph ? c->iter_launches : c->iter1_launches;
         const int nblk = (int)c->blk.size();
         int nan = 0;
         for (int q = 0; q < m; ++q) {
