@@ -210,6 +210,21 @@ double trans_probe_chain_us(int chained, int grid);
  * norms as for trans_iterate (last iteration).  No reference counterpart: benchmarking. */
 int trans_time_iterations(void* ctx, int ki_first, int n, double* ms, trans_norms* norms);
 int trans_sync(void* ctx);
+/*
+ * Cross-rank 1-to-1 interfaces (BC/PARALLEL_BC_P2P.F90:1-257, PARALLEL_BC_sendrecv_blk, as
+ * Common/PARALLEL_Funcs.F90:57-87 calls it after BC_Boundarys): a kind-9 connection whose target
+ * block is not in the context is left out of the context's boundary pass; the caller exchanges
+ * it after TRANS_STAGE_BC_STATE (sweep -1) and TRANS_STAGE_BC_GRAD (sweep 0).
+ * trans_halo_pack writes segment iconn of block ib's words into buf (host memory), face cells in
+ * the segment's K, J, I order: sweep -1 36 words per face cell (layer 0: V(1:7), PP, T, Rmiu,
+ * Rds(1:3), shock; layers 1 and 2: V(1:7), PP, T, Rmiu, shock), sweep 0 18 (DqDxyz of layer 0),
+ * in FP64 (the reference sends MPI_REAL).  trans_halo_unpack fills the segment's ghost layers
+ * from the partner segment's words (partner = the target block's connection TargetConn) through
+ * the same index transform and rotation as the same-rank copy, so a split case iterates as the
+ * whole case does.  Synchronous; TRANS_E_ARG for a connection that is not of kind 9.
+ */
+int trans_halo_pack(void* ctx, int sweep, int ib, int iconn, double* buf);
+int trans_halo_unpack(void* ctx, int sweep, int ib, int iconn, const trans_conn* partner, const double* buf);
 /* Integrated quantities of the current state (after the last iteration's update; ghost cells
  * as the last boundary pass left them, as the reference's output routines see them). */
 int trans_get_integrals(void* ctx, trans_integrals* out);

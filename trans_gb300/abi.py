@@ -169,6 +169,8 @@ def bind_common(lib):
     lib.trans_get_integrals.argtypes = [vp, C.POINTER(TransIntegrals)]
     lib.trans_get_wall_cp.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
     lib.trans_get_wall_forces.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    lib.trans_halo_pack.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    lib.trans_halo_unpack.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(TransConn), C.POINTER(C.c_double)]
     lib.trans_batch_get_integrals.argtypes = [vp, C.c_int, C.POINTER(TransIntegrals)]
     lib.trans_batch_integrals.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(TransIntegrals), C.c_int]
     lib.trans_batch_get_wall_cp.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
@@ -196,7 +198,7 @@ EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field
             "trans_kernel_class", "trans_batch_create", "trans_batch_case_bytes", "trans_batch_add",
             "trans_batch_remove", "trans_batch_set_field", "trans_batch_get_field", "trans_batch_iterate",
             "trans_batch_case_norms", "trans_batch_bytes_in_use", "trans_batch_cases", "trans_prepare",
-            "trans_batch_time_iterations", "trans_get_integrals", "trans_get_wall_cp", "trans_get_wall_forces",
+            "trans_batch_time_iterations", "trans_get_integrals", "trans_get_wall_cp", "trans_get_wall_forces", "trans_halo_pack", "trans_halo_unpack",
             "trans_batch_get_integrals", "trans_batch_integrals", "trans_batch_get_wall_cp", "trans_wall_distance",
             "trans_set_fields", "trans_get_fields", "trans_batch_set_fields", "trans_batch_get_fields",
             "trans_block_metrics"]

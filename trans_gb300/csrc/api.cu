@@ -166,6 +166,16 @@ int trans_get_wall_forces(void* ctx, int ib, int iconn, double* forces) {
     return c ? wall_cp(c, first_case(c), ib, iconn, forces, true) : TRANS_E_ARG;
 }
 
+int trans_halo_pack(void* ctx, int sweep, int ib, int iconn, double* buf) {
+    Ctx* c = as_ctx(ctx);
+    return c ? halo_io(c, first_case(c), sweep, ib, iconn, nullptr, buf, true) : TRANS_E_ARG;
+}
+
+int trans_halo_unpack(void* ctx, int sweep, int ib, int iconn, const trans_conn* partner, const double* buf) {
+    Ctx* c = as_ctx(ctx);
+    return c ? halo_io(c, first_case(c), sweep, ib, iconn, partner, const_cast<double*>(buf), false) : TRANS_E_ARG;
+}
+
 int trans_sync(void* ctx) {
     Ctx* c = as_ctx(ctx);
     if (!c) return TRANS_E_ARG;

@@ -246,6 +246,8 @@ void ctx_free(Ctx* c) {
     dfree(c->d_sync);
     if (c->h_sync) { cudaFreeHost(c->h_sync); c->h_sync = nullptr; }
     dfree(c->d_kerr);
+    dfree(c->d_halo);
+    c->halo_bytes = 0;
     if (c->h_kerr) { cudaFreeHost(c->h_kerr); c->h_kerr = nullptr; }
     if (c->copy_done) { cudaEventDestroy(c->copy_done); c->copy_done = nullptr; }
     if (c->stream) { cudaStreamDestroy(c->stream); c->stream = nullptr; }

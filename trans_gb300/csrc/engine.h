@@ -80,6 +80,8 @@ struct Ctx {
     int n_rtiles[3] = {0, 0, 0};
     void* d_rmaps = nullptr;
     unsigned resid_spin = RT_WAIT_LIMIT; // polls of a tile's staging wait (TRANS_RESID_SPIN overrides)
+    void* d_halo = nullptr;              // staging of the cross-rank interface exchange
+    size_t halo_bytes = 0;
     int* d_kerr = nullptr;               // set by a kernel whose bounded wait gave up
     int* h_kerr = nullptr;               // pinned
     std::vector<BCEntry> bc, outlet;
@@ -201,6 +203,11 @@ int integrals(Ctx* c, CaseRec* cs, trans_integrals* out);
 int all_integrals(Ctx* c, std::vector<trans_integrals>& out);     // every case, in c->cases order
 // Cp of each face of a wall segment, or (forces) its pressure and viscous force, 6 per face
 int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp, bool forces = false);
+// the words of a cross-rank 1-to-1 segment out of (pack) or into (unpack) the context
+int halo_io(Ctx* c, CaseRec* cs, int sweep, int ib, int iconn, const trans_conn* partner, double* buf, bool pack);
+int block_index(const CaseRec* cs, int id);
+// Geom/startup.F90:1-25: the target face cell of a 1-to-1 interface's local face cell
+void ijk_start_end(int I, int J, int K, int& Is, int& Js, int& Ks, const int* TL, const int* TT, int lcross);
 int finalize_geometry(Ctx* c);
 int reduce_norms(Ctx* c);
 int run_iteration(Ctx* c);               // one outer iteration of every case at its KI

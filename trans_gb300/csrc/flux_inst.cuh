@@ -21,6 +21,9 @@ void ff(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev*
 void ga(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
     if (nt > 0) k_gather<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, cd);
 }
+void hu(cudaStream_t s, const DevBlock& b, const int* tab, int n, int sweep, double cost, double sint, const double* in) {
+    if (n > 0) k_halo_unpack<TG_R><<<(n + 127) / 128, 128, 0, s>>>(b, tab, n, sweep, cost, sint, in);
+}
 void fc(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
     if (nt > 0) k_sst_fc1<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, cd);
 }
@@ -143,7 +146,7 @@ void scat(cudaStream_t s, const DevBlock* b, const SweepView& v, int l0) {
 }  // namespace
 
 const FluxLaunchers& TG_NAME() {
-    static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, prep, jac, swl, swu, swa, swa_occ, swf, swf_occ,
+    static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, hu, prep, jac, swl, swu, swa, swa_occ, swf, swf_occ,
                                     swt, swt_occ, scat, sizeof(TG_R), sizeof(TG_R) == 4 ? (int)NCREC : (int)NREC};
     return L;
 }

@@ -46,6 +46,9 @@ void launch_geom_static(cudaStream_t s, const DevBlock* blks, int nblk, long lon
 }  // namespace tg
 
 namespace tg {
+void launch_halo_pack(cudaStream_t s, const DevBlock& b, const int* cells, int n, int sweep, int dq_fp32, double* out) {
+    if (n > 0) k_halo_pack<<<(n + 127) / 128, 128, 0, s>>>(b, cells, n, sweep, dq_fp32, out);
+}
 void launch_fields_xfer(cudaStream_t s, const XferBatch& x, long long total, int to_slots, int chunk) {
     if (total > 0) k_fields_xfer<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(x, total, to_slots, chunk);
 }

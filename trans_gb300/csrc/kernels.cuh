@@ -538,6 +538,66 @@ __global__ void k_shock_ghost(const DevBlock* __restrict__ blks, const Tile* __r
 }
 
 // BC_Boundarys(0): gradients of the first ghost layer (BC/*.F90 sweep 0, BC/BC_P2P.F90:140-184)
+// the 18 gradient components of a ghost cell across a 1-to-1 interface rotated by the
+// interface's angle (BC/BC_P2P.F90:140-181): g = the source cell's, o = the ghost's
+template <typename R>
+__device__ inline void p2p_grad_rotate(const R* g, R cost, R sint, R* o) {
+    const R cos2t = cost * cost, sin2t = sint * sint, sct = sint * cost;
+    const R ugx = g[0], ugy = g[1], ugz = g[2];
+    const R vgx = g[3], vgy = g[4], vgz = g[5];
+    const R wgx = g[6], wgy = g[7], wgz = g[8];
+    o[0] = ugx;
+    o[1] = cost * ugy + sint * ugz;
+    o[2] = -sint * ugy + cost * ugz;
+    o[3] = cost * vgx + sint * wgx;
+    o[4] = cos2t * vgy + sct * (vgz + wgy) + sin2t * wgz;
+    o[5] = cos2t * vgz + sct * (-vgy + wgz) - sin2t * wgy;
+    o[6] = -sint * vgx + cost * wgx;
+    o[7] = -sin2t * vgz + sct * (-vgy + wgz) + cos2t * wgy;
+    o[8] = sin2t * vgy + sct * (vgz + wgy) + cos2t * wgz;
+    for (int LL = 4; LL <= 6; ++LL) {
+        const int L = (LL - 1) * 3;            // 0-based first component of the group
+        o[L] = g[L];
+        const R gy = g[L + 1], gz = g[L + 2];
+        o[L + 1] = cost * gy + sint * gz;
+        o[L + 2] = -sint * gy + cost * gz;
+    }
+}
+
+// unpack of a cross-rank 1-to-1 segment (see k_halo_pack): sweep -1 writes the FP64 state with
+// R = double; sweep 0 the gradients in R (the FP32 copies in the mixed path), so each runs in
+// the translation unit, and with the contraction, of the same-rank copy it stands in for
+template <typename R>
+__global__ void k_halo_unpack(DevBlock b, const int* __restrict__ tab, int n, int sweep, double cost, double sint,
+                              const double* __restrict__ in) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    if (sweep == -1) {
+        const double* w = in + (size_t)36 * tab[4 * q];
+        const int off[3] = {0, 14, 25};
+        for (int L = 0; L < 3; ++L) {
+            const double* x = w + off[L];
+            const int il = tab[4 * q + 1 + L];
+            slot(b, S_V)[il] = x[0];
+            slot(b, S_V + 1)[il] = x[1];
+            const double txy = x[2], txz = x[3];
+            slot(b, S_V + 2)[il] = cost * txy + sint * txz;
+            slot(b, S_V + 3)[il] = -sint * txy + cost * txz;
+            for (int m = 4; m < 7; ++m) slot(b, S_V + m)[il] = x[m];
+            slot(b, S_PP)[il] = x[7];
+            slot(b, S_T)[il] = x[8];
+            slot(b, S_RMIU)[il] = x[9];
+        }
+    } else {
+        const double* w = in + (size_t)18 * tab[4 * q];
+        const int il = tab[4 * q + 1];
+        R g[18], o[18];
+        for (int m = 0; m < 18; ++m) g[m] = R(w[m]);
+        p2p_grad_rotate<R>(g, R(cost), R(sint), o);
+        for (int m = 0; m < 18; ++m) rs<R>(b, S_DQ + m)[il] = o[m];
+    }
+}
+
 template <typename R>
 __global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent, int n) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -550,29 +610,10 @@ __global__ void k_bc_grad(const DevBlock* __restrict__ blks, const BCEntry* __re
         return;
     }
     const DevBlock r = blks[E.src_blk];
-    R cost = R(E.cost), sint = R(E.sint);
-    R cos2t = cost * cost, sin2t = sint * sint, sct = sint * cost;
-    auto R_ = [&](int L) { return rs<R>(r, S_DQ + L - 1)[is]; };
-    auto W_ = [&](int L, R v) { rs<R>(b, S_DQ + L - 1)[il] = v; };
-    R ugx = R_(1), ugy = R_(2), ugz = R_(3);
-    R vgx = R_(4), vgy = R_(5), vgz = R_(6);
-    R wgx = R_(7), wgy = R_(8), wgz = R_(9);
-    W_(1, ugx);
-    W_(2, cost * ugy + sint * ugz);
-    W_(3, -sint * ugy + cost * ugz);
-    W_(4, cost * vgx + sint * wgx);
-    W_(5, cos2t * vgy + sct * (vgz + wgy) + sin2t * wgz);
-    W_(6, cos2t * vgz + sct * (-vgy + wgz) - sin2t * wgy);
-    W_(7, -sint * vgx + cost * wgx);
-    W_(8, -sin2t * vgz + sct * (-vgy + wgz) + cos2t * wgy);
-    W_(9, sin2t * vgy + sct * (vgz + wgy) + cos2t * wgz);
-    for (int LL = 4; LL <= 6; ++LL) {
-        int L = (LL - 1) * 3 + 1;
-        W_(L, R_(L));
-        R gy = R_(L + 1), gz = R_(L + 2);
-        W_(L + 1, cost * gy + sint * gz);
-        W_(L + 2, -sint * gy + cost * gz);
-    }
+    R g[18], o[18];
+    for (int L = 0; L < 18; ++L) g[L] = rs<R>(r, S_DQ + L)[is];
+    p2p_grad_rotate<R>(g, R(E.cost), R(E.sint), o);
+    for (int L = 0; L < 18; ++L) rs<R>(b, S_DQ + L)[il] = o[L];
 }
 
 // ---------------------------------------------------------------------------------------
@@ -2111,6 +2152,37 @@ __global__ void k_field_xfer(DevBlock b, int slot0, int ncomp, int lb, int is_sd
     double* sl = slot(b, slot0 + so);
     if (to_slots) sl[c] = stage[e];
     else stage[e] = sl[c];
+}
+
+// Cross-rank 1-to-1 interfaces (BC/PARALLEL_BC_P2P.F90:1-257): the words of a segment's face
+// cells in the reference's buffer layout.  Pack: cells[3q+L] is the source cell of layer L of
+// face cell q; sweep -1 sends per face cell layer 0: V(1:7), PP, T, Rmiu, Rds(1:3), shock and
+// layers 1, 2: V(1:7), PP, T, Rmiu, shock (36 words); sweep 0 the 18 gradients of layer 0
+// (from the FP32 copies when dq_fp32).  Unpack (k_halo_unpack): tab[4q] is the partner's face
+// cell whose words fill face cell q, tab[4q+1+L] the ghost cell of layer L; the state and
+// gradients are rotated by the interface's angle exactly as the same-rank copy (k_bc_state,
+// k_bc_grad) rotates them; Rds and shock travel but are not written (the ghost shock is
+// overwritten by the extrapolation, the ghost Rds is read by nothing).
+__global__ void k_halo_pack(DevBlock b, const int* __restrict__ cells, int n, int sweep, int dq_fp32, double* __restrict__ out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    if (sweep == -1) {
+        double* w = out + (size_t)36 * q;
+        int k = 0;
+        for (int L = 0; L < 3; ++L) {
+            const int c = cells[3 * q + L];
+            for (int m = 0; m < 7; ++m) w[k++] = slot(b, S_V + m)[c];
+            w[k++] = slot(b, S_PP)[c];
+            w[k++] = slot(b, S_T)[c];
+            w[k++] = slot(b, S_RMIU)[c];
+            if (L == 0)
+                for (int d = 0; d < 3; ++d) w[k++] = slot(b, S_RDS + d)[c];
+            w[k++] = dq_fp32 ? (double)fslot(b, S_SHOCK)[c] : slot(b, S_SHOCK)[c];
+        }
+    } else {
+        const int c = cells[3 * q];
+        for (int m = 0; m < 18; ++m) out[(size_t)18 * q + m] = dq_fp32 ? (double)fslot(b, S_DQ + m)[c] : slot(b, S_DQ + m)[c];
+    }
 }
 
 // Several Fortran-layout arrays in page-locked host memory <-> slots in one launch: each thread

@@ -37,6 +37,8 @@ void launch_rk_update(cudaStream_t s, const DevBlock* blks, const Tile* tiles, i
 void launch_rk_vupdate(cudaStream_t s, const DevBlock* blks, const Tile* tiles, int nt, const CaseDev* cdev, NormPart* parts,
                        int d_fp32);
 void launch_field_xfer(cudaStream_t s, const DevBlock& b, int slot0, int ncomp, int lb, int is_sd, double* stage, int to_slots);
+// the words of a cross-rank 1-to-1 segment's face cells (k_halo_pack)
+void launch_halo_pack(cudaStream_t s, const DevBlock& b, const int* cells, int n, int sweep, int dq_fp32, double* out);
 // several page-locked Fortran-layout arrays <-> slots in one launch (total = chunks of `chunk`
 // consecutive elements)
 void launch_fields_xfer(cudaStream_t s, const XferBatch& x, long long total, int to_slots, int chunk);
@@ -82,6 +84,9 @@ struct FluxLaunchers {
     void (*face_flux[3])(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
     void (*gather)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
     void (*sst_fc1)(cudaStream_t, const DevBlock*, const Tile*, int, const CaseDev*);
+    // cross-rank 1-to-1 segment: words (host-built table, device staging) into the ghost layers
+    void (*halo_unpack)(cudaStream_t, const DevBlock&, const int* tab, int n, int sweep, double cost, double sint,
+                        const double* in);
     // LU-SGS right-hand sides + neighbour Jacobian terms into the sweep-order arrays
     // (cell order over the cell tiles; qpos = sweep position of each tile slot)
     void (*prep)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const SweepView&, const CaseDev*);

@@ -884,6 +884,7 @@ int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp, bool forces) {
     for (int nb = 0; nb <= ib; ++nb)
         for (int ic = 0; ic < (int)cs->hb[nb].conn.size(); ++ic) {
             const trans_conn& a = cs->hb[nb].conn[ic];
+            if (a.BCType == 9 && block_index(cs, a.TargetBlock) < 0) continue;     // cross-rank: not in the table
             long long cnt = 1;
             for (int q = 0; q < 3; ++q) cnt *= (long long)(a.pointEnd[q] - a.pointStart[q] + 1);
             if (nb == ib && ic == iconn - 1) { n = cnt; break; }
@@ -905,6 +906,89 @@ int wall_cp(Ctx* c, CaseRec* cs, int ib, int iconn, double* cp, bool forces) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(cp, c->d_stage, sizeof(double) * words, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    return TRANS_OK;
+}
+
+// Cross-rank 1-to-1 interfaces (BC/PARALLEL_BC_P2P.F90:1-257, Common/PARALLEL_Funcs.F90:57-87):
+// the caller exchanges the words of a segment whose target block is in another context after
+// BC_STATE (sweep -1) and BC_GRAD (sweep 0).  Pack: this segment's interior layers, face cells in
+// the segment's K, J, I order.  Unpack: this segment's ghost layers from the partner segment's
+// words, through the same index transform and rotation as the same-rank copy.  The buffers are
+// host memory; the tables and words go through a device staging area of the context.
+int halo_io(Ctx* c, CaseRec* cs, int sweep, int ib, int iconn, const trans_conn* partner, double* buf, bool pack) {
+    if (!c || !cs || !buf || (sweep != -1 && sweep != 0) || (!pack && !partner)) return TRANS_E_ARG;
+    if (ib < 0 || ib >= (int)cs->hb.size()) return fail(c, TRANS_E_ARG, "bad block index");
+    const HostBlock& h = cs->hb[ib];
+    if (iconn < 1 || iconn > (int)h.conn.size() || h.conn[iconn - 1].BCType != 9)
+        return fail(c, TRANS_E_ARG, "connection is not a 1-to-1 interface (kind 9)");
+    int rc;
+    if (!c->built && (rc = rebuild(c))) return rc;
+    const trans_conn& a = h.conn[iconn - 1];
+    const DevBlock& b = cs->blk[ib];
+    const int W = sweep == -1 ? 36 : 18;
+    std::vector<int> tab;
+    int n = 0;
+    const int* S3[3] = {a.CIJKAdd, a.CIJKAdd1, a.CIJKAdd2};
+    const int* E3[3] = {a.CEIJKAdd, a.CEIJKAdd1, a.CEIJKAdd2};
+    long long nwords = 0;
+    if (pack) {
+        for (int K = a.pointStart[2]; K <= a.pointEnd[2]; ++K)
+            for (int J = a.pointStart[1]; J <= a.pointEnd[1]; ++J)
+                for (int I = a.pointStart[0]; I <= a.pointEnd[0]; ++I, ++n)
+                    for (int L = 0; L < 3; ++L) tab.push_back(cidx(b, I + S3[L][0], J + S3[L][1], K + S3[L][2]));
+        nwords = (long long)n * W;
+    } else {
+        const trans_conn& t = *partner;
+        const int ti = t.pointEnd[0] - t.pointStart[0] + 1, tj = t.pointEnd[1] - t.pointStart[1] + 1;
+        const int tk = t.pointEnd[2] - t.pointStart[2] + 1;
+        if (ti < 1 || tj < 1 || tk < 1) return fail(c, TRANS_E_ARG, "bad partner segment");
+        const int IIadd = a.pointEnd[0] - a.pointStart[0] + 2, JJadd = a.pointEnd[1] - a.pointStart[1] + 2;
+        const int KKadd = a.pointEnd[2] - a.pointStart[2] + 2;
+        for (int K = a.pointStart[2]; K <= a.pointEnd[2]; ++K)
+            for (int J = a.pointStart[1]; J <= a.pointEnd[1]; ++J)
+                for (int I = a.pointStart[0]; I <= a.pointEnd[0]; ++I, ++n) {
+                    int iL = I - a.pointStart[0] + 1, jL = J - a.pointStart[1] + 1, kL = K - a.pointStart[2] + 1;
+                    iL = a.revMatrix[0] * IIadd + (1 - 2 * a.revMatrix[0]) * iL;
+                    jL = a.revMatrix[1] * JJadd + (1 - 2 * a.revMatrix[1]) * jL;
+                    kL = a.revMatrix[2] * KKadd + (1 - 2 * a.revMatrix[2]) * kL;
+                    int pb, pj, pk;
+                    ijk_start_end(iL, jL, kL, pb, pj, pk, a.Transform, a.TransformT, a.lcross);
+                    pb -= 1; pj -= 1; pk -= 1;
+                    if (pb < 0 || pb >= ti || pj < 0 || pj >= tj || pk < 0 || pk >= tk)
+                        return fail(c, TRANS_E_ARG, "partner face cell outside the partner segment");
+                    tab.push_back(pb + ti * (pj + tj * pk));
+                    for (int L = 0; L < 3; ++L) tab.push_back(cidx(b, I + E3[L][0], J + E3[L][1], K + E3[L][2]));
+                }
+        nwords = (long long)ti * tj * tk * W;
+    }
+    // device staging: the table, then the words (16-byte aligned)
+    const size_t tbytes = (tab.size() * sizeof(int) + 15) / 16 * 16;
+    const size_t need = tbytes + (size_t)nwords * sizeof(double);
+    if (c->halo_bytes < need) {
+        CK(cudaStreamSynchronize(c->stream));
+        if (c->d_halo) cudaFree(c->d_halo);
+        c->d_halo = nullptr;
+        c->halo_bytes = 0;
+        CK(cudaMalloc(&c->d_halo, need));
+        c->halo_bytes = need;
+    }
+    int* d_tab = (int*)c->d_halo;
+    double* d_words = (double*)((char*)c->d_halo + tbytes);
+    cudaStream_t s = c->stream;
+    CK(cudaMemcpyAsync(d_tab, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (pack) {
+        launch_halo_pack(s, b, d_tab, n, sweep, c->mixed ? 1 : 0, d_words);
+        CK(cudaMemcpyAsync(buf, d_words, (size_t)nwords * sizeof(double), cudaMemcpyDeviceToHost, s));
+    } else {
+        CK(cudaMemcpyAsync(d_words, buf, (size_t)nwords * sizeof(double), cudaMemcpyHostToDevice, s));
+        // the state in FP64 (the FP64 unit's contraction, as k_bc_state); the gradients in the
+        // context's precision (as k_bc_grad of that precision)
+        const FluxLaunchers& fl = sweep == -1 ? flux_launchers_f64() : *c->fl;
+        fl.halo_unpack(s, b, d_tab, n, sweep, std::cos(a.rotateAngle), std::sin(a.rotateAngle), d_words);
+    }
+    c->launches++;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
     return TRANS_OK;
 }
 

@@ -13,16 +13,6 @@
 namespace tg {
 namespace eng {
 
-namespace {
-
-int upload_vec(Ctx* c, const void* h, size_t bytes, void** d) {
-    if (*d) { cudaFree(*d); *d = nullptr; }
-    if (bytes == 0) return TRANS_OK;
-    CK(cudaMalloc(d, bytes));
-    CK(cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice));
-    return TRANS_OK;
-}
-
 // Geom/startup.F90:1-25
 void ijk_start_end(int I, int J, int K, int& Is, int& Js, int& Ks, const int* TL, const int* TT, int lcross) {
     int l1 = 1 - lcross;
@@ -38,6 +28,16 @@ int block_index(const CaseRec* cs, int id) {
     for (size_t n = 0; n < cs->hb.size(); ++n)
         if (cs->hb[n].id == id) return (int)n;
     return -1;
+}
+
+namespace {
+
+int upload_vec(Ctx* c, const void* h, size_t bytes, void** d) {
+    if (*d) { cudaFree(*d); *d = nullptr; }
+    if (bytes == 0) return TRANS_OK;
+    CK(cudaMalloc(d, bytes));
+    CK(cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice));
+    return TRANS_OK;
 }
 
 // Gather tables of BC_Boundarys (BC/Boundary.F90:22-47) for one case: one entry per boundary
@@ -57,7 +57,10 @@ int build_bc(Ctx* c, const CaseRec* cs) {
             const trans_conn* ta = nullptr;
             if (kind == 9) {
                 tb = block_index(cs, a.TargetBlock);
-                if (tb < 0 || a.TargetConn < 1 || a.TargetConn > (int)cs->hb[tb].conn.size())
+                // a target block outside the case: a cross-rank interface, which the caller
+                // exchanges with trans_halo_pack / trans_halo_unpack (PARALLEL_BCs)
+                if (tb < 0) continue;
+                if (a.TargetConn < 1 || a.TargetConn > (int)cs->hb[tb].conn.size())
                     return fail(c, TRANS_E_ARG, "bad 1-to-1 target");
                 ta = &cs->hb[tb].conn[a.TargetConn - 1];
             }

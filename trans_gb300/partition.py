@@ -98,7 +98,9 @@ class HaloExchange:
         self._unpack.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(abi.TransConn), dp]
         self.words_moved = 0
 
-    def exchange(self, sweep):
+    def pack_all(self, sweep):
+        """This rank's send buffers of one pass and the receives it expects: (sends, recvs) in
+        the transport's form."""
         w = WORDS[sweep]
         sends, recvs = [], []
         for sg in self.segments:
@@ -109,7 +111,14 @@ class HaloExchange:
             # the partner receives it for its segment (target, tconn); keys name the receiver's segment
             sends.append((sg.peer, (sg.target, sg.tconn, sweep), buf))
             recvs.append((sg.peer, (sg.block, sg.iconn, sweep), face_cells(sg.partner) * w))
-        got = self.transport(sends, recvs)
+        return sends, recvs
+
+    def exchange(self, sweep):
+        sends, recvs = self.pack_all(sweep)
+        return self.unpack_all(sweep, self.transport(sends, recvs))
+
+    def unpack_all(self, sweep, got):
+        """Unpack the received buffers of one pass ({key: buffer}, keys as pack_all names them)."""
         for sg in self.segments:
             buf = np.ascontiguousarray(got[(sg.block, sg.iconn, sweep)], dtype=np.float64)
             partner = abi.TransConn()
