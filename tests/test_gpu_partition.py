@@ -80,3 +80,66 @@ def test_two_context_split_matches_whole_case(gpu_lib, monkeypatch, precision, s
     for _, s, _ in ranks:
         s.close()
     whole.close()
+
+
+def _rank(rank, world, port, out):
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    try:
+        import torch.distributed as dist
+        from trans_gb300 import partition as P
+        from trans_gb300.solver import Solver
+        dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+        c, conns, geo, st = _case("fp64", Kind_Spatial=3, Kind_Roe=3)
+        owner = P.partition_blocks(c.blocks, world)
+        mine = P.local_case(c, owner, rank)
+        s = Solver(mine, conns, geo, st)
+        drv = P.StageDriver(s, P.HaloExchange(s.lib, "trans_", s.ctx, P.halo_segments(c, conns, owner, rank),
+                                              P.torch_transport()))
+        hist = [[n["DRSa"] for n in drv.iterate(ki)] for ki in range(1, ITERS + 1)]
+        fields = {b.id: {f: s.get_field(ib, f) for f in ("V", "PP")} for ib, b in enumerate(mine.blocks)}
+        out.put((rank, [b.id for b in mine.blocks], hist, fields, None))
+        s.close()
+        dist.barrier()
+        dist.destroy_process_group()
+    except Exception:                       # reported to the parent, which fails the test
+        import traceback
+        out.put((rank, None, None, None, traceback.format_exc()))
+
+
+def test_two_process_split_with_torch_transport(gpu_lib):
+    """The same split as two processes (two ranks on the one GPU, each its own CUDA context),
+    the segments moved by torch.distributed point-to-point operations over gloo
+    (partition.torch_transport) and each rank driven by partition.StageDriver: every block's
+    state and residual history bit-identical to the whole case in one context."""
+    import socket
+    import torch
+    from trans_gb300 import partition as P
+    from trans_gb300.solver import Solver
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    mp = torch.multiprocessing.get_context("spawn")
+    q = mp.Queue()
+    procs = [mp.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted((q.get(timeout=600) for _ in procs), key=lambda x: x[0])
+    for p in procs:
+        p.join(timeout=120)
+    for r in res:
+        assert r[4] is None, r[4]
+    c, conns, geo, st = _case("fp64", Kind_Spatial=3, Kind_Roe=3)
+    whole = Solver(c, conns, geo, st, lib=gpu_lib)
+    href = [[n["DRSa"] for n in whole.iterate(ki)] for ki in range(1, ITERS + 1)]
+    owner = P.partition_blocks(c.blocks, 2)
+    for ib, b in enumerate(c.blocks):
+        r = res[owner[b.id]]
+        k = r[1].index(b.id)
+        assert [h[k] for h in r[2]] == [h[ib] for h in href], f"block {b.id}: residual history differs"
+        m = interior(b.dims)
+        for f in ("V", "PP"):
+            assert bit_equal_fraction(r[3][b.id][f], whole.get_field(ib, f), m) == 1.0, (b.id, f)
+    whole.close()
