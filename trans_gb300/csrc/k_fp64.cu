@@ -14,7 +14,7 @@ void launch_bc_state(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, i
 }
 void launch_bc_outlet(cudaStream_t s, const DevBlock* blks, const BCEntry* ent, const OutletLine* lines, int nl,
                       const CaseDev* cdev) {
-    if (nl > 0) k_bc_outlet<<<(nl + 63) / 64, 64, 0, s>>>(blks, ent, lines, nl, cdev);
+    if (nl > 0) k_bc_outlet<<<(nl + 3) / 4, 128, 0, s>>>(blks, ent, lines, nl, cdev);     // a warp per line
 }
 void launch_prims(cudaStream_t s, const DevBlock* blks, int nblk, long long total, const long long* off) {
     if (total > 0) k_prims<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(blks, nblk, total, off);

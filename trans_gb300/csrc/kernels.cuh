@@ -331,14 +331,20 @@ __global__ void k_bc_state(const DevBlock* __restrict__ blks, const BCEntry* __r
     }
 }
 
-// BC/BC_Outlet.F90:50-106: the static pressure recurrence runs along j, one thread per line
+// BC/BC_Outlet.F90:50-106: the static pressure recurrence runs along j, one warp per line.
+// Each pass loads 32 entries at once (their interior values, radii and angles) and forms the
+// terms that do not depend on the previous j (rcs1 - rcs2, rcs2 + tiny, omega * rcs2: the same
+// operations the sequential loop does, issued earlier); the recurrence itself then runs entry
+// by entry in the sequential loop's operation order, every lane repeating it on the entry's
+// operands taken by shuffle, so the result is bit for bit the sequential one; the ghost writes
+// are parallel again.
 __global__ void k_bc_outlet(const DevBlock* __restrict__ blks, const BCEntry* __restrict__ ent,
                             const OutletLine* __restrict__ lines, int nl, const CaseDev* __restrict__ cdev) {
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nl) return;
-    const OutletLine Ln = lines[q];
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nl) return;                                   // whole warps leave together
+    const OutletLine Ln = lines[w];
     const DevBlock b = blks[Ln.blk];
-    const Params p = cdev[b.cs].p;
+    const Params& p = cdev[b.cs].p;
     const int turb = cdev[b.cs].turb;
     double* V[7];
     for (int m = 0; m < 7; ++m) V[m] = slot(b, S_V + m);
@@ -348,47 +354,71 @@ __global__ void k_bc_outlet(const DevBlock* __restrict__ blks, const BCEntry* __
     const double* rad = slot(b, S_RAD);
     const double* sint = slot(b, S_SINT);
     const double* cost = slot(b, S_COST);
-    // the recurrence values of the previous j stay in registers (PP, rho, rho*v, rho*w of the
-    // first ghost layer at j-1), so each step is a short dependent chain
+    // the previous j's ghost values (PP, rho, rho*v, rho*w of the first ghost layer)
     double pp_prev = 0.0, den_prev = 1.0, v3_prev = 0.0, v4_prev = 0.0;
-    for (int e = Ln.first; e < Ln.first + Ln.n; ++e) {
-        const BCEntry E = ent[e];
-        int s0 = E.s[0], l0 = E.l[0];
-        double Tl = T[s0];
-        T[l0] = Tl;
-        double pp;
-        if (E.sub == 1) {                              // j == Jbgn
-            pp = p.Pouthub;
-        } else {
-            int lm = l0 - b.PI;                         // (il, jl-1, kl)
-            double rcs1 = rad[l0], rcs2 = rad[lm];
-            double sinr = sint[lm], cosr = cost[lm];
-            double RoVr2 = sq(v4_prev / den_prev * cosr - sinr * v3_prev / den_prev + p.omega0 * rcs2);
-            pp = pp_prev + fabs((rcs1 - rcs2) * den_prev * RoVr2) / (rcs2 + p.Tiny);
+    for (int j0 = 0; j0 < Ln.n; j0 += 32) {
+        const bool act = j0 + lane < Ln.n;
+        BCEntry E;
+        int first = 1;
+        double Tl = 1.0, v1s = 1.0, v3s = 0.0, v4s = 0.0, dr = 0.0, rt = 1.0, wr = 0.0, sinr = 0.0, cosr = 0.0;
+        if (act) {
+            E = ent[Ln.first + j0 + lane];
+            const int s0 = E.s[0];
+            Tl = T[s0];
+            v1s = V[0][s0];
+            v3s = V[2][s0];
+            v4s = V[3][s0];
+            first = E.sub == 1;
+            if (!first) {
+                const int lm = E.l[0] - b.PI;              // (il, jl-1, kl)
+                const double rcs1 = rad[E.l[0]], rcs2 = rad[lm];
+                dr = rcs1 - rcs2;
+                rt = rcs2 + p.Tiny;
+                wr = p.omega0 * rcs2;
+                sinr = sint[lm];
+                cosr = cost[lm];
+            }
         }
-        PP[l0] = pp;
-        double den = pp / Tl * p.RXM2;
-        V[0][l0] = den;
-        double den_ratio = den / V[0][s0];
-        double v2 = V[1][s0] * den_ratio, v3 = V[2][s0] * den_ratio, v4 = V[3][s0] * den_ratio;
-        V[1][l0] = v2;
-        V[2][l0] = v3;
-        V[3][l0] = v4;
-        for (int L = 1; L < 3; ++L) {
-            int ig = E.l[L];
+        const int cnt = min(32, Ln.n - j0);
+        double pp = 0.0, den = 0.0, ratio = 0.0;
+        for (int i = 0; i < cnt; ++i) {
+            const int fi = __shfl_sync(0xffffffffu, first, i);
+            const double tli = __shfl_sync(0xffffffffu, Tl, i), v1i = __shfl_sync(0xffffffffu, v1s, i);
+            const double v3i = __shfl_sync(0xffffffffu, v3s, i), v4i = __shfl_sync(0xffffffffu, v4s, i);
+            const double dri = __shfl_sync(0xffffffffu, dr, i), rti = __shfl_sync(0xffffffffu, rt, i);
+            const double wri = __shfl_sync(0xffffffffu, wr, i);
+            const double si = __shfl_sync(0xffffffffu, sinr, i), ci = __shfl_sync(0xffffffffu, cosr, i);
+            double ppi;
+            if (fi) {                                       // j == Jbgn
+                ppi = p.Pouthub;
+            } else {
+                const double RoVr2 = sq(v4_prev / den_prev * ci - si * v3_prev / den_prev + wri);
+                ppi = pp_prev + fabs(dri * den_prev * RoVr2) / rti;
+            }
+            const double deni = ppi / tli * p.RXM2;
+            const double ri = deni / v1i;
+            if (lane == i) { pp = ppi; den = deni; ratio = ri; }
+            pp_prev = ppi;
+            den_prev = deni;
+            v3_prev = v3i * ri;
+            v4_prev = v4i * ri;
+        }
+        if (!act) continue;
+        const int s0 = E.s[0];
+        const double v2 = V[1][s0] * ratio, v3 = v3s * ratio, v4 = v4s * ratio;
+        for (int L = 0; L < 3; ++L) {
+            const int ig = E.l[L];
             V[0][ig] = den; V[1][ig] = v2; V[2][ig] = v3; V[3][ig] = v4;
             PP[ig] = pp;
             T[ig] = Tl;
         }
         if (turb) {
-            double k6 = V[5][s0], k7 = V[6][s0], rm = Rm[s0];
-            V[5][l0] = k6; V[6][l0] = k7; Rm[l0] = rm;
-            for (int L = 1; L < 3; ++L) {
-                int ig = E.l[L];
+            const double k6 = V[5][s0], k7 = V[6][s0], rm = Rm[s0];
+            for (int L = 0; L < 3; ++L) {
+                const int ig = E.l[L];
                 V[5][ig] = k6; V[6][ig] = k7; Rm[ig] = rm;
             }
         }
-        pp_prev = pp; den_prev = den; v3_prev = v3; v4_prev = v4;
     }
 }
 
