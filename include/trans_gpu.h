@@ -338,6 +338,14 @@ const char* trans_kernel_class(int k);
 /* The schedule the context's tuner picked for the LU-SGS sweeps and what it measured (no
  * reference counterpart).  The string lives until the next call on this thread. */
 const char* trans_tuning(void* ctx);
+/* Diagnostic, no reference counterpart: checks on the current device the integer-pipe
+ * double <-> float conversions the mixed-precision kernels use against the hardware
+ * conversions, on n bit patterns (1..2^32) drawn from seed plus a fixed set of edge cases
+ * (signed zeros, infinities, NaN, the float range limits, rounding ties).  mismatches[0]
+ * counts double -> float results that differ in any bit, mismatches[1] float -> double (NaN
+ * equals NaN); both are 0 on a correct build.  Errors: TRANS_E_ARG, TRANS_E_CUDA (message in
+ * trans_last_error(NULL)). */
+int trans_check_conversions(long long n, unsigned long long seed, long long* mismatches);
 /* Message of the last failed call on ctx; with ctx = NULL, of the last failed context-free call
  * (trans_wall_distance) on this thread. */
 const char* trans_last_error(void* ctx);

@@ -184,6 +184,7 @@ def bind_common(lib):
     lib.trans_get_fields.argtypes = [vp, C.c_int, IP, IP, PP]
     lib.trans_batch_set_fields.argtypes = [vp, C.c_int, C.c_int, IP, IP, PP]
     lib.trans_batch_get_fields.argtypes = [vp, C.c_int, C.c_int, IP, IP, PP]
+    lib.trans_check_conversions.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
     lib.trans_tuning.argtypes = [vp]
     lib.trans_tuning.restype = C.c_char_p
     lib.trans_last_error.argtypes = [vp]
@@ -201,5 +202,5 @@ EXPORTED = ["trans_create", "trans_destroy", "trans_set_field", "trans_get_field
             "trans_batch_time_iterations", "trans_get_integrals", "trans_get_wall_cp", "trans_get_wall_forces", "trans_halo_pack", "trans_halo_unpack",
             "trans_batch_get_integrals", "trans_batch_integrals", "trans_batch_get_wall_cp", "trans_wall_distance",
             "trans_set_fields", "trans_get_fields", "trans_batch_set_fields", "trans_batch_get_fields",
-            "trans_block_metrics"]
+            "trans_block_metrics", "trans_check_conversions"]
 TRANS_NKCLASS = 17

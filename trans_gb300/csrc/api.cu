@@ -211,6 +211,19 @@ int trans_kernel_times(void* ctx, int ki, double* ms, int* launches, int n) {
     return kernel_times(c, ms, launches);
 }
 
+int trans_check_conversions(long long n, unsigned long long seed, long long* mismatches) {
+    if (n < 1 || n > (1LL << 32) || !mismatches) {
+        g_stateless_err = "trans_check_conversions: n must be 1..2^32 and mismatches non-NULL";
+        return TRANS_E_ARG;
+    }
+    const cudaError_t e = check_conversions(n, seed, mismatches);
+    if (e != cudaSuccess) {
+        g_stateless_err = std::string("trans_check_conversions: ") + cudaGetErrorString(e);
+        return TRANS_E_CUDA;
+    }
+    return TRANS_OK;
+}
+
 const char* trans_kernel_class(int k) { return (k >= 0 && k < NKCLASS) ? kclass_name[k] : ""; }
 
 const char* trans_tuning(void* ctx) {

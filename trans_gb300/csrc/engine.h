@@ -17,6 +17,7 @@
 #include "types.cuh"
 
 namespace tg {
+extern thread_local std::string g_stateless_err;   // the message stateless_error() returns
 namespace eng {
 
 struct HostBlock {

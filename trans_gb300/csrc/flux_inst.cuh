@@ -138,10 +138,8 @@ int swt_occ(int block) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tiles<TG_R>, block, 0) != cudaSuccess) return 0;
     return n;
 }
-void scat(cudaStream_t s, const DevBlock* b, const SweepView& v, int l0) {
-    if (v.n > 0)
-        k_sweep_scatter<TG_R><<<(unsigned)((v.n + CELL_TILE - 1) / CELL_TILE), CELL_TILE, 0, s>>>(b, v.cells, (const TG_R*)v.dq, v.n,
-                                                                                                  l0);
+void scat(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const int* qpos, const SweepView& v, int l0) {
+    if (nt > 0 && v.n > 0) k_sweep_scatter<TG_R><<<nt, CELL_TILE, 0, s>>>(b, tiles, qpos, (const TG_R*)v.dq, l0);
 }
 }  // namespace
 

@@ -175,3 +175,76 @@ double probe_chain_us(int chained, int grid) {
     return us;
 }
 }  // namespace tg
+
+// ---------------------------------------------------------------------------------------
+// Check of the integer-pipe conversions (cvt.cuh) against the hardware conversions: n bit
+// patterns from a counter-based generator (seed), a quarter each uniform over all doubles,
+// with exponents around the float range, at and next to rounding ties, and float patterns for
+// float -> double; the first CVT_NSPECIAL indices take the fixed patterns below.  NaN results
+// compare equal to NaN results.
+// ---------------------------------------------------------------------------------------
+namespace tg {
+namespace {
+constexpr int CVT_NSPECIAL = 16;
+__constant__ unsigned long long cvt_special[CVT_NSPECIAL] = {
+    0x0000000000000000ull, 0x8000000000000000ull,    // +-0
+    0x7ff0000000000000ull, 0xfff0000000000000ull,    // +-inf
+    0x7ff8000000000000ull, 0x0000000000000001ull,    // NaN, the smallest double
+    0x47efffffe0000000ull, 0x47efffffefffffffull,    // the largest float; just below its rounding tie
+    0x47effffff0000000ull, 0x3810000000000000ull,    // the tie to infinity; the smallest normal float
+    0x380fffffffffffffull, 0x3690000000000000ull,    // just below it (a float subnormal); 2^-150
+    0x3ff0000010000000ull, 0x3ff0000030000000ull,    // 1 + half an ulp (to even: 1), 1 + 1.5 ulp (up)
+    0xbff0000010000001ull, 0x3fefffffffffffffull};   // -(1 + just above half an ulp), 1 - 2^-53
+__device__ __forceinline__ unsigned long long cvt_mix(unsigned long long z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+__global__ void k_check_cvt(long long n, unsigned long long seed, unsigned long long* __restrict__ bad) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const unsigned long long z = cvt_mix((unsigned long long)g ^ (seed * 0x2545f4914f6cdd1dull));
+    unsigned long long u;
+    const int kind = (int)(g & 3);
+    if (g < CVT_NSPECIAL) {
+        u = cvt_special[g];
+        const unsigned f = (unsigned)(u >> 32) ^ (unsigned)u;     // a float pattern from it too
+        const double a = f64_of(__uint_as_float(f)), h = (double)__uint_as_float(f);
+        if (__double_as_longlong(a) != __double_as_longlong(h) && !(isnan(a) && isnan(h))) atomicAdd(bad + 1, 1ull);
+    } else if (kind == 0) {
+        u = z;
+    } else if (kind == 1) {                                       // exponents 880..1170
+        u = (z & 0x800fffffffffffffull) | ((880ull + (z >> 55) % 291ull) << 52);
+    } else if (kind == 2) {                                       // the tie, one below, one or two above
+        const unsigned long long m = ((z & 0xfffffe0000000ull) | 0x10000000ull) + ((z >> 40) & 3ull) - 1ull;
+        u = (z & 0x8000000000000000ull) | ((890ull + (z >> 55) % 270ull) << 52) | (m & 0xfffffffffffffull);
+    } else {                                                      // float -> double
+        const unsigned f = (unsigned)z;
+        const double a = f64_of(__uint_as_float(f)), h = (double)__uint_as_float(f);
+        if (__double_as_longlong(a) != __double_as_longlong(h) && !(isnan(a) && isnan(h))) atomicAdd(bad + 1, 1ull);
+        return;
+    }
+    const double x = __longlong_as_double((long long)u);
+    const float a = f32_rn(x), h = (float)x;
+    if (__float_as_uint(a) != __float_as_uint(h) && !(isnan(a) && isnan(h))) atomicAdd(bad, 1ull);
+}
+}  // namespace
+
+cudaError_t check_conversions(long long n, unsigned long long seed, long long* mismatches) {
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 2 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return e;
+    unsigned long long h[2] = {0, 0};
+    e = cudaMemset(d, 0, sizeof(h));
+    if (e == cudaSuccess) {
+        k_check_cvt<<<(unsigned)((n + 255) / 256), 256>>>(n, seed, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    mismatches[0] = (long long)h[0];
+    mismatches[1] = (long long)h[1];
+    return e;
+}
+}  // namespace tg

@@ -483,7 +483,9 @@ __global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __rest
                       rs<R>(b, S_PRIM + 3), rs<R>(b, S_PRIM + 4)};
     int nq = turb ? 6 : 4;
     const R* SD = rs<R>(b, S_SD);
-    R g9[3][3];
+    // the gradients stay in registers until every stencil load is issued (a load after a store
+    // to the same arena would wait for the previous round trip), then go out together
+    R gq[6][3];
     for (int q = 0; q < nq; ++q) {
         R fw[3], fe[3];
         for (int d = 0; d < 3; ++d) {
@@ -498,13 +500,14 @@ __global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __rest
             const R* S3 = SD + (size_t)(2 * 3 + m) * b.ncell;
             R g = volinv * (fe[0] * S1[c + st[0]] - fw[0] * S1[c] + fe[1] * S2[c + st[1]] - fw[1] * S2[c]
                                  + fe[2] * S3[c + st[2]] - fw[2] * S3[c]);
-            rs<R>(b, S_DQ + 3 * q + m)[c] = g;
-            if (q < 3) g9[q][m] = g;
+            gq[q][m] = g;
         }
     }
-    R DuDx = g9[0][0], DuDy = g9[0][1], DuDz = g9[0][2];
-    R DvDx = g9[1][0], DvDy = g9[1][1], DvDz = g9[1][2];
-    R DwDx = g9[2][0], DwDy = g9[2][1], DwDz = g9[2][2];
+    for (int q = 0; q < nq; ++q)
+        for (int m = 0; m < 3; ++m) rs<R>(b, S_DQ + 3 * q + m)[c] = gq[q][m];
+    R DuDx = gq[0][0], DuDy = gq[0][1], DuDz = gq[0][2];
+    R DvDx = gq[1][0], DvDy = gq[1][1], DvDz = gq[1][2];
+    R DwDx = gq[2][0], DwDy = gq[2][1], DwDz = gq[2][2];
     R W12 = (DuDy - DvDx) / R(2.0), W13 = (DuDz - DwDx) / R(2.0), W23 = (DvDz - DwDy) / R(2.0);
     R Vort = sqrt(R(2.0) * (R(2.0) * W12 * W12 + R(2.0) * W13 * W13 + R(2.0) * W23 * W23));
     R DivU = sqrt(DuDx * DuDx + DvDy * DvDy + DwDz * DwDz);
@@ -954,7 +957,7 @@ __global__ void k_gather(const DevBlock* __restrict__ blks, const Tile* __restri
     // rotating-frame source of DIFFUSION_Centered (:812-822), after its viscous terms: Coriolis
     // and centrifugal force on y and z momentum times the cell volume.  With omega(1) = 0 it adds
     // a signed zero, which leaves a sum that started at +0 unchanged, so it is skipped.
-    const R om = R(cdev[b.cs].p.omega0);
+    const R om = cparams<R>(cdev[b.cs]).omega0;
     for (int L = 1; L < 5; ++L) {
         R acc = R(0.0);
         for (int d = 0; d < 3; ++d) { acc = acc - fx(d, FX_VX + L - 1, c); acc = acc + fx(d, FX_VX + L - 1, c + st[d]); }
@@ -1118,7 +1121,9 @@ __global__ void __launch_bounds__(CELL_TILE, sizeof(R) == 4 ? 2 : 1) k_lusgs_pre
     auto DQ = [&](int L) -> R& { return dq[sw_at(q, L, DQ_STRIDE)]; };
     // BDF2 right-hand side and the mean-flow diagonal (TIME_LUSGS.F90:73-108).  FP64 path: the
     // reference's operations.  Mixed path: the time-level difference 3V - 4Wt0 + Wt1 in FP64
-    // (it cancels), everything else in FP32 with one reciprocal of the volume.
+    // (it cancels), everything else in FP32 with one reciprocal of the volume.  (This kernel is
+    // bound by load latency at its register limit, so the hardware conversion stays: the
+    // integer-pipe one of cvt.cuh measured 50% slower here.)
     const double DT = pd.DT_LUSGS_Main;
     constexpr bool MIXED = sizeof(R) == 4;
     R stept, cvs, fm;
@@ -1826,17 +1831,26 @@ __global__ void k_sweep_tiles(const int* __restrict__ nbp, const R* __restrict__
     }
 }
 
-// DeltaQ back to the cells (the update and trans_get_field read it there)
-// (components l0..6: the Runge-Kutta path sweeps and returns only k and omega, l0 = 5)
+// DeltaQ back to the cells (the update and trans_get_field read it there), one thread per
+// interior cell of the cell tiles: a sweep position's components share one sector of dq, so
+// each cell reads one sector and the stores to the D slots are coalesced (components l0..6:
+// the Runge-Kutta path sweeps and returns only k and omega, l0 = 5)
 template <typename R>
-__global__ void k_sweep_scatter(const DevBlock* __restrict__ blks, const SweepCell* __restrict__ cells, const R* __restrict__ dq,
-                                long long N, int l0) {
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= N) return;
-    const SweepCell sc = cells[q];
-    const DevBlock b = blks[sc.blk];
-    const int c = cidx(b, sc.i, sc.j, sc.k);
-    for (int L = l0; L < 7; ++L) rs<R>(b, S_D + L)[c] = dq[sw_at(q, L, DQ_STRIDE)];
+__global__ void k_sweep_scatter(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
+                                const R* __restrict__ dq, int l0) {
+    const Tile t = tiles[blockIdx.x];
+    if ((int)threadIdx.x >= t.count) return;
+    const DevBlock b = blks[t.blk];
+    const int n = t.start + threadIdx.x;
+    const int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
+    const int c = cidx(b, I, J, K);
+    const long long q = qpos[(size_t)blockIdx.x * CELL_TILE + threadIdx.x];
+    R d[7];
+#pragma unroll
+    for (int L = 0; L < 7; ++L) d[L] = L >= l0 ? dq[sw_at(q, L, DQ_STRIDE)] : R(0);
+#pragma unroll
+    for (int L = 0; L < 7; ++L)
+        if (L >= l0) rs<R>(b, S_D + L)[c] = d[L];
 }
 
 #ifdef TG_COMMON_KERNELS
@@ -2127,9 +2141,18 @@ __global__ void k_update_u(const DevBlock* __restrict__ blks, const Tile* __rest
     int n = t.start + threadIdx.x;
     int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     int c = cidx(b, I, J, K);
+    // every load before the first store: the slots share one arena, so loads placed after a
+    // store would each wait for the previous component's round trip
+    double w0[7], v[7];
+#pragma unroll
     for (int L = 0; L < 7; ++L) {
-        if (kind_dual == 2) slot(b, S_WT1 + L)[c] = slot(b, S_WT0 + L)[c];
-        slot(b, S_WT0 + L)[c] = slot(b, S_V + L)[c];
+        w0[L] = slot(b, S_WT0 + L)[c];
+        v[L] = slot(b, S_V + L)[c];
+    }
+#pragma unroll
+    for (int L = 0; L < 7; ++L) {
+        if (kind_dual == 2) slot(b, S_WT1 + L)[c] = w0[L];
+        slot(b, S_WT0 + L)[c] = v[L];
     }
 }
 

@@ -1,26 +1,33 @@
 // kernels_mixed.cuh -- the FP64-state kernels of the mixed-precision path in a reduced-operation
 // form (included by k_mixed.cu only).
 //
-// On GB300 every FP64 instruction issues at 1/64 of the FP32 rate, and a double division or
-// square root is ~10 of them.  The FP64 path evaluates Time/SpectralRadius.F90 and
-// Time/TIME_Update_V.F90 operation by operation (bit-identical to the reference's arithmetic);
-// these mixed-path versions keep the same quantities in FP64 -- the conserved-variable update,
-// the local time step and the residual norms -- but
-//   - divide once per cell (a reciprocal) where the reference divides by the same value
-//     several times,
-//   - evaluate the increments of the positivity-preserving update, p*exp(dp/p) = p + p*expm1(dp/p),
-//     as an FP32 expm1 added to the FP64 value (the FP32 error scales with the increment, so it
-//     vanishes as the iteration converges),
-//   - evaluate the SST model algebra of the update (the F2-limited C_mu and the realizability
-//     limits of omega and k) and the spectral radii's square roots and Sutherland law in FP32,
-//     like the other SST and sweep arithmetic of the mixed path.
+// On GB300 every FP64 instruction -- and every double <-> float conversion -- issues at 1/64 of
+// the FP32 rate, and a double division or square root is ~10 of them.  The FP64 path evaluates
+// Time/SpectralRadius.F90 and Time/TIME_Update_V.F90 operation by operation (bit-identical to
+// the reference's arithmetic); these mixed-path versions keep the state in FP64 -- the
+// conserved variables and pressure are FP64 values that FP32 increments are added to -- and
+//   - convert between double and float on the integer pipe (cvt.cuh),
+//   - evaluate the increments of the update (velocity, pressure, the norms' |D/V| terms) in
+//     FP32, from the FP32 DeltaQ the sweeps produce: the momentum update
+//     rho'(m/rho + a) = m + (m r + rho' a), with r = rho'/rho - 1, becomes one FP32 increment
+//     added to the FP64 momentum, so no FP64 division is left per cell,
+//   - evaluate the positivity-preserving update p*exp(dp/p) = p + p*expm1(dp/p) with an FP32
+//     expm1 scaled by the FP64 value (the FP32 error scales with the increment, so it vanishes
+//     as the iteration converges),
+//   - evaluate the spectral radii and the local time step in FP32 (they set the pseudo-time
+//     step, not the converged solution), and the SST model algebra of the update (the
+//     F2-limited C_mu, the realizability limits of omega and k) in FP32, like the other SST and
+//     sweep arithmetic of the mixed path,
+//   - reduce the residual norms in FP32 within a warp and in FP64 across the CTA's warps.
 #pragma once
+#include "cvt.cuh"
 
 namespace tg {
 
 // ---------------------------------------------------------------------------------------
-// Time/SpectralRadius.F90:47-180, mixed path: spectral radii with FP32 square roots and
-// Sutherland law, accumulated in FP64; the local time step divides in FP64.
+// Time/SpectralRadius.F90:47-180, mixed path: spectral radii and local time step in FP32 from
+// the FP64 state (converted on the integer pipe) and the FP32 copies of the metrics; written to
+// the FP64 slots (exact values of the FP32 results), which k_prims_mixed copies for the sweeps.
 // ---------------------------------------------------------------------------------------
 __global__ void k_specrad_mixed(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
                                 const CaseDev* __restrict__ cdev) {
@@ -28,42 +35,46 @@ __global__ void k_specrad_mixed(const DevBlock* __restrict__ blks, const Tile* _
     if ((int)threadIdx.x >= t.count) return;
     const DevBlock b = blks[t.blk];
     const CaseDev& cd = cdev[b.cs];
-    const Params& p = cd.p;
-    const double CFL_sub = cd.CFL_sub;
+    const ParamsT<float>& pf = cd.pf;
     const int n = t.start + threadIdx.x;
     const int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
     const int c = cidx(b, I, J, K);
-    const double Den = slot(b, S_V)[c];
-    const double rden = 1.0 / Den;
-    const double Vxi = slot(b, S_V + 1)[c] * rden, Vyi = slot(b, S_V + 2)[c] * rden, Vzi = slot(b, S_V + 3)[c] * rden;
-    const double AAc = (double)sqrtf((float)(1.4 * slot(b, S_PP)[c] * rden));
-    const double RmiuL = (double)mu_suth<float>(cd.pf, (float)slot(b, S_T)[c]);
-    const double RmiuTL = slot(b, S_RMIU)[c];
-    const double uvmu = (RmiuL + RmiuTL + 1.0e-20) * (4.0 / 3.0);
-    const double uvmupr = (RmiuL * (1.0 / 0.72) + RmiuTL * (1.0 / 0.9) + 1.0e-20) * 1.4;
-    const double vol = slot(b, S_VOL)[c];
-    const double visc = 2.0 * dmax(uvmu, uvmupr) * rden / (vol * p.Ref);
-    double rs = 0.0;
+    const float rden = 1.0f / f32_rn(slot(b, S_V)[c]);
+    const float Vxi = f32_rn(slot(b, S_V + 1)[c]) * rden, Vyi = f32_rn(slot(b, S_V + 2)[c]) * rden;
+    const float Vzi = f32_rn(slot(b, S_V + 3)[c]) * rden;
+    const float AAc = sqrtf(1.4f * f32_rn(slot(b, S_PP)[c]) * rden);
+    const float RmiuL = mu_suth<float>(pf, f32_rn(slot(b, S_T)[c]));
+    const float RmiuTL = f32_rn(slot(b, S_RMIU)[c]);
+    const float uvmu = (RmiuL + RmiuTL + 1.0e-20f) * (4.0f / 3.0f);
+    const float uvmupr = (RmiuL * (1.0f / 0.72f) + RmiuTL * (1.0f / 0.9f) + 1.0e-20f) * 1.4f;
+    const float vol = fslot(b, S_VOL)[c];
+    float A[9];                                      // all loads before the first store
+#pragma unroll
+    for (int q = 0; q < 9; ++q) A[q] = fslot(b, S_ASD + q)[c];
+    const float visc = 2.0f * fmaxf(uvmu, uvmupr) * rden / (vol * pf.Ref);
+    float rs = 0.0f;
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double ARX = slot(b, S_ASD + 3 * d)[c], ARY = slot(b, S_ASD + 3 * d + 1)[c], ARZ = slot(b, S_ASD + 3 * d + 2)[c];
-        const double STsq = ARX * ARX + ARY * ARY + ARZ * ARZ;
-        const double UU = Vxi * ARX + Vyi * ARY + Vzi * ARZ;
-        const double Rd = fabs(UU) + (double)sqrtf((float)STsq) * AAc + STsq * visc;
-        slot(b, S_RDS + d)[c] = Rd;
+        const float ARX = A[3 * d], ARY = A[3 * d + 1], ARZ = A[3 * d + 2];
+        const float STsq = ARX * ARX + ARY * ARY + ARZ * ARZ;
+        const float UU = Vxi * ARX + Vyi * ARY + Vzi * ARZ;
+        const float Rd = fabsf(UU) + sqrtf(STsq) * AAc + STsq * visc;
+        slot(b, S_RDS + d)[c] = f64_of(Rd);
         rs += Rd;
     }
-    const double Dtm_local = vol / rs;
-    double dtm = p.IF_Local_Main == 1 ? p.CFL_Main * Dtm_local : p.DT_LUSGS_Main;
-    if (p.Kind_Dual != 0) dtm = p.IF_Local_Sub == 1 ? CFL_sub * Dtm_local : p.DT_LUSGS_Sub;
+    const float Dtm_local = vol / rs;
+    const Params& p = cd.p;
+    double dtm = p.IF_Local_Main == 1 ? f64_of(pf.CFL_Main * Dtm_local) : p.DT_LUSGS_Main;
+    if (p.Kind_Dual != 0) dtm = p.IF_Local_Sub == 1 ? f64_of(f32_rn(cd.CFL_sub) * Dtm_local) : p.DT_LUSGS_Sub;
     slot(b, S_DTM)[c] = dtm;
 }
 
 // ---------------------------------------------------------------------------------------
 // Mixed path: the FP32 copies the FP32 kernels read, in one pass over every padded cell: the
 // state V(7), p, T, mu_t, the spectral radii and time step, and the primitives u, v, w,
-// k/rho, omega/rho, 1/rho and the LU-SGS velocities from one FP64 reciprocal of rho (the FP64
+// k/rho, omega/rho, 1/rho and the LU-SGS velocities from one FP32 reciprocal of rho (the FP64
 // path's k_prims divides per component and keeps FP64 primitives, which nothing in the mixed
-// path reads).
+// path reads).  The conversions run on the integer pipe (cvt.cuh).
 // ---------------------------------------------------------------------------------------
 __global__ void k_prims_mixed(const DevBlock* __restrict__ blks, int nblk, long long total, const long long* __restrict__ off) {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -72,21 +83,33 @@ __global__ void k_prims_mixed(const DevBlock* __restrict__ blks, int nblk, long 
     while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (off[mid] <= g) lo = mid; else hi = mid - 1; }
     const DevBlock b = blks[lo];
     const int c = (int)(g - off[lo]);
-    double v[7];
+    // every load before the first store (the FP32 copies could alias the FP64 slots as far as
+    // the compiler knows, and a load after a store would wait for the previous round trip)
+    double x[14];
+#pragma unroll
+    for (int L = 0; L < 7; ++L) x[L] = slot(b, S_V + L)[c];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) x[7 + q] = slot(b, S_PP + q)[c];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) x[10 + q] = slot(b, S_RDS + q)[c];
+    float v[7];
+#pragma unroll
     for (int L = 0; L < 7; ++L) {
-        v[L] = slot(b, S_V + L)[c];
-        fslot(b, S_V + L)[c] = (float)v[L];
+        v[L] = f32_rn(x[L]);
+        fslot(b, S_V + L)[c] = v[L];
     }
-    for (int q = S_PP; q <= S_RMIU; ++q) fslot(b, q)[c] = (float)slot(b, q)[c];
-    for (int q = S_RDS; q <= S_DTM; ++q) fslot(b, q)[c] = (float)slot(b, q)[c];
-    const double ri = 1.0 / v[0];
-    const float u = (float)(v[1] * ri), vv = (float)(v[2] * ri), w = (float)(v[3] * ri);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) fslot(b, S_PP + q)[c] = f32_rn(x[7 + q]);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) fslot(b, S_RDS + q)[c] = f32_rn(x[10 + q]);
+    const float ri = 1.0f / v[0];
+    const float u = v[1] * ri, vv = v[2] * ri, w = v[3] * ri;
     fslot(b, S_PRIM)[c] = u;
     fslot(b, S_PRIM + 1)[c] = vv;
     fslot(b, S_PRIM + 2)[c] = w;
-    fslot(b, S_PRIM + 3)[c] = (float)(v[5] * ri);
-    fslot(b, S_PRIM + 4)[c] = (float)(v[6] * ri);
-    fslot(b, S_RINV)[c] = (float)ri;
+    fslot(b, S_PRIM + 3)[c] = v[5] * ri;
+    fslot(b, S_PRIM + 4)[c] = v[6] * ri;
+    fslot(b, S_RINV)[c] = ri;
     fslot(b, S_SVEL)[c] = u;
     fslot(b, S_SVEL + 1)[c] = vv;
     fslot(b, S_SVEL + 2)[c] = w;
@@ -182,15 +205,53 @@ __global__ void k_bc_outlet_mixed(const DevBlock* __restrict__ blks, const BCEnt
 }
 
 // p + p*expm1(dp/(p+1e-10)) for dp < 0, p + dp otherwise (Time/TIME_Update_V.F90:660-675)
-__device__ inline double positive_add(double p, double dp) {
-    if (dp >= 0.0) return p + dp;
-    const float x = (float)dp / ((float)p + 1.0e-10f);
-    return p + p * (double)expm1f(x);
+__device__ inline double positive_add(double p, float dp) {
+    if (dp >= 0.0f) return p + f64_of(dp);
+    const float x = dp / (f32_rn(p) + 1.0e-10f);
+    return p + p * f64_of(expm1f(x));
+}
+
+// Residual-norm partials of one thread in FP32 (the terms |D/V| come from FP32 increments),
+// joined as NormPart's (the later cell kept on ties of the maximum); a warp reduces them by
+// shuffles in FP32, the CTA's warps then in FP64 as norm_reduce_cta does.
+struct NormPartF {
+    float sa, ma, sk, mk, so, mo;
+    int ia, nan;
+};
+__device__ inline void normf_join(NormPartF& a, const NormPartF& b) {
+    a.sa += b.sa; a.sk += b.sk; a.so += b.so;
+    if (b.ma > a.ma || (b.ma == a.ma && b.ia > a.ia)) { a.ma = b.ma; a.ia = b.ia; }
+    a.mk = fmaxf(a.mk, b.mk); a.mo = fmaxf(a.mo, b.mo);
+    a.nan |= b.nan;
+}
+__device__ inline NormPart norm_reduce_cta_f(NormPartF a) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int w = 16; w > 0; w >>= 1) {
+        NormPartF o;
+        o.sa = __shfl_down_sync(full, a.sa, w); o.ma = __shfl_down_sync(full, a.ma, w);
+        o.sk = __shfl_down_sync(full, a.sk, w); o.mk = __shfl_down_sync(full, a.mk, w);
+        o.so = __shfl_down_sync(full, a.so, w); o.mo = __shfl_down_sync(full, a.mo, w);
+        o.ia = __shfl_down_sync(full, a.ia, w); o.nan = __shfl_down_sync(full, a.nan, w);
+        if (lane + w < 32) normf_join(a, o);
+    }
+    __shared__ NormPart s_warp[32];
+    if (lane == 0) {
+        NormPart d;
+        d.sa = f64_of(a.sa); d.ma = f64_of(a.ma); d.sk = f64_of(a.sk); d.mk = f64_of(a.mk);
+        d.so = f64_of(a.so); d.mo = f64_of(a.mo); d.ia = a.ia; d.nan = a.nan; d.pad_ = 0;
+        s_warp[wid] = d;
+    }
+    __syncthreads();
+    NormPart r = norm_identity();
+    if (wid == 0) r = norm_reduce_warp(lane < (int)(blockDim.x >> 5) ? s_warp[lane] : norm_identity());
+    return r;
 }
 
 // ---------------------------------------------------------------------------------------
 // Time/TIME_Update_V.F90:106-294 (norms) and :621-816 (update), mixed path.  DeltaQ and the
-// gradients come from the FP32 copies.
+// gradients come from the FP32 copies; the increments are FP32, the state they are added to
+// FP64.
 // ---------------------------------------------------------------------------------------
 __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
                                const CaseDev* __restrict__ cdev, NormPart* __restrict__ parts) {
@@ -199,9 +260,8 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
     const CaseDev& cd = cdev[b.cs];
     const int turb_upd = cd.turb_upd;
     const int tid = threadIdx.x;
-    double sa = 0, ma = -1, sk = 0, mk = 0, so = 0, mo = 0;
-    long long ia = -1;
-    int nanf = 0;
+    NormPartF P;
+    P.sa = 0.0f; P.ma = -1.0f; P.sk = 0.0f; P.mk = 0.0f; P.so = 0.0f; P.mo = 0.0f; P.ia = -1; P.nan = 0;
     if (tid < t.count) {
         const int n = t.start + tid;
         const int I = n % b.NI1 + 1, J = (n / b.NI1) % b.NJ1 + 1, K = n / (b.NI1 * b.NJ1) + 1;
@@ -211,47 +271,65 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
         double* V2 = slot(b, S_V + 2);
         double* V3 = slot(b, S_V + 3);
         double* V4 = slot(b, S_V + 4);
-        auto Dq = [&](int L) { return (double)fslot(b, S_D + L)[c]; };
-        const double AinRo = Dq(0), AinRx = Dq(1), AinRy = Dq(2), AinRz = Dq(3), AinRe = Dq(4);
-        const double d6 = Dq(5), d7 = Dq(6);
-        double pRo = V0[c];
-        const double roinv = 1.0 / pRo;
-        nanf = isnan(AinRo) ? 1 : 0;
-        const double DR = fabs(AinRo) * roinv, DRk = fabs(d6) * roinv, DRo = fabs(d7) * roinv;
-        sa = DR * DR; ma = DR; ia = n;
-        sk = DRk * DRk; mk = DRk; so = DRo * DRo; mo = DRo;
-        double pVx = V1[c] * roinv, pVy = V2[c] * roinv, pVz = V3[c] * roinv;
-        const double AinX = (AinRx - pVx * AinRo) * roinv;
-        const double AinY = (AinRy - pVy * AinRo) * roinv;
-        const double AinZ = (AinRz - pVz * AinRo) * roinv;
-        const double AinP = (1.4 - 1.0) * (AinRe - 0.5 * AinRo * (pVx * pVx + pVy * pVy + pVz * pVz)
-                                           - pRo * (AinX * pVx + AinY * pVy + AinZ * pVz));
-        pRo = fabs(positive_add(pRo, AinRo));
+        auto Dq = [&](int L) { return fslot(b, S_D + L)[c]; };
+        const float AinRo = Dq(0), AinRx = Dq(1), AinRy = Dq(2), AinRz = Dq(3), AinRe = Dq(4);
+        const float d6 = Dq(5), d7 = Dq(6);
         double* PP = slot(b, S_PP);
-        const double pp = fabs(positive_add(PP[c], AinP));
+        const double rho0 = V0[c], m1 = V1[c], m2 = V2[c], m3 = V3[c], p0 = PP[c];
+        const float radc = fslot(b, S_RAD)[c];
+        const float rof = f32_rn(rho0), roinv = 1.0f / rof;
+        const float m1f = f32_rn(m1), m2f = f32_rn(m2), m3f = f32_rn(m3);
+        P.nan = isnan(AinRo) ? 1 : 0;
+        const float DR = fabsf(AinRo) * roinv, DRk = fabsf(d6) * roinv, DRo = fabsf(d7) * roinv;
+        P.sa = DR * DR; P.ma = DR; P.ia = n;
+        P.sk = DRk * DRk; P.mk = DRk; P.so = DRo * DRo; P.mo = DRo;
+        const float pVx = m1f * roinv, pVy = m2f * roinv, pVz = m3f * roinv;
+        const float AinX = (AinRx - pVx * AinRo) * roinv;
+        const float AinY = (AinRy - pVy * AinRo) * roinv;
+        const float AinZ = (AinRz - pVz * AinRo) * roinv;
+        const float AinP = (1.4f - 1.0f) * (AinRe - 0.5f * AinRo * (pVx * pVx + pVy * pVy + pVz * pVz)
+                                            - rof * (AinX * pVx + AinY * pVy + AinZ * pVz));
+        // density rho' = |rho exp(dRo/rho)| (rho + dRo for dRo >= 0); r = rho'/rho - 1
+        float r;
+        double rho;
+        if (AinRo >= 0.0f) {
+            r = AinRo * roinv;
+            rho = rho0 + f64_of(AinRo);
+        } else {
+            r = expm1f(AinRo / (rof + 1.0e-10f));
+            rho = rho0 + rho0 * f64_of(r);
+        }
+        rho = fabs(rho);
+        const float rhof = f32_rn(rho);
+        // momentum rho'(m/rho + a) = m + (m r + rho' a)
+        V1[c] = m1 + f64_of(m1f * r + rhof * AinX);
+        V2[c] = m2 + f64_of(m2f * r + rhof * AinY);
+        V3[c] = m3 + f64_of(m3f * r + rhof * AinZ);
+        V0[c] = rho;
+        const double pp = fabs(positive_add(p0, AinP));
         PP[c] = pp;
-        const double T = cd.p.RXM2 * pp / pRo;
-        slot(b, S_T)[c] = T;
-        pVx += AinX; pVy += AinY; pVz += AinZ;
-        V0[c] = pRo;
-        V1[c] = pRo * pVx;
-        V2[c] = pRo * pVy;
-        V3[c] = pRo * pVz;
-        const double rr = cd.p.omega0 * slot(b, S_RAD)[c];
-        V4[c] = pp * (1.0 / (1.4 - 1.0)) + (0.5 * (pVx * pVx + pVy * pVy + pVz * pVz) - 0.5 * rr * rr) * pRo;
+        const float Tf = cd.pf.RXM2 * f32_rn(pp) / rhof;
+        slot(b, S_T)[c] = f64_of(Tf);
+        const float ux = pVx + AinX, uy = pVy + AinY, uz = pVz + AinZ;
+        const float rr = cd.pf.omega0 * radc;
+        V4[c] = pp * (1.0 / (1.4 - 1.0)) + f64_of((0.5f * (ux * ux + uy * uy + uz * uz) - 0.5f * rr * rr) * rhof);
         if (turb_upd) {   // TIME_Update_V.F90:709-816
+            // the SST inputs as one batch of loads after the mean-flow stores (hoisting them
+            // above those too raised the kernel from 56 to 70 registers and measured slower)
             double* V5 = slot(b, S_V + 5);
             double* V6 = slot(b, S_V + 6);
             double ARTk = dmax(positive_add(V5[c], d6), 1.0e-10);
             double ARTO = dmax(positive_add(V6[c], d7), 1.0e-10);
             const ParamsT<float>& p = cd.pf;
-            const float ro = (float)pRo, kf = (float)ARTk;
-            float of = (float)ARTO;
-            const float RmiuL = mu_suth<float>(p, (float)T);
+            const float ro = rhof, kf = f32_rn(ARTk);
+            float of = f32_rn(ARTO);
+            const float RmiuL = mu_suth<float>(p, Tf);
             const float DistN = fslot(b, S_DST)[c];
-            auto G = [&](int q) { return fslot(b, S_DQ + q)[c]; };
-            const float Dudx = G(0), Dudy = G(1), Dudz = G(2), Dvdx = G(3), Dvdy = G(4), Dvdz = G(5);
-            const float Dwdx = G(6), Dwdy = G(7), Dwdz = G(8);
+            float Gq[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) Gq[q] = fslot(b, S_DQ + q)[c];
+            const float Dudx = Gq[0], Dudy = Gq[1], Dudz = Gq[2], Dvdx = Gq[3], Dvdy = Gq[4], Dvdz = Gq[5];
+            const float Dwdx = Gq[6], Dwdy = Gq[7], Dwdz = Gq[8];
             const float Div = Dudx + Dvdy + Dwdz;
             const float prod = 2.0f * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz) + sq(Dudy + Dvdx) + sq(Dvdz + Dwdy)
                                + sq(Dwdx + Dudz) - (2.0f / 3.0f) * Div * Div;
@@ -261,13 +339,14 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
                 const float Sii = Dudx - t3, Sjj = Dvdy - t3, Skk = Dwdz - t3;
                 const float Sij = 0.5f * (Dudy + Dvdx), Sik = 0.5f * (Dudz + Dwdx), Sjk = 0.5f * (Dvdz + Dwdy);
                 const float Skl = sqrtf(Sii * Sii + Sjj * Sjj + Skk * Skk + 2.0f * (Sij * Sij + Sik * Sik + Sjk * Sjk));
-                ARTO = dmax(ARTO, (double)(sqrtf(ro * fabsf(prod) / (p.Prod_Lmt * Bs)) / Ref));
-                of = (float)ARTO;
-                ARTk = dmin(ARTk, (double)(100000.0f * RmiuL * of / ro));
+                of = fmaxf(of, sqrtf(ro * fabsf(prod) / (p.Prod_Lmt * Bs)) / Ref);
+                const float kl = fminf(kf, 100000.0f * RmiuL * of / ro);
+                ARTO = of == f32_rn(ARTO) ? ARTO : f64_of(of);
+                ARTk = kl == kf ? ARTk : f64_of(kl);
                 V5[c] = ARTk;
                 V6[c] = ARTO;
                 const float om = fmaxf(of, 0.875f * ro * sqrtf(Skl * Skl * (2.0f / 0.09f)) / Ref);
-                slot(b, S_RMIU)[c] = (double)((float)ARTk / om * ro);
+                slot(b, S_RMIU)[c] = f64_of(kl / om * ro);
             } else {
             float arg2 = 2.0f * sqrtf(kf / ro) / Bs / (of / ro) / DistN / Ref;
             arg2 = fmaxf(arg2, 500.0f * RmiuL / DistN / DistN / of / Ref / Ref);
@@ -275,19 +354,18 @@ __global__ void k_update_mixed(const DevBlock* __restrict__ blks, const Tile* __
             const float Sij = 0.5f * (Dudy + Dvdx), Sik = 0.5f * (Dudz + Dwdx), Sjk = 0.5f * (Dvdz + Dwdy);
             const float Skl = sqrtf(2.0f * (Dudx * Dudx + Dvdy * Dvdy + Dwdz * Dwdz + 2.0f * (Sij * Sij + Sik * Sik + Sjk * Sjk)));
             const float Cmua = fminf(1.0f, p.A1 * of / ro / (Skl * arg2 + 1.e-10f) * Ref);
-            ARTO = dmax(ARTO, (double)(sqrtf(ro * Cmua * fabsf(prod) / (p.Prod_Lmt * Bs)) / Ref));
-            of = (float)ARTO;
-            ARTk = dmin(ARTk, (double)(100000.0f * RmiuL * of / ro / Cmua));
+            of = fmaxf(of, sqrtf(ro * Cmua * fabsf(prod) / (p.Prod_Lmt * Bs)) / Ref);
+            const float kl = fminf(kf, 100000.0f * RmiuL * of / ro / Cmua);
+            ARTO = of == f32_rn(ARTO) ? ARTO : f64_of(of);
+            ARTk = kl == kf ? ARTk : f64_of(kl);
             V5[c] = ARTk;
             V6[c] = ARTO;
-            slot(b, S_RMIU)[c] = (double)(Cmua * (float)ARTk / of * ro);
+            slot(b, S_RMIU)[c] = f64_of(Cmua * kl / of * ro);
             }
         }
     }
-    NormPart P;
-    P.sa = sa; P.ma = ma; P.sk = sk; P.mk = mk; P.so = so; P.mo = mo; P.ia = ia; P.nan = nanf; P.pad_ = 0;
-    P = norm_reduce_cta(P);
-    if (tid == 0) parts[blockIdx.x] = P;
+    const NormPart R = norm_reduce_cta_f(P);
+    if (tid == 0) parts[blockIdx.x] = R;
 }
 
 // ---------------------------------------------------------------------------------------

@@ -65,6 +65,9 @@ constexpr int RT_NARROW = RT_D + 2;       // ... of the two-point fields
 constexpr int NRMAP = 5;                  // tensor maps per block: direction 1; 2 stencil, two-point; 3 stencil, two-point
 constexpr unsigned RT_WAIT_LIMIT = 1u << 20;   // polls of the tile's mbarrier before the kernel gives up
 cudaError_t prepare_resid_tma();          // the kernels' dynamic shared-memory opt-in
+// the integer-pipe double <-> float conversions against the hardware ones on n patterns
+// (mismatches[0]: double -> float, [1]: float -> double)
+cudaError_t check_conversions(long long n, unsigned long long seed, long long* mismatches);
 void launch_resid_tma(int dir, cudaStream_t s, const DevBlock* blks, const ResidTile* tiles, int nt, const CaseDev* cdev,
                       const void* maps, int* err, unsigned limit);
 
@@ -112,7 +115,8 @@ struct FluxLaunchers {
     cudaError_t (*sweep_tiles)(cudaStream_t, const SweepView&, const TileView&, int lanes, int* flags, int* counter, SweepSync*,
                                int grid, int block, unsigned limit);
     int (*sweep_tiles_occupancy)(int block);
-    void (*scatter)(cudaStream_t, const DevBlock*, const SweepView&, int l0);   // DeltaQ l0..6 back to cell order
+    // DeltaQ l0..6 back to cell order, one thread per interior cell of the cell tiles
+    void (*scatter)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const SweepView&, int l0);
     size_t elem;                                    // bytes of the sweep arithmetic type
     int rec_width;                                  // sweep record entries per position (NREC, or NCREC in FP32)
 };

@@ -617,7 +617,7 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
                 else rc = run_sweeps(c);
                 if (rc) return rc;
             }
-            { KScope t(c, K_SCATTER); c->fl->scatter(s, c->d_blk, c->sv, c->sweep_lanes == 2 ? 5 : 0); }
+            { KScope t(c, K_SCATTER); c->fl->scatter(s, c->d_blk, c->d_cell, nct, c->d_qpos, c->sv, c->sweep_lanes == 2 ? 5 : 0); }
             c->launches++;
             break;
         }
