@@ -483,8 +483,10 @@ __global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __rest
                       rs<R>(b, S_PRIM + 3), rs<R>(b, S_PRIM + 4)};
     int nq = turb ? 6 : 4;
     const R* SD = rs<R>(b, S_SD);
-    // the gradients stay in registers until every stencil load is issued (a load after a store
-    // to the same arena would wait for the previous round trip), then go out together
+    // FP32: the gradients stay in registers until every stencil load is issued (a load after a
+    // store to the same arena would wait for the previous round trip), then go out together;
+    // FP64: stored as they come (holding them raised the FP64 kernel from 128 to 158 registers,
+    // and it is bound by the FP64 pipe, not by load latency)
     R gq[6][3];
     for (int q = 0; q < nq; ++q) {
         R fw[3], fe[3];
@@ -501,10 +503,12 @@ __global__ void k_gradient(const DevBlock* __restrict__ blks, const Tile* __rest
             R g = volinv * (fe[0] * S1[c + st[0]] - fw[0] * S1[c] + fe[1] * S2[c + st[1]] - fw[1] * S2[c]
                                  + fe[2] * S3[c + st[2]] - fw[2] * S3[c]);
             gq[q][m] = g;
+            if constexpr (sizeof(R) == 8) rs<R>(b, S_DQ + 3 * q + m)[c] = g;
         }
     }
-    for (int q = 0; q < nq; ++q)
-        for (int m = 0; m < 3; ++m) rs<R>(b, S_DQ + 3 * q + m)[c] = gq[q][m];
+    if constexpr (sizeof(R) == 4)
+        for (int q = 0; q < nq; ++q)
+            for (int m = 0; m < 3; ++m) rs<R>(b, S_DQ + 3 * q + m)[c] = gq[q][m];
     R DuDx = gq[0][0], DuDy = gq[0][1], DuDz = gq[0][2];
     R DvDx = gq[1][0], DvDy = gq[1][1], DvDz = gq[1][2];
     R DwDx = gq[2][0], DwDy = gq[2][1], DwDz = gq[2][2];
