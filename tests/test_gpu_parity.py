@@ -233,7 +233,8 @@ def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
     dataflow schedule, the tiled wavefront (two tile shapes), each with the lane-major and the
     warp-per-component thread mapping (FP64), the chaining, prefetch and CTA-size variants of the
     hyperplane launches, the mixed path's cluster-barrier schedule (one thread-block cluster per
-    block; the FP64 path runs planes for it), and the tuner's pick compute every DeltaQ with
+    block) and two-plane schedule (the positions of a plane recomputed by each neighbour on the
+    next; the FP64 path runs planes for both), and the tuner's pick compute every DeltaQ with
     the same operations: states after 6 iterations are bit-identical."""
     from helpers import small_cascade
     from trans_gb300 import abi
@@ -241,7 +242,7 @@ def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
     out = {}
     modes = ("planes", "planes_unchained", "coop", "flow", "tiles", "tiles_4x2x3", "planes_wpc", "planes_unchained_wpc",
              "coop_wpc", "tiles_4x2x3_wpc", "planes_pf2", "planes_wpc_pf1", "planes_early_cta32", "planes_early_pf2_cta64",
-             "clusters", "clusters_pf2", "auto")
+             "clusters", "clusters_pf2", "pairs", "pairs_unchained", "pairs_early_cta32", "pairs_early_pf1_cta128", "auto")
     for mode in modes:
         parts = mode.split("_")
         monkeypatch.setenv("TRANS_SWEEP", parts[0])
@@ -261,6 +262,29 @@ def test_sweep_schedules_agree_bitwise(gpu_lib, precision, monkeypatch):
         for ib in range(len(out["planes"])):
             m = interior(c.blocks[ib].dims)
             assert bit_equal_fraction(out[mode][ib], out["planes"][ib], m) == 1.0, (mode, ib)
+
+
+def test_pair_sweeps_runge_kutta_bitwise(gpu_lib, monkeypatch):
+    """Mixed path, SSP-RK3 (the sweeps carry only k and omega, the other components pass through
+    the two DeltaQ arrays unchanged): the two-plane schedule equals one launch per plane bit for
+    bit, on the channel and on the five-block cascade."""
+    from helpers import small_cascade
+    from trans_gb300 import abi
+    from trans_gb300.solver import Solver
+    for make in (small_channel, small_cascade):
+        out = {}
+        for mode in ("planes", "pairs"):
+            monkeypatch.setenv("TRANS_SWEEP", mode)
+            c, conns, geo, st = make(Kind_Spatial=3, Kind_Roe=3, IF_RK=1, CFL_Sub_start=1.0, CFL_Sub_end=1.0)
+            c.params.precision = abi.TRANS_MIXED
+            s = Solver(c, conns, geo, st)
+            for ki in range(1, 4):
+                s.iterate(ki)
+            out[mode] = [s.get_field(ib, "V") for ib in range(len(c.blocks))]
+            s.close()
+        for ib in range(len(out["planes"])):
+            m = interior(c.blocks[ib].dims)
+            assert bit_equal_fraction(out["pairs"][ib], out["planes"][ib], m) == 1.0, (make.__name__, ib)
 
 
 def test_long_run_field_parity(gpu_lib):

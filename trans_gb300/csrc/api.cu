@@ -189,7 +189,8 @@ long long trans_device_bytes(void* ctx) {
     long long b = 0;
     for (const CaseRec* cs : c->cases)
         b += (long long)(cs->arena_doubles * (sizeof(double) + (cs->farena ? sizeof(float) : 0)));
-    b += (c->sv.n + 31) / 32 * 32 * ((long long)(c->fl->rec_width + DQ_STRIDE) * (long long)c->fl->elem + 8LL * (long long)sizeof(int));
+    const long long dq_arrays = c->fl->sweep_pair ? 2 : 1;      // the mixed path's two-plane schedule keeps a second one
+    b += (c->sv.n + 31) / 32 * 32 * ((long long)(c->fl->rec_width + dq_arrays * DQ_STRIDE) * (long long)c->fl->elem + 8LL * (long long)sizeof(int));
     return b;
 }
 
@@ -232,11 +233,14 @@ const char* trans_tuning(void* ctx) {
     static thread_local std::string out;
     const std::string tiles = c->sweep_mode == 3 ? std::to_string(c->tile_shape[0]) + "x" + std::to_string(c->tile_shape[1]) + "x"
                                                        + std::to_string(c->tile_shape[2]) + "/" : std::string();
-    out = "sweep=" + std::string(c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : c->sweep_mode == 2 ? "flow " : c->sweep_mode == 4 ? "clusters " : "tiles ")
+    const std::string chain = c->pdl ? (c->pdl == 2 ? "-early" : "-chained") : "";
+    out = "sweep=" + std::string(c->sweep_mode == 5 ? "pairs" + chain
+                                 : c->sweep_mode >= 1 ? std::string(c->sweep_mode == 1 ? "coop " : c->sweep_mode == 2 ? "flow " : c->sweep_mode == 4 ? "clusters " : "tiles ")
                                                       + tiles + std::to_string(c->sweep_grid) + "x" + std::to_string(c->sweep_block)
                                  : c->sweep_mode == 0 ? (c->pdl ? (c->pdl == 2 ? "planes-early" : "planes-chained") : "planes") : "untuned")
-          + (c->sweep_wpc ? "/wpc" : "") + (c->sweep_pf && (c->sweep_mode == 0 || c->sweep_mode == 4) ? "/pf" + std::to_string(c->sweep_pf) : "")
-          + (c->sweep_cta && c->sweep_mode == 0 ? "/cta" + std::to_string(c->sweep_cta) : "")
+          + (c->sweep_wpc ? "/wpc" : "")
+          + (c->sweep_pf && (c->sweep_mode == 0 || c->sweep_mode == 4 || c->sweep_mode == 5) ? "/pf" + std::to_string(c->sweep_pf) : "")
+          + (c->sweep_cta && (c->sweep_mode == 0 || c->sweep_mode == 5) ? "/cta" + std::to_string(c->sweep_cta) : "")
           + "; measured: " + c->sweep_tuning
           + (c->mixed ? std::string("; residual=") + (c->resid_tma == 1 ? "tma" : c->resid_tma == 0 ? "gather" : "untuned")
                             + (c->resid_tuning.empty() ? std::string() : " (" + c->resid_tuning + ")")

@@ -130,7 +130,9 @@ long long case_bytes(const trans_params* p, int nblocks, const trans_block* bloc
     const long long elem = precision == TRANS_MIXED ? 4 : 8;
     long long b = padded * case_slots(*p) * (8 + (precision == TRANS_MIXED ? 4 : 0));
     const long long rec = precision == TRANS_MIXED ? NCREC : NREC;      // sweep record entries per position
-    b += interior * ((rec + 2LL * DQ_STRIDE) * elem + 8LL * 4 + (long long)sizeof(SweepCell));
+    // DeltaQ arrays: the sweep's, the tuner's copy, and in the mixed path the two-plane schedule's second one
+    const long long ndq = precision == TRANS_MIXED ? 3 : 2;
+    b += interior * ((rec + ndq * DQ_STRIDE) * elem + 8LL * 4 + (long long)sizeof(SweepCell));
     if (p->IF_Precondition == 1) b += interior * 6LL * NPC * 8;          // the neighbours' PrecondDW coefficients
     b += interior / 16 + 4096;           // tiles, norm partials, boundary tables (rounded up)
     return b;
@@ -184,7 +186,8 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     // polls (for tests of the timeout path: a small n makes the waits run out)
     const char* sp = std::getenv("TRANS_SWEEP_SPIN");
     if (sp) c->spin_limit = (unsigned)std::max(0L, std::strtol(sp, nullptr, 10));
-    // sweep schedule: TRANS_SWEEP=planes | coop | flow | tiles forces one (for tests); default: tuned
+    // sweep schedule: TRANS_SWEEP=planes | coop | flow | tiles | clusters | pairs forces one (for tests);
+    // default: tuned
     const char* m = std::getenv("TRANS_SWEEP");
     std::string ms = m ? m : "";
     // clusters: the mixed path's cluster-barrier schedule (the FP64 path takes planes)
@@ -194,6 +197,12 @@ int ctx_init(Ctx* c, int precision, long long budget) {
         c->sweep_mode = 4; c->sweep_grid = 8; c->sweep_block = 256;
         const char* pfs = std::getenv("TRANS_SWEEP_PF");
         c->sweep_pf = pfs ? std::max(0, std::atoi(pfs)) : 0;
+    }
+    // pairs: two hyperplanes per launch (mixed path; the FP64 path takes planes)
+    if (ms == "pairs") ms = c->mixed ? "pairs" : "planes";
+    if (ms == "pairs") {
+        c->sweep_forced = true;
+        c->sweep_mode = 5;
     }
     if (ms == "planes" || ms == "coop" || ms == "flow" || ms == "tiles") {
         int dev = 0, nsm = 0;
@@ -220,7 +229,8 @@ void free_worklists(Ctx* c) {
     for (int d = 0; d < 3; ++d) { dfree(c->d_face[d]); dfree(c->d_rtiles[d]); c->n_rtiles[d] = 0; }
     dfree(c->d_rmaps);
     dfree(c->d_bc); dfree(c->d_outlet); dfree(c->d_lines); dfree(c->d_sweep); dfree(c->d_plane_off); dfree(c->d_pb_off);
-    dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq_save); dfree(c->d_parts); dfree(c->d_pc);
+    dfree(c->d_nbp); dfree(c->d_flags); dfree(c->d_rec); dfree(c->d_dqs); dfree(c->d_dq2); dfree(c->d_orph); dfree(c->d_dq_save);
+    c->pair_lo.clear(); c->pair_up.clear(); dfree(c->d_parts); dfree(c->d_pc);
     dfree(c->d_cdev); dfree(c->d_stage); dfree(c->d_tile_first); dfree(c->d_norms);
     dfree(c->d_tiles); dfree(c->d_tflags); dfree(c->d_qpos); dfree(c->d_bc_first); dfree(c->d_intg);
     c->tv = TileView{};

@@ -103,7 +103,13 @@ struct Ctx {
     int* d_flags = nullptr;
     void* d_rec = nullptr;
     void* d_dqs = nullptr;
+    void* d_dq2 = nullptr;               // the lower sweep's results in the two-plane schedule (mixed path)
     void* d_dq_save = nullptr;
+    // two-plane schedule (sweep_mode 5): per launch the second plane's positions and the first
+    // plane's positions that no position of the second plane reaches (offsets into d_orph)
+    struct SweepPair { int p_first, p_count, o_off, o_count; };
+    std::vector<SweepPair> pair_lo, pair_up;
+    int* d_orph = nullptr;
     double* d_pc = nullptr;              // PrecondDW coefficients of the sweep neighbours (IF_Precondition = 1)
     NormPart* d_parts = nullptr;
     std::vector<NormPart> h_parts;
@@ -130,7 +136,8 @@ struct Ctx {
     // 0 = one launch per hyperplane (graph), 1 = one cooperative launch with grid barriers,
     // 2 = dataflow over ready flags, 3 = tiled wavefront, 4 = one thread-block cluster per
     // block with cluster barriers between hyperplanes (mixed path; sweep_grid = CTAs per
-    // cluster); -1 = pick the fastest on first use
+    // cluster), 5 = two hyperplanes per launch (mixed path, graph); -1 = pick the fastest on
+    // first use
     // (all bit-identical)
     int sweep_mode = -1, sweep_grid = 0, sweep_block = 0;
     int tile_shape[3] = {0, 0, 0};       // tiles of the tiled wavefront (built for this shape)
@@ -144,6 +151,7 @@ struct Ctx {
                                          // 2 = the mixed path's release of the next launch at entry)
     int pdl_allowed = 1;                 // chaining may be picked by the tuner (TRANS_PDL=0 forbids it)
     int sweep_exec_pdl = -1;             // chaining the sweep graph was captured with
+    int sweep_exec_mode = -1;            // schedule (0 or 5) the sweep graph was captured with
     int sweep_wpc = 0;                   // SWEEP_WPC: warp-per-component thread mapping (0: lane-major)
     int sweep_exec_wpc = -1;             // mapping the sweep graph was captured with
     int sweep_pf = 0;                    // L2 prefetch distance of the hyperplane launches (0 = none)

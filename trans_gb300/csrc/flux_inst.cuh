@@ -1,5 +1,7 @@
 // flux_inst.cuh -- instantiation of the templated flux/source/sweep kernels for one type R.
 // Included once per precision translation unit with TG_R and TG_NAME defined.
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "launch.h"
 
@@ -138,6 +140,31 @@ int swt_occ(int block) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tiles<TG_R>, block, 0) != cudaSuccess) return 0;
     return n;
 }
+void swpair(cudaStream_t s, const SweepView& v, void* y, bool lower, int p_first, int p_count, const int* orph, int o_count,
+            int turb, int chained, int pf_first, int pf_count, int cta) {
+    if constexpr (sizeof(TG_R) == 4) {
+        const int n = p_count + o_count;
+        if (n <= 0) return;
+        const int CTA = std::min(cta > 0 ? cta : SWEEP_CTA, 128);      // the kernel's launch bound
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((n + CTA - 1) / CTA);
+        cfg.blockDim = dim3(CTA);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = chained ? 1 : 0;
+        float* X = (float*)v.dq;
+        float* Y = (float*)y;
+        if (lower)
+            cudaLaunchKernelEx(&cfg, k_sweep_pair<true>, (const int*)v.nbp, (const float*)v.rec, X, Y, p_first, p_count, orph,
+                               o_count, turb & 3, chained, pf_first, pf_count);
+        else
+            cudaLaunchKernelEx(&cfg, k_sweep_pair<false>, (const int*)v.nbp, (const float*)v.rec, X, Y, p_first, p_count, orph,
+                               o_count, turb & 3, chained, pf_first, pf_count);
+    }
+}
 void scat(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const int* qpos, const SweepView& v, int l0) {
     if (nt > 0 && v.n > 0) k_sweep_scatter<TG_R><<<nt, CELL_TILE, 0, s>>>(b, tiles, qpos, (const TG_R*)v.dq, l0);
 }
@@ -145,7 +172,8 @@ void scat(cudaStream_t s, const DevBlock* b, const Tile* tiles, int nt, const in
 
 const FluxLaunchers& TG_NAME() {
     static const FluxLaunchers L = {grd, shg, bcg, {ff<1>, ff<2>, ff<3>}, ga, fc, hu, prep, jac, swl, swu, swa, swa_occ, swf, swf_occ,
-                                    swt, swt_occ, scat, sizeof(TG_R), sizeof(TG_R) == 4 ? (int)NCREC : (int)NREC};
+                                    swt, swt_occ, scat, sizeof(TG_R) == 4 ? swpair : nullptr, sizeof(TG_R),
+                                    sizeof(TG_R) == 4 ? (int)NCREC : (int)NREC};
     return L;
 }
 }  // namespace tg

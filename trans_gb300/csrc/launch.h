@@ -117,6 +117,11 @@ struct FluxLaunchers {
     int (*sweep_tiles_occupancy)(int block);
     // DeltaQ l0..6 back to cell order, one thread per interior cell of the cell tiles
     void (*scatter)(cudaStream_t, const DevBlock*, const Tile*, int nt, const int* qpos, const SweepView&, int l0);
+    // two hyperplanes per launch (mixed path only; null in FP64): the lower sweep reads v.dq and
+    // writes y, the upper reads y and writes v.dq; p_first/p_count: the second plane, orph/o_count:
+    // the first plane's positions with no neighbour on the second
+    void (*sweep_pair)(cudaStream_t, const SweepView&, void* y, bool lower, int p_first, int p_count, const int* orph,
+                       int o_count, int lanes, int chained, int pf_first, int pf_count, int cta);
     size_t elem;                                    // bytes of the sweep arithmetic type
     int rec_width;                                  // sweep record entries per position (NREC, or NCREC in FP32)
 };

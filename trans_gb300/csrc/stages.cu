@@ -271,8 +271,8 @@ namespace {
 
 int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
     const int lanes = c->sweep_lanes | c->sweep_wpc;
-    if (mode == 0 && c->sweep_exec &&
-        (c->sweep_exec_pdl != c->pdl || c->sweep_exec_wpc != c->sweep_wpc || c->sweep_exec_pf != c->sweep_pf ||
+    if ((mode == 0 || mode == 5) && c->sweep_exec &&
+        (c->sweep_exec_mode != mode || c->sweep_exec_pdl != c->pdl || c->sweep_exec_wpc != c->sweep_wpc || c->sweep_exec_pf != c->sweep_pf ||
          c->sweep_exec_cta != c->sweep_cta)) {   // changed
         cudaGraphExecDestroy(c->sweep_exec);
         c->sweep_exec = nullptr;
@@ -315,10 +315,37 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         c->launches++;
         return TRANS_OK;
     }
-    // one launch per hyperplane, L ascending then U descending, replayed as one graph (or
-    // captured directly into the caller's graph)
+    // one launch per hyperplane (mode 0) or per two (mode 5), L ascending then U descending,
+    // replayed as one graph (or captured directly into the caller's graph)
     // hyperplane h of the L sweep prefetches hyperplane h + sweep_pf into L2, the U sweep h - sweep_pf
+    // (mode 5: the planes of the pair sweep_pf launches ahead)
+    if (mode == 5 && !c->fl->sweep_pair) return fail(c, TRANS_E_ARG, "two-plane sweeps are a mixed-path schedule");
+    auto pairs = [&]() {
+        const int d = c->sweep_pf;
+        const int np = (int)c->pair_lo.size();
+        auto pf_range = [&](const std::vector<Ctx::SweepPair>& v, int k, int& first, int& count) {
+            first = 0; count = 0;
+            if (!d || k + d >= (int)v.size()) return;
+            const Ctx::SweepPair& a = v[k + d];
+            if (a.p_count) { first = a.p_first; count = a.p_count; }
+        };
+        for (int k = 0; k < np; ++k) {
+            const Ctx::SweepPair& a = c->pair_lo[k];
+            int pf0, pfn;
+            pf_range(c->pair_lo, k, pf0, pfn);
+            c->fl->sweep_pair(s, c->sv, c->d_dq2, true, a.p_first, a.p_count, c->d_orph + a.o_off, a.o_count, lanes,
+                              c->pdl, pf0, pfn, c->sweep_cta);
+        }
+        for (int k = 0; k < (int)c->pair_up.size(); ++k) {
+            const Ctx::SweepPair& a = c->pair_up[k];
+            int pf0, pfn;
+            pf_range(c->pair_up, k, pf0, pfn);
+            c->fl->sweep_pair(s, c->sv, c->d_dq2, false, a.p_first, a.p_count, c->d_orph + a.o_off, a.o_count, lanes,
+                              c->pdl, pf0, pfn, c->sweep_cta);
+        }
+    };
     auto planes = [&]() {
+        if (mode == 5) { pairs(); return; }
         const int d = c->sweep_pf;
         auto cnt = [&](int h) { return (h >= 0 && h < nh) ? c->plane_off[h + 1] - c->plane_off[h] : 0; };
         for (int h = 0; h < nh; ++h)
@@ -331,6 +358,11 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
                                    d ? cnt(h - d) : 0, c->sweep_cta);
     };
     auto count_planes = [&]() {
+        if (mode == 5) {
+            for (const auto* v : {&c->pair_lo, &c->pair_up})
+                for (const Ctx::SweepPair& a : *v) c->launches += (a.p_count + a.o_count > 0) ? 1 : 0;
+            return;
+        }
         for (int h = 0; h < nh; ++h) c->launches += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
     };
     if (capture) {              // captured into the caller's graph: every hyperplane launch counts per replay
@@ -347,6 +379,7 @@ int sweep_once(Ctx* c, int mode, int grid, int block, bool capture = false) {
         e = cudaGraphInstantiate(&c->sweep_exec, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return fail(c, TRANS_E_CUDA, std::string("sweep graph instantiate: ") + cudaGetErrorString(e));
+        c->sweep_exec_mode = mode;
         c->sweep_exec_pdl = c->pdl;
         c->sweep_exec_wpc = c->sweep_wpc;
         c->sweep_exec_pf = c->sweep_pf;
@@ -381,6 +414,10 @@ int tune_sweeps(Ctx* c) {
         for (int pdl : {0, 1, 2})
             for (int pf : {0, 2})
                 for (int cta : {32, 64, 128}) cands.push_back({0, 0, 0, pdl, 0, 0, 0, 0, pf, cta});
+        // two hyperplanes per launch, chained
+        for (int pdl : {1, 2})
+            for (int pf : {0, 1})
+                for (int cta : {32, 64, 128}) cands.push_back({5, 0, 0, pdl, 0, 0, 0, 0, pf, cta});
         const int occ = c->fl->sweep_all_occupancy(256);
         if (occ >= 1) cands.push_back({1, nsm, 256, 0, 0, 0, 0, 0, 0});
         const int tocc = c->fl->sweep_tiles_occupancy(256);
@@ -421,7 +458,7 @@ int tune_sweeps(Ctx* c) {
     c->sweep_tuning.clear();
     int rc = save_dq(c, false);
     for (const Cand& k : cands) {
-        if (k.mode == 0) c->pdl = pdl0 ? k.pdl : 0;
+        if (k.mode == 0 || k.mode == 5) c->pdl = pdl0 ? k.pdl : 0;
         c->sweep_wpc = k.wpc;
         c->sweep_pf = k.pf;
         c->sweep_cta = k.cta;
@@ -436,7 +473,9 @@ int tune_sweeps(Ctx* c) {
             float ms = 0;
             CK(cudaEventElapsedTime(&ms, e0, e1));
             if (rep == 1) {
-                c->sweep_tuning += (k.mode ? std::string(k.mode == 1 ? "coop " : k.mode == 2 ? "flow " : k.mode == 4 ? "clusters " : "tiles ")
+                const std::string chain = c->pdl ? (c->pdl == 2 ? "-early" : "-chained") : "";
+                c->sweep_tuning += (k.mode == 5 ? "pairs" + chain
+                                    : k.mode ? std::string(k.mode == 1 ? "coop " : k.mode == 2 ? "flow " : k.mode == 4 ? "clusters " : "tiles ")
                                                  + (k.mode == 3 ? std::to_string(k.ti) + "x" + std::to_string(k.tj) + "x"
                                                                       + std::to_string(k.tk) + "/" : std::string())
                                                  + std::to_string(k.grid) + "x" + std::to_string(k.block)
@@ -463,7 +502,7 @@ int tune_sweeps(Ctx* c) {
     c->sweep_wpc = pick.wpc;
     c->sweep_pf = pick.pf;
     c->sweep_cta = pick.cta;
-    c->pdl = pick.mode == 0 ? (pdl0 ? pick.pdl : 0) : 0;
+    c->pdl = (pick.mode == 0 || pick.mode == 5) ? (pdl0 ? pick.pdl : 0) : 0;
     return TRANS_OK;
 }
 
@@ -611,8 +650,13 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             c->launches += 2;
             {
                 int nh = (int)c->plane_off.size() - 1, nl = 0;
-                for (int h = 0; h < nh; ++h) nl += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
-                KScope t(c, K_SWEEP, c->sweep_mode >= 1 ? 1 : nl);
+                if (c->sweep_mode == 5) {
+                    for (const auto* v : {&c->pair_lo, &c->pair_up})
+                        for (const Ctx::SweepPair& a : *v) nl += (a.p_count + a.o_count > 0) ? 1 : 0;
+                } else {
+                    for (int h = 0; h < nh; ++h) nl += (c->plane_off[h + 1] > c->plane_off[h]) ? 2 : 0;
+                }
+                KScope t(c, K_SWEEP, (c->sweep_mode >= 1 && c->sweep_mode != 5) ? 1 : nl);
                 if (capture) rc = sweep_once(c, c->sweep_mode, c->sweep_grid, c->sweep_block, true);
                 else rc = run_sweeps(c);
                 if (rc) return rc;

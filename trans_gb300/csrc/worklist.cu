@@ -333,6 +333,30 @@ int rebuild(Ctx* c) {
         if ((rc = upload_vec(c, qpos.data(), sizeof(int) * qpos.size(), (void**)&c->d_qpos))) return rc;
         CK(cudaMalloc(&c->d_rec, (size_t)c->fl->rec_width * Np * c->fl->elem));
         CK(cudaMalloc(&c->d_dqs, (size_t)DQ_STRIDE * Np * c->fl->elem));
+        if (c->fl->sweep_pair) {
+            // two-plane schedule: the second DeltaQ array, and per launch the first plane's
+            // positions that no neighbour on the second plane computes (block corners)
+            CK(cudaMalloc(&c->d_dq2, (size_t)DQ_STRIDE * Np * c->fl->elem));
+            const int nh = (int)c->plane_off.size() - 1;
+            std::vector<int> orph;
+            auto add = [&](std::vector<Ctx::SweepPair>& out, int h, int h1, int side) {
+                Ctx::SweepPair sp{0, 0, (int)orph.size(), 0};
+                if (h1 >= 0 && h1 < nh) { sp.p_first = c->plane_off[h1]; sp.p_count = c->plane_off[h1 + 1] - c->plane_off[h1]; }
+                for (int q = c->plane_off[h]; q < c->plane_off[h + 1]; ++q) {
+                    bool reached = false;
+                    for (int d = 0; d < 3; ++d) reached |= nbp[sw_at(q, side + d, 6)] >= 0;
+                    if (!reached || sp.p_count == 0) orph.push_back(q);
+                }
+                sp.o_count = (int)orph.size() - sp.o_off;
+                out.push_back(sp);
+            };
+            c->pair_lo.clear();
+            c->pair_up.clear();
+            for (int h = 0; h < nh; h += 2) add(c->pair_lo, h, h + 1, 3);        // reached from its upper neighbours
+            for (int h = nh - 1; h >= 0; h -= 2) add(c->pair_up, h, h - 1, 0);   // from its lower neighbours
+            if (orph.empty()) orph.push_back(0);
+            if ((rc = upload_vec(c, orph.data(), sizeof(int) * orph.size(), (void**)&c->d_orph))) return rc;
+        }
         CK(cudaMalloc(&c->d_flags, (size_t)2 * Np * sizeof(int)));
         c->sv.cells = c->d_sweep; c->sv.nbp = c->d_nbp; c->sv.rec = c->d_rec; c->sv.dq = c->d_dqs; c->sv.n = N;
         c->sv.pc = nullptr;
