@@ -143,7 +143,7 @@ int swt_occ(int block) {
 void swpair(cudaStream_t s, const SweepView& v, void* y, bool lower, int p_first, int p_count, const int* orph, int o_count,
             int turb, int chained, int pf_first, int pf_count, int cta) {
     if constexpr (sizeof(TG_R) == 4) {
-        const int n = p_count + o_count;
+        const int n = 4 * (p_count + o_count);                        // four lanes per item
         if (n <= 0) return;
         const int CTA = std::min(cta > 0 ? cta : SWEEP_CTA, 128);      // the kernel's launch bound
         cudaLaunchConfig_t cfg = {};

@@ -1690,20 +1690,21 @@ __global__ void k_sweep_c(const int* __restrict__ nbp, const float* __restrict__
     if (chained == 1) asm volatile("griddepcontrol.launch_dependents;");
 }
 
-// Two hyperplanes per launch (mixed path): the thread of position p on the second plane first
-// computes its up to three neighbours on the first plane -- each from its own neighbours on
-// the plane before, which the previous launch finished -- and then p from those values in
-// registers.  A position of the first plane is so computed by each of its neighbours on the
-// second plane, with the same inputs and arithmetic (sweep_core), and each of them stores the
-// same value; positions of the first plane with no neighbour on the second (block corners)
-// come as a list of their own (orph) and are computed alone.  One dependent launch and one L2
-// round trip per two planes instead of per plane, for up to four times the arithmetic.
-// Reads and writes go to different arrays, so that no thread can see a value another one is
-// replacing: the lower sweep reads the right-hand sides from X and writes Y, the upper sweep
-// reads the lower results from Y and writes the final DeltaQ back to X.  p_first, p_count:
-// the second plane's positions; chained, pf_first, pf_count as in k_sweep_c.  (A host-built
-// table of the neighbours' neighbours, one load round before the wait instead of two
-// dependent ones, measured slower: 1.64 against 1.41 ms of sweeps per cascade iteration.)
+// Two hyperplanes per launch (mixed path): four lanes per position p of the second plane.
+// Lanes 0-2 compute p's neighbour on the first plane in direction 0-2 -- each from its own
+// neighbours on the plane before, which the previous launch finished -- and pass it to lane 3
+// by warp shuffle, which then computes p.  A position of the first plane is so computed by
+// each of its neighbours on the second plane, with the same inputs and arithmetic (sweep_core,
+// shared with k_sweep_c), and each stores the same value; positions of the first plane with no
+// neighbour on the second (block corners) come as a list of their own (orph) and are computed
+// by lane 0 of an item alone.  One dependent launch and one L2 round trip per two planes
+// instead of per plane.  Reads and writes go to different arrays, so that no thread can see a
+// value another one is replacing: the lower sweep reads the right-hand sides from X and
+// writes Y, the upper sweep reads the lower results from Y and writes the final DeltaQ back to
+// X.  p_first, p_count: the second plane's positions; chained, pf_first, pf_count as in
+// k_sweep_c.  (One thread computing all four positions held 255 registers and took 1.40 ms of
+// sweeps per cascade iteration; a host-built table of the neighbours' neighbours, one load
+// round before the wait instead of two dependent ones, measured slower still.)
 template <bool LOWER>
 __global__ void __launch_bounds__(128) k_sweep_pair(const int* __restrict__ nbp, const float* __restrict__ rec, float* X, float* Y,
                                                     int p_first, int p_count, const int* __restrict__ orph, int o_count, int turb,
@@ -1715,56 +1716,55 @@ __global__ void __launch_bounds__(128) k_sweep_pair(const int* __restrict__ nbp,
         prefetch_l2_range(rec + sw_at(pf_first, 0, NCREC), (size_t)pf_count * NCREC * sizeof(float), g, T);
         prefetch_l2_range(nbp + sw_at(pf_first, 0, 6), (size_t)pf_count * 6 * sizeof(int), g, T);
     }
-    if (g >= p_count + o_count) {
-        if (chained) asm volatile("griddepcontrol.wait;" ::: "memory");
-        if (chained == 1) asm volatile("griddepcontrol.launch_dependents;");
-        return;
-    }
+    const int item = g >> 2, l = g & 3;
+    const bool valid = item < p_count + o_count;
+    const bool pair = item < p_count;
     const float* own_src = LOWER ? X : Y;          // the DeltaQ this sweep starts from
     float* dst = LOWER ? Y : X;                    // this sweep's results (neighbours read here)
     const float4* R4 = reinterpret_cast<const float4*>(rec);
     const float4* O4 = reinterpret_cast<const float4*>(own_src);
-    const bool pair = g < p_count;
-    const long long p = pair ? (long long)p_first + g : (long long)orph[g - p_count];
-    SweepStatic sp, sn[3];
-    sweep_static<LOWER>(nbp, R4, p, sp);
-    if (pair) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-            if (sp.np[d] >= 0) sweep_static<LOWER>(nbp, R4, sp.np[d], sn[d]);
+    // the position this lane computes: p (lane 3 of a pair item, lane 0 of an orphan) or p's
+    // neighbour on the first plane in direction l (lanes 0-2 of a pair item), -1 = none
+    long long p = -1, q = -1;
+    if (valid) {
+        p = pair ? (long long)p_first + item : (long long)orph[item - p_count];
+        if (!pair) q = l == 0 ? p : -1;
+        else if (l == 3) q = p;
+        else q = nbp[sw_at(p, (LOWER ? 0 : 3) + l, 6)];
     }
+    SweepStatic st;
+    if (q >= 0) sweep_static<LOWER>(nbp, R4, q, st);
     if (chained) asm volatile("griddepcontrol.wait;" ::: "memory");
-    const float4 po0 = __ldcg(O4 + (size_t)p * 2), po1 = __ldcg(O4 + (size_t)p * 2 + 1);
-    float4 a[3], t[3];
-    if (pair) {
-        // the first plane's neighbours from the plane before (all loads issued together)
-        float4 qa[3][3], qt[3][3], qo0[3], qo1[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const long long q = sp.np[d] >= 0 ? sp.np[d] : p;
-            if (sp.np[d] >= 0) sweep_nbvals(dst, sn[d], q, qa[d], qt[d]);
-            qo0[d] = __ldcg(O4 + (size_t)q * 2);
-            qo1[d] = __ldcg(O4 + (size_t)q * 2 + 1);
-        }
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            if (sp.np[d] < 0) {
-                a[d] = make_float4(0.f, 0.f, 0.f, 0.f);
-                t[d] = a[d];
-                continue;
-            }
-            float outq[8];
-            sweep_core<LOWER>(sn[d], qo0[d], qo1[d], qa[d], qt[d], turb, outq);
-            sweep_store(dst, sp.np[d], outq);
-            a[d] = make_float4(outq[0], outq[1], outq[2], outq[3]);
-            t[d] = make_float4(outq[4], outq[5], outq[6], outq[7]);
-        }
-    } else {
-        sweep_nbvals(dst, sp, p, a, t);
+    float out[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const bool first = q >= 0 && (!pair || l < 3);     // computes from the plane before
+    float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0;
+    if (q >= 0) {
+        o0 = __ldcg(O4 + (size_t)q * 2);
+        o1 = __ldcg(O4 + (size_t)q * 2 + 1);
     }
-    float out[8];
-    sweep_core<LOWER>(sp, po0, po1, a, t, turb, out);
-    sweep_store(dst, p, out);
+    if (first) {
+        float4 a[3], t[3];
+        sweep_nbvals(dst, st, q, a, t);
+        sweep_core<LOWER>(st, o0, o1, a, t, turb, out);
+        sweep_store(dst, q, out);
+    }
+    // lane 3 takes the first-plane values of lanes 0-2 (every lane shuffles)
+    float nb[3][8];
+    const int base = threadIdx.x & ~3 & 31;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int m = 0; m < 8; ++m) nb[d][m] = __shfl_sync(0xffffffffu, out[m], base + d);
+    if (pair && l == 3) {
+        float4 a[3], t[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            a[d] = make_float4(nb[d][0], nb[d][1], nb[d][2], nb[d][3]);
+            t[d] = make_float4(nb[d][4], nb[d][5], nb[d][6], nb[d][7]);
+        }
+        sweep_core<LOWER>(st, o0, o1, a, t, turb, out);
+        sweep_store(dst, q, out);
+    }
     if (chained == 1) asm volatile("griddepcontrol.launch_dependents;");
 }
 
