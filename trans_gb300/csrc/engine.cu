@@ -199,7 +199,7 @@ int ctx_init(Ctx* c, int precision, long long budget) {
         c->sweep_pf = pfs ? std::max(0, std::atoi(pfs)) : 0;
     }
     // pairs: two hyperplanes per launch (mixed path; the FP64 path takes planes)
-    if (ms == "pairs") ms = c->mixed ? "pairs" : "planes";
+    if (ms == "pairs" && !c->mixed) ms = "planes";
     if (ms == "pairs") {
         c->sweep_forced = true;
         c->sweep_mode = 5;

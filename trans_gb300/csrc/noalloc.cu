@@ -66,7 +66,7 @@ extern "C" int trans_update_static_scratch(void* ctx, int ki, trans_norms* norms
     CK(cudaMemcpyAsync(c->h_parts.data(), scratch, sizeof(NormPart) * c->h_parts.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     // a cooperative sweep of this iteration that gave up on a bounded wait left DeltaQ partial
-    if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
+    if (c->sweep_mode >= 1 && c->sweep_mode <= 3 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
     rc = reduce_norms(c);
     if (norms) std::copy(c->cases[0]->norms.begin(), c->cases[0]->norms.end(), norms);
     return rc;

@@ -469,7 +469,7 @@ int tune_sweeps(Ctx* c) {
             if ((rc = sweep_once(c, k.mode, k.grid, k.block))) break;
             CK(cudaEventRecord(e1, c->stream));
             CK(cudaEventSynchronize(e1));
-            if (k.mode != 0 && c->h_sync->err) { rc = -100; break; }
+            if (k.mode >= 1 && k.mode <= 3 && c->h_sync->err) { rc = -100; break; }   // the cooperative schedules report there
             float ms = 0;
             CK(cudaEventElapsedTime(&ms, e0, e1));
             if (rep == 1) {
@@ -680,7 +680,7 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
             CK(cudaMemcpyAsync(c->h_norms, c->d_norms, sizeof(BlockNorms) * nblk, cudaMemcpyDeviceToHost, s));
             CK(cudaMemcpyAsync(c->h_kerr, c->d_kerr, sizeof(int), cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
-            if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
+            if (c->sweep_mode >= 1 && c->sweep_mode <= 3 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
             if (*c->h_kerr) return fail(c, TRANS_E_TIMEOUT, "residual tile staging wait timed out");
             if ((rc = collect_norms(c, c->h_norms))) return rc;
             break;
@@ -834,7 +834,7 @@ int run_iterations(Ctx* c, int n) {
         }
         for (int q = 1; q < m; ++q) advance();  // KI of the last replayed iteration
         done += m;
-        if (c->sweep_mode >= 1 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
+        if (c->sweep_mode >= 1 && c->sweep_mode <= 3 && c->h_sync->err) return fail(c, TRANS_E_TIMEOUT, "LU-SGS sweep wait timed out");
         if (*c->h_kerr) return fail(c, TRANS_E_TIMEOUT, "residual tile staging wait timed out");
         if (nan) return fail(c, TRANS_E_NAN, "NaN in the density increment");
     }
