@@ -462,13 +462,16 @@ def roofline(lib, c, kt, nsub, precision, sched):
         roof["traffic"] = FACE_DRAM_BYTES * nunit / dom_n
         roof["traffic_source"] = FACE_DRAM_SOURCE
     elif dom == "k_sweep":
-        # the sweeps are bound by one dependent step per i+j+k hyperplane: report the measured
-        # step against the floor of a dependent launch chain of the same width (graph replay)
-        roof["binding"] = "latency (one dependent step per i+j+k hyperplane)"
-        if sched.startswith("sweep=planes"):
-            cells_per_plane = interior_cells(c) * nsub * 2 / dom_n      # dom_n counts both sweeps' hyperplanes
-            # threads per hyperplane: 8 per position in the FP64 path, 1 in the mixed path
-            threads = cells_per_plane * (8 if precision == "fp64" else 1)
+        # the sweeps are bound by one dependent step per i+j+k hyperplane (per two with the mixed
+        # path's two-plane launches): report the measured step against the floor of a dependent
+        # launch chain of the same width (graph replay)
+        pairs = sched.startswith("sweep=pairs")
+        roof["binding"] = "latency (one dependent step per " + ("two i+j+k hyperplanes" if pairs else "i+j+k hyperplane") + ")"
+        if sched.startswith("sweep=planes") or pairs:
+            cells_per_plane = interior_cells(c) * nsub * 2 / dom_n      # dom_n counts both sweeps' launches
+            # threads per launch: 8 per position in the FP64 path, 1 in the mixed path, 4 per
+            # second-plane position (half a launch's positions) in the two-plane launches
+            threads = cells_per_plane * (8 if precision == "fp64" else (2 if pairs else 1))
             grid = max(1, int(round(threads / 128)))
             chained = "chained" in sched.split(";")[0] or "early" in sched.split(";")[0]
             floor_us = lib.trans_probe_chain_us(1 if chained else 0, grid)
