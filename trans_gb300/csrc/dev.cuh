@@ -348,6 +348,41 @@ template <typename R> __device__ inline void mdcd_pair(const R* s6, R gama, R& q
     }
 }
 
+// The mixed path's FP32 form of mdcd_pair (the same states in another association): the left
+// and right states of a face use the same four three-cell stencils s0..s3 of the six cells.
+// With D_k = s_k - 2 s_{k+1} + s_{k+2} (k = 0..3), the smoothness indicators' second terms
+// beta^2 D^2 are shared (left ISK_k and right ISK_(5-k) use D_(k-1)), and of the first terms
+// four determine the rest: F3 = -(G2 + D2), F4 = G1 + D3, G3 = -(F2 + D1), G4 = F1 + D0 (F:
+// left, G: right); the four candidate values qq0..qq3 of the left state are those of the
+// right state in reverse order (1/3 = 2/6); the weights divide by one reciprocal of their sum.
+template <> __device__ inline void mdcd_pair<float>(const float* s6, float gama, float& ql, float& qr) {
+    const float b2 = 13.0f / 12.0f;                  // beta^2
+    const float epsm = 1.0e-6f;
+    const float aw0 = 1.5f * (0.0463783f + gama);
+    const float aw1 = (0.5f - 1.5f * 0.0463783f) + 4.5f * gama;
+    const float aw2 = (0.5f - 1.5f * 0.0463783f) - 4.5f * gama;
+    const float aw3 = 1.5f * (0.0463783f - gama);
+    const float s0 = s6[0], s1 = s6[1], s2 = s6[2], s3 = s6[3], s4 = s6[4], s5 = s6[5];
+    const float D0 = s0 - 2.0f * s1 + s2, D1 = s1 - 2.0f * s2 + s3, D2 = s2 - 2.0f * s3 + s4, D3 = s3 - 2.0f * s4 + s5;
+    const float E0 = b2 * D0 * D0, E1 = b2 * D1 * D1, E2 = b2 * D2 * D2, E3 = b2 * D3 * D3;
+    const float F1 = 0.5f * s0 - 2.0f * s1 + 1.5f * s2, F2 = 0.5f * (s3 - s1);
+    const float G1 = 0.5f * s5 - 2.0f * s4 + 1.5f * s3, G2 = 0.5f * (s2 - s4);
+    const float F3 = G2 + D2, F4 = G1 + D3, G3 = F2 + D1, G4 = F1 + D0;      // up to sign, squared next
+    const float c13 = 1.0f / 3.0f, c76 = 7.0f / 6.0f, c116 = 11.0f / 6.0f, c16 = 1.0f / 6.0f, c56 = 5.0f / 6.0f;
+    const float qq0 = c13 * s0 - c76 * s1 + c116 * s2;
+    const float qq1 = -(c16 * s1) + c56 * s2 + c13 * s3;
+    const float qq2 = c13 * s2 + c56 * s3 - c16 * s4;
+    const float qq3 = c116 * s3 - c76 * s4 + c13 * s5;
+    auto state = [&](float I1, float I2, float I3, float I4, float r0, float r1, float r2, float r3) {
+        I4 = fmaxf(fmaxf(fmaxf(I1, I2), I3), I4);
+        const float a1 = aw0 / sq(epsm + I1), a2 = aw1 / sq(epsm + I2), a3 = aw2 / sq(epsm + I3), a4 = aw3 / sq(epsm + I4);
+        const float rs = 1.0f / (a1 + a2 + a3 + a4);
+        return (a1 * r0 + a2 * r1 + a3 * r2 + a4 * r3) * rs;
+    };
+    ql = state(F1 * F1 + E0, F2 * F2 + E1, F3 * F3 + E2, F4 * F4 + E3, qq0, qq1, qq2, qq3);
+    qr = state(G1 * G1 + E3, G2 * G2 + E2, G3 * G3 + E1, G4 * G4 + E0, qq3, qq2, qq1, qq0);
+}
+
 // Roe_Common of the rotated scheme (Space/CONVECT_Roe_Rotated.F90:597-752), non-preconditioned:
 // adds 0.5 |A| dQ along (sav1..3)/sav, times sav and Funscheme, to dr.  rLo, rRo = rccl, rccr
 // times omega(1), the frame speeds of the two states.
