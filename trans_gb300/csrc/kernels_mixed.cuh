@@ -213,7 +213,8 @@ __device__ inline double positive_add(double p, float dp) {
 
 // Residual-norm partials of one thread in FP32 (the terms |D/V| come from FP32 increments),
 // joined as NormPart's (the later cell kept on ties of the maximum); a warp reduces them by
-// shuffles in FP32, the CTA's warps then in FP64 as norm_reduce_cta does.
+// shuffles in FP32, warp 0 then the CTA's warps the same way, and the CTA's result goes out as
+// a NormPart (FP64), which k_block_norms sums over the tiles of a block in FP64.
 struct NormPartF {
     float sa, ma, sk, mk, so, mo;
     int ia, nan;
@@ -224,9 +225,9 @@ __device__ inline void normf_join(NormPartF& a, const NormPartF& b) {
     a.mk = fmaxf(a.mk, b.mk); a.mo = fmaxf(a.mo, b.mo);
     a.nan |= b.nan;
 }
-__device__ inline NormPart norm_reduce_cta_f(NormPartF a) {
+__device__ inline NormPartF normf_reduce_warp(NormPartF a) {
     const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     for (int w = 16; w > 0; w >>= 1) {
         NormPartF o;
         o.sa = __shfl_down_sync(full, a.sa, w); o.ma = __shfl_down_sync(full, a.ma, w);
@@ -235,16 +236,23 @@ __device__ inline NormPart norm_reduce_cta_f(NormPartF a) {
         o.ia = __shfl_down_sync(full, a.ia, w); o.nan = __shfl_down_sync(full, a.nan, w);
         if (lane + w < 32) normf_join(a, o);
     }
-    __shared__ NormPart s_warp[32];
-    if (lane == 0) {
-        NormPart d;
-        d.sa = f64_of(a.sa); d.ma = f64_of(a.ma); d.sk = f64_of(a.sk); d.mk = f64_of(a.mk);
-        d.so = f64_of(a.so); d.mo = f64_of(a.mo); d.ia = a.ia; d.nan = a.nan; d.pad_ = 0;
-        s_warp[wid] = d;
-    }
+    return a;
+}
+// the CTA's reduction, valid in thread 0 (blockDim a multiple of 32); every thread calls it
+__device__ inline NormPart norm_reduce_cta_f(NormPartF a) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    a = normf_reduce_warp(a);
+    __shared__ NormPartF s_warp[32];
+    if (lane == 0) s_warp[wid] = a;
     __syncthreads();
     NormPart r = norm_identity();
-    if (wid == 0) r = norm_reduce_warp(lane < (int)(blockDim.x >> 5) ? s_warp[lane] : norm_identity());
+    if (wid == 0) {
+        NormPartF e;
+        e.sa = 0.0f; e.ma = -1.0f; e.sk = 0.0f; e.mk = 0.0f; e.so = 0.0f; e.mo = 0.0f; e.ia = -1; e.nan = 0;
+        const NormPartF b = normf_reduce_warp(lane < (int)(blockDim.x >> 5) ? s_warp[lane] : e);
+        r.sa = f64_of(b.sa); r.ma = f64_of(b.ma); r.sk = f64_of(b.sk); r.mk = f64_of(b.mk);
+        r.so = f64_of(b.so); r.mo = f64_of(b.mo); r.ia = b.ia; r.nan = b.nan; r.pad_ = 0;
+    }
     return r;
 }
 
