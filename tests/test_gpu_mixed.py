@@ -133,8 +133,9 @@ def _first_residual(case, precision, env="1"):
                          ids=["channel_mdcd_ausmpw", "channel_muscl_roe", "cascade_mdcd_ausmpw", "cascade_mdcdhyb_ausmpw",
                               "annular_rotating_mdcd_roe"])
 def test_tma_tiles_match_face_flux_kernels(gpu_lib, make, scheme):
-    """The mixed path's residual from TMA-staged shared-memory tiles (k_resid_tma, the default)
-    against its residual from k_face_flux<float> + k_gather<float> (TRANS_RESID_TMA=0), both
+    """The mixed path's residual from TMA-staged shared-memory tiles (k_resid_tma,
+    TRANS_RESID_TMA=1) against its residual from k_face_flux<float> + k_gather<float> (the
+    default, TRANS_RESID_TMA=0), both
     against the FP64 residual: the same FP32 face arithmetic, summed per direction instead of in
     the gather's order.  D is a difference of fluxes many times its size, so FP32 rounding of the
     fluxes shows in D well above FP32's own precision (1e-2 of the largest density residual of
@@ -156,3 +157,26 @@ def test_tma_tiles_match_face_flux_kernels(gpu_lib, make, scheme):
             e_t = max(np.max(np.abs(D_t[ib][q][m] - D_64[ib][q][m])) for q in grp) / scale
             e_g = max(np.max(np.abs(D_g[ib][q][m] - D_64[ib][q][m])) for q in grp) / scale
             assert e_t <= 3.0 * e_g + 1e-6, f"block {b.id} D{grp}: tiled {e_t:.3e}, gather {e_g:.3e}"
+
+
+def test_residual_form_tuner_on_request(gpu_lib, monkeypatch):
+    """TRANS_RESID_TMA=auto: the context times both residual forms on its first residual,
+    reports both times in trans_tuning and keeps one of them; without it the gather form runs
+    and nothing is timed."""
+    from trans_gb300 import abi
+    from trans_gb300.solver import Solver
+    for env, timed in (("auto", True), (None, False)):
+        if env:
+            monkeypatch.setenv("TRANS_RESID_TMA", env)
+        else:
+            monkeypatch.delenv("TRANS_RESID_TMA", raising=False)
+        c, conns, geo, st = small_cascade(Kind_Spatial=3, Kind_Roe=3)
+        c.params.precision = abi.TRANS_MIXED
+        s = Solver(c, conns, geo, st)
+        s.iterate(1)
+        tuning = s.lib.trans_tuning(s.ctx).decode()
+        s.close()
+        assert ("tma:" in tuning and "gather:" in tuning) == timed, tuning
+        assert "residual=tma" in tuning or "residual=gather" in tuning, tuning
+        if not timed:
+            assert "residual=gather" in tuning, tuning

@@ -47,9 +47,11 @@ def test_tile_staging_wait_runs_out(gpu_lib, monkeypatch):
     """The mixed path's residual tiles wait on an mbarrier for their TMA copies.  Allowed no
     polls (TRANS_RESID_SPIN=0), every CTA records the error, waits for its copies in flight with
     the default bound (they land; the shared memory they write must outlive them) and returns;
-    the UPDATE stage reports TRANS_E_TIMEOUT, and a context with the default limit iterates."""
+    the UPDATE stage reports TRANS_E_TIMEOUT, and a context with the default limit iterates.
+    (The tiled form is selected explicitly: the default is k_face_flux + k_gather.)"""
     from trans_gb300 import abi
     from trans_gb300.solver import Solver
+    monkeypatch.setenv("TRANS_RESID_TMA", "1")
     monkeypatch.setenv("TRANS_RESID_SPIN", "0")
     c, conns, geo, st = small_cascade(Kind_Spatial=3, Kind_Roe=3)
     c.params.precision = abi.TRANS_MIXED

@@ -151,11 +151,13 @@ int ctx_init(Ctx* c, int precision, long long budget) {
     CK(cudaMemset(c->d_kerr, 0, sizeof(int)));
     CK(cudaMallocHost(&c->h_kerr, sizeof(int)));
     *c->h_kerr = 0;
-    // TRANS_RESID_TMA=0 | 1: the mixed path's residual from k_face_flux + k_gather, or from the
-    // TMA-staged tiles (for comparisons); default: the faster on the context's first residual
+    // TRANS_RESID_TMA=0 | 1 | auto: the mixed path's residual from k_face_flux + k_gather (the
+    // default), from the TMA-staged tiles, or the faster of the two on the context's first
+    // residual
     const char* rt = std::getenv("TRANS_RESID_TMA");
     if (rt && std::string(rt) == "0") c->resid_tma = 0;
     if (rt && std::string(rt) == "1") c->resid_tma = 1;
+    if (rt && std::string(rt) == "auto") c->resid_tma = -1;
     // TRANS_XFER_BATCH=0: trans_set/get_fields transfer the arrays one launch each (for comparisons)
     const char* xb = std::getenv("TRANS_XFER_BATCH");
     if (xb && std::string(xb) == "0") c->xfer_batch = false;

@@ -71,9 +71,12 @@ struct Ctx {
     Tile *d_cell = nullptr, *d_face[3] = {nullptr, nullptr, nullptr}, *d_ghost = nullptr;
     std::vector<int> cell_tile_blk;      // block of each cell tile (norm reduction)
     // mixed path: the residual from TMA-staged tiles (one tile list per face direction, NRMAP
-    // tensor maps per block over its FP32 slots); resid_tma = 0 uses k_face_flux + k_gather,
-    // -1 times both on the first residual and keeps the faster
-    int resid_tma = -1;
+    // tensor maps per block over its FP32 slots) when 1; 0 (the default) uses k_face_flux +
+    // k_gather; -1 times both on the first residual and keeps the faster.  The two forms sum a
+    // cell's fluxes in different orders, so a timed choice can differ between contexts and
+    // their results then only agree to FP32 rounding; the fixed default keeps a case's result
+    // the same alone and in any batch.
+    int resid_tma = 0;
     bool xfer_batch = true;              // trans_set/get_fields: page-locked arrays in one launch
     bool xfer_mapped = true;             // page-locked arrays read in place (false: copied by DMA through the staging buffer)
     std::string resid_tuning;

@@ -671,12 +671,14 @@ struct FaceGlobal {
     __device__ R v(int slot, int o) const { return R(rs<R>(b, slot)[c + o * s]); }
 };
 
-template <typename R, int DIR, class A>
+// PART 0: every flux; 1: the viscous and k-omega diffusion fluxes only; 2: the convective ones
+template <typename R, int DIR, int PART = 0, class A>
 __device__ __forceinline__ void face_flux_body(const ParamsT<R>& p, int turb, const A& q, R* F) {
     constexpr int d = DIR - 1;
     constexpr int AL = S_ALAGM + d, AIN = S_AINV + d, SDD = S_SD + 3 * d;
     // face average of a slot at the face o steps from this one (SPACEINTERP_GetSurfCenterVars)
     auto fa = [&](int slot, int o) { return (q.v(AL, o) * q.v(slot, o - 1) + q.v(AL, o - 1) * q.v(slot, o)) * q.v(AIN, o); };
+    if constexpr (PART != 2) {
     // ---------------- viscous flux (DIFFUSION_Centered) ----------------
     const bool wall = q.v(S_WALL + d, 0) != R(0.0);
     const R vinv = q.v(S_VINV + d, 0);
@@ -781,6 +783,8 @@ __device__ __forceinline__ void face_flux_body(const ParamsT<R>& p, int turb, co
         F[FX_TK] = (vmute * (gt[0][0] * Dx + gt[0][1] * Dy + gt[0][2] * Dz)) / Ref;
         F[FX_TO] = (vmuoq * (gt[1][0] * Dx + gt[1][1] * Dy + gt[1][2] * Dz)) / Ref;
     }
+    }   // PART != 2
+    if constexpr (PART == 1) return;
     // ---------------- reconstruction ----------------
     R qL[7], qR[7];
     constexpr int qc[5] = {S_PRIM, S_PRIM + 1, S_PRIM + 2, S_PP, S_T};
@@ -881,7 +885,7 @@ __device__ __forceinline__ void face_flux_body(const ParamsT<R>& p, int turb, co
             // is off), and Alagm(d) of the face's cell (Space/CONVECT_Roe_Original.F90:86-87)
             const R RmiuTf = (p.IF_Precondition && turb) ? fa(S_RMIU, 0) : R(0.0);
             roe_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, rLo, rRo,
-                        f, RmiuTf, a0);
+                        f, RmiuTf, q.v(AL, 0));
         } else
             ausmpw_flux<R>(p, qL[3], qR[3], qL[4], qR[4], qL[0], qR[0], qL[1], qR[1], qL[2], qR[2], sav1, sav2, sav3, sav, f);
 #pragma unroll
@@ -903,11 +907,18 @@ __device__ __forceinline__ void face_flux_body(const ParamsT<R>& p, int turb, co
 }
 
 #ifndef TG_FACE_MINB
-#define TG_FACE_MINB 5      // resident CTAs per SM asked of the FP32 face-flux kernels (96 registers)
+#define TG_FACE_MINB 8      // resident CTAs per SM asked of the FP32 convective-flux kernels (64 registers)
 #endif
-// one thread per face; the fluxes go to the FX slots, k_gather sums them per cell
-template <typename R, int DIR>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
+#ifndef TG_FACE_MINB_VISC
+#define TG_FACE_MINB_VISC 6 // ... of the FP32 viscous-flux kernels (80 registers)
+#endif
+// one thread per face; the fluxes go to the FX slots, k_gather sums them per cell.  PART 0: all
+// of them (FP64 path); the mixed path launches the viscous and k-omega diffusion fluxes (PART 1)
+// and the convective ones (PART 2) as two kernels, which share few inputs and write disjoint
+// FX words, so that each gets its own register budget: as one kernel the FP32 fluxes needed 96
+// registers (five CTAs per SM) and were issue-latency bound; split, 80 and 64 (six and eight)
+template <typename R, int DIR, int PART = 0>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? (PART == 1 ? TG_FACE_MINB_VISC : TG_FACE_MINB) : 1) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
                                                           const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
@@ -921,18 +932,24 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? TG_FACE_MINB : 1) k_face
     const int c = cidx(b, i, j, k);
     const FaceGlobal<R> q{b, c, s};
     R F[NFX];
-    face_flux_body<R, DIR>(p, turb, q, F);
+    face_flux_body<R, DIR, PART>(p, turb, q, F);
     const size_t nc = (size_t)b.ncell;
     R* FX = rs<R>(b, S_FX + NFX * (DIR - 1));
+    if constexpr (PART != 2) {
 #pragma unroll
-    for (int m = 0; m < FX_TK; ++m) FX[(size_t)m * nc + c] = F[m];
+        for (int m = 0; m < FX_TK; ++m) FX[(size_t)m * nc + c] = F[m];
+        if (turb) {
+            FX[(size_t)FX_TK * nc + c] = F[FX_TK];
+            FX[(size_t)FX_TO * nc + c] = F[FX_TO];
+        }
+    }
+    if constexpr (PART != 1) {
 #pragma unroll
-    for (int m = FX_C0; m < FX_CK; ++m) FX[(size_t)m * nc + c] = F[m];
-    if (turb) {
-        FX[(size_t)FX_TK * nc + c] = F[FX_TK];
-        FX[(size_t)FX_TO * nc + c] = F[FX_TO];
-        FX[(size_t)FX_CK * nc + c] = F[FX_CK];
-        FX[(size_t)FX_CO * nc + c] = F[FX_CO];
+        for (int m = FX_C0; m < FX_CK; ++m) FX[(size_t)m * nc + c] = F[m];
+        if (turb) {
+            FX[(size_t)FX_CK * nc + c] = F[FX_CK];
+            FX[(size_t)FX_CO * nc + c] = F[FX_CO];
+        }
     }
 }
 
