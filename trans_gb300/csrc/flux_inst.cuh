@@ -19,12 +19,9 @@ void bcg(cudaStream_t s, const DevBlock* b, const BCEntry* e, int n) {
 template <int DIR>
 void ff(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
     if (nt <= 0) return;
-    if constexpr (sizeof(TG_R) == 4) {      // viscous, then convective fluxes (two register budgets)
-        k_face_flux<TG_R, DIR, 1><<<nt, FACE_TILE, 0, s>>>(b, t, cd);
-        k_face_flux<TG_R, DIR, 2><<<nt, FACE_TILE, 0, s>>>(b, t, cd);
-    } else {
-        k_face_flux<TG_R, DIR, 0><<<nt, FACE_TILE, 0, s>>>(b, t, cd);
-    }
+    // viscous, then convective fluxes (two register budgets)
+    k_face_flux<TG_R, DIR, 1><<<nt, FACE_TILE, 0, s>>>(b, t, cd);
+    k_face_flux<TG_R, DIR, 2><<<nt, FACE_TILE, 0, s>>>(b, t, cd);
 }
 void ga(cudaStream_t s, const DevBlock* b, const Tile* t, int nt, const CaseDev* cd) {
     if (nt > 0) k_gather<TG_R><<<nt, CELL_TILE, 0, s>>>(b, t, cd);

@@ -913,12 +913,14 @@ __device__ __forceinline__ void face_flux_body(const ParamsT<R>& p, int turb, co
 #define TG_FACE_MINB_VISC 6 // ... of the FP32 viscous-flux kernels (80 registers)
 #endif
 // one thread per face; the fluxes go to the FX slots, k_gather sums them per cell.  PART 0: all
-// of them (FP64 path); the mixed path launches the viscous and k-omega diffusion fluxes (PART 1)
+// of them in one kernel; both paths launch the viscous and k-omega diffusion fluxes (PART 1)
 // and the convective ones (PART 2) as two kernels, which share few inputs and write disjoint
-// FX words, so that each gets its own register budget: as one kernel the FP32 fluxes needed 96
-// registers (five CTAs per SM) and were issue-latency bound; split, 80 and 64 (six and eight)
+// FX words, so that each gets its own register budget (the same arithmetic, so the FP64
+// fluxes stay bit-identical): as one kernel the FP32 fluxes needed 96 registers (five CTAs per
+// SM) and were issue-latency bound, split 80 and 64 (six and eight); the FP64 ones 250 (two),
+// split at most 168 and 142 (three each)
 template <typename R, int DIR, int PART = 0>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? (PART == 1 ? TG_FACE_MINB_VISC : TG_FACE_MINB) : 1) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? (PART == 1 ? TG_FACE_MINB_VISC : TG_FACE_MINB) : (PART == 0 ? 1 : 3)) k_face_flux(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles,
                                                           const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;

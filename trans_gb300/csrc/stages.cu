@@ -622,12 +622,12 @@ int stage_exec(Ctx* c, int stage, int itr, bool capture, int slot) {
                 break;
             }
             for (int d = 0; d < 3; ++d) {
-                // the mixed path launches the viscous and the convective fluxes of a direction apart
-                KScope t(c, K_FACE, c->mixed ? 2 : 1);
+                // the viscous and the convective fluxes of a direction are two launches
+                KScope t(c, K_FACE, 2);
                 c->fl->face_flux[d](s, c->d_blk, c->d_face[d], (int)c->face_tiles[d].size(), c->d_cdev);
             }
             { KScope t(c, K_GATHER); c->fl->gather(s, c->d_blk, c->d_cell, nct, c->d_cdev); }
-            c->launches += c->mixed ? 7 : 4;
+            c->launches += 7;
             break;
         case TRANS_STAGE_LUSGS: {
             if (!capture && (rc = upload_cdev(c))) return rc;
