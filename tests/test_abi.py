@@ -126,3 +126,13 @@ def test_rotated_roe_is_fp64_only(lib):
     blk[0].ni = blk[0].nj = blk[0].nk = 8
     ctx = C.c_void_p()
     assert lib.trans_create(C.byref(p), 1, blk, C.byref(ctx)) == abi.TRANS_E_ARG
+
+
+def test_conversion_check_validates_arguments_before_any_device_work(lib):
+    """trans_check_conversions rejects a pattern count outside 1..2^32 or a NULL result array
+    with TRANS_E_ARG and a message, before it touches the device (so this runs without one)."""
+    bad = (C.c_longlong * 2)()
+    assert lib.trans_check_conversions(0, 1, bad) == abi.TRANS_E_ARG
+    assert lib.trans_check_conversions((1 << 32) + 1, 1, bad) == abi.TRANS_E_ARG
+    assert lib.trans_check_conversions(16, 1, None) == abi.TRANS_E_ARG
+    assert b"trans_check_conversions" in lib.trans_last_error(None)
