@@ -179,11 +179,13 @@ ALG_WORDS = {
     "k_update": 37, "k_gradient": 46, "k_specrad": 24, "k_lusgs_prep": 60, "k_gather": 46,
 }
 # FP64 thread-instructions per face of k_face_flux<double> (MDCD + AUSMPW+ + SST), counted by
-# ncu (DADD + DMUL + DFMA over the three directions) on the 339,968-cell cascade, and DRAM
-# bytes per face from the same capture (profiles/k_face_flux_fp64_cascade_339968cells.md)
+# ncu (DADD + DMUL + DFMA over the three directions) on the 339,968-cell cascade
+# (profiles/k_face_flux_fp64_cascade_339968cells.md), and DRAM bytes per face of the viscous
+# and convective kernels the flux is now split into (profiles/launches_cascade_5blk_1966080cells_fp64.md)
 FACE_FP64_INST = 2541.0
-FACE_DRAM_BYTES = 391.3
-FACE_DRAM_SOURCE = "ncu dram__bytes_read+write per face on the 339,968-cell cascade, scaled by faces"
+FACE_DRAM_BYTES = 479.1
+FACE_DRAM_SOURCE = ("ncu dram__bytes_read+write per face of the viscous and convective kernels together on the "
+                    "491,520-cell cascade, scaled by faces")
 # kernel classes that run in FP32 in the mixed path (their algorithmic words are 4 bytes there)
 FP32_KERNELS = ("k_face_flux", "k_resid_tma", "k_gather", "k_sweep", "k_gradient")
 # bounded serving leg of the default line: 4 requests/s as the serving configuration states,
