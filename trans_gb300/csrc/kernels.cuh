@@ -1127,8 +1127,11 @@ __device__ inline R rc_fr1(const ParamsT<R>& p, const DevBlock& b, int I, int J,
 }
 
 // (FP32: two resident CTAs of 256 threads per SM, i.e. at most 128 registers)
+#ifndef TG_PREP_MINB
+#define TG_PREP_MINB 3      // resident CTAs per SM of the FP32 preparation (84 registers, 80-byte spill)
+#endif
 template <typename R>
-__global__ void __launch_bounds__(CELL_TILE, sizeof(R) == 4 ? 2 : 1) k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
+__global__ void __launch_bounds__(CELL_TILE, sizeof(R) == 4 ? TG_PREP_MINB : 1) k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
                              R* __restrict__ rec, R* __restrict__ dq, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
