@@ -1130,8 +1130,11 @@ __device__ inline R rc_fr1(const ParamsT<R>& p, const DevBlock& b, int I, int J,
 #ifndef TG_PREP_MINB
 #define TG_PREP_MINB 3      // resident CTAs per SM of the FP32 preparation (84 registers, 80-byte spill)
 #endif
+#ifndef TG_PREP_MINB_F64
+#define TG_PREP_MINB_F64 2  // ... and of the FP64 one (128 registers, 84-byte spill; 254 at one CTA per SM)
+#endif
 template <typename R>
-__global__ void __launch_bounds__(CELL_TILE, sizeof(R) == 4 ? TG_PREP_MINB : 1) k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
+__global__ void __launch_bounds__(CELL_TILE, sizeof(R) == 4 ? TG_PREP_MINB : TG_PREP_MINB_F64) k_lusgs_prep(const DevBlock* __restrict__ blks, const Tile* __restrict__ tiles, const int* __restrict__ qpos,
                              R* __restrict__ rec, R* __restrict__ dq, const CaseDev* __restrict__ cdev) {
     const Tile t = tiles[blockIdx.x];
     if ((int)threadIdx.x >= t.count) return;
